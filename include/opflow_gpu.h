@@ -1,0 +1,268 @@
+/* opflow_gpu.h -- C ABI of the GB300 engine for OpFlow's two data-parallel paths on structured
+ * Cartesian grids:
+ *   (E) explicit evaluation of a stencil expression into a field  (`u = u + dt*a*(d2x(u)+d2y(u))`),
+ *   (I) implicit solve of a stencil-generated linear equation      (`Solve(f, p, PCG, PFMG)`).
+ *
+ * OpFlow itself is a header-only C++ template library with no FFI; the entry points below are what a
+ * C++ adapter (include/opflow_gb300/OpFlowGPU.hpp) or any FFI (ctypes, cgo, JNI) binds in place of
+ * the reference's template machinery.  Each declaration names the reference interface it replaces
+ * (paths relative to the OpFlow source tree).
+ *
+ * Conventions
+ *   - Every call returns an int status (OPFLOW_OK == 0).  The library never aborts; the message of the
+ *     last failure on the calling thread is returned by opflow_last_error().
+ *   - No torch or CUDA types appear in signatures: handles are opaque pointers, buffers are plain
+ *     pointers with element counts.  CUDA streams are passed as void*.
+ *   - Field data layout is the reference's PlainTensor layout (src/DataStructures/Arrays/Tensor/
+ *     PlainTensor.hpp:204-213): x fastest, over the padded local range
+ *     localRange.getInnerRange(-padding), float64.
+ */
+#ifndef OPFLOW_GPU_H
+#define OPFLOW_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OPFLOW_GPU_ABI_VERSION 1
+
+/* ---- status codes ---------------------------------------------------------------------------- */
+enum opflow_status {
+    OPFLOW_OK = 0,
+    OPFLOW_E_INVALID = 1,       /* bad argument / inconsistent description (reference: OP_ABORT)      */
+    OPFLOW_E_NOMEM = 2,         /* device allocation or HBM admission budget exhausted               */
+    OPFLOW_E_CUDA = 3,          /* a CUDA runtime call failed                                        */
+    OPFLOW_E_TIMEOUT = 4,       /* a bounded device-side wait expired                                */
+    OPFLOW_E_NOT_CONVERGED = 5, /* maxIter reached before the tolerance                              */
+    OPFLOW_E_UNSUPPORTED = 6,   /* expression / stencil shape outside what the engine lowers         */
+    OPFLOW_E_RANGE = 7,         /* a stencil read would leave the field's readable range             */
+    OPFLOW_E_NAN = 8            /* non-finite input (e.g. NaN in a right-hand side)                  */
+};
+
+/* Reference enums: LocOnMesh (src/Core/Field/MeshBased/StructuredFieldExpr*), BCType (src/Core/BC/BCBase.hpp) */
+enum opflow_loc { OPFLOW_CORNER = 0, OPFLOW_CENTER = 1 };
+enum opflow_bc {
+    OPFLOW_BC_UNDEFINED = 0,
+    OPFLOW_BC_DIRC = 1,
+    OPFLOW_BC_NEUM = 2,
+    OPFLOW_BC_PERIODIC = 3,
+    OPFLOW_BC_SYMM = 4,
+    OPFLOW_BC_ASYMM = 5
+};
+
+/* BasicArithOp of FieldAssigner::assign<Op> (src/Core/Loops/FieldAssigner.hpp:26-84) */
+enum opflow_arith { OPFLOW_ASSIGN_EQ = 0, OPFLOW_ASSIGN_ADD = 1, OPFLOW_ASSIGN_SUB = 2, OPFLOW_ASSIGN_MUL = 3, OPFLOW_ASSIGN_DIV = 4 };
+
+typedef struct opflow_ctx_s* opflow_ctx;
+typedef struct opflow_field_s* opflow_field;
+typedef struct opflow_solver_s* opflow_solver;
+typedef struct opflow_batch_s* opflow_batch;
+typedef struct opflow_server_s* opflow_server;
+
+/* ---- context --------------------------------------------------------------------------------- */
+/* Replaces EnvironmentGardian / the global ParallelPlan (src/Core/Environment.hpp:41-62): one context
+ * per device, owning one CUDA stream. */
+int opflow_ctx_create(int device, opflow_ctx* out);
+int opflow_ctx_destroy(opflow_ctx ctx);
+int opflow_ctx_set_stream(opflow_ctx ctx, void* cuda_stream);
+int opflow_ctx_get_stream(opflow_ctx ctx, void** cuda_stream);
+int opflow_ctx_synchronize(opflow_ctx ctx);
+/* Message of the last failed call on this thread ("" if none). */
+const char* opflow_last_error(void);
+/* Number of kernels this library has launched in this process (for launch accounting). */
+int opflow_kernel_launch_count(uint64_t* out);
+int opflow_abi_version(void);
+
+/* ---- mesh + field ---------------------------------------------------------------------------- */
+/* Replaces MeshBuilder<CartesianMesh<Dim>> (src/Core/Mesh/Structured/CartesianMesh.hpp:122-305) and
+ * ExprBuilder<CartesianField> (src/Core/Field/MeshBased/Structured/CartesianField.hpp:796-1033).
+ * The mesh is given by its node coordinates over the extended range
+ * [start-pad_width, start+dims+pad_width) per dimension (what MeshBuilder::build produces);
+ * opflow_mesh_uniform() fills that from setMeshOfDim(d, min, max). */
+typedef struct {
+    int ndim;
+    int dims[3];      /* nodes per dimension                                        */
+    int start[3];     /* first node index (MeshBuilder::setStart, default 0)        */
+    int pad_width;    /* mesh ghost extension (MeshBuilder padding_width, default 5) */
+    const double* x[3];  /* dims[d] + 2*pad_width node coordinates (CartesianMesh::_x)  */
+    const double* dx[3]; /* dims[d] + 2*pad_width - 1 spacings (CartesianMesh::_dx)      */
+} opflow_mesh_desc;
+
+typedef struct {
+    int ndim;
+    int loc[3];             /* enum opflow_loc                                       */
+    int bc_type[3][2];      /* [dim][start/end], enum opflow_bc                      */
+    double bc_value[3][2];  /* constant Dirichlet value / Neumann gradient           */
+    int ext[3][2];          /* ExprBuilder::setExt widths                           */
+    int padding;            /* ExprBuilder::setPadding (final padding = max(padding, ext)) */
+} opflow_field_desc;
+
+typedef struct {
+    int ndim;
+    int padding;
+    int data_dims[3];        /* extents of the data array (padded local range)          */
+    int data_offset[3];      /* index of data element 0 (CartesianField::offset)        */
+    int logical[3][2], accessible[3][2], assignable[3][2], local[3][2];
+    size_t count;            /* data_dims product                                       */
+} opflow_field_info;
+
+/* Node coordinates and spacings of MeshBuilder::set1DMesh(min, max) including its Symm ghost extension
+ * (CartesianMesh.hpp:209-303).  x_out holds dims + 2*pad_width values, dx_out one fewer. */
+int opflow_mesh_uniform(int dims, int start, int pad_width, double min, double max, double* x_out, double* dx_out);
+
+/* The ranges and data extents ExprBuilder<CartesianField>::calculateRanges / validateRanges compute
+ * (CartesianField.hpp:941-1029), without allocating anything (no GPU needed). */
+int opflow_field_describe(const opflow_mesh_desc* mesh, const opflow_field_desc* desc, opflow_field_info* out);
+
+/* ExprBuilder<CartesianField>::build (CartesianField.hpp:929-1029): computes the ranges, allocates the
+ * device data array (zero-filled) and applies updatePadding. */
+int opflow_field_create(opflow_ctx ctx, const opflow_mesh_desc* mesh, const opflow_field_desc* desc, opflow_field* out);
+int opflow_field_destroy(opflow_field f);
+int opflow_field_get_info(opflow_field f, opflow_field_info* out);
+/* Full data array (layout above); count must equal info.count.  Upload is followed by nothing: call
+ * opflow_field_update_padding if the host data's padding is stale. */
+int opflow_field_upload(opflow_field f, const double* host, size_t count);
+int opflow_field_download(opflow_field f, double* host, size_t count);
+/* Device pointer of the current data array (it alternates between two buffers across aliased
+ * assignments, so re-query after each assign). */
+int opflow_field_device_ptr(opflow_field f, double** dptr);
+/* CartesianField::updatePaddingImpl_final (CartesianField.hpp:349-629), single-rank branch. */
+int opflow_field_update_padding(opflow_field f);
+/* `f = c` for a constant (CartesianField::assignImpl_final(const D&), CartesianField.hpp:236-280). */
+int opflow_field_fill(opflow_field f, int arith, double c);
+/* `dst = src` between two fields of identical shape (data copy, then padding). */
+int opflow_field_copy(opflow_field dst, opflow_field src);
+
+/* ---- expressions (path E) ---------------------------------------------------------------------- */
+/* One node of an expression tree, children before parents; the root is the last node.
+ * Mirrors Expression<Op, Args...> (src/Core/Expr/Expression.hpp) with the operators of
+ * src/Core/Operator/{Arithmetic/AMDS.hpp, FDMOperators, Interpolator/D1Linear.hpp}. */
+enum opflow_node_kind {
+    OPFLOW_NODE_FIELD = 1,      /* leaf: field slot `field`                                        */
+    OPFLOW_NODE_CONST = 2,      /* ScalarExpr<double> `value`                                     */
+    OPFLOW_NODE_ADD = 3,        /* AddOp                                                          */
+    OPFLOW_NODE_SUB = 4,        /* SubOp                                                          */
+    OPFLOW_NODE_MUL = 5,        /* MulOp                                                          */
+    OPFLOW_NODE_DIV = 6,        /* DivOp                                                          */
+    OPFLOW_NODE_NEG = 7,        /* unary minus                                                    */
+    OPFLOW_NODE_D2 = 8,         /* D2SecondOrderCentered<dim>   (D2SecondOrderCentered.hpp:160-171) */
+    OPFLOW_NODE_D1 = 9,         /* D1FirstOrderCentered<dim>    (D1FirstOrderCentered.hpp:31-36)    */
+    OPFLOW_NODE_WENO53_DOWN = 10,/* D1WENO53Downwind<dim>       (D1WENO53Downwind.hpp:136-154)      */
+    OPFLOW_NODE_WENO53_UP = 11, /* D1WENO53Upwind<dim>          (D1WENO53Upwind.hpp:133-151)        */
+    OPFLOW_NODE_INTP_C2C = 12   /* D1Linear Cen2Cor, d1IntpCenterToCorner<dim> (D1Linear.hpp:35-45) */
+};
+
+typedef struct {
+    int kind;     /* enum opflow_node_kind               */
+    int a, b;     /* child node indices, -1 if unused    */
+    int dim;      /* operator direction                  */
+    int field;    /* leaf slot for OPFLOW_NODE_FIELD     */
+    double value; /* constant for OPFLOW_NODE_CONST      */
+} opflow_node;
+
+/* Evaluation modes of the explicit path. */
+enum opflow_eval_mode {
+    OPFLOW_EVAL_EXACT = 0, /* IEEE float64 in the reference's operation order: bit-identical results */
+    OPFLOW_EVAL_FAST = 1   /* linear constant-coefficient stencils in exact 64-bit fixed point with one
+                              rounding per point (normwise relative error <= 1e-14 per 1000 steps);
+                              falls back to EXACT for anything else                                 */
+};
+
+/* `dst <op>= expr` for a Cartesian field: replaces internal::FieldAssigner::assign<Op>
+ * (src/Core/Loops/FieldAssigner.hpp:27-36) reached from Expr::operator= / += / -= / *= / /=
+ * (src/Core/Expr/Expr.hpp:53-81) through CartesianField::assignImpl_final (CartesianField.hpp:195-234).
+ * Evaluates over commonRange(dst.assignableRange, dst.localRange) and then updates dst's padding.
+ * An expression that reads dst itself is evaluated out of place, as the reference does. */
+int opflow_assign(opflow_ctx ctx, opflow_field dst, int arith, const opflow_node* nodes, int n_nodes,
+                  const opflow_field* leaves, int n_leaves, int mode);
+
+/* Runs `steps` repetitions of the same assignment (one fused kernel per step where the expression has
+ * a specialised kernel; the launches are recorded once into a CUDA graph and replayed). */
+int opflow_assign_repeat(opflow_ctx ctx, opflow_field dst, int arith, const opflow_node* nodes, int n_nodes,
+                         const opflow_field* leaves, int n_leaves, int mode, int steps);
+
+/* Shu-Osher RK3 step of u_t + L(u) = 0 with L = dt * d1<WENO53 kind, dim>(.), the three stages
+ *   u1 = u - dt*L(u);  u2 = 0.75*u + 0.25*(u1 - dt*L(u1));  u = 1/3*u + 2/3*(u2 - dt*L(u2))
+ * fused into one pass (stages in shared memory), bit-identical to three reference assignments.
+ * `kind` is OPFLOW_NODE_WENO53_DOWN or OPFLOW_NODE_WENO53_UP.  u1 and u2 receive the stage fields. */
+int opflow_weno_rk3(opflow_ctx ctx, opflow_field u, opflow_field u1, opflow_field u2, int kind, int dim, double dt, int steps);
+
+/* ---- implicit path (path I) -------------------------------------------------------------------- */
+/* The equation `lhs == rhs` is given as the tree of `lhs - rhs` (Equation.hpp:41-55) in which the
+ * unknown appears as the leaf slot `unknown_slot`; the other leaves are known fields.  This replaces
+ * HYPREEqnSolveHandler::initStencil/generateAb (src/Core/Equation/HYPREEqnSolveHandler.hpp:79-166),
+ * i.e. StencilField evaluation with StencilPad arithmetic (StencilField.hpp:123-350,
+ * StencilPad.hpp:137-336). */
+
+/* Assembly for parity checks: writes, for every cell of commonRange(target.assignable, target.local)
+ * in x-fastest order, the coefficients of the stencil entries and the right-hand side b = -bias,
+ * exactly as generateAb hands them to HYPRE_StructMatrixSetValues / HYPRE_StructVectorSetValues,
+ * including the pinned first row when pin != 0.  offsets_out receives n_entries*ndim ints in the
+ * order of the middle cell's StencilPad (commStencil).  Pass NULL buffers to query sizes. */
+int opflow_assemble(opflow_ctx ctx, opflow_field target, const opflow_node* nodes, int n_nodes,
+                    const opflow_field* leaves, int n_leaves, int unknown_slot, int pin,
+                    int* n_entries, int* offsets_out, double* coef_out, double* rhs_out, size_t* n_cells);
+
+/* Solver parameters: StructSolverParamsBase (src/Core/Solvers/Struct/StructSolver.hpp:39-51) plus the
+ * PFMG preconditioner knobs (StructSolverPFMG.hpp:23-33) and the GPU extensions. */
+enum opflow_precision { OPFLOW_PREC_FP64 = 0, OPFLOW_PREC_MIXED = 1 };
+typedef struct {
+    double tol;           /* relative residual ||b-Ax||_2/||b||_2 target (reference: tol)        */
+    int max_iter;         /* reference: maxIter                                                  */
+    int static_mat;       /* reference: staticMat (reuse A, regenerate b only)                   */
+    int pin_value;        /* reference: pinValue (pin the first unknown to 0)                    */
+    int precision;        /* enum opflow_precision                                               */
+    int pre_sweeps;       /* V-cycle smoothing sweeps (red-black Gauss-Seidel), default 2        */
+    int post_sweeps;      /* default 2                                                           */
+    int coarse_max;       /* coarsest level size bound for the direct solve, default 512         */
+    int zero_guess;       /* 1: start from x = 0 instead of the target's values                  */
+} opflow_solve_params;
+
+typedef struct {
+    int iterations;       /* EqnSolveState::niter (EqnSolveHandler.hpp:17-25)                    */
+    double rel_residual;  /* ||b - A x||_2 / ||b||_2 of the reference's system (pinned if pinned) */
+    double abs_residual;
+    int converged;
+    double setup_ms, solve_ms;
+} opflow_solve_state;
+
+void opflow_solve_params_default(opflow_solve_params* p);
+
+/* makeEqnSolveHandler(f, target, PrecondStructSolver<PCG,PFMG>) (HYPREEqnSolveHandler.hpp:44-48):
+ * assembles the operator on the device and builds the multigrid hierarchy. */
+int opflow_solver_create(opflow_ctx ctx, opflow_field target, const opflow_node* nodes, int n_nodes,
+                         const opflow_field* leaves, int n_leaves, int unknown_slot,
+                         const opflow_solve_params* params, opflow_solver* out);
+/* EqnSolveHandler::solve (HYPREEqnSolveHandler.hpp:190-209): regenerates A and b (or only b when
+ * static_mat), solves, writes the solution into the target field and updates its padding. */
+int opflow_solver_solve(opflow_solver s, opflow_solve_state* state);
+int opflow_solver_destroy(opflow_solver s);
+
+/* ---- batched uneven solves ------------------------------------------------------------------- */
+/* Many independent 2D/3D problems of different sizes in one persistent launch per multigrid
+ * operation.  The description is a compact physics form (no expression trees), one per problem:
+ *   alpha*u - beta*Lap(u) = f   on an n[0] x n[1] (x n[2]) grid of cells (loc CENTER) or nodes (CORNER),
+ * Dirichlet (value 0) or Neumann (gradient 0) on every side. */
+typedef struct {
+    int ndim;
+    int n[3];           /* cells (CENTER) or nodes (CORNER) per dimension              */
+    int loc;            /* enum opflow_loc                                             */
+    int bc;             /* OPFLOW_BC_DIRC or OPFLOW_BC_NEUM on all sides               */
+    double h[3];        /* grid spacing                                                */
+    double alpha, beta; /* alpha*u - beta*Lap(u)                                       */
+} opflow_problem_desc;
+
+int opflow_batch_create(opflow_ctx ctx, const opflow_problem_desc* problems, int n_problems,
+                        const opflow_solve_params* params, opflow_batch* out);
+/* Device pointers of problem i's unknown vector and right-hand side (x fastest over the unknowns). */
+int opflow_batch_vectors(opflow_batch b, int i, double** x, double** f, size_t* n_unknowns);
+int opflow_batch_solve(opflow_batch b, opflow_solve_state* states /* n_problems */);
+int opflow_batch_destroy(opflow_batch b);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OPFLOW_GPU_H */

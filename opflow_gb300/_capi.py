@@ -1,0 +1,146 @@
+"""ctypes binding of include/opflow_gpu.h (libopflow_gpu.so).
+
+This is the only place the Python side touches the library.  Loading fails loudly when the shared
+library has not been built: there is no CPU fallback behind any call.
+"""
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libopflow_gpu.so")
+
+# ---- enums (include/opflow_gpu.h) --------------------------------------------------------------------
+OK, E_INVALID, E_NOMEM, E_CUDA, E_TIMEOUT, E_NOT_CONVERGED, E_UNSUPPORTED, E_RANGE, E_NAN = range(9)
+CORNER, CENTER = 0, 1
+BC_UNDEFINED, BC_DIRC, BC_NEUM, BC_PERIODIC, BC_SYMM, BC_ASYMM = range(6)
+ASSIGN_EQ, ASSIGN_ADD, ASSIGN_SUB, ASSIGN_MUL, ASSIGN_DIV = range(5)
+(NODE_FIELD, NODE_CONST, NODE_ADD, NODE_SUB, NODE_MUL, NODE_DIV, NODE_NEG, NODE_D2, NODE_D1,
+ NODE_WENO53_DOWN, NODE_WENO53_UP, NODE_INTP_C2C) = range(1, 13)
+EVAL_EXACT, EVAL_FAST = 0, 1
+PREC_FP64, PREC_MIXED = 0, 1
+
+STATUS_NAMES = {OK: "OK", E_INVALID: "E_INVALID", E_NOMEM: "E_NOMEM", E_CUDA: "E_CUDA", E_TIMEOUT: "E_TIMEOUT",
+                E_NOT_CONVERGED: "E_NOT_CONVERGED", E_UNSUPPORTED: "E_UNSUPPORTED", E_RANGE: "E_RANGE", E_NAN: "E_NAN"}
+
+
+class MeshDesc(C.Structure):
+    _fields_ = [("ndim", C.c_int), ("dims", C.c_int * 3), ("start", C.c_int * 3), ("pad_width", C.c_int),
+                ("x", C.POINTER(C.c_double) * 3), ("dx", C.POINTER(C.c_double) * 3)]
+
+
+class FieldDesc(C.Structure):
+    _fields_ = [("ndim", C.c_int), ("loc", C.c_int * 3), ("bc_type", (C.c_int * 2) * 3),
+                ("bc_value", (C.c_double * 2) * 3), ("ext", (C.c_int * 2) * 3), ("padding", C.c_int)]
+
+
+class FieldInfo(C.Structure):
+    _fields_ = [("ndim", C.c_int), ("padding", C.c_int), ("data_dims", C.c_int * 3), ("data_offset", C.c_int * 3),
+                ("logical", (C.c_int * 2) * 3), ("accessible", (C.c_int * 2) * 3),
+                ("assignable", (C.c_int * 2) * 3), ("local", (C.c_int * 2) * 3), ("count", C.c_size_t)]
+
+
+class Node(C.Structure):
+    _fields_ = [("kind", C.c_int), ("a", C.c_int), ("b", C.c_int), ("dim", C.c_int), ("field", C.c_int),
+                ("value", C.c_double)]
+
+
+class SolveParams(C.Structure):
+    _fields_ = [("tol", C.c_double), ("max_iter", C.c_int), ("static_mat", C.c_int), ("pin_value", C.c_int),
+                ("precision", C.c_int), ("pre_sweeps", C.c_int), ("post_sweeps", C.c_int), ("coarse_max", C.c_int),
+                ("zero_guess", C.c_int)]
+
+
+class SolveState(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("rel_residual", C.c_double), ("abs_residual", C.c_double),
+                ("converged", C.c_int), ("setup_ms", C.c_double), ("solve_ms", C.c_double)]
+
+
+class ProblemDesc(C.Structure):
+    _fields_ = [("ndim", C.c_int), ("n", C.c_int * 3), ("loc", C.c_int), ("bc", C.c_int), ("h", C.c_double * 3),
+                ("alpha", C.c_double), ("beta", C.c_double)]
+
+
+class OpflowError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s: %s" % (STATUS_NAMES.get(code, code), msg))
+        self.code = code
+
+
+_lib = None
+
+_SIGS = {
+    "opflow_ctx_create": [C.c_int, C.POINTER(C.c_void_p)],
+    "opflow_ctx_destroy": [C.c_void_p],
+    "opflow_ctx_set_stream": [C.c_void_p, C.c_void_p],
+    "opflow_ctx_get_stream": [C.c_void_p, C.POINTER(C.c_void_p)],
+    "opflow_ctx_synchronize": [C.c_void_p],
+    "opflow_kernel_launch_count": [C.POINTER(C.c_uint64)],
+    "opflow_mesh_uniform": [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double)],
+    "opflow_field_describe": [C.POINTER(MeshDesc), C.POINTER(FieldDesc), C.POINTER(FieldInfo)],
+    "opflow_field_create": [C.c_void_p, C.POINTER(MeshDesc), C.POINTER(FieldDesc), C.POINTER(C.c_void_p)],
+    "opflow_field_destroy": [C.c_void_p],
+    "opflow_field_get_info": [C.c_void_p, C.POINTER(FieldInfo)],
+    "opflow_field_upload": [C.c_void_p, C.POINTER(C.c_double), C.c_size_t],
+    "opflow_field_download": [C.c_void_p, C.POINTER(C.c_double), C.c_size_t],
+    "opflow_field_device_ptr": [C.c_void_p, C.POINTER(C.c_void_p)],
+    "opflow_field_update_padding": [C.c_void_p],
+    "opflow_field_fill": [C.c_void_p, C.c_int, C.c_double],
+    "opflow_field_copy": [C.c_void_p, C.c_void_p],
+    "opflow_assign": [C.c_void_p, C.c_void_p, C.c_int, C.POINTER(Node), C.c_int, C.POINTER(C.c_void_p), C.c_int, C.c_int],
+    "opflow_assign_repeat": [C.c_void_p, C.c_void_p, C.c_int, C.POINTER(Node), C.c_int, C.POINTER(C.c_void_p), C.c_int,
+                             C.c_int, C.c_int],
+    "opflow_weno_rk3": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_int],
+    "opflow_assemble": [C.c_void_p, C.c_void_p, C.POINTER(Node), C.c_int, C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_int,
+                        C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_double),
+                        C.POINTER(C.c_size_t)],
+    "opflow_solve_params_default": [C.POINTER(SolveParams)],
+    "opflow_solver_create": [C.c_void_p, C.c_void_p, C.POINTER(Node), C.c_int, C.POINTER(C.c_void_p), C.c_int, C.c_int,
+                             C.POINTER(SolveParams), C.POINTER(C.c_void_p)],
+    "opflow_solver_solve": [C.c_void_p, C.POINTER(SolveState)],
+    "opflow_solver_destroy": [C.c_void_p],
+    "opflow_batch_create": [C.c_void_p, C.POINTER(ProblemDesc), C.c_int, C.POINTER(SolveParams), C.POINTER(C.c_void_p)],
+    "opflow_batch_vectors": [C.c_void_p, C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_size_t)],
+    "opflow_batch_solve": [C.c_void_p, C.POINTER(SolveState)],
+    "opflow_batch_destroy": [C.c_void_p],
+}
+
+
+def declared_symbols():
+    """Every function declared in include/opflow_gpu.h (parsed from the header)."""
+    import re
+    hdr = os.path.join(HERE, "..", "include", "opflow_gpu.h")
+    txt = open(hdr).read()
+    return sorted(set(re.findall(r"^\s*(?:int|void|const char\*)\s+(opflow_\w+)\s*\(", txt, flags=re.M)))
+
+
+def lib():
+    """The loaded library; raises if it was not built (no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise OpflowError(E_CUDA, "libopflow_gpu.so is not built; run `python -c 'import __graft_entry__ as g; g.build()'`")
+    L = C.CDLL(LIB_PATH)
+    for name, args in _SIGS.items():
+        fn = getattr(L, name, None)
+        if fn is None:
+            continue
+        fn.argtypes = args
+        fn.restype = None if name == "opflow_solve_params_default" else C.c_int
+    L.opflow_last_error.restype = C.c_char_p
+    L.opflow_last_error.argtypes = []
+    L.opflow_abi_version.restype = C.c_int
+    _lib = L
+    return L
+
+
+def check(rc):
+    if rc != OK:
+        raise OpflowError(rc, lib().opflow_last_error().decode(errors="replace"))
+    return rc
+
+
+def launch_count():
+    v = C.c_uint64(0)
+    check(lib().opflow_kernel_launch_count(C.byref(v)))
+    return v.value

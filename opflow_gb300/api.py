@@ -1,0 +1,521 @@
+"""Python mirror of OpFlow's user-facing API for the two accelerated paths.
+
+Names, argument meanings and error behaviour follow the reference (paths relative to the OpFlow tree):
+
+  MeshBuilder(CartesianMesh).newMesh(...).setMeshOfDim(d, min, max).build()
+                                   -> src/Core/Mesh/Structured/CartesianMesh.hpp:122-305
+  ExprBuilder().setMesh(m).setBC(d, DimPos.start, BCType.Dirc, v).setLoc(..).setExt(..).build()
+                                   -> src/Core/Field/MeshBased/Structured/CartesianField.hpp:796-1033
+  u.assign(u + dt * a * (d2x(u) + d2y(u)))        ( C++: u = u + dt*a*(d2x<D2SecondOrderCentered>(u) + ...) )
+                                   -> src/Core/Loops/FieldAssigner.hpp:27-84
+  Solve(lambda e: f == d2x(e) + d2y(e), p, params) / makeEqnSolveHandler(...)
+                                   -> src/Core/Equation/UnifiedSolve.hpp:36-43, HYPREEqnSolveHandler.hpp:44-48
+
+Python cannot overload `=`, so `u = expr` is spelled `u.assign(expr)` (and `u += expr` is
+`u.assign(expr, op="+")`).  Every call goes through the C ABI of libopflow_gpu.so.
+"""
+import ctypes as C
+import threading
+
+import numpy as np
+
+from . import _capi as capi
+from ._capi import check, lib
+
+
+class LocOnMesh:
+    Corner = capi.CORNER
+    Center = capi.CENTER
+
+
+class BCType:
+    Undefined = capi.BC_UNDEFINED
+    Dirc = capi.BC_DIRC
+    Neum = capi.BC_NEUM
+    Periodic = capi.BC_PERIODIC
+    Symm = capi.BC_SYMM
+    ASymm = capi.BC_ASYMM
+
+
+class DimPos:
+    start = 0
+    end = 1
+
+
+# ---------------------------------------------------------------------------------------------- context
+_ctx_lock = threading.Lock()
+_default_ctx = {}
+
+
+class Context:
+    """One device + one CUDA stream (opflow_ctx)."""
+
+    def __init__(self, device=0):
+        h = C.c_void_p()
+        check(lib().opflow_ctx_create(device, C.byref(h)))
+        self.handle = h
+        self.device = device
+
+    def synchronize(self):
+        check(lib().opflow_ctx_synchronize(self.handle))
+
+    def set_stream(self, stream_ptr):
+        check(lib().opflow_ctx_set_stream(self.handle, C.c_void_p(stream_ptr)))
+
+    def close(self):
+        if self.handle:
+            lib().opflow_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def default_context(device=0):
+    with _ctx_lock:
+        if device not in _default_ctx:
+            _default_ctx[device] = Context(device)
+        return _default_ctx[device]
+
+
+# ------------------------------------------------------------------------------------------------- mesh
+class CartesianMesh:
+    def __init__(self, ndim, dims, start, pad_width, x, dx):
+        self.ndim = ndim
+        self.dims = list(dims)
+        self.start = list(start)
+        self.pad_width = pad_width
+        self.x = [np.ascontiguousarray(v, dtype=np.float64) for v in x]
+        self.dx = [np.ascontiguousarray(v, dtype=np.float64) for v in dx]
+
+    def desc(self):
+        d = capi.MeshDesc()
+        d.ndim = self.ndim
+        for k in range(self.ndim):
+            d.dims[k] = self.dims[k]
+            d.start[k] = self.start[k]
+            d.x[k] = self.x[k].ctypes.data_as(C.POINTER(C.c_double))
+            d.dx[k] = self.dx[k].ctypes.data_as(C.POINTER(C.c_double))
+        d.pad_width = self.pad_width
+        d._keep = (self.x, self.dx)
+        return d
+
+    def getDims(self):
+        return list(self.dims)
+
+    def x_at(self, d, i):
+        return self.x[d][i - (self.start[d] - self.pad_width)]
+
+    def dx_at(self, d, i):
+        return self.dx[d][i - (self.start[d] - self.pad_width)]
+
+
+class MeshBuilder:
+    """MeshBuilder<CartesianMesh<Meta::int_<ndim>>>; padding width 5 and start 0 by default."""
+
+    def __init__(self, ndim=None):
+        self._ndim = ndim
+        self._dims = None
+        self._pad = 5
+        self._start = None
+        self._minmax = {}
+
+    def newMesh(self, *dims):
+        self._dims = [int(v) for v in dims]
+        if self._ndim is None:
+            self._ndim = len(self._dims)
+        if len(self._dims) != self._ndim:
+            raise ValueError("newMesh got %d extents for a %d-D mesh" % (len(self._dims), self._ndim))
+        return self
+
+    def setPadWidth(self, w):
+        self._pad = int(w)
+        return self
+
+    def setStart(self, s):
+        self._start = [int(v) for v in s]
+        return self
+
+    def setMeshOfDim(self, k, vmin, vmax):
+        self._minmax[int(k)] = (float(vmin), float(vmax))
+        return self
+
+    def build(self):
+        if self._dims is None:
+            raise ValueError("newMesh() was not called")
+        start = self._start or [0] * self._ndim
+        xs, dxs = [], []
+        for k in range(self._ndim):
+            n = self._dims[k] + 2 * self._pad
+            x = np.zeros(n)
+            dx = np.zeros(n - 1)
+            lo, hi = self._minmax.get(k, (0.0, 1.0))
+            check(lib().opflow_mesh_uniform(self._dims[k], start[k], self._pad, lo, hi,
+                                            x.ctypes.data_as(C.POINTER(C.c_double)),
+                                            dx.ctypes.data_as(C.POINTER(C.c_double))))
+            xs.append(x)
+            dxs.append(dx)
+        return CartesianMesh(self._ndim, self._dims, start, self._pad, xs, dxs)
+
+
+# ------------------------------------------------------------------------------------------ expressions
+class Expr:
+    """Base of every expression node; arithmetic builds trees (Expression<Op, Args...>)."""
+
+    def __add__(self, o):
+        return ExprNode(capi.NODE_ADD, self, _wrap(o))
+
+    def __radd__(self, o):
+        return ExprNode(capi.NODE_ADD, _wrap(o), self)
+
+    def __sub__(self, o):
+        return ExprNode(capi.NODE_SUB, self, _wrap(o))
+
+    def __rsub__(self, o):
+        return ExprNode(capi.NODE_SUB, _wrap(o), self)
+
+    def __mul__(self, o):
+        return ExprNode(capi.NODE_MUL, self, _wrap(o))
+
+    def __rmul__(self, o):
+        return ExprNode(capi.NODE_MUL, _wrap(o), self)
+
+    def __truediv__(self, o):
+        return ExprNode(capi.NODE_DIV, self, _wrap(o))
+
+    def __rtruediv__(self, o):
+        return ExprNode(capi.NODE_DIV, _wrap(o), self)
+
+    def __neg__(self):
+        return ExprNode(capi.NODE_NEG, self)
+
+    def __eq__(self, o):  # lhs == rhs -> Equation (Equation.hpp:41-55)
+        return Equation(self, _wrap(o))
+
+    def __hash__(self):
+        return id(self)
+
+
+class ScalarExpr(Expr):
+    def __init__(self, v):
+        self.value = float(v)
+
+
+def _wrap(o):
+    if isinstance(o, Expr):
+        return o
+    if isinstance(o, (int, float, np.floating, np.integer)):
+        return ScalarExpr(o)
+    raise TypeError("cannot use %r in an expression" % (o,))
+
+
+class ExprNode(Expr):
+    def __init__(self, kind, a=None, b=None, dim=0):
+        self.kind, self.a, self.b, self.dim = kind, a, b, dim
+
+
+class Equation:
+    """`lhs == rhs` (Equation.hpp:27-55); the solver works on the tree of `lhs - rhs`."""
+
+    def __init__(self, lhs, rhs):
+        self.lhs, self.rhs = lhs, rhs
+
+    def residual_expr(self):
+        return ExprNode(capi.NODE_SUB, self.lhs, self.rhs)
+
+
+def Eq(lhs, rhs):
+    """`lhs == rhs` with the operands kept in this order even when lhs is a plain number (Python
+    would otherwise reflect `1.0 == expr` into `expr == 1.0`)."""
+    return Equation(_wrap(lhs), _wrap(rhs))
+
+
+def _diff(kind, dim):
+    def f(e):
+        return ExprNode(kind, _wrap(e), None, dim)
+    return f
+
+
+# D2SecondOrderCentered<d> (DiffsInterface.hpp:47)
+def d2(e, dim):
+    return ExprNode(capi.NODE_D2, _wrap(e), None, dim)
+
+
+d2x, d2y, d2z = _diff(capi.NODE_D2, 0), _diff(capi.NODE_D2, 1), _diff(capi.NODE_D2, 2)
+
+
+# D1FirstOrderCentered<d>: dx/dy/dz<D1FirstOrderCentered>
+def d1(e, dim):
+    return ExprNode(capi.NODE_D1, _wrap(e), None, dim)
+
+
+dx, dy, dz = _diff(capi.NODE_D1, 0), _diff(capi.NODE_D1, 1), _diff(capi.NODE_D1, 2)
+
+
+# d1<D1WENO53Downwind<d>> / d1<D1WENO53Upwind<d>>
+def d1_weno53_downwind(e, dim=0):
+    return ExprNode(capi.NODE_WENO53_DOWN, _wrap(e), None, dim)
+
+
+def d1_weno53_upwind(e, dim=0):
+    return ExprNode(capi.NODE_WENO53_UP, _wrap(e), None, dim)
+
+
+# d1IntpCenterToCorner<d> (IntpInterface.hpp:22-33, D1Linear Cen2Cor)
+def d1IntpCenterToCorner(e, dim):
+    return ExprNode(capi.NODE_INTP_C2C, _wrap(e), None, dim)
+
+
+def serialize(expr, extra_leaves=()):
+    """Postfix node list (children first, root last) and the ordered leaf fields."""
+    nodes = []
+    leaves = list(extra_leaves)
+    memo = {}
+
+    def leaf_slot(f):
+        for i, g in enumerate(leaves):
+            if g is f:
+                return i
+        leaves.append(f)
+        return len(leaves) - 1
+
+    def rec(e):
+        key = id(e)
+        is_leaf = getattr(e, "_is_field", False)
+        if key in memo and not is_leaf:
+            return memo[key]
+        if is_leaf:
+            n = (capi.NODE_FIELD, -1, -1, 0, leaf_slot(e), 0.0)
+        elif isinstance(e, ScalarExpr):
+            n = (capi.NODE_CONST, -1, -1, 0, 0, e.value)
+        elif isinstance(e, ExprNode):
+            a = rec(e.a) if e.a is not None else -1
+            b = rec(e.b) if e.b is not None else -1
+            n = (e.kind, a, b, e.dim, 0, 0.0)
+        else:
+            raise TypeError("not an expression: %r" % (e,))
+        nodes.append(n)
+        memo[key] = len(nodes) - 1
+        return len(nodes) - 1
+
+    rec(_wrap(expr))
+    arr = (capi.Node * len(nodes))()
+    for i, (k, a, b, d, f, v) in enumerate(nodes):
+        arr[i].kind, arr[i].a, arr[i].b, arr[i].dim, arr[i].field, arr[i].value = k, a, b, d, f, v
+    return arr, leaves
+
+
+# ------------------------------------------------------------------------------------------------ field
+_ARITH = {"=": capi.ASSIGN_EQ, "+": capi.ASSIGN_ADD, "-": capi.ASSIGN_SUB, "*": capi.ASSIGN_MUL, "/": capi.ASSIGN_DIV}
+_MODES = {"exact": capi.EVAL_EXACT, "fast": capi.EVAL_FAST}
+
+
+class CartesianField(Expr):
+    """CartesianField<Real, CartesianMesh<Dim>> whose data lives in HBM."""
+
+    _is_field = True
+
+    def __init__(self, mesh, desc, ctx, name="field"):
+        self.mesh = mesh
+        self.desc = desc
+        self.ctx = ctx
+        self.name = name
+        h = C.c_void_p()
+        md = mesh.desc()
+        check(lib().opflow_field_create(ctx.handle, C.byref(md), C.byref(desc), C.byref(h)))
+        self.handle = h
+        info = capi.FieldInfo()
+        check(lib().opflow_field_get_info(h, C.byref(info)))
+        self.info = info
+
+    # ---- ranges (CartesianField / StructuredFieldExpr members) ----
+    def _rng(self, which):
+        r = getattr(self.info, which)
+        return [(r[d][0], r[d][1]) for d in range(self.info.ndim)]
+
+    @property
+    def assignableRange(self):
+        return self._rng("assignable")
+
+    @property
+    def accessibleRange(self):
+        return self._rng("accessible")
+
+    @property
+    def logicalRange(self):
+        return self._rng("logical")
+
+    @property
+    def localRange(self):
+        return self._rng("local")
+
+    @property
+    def padding(self):
+        return self.info.padding
+
+    @property
+    def shape(self):
+        """numpy shape of the full data array (z, y, x order; x fastest)."""
+        D = self.info.ndim
+        return tuple(self.info.data_dims[d] for d in reversed(range(D)))
+
+    @property
+    def offset(self):
+        return [self.info.data_offset[d] for d in range(self.info.ndim)]
+
+    # ---- data movement ----
+    def download(self):
+        a = np.empty(self.info.count, dtype=np.float64)
+        check(lib().opflow_field_download(self.handle, a.ctypes.data_as(C.POINTER(C.c_double)), a.size))
+        return a.reshape(self.shape)
+
+    def upload(self, arr, update_padding=True):
+        a = np.ascontiguousarray(arr, dtype=np.float64).reshape(-1)
+        check(lib().opflow_field_upload(self.handle, a.ctypes.data_as(C.POINTER(C.c_double)), a.size))
+        if update_padding:
+            self.updatePadding()
+
+    def updatePadding(self):
+        check(lib().opflow_field_update_padding(self.handle))
+
+    def device_ptr(self):
+        p = C.c_void_p()
+        check(lib().opflow_field_device_ptr(self.handle, C.byref(p)))
+        return p.value
+
+    def index_slices(self, ranges):
+        """numpy slices (z, y, x order) of the data array covering the given index ranges."""
+        D = self.info.ndim
+        sl = []
+        for d in reversed(range(D)):
+            lo, hi = ranges[d]
+            o = self.info.data_offset[d]
+            sl.append(slice(lo - o, hi - o))
+        return tuple(sl)
+
+    # ---- assignment ----
+    def assign(self, expr, op="=", mode="exact", steps=1):
+        """`self <op>= expr` (Expr::operator=, +=, ... through FieldAssigner::assign)."""
+        if isinstance(expr, (int, float)):
+            check(lib().opflow_field_fill(self.handle, _ARITH[op], float(expr)))
+            return self
+        if isinstance(expr, CartesianField) and op == "=" and expr is not self:
+            if expr.info.count == self.info.count:
+                check(lib().opflow_field_copy(self.handle, expr.handle))
+                return self
+        nodes, leaves = serialize(expr)
+        hs = (C.c_void_p * max(1, len(leaves)))(*[f.handle.value for f in leaves])
+        check(lib().opflow_assign_repeat(self.ctx.handle, self.handle, _ARITH[op], nodes, len(nodes), hs, len(leaves),
+                                         _MODES[mode], int(steps)))
+        return self
+
+    def initBy(self, fn):
+        """CartesianField::initBy (CartesianField.hpp:282-294): fn(coords) at nodes or cell centres."""
+        D = self.info.ndim
+        a = self.download()
+        rng = [(max(self.info.assignable[d][0], self.info.local[d][0]), min(self.info.assignable[d][1], self.info.local[d][1]))
+               for d in range(D)]
+        grids = []
+        for d in range(D):
+            idx = np.arange(rng[d][0], rng[d][1])
+            x = np.array([self.mesh.x_at(d, i) for i in idx])
+            if self.desc.loc[d] == capi.CENTER:
+                x = x + .5 * np.array([self.mesh.dx_at(d, i) for i in idx])
+            grids.append(x)
+        mesh = np.meshgrid(*grids, indexing="ij")
+        vals = np.asarray(fn(mesh), dtype=np.float64)
+        a[self.index_slices(rng)] = np.transpose(vals) if D > 1 else vals
+        self.upload(a)
+        return self
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().opflow_field_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class ExprBuilder:
+    """ExprBuilder<CartesianField<Real, Mesh>>."""
+
+    def __init__(self):
+        self._mesh = None
+        self._name = "field"
+        self._loc = None
+        self._bc = {}
+        self._ext = {}
+        self._padding = 0
+
+    def setName(self, n):
+        self._name = n
+        return self
+
+    def setMesh(self, m):
+        self._mesh = m
+        return self
+
+    def setLoc(self, loc):
+        if isinstance(loc, (list, tuple)):
+            self._loc = list(loc)
+        else:
+            self._loc = loc
+        return self
+
+    def setLocOfDim(self, d, loc):
+        if not isinstance(self._loc, list):
+            self._loc = [self._loc if self._loc is not None else LocOnMesh.Corner] * 3
+        self._loc[d] = loc
+        return self
+
+    def setBC(self, d, pos, bctype, value=0.0):
+        self._bc[(d, pos)] = (bctype, float(value))
+        return self
+
+    def setExt(self, *args):
+        if len(args) == 1:
+            for d in range(3):
+                self._ext[(d, 0)] = self._ext[(d, 1)] = int(args[0])
+        else:
+            d, pos, w = args
+            self._ext[(d, pos)] = int(w)
+        return self
+
+    def setPadding(self, p):
+        self._padding = int(p)
+        return self
+
+    def desc(self):
+        if self._mesh is None:
+            raise ValueError("setMesh() was not called")
+        D = self._mesh.ndim
+        fd = capi.FieldDesc()
+        fd.ndim = D
+        loc = self._loc
+        for d in range(D):
+            fd.loc[d] = loc[d] if isinstance(loc, list) else (loc if loc is not None else LocOnMesh.Corner)
+            for s in range(2):
+                t, v = self._bc.get((d, s), (BCType.Undefined, 0.0))
+                fd.bc_type[d][s] = t
+                fd.bc_value[d][s] = v
+                fd.ext[d][s] = self._ext.get((d, s), 0)
+        fd.padding = self._padding
+        return fd
+
+    def build(self, ctx=None):
+        return CartesianField(self._mesh, self.desc(), ctx or default_context(), self._name)
+
+
+def describe(mesh, desc):
+    """Ranges ExprBuilder::build computes, without touching a GPU (opflow_field_describe)."""
+    info = capi.FieldInfo()
+    md = mesh.desc()
+    check(lib().opflow_field_describe(C.byref(md), C.byref(desc), C.byref(info)))
+    return info

@@ -1,0 +1,102 @@
+// Internal declarations shared by the translation units of libopflow_gpu.so.
+#pragma once
+#include "../../include/opflow_gpu.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <array>
+#include <atomic>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+namespace opg {
+
+// ---- errors -----------------------------------------------------------------------------------------
+void set_error(const char* fmt, ...);
+int fail(int code, const char* fmt, ...);
+#define OPG_CUDA(call)                                                                                         \
+    do {                                                                                                       \
+        cudaError_t e_ = (call);                                                                               \
+        if (e_ != cudaSuccess) return ::opg::fail(OPFLOW_E_CUDA, "%s failed: %s (%s:%d)", #call,              \
+                                                  cudaGetErrorString(e_), __FILE__, __LINE__);                \
+    } while (0)
+#define OPG_TRY(call)                                                                                          \
+    do {                                                                                                       \
+        int rc_ = (call);                                                                                      \
+        if (rc_ != OPFLOW_OK) return rc_;                                                                      \
+    } while (0)
+
+// Every kernel launch goes through this counter (gpu_launches accounting in the bench).
+extern std::atomic<uint64_t> g_launches;
+#define OPG_LAUNCHED() (::opg::g_launches.fetch_add(1, std::memory_order_relaxed))
+int check_launch(const char* what);
+
+// ---- geometry ---------------------------------------------------------------------------------------
+struct Box {
+    int lo[3] = {0, 0, 0}, hi[3] = {1, 1, 1};
+    long long count() const {
+        long long c = 1;
+        for (int d = 0; d < 3; ++d) c *= (hi[d] > lo[d] ? hi[d] - lo[d] : 0);
+        return c;
+    }
+    bool empty() const { return count() == 0; }
+};
+
+// Device view of a field's data array and the ranges the kernels need.
+struct FieldView {
+    double* data;
+    int off[3];      // index of element 0
+    int dims[3];     // data extents
+    long long sy, sz;  // strides (x fastest)
+};
+
+struct MeshDev {
+    int ndim;
+    int es[3];          // first index of the extended mesh range (start - pad_width)
+    int n[3];           // number of nodes in the extended range
+    double* x[3];       // device arrays
+    double* dx[3];
+    // host copies
+    std::vector<double> hx[3], hdx[3];
+    bool uniform[3];
+    double h[3];        // uniform spacing (valid when uniform[d])
+};
+
+}  // namespace opg
+
+struct opflow_ctx_s {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int num_sms = 0;
+    // scratch for reductions (grown on demand)
+    void* scratch = nullptr;
+    size_t scratch_bytes = 0;
+};
+
+struct opflow_field_s {
+    opflow_ctx ctx = nullptr;
+    opflow_field_desc desc{};
+    opflow_field_info info{};
+    opg::MeshDev* mesh = nullptr;  // shared (reference counted by owner fields)
+    int mesh_refs_owner = 1;
+    double* buf[2] = {nullptr, nullptr};  // front = buf[cur]; back allocated on the first aliased assign
+    int cur = 0;
+    opg::FieldView view() const;
+    opg::FieldView view_back() const;
+};
+
+namespace opg {
+int mesh_create(const opflow_mesh_desc* m, MeshDev** out);
+void mesh_destroy(MeshDev* m);
+bool mesh_equal(const MeshDev* a, const MeshDev* b);
+int ensure_back(opflow_field f);
+int update_padding_buf(opflow_field f, double* data);
+int ensure_scratch(opflow_ctx ctx, size_t bytes);
+int compute_info(const opflow_mesh_desc* m, const opflow_field_desc* f, opflow_field_info* o);
+Box assign_box(const opflow_field_info& r);
+}  // namespace opg

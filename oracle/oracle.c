@@ -1,0 +1,872 @@
+/* oracle.c -- CPU restatement of OpFlow's explicit-evaluation and stencil-assembly paths.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the checker the tests, __graft_entry__.smoke() and the
+ * CPU-baseline leg of bench.py compare the CUDA library against.  It is never linked into, loaded by or
+ * called from the product path (opflow_gb300/).
+ *
+ * Parity is pinned: tests/test_oracle_golden.py checks this restatement bit-for-bit against dumps of
+ * the reference itself (oracle/_ref/ref_driver built from the OpFlow sources by oracle/build_ref.sh,
+ * stored under tests/golden/) and against the literal CSR matrices of the reference's
+ * test/Core/Equation/CSRMatrixGeneratorTest.cpp.
+ *
+ * Everything follows the reference's evaluation order operation by operation and is compiled with
+ * -ffp-contract=off, so no multiply-add is fused that the reference (built for x86-64, no FMA) keeps
+ * separate.  File:line citations are relative to the OpFlow source tree.
+ */
+#include "../include/opflow_gpu.h"
+
+#include <math.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define MAXD 3
+static char g_err[512];
+const char* or_last_error(void) { return g_err; }
+static int fail(int code, const char* msg) {
+    snprintf(g_err, sizeof g_err, "%s", msg);
+    return code;
+}
+
+/* ------------------------------------------------------------------------------------------------ */
+/* seeded inputs (counter-based splitmix64), identical to the generator used by the tests           */
+/* ------------------------------------------------------------------------------------------------ */
+static inline uint64_t mix64(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+double or_u01(uint64_t seed, uint64_t k) {
+    return (double) (mix64(seed + (k + 1) * 0x9E3779B97F4A7C15ull) >> 11) * 0x1.0p-53;
+}
+
+/* ------------------------------------------------------------------------------------------------ */
+/* mesh: MeshBuilder<CartesianMesh>::set1DRange / set1DMesh(min,max) / setExtMesh (Symm)             */
+/* CartesianMesh.hpp:209-217, 219-237, 268-276, 292-303                                              */
+/* ------------------------------------------------------------------------------------------------ */
+int or_mesh_uniform(int dims, int start, int pad, double min, double max, double* x, double* dx) {
+    if (dims < 2 || pad < 0) return fail(OPFLOW_E_INVALID, "mesh needs >= 2 nodes");
+    const int es = start - pad, end = start + dims, ee = end + pad;
+    for (int i = start; i < end; ++i) x[i - es] = (max - min) / (double) (dims - 1) * (double) (i - start) + min;
+    for (int j = start; j < end - 1; ++j) dx[j - es] = (max - min) / (double) (dims - 1);
+    /* Symm extension of dx (the default MeshExtMode) */
+    for (int i = es; i < start; ++i) dx[i - es] = dx[2 * start - 1 - i - es];
+    for (int i = end - 1; i < ee - 1; ++i) dx[i - es] = dx[2 * end - 3 - i - es];
+    /* integrate x into the ghost extension */
+    for (int i = start - 1; i >= es; --i) x[i - es] = x[i + 1 - es] - dx[i - es];
+    for (int i = end; i < ee; ++i) x[i - es] = x[i - 1 - es] + dx[i - 1 - es];
+    return OPFLOW_OK;
+}
+
+typedef struct {
+    const opflow_mesh_desc* m;
+} Mesh;
+static inline double mesh_x(const opflow_mesh_desc* m, int d, int i) { return m->x[d][i - (m->start[d] - m->pad_width)]; }
+static inline double mesh_dx(const opflow_mesh_desc* m, int d, int i) { return m->dx[d][i - (m->start[d] - m->pad_width)]; }
+
+/* ------------------------------------------------------------------------------------------------ */
+/* field ranges: ExprBuilder::calculateRanges / validateRanges / build (CartesianField.hpp:929-1029) */
+/* ------------------------------------------------------------------------------------------------ */
+static inline int imax(int a, int b) { return a > b ? a : b; }
+static inline int imin(int a, int b) { return a < b ? a : b; }
+
+int or_field_info(const opflow_mesh_desc* m, const opflow_field_desc* f, opflow_field_info* o) {
+    if (!m || !f || !o || f->ndim != m->ndim || f->ndim < 1 || f->ndim > 3) return fail(OPFLOW_E_INVALID, "bad field description");
+    memset(o, 0, sizeof *o);
+    const int D = f->ndim;
+    o->ndim = D;
+    int pad = f->padding;
+    for (int d = 0; d < D; ++d) pad = imax(pad, imax(f->ext[d][0], f->ext[d][1]));
+    o->padding = pad;
+    for (int d = 0; d < D; ++d) {
+        int s = m->start[d], e = m->start[d] + m->dims[d];
+        o->logical[d][0] = o->assignable[d][0] = o->local[d][0] = o->accessible[d][0] = s;
+        o->logical[d][1] = o->assignable[d][1] = o->local[d][1] = o->accessible[d][1] = e;
+    }
+    for (int d = 0; d < D; ++d) {
+        const int loc = f->loc[d];
+        switch (f->bc_type[d][0]) {
+            case OPFLOW_BC_DIRC:
+                if (loc == OPFLOW_CORNER) o->assignable[d][0]++;
+                break;
+            case OPFLOW_BC_NEUM: case OPFLOW_BC_UNDEFINED: case OPFLOW_BC_SYMM: case OPFLOW_BC_ASYMM: case OPFLOW_BC_PERIODIC:
+                break;
+            default: return fail(OPFLOW_E_INVALID, "unknown bc type");
+        }
+        switch (f->bc_type[d][1]) {
+            case OPFLOW_BC_DIRC:
+                if (loc == OPFLOW_CORNER) o->assignable[d][1]--;
+                else { o->accessible[d][1]--; o->assignable[d][1]--; }
+                break;
+            case OPFLOW_BC_NEUM: case OPFLOW_BC_UNDEFINED: case OPFLOW_BC_SYMM: case OPFLOW_BC_ASYMM:
+                if (loc == OPFLOW_CENTER) { o->accessible[d][1]--; o->assignable[d][1]--; }
+                break;
+            case OPFLOW_BC_PERIODIC:
+                o->accessible[d][1]--; o->assignable[d][1]--;
+                break;
+            default: return fail(OPFLOW_E_INVALID, "unknown bc type");
+        }
+        o->logical[d][0] = o->accessible[d][0] - f->ext[d][0];
+        o->logical[d][1] = o->accessible[d][1] + f->ext[d][1];
+    }
+    for (int d = 0; d < D; ++d) {
+        o->local[d][0] = o->accessible[d][0];
+        o->local[d][1] = o->accessible[d][1];
+        /* validateRanges */
+        o->accessible[d][0] = imax(o->accessible[d][0], o->logical[d][0]);
+        o->accessible[d][1] = imin(o->accessible[d][1], o->logical[d][1]);
+        o->local[d][0] = imax(o->local[d][0], o->logical[d][0]);
+        o->local[d][1] = imin(o->local[d][1], o->logical[d][1]);
+        o->assignable[d][0] = imax(o->assignable[d][0], o->accessible[d][0]);
+        o->assignable[d][1] = imin(o->assignable[d][1], o->accessible[d][1]);
+    }
+    o->count = 1;
+    for (int d = 0; d < 3; ++d) {
+        if (d < D) {
+            o->data_offset[d] = o->local[d][0] - pad;
+            o->data_dims[d] = o->local[d][1] - o->local[d][0] + 2 * pad;
+        } else {
+            o->data_offset[d] = 0;
+            o->data_dims[d] = 1;
+            o->logical[d][1] = o->accessible[d][1] = o->assignable[d][1] = o->local[d][1] = 1;
+        }
+        o->count *= (size_t) o->data_dims[d];
+    }
+    return OPFLOW_OK;
+}
+
+/* ------------------------------------------------------------------------------------------------ */
+/* a field = description + ranges + host data                                                       */
+/* ------------------------------------------------------------------------------------------------ */
+typedef struct {
+    const opflow_field_desc* d;
+    opflow_field_info r;
+    double* data;
+} Field;
+
+static int g_range_err;
+static inline int in_data(const Field* f, const int* i) {
+    for (int d = 0; d < f->r.ndim; ++d)
+        if (i[d] < f->r.data_offset[d] || i[d] >= f->r.data_offset[d] + f->r.data_dims[d]) return 0;
+    return 1;
+}
+/* PlainTensor::getOffset (PlainTensor.hpp:204-213): x fastest */
+static inline size_t lin(const Field* f, const int* i) {
+    size_t o = 0;
+    for (int d = f->r.ndim - 1; d >= 0; --d) o = o * (size_t) f->r.data_dims[d] + (size_t) (i[d] - f->r.data_offset[d]);
+    return o;
+}
+static inline double fget(const Field* f, const int* i) {
+    if (!in_data(f, i)) { g_range_err = 1; return NAN; }
+    return f->data[lin(f, i)];
+}
+static inline void fset(Field* f, const int* i, double v) {
+    if (!in_data(f, i)) { g_range_err = 1; return; }
+    f->data[lin(f, i)] = v;
+}
+
+/* iterate a box [lo, hi) x fastest */
+#define BOX_FOR(D, lo, hi, idx)                                                                               \
+    for (idx[2] = (D > 2 ? lo[2] : 0); idx[2] < (D > 2 ? hi[2] : 1); ++idx[2])                              \
+        for (idx[1] = (D > 1 ? lo[1] : 0); idx[1] < (D > 1 ? hi[1] : 1); ++idx[1])                          \
+            for (idx[0] = lo[0]; idx[0] < hi[0]; ++idx[0])
+
+/* Interpolator1D::intp(x1, y1, x2, y2, x) (src/Math/Interpolator/Interpolator.hpp:21-23,38-40) */
+static inline double intp_d(double x1, double y1, double x2, double y2, double x) {
+    double a = x1 - x, b = x2 - x;
+    return (a * y2 - b * y1) / (a - b);
+}
+
+/* ------------------------------------------------------------------------------------------------ */
+/* CartesianField::updatePaddingImpl_final, single-rank branch (CartesianField.hpp:349-629)         */
+/* ------------------------------------------------------------------------------------------------ */
+static void update_padding(const opflow_mesh_desc* m, Field* f) {
+    const int D = f->r.ndim;
+    const opflow_field_info* R = &f->r;
+    int idx[3], lo[3], hi[3];
+    /* step 0: Dirichlet values on corner-located boundary nodes (lines 350-364) */
+    for (int i = 0; i < D; ++i) {
+        if (R->local[i][0] == R->accessible[i][0] && f->d->bc_type[i][0] == OPFLOW_BC_DIRC && f->d->loc[i] == OPFLOW_CORNER) {
+            for (int k = 0; k < 3; ++k) { lo[k] = R->local[k][0]; hi[k] = R->local[k][1]; }
+            lo[i] = R->local[i][0]; hi[i] = lo[i] + 1;
+            BOX_FOR(D, lo, hi, idx) fset(f, idx, f->d->bc_value[i][0]);
+        }
+        if (R->local[i][1] == R->accessible[i][1] && f->d->bc_type[i][1] == OPFLOW_BC_DIRC && f->d->loc[i] == OPFLOW_CORNER) {
+            for (int k = 0; k < 3; ++k) { lo[k] = R->local[k][0]; hi[k] = R->local[k][1]; }
+            lo[i] = R->local[i][1] - 1; hi[i] = lo[i] + 1;
+            BOX_FOR(D, lo, hi, idx) fset(f, idx, f->d->bc_value[i][1]);
+        }
+    }
+    /* step 1: padding zones by BC extension (lines 365-606) */
+    int st[3] = {0, 0, 0}, en[3] = {0, 0, 0};
+    for (int i = 0; i < D; ++i) {
+        for (int side = 0; side < 2; ++side) {
+            const int bct = f->d->bc_type[i][side];
+            const double bcv = f->d->bc_value[i][side];
+            const int at_bound = side == 0 ? R->local[i][0] == R->accessible[i][0] : R->local[i][1] == R->accessible[i][1];
+            if (!(at_bound && bct != OPFLOW_BC_UNDEFINED && bct != OPFLOW_BC_PERIODIC)) {
+                if (side == 0) st[i] = R->local[i][0];
+                else en[i] = R->local[i][1];
+                continue;
+            }
+            if (side == 0) st[i] = R->logical[i][0];
+            else en[i] = R->logical[i][1];
+            for (int k = 0; k < 3; ++k) { lo[k] = R->local[k][0]; hi[k] = R->local[k][1]; }
+            for (int j = 0; j < i; ++j) { lo[j] = st[j]; hi[j] = en[j]; }
+            if (side == 0) { lo[i] = st[i]; hi[i] = R->local[i][0]; }
+            else { lo[i] = R->local[i][1]; hi[i] = R->logical[i][1]; }
+            const int corner = f->d->loc[i] == OPFLOW_CORNER;
+            BOX_FOR(D, lo, hi, idx) {
+                int mi[3] = {idx[0], idx[1], idx[2]};
+                if (corner) mi[i] = side == 0 ? 2 * R->local[i][0] - idx[i] : 2 * R->local[i][1] - 2 - idx[i];
+                else mi[i] = side == 0 ? 2 * R->local[i][0] - 1 - idx[i] : 2 * R->local[i][1] - 1 - idx[i];
+                double v = 0.;
+                switch (bct) {
+                    case OPFLOW_BC_DIRC:
+                        if (corner) {
+                            double xb = mesh_x(m, i, side == 0 ? R->local[i][0] : R->local[i][1] - 1);
+                            v = intp_d(xb, bcv, mesh_x(m, i, mi[i]), fget(f, mi), mesh_x(m, i, idx[i]));
+                        } else {
+                            double xb = mesh_x(m, i, side == 0 ? R->local[i][0] : R->local[i][1]);
+                            v = intp_d(xb, bcv, mesh_x(m, i, mi[i]) + mesh_dx(m, i, mi[i]) / 2., fget(f, mi),
+                                       mesh_x(m, i, idx[i]) + mesh_dx(m, i, idx[i]) / 2.);
+                        }
+                        break;
+                    case OPFLOW_BC_NEUM:
+                        if (corner) v = fget(f, mi) + bcv * (mesh_x(m, i, idx[i]) - mesh_x(m, i, mi[i]));
+                        else
+                            v = fget(f, mi) + bcv * (mesh_x(m, i, idx[i]) + mesh_dx(m, i, idx[i]) / 2. - mesh_x(m, i, mi[i])
+                                                     - mesh_dx(m, i, mi[i]) / 2.);
+                        break;
+                    case OPFLOW_BC_SYMM: v = fget(f, mi); break;
+                    case OPFLOW_BC_ASYMM: v = -fget(f, mi); break;
+                }
+                fset(f, idx, v);
+            }
+        }
+    }
+    /* step 2: periodic copies over the logical range (lines 609-629) */
+    for (int i = 0; i < D; ++i) {
+        if (f->d->bc_type[i][0] != OPFLOW_BC_PERIODIC) continue;
+        const int period = R->accessible[i][1] - R->accessible[i][0];
+        for (int k = 0; k < 3; ++k) { lo[k] = R->logical[k][0]; hi[k] = R->logical[k][1]; }
+        lo[i] = R->logical[i][0]; hi[i] = R->accessible[i][0];
+        BOX_FOR(D, lo, hi, idx) {
+            int mi[3] = {idx[0], idx[1], idx[2]};
+            mi[i] += period;
+            fset(f, idx, fget(f, mi));
+        }
+        for (int k = 0; k < 3; ++k) { lo[k] = R->logical[k][0]; hi[k] = R->logical[k][1]; }
+        lo[i] = R->accessible[i][1]; hi[i] = R->logical[i][1];
+        BOX_FOR(D, lo, hi, idx) {
+            int mi[3] = {idx[0], idx[1], idx[2]};
+            mi[i] -= period;
+            fset(f, idx, fget(f, mi));
+        }
+    }
+}
+
+int or_update_padding(const opflow_mesh_desc* m, const opflow_field_desc* fd, double* data) {
+    Field f = {fd, {0}, data};
+    int rc = or_field_info(m, fd, &f.r);
+    if (rc) return rc;
+    g_range_err = 0;
+    update_padding(m, &f);
+    return g_range_err ? fail(OPFLOW_E_RANGE, "padding read outside the data array") : OPFLOW_OK;
+}
+
+/* ------------------------------------------------------------------------------------------------ */
+/* expression trees: location propagation (the operators' prepare())                                */
+/* ------------------------------------------------------------------------------------------------ */
+typedef struct {
+    const opflow_mesh_desc* m;
+    const opflow_node* nodes;
+    int n;
+    Field* fields;
+    int nf;
+    int loc[64][3]; /* loc per node, -1 for scalar-valued nodes */
+    int unknown;    /* leaf slot of the unknown for stencil evaluation, -1 otherwise */
+    int pin;
+    /* StencilField ranges (after ignorePeriodicBC, StencilField.hpp:112-121) */
+    int st_assignable[3][2], st_accessible[3][2], st_logical[3][2];
+    int pin_index[3];
+} Ctx;
+
+static int compute_locs(Ctx* c) {
+    if (c->n > 64) return fail(OPFLOW_E_UNSUPPORTED, "expression too large");
+    for (int k = 0; k < c->n; ++k) {
+        const opflow_node* nd = &c->nodes[k];
+        int* L = c->loc[k];
+        L[0] = L[1] = L[2] = -1;
+        if ((nd->a >= k) || (nd->b >= k)) return fail(OPFLOW_E_INVALID, "children must precede parents");
+        switch (nd->kind) {
+            case OPFLOW_NODE_FIELD:
+                if (nd->field < 0 || nd->field >= c->nf) return fail(OPFLOW_E_INVALID, "bad leaf slot");
+                for (int d = 0; d < 3; ++d) L[d] = c->fields[nd->field].d->loc[d];
+                break;
+            case OPFLOW_NODE_CONST: break;
+            case OPFLOW_NODE_ADD: case OPFLOW_NODE_SUB: case OPFLOW_NODE_MUL: case OPFLOW_NODE_DIV: {
+                /* initPropsFrom(arg1), or arg2 when arg1 is a scalar (BinOpDefMacros.hpp.in:18-71) */
+                const int* La = c->loc[nd->a];
+                const int* Lb = c->loc[nd->b];
+                for (int d = 0; d < 3; ++d) L[d] = La[0] >= 0 ? La[d] : Lb[d];
+                break;
+            }
+            case OPFLOW_NODE_NEG: case OPFLOW_NODE_D2: case OPFLOW_NODE_WENO53_DOWN: case OPFLOW_NODE_WENO53_UP:
+                for (int d = 0; d < 3; ++d) L[d] = c->loc[nd->a][d];
+                break;
+            case OPFLOW_NODE_D1: /* D1FirstOrderCentered.hpp:38-56: the location flips along dim */
+                for (int d = 0; d < 3; ++d) L[d] = c->loc[nd->a][d];
+                L[nd->dim] = L[nd->dim] == OPFLOW_CENTER ? OPFLOW_CORNER : OPFLOW_CENTER;
+                break;
+            case OPFLOW_NODE_INTP_C2C: /* D1Linear.hpp:48-58 */
+                for (int d = 0; d < 3; ++d) L[d] = c->loc[nd->a][d];
+                L[nd->dim] = OPFLOW_CORNER;
+                break;
+            default: return fail(OPFLOW_E_UNSUPPORTED, "unknown node kind");
+        }
+        if (nd->kind >= OPFLOW_NODE_D2 && (nd->dim < 0 || nd->dim >= c->m->ndim)) return fail(OPFLOW_E_INVALID, "bad operator dim");
+        if (nd->kind != OPFLOW_NODE_FIELD && nd->kind != OPFLOW_NODE_CONST && nd->a < 0) return fail(OPFLOW_E_INVALID, "missing operand");
+        if (nd->kind >= OPFLOW_NODE_ADD && nd->kind <= OPFLOW_NODE_DIV && nd->b < 0) return fail(OPFLOW_E_INVALID, "missing operand");
+    }
+    return OPFLOW_OK;
+}
+
+/* ------------------------------------------------------------------------------------------------ */
+/* double-valued evaluation: Expression::evalAtImpl_final recursion (Expression.hpp:51-88)          */
+/* ------------------------------------------------------------------------------------------------ */
+static inline double pow2d(double a) { return a * a; } /* Math::pow2 (Numeric.hpp:104) */
+
+/* D1WENO53Downwind::kernel (D1WENO53Downwind.hpp:136-154); D1WENO53Upwind::kernel has the same body
+ * (D1WENO53Upwind.hpp:133-151) with its arguments taken from the other side. */
+static double weno_kernel(double pm3, double pm2, double pm1, double p0, double pp1, double pp2, double h) {
+    double d1 = (pm2 - pm3) / h, d2 = (pm1 - pm2) / h, d3 = (p0 - pm1) / h, d4 = (pp1 - p0) / h, d5 = (pp2 - pp1) / h;
+    double ddx1 = d1 / 3. - 7. * d2 / 6. + 11. * d3 / 6.;
+    double ddx2 = -d2 / 6. + 5 * d3 / 6 + d4 / 3;
+    double ddx3 = d3 / 3 + 5 * d4 / 6 - d5 / 6;
+    double s1 = 13. / 12. * pow2d(d1 - 2 * d2 + d3) + pow2d(d1 - 4 * d2 + 3 * d3) / 4;
+    double s2 = 13. / 12. * pow2d(d2 - 2 * d3 + d4) + pow2d(d2 - d4) / 4.;
+    double s3 = 13. / 12. * pow2d(d3 - 2 * d4 + d5) + pow2d(3 * d3 - 4 * d4 + d5) / 4.;
+    /* std::max({...}) over an initializer list: first maximal element, compared with < */
+    double mx = d1 * d1, t;
+    t = d2 * d2; if (mx < t) mx = t;
+    t = d3 * d3; if (mx < t) mx = t;
+    t = d4 * d4; if (mx < t) mx = t;
+    t = d5 * d5; if (mx < t) mx = t;
+    const double eps = 1e-6 * mx + 1e-99;
+    double a1 = .1 / pow2d(s1 + eps);
+    double a2 = .6 / pow2d(s2 + eps);
+    double a3 = .3 / pow2d(s3 + eps);
+    double w1 = a1 / (a1 + a2 + a3);
+    double w2 = a2 / (a1 + a2 + a3);
+    double w3 = a3 / (a1 + a2 + a3);
+    return w1 * ddx1 + w2 * ddx2 + w3 * ddx3;
+}
+
+static double ev(Ctx* c, int k, const int* i) {
+    const opflow_node* nd = &c->nodes[k];
+    switch (nd->kind) {
+        case OPFLOW_NODE_FIELD: return fget(&c->fields[nd->field], i);
+        case OPFLOW_NODE_CONST: return nd->value;
+        case OPFLOW_NODE_ADD: return ev(c, nd->a, i) + ev(c, nd->b, i);
+        case OPFLOW_NODE_SUB: return ev(c, nd->a, i) - ev(c, nd->b, i);
+        case OPFLOW_NODE_MUL: return ev(c, nd->a, i) * ev(c, nd->b, i);
+        case OPFLOW_NODE_DIV: return ev(c, nd->a, i) / ev(c, nd->b, i);
+        case OPFLOW_NODE_NEG: return -ev(c, nd->a, i);
+        case OPFLOW_NODE_D2: { /* D2SecondOrderCentered::eval (D2SecondOrderCentered.hpp:160-171) */
+            const int d = nd->dim, corner = c->loc[nd->a][d] == OPFLOW_CORNER;
+            int ip[3] = {i[0], i[1], i[2]}, im[3] = {i[0], i[1], i[2]};
+            ip[d]++; im[d]--;
+            double l = ev(c, nd->a, im), ce = ev(c, nd->a, i), r = ev(c, nd->a, ip);
+            const opflow_mesh_desc* m = c->m;
+            double dxl = corner ? mesh_dx(m, d, i[d] - 1) : (mesh_dx(m, d, i[d] - 1) + mesh_dx(m, d, i[d])) * 0.5;
+            double dxr = corner ? mesh_dx(m, d, i[d]) : (mesh_dx(m, d, i[d]) + mesh_dx(m, d, i[d] + 1)) * 0.5;
+            double dxc = (dxl + dxr) * 0.5;
+            return ((r - ce) / dxr - (ce - l) / dxl) / dxc;
+        }
+        case OPFLOW_NODE_D1: { /* D1FirstOrderCentered::eval (D1FirstOrderCentered.hpp:31-36) */
+            const int d = nd->dim;
+            int ip[3] = {i[0], i[1], i[2]}, im[3] = {i[0], i[1], i[2]};
+            ip[d]++; im[d]--;
+            if (c->loc[nd->a][d] == OPFLOW_CENTER)
+                return (ev(c, nd->a, i) - ev(c, nd->a, im)) / (mesh_dx(c->m, d, i[d] - 1) + mesh_dx(c->m, d, i[d])) * 2;
+            return (ev(c, nd->a, ip) - ev(c, nd->a, i)) / (mesh_dx(c->m, d, i[d]));
+        }
+        case OPFLOW_NODE_WENO53_DOWN: case OPFLOW_NODE_WENO53_UP: {
+            const int d = nd->dim, up = nd->kind == OPFLOW_NODE_WENO53_UP;
+            double v[6];
+            for (int o = 0; o < 6; ++o) {
+                int j[3] = {i[0], i[1], i[2]};
+                j[d] += up ? (3 - o) : (o - 3); /* Upwind passes (pp3..pm2) in the kernel's pm3..pp2 slots */
+                v[o] = ev(c, nd->a, j);
+            }
+            double h = mesh_dx(c->m, d, i[d]);
+            /* Upwind's differences are the negated Downwind differences of the mirrored stencil, and
+             * every operation of the kernel is odd in them, so the result is the exact negation. */
+            double r = weno_kernel(v[0], v[1], v[2], v[3], v[4], v[5], h);
+            return up ? -r : r;
+        }
+        case OPFLOW_NODE_INTP_C2C: { /* D1Linear<Cen2Cor>::eval (D1Linear.hpp:35-45) */
+            const int d = nd->dim;
+            int im[3] = {i[0], i[1], i[2]};
+            im[d]--;
+            double x1 = mesh_x(c->m, d, i[d] - 1) + 0.5 * mesh_dx(c->m, d, i[d] - 1);
+            double x2 = mesh_x(c->m, d, i[d]) + 0.5 * mesh_dx(c->m, d, i[d]);
+            double y1 = ev(c, nd->a, im), y2 = ev(c, nd->a, i);
+            return intp_d(x1, y1, x2, y2, mesh_x(c->m, d, i[d]));
+        }
+    }
+    return NAN;
+}
+
+static int setup_ctx(Ctx* c, const opflow_mesh_desc* m, const opflow_field_desc* descs, double** datas, int nf,
+                     const opflow_node* nodes, int n, Field* fields) {
+    memset(c, 0, sizeof *c);
+    c->m = m; c->nodes = nodes; c->n = n; c->fields = fields; c->nf = nf; c->unknown = -1;
+    if (n < 1) return fail(OPFLOW_E_INVALID, "empty expression");
+    for (int k = 0; k < nf; ++k) {
+        fields[k].d = &descs[k];
+        fields[k].data = datas[k];
+        int rc = or_field_info(m, &descs[k], &fields[k].r);
+        if (rc) return rc;
+    }
+    return compute_locs(c);
+}
+
+/* internal::FieldAssigner::assign<Op> (FieldAssigner.hpp:27-84) followed by the updatePadding of
+ * CartesianField::assignImpl_final (CartesianField.hpp:195-234).  `dst` is a slot of `datas`; when the
+ * expression reads it, the evaluation goes to a temporary copy first, as the reference does. */
+int or_assign(const opflow_mesh_desc* m, const opflow_field_desc* descs, double** datas, int nf, int dst, int arith,
+              const opflow_node* nodes, int n) {
+    Field fields[16];
+    Ctx c;
+    if (nf > 16 || dst < 0 || dst >= nf) return fail(OPFLOW_E_INVALID, "bad field slots");
+    int rc = setup_ctx(&c, m, descs, datas, nf, nodes, n, fields);
+    if (rc) return rc;
+    Field* out = &fields[dst];
+    int aliased = 0;
+    for (int k = 0; k < n; ++k) aliased |= nodes[k].kind == OPFLOW_NODE_FIELD && nodes[k].field == dst;
+    const opflow_field_info* R = &out->r;
+    int lo[3], hi[3], idx[3];
+    for (int d = 0; d < 3; ++d) {
+        lo[d] = imax(R->assignable[d][0], R->local[d][0]);
+        hi[d] = imin(R->assignable[d][1], R->local[d][1]);
+    }
+    double* tmp = NULL;
+    g_range_err = 0;
+    if (aliased) {
+        /* temp = dst; assign_impl<Eq>(src, temp); assign_impl<Op>(temp, dst) */
+        tmp = (double*) malloc(R->count * sizeof(double));
+        if (!tmp) return fail(OPFLOW_E_NOMEM, "host allocation failed");
+        memcpy(tmp, out->data, R->count * sizeof(double));
+        Field t = *out;
+        t.data = tmp;
+        BOX_FOR(R->ndim, lo, hi, idx) fset(&t, idx, ev(&c, n - 1, idx));
+        update_padding(m, &t);
+        BOX_FOR(R->ndim, lo, hi, idx) {
+            double v = fget(&t, idx), o = fget(out, idx);
+            switch (arith) {
+                case OPFLOW_ASSIGN_EQ: o = v; break;
+                case OPFLOW_ASSIGN_ADD: o += v; break;
+                case OPFLOW_ASSIGN_SUB: o -= v; break;
+                case OPFLOW_ASSIGN_MUL: o *= v; break;
+                case OPFLOW_ASSIGN_DIV: o /= v; break;
+            }
+            fset(out, idx, o);
+        }
+        free(tmp);
+    } else {
+        BOX_FOR(R->ndim, lo, hi, idx) {
+            double v = ev(&c, n - 1, idx), o = fget(out, idx);
+            switch (arith) {
+                case OPFLOW_ASSIGN_EQ: o = v; break;
+                case OPFLOW_ASSIGN_ADD: o += v; break;
+                case OPFLOW_ASSIGN_SUB: o -= v; break;
+                case OPFLOW_ASSIGN_MUL: o *= v; break;
+                case OPFLOW_ASSIGN_DIV: o /= v; break;
+            }
+            fset(out, idx, o);
+        }
+    }
+    update_padding(m, out); /* assign_impl's dst.updatePadding() */
+    update_padding(m, out); /* assignImpl_final's this->updatePadding() (idempotent) */
+    return g_range_err ? fail(OPFLOW_E_RANGE, "stencil read outside a field's data array") : OPFLOW_OK;
+}
+
+/* ------------------------------------------------------------------------------------------------ */
+/* StencilPad arithmetic (StencilPad.hpp:137-298) with fake_map insertion order (StencilPad.hpp:26-134) */
+/* ------------------------------------------------------------------------------------------------ */
+#define PADMAX 16
+typedef struct {
+    int n;
+    int key[PADMAX][3];
+    double val[PADMAX];
+    double bias;
+} Pad;
+typedef struct {
+    int is_pad;
+    double v;
+    Pad p;
+} Val;
+
+static int g_pad_err;
+static int pad_find(const Pad* p, const int* k) {
+    for (int e = 0; e < p->n; ++e)
+        if (p->key[e][0] == k[0] && p->key[e][1] == k[1] && p->key[e][2] == k[2]) return e;
+    return -1;
+}
+static double* pad_at(Pad* p, const int* k) { /* fake_map::operator[] (appends a missing key) */
+    int e = pad_find(p, k);
+    if (e >= 0) return &p->val[e];
+    if (p->n >= PADMAX) { g_pad_err = 1; return &p->val[0]; }
+    e = p->n++;
+    memcpy(p->key[e], k, sizeof(int) * 3);
+    p->val[e] = 0.;
+    return &p->val[e];
+}
+static void pad_scale(Pad* p, double r) { /* operator*(pad, num) */
+    for (int e = 0; e < p->n; ++e) p->val[e] *= r;
+    p->bias *= r;
+}
+static void pad_add_assign(Pad* a, const Pad* b) { /* operator+=(pad) */
+    for (int e = 0; e < b->n; ++e) {
+        int f = pad_find(a, b->key[e]);
+        if (f >= 0) a->val[f] += b->val[e];
+        else *pad_at(a, b->key[e]) = b->val[e];
+    }
+    a->bias += b->bias;
+}
+static Val vnum(double v) { Val r; r.is_pad = 0; r.v = v; r.p.n = 0; r.p.bias = 0.; return r; }
+static Val vpad_bias(double b) { Val r; r.is_pad = 1; r.v = 0.; r.p.n = 0; r.p.bias = b; return r; }
+
+static Val v_add(Val a, Val b) {
+    if (!a.is_pad && !b.is_pad) return vnum(a.v + b.v);
+    if (a.is_pad && b.is_pad) { Val r = a; pad_add_assign(&r.p, &b.p); return r; }
+    if (a.is_pad) { Val r = a; r.p.bias += b.v; return r; }       /* pad + num */
+    Val r = b; r.p.bias += a.v; return r;                           /* num + pad: ret = b; ret += a */
+}
+static Val v_neg_scale(Val b) { Val r = b; pad_scale(&r.p, -1.0); return r; }
+static Val v_sub(Val a, Val b) {
+    if (!a.is_pad && !b.is_pad) return vnum(a.v - b.v);
+    if (a.is_pad && b.is_pad) return v_add(a, v_neg_scale(b));      /* a + (b * -1.0) */
+    if (a.is_pad) { Val r = a; r.p.bias += -b.v; return r; }      /* a + (-b) */
+    return v_add(vpad_bias(a.v), v_neg_scale(b));                   /* StencilPad(a) - b */
+}
+static Val v_mul(Val a, Val b) {
+    if (!a.is_pad && !b.is_pad) return vnum(a.v * b.v);
+    if (a.is_pad && b.is_pad) { g_pad_err = 2; return a; }          /* nonlinear: not a linear equation */
+    if (a.is_pad) { Val r = a; pad_scale(&r.p, b.v); return r; }
+    Val r = b; pad_scale(&r.p, a.v); return r;
+}
+static Val v_div(Val a, Val b) {
+    if (!a.is_pad && !b.is_pad) return vnum(a.v / b.v);
+    if (b.is_pad) { g_pad_err = 2; return a; }
+    Val r = a; pad_scale(&r.p, 1. / b.v); return r;                 /* a * (1. / b) */
+}
+static Val v_neg(Val a) { /* unary operator-: v = -v, bias = -bias */
+    if (!a.is_pad) return vnum(-a.v);
+    Val r = a;
+    for (int e = 0; e < r.p.n; ++e) r.p.val[e] = -r.p.val[e];
+    r.p.bias = -r.p.bias;
+    return r;
+}
+static Val v_scal(Val a, double s) { /* double * pad or pad * double */
+    if (!a.is_pad) return vnum(a.v * s);
+    Val r = a; pad_scale(&r.p, s); return r;
+}
+
+/* StencilField::evalAtImpl_final (StencilField.hpp:123-350) */
+static Val st_eval(Ctx* c, const int* idx) {
+    const int D = c->m->ndim;
+    const Field* base = &c->fields[c->unknown];
+    int inA = 1, inL = 1;
+    for (int d = 0; d < D; ++d) {
+        inA &= c->st_assignable[d][0] <= idx[d] && idx[d] < c->st_assignable[d][1];
+        inL &= c->st_logical[d][0] <= idx[d] && idx[d] < c->st_logical[d][1];
+    }
+    if (inA) {
+        Val r = vpad_bias(0.);
+        int pinned = c->pin;
+        for (int d = 0; d < D; ++d) pinned &= idx[d] == c->pin_index[d];
+        if (!pinned) {
+            int k[3] = {idx[0], idx[1], idx[2]};
+            *pad_at(&r.p, k) = 1.0;
+        }
+        return r;
+    }
+    if (!inL) { g_pad_err = 3; return vpad_bias(NAN); }
+    const opflow_mesh_desc* m = c->m;
+    /* case 1: fold an index outside the accessible range back into it */
+    for (int i = 0; i < D; ++i) {
+        if (c->st_accessible[i][0] <= idx[i] && idx[i] < c->st_accessible[i][1]) continue;
+        const int lower = idx[i] < c->st_accessible[i][0];
+        const int bct = base->d->bc_type[i][lower ? 0 : 1];
+        const double bcv = base->d->bc_value[i][lower ? 0 : 1];
+        int mi[3] = {idx[0], idx[1], idx[2]};
+        const int as = c->st_accessible[i][0], ae = c->st_accessible[i][1];
+        if (base->d->loc[i] == OPFLOW_CORNER) {
+            mi[i] = lower ? 2 * as - idx[i] : 2 * ae - 2 - idx[i];
+            switch (bct) {
+                case OPFLOW_BC_DIRC: {
+                    /* intp(x1, y1=bc pad, x2, y2=mirror pad, x): (x1'*y2 - x2'*y1) / (x1' - x2') in pad arithmetic */
+                    double x1 = mesh_x(m, i, lower ? as : ae - 1) - mesh_x(m, i, idx[i]);
+                    double x2 = mesh_x(m, i, mi[i]) - mesh_x(m, i, idx[i]);
+                    Val y1 = vpad_bias(bcv), y2 = st_eval(c, mi);
+                    return v_div(v_sub(v_scal(y2, x1), v_scal(y1, x2)), vnum(x1 - x2));
+                }
+                case OPFLOW_BC_NEUM:
+                    return v_add(st_eval(c, mi), v_scal(vpad_bias(bcv), mesh_x(m, i, idx[i]) - mesh_x(m, i, mi[i])));
+                case OPFLOW_BC_SYMM: return st_eval(c, mi);
+                case OPFLOW_BC_ASYMM: return v_scal(st_eval(c, mi), -1.);
+                case OPFLOW_BC_PERIODIC:
+                    mi[i] = idx[i] + (lower ? (ae - as) : -(ae - as));
+                    return st_eval(c, mi);
+                default: g_pad_err = 4; return vpad_bias(NAN);
+            }
+        } else {
+            mi[i] = lower ? 2 * as - 1 - idx[i] : 2 * ae - 1 - idx[i];
+            switch (bct) {
+                case OPFLOW_BC_DIRC: {
+                    double xb = mesh_x(m, i, lower ? as : ae);
+                    double xm = mesh_x(m, i, mi[i]) + mesh_dx(m, i, mi[i]) / 2.;
+                    double xg = mesh_x(m, i, idx[i]) + mesh_dx(m, i, idx[i]) / 2.;
+                    double x1 = xb - xg, x2 = xm - xg;
+                    Val y1 = vpad_bias(bcv), y2 = st_eval(c, mi);
+                    return v_div(v_sub(v_scal(y2, x1), v_scal(y1, x2)), vnum(x1 - x2));
+                }
+                case OPFLOW_BC_NEUM:
+                    return v_add(st_eval(c, mi),
+                                 v_scal(vpad_bias(bcv), mesh_x(m, i, idx[i]) + mesh_dx(m, i, idx[i]) / 2. - mesh_x(m, i, mi[i])
+                                                                - mesh_dx(m, i, mi[i]) / 2.));
+                case OPFLOW_BC_SYMM: return st_eval(c, mi);
+                case OPFLOW_BC_ASYMM: return v_scal(st_eval(c, mi), -1.0);
+                case OPFLOW_BC_PERIODIC:
+                    mi[i] = idx[i] + (lower ? (ae - as) : -(ae - as));
+                    return st_eval(c, mi);
+                default: g_pad_err = 4; return vpad_bias(NAN);
+            }
+        }
+    }
+    /* case 2: the index sits on a Dirichlet boundary node */
+    for (int i = 0; i < D; ++i) {
+        if (base->d->loc[i] == OPFLOW_CORNER && base->d->bc_type[i][0] == OPFLOW_BC_DIRC && idx[i] == c->st_accessible[i][0])
+            return vpad_bias(base->d->bc_value[i][0]);
+        if (base->d->loc[i] == OPFLOW_CORNER && base->d->bc_type[i][1] == OPFLOW_BC_DIRC && idx[i] == c->st_accessible[i][1] - 1)
+            return vpad_bias(base->d->bc_value[i][1]);
+    }
+    g_pad_err = 5;
+    return vpad_bias(NAN);
+}
+
+static Val evp(Ctx* c, int k, const int* i) {
+    const opflow_node* nd = &c->nodes[k];
+    switch (nd->kind) {
+        case OPFLOW_NODE_FIELD:
+            if (nd->field == c->unknown) return st_eval(c, i);
+            return vnum(fget(&c->fields[nd->field], i));
+        case OPFLOW_NODE_CONST: return vnum(nd->value);
+        case OPFLOW_NODE_ADD: { Val a = evp(c, nd->a, i); return v_add(a, evp(c, nd->b, i)); }
+        case OPFLOW_NODE_SUB: { Val a = evp(c, nd->a, i); return v_sub(a, evp(c, nd->b, i)); }
+        case OPFLOW_NODE_MUL: { Val a = evp(c, nd->a, i); return v_mul(a, evp(c, nd->b, i)); }
+        case OPFLOW_NODE_DIV: { Val a = evp(c, nd->a, i); return v_div(a, evp(c, nd->b, i)); }
+        case OPFLOW_NODE_NEG: return v_neg(evp(c, nd->a, i));
+        case OPFLOW_NODE_D2: {
+            const int d = nd->dim, corner = c->loc[nd->a][d] == OPFLOW_CORNER;
+            int ip[3] = {i[0], i[1], i[2]}, im[3] = {i[0], i[1], i[2]};
+            ip[d]++; im[d]--;
+            Val l = evp(c, nd->a, im), ce = evp(c, nd->a, i), r = evp(c, nd->a, ip);
+            const opflow_mesh_desc* m = c->m;
+            double dxl = corner ? mesh_dx(m, d, i[d] - 1) : (mesh_dx(m, d, i[d] - 1) + mesh_dx(m, d, i[d])) * 0.5;
+            double dxr = corner ? mesh_dx(m, d, i[d]) : (mesh_dx(m, d, i[d]) + mesh_dx(m, d, i[d] + 1)) * 0.5;
+            double dxc = (dxl + dxr) * 0.5;
+            return v_div(v_sub(v_div(v_sub(r, ce), vnum(dxr)), v_div(v_sub(ce, l), vnum(dxl))), vnum(dxc));
+        }
+        case OPFLOW_NODE_D1: {
+            const int d = nd->dim;
+            int ip[3] = {i[0], i[1], i[2]}, im[3] = {i[0], i[1], i[2]};
+            ip[d]++; im[d]--;
+            if (c->loc[nd->a][d] == OPFLOW_CENTER) {
+                Val a = evp(c, nd->a, i), b = evp(c, nd->a, im);
+                return v_mul(v_div(v_sub(a, b), vnum(mesh_dx(c->m, d, i[d] - 1) + mesh_dx(c->m, d, i[d]))), vnum(2));
+            }
+            Val a = evp(c, nd->a, ip), b = evp(c, nd->a, i);
+            return v_div(v_sub(a, b), vnum(mesh_dx(c->m, d, i[d])));
+        }
+        case OPFLOW_NODE_INTP_C2C: {
+            const int d = nd->dim;
+            int im[3] = {i[0], i[1], i[2]};
+            im[d]--;
+            double x1 = mesh_x(c->m, d, i[d] - 1) + 0.5 * mesh_dx(c->m, d, i[d] - 1);
+            double x2 = mesh_x(c->m, d, i[d]) + 0.5 * mesh_dx(c->m, d, i[d]);
+            double x = mesh_x(c->m, d, i[d]);
+            Val y1 = evp(c, nd->a, im), y2 = evp(c, nd->a, i);
+            double a = x1 - x, b = x2 - x;
+            return v_div(v_sub(v_scal(y2, a), v_scal(y1, b)), vnum(a - b));
+        }
+        default:
+            /* WENO and the other nonlinear operators have no StencilPad form */
+            g_pad_err = 2;
+            return vnum(NAN);
+    }
+}
+
+/* HYPREEqnSolveHandler::initStencil + generateAb (HYPREEqnSolveHandler.hpp:79-166) with the
+ * HYPRE_Struct*SetValues calls replaced by writes into coef[cell][entry] / rhs[cell]. */
+int or_assemble(const opflow_mesh_desc* m, const opflow_field_desc* descs, double** datas, int nf, int target,
+                const opflow_node* nodes, int n, int pin, int* n_entries, int* offsets, double* coef, double* rhs,
+                size_t* n_cells) {
+    Field fields[16];
+    Ctx c;
+    if (nf > 16 || target < 0 || target >= nf) return fail(OPFLOW_E_INVALID, "bad field slots");
+    int rc = setup_ctx(&c, m, descs, datas, nf, nodes, n, fields);
+    if (rc) return rc;
+    c.unknown = target;
+    c.pin = pin;
+    const Field* T = &fields[target];
+    const int D = m->ndim;
+    for (int d = 0; d < 3; ++d) {
+        for (int s = 0; s < 2; ++s) {
+            c.st_assignable[d][s] = T->r.assignable[d][s];
+            c.st_accessible[d][s] = T->r.accessible[d][s];
+            c.st_logical[d][s] = T->r.logical[d][s];
+        }
+        c.pin_index[d] = T->r.assignable[d][0];
+        /* ignorePeriodicBC (StencilField.hpp:112-121) */
+        if (d < D && T->d->bc_type[d][0] == OPFLOW_BC_PERIODIC)
+            for (int s = 0; s < 2; ++s) c.st_assignable[d][s] = c.st_accessible[d][s] = T->r.logical[d][s];
+    }
+    int lo[3], hi[3], mid[3] = {0, 0, 0}, idx[3];
+    size_t cells = 1;
+    for (int d = 0; d < 3; ++d) {
+        lo[d] = imax(T->r.assignable[d][0], T->r.local[d][0]);
+        hi[d] = imin(T->r.assignable[d][1], T->r.local[d][1]);
+        if (d < D) mid[d] = (T->r.assignable[d][0] + T->r.assignable[d][1]) / 2;
+        cells *= (size_t) (hi[d] - lo[d]);
+    }
+    g_pad_err = 0;
+    g_range_err = 0;
+    /* commStencil: the middle cell's pad, offset to the middle (lines 97-107) */
+    Val vm = evp(&c, n - 1, mid);
+    if (!vm.is_pad) return fail(OPFLOW_E_INVALID, "the equation does not contain the unknown");
+    Pad comm = vm.p;
+    for (int e = 0; e < comm.n; ++e)
+        for (int d = 0; d < 3; ++d) comm.key[e][d] -= mid[d];
+    *n_entries = comm.n;
+    *n_cells = cells;
+    if (g_pad_err) return fail(OPFLOW_E_UNSUPPORTED, "equation is not linear in the unknown or leaves the logical range");
+    if (!coef) return OPFLOW_OK;
+    if (offsets)
+        for (int e = 0; e < comm.n; ++e)
+            for (int d = 0; d < D; ++d) offsets[e * D + d] = comm.key[e][d];
+    size_t cell = 0;
+    BOX_FOR(D, lo, hi, idx) {
+        Val v = evp(&c, n - 1, idx);
+        Pad cur = v.p;
+        for (int e = 0; e < cur.n; ++e)
+            for (int d = 0; d < 3; ++d) cur.key[e][d] -= idx[d];
+        for (int e = 0; e < comm.n; ++e) {
+            int f = pad_find(&cur, comm.key[e]);
+            double x = f >= 0 ? cur.val[f] : 0.;
+            coef[cell * comm.n + e] = x == 0. ? 0. : x; /* +0 for -0 */
+        }
+        rhs[cell] = -cur.bias;
+        ++cell;
+    }
+    if (pin) {
+        /* the first unknown's row: identity, rhs 0 (lines 145-163) */
+        for (int e = 0; e < comm.n; ++e) {
+            int centre = comm.key[e][0] == 0 && comm.key[e][1] == 0 && comm.key[e][2] == 0;
+            coef[e] = centre ? 1.0 : 0.0;
+        }
+        rhs[0] = 0.;
+    }
+    if (g_pad_err || g_range_err) return fail(OPFLOW_E_UNSUPPORTED, "assembly failed (nonlinear term or out-of-range read)");
+    return OPFLOW_OK;
+}
+
+/* ------------------------------------------------------------------------------------------------ */
+/* FP64 reference solve of an assembled structured system (the checker for the GPU solvers):        */
+/* conjugate gradients with a Jacobi preconditioner, periodic offsets wrapped like HYPRE's periodic  */
+/* grid.  coef is [cell][entry] over the box `dims`, x fastest.                                      */
+/* ------------------------------------------------------------------------------------------------ */
+static void or_matvec(int D, const int* dims, const int* periodic, int ne, const int* off, const double* coef,
+                      const double* x, double* y) {
+    size_t n = (size_t) dims[0] * dims[1] * dims[2];
+    for (size_t c = 0; c < n; ++c) {
+        int i[3] = {(int) (c % dims[0]), (int) ((c / dims[0]) % dims[1]), (int) (c / ((size_t) dims[0] * dims[1]))};
+        double s = 0.;
+        for (int e = 0; e < ne; ++e) {
+            int j[3] = {i[0], i[1], i[2]}, ok = 1;
+            for (int d = 0; d < D; ++d) {
+                j[d] += off[e * D + d];
+                if (j[d] < 0 || j[d] >= dims[d]) {
+                    if (periodic[d]) j[d] = (j[d] % dims[d] + dims[d]) % dims[d];
+                    else ok = 0;
+                }
+            }
+            if (!ok) continue;
+            s += coef[c * ne + e] * x[((size_t) j[2] * dims[1] + j[1]) * dims[0] + j[0]];
+        }
+        y[c] = s;
+    }
+}
+
+double or_residual(int D, const int* dims, const int* periodic, int ne, const int* off, const double* coef,
+                   const double* rhs, const double* x, double* bnorm_out) {
+    size_t n = (size_t) dims[0] * dims[1] * dims[2];
+    double* y = (double*) malloc(n * sizeof(double));
+    or_matvec(D, dims, periodic, ne, off, coef, x, y);
+    double rr = 0., bb = 0.;
+    for (size_t c = 0; c < n; ++c) {
+        double r = rhs[c] - y[c];
+        rr += r * r;
+        bb += rhs[c] * rhs[c];
+    }
+    free(y);
+    if (bnorm_out) *bnorm_out = sqrt(bb);
+    return sqrt(rr);
+}
+
+int or_pcg(int D, const int* dims_in, const int* periodic, int ne, const int* off, const double* coef, const double* rhs,
+           double* x, double tol, int maxit, int* iters, double* relres) {
+    int dims[3] = {dims_in[0], D > 1 ? dims_in[1] : 1, D > 2 ? dims_in[2] : 1};
+    size_t n = (size_t) dims[0] * dims[1] * dims[2];
+    int ci = -1;
+    for (int e = 0; e < ne; ++e) {
+        int z = 1;
+        for (int d = 0; d < D; ++d) z &= off[e * D + d] == 0;
+        if (z) ci = e;
+    }
+    if (ci < 0) return fail(OPFLOW_E_INVALID, "stencil has no centre entry");
+    double *r = malloc(n * 8), *z = malloc(n * 8), *p = malloc(n * 8), *q = malloc(n * 8);
+    or_matvec(D, dims, periodic, ne, off, coef, x, q);
+    double bb = 0., rz = 0.;
+    for (size_t c = 0; c < n; ++c) {
+        r[c] = rhs[c] - q[c];
+        bb += rhs[c] * rhs[c];
+    }
+    double bn = sqrt(bb) > 0 ? sqrt(bb) : 1.;
+    for (size_t c = 0; c < n; ++c) { z[c] = r[c] / coef[c * ne + ci]; p[c] = z[c]; rz += r[c] * z[c]; }
+    int it = 0;
+    double rn = 0.;
+    for (; it < maxit; ++it) {
+        rn = 0.;
+        for (size_t c = 0; c < n; ++c) rn += r[c] * r[c];
+        if (sqrt(rn) / bn <= tol) break;
+        or_matvec(D, dims, periodic, ne, off, coef, p, q);
+        double pq = 0.;
+        for (size_t c = 0; c < n; ++c) pq += p[c] * q[c];
+        double al = rz / pq;
+        for (size_t c = 0; c < n; ++c) { x[c] += al * p[c]; r[c] -= al * q[c]; }
+        double rz2 = 0.;
+        for (size_t c = 0; c < n; ++c) { z[c] = r[c] / coef[c * ne + ci]; rz2 += r[c] * z[c]; }
+        double be = rz2 / rz;
+        rz = rz2;
+        for (size_t c = 0; c < n; ++c) p[c] = z[c] + be * p[c];
+    }
+    *iters = it;
+    *relres = or_residual(D, dims, periodic, ne, off, coef, rhs, x, NULL) / bn;
+    free(r); free(z); free(p); free(q);
+    return OPFLOW_OK;
+}

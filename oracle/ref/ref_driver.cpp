@@ -1,0 +1,391 @@
+// Runs OpFlow's own CPU implementation of the explicit-evaluation and stencil-assembly paths on small
+// cases and writes raw dumps, so that the restated oracle (oracle/oracle.c) and the CUDA library can be
+// checked against the reference's actual output.  Test infrastructure only: it is compiled by
+// oracle/build_ref.sh into oracle/_ref/ and used to (re)generate tests/golden/ fixtures.
+//
+// Output format (little-endian, one file per run): a sequence of records, each a text line
+// "FIELD <json>\n" or "STENCIL <json>\n" followed by the raw float64 payload the json describes.
+#include "OpFlowCoreNoSolvers.hpp"
+#include "DataStructures/StencilPad.hpp"
+#include "Math/Function/Numeric.hpp"
+
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+using namespace OpFlow;
+
+// ---- seeded inputs shared with the oracle and the tests (counter-based splitmix64) ----
+static inline uint64_t mix64(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+static inline double u01(uint64_t seed, uint64_t k) {
+    return (double) (mix64(seed + (k + 1) * 0x9E3779B97F4A7C15ull) >> 11) * 0x1.0p-53;
+}
+
+static FILE* g_out = nullptr;
+static void put(const std::vector<double>& v) { fwrite(v.data(), sizeof(double), v.size(), g_out); }
+
+// Dump the readable range of a field (padded local range clipped to the logical range), x fastest,
+// together with the field's ranges.
+template <typename F>
+static void dump_field(const F& u, const char* name) {
+    constexpr int dim = internal::CartesianFieldExprTrait<F>::dim;
+    auto rr = u.getLocalReadableRange();
+    std::string js = std::format("{{\"name\":\"{}\",\"dim\":{},\"padding\":{}", name, dim, u.padding);
+    auto rng = [&](const char* nm, const auto& r) {
+        js += std::format(",\"{}\":[", nm);
+        for (int d = 0; d < dim; ++d) js += std::format("{}[{},{}]", d ? "," : "", r.start[d], r.end[d]);
+        js += "]";
+    };
+    rng("readable", rr);
+    rng("logical", u.logicalRange);
+    rng("accessible", u.accessibleRange);
+    rng("assignable", u.assignableRange);
+    rng("local", u.localRange);
+    js += std::format(",\"count\":{}}}", rr.count());
+    fprintf(g_out, "FIELD %s\n", js.c_str());
+    std::vector<double> v;
+    v.reserve(rr.count());
+    rangeFor_s(rr, [&](auto&& i) { v.push_back(u.evalAt(i)); });
+    put(v);
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Explicit path
+// ---------------------------------------------------------------------------------------------------
+static int run_ftcs2d(int n, int steps, uint64_t seed, double bcv, double cfl) {
+    using Mesh = CartesianMesh<Meta::int_<2>>;
+    using Field = CartesianField<Real, Mesh>;
+    auto mesh = MeshBuilder<Mesh>().newMesh(n, n).setMeshOfDim(0, 0., 1.).setMeshOfDim(1, 0., 1.).build();
+    auto u = ExprBuilder<Field>()
+                     .setName("u")
+                     .setMesh(mesh)
+                     .setBC(0, DimPos::start, BCType::Dirc, bcv)
+                     .setBC(0, DimPos::end, BCType::Dirc, bcv)
+                     .setBC(1, DimPos::start, BCType::Dirc, bcv)
+                     .setBC(1, DimPos::end, BCType::Dirc, bcv)
+                     .build();
+    rangeFor_s(u.assignableRange, [&](auto&& i) { u[i] = u01(seed, (uint64_t) i[1] * n + i[0]); });
+    u.updatePadding();
+    const Real h = 1.0 / (n - 1);
+    const Real dt = cfl * h * h, alpha = 1.0;
+    for (int s = 0; s < steps; ++s)
+        u = u + dt * alpha * (d2x<D2SecondOrderCentered>(u) + d2y<D2SecondOrderCentered>(u));
+    dump_field(u, "u");
+    return 0;
+}
+
+static int run_ftcs3d(int n, int steps, uint64_t seed, double cfl) {
+    using Mesh = CartesianMesh<Meta::int_<3>>;
+    using Field = CartesianField<Real, Mesh>;
+    auto mesh = MeshBuilder<Mesh>()
+                        .newMesh(n, n, n)
+                        .setMeshOfDim(0, 0., 1.)
+                        .setMeshOfDim(1, 0., 1.)
+                        .setMeshOfDim(2, 0., 1.)
+                        .build();
+    auto b = ExprBuilder<Field>().setName("u").setMesh(mesh);
+    for (int d = 0; d < 3; ++d) {
+        b.setBC(d, DimPos::start, BCType::Dirc, 0.);
+        b.setBC(d, DimPos::end, BCType::Dirc, 0.);
+    }
+    auto u = b.build();
+    // 8 Gaussians: centre in [0.2,0.8]^3, width in [0.03,0.1], amplitude in [0.5,1]
+    double c[8][3], w[8], a[8];
+    for (int g = 0; g < 8; ++g) {
+        for (int d = 0; d < 3; ++d) c[g][d] = 0.2 + 0.6 * u01(seed, 5 * g + d);
+        w[g] = 0.03 + 0.07 * u01(seed, 5 * g + 3);
+        a[g] = 0.5 + 0.5 * u01(seed, 5 * g + 4);
+    }
+    u.initBy([&](auto&& x) {
+        double s = 0.;
+        for (int g = 0; g < 8; ++g) {
+            double r2 = (x[0] - c[g][0]) * (x[0] - c[g][0]) + (x[1] - c[g][1]) * (x[1] - c[g][1])
+                        + (x[2] - c[g][2]) * (x[2] - c[g][2]);
+            s += a[g] * std::exp(-r2 / (w[g] * w[g]));
+        }
+        return s;
+    });
+    dump_field(u, "u0");
+    const Real h = 1.0 / (n - 1);
+    const Real dt = cfl * h * h, alpha = 1.0;
+    for (int s = 0; s < steps; ++s)
+        u = u
+            + dt * alpha
+                      * (d2x<D2SecondOrderCentered>(u) + d2y<D2SecondOrderCentered>(u)
+                         + d2z<D2SecondOrderCentered>(u));
+    dump_field(u, "u");
+    return 0;
+}
+
+// Periodic WENO5-JS + Shu-Osher RK3 on a 2D cell-centred field, derivative along dim 0 only.
+static int run_weno(int nx, int ny, int steps, uint64_t seed, int upwind_kernel) {
+    using Mesh = CartesianMesh<Meta::int_<2>>;
+    using Field = CartesianField<Real, Mesh>;
+    const double Lx = 1.0, Ly = 1.0;
+    auto mesh = MeshBuilder<Mesh>().newMesh(nx + 1, ny + 1).setMeshOfDim(0, 0., Lx).setMeshOfDim(1, 0., Ly).build();
+    auto u = ExprBuilder<Field>()
+                     .setName("u")
+                     .setMesh(mesh)
+                     .setLoc(LocOnMesh::Center)
+                     .setBC(0, DimPos::start, BCType::Periodic)
+                     .setBC(0, DimPos::end, BCType::Periodic)
+                     .setBC(1, DimPos::start, BCType::Periodic)
+                     .setBC(1, DimPos::end, BCType::Periodic)
+                     .setExt(3)
+                     .build();
+    // per line: a square pulse [x0, x0+wd) of height A plus a sine of amplitude B and wave number m
+    rangeFor_s(u.assignableRange, [&](auto&& i) {
+        uint64_t line = (uint64_t) i[1];
+        double x0 = 0.6 * u01(seed, 4 * line), wd = 0.1 + 0.2 * u01(seed, 4 * line + 1);
+        double A = 0.5 + u01(seed, 4 * line + 2);
+        double B = 0.5 * u01(seed, 4 * line + 3);
+        int m = 1 + (int) (line % 4);
+        double x = (i[0] + 0.5) / nx;
+        u[i] = (x >= x0 && x < x0 + wd ? A : 0.0) + B * std::sin(2.0 * 3.141592653589793 * m * x);
+    });
+    u.updatePadding();
+    dump_field(u, "u0");
+    auto u1 = u, u2 = u;
+    const Real h = Lx / nx, dt = 0.5 * h;
+    for (int s = 0; s < steps; ++s) {
+        if (upwind_kernel) {
+            u1 = u - dt * d1<D1WENO53Upwind<0>>(u);
+            u2 = 0.75 * u + 0.25 * (u1 - dt * d1<D1WENO53Upwind<0>>(u1));
+            u = 1.0 / 3.0 * u + 2.0 / 3.0 * (u2 - dt * d1<D1WENO53Upwind<0>>(u2));
+        } else {
+            u1 = u - dt * d1<D1WENO53Downwind<0>>(u);
+            u2 = 0.75 * u + 0.25 * (u1 - dt * d1<D1WENO53Downwind<0>>(u1));
+            u = 1.0 / 3.0 * u + 2.0 / 3.0 * (u2 - dt * d1<D1WENO53Downwind<0>>(u2));
+        }
+    }
+    dump_field(u, "u");
+    return 0;
+}
+
+// Field construction + padding rules: one field per (loc, bc) combination, initialised by a smooth
+// function of the coordinates, dumped over its readable range.
+static int run_padding(int nx, int ny, int loc_i, int bc_lo, int bc_hi, int ext) {
+    using Mesh = CartesianMesh<Meta::int_<2>>;
+    using Field = CartesianField<Real, Mesh>;
+    auto mesh = MeshBuilder<Mesh>().newMesh(nx, ny).setMeshOfDim(0, 0., 1.).setMeshOfDim(1, 0., 2.).build();
+    auto b = ExprBuilder<Field>().setName("f").setMesh(mesh).setLoc(loc_i ? LocOnMesh::Center : LocOnMesh::Corner);
+    auto setbc = [&](int d, DimPos pos, int t, double v) {
+        switch (t) {
+            case 0: b.setBC(d, pos, BCType::Dirc, v); break;
+            case 1: b.setBC(d, pos, BCType::Neum, v); break;
+            case 2: b.setBC(d, pos, BCType::Periodic); break;
+            case 3: b.setBC(d, pos, BCType::Symm); break;
+            case 4: b.setBC(d, pos, BCType::ASymm); break;
+        }
+    };
+    // dim 0 uses (bc_lo, bc_hi); dim 1 uses the same types swapped, with different constants
+    setbc(0, DimPos::start, bc_lo, 0.25);
+    setbc(0, DimPos::end, bc_hi, -0.5);
+    setbc(1, DimPos::start, bc_hi, 0.75);
+    setbc(1, DimPos::end, bc_lo, 1.5);
+    b.setExt(ext);
+    auto f = b.build();
+    f.initBy([](auto&& x) { return 1.0 + x[0] * x[0] - 0.5 * x[1] + 0.25 * x[0] * x[1]; });
+    dump_field(f, "f");
+    return 0;
+}
+
+// ---------------------------------------------------------------------------------------------------
+// Implicit path: the assembly HYPREEqnSolveHandler::generateAb performs, without HYPRE.
+// ---------------------------------------------------------------------------------------------------
+template <typename Field, typename Getter>
+static void assemble_dump(Field& target, Getter&& getter, bool pin) {
+    constexpr int dim = internal::CartesianFieldExprTrait<Field>::dim;
+    auto st = target.getStencilField();
+    st.pin(pin);
+    auto stf = std::make_unique<StencilField<Field>>(std::move(st));
+    stf->ignorePeriodicBC();
+    auto eqn = getter(*stf);
+    auto t = eqn.lhs - eqn.rhs;
+    t.prepare();
+    DS::MDIndex<dim> middle;
+    for (int i = 0; i < dim; ++i) middle[i] = (target.assignableRange.start[i] + target.assignableRange.end[i]) / 2;
+    auto comm = getOffsetStencil(t.evalAt(middle), middle);
+    auto rr = DS::commonRange(target.assignableRange, target.localRange);
+    std::string js = std::format("{{\"dim\":{},\"nent\":{},\"range\":[", dim, comm.pad.size());
+    for (int d = 0; d < dim; ++d) js += std::format("{}[{},{}]", d ? "," : "", rr.start[d], rr.end[d]);
+    js += "],\"offsets\":[";
+    int e = 0;
+    for (const auto& [k, v] : comm.pad) {
+        js += e++ ? ",[" : "[";
+        for (int d = 0; d < dim; ++d) js += std::format("{}{}", d ? "," : "", k[d]);
+        js += "]";
+    }
+    js += std::format("],\"count\":{}}}", rr.count());
+    fprintf(g_out, "STENCIL %s\n", js.c_str());
+    std::vector<double> vals, rhs;
+    rangeFor_s(rr, [&](auto&& k) {
+        auto cur = getOffsetStencil(t.evalAt(k), k);
+        auto ext = commonStencil(cur, comm);
+        for (const auto& [key, val] : comm.pad) vals.push_back(ext.pad[key]);
+        rhs.push_back(-ext.bias);
+    });
+    if (pin) {
+        // the first unknown's row becomes the identity and its rhs 0
+        int e2 = 0;
+        for (const auto& [key, val] : comm.pad) {
+            bool centre = true;
+            for (int d = 0; d < dim; ++d) centre &= key[d] == 0;
+            vals[e2++] = centre ? 1.0 : 0.0;
+        }
+        rhs[0] = 0.0;
+    }
+    put(vals);
+    put(rhs);
+}
+
+static int run_assemble(const std::string& which, int n) {
+    using Mesh2 = CartesianMesh<Meta::int_<2>>;
+    using Field2 = CartesianField<Real, Mesh2>;
+    using Mesh3 = CartesianMesh<Meta::int_<3>>;
+    using Field3 = CartesianField<Real, Mesh3>;
+    if (which == "csr_dirc" || which == "csr_neum" || which == "csr_periodic") {
+        // the CSRMatrixGeneratorTest cases: 4x4 cells, h = 1, 1.0 == d2x(e) + d2y(e)
+        auto m = MeshBuilder<Mesh2>().newMesh(5, 5).setMeshOfDim(0, 0., 4.).setMeshOfDim(1, 0., 4.).build();
+        auto b = ExprBuilder<Field2>().setMesh(m).setName("p").setLoc(LocOnMesh::Center).setExt(1);
+        for (int d = 0; d < 2; ++d)
+            for (auto pos : {DimPos::start, DimPos::end}) {
+                if (which == "csr_dirc") b.setBC(d, pos, BCType::Dirc, 0.);
+                else if (which == "csr_neum") b.setBC(d, pos, BCType::Neum, 0.);
+                else b.setBC(d, pos, BCType::Periodic);
+            }
+        auto p = b.build();
+        assemble_dump(p, [](auto&& e) { return 1.0 == d2x<D2SecondOrderCentered>(e) + d2y<D2SecondOrderCentered>(e); },
+                      which == "csr_neum");
+        return 0;
+    }
+    if (which == "neum2d" || which == "dirc2d" || which == "periodic2d") {
+        // -Lap(p) = f in the SPD form f == d2x(e) + d2y(e): A = -L, b = -f
+        auto m = MeshBuilder<Mesh2>().newMesh(n + 1, n + 1).setMeshOfDim(0, 0., 1.).setMeshOfDim(1, 0., 1.).build();
+        auto b = ExprBuilder<Field2>().setMesh(m).setName("p").setLoc(LocOnMesh::Center).setExt(1);
+        for (int d = 0; d < 2; ++d)
+            for (auto pos : {DimPos::start, DimPos::end}) {
+                if (which == "dirc2d") b.setBC(d, pos, BCType::Dirc, 0.);
+                else if (which == "neum2d") b.setBC(d, pos, BCType::Neum, 0.);
+                else b.setBC(d, pos, BCType::Periodic);
+            }
+        auto p = b.build();
+        auto f = p;
+        rangeFor_s(f.assignableRange, [&](auto&& i) { f[i] = u01(7, (uint64_t) i[1] * n + i[0]) - 0.5; });
+        f.updatePadding();
+        assemble_dump(p, [&](auto&& e) { return f == d2x<D2SecondOrderCentered>(e) + d2y<D2SecondOrderCentered>(e); },
+                      which != "dirc2d");
+        return 0;
+    }
+    if (which == "var2d") {
+        // the DircEqnTest operator: dx(dx(e)/intp(r)) + dy(dy(e)/intp(r)), r with a 1000:1 jump
+        auto m = MeshBuilder<Mesh2>().newMesh(n + 1, n + 1).setMeshOfDim(0, 0., 1.).setMeshOfDim(1, 0., 1.).build();
+        auto mk = [&](double bcv) {
+            return ExprBuilder<Field2>()
+                    .setMesh(m)
+                    .setName("p")
+                    .setBC(0, DimPos::start, BCType::Dirc, bcv)
+                    .setBC(0, DimPos::end, BCType::Dirc, bcv)
+                    .setBC(1, DimPos::start, BCType::Dirc, bcv)
+                    .setBC(1, DimPos::end, BCType::Dirc, bcv)
+                    .setExt(1)
+                    .setLoc({LocOnMesh::Center, LocOnMesh::Center})
+                    .build();
+        };
+        auto p = mk(0.);
+        auto r = mk(1.);
+        auto bb = mk(0.);
+        r.initBy([&](auto&& x) {
+            auto dist = Math::norm2(x[0] - 0.5, x[1] - 0.5);
+            auto hevi = Math::smoothHeviside(r.getMesh().dx(0, 0) * 8, dist - 0.2);
+            return 1. * hevi + (1. - hevi) * 1000;
+        });
+        rangeFor_s(bb.assignableRange, [&](auto&& i) { bb[i] = u01(11, (uint64_t) i[1] * n + i[0]) - 0.5; });
+        bb.updatePadding();
+        dump_field(r, "r");
+        dump_field(bb, "b");
+        assemble_dump(p,
+                      [&](auto&& e) {
+                          return bb
+                                 == dx<D1FirstOrderCentered>(dx<D1FirstOrderCentered>(e) / d1IntpCenterToCorner<0>((r)))
+                                            + dy<D1FirstOrderCentered>(dy<D1FirstOrderCentered>(e)
+                                                                       / d1IntpCenterToCorner<1>(r));
+                      },
+                      false);
+        return 0;
+    }
+    if (which == "helm_corner") {
+        // (I - k Lap) u = f on a node grid with Dirichlet nodes: e - k*(d2x(e)+d2y(e)) == f
+        auto m = MeshBuilder<Mesh2>().newMesh(n, n).setMeshOfDim(0, 0., 1.).setMeshOfDim(1, 0., 1.).build();
+        auto b = ExprBuilder<Field2>().setMesh(m).setName("u").setLoc(LocOnMesh::Corner);
+        for (int d = 0; d < 2; ++d)
+            for (auto pos : {DimPos::start, DimPos::end}) b.setBC(d, pos, BCType::Dirc, 0.125);
+        auto u = b.build();
+        auto f = u;
+        rangeFor_s(f.assignableRange, [&](auto&& i) { f[i] = u01(13, (uint64_t) i[1] * n + i[0]); });
+        const double k = 0.0123;
+        assemble_dump(u, [&](auto&& e) { return e - k * (d2x<D2SecondOrderCentered>(e) + d2y<D2SecondOrderCentered>(e)) == f; },
+                      false);
+        return 0;
+    }
+    if (which == "var3d") {
+        // flux form with face coefficient intp(K): f == sum_d dd(intp_d(K) * dd(e)), Neumann, pinned
+        auto m = MeshBuilder<Mesh3>()
+                         .newMesh(n + 1, n + 1, n + 1)
+                         .setMeshOfDim(0, 0., 1.)
+                         .setMeshOfDim(1, 0., 1.)
+                         .setMeshOfDim(2, 0., 1.)
+                         .build();
+        auto b = ExprBuilder<Field3>().setMesh(m).setName("p").setLoc(LocOnMesh::Center).setExt(1);
+        for (int d = 0; d < 3; ++d)
+            for (auto pos : {DimPos::start, DimPos::end}) b.setBC(d, pos, BCType::Neum, 0.);
+        auto p = b.build();
+        auto K = p, f = p;
+        K.initBy([](auto&& x) { return std::exp(std::sin(6.0 * x[0]) * std::cos(4.0 * x[1]) + 0.5 * x[2]); });
+        rangeFor_s(f.assignableRange, [&](auto&& i) { f[i] = u01(17, ((uint64_t) i[2] * n + i[1]) * n + i[0]) - 0.5; });
+        f.updatePadding();
+        dump_field(K, "K");
+        dump_field(f, "f");
+        assemble_dump(p,
+                      [&](auto&& e) {
+                          return f
+                                 == dx<D1FirstOrderCentered>(d1IntpCenterToCorner<0>(K) * dx<D1FirstOrderCentered>(e))
+                                            + dy<D1FirstOrderCentered>(d1IntpCenterToCorner<1>(K)
+                                                                       * dy<D1FirstOrderCentered>(e))
+                                            + dz<D1FirstOrderCentered>(d1IntpCenterToCorner<2>(K)
+                                                                       * dz<D1FirstOrderCentered>(e));
+                      },
+                      true);
+        return 0;
+    }
+    fprintf(stderr, "unknown assemble case %s\n", which.c_str());
+    return 2;
+}
+
+int main(int argc, char** argv) {
+    if (argc < 3) {
+        fprintf(stderr, "usage: ref_driver <out.bin> <cmd> args...\n");
+        return 2;
+    }
+    g_out = fopen(argv[1], "wb");
+    if (!g_out) return 3;
+    std::string cmd = argv[2];
+    auto I = [&](int k) { return std::atoi(argv[k]); };
+    auto D = [&](int k) { return std::atof(argv[k]); };
+    int rc = 2;
+    if (cmd == "ftcs2d") rc = run_ftcs2d(I(3), I(4), std::strtoull(argv[5], nullptr, 10), D(6), D(7));
+    else if (cmd == "ftcs3d") rc = run_ftcs3d(I(3), I(4), std::strtoull(argv[5], nullptr, 10), D(6));
+    else if (cmd == "weno") rc = run_weno(I(3), I(4), I(5), std::strtoull(argv[6], nullptr, 10), I(7));
+    else if (cmd == "padding") rc = run_padding(I(3), I(4), I(5), I(6), I(7), I(8));
+    else if (cmd == "assemble") rc = run_assemble(argv[3], argc > 4 ? I(4) : 0);
+    fclose(g_out);
+    return rc;
+}

@@ -1,0 +1,91 @@
+"""Shared helpers for the tests: meshes, field descriptions, expressions and golden fixtures."""
+import ctypes as C
+import json
+import os
+
+import numpy as np
+
+import oracle_lib as orc
+from opflow_gb300 import _capi as capi
+from opflow_gb300 import api
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def golden(name):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    meta = json.loads(str(z["meta"]))
+    return meta, {k: z[k] for k in z.files if k != "meta"}
+
+
+def record(meta, key):
+    for r in meta["records"]:
+        if r["key"] == key:
+            return r["meta"]
+    raise KeyError(key)
+
+
+def mesh_uniform(dims, ranges=None, pad=5):
+    """CartesianMesh built by the oracle's restatement of MeshBuilder::set1DMesh (no GPU, no library)."""
+    xs, dxs = [], []
+    for k, n in enumerate(dims):
+        lo, hi = (ranges[k] if ranges else (0.0, 1.0))
+        x = np.zeros(n + 2 * pad)
+        dx = np.zeros(n + 2 * pad - 1)
+        orc.lib().or_mesh_uniform(n, 0, pad, lo, hi, orc.dptr(x), orc.dptr(dx))
+        xs.append(x)
+        dxs.append(dx)
+    return api.CartesianMesh(len(dims), dims, [0] * len(dims), pad, xs, dxs)
+
+
+def field_desc(ndim, loc, bcs, values=None, ext=0, padding=0):
+    """bcs: list per dim of (lo, hi) BC types; values likewise (default 0)."""
+    fd = capi.FieldDesc()
+    fd.ndim = ndim
+    for d in range(ndim):
+        fd.loc[d] = loc[d] if isinstance(loc, (list, tuple)) else loc
+        for s in range(2):
+            fd.bc_type[d][s] = bcs[d][s]
+            fd.bc_value[d][s] = values[d][s] if values else 0.0
+            e = ext[d][s] if isinstance(ext, (list, tuple)) else ext
+            fd.ext[d][s] = e
+    fd.padding = padding
+    return fd
+
+
+class Leaf(api.Expr):
+    """Expression leaf standing for a field slot (oracle-side)."""
+    _is_field = True
+
+    def __init__(self, tag):
+        self.tag = tag
+
+
+def ftcs_expr(u, s, ndim):
+    t = api.d2x(u) + api.d2y(u) if ndim >= 2 else api.d2x(u)
+    if ndim == 3:
+        t = t + api.d2z(u)
+    return u + s * t
+
+
+def weno_stage_exprs(u, u1, u2, dt, upwind=False):
+    L = api.d1_weno53_upwind if upwind else api.d1_weno53_downwind
+    e1 = u - dt * L(u, 0)
+    e2 = 0.75 * u + 0.25 * (u1 - dt * L(u1, 0))
+    e3 = 1.0 / 3.0 * u + 2.0 / 3.0 * (u2 - dt * L(u2, 0))
+    return e1, e2, e3
+
+
+def readable(info):
+    return [(max(info.local[d][0] - info.padding, info.logical[d][0]), min(info.local[d][1] + info.padding, info.logical[d][1]))
+            for d in range(info.ndim)]
+
+
+def seeded_interior(hf, seed, n_line):
+    """u01(seed, j*n + i) on the assignable range (the reference driver's initialisation)."""
+    rng = hf.assignable()
+    if hf.info.ndim == 2:
+        j, i = np.meshgrid(np.arange(*rng[1]), np.arange(*rng[0]), indexing="ij")
+        hf.data[hf.slices(rng)] = orc.u01(seed, (j.astype(np.uint64) * np.uint64(n_line) + i.astype(np.uint64)))
+    else:
+        raise NotImplementedError

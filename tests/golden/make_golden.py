@@ -1,0 +1,97 @@
+"""Regenerates the golden fixtures in this directory from the reference itself.
+
+Runs oracle/_ref/ref_driver (OpFlow's own CPU code, built by oracle/build_ref.sh from the reference
+sources) on small cases and stores every dump as a .npz next to this script.  Needs the reference tree
+(present only where the fixtures are generated); the fixtures themselves are committed so the tests
+run anywhere.
+
+    python tests/golden/make_golden.py
+"""
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
+
+CASES = {
+    # FTCS2D (Corner, Dirichlet all sides): n, steps, seed, bc value, dt/h^2
+    "ftcs2d_n17": ["ftcs2d", "17", "50", "1", "0.0", "0.2"],
+    "ftcs2d_n33_bc1": ["ftcs2d", "33", "20", "2", "1.0", "0.2"],
+    "ftcs2d_n20_nonpow2": ["ftcs2d", "20", "30", "3", "0.5", "0.2"],
+    "ftcs2d_n65": ["ftcs2d", "65", "100", "4", "0.0", "0.25"],
+    # FTCS3D (Corner, Dirichlet 0, 8 Gaussians): n, steps, seed, dt/h^2
+    "ftcs3d_n9": ["ftcs3d", "9", "10", "5", "0.1"],
+    "ftcs3d_n12_nonpow2": ["ftcs3d", "12", "6", "6", "0.1"],
+    # WENO5-JS + RK3, periodic cell-centred lines: nx, ny, steps, seed, upwind-kernel flag
+    "weno_down_32x4": ["weno", "32", "4", "5", "7", "0"],
+    "weno_up_64x3": ["weno", "64", "3", "8", "8", "1"],
+    "weno_down_40x2_nonpow2": ["weno", "40", "2", "3", "9", "0"],
+    # assembly (StencilField + StencilPad, generateAb without HYPRE)
+    "asm_csr_dirc": ["assemble", "csr_dirc"],
+    "asm_csr_neum": ["assemble", "csr_neum"],
+    "asm_csr_periodic": ["assemble", "csr_periodic"],
+    "asm_neum2d_n8": ["assemble", "neum2d", "8"],
+    "asm_dirc2d_n8": ["assemble", "dirc2d", "8"],
+    "asm_periodic2d_n8": ["assemble", "periodic2d", "8"],
+    "asm_var2d_n16": ["assemble", "var2d", "16"],
+    "asm_helm_corner_n9": ["assemble", "helm_corner", "9"],
+    "asm_var3d_n6": ["assemble", "var3d", "6"],
+}
+# field construction + padding: nx, ny, loc (0 corner / 1 centre), bc_lo, bc_hi, ext
+# bc codes: 0 Dirc, 1 Neum, 2 Periodic, 3 Symm, 4 ASymm
+for loc in (0, 1):
+    for lo, hi in ((0, 0), (0, 1), (1, 0), (1, 1), (2, 2), (3, 4), (4, 3), (0, 3), (1, 4)):
+        for ext in (1, 2):
+            CASES["pad_l%d_b%d%d_e%d" % (loc, lo, hi, ext)] = ["padding", "9", "7", str(loc), str(lo), str(hi), str(ext)]
+
+
+def parse(path):
+    raw = open(path, "rb").read()
+    pos, out = 0, []
+    while pos < len(raw):
+        nl = raw.index(b"\n", pos)
+        kind, js = raw[pos:nl].decode().split(" ", 1)
+        meta = json.loads(js)
+        pos = nl + 1
+        if kind == "FIELD":
+            n = meta["count"]
+            arr = np.frombuffer(raw[pos:pos + 8 * n], dtype="<f8").copy()
+            pos += 8 * n
+            out.append((kind, meta, {"data": arr}))
+        else:
+            n, ne = meta["count"], meta["nent"]
+            coef = np.frombuffer(raw[pos:pos + 8 * n * ne], dtype="<f8").copy().reshape(n, ne)
+            pos += 8 * n * ne
+            rhs = np.frombuffer(raw[pos:pos + 8 * n], dtype="<f8").copy()
+            pos += 8 * n
+            out.append((kind, meta, {"coef": coef, "rhs": rhs}))
+    return out
+
+
+def main():
+    if not os.path.exists(DRIVER):
+        subprocess.check_call([os.path.join(ROOT, "oracle", "build_ref.sh")])
+    for name, args in sorted(CASES.items()):
+        with tempfile.TemporaryDirectory() as td:
+            out = os.path.join(td, "o.bin")
+            subprocess.check_call([DRIVER, out] + args)
+            recs = parse(out)
+        arrays, metas = {}, []
+        for kind, meta, arrs in recs:
+            key = meta.get("name", "stencil")
+            metas.append({"kind": kind, "key": key, "meta": meta})
+            for k, v in arrs.items():
+                arrays["%s__%s" % (key, k)] = v
+        arrays["meta"] = np.array(json.dumps({"args": args, "records": metas}))
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrays)
+        print(name, [m["key"] for m in metas])
+
+
+if __name__ == "__main__":
+    sys.exit(main())
