@@ -14,6 +14,7 @@ Names, argument meanings and error behaviour follow the reference (paths relativ
 Python cannot overload `=`, so `u = expr` is spelled `u.assign(expr)` (and `u += expr` is
 `u.assign(expr, op="+")`).  Every call goes through the C ABI of libopflow_gpu.so.
 """
+import atexit
 import ctypes as C
 import threading
 
@@ -45,6 +46,14 @@ class DimPos:
 # ---------------------------------------------------------------------------------------------- context
 _ctx_lock = threading.Lock()
 _default_ctx = {}
+_exiting = [False]
+
+
+@atexit.register
+def _mark_exit():
+    # at interpreter shutdown objects are finalised in no particular order; device memory is released
+    # with the process instead of through destructors that may outlive their context
+    _exiting[0] = True
 
 
 class Context:
@@ -63,9 +72,9 @@ class Context:
         check(lib().opflow_ctx_set_stream(self.handle, C.c_void_p(stream_ptr)))
 
     def close(self):
-        if self.handle:
+        if self.handle and not _exiting[0]:
             lib().opflow_ctx_destroy(self.handle)
-            self.handle = None
+        self.handle = None
 
     def __del__(self):
         try:
@@ -432,9 +441,9 @@ class CartesianField(Expr):
         return self
 
     def close(self):
-        if getattr(self, "handle", None):
+        if getattr(self, "handle", None) and not _exiting[0]:
             lib().opflow_field_destroy(self.handle)
-            self.handle = None
+        self.handle = None
 
     def __del__(self):
         try:
@@ -519,3 +528,108 @@ def describe(mesh, desc):
     md = mesh.desc()
     check(lib().opflow_field_describe(C.byref(md), C.byref(desc), C.byref(info)))
     return info
+
+
+# ------------------------------------------------------------------------------------------ implicit path
+class StructSolverParams:
+    """StructSolverParamsBase (src/Core/Solvers/Struct/StructSolver.hpp:39-51) with the PFMG knobs
+    (StructSolverPFMG.hpp:23-33) and the GPU extensions (precision form, coarse size)."""
+
+    def __init__(self, tol=1e-10, maxIter=200, staticMat=False, pinValue=False, precision="fp64", preSweeps=2,
+                 postSweeps=2, coarseMax=256, zeroGuess=False):
+        self.tol, self.maxIter, self.staticMat, self.pinValue = tol, maxIter, staticMat, pinValue
+        self.precision, self.preSweeps, self.postSweeps, self.coarseMax, self.zeroGuess = (precision, preSweeps, postSweeps,
+                                                                                           coarseMax, zeroGuess)
+
+    def to_c(self):
+        p = capi.SolveParams()
+        p.tol = float(self.tol)
+        p.max_iter = int(self.maxIter)
+        p.static_mat = int(bool(self.staticMat))
+        p.pin_value = int(bool(self.pinValue))
+        p.precision = {"fp64": capi.PREC_FP64, "mixed": capi.PREC_MIXED}[self.precision]
+        p.pre_sweeps, p.post_sweeps = int(self.preSweeps), int(self.postSweeps)
+        p.coarse_max = int(self.coarseMax)
+        p.zero_guess = int(bool(self.zeroGuess))
+        return p
+
+
+class EqnSolveState:
+    """EqnSolveState{niter, relerr, abserr} (src/Core/Equation/EqnSolveHandler.hpp:17-25)."""
+
+    def __init__(self, st):
+        self.niter = st.iterations
+        self.relerr = st.rel_residual
+        self.abserr = st.abs_residual
+        self.converged = bool(st.converged)
+        self.setup_ms = st.setup_ms
+        self.solve_ms = st.solve_ms
+
+    def __repr__(self):
+        return "EqnSolveState(niter=%d, relerr=%.3g)" % (self.niter, self.relerr)
+
+
+class EqnSolveHandler:
+    """makeEqnSolveHandler(getter, target, PrecondStructSolver<PCG,PFMG>) (HYPREEqnSolveHandler.hpp:44-231):
+    `getter(e)` builds the equation in the unknown `e`; the target field is the StencilField's base."""
+
+    def __init__(self, getter, target, params=None):
+        self.target = target
+        self.params = params or StructSolverParams()
+        eq = getter(target)
+        if not isinstance(eq, Equation):
+            raise TypeError("the equation getter must return `lhs == rhs` (use api.Eq for a scalar lhs)")
+        nodes, leaves = serialize(eq.residual_expr(), [target])
+        self._leaves = leaves
+        hs = (C.c_void_p * len(leaves))(*[f.handle.value for f in leaves])
+        p = self.params.to_c()
+        h = C.c_void_p()
+        check(lib().opflow_solver_create(target.ctx.handle, target.handle, nodes, len(nodes), hs, len(leaves), 0, C.byref(p), C.byref(h)))
+        self.handle = h
+
+    def solve(self):
+        st = capi.SolveState()
+        rc = lib().opflow_solver_solve(self.handle, C.byref(st))
+        if rc not in (capi.OK, capi.E_NOT_CONVERGED):
+            check(rc)
+        return EqnSolveState(st)
+
+    def close(self):
+        if getattr(self, "handle", None) and not _exiting[0]:
+            lib().opflow_solver_destroy(self.handle)
+        self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def makeEqnSolveHandler(getter, target, params=None):
+    return EqnSolveHandler(getter, target, params)
+
+
+def Solve(getter, target, params=None, pparams=None):
+    """Solve(f, target, params, pparams) (src/Core/Equation/UnifiedSolve.hpp:36-43): one solve."""
+    return EqnSolveHandler(getter, target, params).solve()
+
+
+def assemble(getter, target, pin=False):
+    """The coefficients and right-hand side HYPREEqnSolveHandler::generateAb would hand to HYPRE
+    (opflow_assemble): (offsets[n_entries, D], coef[cells, n_entries], rhs[cells])."""
+    eq = getter(target)
+    nodes, leaves = serialize(eq.residual_expr(), [target])
+    hs = (C.c_void_p * len(leaves))(*[f.handle.value for f in leaves])
+    ne, nc = C.c_int(0), C.c_size_t(0)
+    L = lib()
+    check(L.opflow_assemble(target.ctx.handle, target.handle, nodes, len(nodes), hs, len(leaves), 0, int(pin), C.byref(ne), None, None,
+                            None, C.byref(nc)))
+    D = target.info.ndim
+    off = np.zeros(ne.value * D, dtype=np.int32)
+    coef = np.zeros(nc.value * ne.value)
+    rhs = np.zeros(nc.value)
+    check(L.opflow_assemble(target.ctx.handle, target.handle, nodes, len(nodes), hs, len(leaves), 0, int(pin), C.byref(ne),
+                            off.ctypes.data_as(C.POINTER(C.c_int)), coef.ctypes.data_as(C.POINTER(C.c_double)),
+                            rhs.ctypes.data_as(C.POINTER(C.c_double)), C.byref(nc)))
+    return off.reshape(ne.value, D), coef.reshape(nc.value, ne.value), rhs

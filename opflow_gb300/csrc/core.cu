@@ -178,7 +178,10 @@ __global__ void pad_kernel(FieldView f, PadOp op, const double* __restrict__ mx,
     const long long nx = op.hi[0] - op.lo[0], ny = op.hi[1] - op.lo[1], nz = op.hi[2] - op.lo[2];
     const long long total = nx * ny * nz;
     for (long long t = blockIdx.x * (long long) blockDim.x + threadIdx.x; t < total; t += (long long) gridDim.x * blockDim.x) {
-        int idx[3] = {op.lo[0] + (int) (t % nx), op.lo[1] + (int) ((t / nx) % ny), op.lo[2] + (int) (t / (nx * ny))};
+        Box bx;
+        for (int d = 0; d < 3; ++d) { bx.lo[d] = op.lo[d]; bx.hi[d] = op.hi[d]; }
+        int idx[3];
+        box_index(t, bx, idx[0], idx[1], idx[2]);
         const long long o = (idx[0] - f.off[0]) + (idx[1] - f.off[1]) * f.sy + (idx[2] - f.off[2]) * f.sz;
         if (op.kind == PAD_FILL) {
             f.data[o] = op.bcv;
@@ -227,7 +230,7 @@ __global__ void pad_kernel(FieldView f, PadOp op, const double* __restrict__ mx,
     }
 }
 
-static int launch_pad(opflow_field f, double* data, const PadOp& op) {
+static int launch_pad_box(opflow_field f, double* data, const PadOp& op) {
     Box b;
     for (int d = 0; d < 3; ++d) { b.lo[d] = op.lo[d]; b.hi[d] = op.hi[d]; }
     const long long n = b.count();
@@ -242,9 +245,36 @@ static int launch_pad(opflow_field f, double* data, const PadOp& op) {
     return check_launch("pad_kernel");
 }
 
+// The reference fills a padding zone in one x-fastest pass.  A periodic zone wider than the period
+// copies from cells of the same zone, so such a zone is filled layer by layer along `dim` in the
+// reference's order.  (Mirror zones read the interior or the other side's zone, never their own.)
+static int launch_pad(opflow_field f, double* data, const PadOp& op) {
+    const int i = op.dim;
+    const int width = op.hi[i] - op.lo[i];
+    const bool overlap = op.kind == PAD_PERIODIC && op.period < width;
+    if (!overlap) return launch_pad_box(f, data, op);
+    for (int l = op.lo[i]; l < op.hi[i]; ++l) {
+        PadOp layer = op;
+        layer.lo[i] = l;
+        layer.hi[i] = l + 1;
+        OPG_TRY(launch_pad_box(f, data, layer));
+    }
+    return OPFLOW_OK;
+}
+
+int update_padding_full(opflow_field f, double* data);
+
 // Step 0 (Dirichlet values on corner-located boundary nodes) is idempotent with what the kernels write,
 // step 1 mirrors, step 2 periodic copies, in the reference's order.
 int update_padding_buf(opflow_field f, double* data) {
+    const int which = data == f->buf[0] ? 0 : 1;
+    if (f->padding_is_step0_only() && f->bc_fresh[which]) return OPFLOW_OK;
+    OPG_TRY(update_padding_full(f, data));
+    f->bc_fresh[which] = true;
+    return OPFLOW_OK;
+}
+
+int update_padding_full(opflow_field f, double* data) {
     const opflow_field_info& R = f->info;
     const opflow_field_desc& F = f->desc;
     const int D = R.ndim;
@@ -316,10 +346,20 @@ int ensure_back(opflow_field f) {
         return fail(OPFLOW_E_NOMEM, "cannot allocate the second buffer of a field (%zu doubles)", f->info.count);
     OPG_CUDA(cudaMemcpyAsync(p, f->buf[f->cur], f->info.count * sizeof(double), cudaMemcpyDeviceToDevice, f->ctx->stream));
     f->buf[1 - f->cur] = p;
+    f->bc_fresh[1 - f->cur] = f->bc_fresh[f->cur];
     return OPFLOW_OK;
 }
 
 }  // namespace opg
+
+// With no ghost layer (padding 0, all ext 0) updatePadding can only write corner-located Dirichlet
+// nodes (step 0), whose values are constants.
+bool opflow_field_s::padding_is_step0_only() const {
+    if (info.padding != 0) return false;
+    for (int d = 0; d < info.ndim; ++d)
+        if (desc.ext[d][0] != 0 || desc.ext[d][1] != 0) return false;
+    return true;
+}
 
 opg::FieldView opflow_field_s::view() const {
     opg::FieldView v;
@@ -459,6 +499,7 @@ int opflow_field_get_info(opflow_field f, opflow_field_info* out) {
 int opflow_field_upload(opflow_field f, const double* host, size_t count) {
     if (!f || !host) return fail(OPFLOW_E_INVALID, "null argument");
     if (count != f->info.count) return fail(OPFLOW_E_INVALID, "upload of %zu values into a field of %zu", count, f->info.count);
+    f->bc_fresh[0] = f->bc_fresh[1] = false;
     OPG_CUDA(cudaMemcpyAsync(f->buf[f->cur], host, count * sizeof(double), cudaMemcpyHostToDevice, f->ctx->stream));
     if (f->buf[1 - f->cur])
         OPG_CUDA(cudaMemcpyAsync(f->buf[1 - f->cur], f->buf[f->cur], count * sizeof(double), cudaMemcpyDeviceToDevice, f->ctx->stream));
@@ -477,12 +518,15 @@ int opflow_field_download(opflow_field f, double* host, size_t count) {
 int opflow_field_device_ptr(opflow_field f, double** p) {
     if (!f || !p) return fail(OPFLOW_E_INVALID, "null argument");
     *p = f->buf[f->cur];
+    f->bc_fresh[0] = f->bc_fresh[1] = false;  // the caller may write through the pointer
     return OPFLOW_OK;
 }
 
 int opflow_field_update_padding(opflow_field f) {
     if (!f) return fail(OPFLOW_E_INVALID, "null field");
-    return update_padding_buf(f, f->buf[f->cur]);
+    OPG_TRY(update_padding_full(f, f->buf[f->cur]));
+    f->bc_fresh[f->cur] = true;
+    return OPFLOW_OK;
 }
 
 }  // extern "C"

@@ -11,6 +11,7 @@
 //   3. Everything else runs in a generic interpreter kernel over a postfix program expanded from the
 //      tree, again in the reference's operation order.
 #include "internal.h"
+#include "stencil.h"
 
 #include <algorithm>
 #include <array>
@@ -284,7 +285,8 @@ __global__ void __launch_bounds__(128) interp_kernel(const Instr* __restrict__ p
     const long long nx = box.hi[0] - box.lo[0], ny = box.hi[1] - box.lo[1], nz = box.hi[2] - box.lo[2];
     const long long total = nx * ny * nz;
     for (long long t = blockIdx.x * (long long) blockDim.x + threadIdx.x; t < total; t += (long long) gridDim.x * blockDim.x) {
-        const int i = box.lo[0] + (int) (t % nx), j = box.lo[1] + (int) ((t / nx) % ny), k = box.lo[2] + (int) (t / (nx * ny));
+        int i, j, k;
+        box_index(t, box, i, j, k);
         const int idx[3] = {i, j, k};
         double st[STACK_MAX];
         int sp = 0;
@@ -344,7 +346,8 @@ __global__ void __launch_bounds__(256) ftcs_exact_kernel(FieldView in, FieldView
     const long long nx = box.hi[0] - box.lo[0], ny = box.hi[1] - box.lo[1], nz = box.hi[2] - box.lo[2];
     const long long total = nx * ny * nz;
     for (long long t = blockIdx.x * (long long) blockDim.x + threadIdx.x; t < total; t += (long long) gridDim.x * blockDim.x) {
-        const int i = box.lo[0] + (int) (t % nx), j = box.lo[1] + (int) ((t / nx) % ny), k = box.lo[2] + (int) (t / (nx * ny));
+        int i, j, k;
+        box_index(t, box, i, j, k);
         const long long o = (i - in.off[0]) + (j - in.off[1]) * in.sy + (k - in.off[2]) * in.sz;
         const double c = in.data[o];
         double sum = 0.;
@@ -491,7 +494,8 @@ __global__ void __launch_bounds__(256) fast_stencil_kernel(FieldView in, FieldVi
     unsigned long long local_max = 0;
     if (blockIdx.x == 0 && threadIdx.x == 0) maxslots[(step + 2) % 3] = 0ull;
     for (long long t = blockIdx.x * (long long) blockDim.x + threadIdx.x; t < total; t += (long long) gridDim.x * blockDim.x) {
-        const int i = box.lo[0] + (int) (t % nx), j = box.lo[1] + (int) ((t / nx) % ny), k = box.lo[2] + (int) (t / (nx * ny));
+        int i, j, k;
+        box_index(t, box, i, j, k);
         const long long o = (i - in.off[0]) + (j - in.off[1]) * in.sy + (k - in.off[2]) * in.sz;
         const long long qc = to_fixed(in.data[o], E);
         long long z[4] = {0, 0, 0, 0};
@@ -529,7 +533,8 @@ __global__ void maxabs_kernel(FieldView in, Box box, unsigned long long* slot) {
     const long long total = nx * ny * nz;
     unsigned long long m = 0;
     for (long long t = blockIdx.x * (long long) blockDim.x + threadIdx.x; t < total; t += (long long) gridDim.x * blockDim.x) {
-        const int i = box.lo[0] + (int) (t % nx), j = box.lo[1] + (int) ((t / nx) % ny), k = box.lo[2] + (int) (t / (nx * ny));
+        int i, j, k;
+        box_index(t, box, i, j, k);
         const unsigned long long b = (unsigned long long) __double_as_longlong(ld(in, i, j, k)) & 0x7FFFFFFFFFFFFFFFull;
         m = b > m ? b : m;
     }
@@ -545,7 +550,8 @@ __global__ void fill_kernel(FieldView f, Box box, int arith, double c) {
     const long long nx = box.hi[0] - box.lo[0], ny = box.hi[1] - box.lo[1], nz = box.hi[2] - box.lo[2];
     const long long total = nx * ny * nz;
     for (long long t = blockIdx.x * (long long) blockDim.x + threadIdx.x; t < total; t += (long long) gridDim.x * blockDim.x) {
-        const int i = box.lo[0] + (int) (t % nx), j = box.lo[1] + (int) ((t / nx) % ny), k = box.lo[2] + (int) (t / (nx * ny));
+        int i, j, k;
+        box_index(t, box, i, j, k);
         const long long o = (i - f.off[0]) + (j - f.off[1]) * f.sy + (k - f.off[2]) * f.sz;
         f.data[o] = arith == OPFLOW_ASSIGN_EQ ? c : apply_arith(arith, f.data[o], c);
     }
@@ -560,7 +566,7 @@ static int grid_for(opflow_ctx ctx, long long n, int threads) {
 }
 
 // ======================================================================================== planning
-enum PlanKind { PLAN_INTERP = 0, PLAN_FTCS_EXACT = 1, PLAN_FAST = 2 };
+enum PlanKind { PLAN_INTERP = 0, PLAN_FTCS_EXACT = 1, PLAN_FAST = 2, PLAN_AXIS_EXACT = 3, PLAN_AXIS_FAST = 4 };
 struct Plan {
     int kind = PLAN_INTERP;
     bool aliased = false;
@@ -571,8 +577,37 @@ struct Plan {
     MeshPtrs mesh{};
     FtcsParams ftcs{};
     FastParams fast{};
+    AxisParams axis{};
     int src_slot = -1;  // field read by the specialised kernels
 };
+
+// The fixed-point form as per-dim weights of (u(i-e_d) - u) + (u(i+e_d) - u), if it has that shape.
+static bool fast_to_axis(const FastParams& F, int ndim, AxisParams* A) {
+    if (ndim < 2 || F.nnb != 2 * ndim) return false;
+    int g_of_dim[3] = {-1, -1, -1};
+    int seen[3][2] = {{0, 0}, {0, 0}, {0, 0}};
+    for (int n = 0; n < F.nnb; ++n) {
+        int d = -1, sgn = 0;
+        for (int q = 0; q < 3; ++q)
+            if (F.off[n][q]) { d = q; sgn = F.off[n][q] > 0; }
+        if (d < 0 || d >= ndim) return false;
+        if (seen[d][sgn]) return false;
+        seen[d][sgn] = 1;
+        if (g_of_dim[d] >= 0 && g_of_dim[d] != F.group[n]) return false;  // x- and x+ weights differ
+        g_of_dim[d] = F.group[n];
+    }
+    std::memset(A, 0, sizeof *A);
+    A->ndim = ndim;
+    A->iso = F.ngroups == 1;
+    for (int d = 0; d < ndim; ++d) {
+        const int g = g_of_dim[d];
+        A->wm[d] = F.wm[g];
+        A->wshift[d] = F.wshift[g];
+        A->wneg[d] = F.wneg[g];
+    }
+    A->bound_bits = F.bound_bits;
+    return true;
+}
 
 // Checks that every read of the program at every point of the box stays inside the leaf's data array.
 static int check_reads(const Compiler& C, const Box& box, const opflow_field* leaves, int nleaves) {
@@ -794,6 +829,7 @@ static int build_plan(opflow_ctx ctx, opflow_field dst, int arith, const opflow_
             plan->kind = PLAN_FAST;
             plan->fast = fp;
             plan->src_slot = slot;
+            if (fast_to_axis(fp, dst->mesh->ndim, &plan->axis)) plan->kind = PLAN_AXIS_FAST;
         } else {
             FtcsParams P{};
             if (match_ftcs(nodes, n, dst->mesh, &P, &slot)) {
@@ -808,6 +844,19 @@ static int build_plan(opflow_ctx ctx, opflow_field dst, int arith, const opflow_
                     plan->kind = PLAN_FTCS_EXACT;
                     plan->ftcs = P;
                     plan->src_slot = slot;
+                    if (P.ndim >= 2) {
+                        AxisParams& A = plan->axis;
+                        std::memset(&A, 0, sizeof A);
+                        A.ndim = P.ndim;
+                        for (int d = 0; d < 3; ++d) {
+                            A.h[d] = P.h[d];
+                            A.inv_h[d] = P.inv_h[d];
+                            A.pow2[d] = P.pow2[d];
+                            A.order[d] = d < P.ndim ? P.dims_order[d] : 0;
+                        }
+                        A.s = P.s;
+                        plan->kind = PLAN_AXIS_EXACT;
+                    }
                 }
             }
         }
@@ -845,6 +894,9 @@ static int run_plan(opflow_ctx ctx, opflow_field dst, int arith, const opflow_fi
                 OPG_TRY(check_launch("ftcs_exact_kernel"));
                 break;
             }
+            case PLAN_AXIS_EXACT: case PLAN_AXIS_FAST:
+                OPG_TRY(axis_launch(ctx, leaves[plan->src_slot]->view(), out, plan->box, plan->axis, plan->kind == PLAN_AXIS_FAST, maxslots, step));
+                break;
             case PLAN_FAST: {
                 const FieldView in = leaves[plan->src_slot]->view();
                 const int g = grid_for(ctx, total, 256);
@@ -886,7 +938,7 @@ int opflow_assign_repeat(opflow_ctx ctx, opflow_field dst, int arith, const opfl
     int rc = build_plan(ctx, dst, arith, nodes, n_nodes, leaves, n_leaves, mode, &plan);
     if (rc) { free_plan(&plan); return rc; }
     unsigned long long* maxslots = nullptr;
-    if (plan.kind == PLAN_FAST) {
+    if (plan.kind == PLAN_FAST || plan.kind == PLAN_AXIS_FAST) {
         rc = ensure_scratch(ctx, 256);
         if (rc) { free_plan(&plan); return rc; }
         maxslots = (unsigned long long*) ctx->scratch;
@@ -927,6 +979,7 @@ int opflow_field_fill(opflow_field f, int arith, double c) {
 int opflow_field_copy(opflow_field dst, opflow_field src) {
     if (!dst || !src) return fail(OPFLOW_E_INVALID, "null field");
     if (dst->info.count != src->info.count) return fail(OPFLOW_E_INVALID, "field shapes differ");
+    dst->bc_fresh[0] = dst->bc_fresh[1] = false;
     OPG_CUDA(cudaMemcpyAsync(dst->buf[dst->cur], src->buf[src->cur], src->info.count * sizeof(double), cudaMemcpyDeviceToDevice, dst->ctx->stream));
     OPG_TRY(update_padding_buf(dst, dst->buf[dst->cur]));
     OPG_CUDA(cudaStreamSynchronize(dst->ctx->stream));

@@ -66,6 +66,24 @@ struct MeshDev {
     double h[3];        // uniform spacing (valid when uniform[d])
 };
 
+#ifdef __CUDACC__
+// Grid-stride linear index -> box index (x fastest), with 32-bit division when the box allows.
+__device__ __forceinline__ void box_index(long long t, const Box& b, int& i, int& j, int& k) {
+    const unsigned nx = (unsigned) (b.hi[0] - b.lo[0]), ny = (unsigned) (b.hi[1] - b.lo[1]);
+    if (t < 0xFFFFFFFFll) {
+        const unsigned tt = (unsigned) t, q = tt / nx, r = q / ny;
+        i = b.lo[0] + (int) (tt - q * nx);
+        j = b.lo[1] + (int) (q - r * ny);
+        k = b.lo[2] + (int) r;
+    } else {
+        const long long q = t / nx, r = q / ny;
+        i = b.lo[0] + (int) (t - q * nx);
+        j = b.lo[1] + (int) (q - r * ny);
+        k = b.lo[2] + (int) r;
+    }
+}
+#endif
+
 }  // namespace opg
 
 struct opflow_ctx_s {
@@ -86,6 +104,11 @@ struct opflow_field_s {
     int mesh_refs_owner = 1;
     double* buf[2] = {nullptr, nullptr};  // front = buf[cur]; back allocated on the first aliased assign
     int cur = 0;
+    // buffer k already holds this field's boundary values (set by a padding update, cleared whenever
+    // the caller may have written the buffer); lets a padding update that can only rewrite constant
+    // Dirichlet nodes be skipped
+    bool bc_fresh[2] = {false, false};
+    bool padding_is_step0_only() const;
     opg::FieldView view() const;
     opg::FieldView view_back() const;
 };

@@ -1,0 +1,881 @@
+// Path I, steps 2-3: the multigrid hierarchy and the flexible-PCG driver.
+//
+// Replaces HYPREEqnSolveHandler::solve with StructSolver<PCG> + StructSolver<PFMG>
+// (src/Core/Equation/HYPREEqnSolveHandler.hpp:190-209, src/Core/Solvers/Struct/StructSolverPCG.hpp,
+// StructSolverPFMG.hpp): a matrix-free geometric multigrid V-cycle preconditions a float64 flexible
+// conjugate-gradient iteration.
+//
+// Coarse levels are rediscretisations of the user's own equation: the same `lhs - rhs` tree is
+// assembled (StencilPad semantics) on a mesh of twice the spacing, with the known fields restricted
+// (cell averages / node injection).  Levels whose coefficients depend only on the position class of a
+// cell (first / interior / last per dim) keep a 27-entry table instead of per-cell arrays, so their
+// smoothing sweeps read no coefficients from HBM.
+//
+// Precision forms: OPFLOW_PREC_FP64 runs the V-cycle in float64; OPFLOW_PREC_MIXED runs it (operator,
+// smoother, residual, transfers) in float32 with float32 accumulation, while the outer residual, the
+// solution update, the inner products and the coarsest dense solve stay float64.
+//
+// A singular system (pure Neumann / periodic: zero row sums) with pinValue is solved as the reference
+// poses it: the pinned system equals the consistent singular system whose pinned-row right-hand side is
+// replaced by minus the sum of the others, followed by a shift that makes the pinned unknown 0.
+#include "solver.h"
+
+#include <chrono>
+#include <cmath>
+
+namespace opg {
+
+// ================================================================================= small kernels
+__global__ void gather_box(FieldView f, Box b, double* out) {
+    const long long nx = b.hi[0] - b.lo[0], ny = b.hi[1] - b.lo[1], nz = b.hi[2] - b.lo[2];
+    for (long long t = blockIdx.x * (long long) blockDim.x + threadIdx.x; t < nx * ny * nz; t += (long long) gridDim.x * blockDim.x) {
+        int i, j, k;
+        box_index(t, b, i, j, k);
+        out[t] = f.data[(i - f.off[0]) + (j - f.off[1]) * f.sy + (k - f.off[2]) * f.sz];
+    }
+}
+__global__ void scatter_box(FieldView f, Box b, const double* in, double shift) {
+    const long long nx = b.hi[0] - b.lo[0], ny = b.hi[1] - b.lo[1], nz = b.hi[2] - b.lo[2];
+    for (long long t = blockIdx.x * (long long) blockDim.x + threadIdx.x; t < nx * ny * nz; t += (long long) gridDim.x * blockDim.x) {
+        int i, j, k;
+        box_index(t, b, i, j, k);
+        f.data[(i - f.off[0]) + (j - f.off[1]) * f.sy + (k - f.off[2]) * f.sz] = in[t] - shift;
+    }
+}
+// restriction of a known field's data to a coarse field: cell averages along centre-located dims,
+// injection along corner-located dims
+__global__ void field_restrict(FieldView fine, FieldView coarse, Box cb, int loc0, int loc1, int loc2, int ndim) {
+    const long long nx = cb.hi[0] - cb.lo[0], ny = cb.hi[1] - cb.lo[1], nz = cb.hi[2] - cb.lo[2];
+    const int locs[3] = {loc0, loc1, loc2};
+    for (long long t = blockIdx.x * (long long) blockDim.x + threadIdx.x; t < nx * ny * nz; t += (long long) gridDim.x * blockDim.x) {
+        int I[3];
+        box_index(t, cb, I[0], I[1], I[2]);
+        double acc = 0.;
+        int cnt = 0;
+        for (int a = 0; a < 2; ++a)
+            for (int b = 0; b < 2; ++b)
+                for (int c = 0; c < 2; ++c) {
+                    const int o[3] = {c, b, a};
+                    int f[3];
+                    bool ok = true;
+                    for (int d = 0; d < 3; ++d) {
+                        if (d >= ndim) { if (o[d]) ok = false; f[d] = 0; continue; }
+                        if (locs[d] == OPFLOW_CORNER) { if (o[d]) ok = false; f[d] = 2 * I[d]; }
+                        else f[d] = 2 * I[d] + o[d];
+                        if (f[d] < fine.off[d] || f[d] >= fine.off[d] + fine.dims[d]) ok = false;
+                    }
+                    if (!ok) continue;
+                    acc += fine.data[(f[0] - fine.off[0]) + (f[1] - fine.off[1]) * fine.sy + (f[2] - fine.off[2]) * fine.sz];
+                    cnt++;
+                }
+        coarse.data[(I[0] - coarse.off[0]) + (I[1] - coarse.off[1]) * coarse.sy + (I[2] - coarse.off[2]) * coarse.sz] = cnt ? acc / cnt : 0.;
+    }
+}
+// coefficients from the assembly's K order into the 7 slots; flags entries outside the slots
+__global__ void map_slots(const double* coef, long long N, const int* kslot, int nk, double* A, int* bad) {
+    for (long long t = blockIdx.x * (long long) blockDim.x + threadIdx.x; t < N; t += (long long) gridDim.x * blockDim.x) {
+        for (int s = 0; s < NSLOT; ++s) A[s * N + t] = 0.;
+        for (int k = 0; k < nk; ++k) {
+            const double v = coef[k * N + t];
+            const int s = kslot[k];
+            if (s < 0) { if (v != 0.) atomicExch(bad, 1); }
+            else A[s * N + t] += v;
+        }
+    }
+}
+__global__ void to_f32(const double* a, float* b, long long n) {
+    for (long long t = blockIdx.x * (long long) blockDim.x + threadIdx.x; t < n; t += (long long) gridDim.x * blockDim.x) b[t] = (float) a[t];
+}
+// compare every cell's coefficients with its class representative
+__global__ void class_check(const double* A, long long N, int n0, int n1, int n2, int ndim, const double* tab, int* bad) {
+    for (long long t = blockIdx.x * (long long) blockDim.x + threadIdx.x; t < N; t += (long long) gridDim.x * blockDim.x) {
+        Box b;
+        b.lo[0] = b.lo[1] = b.lo[2] = 0;
+        b.hi[0] = n0; b.hi[1] = n1; b.hi[2] = n2;
+        int i, j, k;
+        box_index(t, b, i, j, k);
+        auto pc = [](int x, int n) { return x == 0 ? 0 : (x == n - 1 ? 2 : 1); };
+        const int cls = pc(i, n0) + 3 * (ndim > 1 ? pc(j, n1) : 0) + 9 * (ndim > 2 ? pc(k, n2) : 0);
+        for (int s = 0; s < NSLOT; ++s)
+            if (__double_as_longlong(A[s * N + t]) != __double_as_longlong(tab[cls * NSLOT + s])) { atomicExch(bad, 1); return; }
+    }
+}
+// max |row sum| and max |diag| (bit patterns of non-negative doubles)
+__global__ void rowsum_stats(const double* A, long long N, int n0, int n1, int n2, int ndim, int p0, int p1, int p2, unsigned long long* out) {
+    unsigned long long ms = 0, md = 0;
+    for (long long t = blockIdx.x * (long long) blockDim.x + threadIdx.x; t < N; t += (long long) gridDim.x * blockDim.x) {
+        Box b;
+        b.lo[0] = b.lo[1] = b.lo[2] = 0;
+        b.hi[0] = n0; b.hi[1] = n1; b.hi[2] = n2;
+        int i, j, k;
+        box_index(t, b, i, j, k);
+        double s = A[t];
+        const int idx[3] = {i, j, k}, n[3] = {n0, n1, n2}, per[3] = {p0, p1, p2};
+        for (int d = 0; d < ndim; ++d) {
+            if (idx[d] > 0 || per[d]) s += A[(1 + 2 * d) * N + t];
+            if (idx[d] < n[d] - 1 || per[d]) s += A[(2 + 2 * d) * N + t];
+        }
+        const unsigned long long bs = (unsigned long long) __double_as_longlong(fabs(s)), bd = (unsigned long long) __double_as_longlong(fabs(A[t]));
+        ms = bs > ms ? bs : ms;
+        md = bd > md ? bd : md;
+    }
+    atomicMax(&out[0], ms);
+    atomicMax(&out[1], md);
+}
+__global__ void sum_partials(const double* v, long long n, double* partial) {
+    __shared__ double sh[256];
+    double s = 0.;
+    for (long long t = blockIdx.x * (long long) blockDim.x + threadIdx.x; t < n; t += (long long) gridDim.x * blockDim.x) s += v[t];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int) threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+}
+__global__ void add_scalar(double* v, long long n, double a) {
+    for (long long t = blockIdx.x * (long long) blockDim.x + threadIdx.x; t < n; t += (long long) gridDim.x * blockDim.x) v[t] += a;
+}
+
+static int gridN(opflow_ctx ctx, long long n) {
+    long long b = (n + 255) / 256;
+    return (int) std::max(1LL, std::min(b, (long long) ctx->num_sms * 16));
+}
+
+// ================================================================================= arena
+void* Arena::alloc(size_t bytes) {
+    bytes = (bytes + 255) & ~(size_t) 255;
+    if (blocks.empty() || used + bytes > cap) {
+        size_t sz = std::max(bytes, (size_t) 256 << 20);
+        void* p = nullptr;
+        if (cudaMalloc(&p, sz) != cudaSuccess) return nullptr;
+        blocks.push_back(p);
+        cap = sz;
+        used = 0;
+    }
+    void* r = (char*) blocks.back() + used;
+    used += bytes;
+    total += bytes;
+    return r;
+}
+void Arena::release() {
+    for (void* p : blocks) cudaFree(p);
+    blocks.clear();
+    cap = used = total = 0;
+}
+
+// ================================================================================= setup
+static int ghost_rule(int bct) {
+    switch (bct) {
+        case OPFLOW_BC_DIRC: case OPFLOW_BC_ASYMM: return GH_ZERO;
+        case OPFLOW_BC_PERIODIC: return GH_WRAP;
+        default: return GH_COPY;
+    }
+}
+
+// Assembles `tree` for `target` (leaves by slot) into level L: slot-ordered FP64 coefficients and,
+// when rhs != nullptr, the right-hand side b = -bias.
+static int assemble_level(MGSystem* S, opflow_field target, const std::vector<opflow_node>& tree, const std::vector<opflow_field>& leaves,
+                          int unknown, LevelHost& L, double* rhs) {
+    opflow_ctx ctx = S->ctx;
+    AsmPlan plan;
+    OPG_TRY(asm_prepare(ctx, target, tree.data(), (int) tree.size(), leaves.data(), (int) leaves.size(), unknown, 0, &plan));
+    const long long N = plan.cells;
+    const int nk = plan.P.nk;
+    double *coef = nullptr, *tmp_rhs = nullptr;
+    int* dks = nullptr;
+    if (cudaMalloc(&coef, (size_t) N * nk * sizeof(double)) != cudaSuccess) return fail(OPFLOW_E_NOMEM, "assembly buffer");
+    if (!rhs && cudaMalloc(&tmp_rhs, (size_t) N * sizeof(double)) != cudaSuccess) { cudaFree(coef); return fail(OPFLOW_E_NOMEM, "assembly buffer"); }
+    int rc = asm_run(ctx, &plan, coef, rhs ? rhs : tmp_rhs);
+    std::vector<int> ks(nk, -1);
+    for (int k = 0; k < nk; ++k) {
+        const int* o = plan.P.K[k];
+        int nz = 0, d = -1;
+        for (int q = 0; q < 3; ++q)
+            if (o[q]) { nz++; d = q; }
+        if (nz == 0) ks[k] = 0;
+        else if (nz == 1 && std::abs(o[d]) == 1) ks[k] = 1 + 2 * d + (o[d] > 0 ? 1 : 0);
+    }
+    if (rc == OPFLOW_OK) {
+        L.A64 = (double*) S->arena.alloc((size_t) NSLOT * N * sizeof(double));
+        if (!L.A64) rc = fail(OPFLOW_E_NOMEM, "operator arrays");
+    }
+    if (rc == OPFLOW_OK) {
+        cudaMalloc(&dks, nk * sizeof(int));
+        cudaMemcpyAsync(dks, ks.data(), nk * sizeof(int), cudaMemcpyHostToDevice, ctx->stream);
+        int* bad = (int*) ctx->scratch;
+        cudaMemsetAsync(bad, 0, sizeof(int), ctx->stream);
+        map_slots<<<gridN(ctx, N), 256, 0, ctx->stream>>>(coef, N, dks, nk, L.A64, bad);
+        OPG_LAUNCHED();
+        int hb = 0;
+        cudaMemcpyAsync(&hb, bad, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+        cudaStreamSynchronize(ctx->stream);
+        if (hb) rc = fail(OPFLOW_E_UNSUPPORTED, "the equation's stencil has entries beyond the (2*dim+1)-point star the multigrid handles");
+    }
+    cudaFree(coef);
+    if (tmp_rhs) cudaFree(tmp_rhs);
+    if (dks) cudaFree(dks);
+    if (rc) return rc;
+    const Box b = plan.P.box;
+    L.ndim = target->info.ndim;
+    L.N = N;
+    for (int d = 0; d < 3; ++d) {
+        L.n[d] = b.hi[d] - b.lo[d];
+        L.lo[d] = b.lo[d];
+        L.per[d] = d < L.ndim && target->desc.bc_type[d][0] == OPFLOW_BC_PERIODIC;
+        L.gh_lo[d] = ghost_rule(target->desc.bc_type[d][0]);
+        L.gh_hi[d] = ghost_rule(target->desc.bc_type[d][1]);
+    }
+    return OPFLOW_OK;
+}
+
+// Position-class table if every cell matches its class representative exactly.
+static int compress_level(MGSystem* S, LevelHost& L) {
+    opflow_ctx ctx = S->ctx;
+    const long long N = L.N;
+    std::vector<double> tab(NCLASS * NSLOT, 0.);
+    std::vector<double> col(1);
+    auto rep = [&](int c, int n) { return c == 0 ? 0 : (c == 1 ? std::min(1, n - 1) : n - 1); };
+    for (int cz = 0; cz < 3; ++cz)
+        for (int cy = 0; cy < 3; ++cy)
+            for (int cx = 0; cx < 3; ++cx) {
+                if ((L.ndim < 2 && cy) || (L.ndim < 3 && cz)) continue;
+                const int i = rep(cx, L.n[0]), j = L.ndim > 1 ? rep(cy, L.n[1]) : 0, k = L.ndim > 2 ? rep(cz, L.n[2]) : 0;
+                const long long cell = i + (long long) L.n[0] * (j + (long long) L.n[1] * k);
+                const int cls = cx + 3 * cy + 9 * cz;
+                for (int s = 0; s < NSLOT; ++s)
+                    cudaMemcpyAsync(&tab[cls * NSLOT + s], L.A64 + s * N + cell, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+            }
+    OPG_CUDA(cudaStreamSynchronize(ctx->stream));
+    double* dtab = (double*) S->arena.alloc(NCLASS * NSLOT * sizeof(double));
+    float* dtab32 = (float*) S->arena.alloc(NCLASS * NSLOT * sizeof(float));
+    if (!dtab || !dtab32) return fail(OPFLOW_E_NOMEM, "class table");
+    std::vector<float> t32(tab.begin(), tab.end());
+    cudaMemcpyAsync(dtab, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemcpyAsync(dtab32, t32.data(), t32.size() * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
+    int* bad = (int*) ctx->scratch;
+    cudaMemsetAsync(bad, 0, sizeof(int), ctx->stream);
+    class_check<<<gridN(ctx, N), 256, 0, ctx->stream>>>(L.A64, N, L.n[0], L.n[1], L.n[2], L.ndim, dtab, bad);
+    OPG_LAUNCHED();
+    int hb = 0;
+    cudaMemcpyAsync(&hb, bad, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+    OPG_CUDA(cudaStreamSynchronize(ctx->stream));
+    L.T64 = dtab;
+    L.T32 = dtab32;
+    L.table = hb == 0;
+    L.tab = tab;
+    if (!L.table) {
+        L.A32 = (float*) S->arena.alloc((size_t) NSLOT * N * sizeof(float));
+        if (!L.A32) return fail(OPFLOW_E_NOMEM, "float32 operator");
+        to_f32<<<gridN(ctx, NSLOT * N), 256, 0, ctx->stream>>>(L.A64, L.A32, NSLOT * N);
+        OPG_LAUNCHED();
+    }
+    return OPFLOW_OK;
+}
+
+// Dense (pseudo-)inverse of the coarsest operator, on the host (N <= a few hundred).
+static int coarse_inverse(MGSystem* S, LevelHost& L, bool singular) {
+    const int N = (int) L.N;
+    std::vector<double> A((size_t) N * N, 0.), coefs((size_t) NSLOT * N);
+    OPG_CUDA(cudaMemcpy(coefs.data(), L.A64, coefs.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    for (int c = 0; c < N; ++c) {
+        const int i = c % L.n[0], j = (c / L.n[0]) % L.n[1], k = c / (L.n[0] * L.n[1]);
+        const int idx[3] = {i, j, k};
+        A[(size_t) c * N + c] += coefs[c];
+        for (int d = 0; d < L.ndim; ++d)
+            for (int sd = 0; sd < 2; ++sd) {
+                int nb[3] = {i, j, k};
+                nb[d] += sd ? 1 : -1;
+                if (nb[d] < 0 || nb[d] >= L.n[d]) {
+                    if (!L.per[d]) continue;
+                    nb[d] = (nb[d] + L.n[d]) % L.n[d];
+                }
+                (void) idx;
+                const int cn = nb[0] + L.n[0] * (nb[1] + L.n[1] * nb[2]);
+                A[(size_t) c * N + cn] += coefs[(size_t) (1 + 2 * d + sd) * N + c];
+            }
+    }
+    // singular: pin unknown 0 (row and column), invert the rest
+    const int off = singular ? 1 : 0;
+    const int M = N - off;
+    std::vector<double> B((size_t) M * M), Inv((size_t) M * M, 0.);
+    for (int r = 0; r < M; ++r)
+        for (int c = 0; c < M; ++c) B[(size_t) r * M + c] = A[(size_t) (r + off) * N + (c + off)];
+    for (int r = 0; r < M; ++r) Inv[(size_t) r * M + r] = 1.;
+    // Gauss-Jordan with partial pivoting
+    for (int col = 0; col < M; ++col) {
+        int piv = col;
+        for (int r = col + 1; r < M; ++r)
+            if (std::fabs(B[(size_t) r * M + col]) > std::fabs(B[(size_t) piv * M + col])) piv = r;
+        if (B[(size_t) piv * M + col] == 0.) return fail(OPFLOW_E_INVALID, "singular coarsest operator");
+        if (piv != col)
+            for (int c = 0; c < M; ++c) {
+                std::swap(B[(size_t) piv * M + c], B[(size_t) col * M + c]);
+                std::swap(Inv[(size_t) piv * M + c], Inv[(size_t) col * M + c]);
+            }
+        const double d = B[(size_t) col * M + col];
+        for (int c = 0; c < M; ++c) { B[(size_t) col * M + c] /= d; Inv[(size_t) col * M + c] /= d; }
+        for (int r = 0; r < M; ++r) {
+            if (r == col) continue;
+            const double f = B[(size_t) r * M + col];
+            if (f == 0.) continue;
+            for (int c = 0; c < M; ++c) {
+                B[(size_t) r * M + c] -= f * B[(size_t) col * M + c];
+                Inv[(size_t) r * M + c] -= f * Inv[(size_t) col * M + c];
+            }
+        }
+    }
+    std::vector<double> Full((size_t) N * N, 0.);
+    for (int r = 0; r < M; ++r)
+        for (int c = 0; c < M; ++c) Full[(size_t) (r + off) * N + (c + off)] = Inv[(size_t) r * M + c];
+    L.Ainv64 = (double*) S->arena.alloc(Full.size() * sizeof(double));
+    if (!L.Ainv64) return fail(OPFLOW_E_NOMEM, "coarse inverse");
+    OPG_CUDA(cudaMemcpy(L.Ainv64, Full.data(), Full.size() * sizeof(double), cudaMemcpyHostToDevice));
+    return OPFLOW_OK;
+}
+
+// Coarse mesh of the same extent: half the cells (centre) or every other node (corner).
+static bool coarse_mesh(const MeshDev* m, const opflow_field_desc& desc, std::vector<std::vector<double>>& xs, std::vector<std::vector<double>>& dxs,
+                        opflow_mesh_desc* out) {
+    std::memset(out, 0, sizeof *out);
+    out->ndim = m->ndim;
+    out->pad_width = m->n[0] > 0 ? (int) ((m->n[0] - (int) m->hx[0].size()) / 2) : 0;
+    const int pad = (int) (m->hx[0].size() - 0);
+    (void) pad;
+    xs.assign(m->ndim, {});
+    dxs.assign(m->ndim, {});
+    for (int d = 0; d < m->ndim; ++d) {
+        const int pw = -m->es[d];  // meshes built with start 0: es = -pad_width
+        const int nodes = (int) m->hx[d].size() - 2 * pw;
+        int nodes_c;
+        if (desc.loc[d] == OPFLOW_CENTER) {
+            const int cells = nodes - 1;
+            if (cells < 4) return false;
+            nodes_c = (cells + 1) / 2 + 1;
+        } else {
+            if (nodes < 5 || (nodes % 2) == 0) return false;
+            nodes_c = (nodes + 1) / 2;
+        }
+        const double x0 = m->hx[d][pw], x1 = m->hx[d][pw + nodes - 1];
+        xs[d].resize(nodes_c + 2 * pw);
+        dxs[d].resize(nodes_c + 2 * pw - 1);
+        opflow_mesh_uniform(nodes_c, 0, pw, x0, x1, xs[d].data(), dxs[d].data());
+        out->dims[d] = nodes_c;
+        out->start[d] = 0;
+        out->x[d] = xs[d].data();
+        out->dx[d] = dxs[d].data();
+        out->pad_width = pw;
+    }
+    return true;
+}
+
+static void release_level_fields(LevelHost& L) {
+    for (auto f : L.owned) opflow_field_destroy(f);
+    L.owned.clear();
+}
+
+int mg_add_problem(MGSystem* S, opflow_field target, const opflow_node* nodes, int n_nodes, const opflow_field* leaves, int n_leaves,
+                   int unknown) {
+    opflow_ctx ctx = S->ctx;
+    OPG_TRY(ensure_scratch(ctx, 4096));
+    ProblemHost P;
+    P.target = target;
+    P.tree.assign(nodes, nodes + n_nodes);
+    P.leaves.assign(leaves, leaves + n_leaves);
+    P.unknown = unknown;
+    for (int d = 0; d < target->info.ndim; ++d)
+        if (target->desc.bc_type[d][0] == OPFLOW_BC_DIRC || target->desc.bc_type[d][1] == OPFLOW_BC_DIRC) P.has_dirichlet = true;
+    // level 0
+    LevelHost L0;
+    const Box box = assign_box(target->info);
+    const long long N0 = box.count();
+    if (N0 <= 0) return fail(OPFLOW_E_INVALID, "the target has no unknowns");
+    P.b = (double*) S->arena.alloc(N0 * sizeof(double));
+    if (!P.b) return fail(OPFLOW_E_NOMEM, "right-hand side");
+    OPG_TRY(assemble_level(S, target, P.tree, P.leaves, unknown, L0, P.b));
+    bool uniform_loc = true;
+    for (int d = 1; d < target->info.ndim; ++d) uniform_loc = uniform_loc && target->desc.loc[d] == target->desc.loc[0];
+    L0.node = target->desc.loc[0] == OPFLOW_CORNER;
+    P.levels.push_back(L0);
+    // singularity: zero row sums
+    {
+        unsigned long long* st = (unsigned long long*) ctx->scratch + 8;
+        cudaMemsetAsync(st, 0, 2 * sizeof(unsigned long long), ctx->stream);
+        const LevelHost& L = P.levels[0];
+        rowsum_stats<<<gridN(ctx, L.N), 256, 0, ctx->stream>>>(L.A64, L.N, L.n[0], L.n[1], L.n[2], L.ndim, L.per[0], L.per[1], L.per[2], st);
+        OPG_LAUNCHED();
+        unsigned long long h[2];
+        cudaMemcpyAsync(h, st, sizeof h, cudaMemcpyDeviceToHost, ctx->stream);
+        OPG_CUDA(cudaStreamSynchronize(ctx->stream));
+        double ms, md;
+        std::memcpy(&ms, &h[0], 8);
+        std::memcpy(&md, &h[1], 8);
+        P.singular = ms <= 1e-10 * md;
+    }
+    // coarser levels by rediscretisation
+    opflow_field cur_target = target;
+    std::vector<opflow_field> cur_leaves = P.leaves;
+    while (uniform_loc && (long long) P.levels.back().N > S->coarse_max && (int) P.levels.size() < 24) {
+        std::vector<std::vector<double>> xs, dxs;
+        opflow_mesh_desc cm;
+        if (!coarse_mesh(cur_target->mesh, cur_target->desc, xs, dxs, &cm)) break;
+        LevelHost Lc;
+        std::vector<opflow_field> nl(cur_leaves.size(), nullptr);
+        opflow_field ct = nullptr;
+        int rc = OPFLOW_OK;
+        for (size_t s = 0; s < cur_leaves.size() && rc == OPFLOW_OK; ++s) {
+            if (cur_leaves[s] == cur_target && ct) { nl[s] = ct; continue; }
+            opflow_field f = nullptr;
+            rc = opflow_field_create(ctx, &cm, &cur_leaves[s]->desc, &f);
+            if (rc) break;
+            Lc.owned.push_back(f);
+            nl[s] = f;
+            if (cur_leaves[s] == cur_target) ct = f;
+            else {
+                const Box cb = assign_box(f->info);
+                Box all = cb;
+                for (int d = 0; d < 3; ++d) { all.lo[d] = f->info.local[d][0]; all.hi[d] = f->info.local[d][1]; }
+                field_restrict<<<gridN(ctx, all.count()), 256, 0, ctx->stream>>>(cur_leaves[s]->view(), f->view(), all, f->desc.loc[0], f->desc.loc[1],
+                                                                                  f->desc.loc[2], f->info.ndim);
+                OPG_LAUNCHED();
+                rc = update_padding_buf(f, f->buf[f->cur]);
+            }
+        }
+        if (rc == OPFLOW_OK && !ct) rc = fail(OPFLOW_E_INVALID, "the target is not among the leaves");
+        if (rc == OPFLOW_OK) rc = assemble_level(S, ct, P.tree, nl, unknown, Lc, nullptr);
+        if (rc) {
+            release_level_fields(Lc);
+            for (auto& L : P.levels) release_level_fields(L);
+            return rc;
+        }
+        Lc.node = P.levels[0].node;
+        P.levels.push_back(Lc);
+        cur_target = ct;
+        cur_leaves = nl;
+    }
+    for (auto& L : P.levels) OPG_TRY(compress_level(S, L));
+    // coarsest: direct solve when small enough, else smoothing only
+    LevelHost& Lc = P.levels.back();
+    if (Lc.N <= std::max(S->coarse_max, 64)) OPG_TRY(coarse_inverse(S, Lc, P.singular && !P.has_dirichlet));
+    S->probs.push_back(std::move(P));
+    return OPFLOW_OK;
+}
+
+// Vectors, device descriptors and chunk lists for every problem added.
+int mg_finalize(MGSystem* S) {
+    opflow_ctx ctx = S->ctx;
+    const bool f32 = S->precision == OPFLOW_PREC_MIXED;
+    std::vector<LvlDev> lv;
+    std::vector<KrylovDev> kd;
+    S->nlevels = 0;
+    for (auto& P : S->probs) S->nlevels = std::max(S->nlevels, (int) P.levels.size());
+    S->smooth_ch.assign(S->nlevels, {});
+    S->restrict_ch.assign(S->nlevels, {});
+    S->prolong_ch.assign(S->nlevels, {});
+    std::vector<int> coarse_list;
+    std::vector<Chunk> k0;
+    std::vector<int> first, count;
+    const int CH = 1024;
+    auto rows = [&](int lvl_index, const LvlDev& L, std::vector<Chunk>& out) {
+        for (int k = 0; k < (L.ndim > 2 ? L.n[2] : 1); ++k)
+            for (int j = 0; j < (L.ndim > 1 ? L.n[1] : 1); ++j)
+                for (int i0 = 0; i0 < L.n[0]; i0 += CH) out.push_back(Chunk{lvl_index, j, k, i0, std::min(CH, L.n[0] - i0)});
+    };
+    for (size_t p = 0; p < S->probs.size(); ++p) {
+        ProblemHost& P = S->probs[p];
+        const int base = (int) lv.size();
+        for (size_t l = 0; l < P.levels.size(); ++l) {
+            LevelHost& H = P.levels[l];
+            LvlDev D{};
+            D.ndim = H.ndim;
+            for (int d = 0; d < 3; ++d) {
+                D.n[d] = d < H.ndim ? H.n[d] : 1;
+                D.lo[d] = d < H.ndim ? H.lo[d] : 0;
+                D.per[d] = H.per[d];
+                D.gh_lo[d] = H.gh_lo[d];
+                D.gh_hi[d] = H.gh_hi[d];
+            }
+            D.N = H.N;
+            D.node = H.node;
+            D.table = H.table;
+            bool odd_periodic = false;
+            for (int d = 0; d < H.ndim; ++d) odd_periodic = odd_periodic || (H.per[d] && (H.n[d] & 1));
+            D.rbgs = !odd_periodic;
+            D.problem = (int) p;
+            D.coarsest = l + 1 == P.levels.size();
+            D.nslot = 2 * H.ndim + 1;
+            D.A64 = H.A64;
+            D.A32 = H.A32;
+            D.T64 = H.T64;
+            D.T32 = H.T32;
+            D.coarse = D.coarsest ? -1 : base + (int) l + 1;
+            D.fine = l == 0 ? -1 : base + (int) l - 1;
+            D.Ainv64 = H.Ainv64;
+            const size_t N = (size_t) H.N;
+            if (f32) {
+                D.x32 = (float*) S->arena.alloc(N * 4);
+                D.b32 = (float*) S->arena.alloc(N * 4);
+                D.r32 = (float*) S->arena.alloc(N * 4);
+                if (!D.x32 || !D.b32 || !D.r32) return fail(OPFLOW_E_NOMEM, "level vectors");
+            } else {
+                D.x64 = (double*) S->arena.alloc(N * 8);
+                D.b64 = (double*) S->arena.alloc(N * 8);
+                D.r64 = (double*) S->arena.alloc(N * 8);
+                if (!D.x64 || !D.b64 || !D.r64) return fail(OPFLOW_E_NOMEM, "level vectors");
+            }
+            lv.push_back(D);
+            const int li = base + (int) l;
+            rows(li, D, S->smooth_ch[l]);
+            if (l > 0) rows(li, D, S->restrict_ch[l]);       // coarse rows of level l (restricted from l-1)
+            if (!D.coarsest) rows(li, D, S->prolong_ch[l]);  // fine rows of level l (prolonged from l+1)
+            if (D.coarsest && H.Ainv64) coarse_list.push_back(li);
+        }
+        KrylovDev K{};
+        const size_t N0 = (size_t) P.levels[0].N;
+        K.b = P.b;
+        K.x = (double*) S->arena.alloc(N0 * 8);
+        K.r = (double*) S->arena.alloc(N0 * 8);
+        K.z = (double*) S->arena.alloc(N0 * 8);
+        K.p = (double*) S->arena.alloc(N0 * 8);
+        K.q = (double*) S->arena.alloc(N0 * 8);
+        if (!K.x || !K.r || !K.z || !K.p || !K.q) return fail(OPFLOW_E_NOMEM, "Krylov vectors");
+        cudaMemsetAsync(K.x, 0, N0 * 8, ctx->stream);
+        K.lvl0 = base;
+        K.pin = -1;
+        kd.push_back(K);
+        P.lvl0 = base;
+        first.push_back((int) k0.size());
+        std::vector<Chunk> mine;
+        rows(base, lv[base], mine);
+        k0.insert(k0.end(), mine.begin(), mine.end());
+        count.push_back((int) mine.size());
+    }
+    S->nlv = (int) lv.size();
+    S->dL = (LvlDev*) S->arena.alloc(lv.size() * sizeof(LvlDev));
+    S->dK = (KrylovDev*) S->arena.alloc(kd.size() * sizeof(KrylovDev));
+    S->dS = (Scal*) S->arena.alloc(S->probs.size() * sizeof(Scal));
+    S->nk0 = (int) k0.size();
+    S->dk0 = (Chunk*) S->arena.alloc(std::max<size_t>(1, k0.size()) * sizeof(Chunk));
+    S->dfirst = (int*) S->arena.alloc(first.size() * sizeof(int));
+    S->dcount = (int*) S->arena.alloc(count.size() * sizeof(int));
+    S->partial = (double*) S->arena.alloc(std::max<size_t>(1, 2 * k0.size()) * sizeof(double));
+    S->red = (double*) S->arena.alloc(2 * S->probs.size() * sizeof(double));
+    S->dcoarse = (int*) S->arena.alloc(std::max<size_t>(1, coarse_list.size()) * sizeof(int));
+    S->d_active = (int*) S->arena.alloc(sizeof(int));
+    S->ncoarse = (int) coarse_list.size();
+    if (!S->dL || !S->dK || !S->dS || !S->dk0 || !S->partial || !S->red || !S->dcoarse) return fail(OPFLOW_E_NOMEM, "solver tables");
+    cudaMemcpyAsync(S->dL, lv.data(), lv.size() * sizeof(LvlDev), cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemcpyAsync(S->dK, kd.data(), kd.size() * sizeof(KrylovDev), cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemsetAsync(S->dS, 0, S->probs.size() * sizeof(Scal), ctx->stream);
+    if (!k0.empty()) cudaMemcpyAsync(S->dk0, k0.data(), k0.size() * sizeof(Chunk), cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemcpyAsync(S->dfirst, first.data(), first.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemcpyAsync(S->dcount, count.data(), count.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->stream);
+    if (!coarse_list.empty()) cudaMemcpyAsync(S->dcoarse, coarse_list.data(), coarse_list.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->stream);
+    auto upload = [&](std::vector<Chunk>& h, ChunkList& d) {
+        d.n = (int) h.size();
+        d.ptr = (Chunk*) S->arena.alloc(std::max<size_t>(1, h.size()) * sizeof(Chunk));
+        if (!h.empty()) cudaMemcpyAsync(d.ptr, h.data(), h.size() * sizeof(Chunk), cudaMemcpyHostToDevice, ctx->stream);
+    };
+    S->d_smooth.assign(S->nlevels, {});
+    S->d_restrict.assign(S->nlevels, {});
+    S->d_prolong.assign(S->nlevels, {});
+    for (int l = 0; l < S->nlevels; ++l) {
+        upload(S->smooth_ch[l], S->d_smooth[l]);
+        upload(S->restrict_ch[l], S->d_restrict[l]);
+        upload(S->prolong_ch[l], S->d_prolong[l]);
+    }
+    S->kd_host = kd;
+    if (!S->h_active) OPG_CUDA(cudaMallocHost(&S->h_active, sizeof(int)));
+    OPG_CUDA(cudaStreamSynchronize(ctx->stream));
+    return OPFLOW_OK;
+}
+
+// One V-cycle on the level-0 residuals of the active problems: z = M r.
+static int vcycle(MGSystem* S) {
+    cudaStream_t s = S->ctx->stream;
+    const int sms = S->ctx->num_sms;
+    const bool f32 = S->precision == OPFLOW_PREC_MIXED;
+    const Scal* sc = S->dS;
+    OPG_TRY(kr_launch_to_vcycle(s, sms, f32, S->dL, S->dK, S->dk0, S->nk0, sc));
+    for (int l = 0; l < S->nlevels; ++l) {
+        if (l > 0) OPG_TRY(mg_launch_restrict(s, sms, f32, S->dL, S->d_restrict[l].ptr, S->d_restrict[l].n, sc));
+        const ChunkList& C = S->d_smooth[l];
+        const bool last = l + 1 == S->nlevels;
+        // problems whose coarsest level is l with no dense inverse only smooth there (pre-smoothing)
+        for (int it = 0; it < S->pre; ++it) {
+            OPG_TRY(mg_launch_smooth(s, sms, f32, S->dL, C.ptr, C.n, 0, sc));
+            OPG_TRY(mg_launch_smooth(s, sms, f32, S->dL, C.ptr, C.n, 1, sc));
+        }
+        (void) last;
+        if (S->d_prolong[l].n) OPG_TRY(mg_launch_residual(s, sms, f32, S->dL, S->d_prolong[l].ptr, S->d_prolong[l].n, sc));
+    }
+    OPG_TRY(mg_launch_coarse(s, sms, f32, S->dL, S->dcoarse, S->ncoarse, sc));
+    for (int l = S->nlevels - 2; l >= 0; --l) {
+        OPG_TRY(mg_launch_prolong(s, sms, f32, S->dL, S->d_prolong[l].ptr, S->d_prolong[l].n, sc));
+        const ChunkList& C = S->d_smooth[l];
+        for (int it = 0; it < S->post; ++it) {
+            OPG_TRY(mg_launch_smooth(s, sms, f32, S->dL, C.ptr, C.n, 1, sc));
+            OPG_TRY(mg_launch_smooth(s, sms, f32, S->dL, C.ptr, C.n, 0, sc));
+        }
+    }
+    return OPFLOW_OK;
+}
+
+// One flexible-PCG iteration (everything after the first direction), recorded into a CUDA graph.
+static int iteration(MGSystem* S) {
+    cudaStream_t s = S->ctx->stream;
+    const int sms = S->ctx->num_sms;
+    const bool f32 = S->precision == OPFLOW_PREC_MIXED;
+    const int np = (int) S->probs.size();
+    OPG_TRY(kr_launch_apply(s, sms, S->dL, S->dK, S->dk0, S->nk0, S->dS, S->partial, 1));  // q = A p
+    OPG_TRY(kr_launch_reduce(s, sms, S->partial, S->dfirst, S->dcount, np, S->red));
+    OPG_TRY(kr_launch_scalars(s, S->dS, S->red, np, 1, S->tol, S->max_iter, 1));
+    OPG_TRY(kr_launch_update(s, sms, S->dL, S->dK, S->dk0, S->nk0, S->dS, S->partial));
+    OPG_TRY(kr_launch_reduce(s, sms, S->partial, S->dfirst, S->dcount, np, S->red));
+    OPG_TRY(kr_launch_scalars(s, S->dS, S->red, np, 2, S->tol, S->max_iter, 1));
+    OPG_TRY(vcycle(S));
+    OPG_TRY(kr_launch_from_vcycle(s, sms, f32, S->dL, S->dK, S->dk0, S->nk0, S->dS, S->partial));
+    OPG_TRY(kr_launch_reduce(s, sms, S->partial, S->dfirst, S->dcount, np, S->red));
+    OPG_TRY(kr_launch_scalars(s, S->dS, S->red, np, 3, S->tol, S->max_iter, 1));
+    OPG_TRY(kr_launch_pupdate(s, sms, S->dL, S->dK, S->dk0, S->nk0, S->dS, 0));
+    OPG_TRY(kr_launch_count(s, S->dS, np, S->d_active));
+    OPG_CUDA(cudaMemcpyAsync(S->h_active, S->d_active, sizeof(int), cudaMemcpyDeviceToHost, s));
+    return OPFLOW_OK;
+}
+
+int mg_solve(MGSystem* S) {
+    cudaStream_t s = S->ctx->stream;
+    const int sms = S->ctx->num_sms;
+    const bool f32 = S->precision == OPFLOW_PREC_MIXED;
+    const int np = (int) S->probs.size();
+    // r = b - A x; bb, rr -> active flags
+    OPG_TRY(kr_launch_apply(s, sms, S->dL, S->dK, S->dk0, S->nk0, nullptr, S->partial, 0));
+    OPG_TRY(kr_launch_reduce(s, sms, S->partial, S->dfirst, S->dcount, np, S->red));
+    OPG_TRY(kr_launch_scalars(s, S->dS, S->red, np, 0, S->tol, S->max_iter, 1));
+    OPG_TRY(vcycle(S));
+    OPG_TRY(kr_launch_from_vcycle(s, sms, f32, S->dL, S->dK, S->dk0, S->nk0, S->dS, S->partial));
+    OPG_TRY(kr_launch_reduce(s, sms, S->partial, S->dfirst, S->dcount, np, S->red));
+    OPG_TRY(kr_launch_scalars(s, S->dS, S->red, np, 4, S->tol, S->max_iter, 1));
+    OPG_TRY(kr_launch_pupdate(s, sms, S->dL, S->dK, S->dk0, S->nk0, S->dS, 1));
+    OPG_TRY(kr_launch_count(s, S->dS, np, S->d_active));
+    OPG_CUDA(cudaMemcpyAsync(S->h_active, S->d_active, sizeof(int), cudaMemcpyDeviceToHost, s));
+    OPG_CUDA(cudaStreamSynchronize(s));
+    if (!S->exec) {
+        // record one iteration as a CUDA graph, replayed until every problem has converged
+        cudaGraph_t g;
+        OPG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        int rc = iteration(S);
+        cudaError_t e = cudaStreamEndCapture(s, &g);
+        if (rc) return rc;
+        if (e != cudaSuccess) return fail(OPFLOW_E_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&S->exec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) { S->exec = nullptr; return fail(OPFLOW_E_CUDA, "graph instantiation failed: %s", cudaGetErrorString(e)); }
+    }
+    for (int it = 0; it < S->max_iter && *S->h_active > 0; ++it) {
+        OPG_CUDA(cudaGraphLaunch(S->exec, s));
+        S->graph_launches++;
+        OPG_CUDA(cudaStreamSynchronize(s));
+    }
+    return OPFLOW_OK;
+}
+
+int mg_states(MGSystem* S, std::vector<Scal>& out) {
+    out.resize(S->probs.size());
+    OPG_CUDA(cudaMemcpyAsync(out.data(), S->dS, out.size() * sizeof(Scal), cudaMemcpyDeviceToHost, S->ctx->stream));
+    OPG_CUDA(cudaStreamSynchronize(S->ctx->stream));
+    return OPFLOW_OK;
+}
+
+void mg_destroy(MGSystem* S) {
+    if (!S) return;
+    cudaStreamSynchronize(S->ctx->stream);
+    if (S->exec) cudaGraphExecDestroy(S->exec);
+    for (auto& P : S->probs)
+        for (auto& L : P.levels) release_level_fields(L);
+    S->arena.release();
+    if (S->h_active) cudaFreeHost(S->h_active);
+    delete S;
+}
+
+// ================================================================================= single-problem API
+static double sum_device(opflow_ctx ctx, const double* v, long long n) {
+    double* part = (double*) ctx->scratch + 64;
+    const int blocks = 256;
+    sum_partials<<<blocks, 256, 0, ctx->stream>>>(v, n, part);
+    OPG_LAUNCHED();
+    double h[256];
+    cudaMemcpyAsync(h, part, sizeof h, cudaMemcpyDeviceToHost, ctx->stream);
+    cudaStreamSynchronize(ctx->stream);
+    double s = 0.;
+    for (int i = 0; i < blocks; ++i) s += h[i];
+    return s;
+}
+
+}  // namespace opg
+
+using namespace opg;
+
+struct opflow_solver_s {
+    opflow_ctx ctx;
+    opflow_field target;
+    std::vector<opflow_node> tree;
+    std::vector<opflow_field> leaves;
+    int unknown;
+    opflow_solve_params params;
+    MGSystem* S = nullptr;
+    bool first = true;
+};
+
+static int build_system(opflow_solver s) {
+    if (s->S) mg_destroy(s->S);
+    s->S = new MGSystem();
+    s->S->ctx = s->ctx;
+    s->S->precision = s->params.precision;
+    s->S->pre = s->params.pre_sweeps;
+    s->S->post = s->params.post_sweeps;
+    s->S->coarse_max = s->params.coarse_max;
+    s->S->tol = s->params.tol;
+    s->S->max_iter = s->params.max_iter;
+    OPG_TRY(mg_add_problem(s->S, s->target, s->tree.data(), (int) s->tree.size(), s->leaves.data(), (int) s->leaves.size(), s->unknown));
+    return mg_finalize(s->S);
+}
+
+extern "C" {
+
+void opflow_solve_params_default(opflow_solve_params* p) {
+    if (!p) return;
+    p->tol = 1e-10;
+    p->max_iter = 200;
+    p->static_mat = 0;
+    p->pin_value = 0;
+    p->precision = OPFLOW_PREC_FP64;
+    p->pre_sweeps = 2;
+    p->post_sweeps = 2;
+    p->coarse_max = 256;
+    p->zero_guess = 0;
+}
+
+int opflow_solver_create(opflow_ctx ctx, opflow_field target, const opflow_node* nodes, int n_nodes, const opflow_field* leaves, int n_leaves,
+                         int unknown_slot, const opflow_solve_params* params, opflow_solver* out) {
+    if (!ctx || !target || !nodes || !leaves || !out) return fail(OPFLOW_E_INVALID, "null argument");
+    opflow_solve_params p;
+    if (params) p = *params;
+    else opflow_solve_params_default(&p);
+    if (!(p.tol > 0) || p.max_iter < 0 || p.pre_sweeps < 0 || p.post_sweeps < 0) return fail(OPFLOW_E_INVALID, "bad solver parameters");
+    if (p.precision != OPFLOW_PREC_FP64 && p.precision != OPFLOW_PREC_MIXED) return fail(OPFLOW_E_INVALID, "bad precision");
+    if (p.coarse_max <= 0) p.coarse_max = 256;
+    auto* s = new opflow_solver_s();
+    s->ctx = ctx;
+    s->target = target;
+    s->tree.assign(nodes, nodes + n_nodes);
+    s->leaves.assign(leaves, leaves + n_leaves);
+    s->unknown = unknown_slot;
+    s->params = p;
+    int rc = build_system(s);
+    if (rc) {
+        if (s->S) mg_destroy(s->S);
+        delete s;
+        return rc;
+    }
+    *out = s;
+    return OPFLOW_OK;
+}
+
+int opflow_solver_solve(opflow_solver s, opflow_solve_state* state) {
+    if (!s) return fail(OPFLOW_E_INVALID, "null solver");
+    using clk = std::chrono::steady_clock;
+    auto t0 = clk::now();
+    opflow_ctx ctx = s->ctx;
+    // generateAb on every solve, generateb only when staticMat (HYPREEqnSolveHandler.hpp:190-209)
+    if (!s->first) {
+        if (s->params.static_mat) {
+            AsmPlan plan;
+            OPG_TRY(asm_prepare(ctx, s->target, s->tree.data(), (int) s->tree.size(), s->leaves.data(), (int) s->leaves.size(), s->unknown, 0,
+                                &plan));
+            double* coef = nullptr;
+            OPG_CUDA(cudaMalloc(&coef, (size_t) plan.cells * plan.P.nk * sizeof(double)));
+            int rc = asm_run(ctx, &plan, coef, s->S->probs[0].b);
+            cudaFree(coef);
+            OPG_TRY(rc);
+        } else {
+            OPG_TRY(build_system(s));
+        }
+    }
+    s->first = false;
+    MGSystem* S = s->S;
+    ProblemHost& P = S->probs[0];
+    const KrylovDev& K = S->kd_host[0];
+    const long long N = P.levels[0].N;
+    const Box box = assign_box(s->target->info);
+    // initial guess: the target's current values (initx)
+    if (s->params.zero_guess) cudaMemsetAsync(K.x, 0, N * 8, ctx->stream);
+    else {
+        gather_box<<<gridN(ctx, N), 256, 0, ctx->stream>>>(s->target->view(), box, K.x);
+        OPG_LAUNCHED();
+    }
+    const bool pinned = P.singular && !P.has_dirichlet && s->params.pin_value;
+    double b_pin = 0.;
+    if (P.singular && !P.has_dirichlet) {
+        const double sb = sum_device(ctx, P.b, N);
+        if (pinned) {
+            // the pinned system equals the singular one with b[0] := -(sum of the others), shifted
+            OPG_CUDA(cudaMemcpy(&b_pin, P.b, 8, cudaMemcpyDeviceToHost));
+            const double nb0 = -(sb - b_pin);
+            OPG_CUDA(cudaMemcpy(P.b, &nb0, 8, cudaMemcpyHostToDevice));
+        } else {
+            add_scalar<<<gridN(ctx, N), 256, 0, ctx->stream>>>(P.b, N, -sb / (double) N);
+            OPG_LAUNCHED();
+        }
+    }
+    auto t1 = clk::now();
+    OPG_TRY(mg_solve(S));
+    std::vector<Scal> st;
+    OPG_TRY(mg_states(S, st));
+    double shift = 0.;
+    if (pinned) {
+        OPG_CUDA(cudaMemcpy(&shift, K.x, 8, cudaMemcpyDeviceToHost));
+        OPG_CUDA(cudaMemcpy(P.b, &b_pin, 8, cudaMemcpyHostToDevice));  // back to the reference's b (pinned row 0 -> 0 below)
+        const double zero = 0.;
+        OPG_CUDA(cudaMemcpy(P.b, &zero, 8, cudaMemcpyHostToDevice));
+        add_scalar<<<gridN(ctx, N), 256, 0, ctx->stream>>>(K.x, N, -shift);
+        OPG_LAUNCHED();
+    }
+    // true residual of the reference's system
+    OPG_TRY(kr_launch_apply(ctx->stream, ctx->num_sms, S->dL, S->dK, S->dk0, S->nk0, nullptr, S->partial, 0));
+    OPG_TRY(kr_launch_reduce(ctx->stream, ctx->num_sms, S->partial, S->dfirst, S->dcount, 1, S->red));
+    double red[2];
+    OPG_CUDA(cudaMemcpyAsync(red, S->red, sizeof red, cudaMemcpyDeviceToHost, ctx->stream));
+    double r0 = 0.;
+    if (pinned) OPG_CUDA(cudaMemcpyAsync(&r0, K.r, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    OPG_CUDA(cudaStreamSynchronize(ctx->stream));
+    double rr = red[1] - (pinned ? r0 * r0 : 0.), bb = red[0];
+    if (rr < 0) rr = 0;
+    scatter_box<<<gridN(ctx, N), 256, 0, ctx->stream>>>(s->target->view(), box, K.x, 0.);
+    OPG_LAUNCHED();
+    s->target->bc_fresh[s->target->cur] = false;
+    OPG_TRY(update_padding_buf(s->target, s->target->buf[s->target->cur]));
+    OPG_CUDA(cudaStreamSynchronize(ctx->stream));
+    auto t2 = clk::now();
+    if (state) {
+        state->iterations = st[0].iters;
+        state->abs_residual = std::sqrt(rr);
+        state->rel_residual = bb > 0 ? std::sqrt(rr / bb) : std::sqrt(rr);
+        state->converged = state->rel_residual <= s->params.tol;
+        state->setup_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+        state->solve_ms = std::chrono::duration<double, std::milli>(t2 - t1).count();
+    }
+    if (state && !state->converged && st[0].iters >= s->params.max_iter)
+        return fail(OPFLOW_E_NOT_CONVERGED, "not converged after %d iterations (relative residual %g)", st[0].iters, state->rel_residual);
+    return OPFLOW_OK;
+}
+
+int opflow_solver_destroy(opflow_solver s) {
+    if (!s) return OPFLOW_OK;
+    mg_destroy(s->S);
+    delete s;
+    return OPFLOW_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,270 @@
+// Tiled stencil kernels for the axis-aligned (2*D+1)-point updates of path E.
+//
+// 3D: a CTA owns a 32x8 column of the xy plane and marches along z through a chunk of planes.  The
+// z-1 / z / z+1 values of its own column stay in registers; the plane z (with a one-cell halo) is staged
+// in shared memory, so every grid value is read from HBM once per step (8 B read + 8 B written per
+// lattice update).  2D: a CTA owns 128 x-points and marches along y.
+//
+// Two arithmetic modes share the tiling:
+//   EXACT - the reference's IEEE operations per point (D2SecondOrderCentered::eval,
+//           D2SecondOrderCentered.hpp:160-171, summed in tree order, then u + s*sum);
+//   FAST  - exact 64-bit fixed point: values are converted once when staged, the second differences
+//           are exact integer sums, one 64x53-bit product per weight group, one rounding back.
+#include "stencil.h"
+
+namespace opg {
+
+__device__ __forceinline__ double ld3(const FieldView& f, int i, int j, int k) {
+    return f.data[(long long) (i - f.off[0]) + (long long) (j - f.off[1]) * f.sy + (long long) (k - f.off[2]) * f.sz];
+}
+
+// correctly rounded x / h: exact multiply for a power-of-two h, else Markstein's three operations
+__device__ __forceinline__ double tdiv(double x, double h, double y, int p2) {
+    if (p2) return __dmul_rn(x, y);
+    const double q = __dmul_rn(x, y);
+    const double r = __fma_rn(-q, h, x);
+    return __fma_rn(r, y, q);
+}
+
+__device__ __forceinline__ double d2_exact(double l, double c, double r, double h, double y, int p2) {
+    const double a = tdiv(__dsub_rn(r, c), h, y, p2);
+    const double b = tdiv(__dsub_rn(c, l), h, y, p2);
+    return tdiv(__dsub_rn(a, b), h, y, p2);
+}
+
+__device__ __forceinline__ long long fx_from(double x, int E) {
+    const unsigned long long b = (unsigned long long) __double_as_longlong(x);
+    const int e = (int) ((b >> 52) & 0x7FF);
+    unsigned long long m = b & 0xFFFFFFFFFFFFFull;
+    int ex;
+    if (e == 0) ex = 1 - 1075;
+    else { m |= 1ull << 52; ex = e - 1075; }
+    const int sh = ex + 58 - E;
+    unsigned long long q;
+    if (sh >= 0) q = m << sh;
+    else if (sh > -64) q = (m + (1ull << (-sh - 1))) >> (-sh);
+    else q = 0;
+    return (b >> 63) ? -(long long) q : (long long) q;
+}
+
+__device__ __forceinline__ double fx_to(long long q, int E) {
+    if (q == 0) return 0.0;
+    const unsigned long long sign = q < 0 ? 1ull : 0ull;
+    const unsigned long long a = q < 0 ? (unsigned long long) (-q) : (unsigned long long) q;
+    const int bl = 64 - __clzll((long long) a);
+    unsigned long long mant;
+    int exp2 = bl - 1 + E - 58;
+    if (bl <= 53) {
+        mant = a << (53 - bl);
+    } else {
+        const int sh = bl - 53;
+        mant = a >> sh;
+        const unsigned long long rem = a & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+        if (rem > half || (rem == half && (mant & 1ull))) {
+            mant++;
+            if (mant == (1ull << 53)) { mant >>= 1; exp2++; }
+        }
+    }
+    return __longlong_as_double((long long) ((sign << 63) | ((unsigned long long) (exp2 + 1023) << 52) | (mant & 0xFFFFFFFFFFFFFull)));
+}
+
+__device__ __forceinline__ long long fx_mul(long long z, unsigned long long w, int sh, int neg) {
+    const bool zn = z < 0;
+    const unsigned long long a = zn ? (unsigned long long) (-z) : (unsigned long long) z;
+    const unsigned long long lo = a * w, hi = __umul64hi(a, w);
+    unsigned long long r;
+    if (sh >= 64) r = hi >> (sh - 64);
+    else if (sh == 0) r = lo;
+    else {
+        const unsigned long long lo2 = lo + (1ull << (sh - 1));
+        const unsigned long long hi2 = hi + (lo2 < lo ? 1ull : 0ull);
+        r = (lo2 >> sh) | (hi2 << (64 - sh));
+    }
+    return (zn != (neg != 0)) ? -(long long) r : (long long) r;
+}
+
+__device__ __forceinline__ int scale_exp(const unsigned long long* maxslots, int step, unsigned long long bound_bits) {
+    unsigned long long m = maxslots[step % 3];
+    if (bound_bits > m) m = bound_bits;
+    if (m == 0) return -1000;
+    return (int) ((m >> 52) & 0x7FF) - 1023 + 1;
+}
+
+__device__ __forceinline__ void block_max_commit(unsigned long long v, unsigned long long* slot) {
+    for (int s = 16; s > 0; s >>= 1) {
+        const unsigned long long o = __shfl_xor_sync(0xffffffffu, v, s);
+        v = o > v ? o : v;
+    }
+    if ((threadIdx.x & 31) == 0 && v) atomicMax(slot, v);
+}
+
+// ------------------------------------------------------------------------------------------------ 3D
+constexpr int TX = 32, TY = 8;
+
+template <bool FAST>
+__global__ void __launch_bounds__(TX * TY) axis3d_kernel(FieldView in, FieldView out, Box box, AxisParams P, unsigned long long* maxslots,
+                                                          int step, int zchunk) {
+    using T = typename std::conditional<FAST, long long, double>::type;
+    __shared__ T tile[TY + 2][TX + 2];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int x0 = box.lo[0] + blockIdx.x * TX, y0 = box.lo[1] + blockIdx.y * TY;
+    const int i = x0 + tx, j = y0 + ty;
+    const bool valid = i < box.hi[0] && j < box.hi[1];
+    const int ic = min(i, box.hi[0]), jc = min(j, box.hi[1]);
+    const int zs = box.lo[2] + blockIdx.z * zchunk;
+    const int ze = min(zs + zchunk, box.hi[2]);
+    if (zs >= ze) return;
+    int E = 0;
+    if (FAST) {
+        E = scale_exp(maxslots, step, P.bound_bits);
+        if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && tx == 0 && ty == 0) maxslots[(step + 2) % 3] = 0ull;
+    }
+    auto conv = [&](double v) -> T {
+        if constexpr (FAST) return fx_from(v, E);
+        else return v;
+    };
+    T below = conv(ld3(in, ic, jc, zs - 1));
+    T cur = conv(ld3(in, ic, jc, zs));
+    unsigned long long vmax = 0;
+    for (int k = zs; k < ze; ++k) {
+        const T above = conv(ld3(in, ic, jc, k + 1));
+        tile[ty + 1][tx + 1] = cur;
+        if (tx == 0) tile[ty + 1][0] = conv(ld3(in, x0 - 1, jc, k));
+        if (tx == TX - 1) tile[ty + 1][TX + 1] = conv(ld3(in, min(x0 + TX, box.hi[0]), jc, k));
+        if (ty == 0) tile[0][tx + 1] = conv(ld3(in, ic, y0 - 1, k));
+        if (ty == TY - 1) tile[TY + 1][tx + 1] = conv(ld3(in, ic, min(y0 + TY, box.hi[1]), k));
+        __syncthreads();
+        if (valid) {
+            const T l = tile[ty + 1][tx], r = tile[ty + 1][tx + 2];
+            const T b = tile[ty][tx + 1], t = tile[ty + 2][tx + 1];
+            double v;
+            if constexpr (FAST) {
+                long long q = cur;
+                if (P.iso) {
+                    const long long z = (l - cur) + (r - cur) + (b - cur) + (t - cur) + (below - cur) + (above - cur);
+                    q += fx_mul(z, P.wm[0], P.wshift[0], P.wneg[0]);
+                } else {
+                    q += fx_mul((l - cur) + (r - cur), P.wm[0], P.wshift[0], P.wneg[0]);
+                    q += fx_mul((b - cur) + (t - cur), P.wm[1], P.wshift[1], P.wneg[1]);
+                    q += fx_mul((below - cur) + (above - cur), P.wm[2], P.wshift[2], P.wneg[2]);
+                }
+                v = fx_to(q, E);
+                const unsigned long long ab = (unsigned long long) __double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
+                vmax = ab > vmax ? ab : vmax;
+            } else {
+                double d2v[3];
+                d2v[0] = d2_exact(l, cur, r, P.h[0], P.inv_h[0], P.pow2[0]);
+                d2v[1] = d2_exact(b, cur, t, P.h[1], P.inv_h[1], P.pow2[1]);
+                d2v[2] = d2_exact(below, cur, above, P.h[2], P.inv_h[2], P.pow2[2]);
+                double sum = d2v[P.order[0]];
+                sum = __dadd_rn(sum, d2v[P.order[1]]);
+                sum = __dadd_rn(sum, d2v[P.order[2]]);
+                v = __dadd_rn(cur, __dmul_rn(P.s, sum));
+            }
+            out.data[(long long) (i - out.off[0]) + (long long) (j - out.off[1]) * out.sy + (long long) (k - out.off[2]) * out.sz] = v;
+        }
+        __syncthreads();
+        below = cur;
+        cur = above;
+    }
+    if (FAST) block_max_commit(vmax, &maxslots[(step + 1) % 3]);
+}
+
+// ------------------------------------------------------------------------------------------------ 2D
+constexpr int TX2 = 128;
+
+template <bool FAST>
+__global__ void __launch_bounds__(TX2) axis2d_kernel(FieldView in, FieldView out, Box box, AxisParams P, unsigned long long* maxslots, int step,
+                                                     int ychunk) {
+    using T = typename std::conditional<FAST, long long, double>::type;
+    __shared__ T row[TX2 + 2];
+    const int tx = threadIdx.x;
+    const int x0 = box.lo[0] + blockIdx.x * TX2;
+    const int i = x0 + tx;
+    const bool vx = i < box.hi[0];
+    const int ic = min(i, box.hi[0]);
+    const int ys = box.lo[1] + blockIdx.y * ychunk;
+    const int ye = min(ys + ychunk, box.hi[1]);
+    if (ys >= ye) return;
+    int E = 0;
+    if (FAST) {
+        E = scale_exp(maxslots, step, P.bound_bits);
+        if (blockIdx.x == 0 && blockIdx.y == 0 && tx == 0) maxslots[(step + 2) % 3] = 0ull;
+    }
+    auto conv = [&](double v) -> T {
+        if constexpr (FAST) return fx_from(v, E);
+        else return v;
+    };
+    const int k = box.lo[2];
+    T below = conv(ld3(in, ic, ys - 1, k));
+    T cur = conv(ld3(in, ic, ys, k));
+    unsigned long long vmax = 0;
+    for (int j = ys; j < ye; ++j) {
+        const T above = conv(ld3(in, ic, j + 1, k));
+        row[tx + 1] = cur;
+        if (tx == 0) row[0] = conv(ld3(in, x0 - 1, j, k));
+        if (tx == TX2 - 1) row[TX2 + 1] = conv(ld3(in, min(x0 + TX2, box.hi[0]), j, k));
+        __syncthreads();
+        if (vx) {
+            const T l = row[tx], r = row[tx + 2];
+            double v;
+            if constexpr (FAST) {
+                long long q = cur;
+                if (P.iso) {
+                    q += fx_mul((l - cur) + (r - cur) + (below - cur) + (above - cur), P.wm[0], P.wshift[0], P.wneg[0]);
+                } else {
+                    q += fx_mul((l - cur) + (r - cur), P.wm[0], P.wshift[0], P.wneg[0]);
+                    q += fx_mul((below - cur) + (above - cur), P.wm[1], P.wshift[1], P.wneg[1]);
+                }
+                v = fx_to(q, E);
+                const unsigned long long ab = (unsigned long long) __double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
+                vmax = ab > vmax ? ab : vmax;
+            } else {
+                double d2v[2];
+                d2v[0] = d2_exact(l, cur, r, P.h[0], P.inv_h[0], P.pow2[0]);
+                d2v[1] = d2_exact(below, cur, above, P.h[1], P.inv_h[1], P.pow2[1]);
+                double sum = __dadd_rn(d2v[P.order[0]], d2v[P.order[1]]);
+                v = __dadd_rn(cur, __dmul_rn(P.s, sum));
+            }
+            out.data[(long long) (i - out.off[0]) + (long long) (j - out.off[1]) * out.sy + (long long) (k - out.off[2]) * out.sz] = v;
+        }
+        __syncthreads();
+        below = cur;
+        cur = above;
+    }
+    if (FAST) block_max_commit(vmax, &maxslots[(step + 1) % 3]);
+}
+
+int axis_launch(opflow_ctx ctx, const FieldView& in, const FieldView& out, const Box& box, const AxisParams& P, bool fast,
+                unsigned long long* maxslots, int step) {
+    const int nx = box.hi[0] - box.lo[0], ny = box.hi[1] - box.lo[1], nz = box.hi[2] - box.lo[2];
+    if (nx <= 0 || ny <= 0 || nz <= 0) return OPFLOW_OK;
+    if (P.ndim == 3) {
+        const int bx = (nx + TX - 1) / TX, by = (ny + TY - 1) / TY;
+        // enough CTAs for ~8 per SM, each marching at least 16 planes
+        int zchunks = (ctx->num_sms * 8 + bx * by - 1) / (bx * by);
+        zchunks = std::max(1, std::min(zchunks, (nz + 15) / 16));
+        const int zchunk = (nz + zchunks - 1) / zchunks;
+        zchunks = (nz + zchunk - 1) / zchunk;
+        dim3 g(bx, by, zchunks), b(TX, TY);
+        if (fast) axis3d_kernel<true><<<g, b, 0, ctx->stream>>>(in, out, box, P, maxslots, step, zchunk);
+        else axis3d_kernel<false><<<g, b, 0, ctx->stream>>>(in, out, box, P, maxslots, step, zchunk);
+        OPG_LAUNCHED();
+        return check_launch("axis3d_kernel");
+    }
+    if (P.ndim == 2) {
+        const int bx = (nx + TX2 - 1) / TX2;
+        int ychunks = (ctx->num_sms * 8 + bx - 1) / bx;
+        ychunks = std::max(1, std::min(ychunks, (ny + 7) / 8));
+        const int ychunk = (ny + ychunks - 1) / ychunks;
+        ychunks = (ny + ychunk - 1) / ychunk;
+        dim3 g(bx, ychunks), b(TX2);
+        if (fast) axis2d_kernel<true><<<g, b, 0, ctx->stream>>>(in, out, box, P, maxslots, step, ychunk);
+        else axis2d_kernel<false><<<g, b, 0, ctx->stream>>>(in, out, box, P, maxslots, step, ychunk);
+        OPG_LAUNCHED();
+        return check_launch("axis2d_kernel");
+    }
+    return fail(OPFLOW_E_UNSUPPORTED, "tiled stencil kernels cover 2D and 3D grids");
+}
+
+}  // namespace opg

@@ -1,0 +1,26 @@
+// Tiled axis-stencil kernels (u_out = f(u at i, i +- e_d)) shared by the expression lowering.
+#pragma once
+#include "internal.h"
+
+#include <type_traits>
+
+namespace opg {
+
+struct AxisParams {
+    int ndim;
+    // EXACT: u + s * (d2<order[0]> + d2<order[1]> [+ d2<order[2]>]) with spacing h per dim
+    double h[3], inv_h[3];
+    int pow2[3];
+    int order[3];
+    double s;
+    // FAST: u + sum_d w_d * ((u(i-e_d) - u) + (u(i+e_d) - u)) in fixed point
+    int iso;                     // one weight for every dim (w[0])
+    unsigned long long wm[3];    // weight mantissas
+    int wshift[3], wneg[3];
+    unsigned long long bound_bits;
+};
+
+int axis_launch(opflow_ctx ctx, const FieldView& in, const FieldView& out, const Box& box, const AxisParams& P, bool fast,
+                unsigned long long* maxslots, int step);
+
+}  // namespace opg

@@ -21,7 +21,19 @@
 #include <stdlib.h>
 #include <string.h>
 
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 #define MAXD 3
+int or_set_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+    return omp_get_max_threads();
+#else
+    (void) n;
+    return 1;
+#endif
+}
 static char g_err[512];
 const char* or_last_error(void) { return g_err; }
 static int fail(int code, const char* msg) {
@@ -434,6 +446,19 @@ static int setup_ctx(Ctx* c, const opflow_mesh_desc* m, const opflow_field_desc*
     return compute_locs(c);
 }
 
+/* dst[i] = expr(i) over a box; rows are independent, so the outer loop may run on several host threads
+ * (the values do not depend on the thread count). */
+static void eval_box(Ctx* c, int D, const int* lo, const int* hi, Field* dst) {
+    const int outer = D == 3 ? 2 : (D == 2 ? 1 : 0);
+#pragma omp parallel for schedule(static)
+    for (int o = lo[outer]; o < hi[outer]; ++o) {
+        int l2[3] = {lo[0], lo[1], lo[2]}, h2[3] = {hi[0], hi[1], hi[2]}, idx[3];
+        l2[outer] = o;
+        h2[outer] = o + 1;
+        BOX_FOR(D, l2, h2, idx) fset(dst, idx, ev(c, c->n - 1, idx));
+    }
+}
+
 /* internal::FieldAssigner::assign<Op> (FieldAssigner.hpp:27-84) followed by the updatePadding of
  * CartesianField::assignImpl_final (CartesianField.hpp:195-234).  `dst` is a slot of `datas`; when the
  * expression reads it, the evaluation goes to a temporary copy first, as the reference does. */
@@ -462,7 +487,7 @@ int or_assign(const opflow_mesh_desc* m, const opflow_field_desc* descs, double*
         memcpy(tmp, out->data, R->count * sizeof(double));
         Field t = *out;
         t.data = tmp;
-        BOX_FOR(R->ndim, lo, hi, idx) fset(&t, idx, ev(&c, n - 1, idx));
+        eval_box(&c, R->ndim, lo, hi, &t);
         update_padding(m, &t);
         BOX_FOR(R->ndim, lo, hi, idx) {
             double v = fget(&t, idx), o = fget(out, idx);
@@ -476,6 +501,8 @@ int or_assign(const opflow_mesh_desc* m, const opflow_field_desc* descs, double*
             fset(out, idx, o);
         }
         free(tmp);
+    } else if (arith == OPFLOW_ASSIGN_EQ) {
+        eval_box(&c, R->ndim, lo, hi, out);
     } else {
         BOX_FOR(R->ndim, lo, hi, idx) {
             double v = ev(&c, n - 1, idx), o = fget(out, idx);

@@ -39,6 +39,8 @@ def lib():
         L.or_u01.argtypes = [C.c_uint64, C.c_uint64]
         L.or_u01.restype = C.c_double
         L.or_last_error.restype = C.c_char_p
+        L.or_set_threads.argtypes = [C.c_int]
+        L.or_set_threads.restype = C.c_int
         _lib = L
     return _lib
 

@@ -1,0 +1,185 @@
+"""Path E on the GPU: the CUDA kernels against the reference's dumps (bit-exact) and the oracle."""
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+
+import common as cm
+import oracle_lib as orc
+from opflow_gb300 import _capi as capi
+from opflow_gb300 import api
+
+pytestmark = pytest.mark.gpu
+
+
+def gpu_field(ctx, mesh, fd, host=None):
+    f = api.CartesianField(mesh, fd, ctx)
+    if host is not None:
+        f.upload(host.data, update_padding=False)
+    return f
+
+
+def readable_of(f):
+    return f.download()[f.index_slices(cm.readable(f.info))].reshape(-1)
+
+
+@pytest.mark.parametrize("name", ["ftcs2d_n17", "ftcs2d_n33_bc1", "ftcs2d_n20_nonpow2", "ftcs2d_n65"])
+def test_ftcs2d_gpu_matches_reference_dump(ctx, name):
+    meta, arr = cm.golden(name)
+    _, n, steps, seed, bcv, cfl = meta["args"]
+    n, steps, seed, bcv, cfl = int(n), int(steps), int(seed), float(bcv), float(cfl)
+    mesh = cm.mesh_uniform([n, n])
+    fd = cm.field_desc(2, capi.CORNER, [(capi.BC_DIRC, capi.BC_DIRC)] * 2, [(bcv, bcv)] * 2)
+    h0 = orc.HostField(mesh, fd)
+    cm.seeded_interior(h0, seed, n)
+    h0.update_padding()
+    u = gpu_field(ctx, mesh, fd, h0)
+    h = 1.0 / (n - 1)
+    u.assign(cm.ftcs_expr(u, cfl * h * h * 1.0, 2), steps=steps)
+    got = readable_of(u)
+    assert np.array_equal(got, arr["u__data"]), np.abs(got - arr["u__data"]).max()
+
+
+@pytest.mark.parametrize("name", ["ftcs3d_n9", "ftcs3d_n12_nonpow2"])
+def test_ftcs3d_gpu_matches_reference_dump(ctx, name):
+    meta, arr = cm.golden(name)
+    _, n, steps, seed, cfl = meta["args"]
+    n, steps, cfl = int(n), int(steps), float(cfl)
+    mesh = cm.mesh_uniform([n, n, n])
+    fd = cm.field_desc(3, capi.CORNER, [(capi.BC_DIRC, capi.BC_DIRC)] * 3)
+    u = gpu_field(ctx, mesh, fd, orc.HostField(mesh, fd, data=arr["u0__data"]))
+    h = 1.0 / (n - 1)
+    u.assign(cm.ftcs_expr(u, cfl * h * h * 1.0, 3), steps=steps)
+    assert np.array_equal(u.download().reshape(-1), arr["u__data"])
+
+
+@pytest.mark.parametrize("name", ["weno_down_32x4", "weno_up_64x3", "weno_down_40x2_nonpow2"])
+def test_weno_rk3_gpu_interpreter_matches_reference_dump(ctx, name):
+    meta, arr = cm.golden(name)
+    _, nx, ny, steps, seed, up = meta["args"]
+    nx, ny, steps, up = int(nx), int(ny), int(steps), int(up)
+    mesh = cm.mesh_uniform([nx + 1, ny + 1])
+    fd = cm.field_desc(2, capi.CENTER, [(capi.BC_PERIODIC, capi.BC_PERIODIC)] * 2, ext=3)
+    h0 = orc.HostField(mesh, fd, data=arr["u0__data"])
+    u, u1, u2 = (gpu_field(ctx, mesh, fd, h0) for _ in range(3))
+    dt = 0.5 * (1.0 / nx)
+    e1, e2, e3 = cm.weno_stage_exprs(u, u1, u2, dt, upwind=bool(up))
+    for _ in range(steps):
+        u1.assign(e1)
+        u2.assign(e2)
+        u.assign(e3)
+    assert np.array_equal(u.download().reshape(-1), arr["u__data"])
+
+
+PAD = sorted(f[:-4] for f in os.listdir(cm.GOLDEN) if f.startswith("pad_"))
+
+
+@pytest.mark.parametrize("name", PAD)
+def test_padding_gpu_matches_reference_dump(ctx, name):
+    meta, arr = cm.golden(name)
+    _, nx, ny, loc, lo, hi, ext = meta["args"]
+    nx, ny, loc, lo, hi, ext = map(int, (nx, ny, loc, lo, hi, ext))
+    code = [capi.BC_DIRC, capi.BC_NEUM, capi.BC_PERIODIC, capi.BC_SYMM, capi.BC_ASYMM]
+    mesh = cm.mesh_uniform([nx, ny], [(0.0, 1.0), (0.0, 2.0)])
+    fd = cm.field_desc(2, capi.CENTER if loc else capi.CORNER, [(code[lo], code[hi]), (code[hi], code[lo])],
+                       [(0.25, -0.5), (0.75, 1.5)], ext=ext)
+    f = api.CartesianField(mesh, fd, ctx)
+    f.initBy(lambda X: 1.0 + X[0] * X[0] - 0.5 * X[1] + 0.25 * X[0] * X[1])
+    assert np.array_equal(readable_of(f), arr["f__data"])
+
+
+def _vc_case(ctx, n, seed):
+    mesh = cm.mesh_uniform([n + 1, n + 1])
+    fd = cm.field_desc(2, capi.CENTER, [(capi.BC_DIRC, capi.BC_NEUM), (capi.BC_SYMM, capi.BC_DIRC)], [(0.5, -1.0), (0.0, 2.0)], ext=1)
+    hosts = []
+    for s in range(3):
+        hf = orc.HostField(mesh, fd)
+        rng = hf.assignable()
+        j, i = np.meshgrid(np.arange(*rng[1]), np.arange(*rng[0]), indexing="ij")
+        hf.data[hf.slices(rng)] = 0.5 + orc.u01(seed + s, j.astype(np.uint64) * np.uint64(977) + i.astype(np.uint64))
+        hf.update_padding()
+        hosts.append(hf)
+    return mesh, fd, hosts
+
+
+def test_generic_interpreter_matches_oracle(ctx):
+    """Flux-form variable-coefficient operator, first-order centred derivatives, linear interpolation,
+    negation and division on a mixed-BC cell-centred field: the generic kernel vs the oracle."""
+    mesh, fd, hosts = _vc_case(ctx, 24, 3)
+    g = [gpu_field(ctx, mesh, fd, h) for h in hosts]
+    L = [cm.Leaf(k) for k in "uvr"]
+
+    def expr(u, v, r):
+        return (api.dx(api.dx(u) / api.d1IntpCenterToCorner(r, 0)) + api.dy(api.dy(u) / api.d1IntpCenterToCorner(r, 1))
+                - (-v) / (u + 2.0) * 0.3)
+
+    nodes, _ = api.serialize(expr(*L), L)
+    out_h = orc.HostField(mesh, fd)
+    orc.assign(out_h, nodes, hosts + [out_h])
+    out = api.CartesianField(mesh, fd, ctx)
+    out.assign(expr(*g))
+    assert np.array_equal(readable_of(out), out_h.data[out_h.slices(cm.readable(out_h.info))].reshape(-1))
+
+
+def test_aliased_incremental_assign_matches_oracle(ctx):
+    """u += d2x(u) * v reads u while writing it: FieldAssigner's out-of-place semantics."""
+    mesh, fd, hosts = _vc_case(ctx, 20, 11)
+    u, v = gpu_field(ctx, mesh, fd, hosts[0]), gpu_field(ctx, mesh, fd, hosts[1])
+    Lu, Lv = cm.Leaf("u"), cm.Leaf("v")
+    nodes, _ = api.serialize(api.d2x(Lu) * Lv, [Lu, Lv])
+    orc.assign(hosts[0], nodes, [hosts[0], hosts[1]], op=capi.ASSIGN_ADD)
+    u.assign(api.d2x(u) * v, op="+")
+    assert np.array_equal(readable_of(u), hosts[0].data[hosts[0].slices(cm.readable(hosts[0].info))].reshape(-1))
+
+
+def test_out_of_range_stencil_is_an_error_not_a_fault(ctx):
+    mesh = cm.mesh_uniform([17, 17])
+    fd = cm.field_desc(2, capi.CENTER, [(capi.BC_PERIODIC, capi.BC_PERIODIC)] * 2, ext=1)
+    u, w = api.CartesianField(mesh, fd, ctx), api.CartesianField(mesh, fd, ctx)
+    with pytest.raises(capi.OpflowError) as e:
+        w.assign(api.d1_weno53_downwind(u, 0))  # needs 3 ghost cells, the field has 1
+    assert e.value.code == capi.E_RANGE
+
+
+def test_ftcs2d_full_config_1025_1000_steps_bitexact(ctx):
+    """The CPU-runnable FTCS2D case at full size: 1025^2 nodes, Dirichlet 0, u0 ~ U[0,1), dt = 0.2 h^2,
+    1000 steps; GPU field vs the oracle, every value."""
+    n, steps = 1025, 1000
+    mesh = cm.mesh_uniform([n, n])
+    fd = cm.field_desc(2, capi.CORNER, [(capi.BC_DIRC, capi.BC_DIRC)] * 2)
+    h0 = orc.HostField(mesh, fd)
+    cm.seeded_interior(h0, 2024, n)
+    h0.update_padding()
+    u = gpu_field(ctx, mesh, fd, h0)
+    h = 1.0 / (n - 1)
+    s = 0.2 * h * h * 1.0
+    u.assign(cm.ftcs_expr(u, s, 2), steps=steps)
+    orc.lib().or_set_threads(os.cpu_count() or 1)
+    leaf = cm.Leaf("u")
+    nodes, _ = api.serialize(cm.ftcs_expr(leaf, s, 2))
+    for _ in range(steps):
+        orc.assign(h0, nodes, [h0])
+    assert np.array_equal(u.download(), h0.data)
+
+
+@pytest.mark.parametrize("dims,steps,cfl", [((257, 257), 400, 0.2), ((65, 65, 65), 120, 0.1), ((48, 40, 33), 60, 0.1)])
+def test_fast_mode_within_1e14_of_exact(ctx, dims, steps, cfl):
+    """OPFLOW_EVAL_FAST (fixed-point) against the bit-exact kernel: normwise relative error <= 1e-14."""
+    D = len(dims)
+    mesh = cm.mesh_uniform(list(dims))
+    fd = cm.field_desc(D, capi.CORNER, [(capi.BC_DIRC, capi.BC_DIRC)] * D, [(0.25, 0.25)] * D)
+    ue, uf = api.CartesianField(mesh, fd, ctx), api.CartesianField(mesh, fd, ctx)
+    a = ue.download()
+    rng = np.random.default_rng(1)
+    inner = tuple(slice(1, -1) for _ in range(D))
+    a[inner] = rng.random(a[inner].shape)
+    ue.upload(a)
+    uf.upload(a)
+    hx = 1.0 / (dims[0] - 1)
+    s = cfl * hx * hx
+    ue.assign(cm.ftcs_expr(ue, s, D), steps=steps, mode="exact")
+    uf.assign(cm.ftcs_expr(uf, s, D), steps=steps, mode="fast")
+    e, f = ue.download(), uf.download()
+    rel = np.abs(e - f).max() / np.abs(e).max()
+    assert rel <= 1e-14, rel
