@@ -217,7 +217,7 @@ typedef struct {
     int precision;        /* enum opflow_precision                                               */
     int pre_sweeps;       /* V-cycle smoothing sweeps (red-black Gauss-Seidel), default 2        */
     int post_sweeps;      /* default 2                                                           */
-    int coarse_max;       /* coarsest level size bound for the direct solve, default 512         */
+    int coarse_max;       /* coarsest level size bound for the dense direct solve, default 64    */
     int zero_guess;       /* 1: start from x = 0 instead of the target's values                  */
 } opflow_solve_params;
 
@@ -259,6 +259,10 @@ int opflow_batch_create(opflow_ctx ctx, const opflow_problem_desc* problems, int
                         const opflow_solve_params* params, opflow_batch* out);
 /* Device pointers of problem i's unknown vector and right-hand side (x fastest over the unknowns). */
 int opflow_batch_vectors(opflow_batch b, int i, double** x, double** f, size_t* n_unknowns);
+/* Host copies: set problem i's right-hand side (and, unless x0 is NULL, its initial guess); read its
+ * solution.  n must equal the problem's number of unknowns. */
+int opflow_batch_set(opflow_batch b, int i, const double* f_host, const double* x0_host, size_t n);
+int opflow_batch_get(opflow_batch b, int i, double* x_host, size_t n);
 int opflow_batch_solve(opflow_batch b, opflow_solve_state* states /* n_problems */);
 int opflow_batch_destroy(opflow_batch b);
 

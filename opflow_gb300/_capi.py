@@ -101,6 +101,8 @@ _SIGS = {
     "opflow_batch_create": [C.c_void_p, C.POINTER(ProblemDesc), C.c_int, C.POINTER(SolveParams), C.POINTER(C.c_void_p)],
     "opflow_batch_vectors": [C.c_void_p, C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_size_t)],
     "opflow_batch_solve": [C.c_void_p, C.POINTER(SolveState)],
+    "opflow_batch_set": [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_size_t],
+    "opflow_batch_get": [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.c_size_t],
     "opflow_batch_destroy": [C.c_void_p],
 }
 

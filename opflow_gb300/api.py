@@ -536,7 +536,7 @@ class StructSolverParams:
     (StructSolverPFMG.hpp:23-33) and the GPU extensions (precision form, coarse size)."""
 
     def __init__(self, tol=1e-10, maxIter=200, staticMat=False, pinValue=False, precision="fp64", preSweeps=2,
-                 postSweeps=2, coarseMax=256, zeroGuess=False):
+                 postSweeps=2, coarseMax=64, zeroGuess=False):
         self.tol, self.maxIter, self.staticMat, self.pinValue = tol, maxIter, staticMat, pinValue
         self.precision, self.preSweeps, self.postSweeps, self.coarseMax, self.zeroGuess = (precision, preSweeps, postSweeps,
                                                                                            coarseMax, zeroGuess)
@@ -633,3 +633,80 @@ def assemble(getter, target, pin=False):
                             off.ctypes.data_as(C.POINTER(C.c_int)), coef.ctypes.data_as(C.POINTER(C.c_double)),
                             rhs.ctypes.data_as(C.POINTER(C.c_double)), C.byref(nc)))
     return off.reshape(ne.value, D), coef.reshape(nc.value, ne.value), rhs
+
+
+def weno_rk3(u, dt, steps=1, upwind=False, dim=0, u1=None, u2=None):
+    """One or more Shu-Osher RK3 steps of u_t + d1<WENO53>(u) = 0 along a periodic dim, fused
+    (opflow_weno_rk3); identical to the three assignments
+        u1 = u - dt*d1<W>(u); u2 = 0.75*u + 0.25*(u1 - dt*d1<W>(u1)); u = 1/3*u + 2/3*(u2 - dt*d1<W>(u2))."""
+    kind = capi.NODE_WENO53_UP if upwind else capi.NODE_WENO53_DOWN
+    check(lib().opflow_weno_rk3(u.ctx.handle, u.handle, u1.handle if u1 else None, u2.handle if u2 else None, kind, dim, float(dt),
+                                int(steps)))
+
+
+# ---------------------------------------------------------------------------------------------- batches
+class Problem:
+    """alpha*u - beta*Lap(u) = f on an n[0] x n[1] (x n[2]) grid of cells (Center) or nodes (Corner) with
+    spacing h, Dirichlet 0 or Neumann 0 on every side (opflow_problem_desc)."""
+
+    def __init__(self, n, h, alpha=1.0, beta=1.0, loc=LocOnMesh.Center, bc=BCType.Dirc):
+        self.n, self.h, self.alpha, self.beta, self.loc, self.bc = list(n), list(h), alpha, beta, loc, bc
+
+    def to_c(self):
+        d = capi.ProblemDesc()
+        d.ndim = len(self.n)
+        for k in range(d.ndim):
+            d.n[k] = self.n[k]
+            d.h[k] = self.h[k]
+        d.loc, d.bc, d.alpha, d.beta = self.loc, self.bc, float(self.alpha), float(self.beta)
+        return d
+
+
+class Batch:
+    """Many independent problems solved together, one launch per multigrid operation for the batch."""
+
+    def __init__(self, problems, params=None, ctx=None):
+        self.ctx = ctx or default_context()
+        self.problems = list(problems)
+        arr = (capi.ProblemDesc * len(self.problems))(*[p.to_c() for p in self.problems])
+        self.params = params or StructSolverParams()
+        p = self.params.to_c()
+        h = C.c_void_p()
+        check(lib().opflow_batch_create(self.ctx.handle, arr, len(self.problems), C.byref(p), C.byref(h)))
+        self.handle = h
+
+    def size(self, i):
+        n = C.c_size_t(0)
+        check(lib().opflow_batch_vectors(self.handle, i, None, None, C.byref(n)))
+        return n.value
+
+    def set(self, i, f, x0=None):
+        f = np.ascontiguousarray(f, dtype=np.float64).reshape(-1)
+        x0p = None
+        if x0 is not None:
+            x0 = np.ascontiguousarray(x0, dtype=np.float64).reshape(-1)
+            x0p = x0.ctypes.data_as(C.POINTER(C.c_double))
+        check(lib().opflow_batch_set(self.handle, i, f.ctypes.data_as(C.POINTER(C.c_double)), x0p, f.size))
+
+    def get(self, i):
+        x = np.empty(self.size(i))
+        check(lib().opflow_batch_get(self.handle, i, x.ctypes.data_as(C.POINTER(C.c_double)), x.size))
+        return x
+
+    def solve(self):
+        st = (capi.SolveState * len(self.problems))()
+        rc = lib().opflow_batch_solve(self.handle, st)
+        if rc not in (capi.OK, capi.E_NOT_CONVERGED):
+            check(rc)
+        return [EqnSolveState(s) for s in st]
+
+    def close(self):
+        if getattr(self, "handle", None) and not _exiting[0]:
+            lib().opflow_batch_destroy(self.handle)
+        self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -339,6 +339,21 @@ int update_padding_full(opflow_field f, double* data) {
     return OPFLOW_OK;
 }
 
+bool padding_self_overlaps(opflow_field f) {
+    for (int d = 0; d < f->info.ndim; ++d) {
+        if (f->desc.bc_type[d][0] != OPFLOW_BC_PERIODIC) continue;
+        const int period = f->info.accessible[d][1] - f->info.accessible[d][0];
+        if (period < f->desc.ext[d][0] || period < f->desc.ext[d][1]) return true;
+    }
+    return false;
+}
+
+int update_padding_assign(opflow_field f) {
+    OPG_TRY(update_padding_buf(f, f->buf[f->cur]));
+    if (padding_self_overlaps(f)) OPG_TRY(update_padding_full(f, f->buf[f->cur]));
+    return OPFLOW_OK;
+}
+
 int ensure_back(opflow_field f) {
     if (f->buf[1 - f->cur]) return OPFLOW_OK;
     double* p = nullptr;

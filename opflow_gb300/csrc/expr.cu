@@ -408,6 +408,8 @@ static int markstein_ok(opflow_ctx ctx, double h, bool* ok) {
     return OPFLOW_OK;
 }
 
+int markstein_ok_public(opflow_ctx ctx, double h, bool* ok) { return markstein_ok(ctx, h, ok); }
+
 // ======================================================================================== fast fixed point
 // Linear constant-coefficient stencil of one field in difference form:
 //   out = c + sum_g sigma_g * sum_{k in g} (u(i + o_k) - c),   c = u(i)
@@ -921,7 +923,7 @@ static int run_plan(opflow_ctx ctx, opflow_field dst, int arith, const opflow_fi
         }
         dst->cur = 1 - dst->cur;
     }
-    return update_padding_buf(dst, dst->buf[dst->cur]);
+    return update_padding_assign(dst);
 }
 
 }  // namespace opg

@@ -38,12 +38,12 @@ int check_launch(const char* what);
 // ---- geometry ---------------------------------------------------------------------------------------
 struct Box {
     int lo[3] = {0, 0, 0}, hi[3] = {1, 1, 1};
-    long long count() const {
+    __host__ __device__ long long count() const {
         long long c = 1;
         for (int d = 0; d < 3; ++d) c *= (hi[d] > lo[d] ? hi[d] - lo[d] : 0);
         return c;
     }
-    bool empty() const { return count() == 0; }
+    __host__ __device__ bool empty() const { return count() == 0; }
 };
 
 // Device view of a field's data array and the ranges the kernels need.
@@ -119,6 +119,10 @@ void mesh_destroy(MeshDev* m);
 bool mesh_equal(const MeshDev* a, const MeshDev* b);
 int ensure_back(opflow_field f);
 int update_padding_buf(opflow_field f, double* data);
+// updatePadding as an assignment does it (assign_impl and assignImpl_final each run one pass; a second
+// pass only changes a periodic zone wider than its period)
+int update_padding_assign(opflow_field f);
+bool padding_self_overlaps(opflow_field f);
 int ensure_scratch(opflow_ctx ctx, size_t bytes);
 int compute_info(const opflow_mesh_desc* m, const opflow_field_desc* f, opflow_field_info* o);
 Box assign_box(const opflow_field_info& r);

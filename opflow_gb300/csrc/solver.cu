@@ -230,37 +230,46 @@ static int assemble_level(MGSystem* S, opflow_field target, const std::vector<op
     return OPFLOW_OK;
 }
 
+// gathers the coefficients of the class representatives: tab[cls][slot] = A[slot][rep[cls]]
+__global__ void gather_classes(const double* A, long long N, const long long* rep, double* tab) {
+    const int t = threadIdx.x;
+    if (t < NCLASS * NSLOT) {
+        const int cls = t / NSLOT, s = t % NSLOT;
+        tab[t] = rep[cls] >= 0 ? A[s * N + rep[cls]] : 0.;
+    }
+}
+
 // Position-class table if every cell matches its class representative exactly.
 static int compress_level(MGSystem* S, LevelHost& L) {
     opflow_ctx ctx = S->ctx;
     const long long N = L.N;
-    std::vector<double> tab(NCLASS * NSLOT, 0.);
-    std::vector<double> col(1);
-    auto rep = [&](int c, int n) { return c == 0 ? 0 : (c == 1 ? std::min(1, n - 1) : n - 1); };
+    std::vector<long long> rep(NCLASS, -1);
+    auto rp = [&](int c, int n) { return c == 0 ? 0 : (c == 1 ? std::min(1, n - 1) : n - 1); };
     for (int cz = 0; cz < 3; ++cz)
         for (int cy = 0; cy < 3; ++cy)
             for (int cx = 0; cx < 3; ++cx) {
                 if ((L.ndim < 2 && cy) || (L.ndim < 3 && cz)) continue;
-                const int i = rep(cx, L.n[0]), j = L.ndim > 1 ? rep(cy, L.n[1]) : 0, k = L.ndim > 2 ? rep(cz, L.n[2]) : 0;
-                const long long cell = i + (long long) L.n[0] * (j + (long long) L.n[1] * k);
-                const int cls = cx + 3 * cy + 9 * cz;
-                for (int s = 0; s < NSLOT; ++s)
-                    cudaMemcpyAsync(&tab[cls * NSLOT + s], L.A64 + s * N + cell, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+                const int i = rp(cx, L.n[0]), j = L.ndim > 1 ? rp(cy, L.n[1]) : 0, k = L.ndim > 2 ? rp(cz, L.n[2]) : 0;
+                rep[cx + 3 * cy + 9 * cz] = i + (long long) L.n[0] * (j + (long long) L.n[1] * k);
             }
-    OPG_CUDA(cudaStreamSynchronize(ctx->stream));
     double* dtab = (double*) S->arena.alloc(NCLASS * NSLOT * sizeof(double));
     float* dtab32 = (float*) S->arena.alloc(NCLASS * NSLOT * sizeof(float));
+    long long* drep = (long long*) ((char*) ctx->scratch + 2048);
     if (!dtab || !dtab32) return fail(OPFLOW_E_NOMEM, "class table");
-    std::vector<float> t32(tab.begin(), tab.end());
-    cudaMemcpyAsync(dtab, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
-    cudaMemcpyAsync(dtab32, t32.data(), t32.size() * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemcpyAsync(drep, rep.data(), NCLASS * sizeof(long long), cudaMemcpyHostToDevice, ctx->stream);
+    gather_classes<<<1, 256, 0, ctx->stream>>>(L.A64, N, drep, dtab);
+    OPG_LAUNCHED();
     int* bad = (int*) ctx->scratch;
     cudaMemsetAsync(bad, 0, sizeof(int), ctx->stream);
     class_check<<<gridN(ctx, N), 256, 0, ctx->stream>>>(L.A64, N, L.n[0], L.n[1], L.n[2], L.ndim, dtab, bad);
     OPG_LAUNCHED();
+    std::vector<double> tab(NCLASS * NSLOT);
     int hb = 0;
+    cudaMemcpyAsync(tab.data(), dtab, tab.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
     cudaMemcpyAsync(&hb, bad, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
     OPG_CUDA(cudaStreamSynchronize(ctx->stream));
+    std::vector<float> t32(tab.begin(), tab.end());
+    cudaMemcpyAsync(dtab32, t32.data(), t32.size() * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
     L.T64 = dtab;
     L.T32 = dtab32;
     L.table = hb == 0;
@@ -271,6 +280,7 @@ static int compress_level(MGSystem* S, LevelHost& L) {
         to_f32<<<gridN(ctx, NSLOT * N), 256, 0, ctx->stream>>>(L.A64, L.A32, NSLOT * N);
         OPG_LAUNCHED();
     }
+    OPG_CUDA(cudaStreamSynchronize(ctx->stream));  // t32 must outlive its copy
     return OPFLOW_OK;
 }
 
@@ -753,7 +763,7 @@ void opflow_solve_params_default(opflow_solve_params* p) {
     p->precision = OPFLOW_PREC_FP64;
     p->pre_sweeps = 2;
     p->post_sweeps = 2;
-    p->coarse_max = 256;
+    p->coarse_max = 64;
     p->zero_guess = 0;
 }
 
@@ -765,7 +775,7 @@ int opflow_solver_create(opflow_ctx ctx, opflow_field target, const opflow_node*
     else opflow_solve_params_default(&p);
     if (!(p.tol > 0) || p.max_iter < 0 || p.pre_sweeps < 0 || p.post_sweeps < 0) return fail(OPFLOW_E_INVALID, "bad solver parameters");
     if (p.precision != OPFLOW_PREC_FP64 && p.precision != OPFLOW_PREC_MIXED) return fail(OPFLOW_E_INVALID, "bad precision");
-    if (p.coarse_max <= 0) p.coarse_max = 256;
+    if (p.coarse_max <= 0) p.coarse_max = 64;
     auto* s = new opflow_solver_s();
     s->ctx = ctx;
     s->target = target;

@@ -72,6 +72,53 @@ def test_weno_rk3_gpu_interpreter_matches_reference_dump(ctx, name):
     assert np.array_equal(u.download().reshape(-1), arr["u__data"])
 
 
+@pytest.mark.parametrize("name", ["weno_down_32x4", "weno_up_64x3", "weno_down_40x2_nonpow2"])
+@pytest.mark.parametrize("fused_steps", [1, 0])
+def test_weno_rk3_fused_kernel_matches_reference_dump(ctx, name, fused_steps):
+    """The one-kernel RK3 step (all stages in shared memory), stepping once per call or all steps in
+    one launch, against the reference's three-assignment result."""
+    meta, arr = cm.golden(name)
+    _, nx, ny, steps, seed, up = meta["args"]
+    nx, ny, steps, up = int(nx), int(ny), int(steps), int(up)
+    mesh = cm.mesh_uniform([nx + 1, ny + 1])
+    fd = cm.field_desc(2, capi.CENTER, [(capi.BC_PERIODIC, capi.BC_PERIODIC)] * 2, ext=3)
+    h0 = orc.HostField(mesh, fd, data=arr["u0__data"])
+    u, u1, u2 = (gpu_field(ctx, mesh, fd, h0) for _ in range(3))
+    dt = 0.5 * (1.0 / nx)
+    if fused_steps:
+        for _ in range(steps):
+            api.weno_rk3(u, dt, 1, upwind=bool(up), u1=u1, u2=u2)
+    else:
+        api.weno_rk3(u, dt, steps, upwind=bool(up))
+    assert np.array_equal(u.download().reshape(-1), arr["u__data"])
+
+
+def test_weno_rk3_fused_4096_lines_matches_oracle(ctx):
+    """Full line length of the WENO configuration (4096 periodic cells) on a few lines."""
+    nx, ny, steps = 4096, 3, 2
+    mesh = cm.mesh_uniform([nx + 1, ny + 1])
+    fd = cm.field_desc(2, capi.CENTER, [(capi.BC_PERIODIC, capi.BC_PERIODIC)] * 2, ext=3)
+    h0 = orc.HostField(mesh, fd)
+    rng = h0.assignable()
+    x = (np.arange(nx) + 0.5) / nx
+    for j in range(ny):
+        h0.data[h0.slices([rng[0], (j, j + 1)])] = (np.where((x > 0.2 + 0.1 * j) & (x < 0.5), 1.0, 0.0) + 0.3 * np.sin(2 * np.pi * (j + 1) * x))
+    h0.update_padding()
+    u = gpu_field(ctx, mesh, fd, h0)
+    dt = 0.5 / nx
+    api.weno_rk3(u, dt, steps)
+    L = [cm.Leaf("u"), cm.Leaf("u1"), cm.Leaf("u2")]
+    e = cm.weno_stage_exprs(L[0], L[1], L[2], dt)
+    ns = [api.serialize(x, L)[0] for x in e]
+    h1 = orc.HostField(mesh, fd, data=h0.data.copy())
+    h2 = orc.HostField(mesh, fd, data=h0.data.copy())
+    for _ in range(steps):
+        orc.assign(h1, ns[0], [h0, h1, h2])
+        orc.assign(h2, ns[1], [h0, h1, h2])
+        orc.assign(h0, ns[2], [h0, h1, h2])
+    assert np.array_equal(u.download(), h0.data)
+
+
 PAD = sorted(f[:-4] for f in os.listdir(cm.GOLDEN) if f.startswith("pad_"))
 
 
