@@ -266,6 +266,22 @@ int opflow_batch_get(opflow_batch b, int i, double* x_host, size_t n);
 int opflow_batch_solve(opflow_batch b, opflow_solve_state* states /* n_problems */);
 int opflow_batch_destroy(opflow_batch b);
 
+/* ---- residual norms without device allocation ------------------------------------------------- */
+/* No counterpart in the reference.  For callers that cannot allocate device memory where they need the
+ * answer - code running inside a CUDA stream capture (cudaMalloc/cudaFree cannot be captured), hosts
+ * whose device memory belongs to their own pool allocator, latency-critical loops that must not
+ * synchronise the device: computes r = b - A x and norms[0] = ||b||_2, norms[1] = ||b - A x||_2 (the
+ * residual the solvers report as EqnSolveState::relerr = norms[1]/norms[0]) with no allocation at all.
+ * Every pointer is device memory the caller owns: coef is the (2*ndim+1)-point operator as seven
+ * float64 slot arrays [7][N] (centre, x-, x+, y-, y+, z-, z+; unused slots ignored), b/x/r hold N
+ * values x fastest, norms two values.  Work is enqueued on `stream` (results valid after it completes).
+ * The partial sums live in one static 1 MiB device array per device: grids needing more than 65536
+ * chunks (one per 1024 cells of every x-row) are rejected with OPFLOW_E_INVALID; calls that overlap on
+ * the GPU race on that array.  The first call on a device looks up the array's address with that
+ * device current: make it before any stream capture begins. */
+int opflow_residual_norms_noalloc(void* stream, int ndim, const int* n, const int* periodic, const double* coef, const double* b,
+                                  const double* x, double* r, double* norms);
+
 #ifdef __cplusplus
 }
 #endif

@@ -104,6 +104,8 @@ _SIGS = {
     "opflow_batch_set": [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_size_t],
     "opflow_batch_get": [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.c_size_t],
     "opflow_batch_destroy": [C.c_void_p],
+    "opflow_residual_norms_noalloc": [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_void_p, C.c_void_p, C.c_void_p,
+                                      C.c_void_p, C.c_void_p],
 }
 
 
