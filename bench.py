@@ -7,6 +7,14 @@ Workloads (seeded synthetic inputs with the configurations' shapes and value dis
   ftcs3d  7-point FTCS heat update, 512^3 node grid, Dirichlet 0, u0 = 8 seeded Gaussians,
           dt = 0.1 h^2 (one step = one update of the whole grid; GLUP/s)
   ftcs2d  the CPU-runnable FTCS2D case: 1025^2 nodes, Dirichlet 0, u0 ~ U[0,1), dt = 0.2 h^2
+  poisson2d  -Lap(p) = f on 2048^2 cells, homogeneous Neumann, pinned (the reference's pinValue), f ~ N(0,1)
+          projected to zero mean, to 1e-10 relative residual: mixed (FP32 V-cycle in FP64 flexible PCG)
+          next to plain FP64 (solves/s)
+  serve   (default) Poisson-process arrivals of 70% one-shot Poisson solves (2D side LogU[129,2049],
+          3D side LogU[64,256], Neumann / Dirichlet 50/50) and 30% backward-Euler heat sessions of
+          10-100 steps, mixed precision to 1e-10: value = device-resident batched solves/s of the
+          window's requests, e2e = the request server's host-to-host solves/s with p50/p99, next to
+          plain FP64 serving one request at a time
 
 `--impl reference` times the reference's CPU algorithm (the C restatement under oracle/, the
 reference itself does not build on the Arm machine) on the host cores for the same metric.
@@ -168,6 +176,19 @@ def run_reference(args):
     if rank != 0:
         return 0
     threads = os.cpu_count() or 1
+    if args.workload in ("poisson2d", "serve"):
+        vals = []
+        for _ in range(max(1, min(args.steps, 3))):
+            v, sample, used = cpu_solve_sample(threads)
+            vals.append(v)
+        value = statistics.median(vals)
+        line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": args.gpus, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1e3 / value, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64", "data": "synthetic", "config": {"workload": args.workload, "sample": sample},
+                "cpu_baseline": {"value": value, "unit": "solves/s", "cores": used, "kind": "port", "sample": sample},
+                "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return 0
     vals = []
     sample = ""
     for _ in range(args.warmup):
@@ -186,6 +207,200 @@ def run_reference(args):
     return 0
 
 
+# ------------------------------------------------------------------------------------------ solves
+ITER_BYTES_PER_CELL = 220.0  # algorithmic bytes per level-0 cell and flexible-PCG iteration
+
+
+def poisson_problem(api, rng, n, ndim, bc):
+    return api.Problem([n] * ndim, [1.0 / n] * ndim, alpha=0.0, beta=1.0, loc=api.LocOnMesh.Center, bc=bc)
+
+
+def rhs_for(np_, rng, p):
+    f = rng.standard_normal(int(np_.prod(p.n)))
+    if p.alpha == 0.0 and p.bc != 1:
+        f -= f.mean()
+    return f
+
+
+def serve_mix(np_, api, seed, count):
+    """Requests of the serving configuration, seeded."""
+    rng = np_.random.default_rng(seed)
+    reqs = []
+    for _ in range(count):
+        u = rng.random()
+        if u < 0.7:
+            if rng.random() < 0.5:
+                n = int(round(np_.exp(rng.uniform(np_.log(129), np_.log(2049)))))
+                ndim = 2
+            else:
+                n = int(round(np_.exp(rng.uniform(np_.log(64), np_.log(256)))))
+                ndim = 3
+            bc = api.BCType.Neum if rng.random() < 0.5 else api.BCType.Dirc
+            p = poisson_problem(api, rng, n, ndim, bc)
+            steps = 1
+        else:
+            n = int(round(np_.exp(rng.uniform(np_.log(129), np_.log(1025)))))
+            dt = 1.0 / n
+            p = api.Problem([n, n], [1.0 / n] * 2, alpha=1.0, beta=dt, loc=api.LocOnMesh.Center, bc=api.BCType.Dirc)
+            steps = int(rng.integers(10, 101))
+        reqs.append((p, rhs_for(np_, rng, p), steps))
+    return reqs
+
+
+def cpu_solve_sample(threads):
+    """The oracle's FP64 CG (Jacobi) on a 256^2 Neumann Poisson sample: solves/s on the host cores."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import numpy as np
+    import common as cm
+    import oracle_lib as orc
+    from opflow_gb300 import _capi as capi
+    from opflow_gb300 import api
+    used = orc.lib().or_set_threads(threads)
+    n = 256
+    mesh = cm.mesh_uniform([n + 1, n + 1])
+    fd = cm.field_desc(2, capi.CENTER, [(capi.BC_NEUM, capi.BC_NEUM)] * 2, ext=1)
+    p, f = orc.HostField(mesh, fd), orc.HostField(mesh, fd)
+    rng = np.random.default_rng(0)
+    v = rng.standard_normal((n, n))
+    f.data[f.slices(f.assignable())] = v - v.mean()
+    L = [cm.Leaf("p"), cm.Leaf("f")]
+    nodes, _ = api.serialize(api.Eq(L[1], api.d2x(L[0]) + api.d2y(L[0])).residual_expr(), L)
+    t0 = time.perf_counter()
+    off, coef, rhs = orc.assemble(p, nodes, [p, f], 0, 1)
+    x, it, rr = orc.pcg([n, n], [0, 0], off, coef, rhs, tol=1e-10, maxit=100000)
+    dt = time.perf_counter() - t0
+    return 1.0 / dt, "256^2 Neumann Poisson, oracle assembly + FP64 Jacobi-PCG to 1e-10 (%d it, %.2f s; HYPRE PFMG is not built here)" % (it, dt), 1
+
+
+def run_poisson2d(args, torch, api, capi, np, ctx, stream, world, rank, local):
+    n = args.grid or 2048
+    mesh = api.MeshBuilder().newMesh(n + 1, n + 1).setMeshOfDim(0, 0., 1.).setMeshOfDim(1, 0., 1.).build()
+    b = api.ExprBuilder().setMesh(mesh).setLoc(api.LocOnMesh.Center).setExt(1)
+    for d in range(2):
+        b.setBC(d, api.DimPos.start, api.BCType.Neum, 0.).setBC(d, api.DimPos.end, api.BCType.Neum, 0.)
+    p = b.build(ctx)
+    f = b.build(ctx)
+    a = f.download()
+    sl = f.index_slices(f.assignableRange)
+    rng = np.random.default_rng(1234 + rank)
+    v = rng.standard_normal(a[sl].shape)
+    a[sl] = v - v.mean()
+    f.upload(a)
+    getter = lambda e: f == api.d2x(e) + api.d2y(e)
+    out = {}
+    for prec in ("mixed", "fp64"):
+        h = api.makeEqnSolveHandler(getter, p, api.StructSolverParams(tol=1e-10, maxIter=200, pinValue=True, staticMat=True,
+                                                                        precision=prec, zeroGuess=True))
+        for _ in range(args.warmup):
+            st = h.solve()
+        torch.cuda.synchronize()
+        l0 = capi.launch_count()
+        t0 = time.perf_counter()
+        its, rels = [], []
+        for _ in range(args.steps):
+            st = h.solve()
+            its.append(st.niter)
+            rels.append(st.relerr)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        out[prec] = dict(solves_per_s=args.steps / dt, ms_per_solve=dt / args.steps * 1e3, iterations=its[-1], rel_residual=max(rels),
+                         launches=capi.launch_count() - l0)
+        h.close()
+    # end-to-end: host f in (upload), solve, host solution out (download)
+    h = api.makeEqnSolveHandler(getter, p, api.StructSolverParams(tol=1e-10, maxIter=200, pinValue=True, staticMat=True,
+                                                                    precision="mixed", zeroGuess=True))
+    h.solve()
+    host = a.copy()
+    t0 = time.perf_counter()
+    e2e_steps = max(1, min(args.steps, 5))
+    for _ in range(e2e_steps):
+        f.upload(host)
+        h.solve()
+        _ = p.download()
+    e2e = e2e_steps / (time.perf_counter() - t0)
+    h.close()
+    N = n * n
+    m = out["mixed"]
+    achieved = ITER_BYTES_PER_CELL * N * m["iterations"] / (m["ms_per_solve"] * 1e-3) / 1e9
+    peak, src = peak_hbm()
+    return dict(value=m["solves_per_s"], unit="solves/s", ms=m["ms_per_solve"], launches=m["launches"], dtype="f64 outer / f32 V-cycle",
+                config=dict(workload="poisson2d", grid=[n, n], loc="cell", bc="neumann 0, pinned", rhs="N(0,1) zero mean", tol=1e-10,
+                            mixed=m, fp64=out["fp64"], mixed_over_fp64=m["solves_per_s"] / out["fp64"]["solves_per_s"],
+                            l2="level-0 vectors 33.5 MB each; the solve streams several of them per iteration (> L2)"),
+                roofline={"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": src,
+                          "traffic": traffic_for("poisson2d"), "kernel": "flexible-PCG iteration (graph: FP32 V-cycle + FP64 Krylov)",
+                          "algorithmic_bytes_per_launch": ITER_BYTES_PER_CELL * N},
+                e2e={"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": a.nbytes, "d2h_bytes_per_step": a.nbytes, "steps": e2e_steps})
+
+
+def run_serve(args, torch, api, capi, np, ctx, stream, world, rank, local):
+    count = args.requests
+    rate = args.rate
+    params = api.StructSolverParams(tol=1e-10, maxIter=200, precision="mixed", zeroGuess=True)
+    reqs = serve_mix(np, api, 77 + rank, count)
+    total_solves = sum(s for _, _, s in reqs)
+    cells = sum(int(np.prod(p.n)) * s for p, _, s in reqs)
+
+    def served(prec, max_active, rq):
+        srv = api.Server(api.StructSolverParams(tol=1e-10, maxIter=200, precision=prec), hbm_budget=120 << 30,
+                         max_active=max_active, ctx=ctx)
+        rng = np.random.default_rng(5)
+        gaps = rng.exponential(1.0 / rate, len(rq))
+        ids = []
+        t0 = time.perf_counter()
+        tnext = t0
+        for (p, f, steps), g in zip(rq, gaps):
+            tnext += g
+            while time.perf_counter() < tnext:
+                time.sleep(min(0.0005, max(0.0, tnext - time.perf_counter())))
+            ids.append(srv.submit(p, f, steps=steps, out=np.zeros(f.size)))
+        res = [srv.result(i) for i in ids]
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+        srv.close()
+        ok = sum(1 for r in res if r["status"] == capi.OK)
+        lat = sorted(r["latency_ms"] for r in res)
+        q = lambda z: lat[min(len(lat) - 1, int(np.ceil(z * len(lat))) - 1)]
+        return dict(solves_per_s=sum(r["solves"] for r in res) / wall, p50_ms=q(0.5), p99_ms=q(0.99), ok=ok, n=len(res),
+                    iterations=sum(r["iterations"] for r in res), max_active_seen=st["max_active_seen"], wall_s=wall,
+                    compositions=st["compositions"])
+
+    # warm-up (allocator, graphs, kernels)
+    served("mixed", 16, serve_mix(np, api, 3, 4))
+    l0 = capi.launch_count()
+    mixed = served("mixed", 64, reqs)
+    launches = capi.launch_count() - l0
+    plain = served("fp64", 1, reqs)
+    # device-resident batched throughput of the same one-shot problems (inputs already in HBM)
+    oneshot = [(p, f) for p, f, s in reqs if s == 1]
+    B = api.Batch([p for p, _ in oneshot], params, ctx)
+    for i, (_, f) in enumerate(oneshot):
+        B.set(i, f)
+    B.solve()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    st = B.solve()
+    torch.cuda.synchronize()
+    dev_rate = len(oneshot) / (time.perf_counter() - t0)
+    B.close()
+    iters = sum(s.niter for s in st)
+    bcells = sum(int(np.prod(p.n)) for p, _ in oneshot)
+    peak, src = peak_hbm()
+    achieved = ITER_BYTES_PER_CELL * bcells * (iters / max(1, len(oneshot))) * dev_rate / max(1, len(oneshot)) / 1e9
+    return dict(value=dev_rate, unit="solves/s", ms=1e3 / dev_rate, launches=launches, dtype="f64 outer / f32 V-cycle",
+                config=dict(workload="serve", requests=count, rate_per_s=rate, mix="70% one-shot Poisson (2D LogU[129,2049] / 3D LogU[64,256], "
+                            "Neumann/Dirichlet 50/50), 30% heat sessions 10-100 backward-Euler steps (2D LogU[129,1025])",
+                            solves_in_window=total_solves, budget_gb=120, served_mixed=mixed, served_plain_fp64_one_at_a_time=plain,
+                            served_speedup=mixed["solves_per_s"] / plain["solves_per_s"],
+                            p99_ratio_mixed_over_plain=mixed["p99_ms"] / plain["p99_ms"],
+                            l2="problems of 2-68 MB each, streamed per iteration (> L2 in aggregate)"),
+                roofline={"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": src,
+                          "traffic": traffic_for("serve"), "kernel": "batched flexible-PCG iteration (graph) over the window's one-shot problems",
+                          "algorithmic_bytes_per_launch": ITER_BYTES_PER_CELL * bcells},
+                e2e={"value": mixed["solves_per_s"], "unit": "solves/s", "h2d_bytes_per_step": 8 * sum(f.size for _, f, _ in reqs),
+                     "d2h_bytes_per_step": 8 * sum(f.size for _, f, _ in reqs), "p50_ms": mixed["p50_ms"], "p99_ms": mixed["p99_ms"]})
+
+
 # ------------------------------------------------------------------------------------------- ours
 def run_ours(args):
     import torch
@@ -202,6 +417,34 @@ def run_ours(args):
     ctx = api.Context(local)
     stream = torch.cuda.current_stream()
     ctx.set_stream(stream.cuda_stream)
+
+    if args.workload in ("poisson2d", "serve"):
+        if world > 1:
+            dist.barrier()
+        with ClockSampler(local) as clk:
+            fn = run_poisson2d if args.workload == "poisson2d" else run_serve
+            r = fn(args, torch, api, capi, np, ctx, stream, world, rank, local)
+        value = r["value"]
+        if world > 1:
+            tt = torch.tensor([value], device=torch.device("cuda", local))
+            dist.all_reduce(tt, op=dist.ReduceOp.MIN)  # every replica does the same work: slowest rank * N
+            value = float(tt.item()) * world
+        cpu = None
+        if rank == 0 and not args.no_cpu_baseline:
+            try:
+                v, sample, used = cpu_solve_sample(os.cpu_count() or 1)
+                cpu = {"value": v, "unit": "solves/s", "cores": used, "kind": "port", "sample": sample}
+            except Exception as ex:
+                cpu = {"value": None, "unit": "solves/s", "cores": 0, "kind": "port", "sample": "failed: %s" % ex}
+        line = {"metric": METRIC, "value": value, "unit": r["unit"], "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": r["ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": r["dtype"],
+                "data": "synthetic", "config": dict(r["config"], parallelism="replicas" if world > 1 else "single"),
+                "roofline": r["roofline"], "cpu_baseline": cpu, "e2e": r["e2e"], "gpu_launches": r["launches"], "clocks": clk.summary()}
+        if rank == 0:
+            print(json.dumps(line), flush=True)
+        if world > 1:
+            dist.destroy_process_group()
+        return 0
 
     cfg = workload_cfg(args.workload)
     if args.grid:
@@ -318,7 +561,9 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="ftcs3d", choices=["ftcs3d", "ftcs2d"])
+    ap.add_argument("--workload", default="serve", choices=["serve", "poisson2d", "ftcs3d", "ftcs2d"])
+    ap.add_argument("--requests", type=int, default=48, help="serve: requests per measurement window")
+    ap.add_argument("--rate", type=float, default=100.0, help="serve: Poisson arrival rate (requests/s)")
     ap.add_argument("--mode", default="fast", choices=["fast", "exact"])
     ap.add_argument("--grid", type=int, default=0, help="override the grid side (profiling a smaller case)")
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU baseline leg (profiling runs)")

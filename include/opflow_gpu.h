@@ -266,6 +266,46 @@ int opflow_batch_get(opflow_batch b, int i, double* x_host, size_t n);
 int opflow_batch_solve(opflow_batch b, opflow_solve_state* states /* n_problems */);
 int opflow_batch_destroy(opflow_batch b);
 
+/* ---- serving ---------------------------------------------------------------------------------- */
+/* A request loop that keeps problems resident on the device and batches whatever is active into one
+ * persistent launch per multigrid operation (continuous batching: requests join at the next iteration
+ * boundary once HBM budget and a slot are free, and leave as soon as they converge).  No counterpart
+ * in the reference, which solves one equation per call (HYPREEqnSolveHandler::solve). */
+typedef struct {
+    opflow_problem_desc problem; /* alpha*u - beta*Lap(u) = f                                          */
+    int steps;                   /* 1: one solve; k > 1: a session of k solves, each taking the previous
+                                    solution as its right-hand side (backward-Euler heat steps)        */
+    const double* f;             /* host right-hand side / initial state, n unknowns (copied at submit) */
+    double* x_out;               /* host buffer for the final solution, n unknowns (may be NULL)        */
+} opflow_request;
+
+typedef struct {
+    long long id;
+    int status;                  /* OPFLOW_OK, OPFLOW_E_NOT_CONVERGED, ...                           */
+    int iterations;              /* flexible-PCG iterations summed over the request's solves          */
+    int solves;
+    double rel_residual;         /* of the last solve                                                */
+    double queue_ms, latency_ms; /* submit -> admission, submit -> result on the host                 */
+} opflow_request_result;
+
+typedef struct {
+    long long submitted, completed, solves;
+    double p50_ms, p99_ms, mean_ms, max_ms;
+    double elapsed_s, solves_per_s;
+    int max_active_seen;
+    long long graph_launches, compositions;
+} opflow_serve_stats;
+
+/* hbm_budget_bytes bounds the resident problems' memory (0: unbounded); max_active bounds the batch
+ * (1 gives one-request-at-a-time serving). */
+int opflow_server_create(opflow_ctx ctx, const opflow_solve_params* params, size_t hbm_budget_bytes, int max_active, opflow_server* out);
+int opflow_server_submit(opflow_server s, const opflow_request* req, long long* id);
+/* wait != 0 blocks until the request is done; otherwise *done tells whether `out` was filled */
+int opflow_server_result(opflow_server s, long long id, int wait, int* done, opflow_request_result* out);
+int opflow_server_drain(opflow_server s);
+int opflow_server_stats(opflow_server s, opflow_serve_stats* out);
+int opflow_server_destroy(opflow_server s);
+
 /* ---- residual norms without device allocation ------------------------------------------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device memory where they need the
  * answer - code running inside a CUDA stream capture (cudaMalloc/cudaFree cannot be captured), hosts

@@ -7,7 +7,7 @@ from ._capi import OpflowError, launch_count  # noqa: F401
 from .api import (  # noqa: F401
     BCType, CartesianField, Eq, CartesianMesh, Context, DimPos, Equation, Expr, ExprBuilder, LocOnMesh, MeshBuilder,
     d1, d1IntpCenterToCorner, d1_weno53_downwind, d1_weno53_upwind, d2, d2x, d2y, d2z, default_context, describe, dx,
-    dy, dz, serialize, StructSolverParams, EqnSolveState, EqnSolveHandler, makeEqnSolveHandler, Solve, assemble, weno_rk3, Problem, Batch,
+    dy, dz, serialize, StructSolverParams, EqnSolveState, EqnSolveHandler, makeEqnSolveHandler, Solve, assemble, weno_rk3, Problem, Batch, Server,
 )
 
 __version__ = "0.1.0"

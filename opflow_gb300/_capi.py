@@ -60,6 +60,22 @@ class ProblemDesc(C.Structure):
                 ("alpha", C.c_double), ("beta", C.c_double)]
 
 
+class Request(C.Structure):
+    _fields_ = [("problem", ProblemDesc), ("steps", C.c_int), ("f", C.POINTER(C.c_double)), ("x_out", C.POINTER(C.c_double))]
+
+
+class RequestResult(C.Structure):
+    _fields_ = [("id", C.c_longlong), ("status", C.c_int), ("iterations", C.c_int), ("solves", C.c_int), ("rel_residual", C.c_double),
+                ("queue_ms", C.c_double), ("latency_ms", C.c_double)]
+
+
+class ServeStats(C.Structure):
+    _fields_ = [("submitted", C.c_longlong), ("completed", C.c_longlong), ("solves", C.c_longlong), ("p50_ms", C.c_double),
+                ("p99_ms", C.c_double), ("mean_ms", C.c_double), ("max_ms", C.c_double), ("elapsed_s", C.c_double),
+                ("solves_per_s", C.c_double), ("max_active_seen", C.c_int), ("graph_launches", C.c_longlong),
+                ("compositions", C.c_longlong)]
+
+
 class OpflowError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__("%s: %s" % (STATUS_NAMES.get(code, code), msg))
@@ -104,6 +120,12 @@ _SIGS = {
     "opflow_batch_set": [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_size_t],
     "opflow_batch_get": [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.c_size_t],
     "opflow_batch_destroy": [C.c_void_p],
+    "opflow_server_create": [C.c_void_p, C.POINTER(SolveParams), C.c_size_t, C.c_int, C.POINTER(C.c_void_p)],
+    "opflow_server_submit": [C.c_void_p, C.POINTER(Request), C.POINTER(C.c_longlong)],
+    "opflow_server_result": [C.c_void_p, C.c_longlong, C.c_int, C.POINTER(C.c_int), C.POINTER(RequestResult)],
+    "opflow_server_drain": [C.c_void_p],
+    "opflow_server_stats": [C.c_void_p, C.POINTER(ServeStats)],
+    "opflow_server_destroy": [C.c_void_p],
     "opflow_residual_norms_noalloc": [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_void_p, C.c_void_p, C.c_void_p,
                                       C.c_void_p, C.c_void_p],
 }

@@ -710,3 +710,62 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+# ------------------------------------------------------------------------------------------------ serving
+class Server:
+    """Request loop with continuous batching (opflow_server_*): requests of any size join the running
+    batch at the next iteration boundary and leave when they converge; heat sessions (steps > 1) stay
+    resident between their steps."""
+
+    def __init__(self, params=None, hbm_budget=0, max_active=64, ctx=None):
+        self.ctx = ctx or default_context()
+        self.params = params or StructSolverParams(precision="mixed")
+        p = self.params.to_c()
+        h = C.c_void_p()
+        check(lib().opflow_server_create(self.ctx.handle, C.byref(p), int(hbm_budget), int(max_active), C.byref(h)))
+        self.handle = h
+        self._keep = {}
+
+    def submit(self, problem, f, steps=1, out=None):
+        f = np.ascontiguousarray(f, dtype=np.float64).reshape(-1)
+        req = capi.Request()
+        req.problem = problem.to_c()
+        req.steps = int(steps)
+        req.f = f.ctypes.data_as(C.POINTER(C.c_double))
+        if out is not None:
+            assert out.dtype == np.float64 and out.flags["C_CONTIGUOUS"]
+            req.x_out = out.ctypes.data_as(C.POINTER(C.c_double))
+        rid = C.c_longlong(0)
+        check(lib().opflow_server_submit(self.handle, C.byref(req), C.byref(rid)))
+        self._keep[rid.value] = (f, out)
+        return rid.value
+
+    def result(self, rid, wait=True):
+        res = capi.RequestResult()
+        done = C.c_int(0)
+        check(lib().opflow_server_result(self.handle, rid, int(wait), C.byref(done), C.byref(res)))
+        if not done.value:
+            return None
+        self._keep.pop(rid, None)
+        return {"id": res.id, "status": res.status, "iterations": res.iterations, "solves": res.solves,
+                "rel_residual": res.rel_residual, "queue_ms": res.queue_ms, "latency_ms": res.latency_ms}
+
+    def drain(self):
+        check(lib().opflow_server_drain(self.handle))
+
+    def stats(self):
+        st = capi.ServeStats()
+        check(lib().opflow_server_stats(self.handle, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in capi.ServeStats._fields_}
+
+    def close(self):
+        if getattr(self, "handle", None) and not _exiting[0]:
+            lib().opflow_server_destroy(self.handle)
+        self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

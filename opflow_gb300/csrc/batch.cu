@@ -12,7 +12,7 @@
 namespace opg {
 
 // alpha*e - beta*(d2<0>(e) + ... ) - f, slots: 0 = e (the unknown), 1 = f
-static std::vector<opflow_node> helmholtz_tree(int ndim, double alpha, double beta) {
+std::vector<opflow_node> helmholtz_tree(int ndim, double alpha, double beta) {
     std::vector<opflow_node> t;
     auto add = [&](int kind, int a, int b, int dim, int field, double v) {
         opflow_node n{kind, a, b, dim, field, v};
@@ -36,6 +36,8 @@ static std::vector<opflow_node> helmholtz_tree(int ndim, double alpha, double be
     return t;
 }
 
+int batch_problem_fields(opflow_ctx ctx, const opflow_problem_desc& pd, opflow_field* tgt, opflow_field* rhs);
+
 }  // namespace opg
 
 using namespace opg;
@@ -47,7 +49,7 @@ struct opflow_batch_s {
     opflow_solve_params params;
 };
 
-static int batch_problem_fields(opflow_ctx ctx, const opflow_problem_desc& pd, opflow_field* tgt, opflow_field* rhs) {
+int opg::batch_problem_fields(opflow_ctx ctx, const opflow_problem_desc& pd, opflow_field* tgt, opflow_field* rhs) {
     if (pd.ndim < 1 || pd.ndim > 3) return fail(OPFLOW_E_INVALID, "problem dimension %d", pd.ndim);
     if (pd.bc != OPFLOW_BC_DIRC && pd.bc != OPFLOW_BC_NEUM) return fail(OPFLOW_E_INVALID, "problem bc must be Dirichlet or Neumann");
     std::vector<double> xs[3], dxs[3];

@@ -1,0 +1,394 @@
+// Request server: continuous batching of independent solves and stateful heat sessions.
+//
+// Every admitted request owns a resident single-problem system (its multigrid hierarchy, Krylov
+// vectors and fields, in its own arena).  The worker thread composes the active requests into one
+// batch table (mg_compose) and replays one recorded flexible-PCG iteration for all of them; a request
+// joins at the next iteration boundary (seeded so that its first batched iteration only forms
+// z = M r and p = z) and leaves as soon as it converges, so requests of different sizes that arrive at
+// different times share every launch while they overlap.  A heat session restarts in place after each
+// step (b := x, no recomposition).  Admission is bounded by an HBM budget and a batch size.
+#include "solver.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <deque>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+
+namespace opg {
+
+using Clock = std::chrono::steady_clock;
+
+double mg_sum(opflow_ctx ctx, const double* v, long long n);
+void mg_add_scalar(opflow_ctx ctx, double* v, long long n, double a);
+std::vector<opflow_node> helmholtz_tree(int ndim, double alpha, double beta);
+int batch_problem_fields(opflow_ctx ctx, const opflow_problem_desc& pd, opflow_field* tgt, opflow_field* rhs);
+
+struct Req {
+    long long id = 0;
+    opflow_problem_desc pd{};
+    int steps = 1;
+    std::vector<double> f;
+    double* x_out = nullptr;
+    Clock::time_point t_submit, t_admit, t_done;
+    MGSystem* sys = nullptr;
+    opflow_field t = nullptr, rhs = nullptr;
+    size_t bytes = 0;
+    int steps_done = 0;
+    int iters = 0;
+    double rel = 0.;
+    int status = OPFLOW_OK;
+    bool pinned = false;
+    bool done = false;
+    long long N = 0;
+};
+
+static size_t estimate_bytes(const opflow_problem_desc& pd) {
+    double n = 1.;
+    for (int d = 0; d < pd.ndim; ++d) n *= (double) (pd.n[d] + 2);
+    return (size_t) (n * 240.0) + (8u << 20);
+}
+
+}  // namespace opg
+
+using namespace opg;
+
+struct opflow_server_s {
+    opflow_ctx_s own_ctx;  // private stream and scratch on the caller's device
+    opflow_solve_params params;
+    size_t budget = 0, used = 0;
+    int max_active = 64;
+    std::thread worker;
+    std::mutex mu;
+    std::condition_variable cv, cv_done;
+    std::deque<Req*> pending;
+    std::vector<Req*> active;
+    std::unordered_map<long long, Req*> reqs;
+    bool stop = false;
+    long long next_id = 1;
+    MGSystem comp;
+    bool dirty = true;
+    std::vector<Scal> state;  // per active request, host copy
+    // stats
+    std::vector<double> lat;
+    long long submitted = 0, completed = 0, solves = 0, compositions = 0;
+    int max_active_seen = 0;
+    Clock::time_point t_first, t_last;
+    bool have_first = false;
+    std::string error;
+};
+
+static void release_req(Req* r) {
+    if (r->sys) { mg_destroy(r->sys); r->sys = nullptr; }
+    if (r->t) { opflow_field_destroy(r->t); r->t = nullptr; }
+    if (r->rhs) { opflow_field_destroy(r->rhs); r->rhs = nullptr; }
+}
+
+// hierarchy, right-hand side, pinning, and the seed of the Krylov scalars
+static int setup_req(opflow_server S, Req* r, Scal* seed) {
+    opflow_ctx ctx = &S->own_ctx;
+    OPG_TRY(batch_problem_fields(ctx, r->pd, &r->t, &r->rhs));
+    r->sys = new MGSystem();
+    MGSystem* M = r->sys;
+    M->ctx = ctx;
+    M->precision = S->params.precision;
+    M->pre = S->params.pre_sweeps;
+    M->post = S->params.post_sweeps;
+    M->coarse_max = S->params.coarse_max > 0 ? S->params.coarse_max : 64;
+    M->tol = S->params.tol;
+    M->max_iter = S->params.max_iter;
+    M->arena.block_hint = 4u << 20;
+    std::vector<opflow_node> tree = helmholtz_tree(r->pd.ndim, r->pd.alpha, r->pd.beta);
+    opflow_field leaves[2] = {r->t, r->rhs};
+    OPG_TRY(mg_add_problem(M, r->t, tree.data(), (int) tree.size(), leaves, 2, 0));
+    OPG_TRY(mg_finalize(M));
+    r->N = M->probs[0].levels[0].N;
+    if ((long long) r->f.size() != r->N) return fail(OPFLOW_E_INVALID, "request %lld: f has %zu values, the problem %lld unknowns", r->id, r->f.size(), r->N);
+    OPG_CUDA(cudaMemcpyAsync(M->probs[0].b, r->f.data(), r->N * 8, cudaMemcpyHostToDevice, ctx->stream));
+    ProblemHost& P = M->probs[0];
+    r->pinned = P.singular && !P.has_dirichlet;
+    if (r->pinned) {
+        // the pinned system (first unknown held at 0): singular system with b[0] = -(sum of the others)
+        const double sb = mg_sum(ctx, P.b, r->N);
+        double b0 = 0.;
+        OPG_CUDA(cudaMemcpy(&b0, P.b, 8, cudaMemcpyDeviceToHost));
+        const double nb0 = -(sb - b0);
+        OPG_CUDA(cudaMemcpy(P.b, &nb0, 8, cudaMemcpyHostToDevice));
+    }
+    OPG_TRY(mg_prepare_problem(M, S->params.tol, M->dS));
+    OPG_CUDA(cudaMemcpyAsync(seed, M->dS, sizeof(Scal), cudaMemcpyDeviceToHost, ctx->stream));
+    OPG_CUDA(cudaStreamSynchronize(ctx->stream));
+    r->bytes = M->arena.total + (size_t) 2 * r->t->info.count * 8;
+    return OPFLOW_OK;
+}
+
+static void finish_req(opflow_server S, Req* r, int status) {
+    opflow_ctx ctx = &S->own_ctx;
+    if (status == OPFLOW_OK && r->sys) {
+        const KrylovDev& K = r->sys->kd_host[0];
+        if (r->pinned) {
+            double x0 = 0.;
+            cudaMemcpy(&x0, K.x, 8, cudaMemcpyDeviceToHost);
+            mg_add_scalar(ctx, K.x, r->N, -x0);
+        }
+        if (r->x_out) cudaMemcpyAsync(r->x_out, K.x, r->N * 8, cudaMemcpyDeviceToHost, ctx->stream);
+        cudaStreamSynchronize(ctx->stream);
+    }
+    r->status = status;
+    r->t_done = Clock::now();
+    std::lock_guard<std::mutex> lk(S->mu);
+    r->done = true;
+    S->completed++;
+    S->lat.push_back(std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count());
+    S->t_last = r->t_done;
+    S->cv_done.notify_all();
+}
+
+static void worker_loop(opflow_server S) {
+    cudaSetDevice(S->own_ctx.device);
+    const int ITERS = 2;
+    std::vector<Req*> retired;
+    for (;;) {
+        std::vector<Req*> admit;
+        {
+            std::unique_lock<std::mutex> lk(S->mu);
+            S->cv.wait(lk, [&] { return S->stop || !S->pending.empty() || !S->active.empty(); });
+            if (S->stop && S->pending.empty() && S->active.empty()) break;
+            while (!S->pending.empty() && (int) (S->active.size() + admit.size()) < S->max_active) {
+                Req* r = S->pending.front();
+                const size_t est = estimate_bytes(r->pd);
+                if (S->budget && S->used + est > S->budget && !(S->active.empty() && admit.empty())) break;
+                S->pending.pop_front();
+                S->used += est;
+                r->bytes = est;
+                admit.push_back(r);
+            }
+        }
+        for (Req* r : admit) {
+            Scal seed{};
+            r->t_admit = Clock::now();
+            const int rc = setup_req(S, r, &seed);
+            if (rc) {
+                r->status = rc;
+                S->error = opflow_last_error();
+                release_req(r);
+                { std::lock_guard<std::mutex> lk(S->mu); S->used -= std::min(S->used, r->bytes); }
+                finish_req(S, r, rc);
+                continue;
+            }
+            S->active.push_back(r);
+            S->state.push_back(seed);
+            S->dirty = true;
+        }
+        if (S->active.empty()) continue;
+        if (S->dirty) {
+            std::vector<MGSystem*> parts;
+            for (Req* r : S->active) parts.push_back(r->sys);
+            if (mg_compose(&S->comp, parts, S->state) != OPFLOW_OK) {
+                S->error = opflow_last_error();
+                for (Req* r : S->active) { release_req(r); finish_req(S, r, OPFLOW_E_CUDA); }
+                S->active.clear();
+                S->state.clear();
+                continue;
+            }
+            S->compositions++;
+            S->dirty = false;
+            for (Req* r : retired) release_req(r);  // nothing in the new tables points at them
+            retired.clear();
+            S->max_active_seen = std::max(S->max_active_seen, (int) S->active.size());
+        }
+        // a few batched iterations, then the per-request scalars
+        if (mg_run_iterations(&S->comp, ITERS) != OPFLOW_OK) {
+            S->error = opflow_last_error();
+            for (Req* r : S->active) { release_req(r); finish_req(S, r, OPFLOW_E_CUDA); }
+            S->active.clear();
+            S->state.clear();
+            S->dirty = true;
+            continue;
+        }
+        cudaMemcpyAsync(S->state.data(), S->comp.dS, S->state.size() * sizeof(Scal), cudaMemcpyDeviceToHost, S->own_ctx.stream);
+        cudaStreamSynchronize(S->own_ctx.stream);
+        std::vector<Req*> keep;
+        std::vector<Scal> keep_state;
+        for (size_t i = 0; i < S->active.size(); ++i) {
+            Req* r = S->active[i];
+            Scal& st = S->state[i];
+            if (st.active) { keep.push_back(r); keep_state.push_back(st); continue; }
+            r->iters += std::max(0, st.iters);
+            r->rel = st.bb > 0 ? std::sqrt(st.rr / st.bb) : std::sqrt(st.rr);
+            r->steps_done++;
+            { std::lock_guard<std::mutex> lk(S->mu); S->solves++; }
+            const bool ok = r->rel <= S->params.tol;
+            if (ok && r->steps_done < r->steps) {
+                // next backward-Euler step: the solution becomes the right-hand side, same operator
+                const KrylovDev& K = r->sys->kd_host[0];
+                cudaMemcpyAsync(r->sys->probs[0].b, K.x, r->N * 8, cudaMemcpyDeviceToDevice, S->own_ctx.stream);
+                mg_prepare_problem(r->sys, S->params.tol, S->comp.dS + i);
+                cudaMemcpyAsync(&st, S->comp.dS + i, sizeof(Scal), cudaMemcpyDeviceToHost, S->own_ctx.stream);
+                cudaStreamSynchronize(S->own_ctx.stream);
+                keep.push_back(r);
+                keep_state.push_back(st);
+                continue;
+            }
+            finish_req(S, r, ok ? OPFLOW_OK : OPFLOW_E_NOT_CONVERGED);
+            { std::lock_guard<std::mutex> lk(S->mu); S->used -= std::min(S->used, r->bytes); }
+            retired.push_back(r);
+            S->dirty = true;
+        }
+        S->active.swap(keep);
+        S->state.swap(keep_state);
+        if (S->active.empty() && !retired.empty()) {
+            for (Req* r : retired) release_req(r);
+            retired.clear();
+        }
+    }
+    for (Req* r : retired) release_req(r);
+}
+
+extern "C" {
+
+int opflow_server_create(opflow_ctx ctx, const opflow_solve_params* params, size_t budget, int max_active, opflow_server* out) {
+    if (!ctx || !out) return fail(OPFLOW_E_INVALID, "null argument");
+    auto* S = new opflow_server_s();
+    S->own_ctx.device = ctx->device;
+    S->own_ctx.num_sms = ctx->num_sms;
+    if (cudaStreamCreateWithFlags(&S->own_ctx.stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete S;
+        return fail(OPFLOW_E_CUDA, "stream creation failed");
+    }
+    S->own_ctx.own_stream = true;
+    if (params) S->params = *params;
+    else opflow_solve_params_default(&S->params);
+    S->budget = budget;
+    S->max_active = max_active > 0 ? max_active : 64;
+    S->comp.ctx = &S->own_ctx;
+    S->comp.precision = S->params.precision;
+    S->comp.pre = S->params.pre_sweeps;
+    S->comp.post = S->params.post_sweeps;
+    S->comp.tol = S->params.tol;
+    S->comp.max_iter = S->params.max_iter;
+    S->comp.arena.block_hint = 1u << 20;
+    if (ensure_scratch(&S->own_ctx, 4096) != OPFLOW_OK) {
+        cudaStreamDestroy(S->own_ctx.stream);
+        delete S;
+        return OPFLOW_E_NOMEM;
+    }
+    S->worker = std::thread(worker_loop, S);
+    *out = S;
+    return OPFLOW_OK;
+}
+
+int opflow_server_submit(opflow_server S, const opflow_request* q, long long* id) {
+    if (!S || !q || !q->f) return fail(OPFLOW_E_INVALID, "null argument");
+    if (q->steps < 1) return fail(OPFLOW_E_INVALID, "steps must be >= 1");
+    const opflow_problem_desc& pd = q->problem;
+    if (pd.ndim < 1 || pd.ndim > 3) return fail(OPFLOW_E_INVALID, "bad problem dimension");
+    long long n = 1;
+    for (int d = 0; d < pd.ndim; ++d) {
+        if (pd.n[d] < 3) return fail(OPFLOW_E_INVALID, "problem extent");
+        const int unk = pd.loc == OPFLOW_CENTER ? pd.n[d] : (pd.bc == OPFLOW_BC_DIRC ? pd.n[d] - 2 : pd.n[d]);
+        n *= unk;
+    }
+    for (long long i = 0; i < n; ++i)
+        if (!std::isfinite(q->f[i])) return fail(OPFLOW_E_NAN, "non-finite value in the right-hand side at %lld", i);
+    auto* r = new Req();
+    r->pd = pd;
+    r->steps = q->steps;
+    r->f.assign(q->f, q->f + n);
+    r->x_out = q->x_out;
+    r->t_submit = Clock::now();
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        if (S->stop) { delete r; return fail(OPFLOW_E_INVALID, "server is shutting down"); }
+        r->id = S->next_id++;
+        S->reqs[r->id] = r;
+        S->pending.push_back(r);
+        S->submitted++;
+        if (!S->have_first) { S->t_first = r->t_submit; S->have_first = true; }
+    }
+    S->cv.notify_one();
+    if (id) *id = r->id;
+    return OPFLOW_OK;
+}
+
+int opflow_server_result(opflow_server S, long long id, int wait, int* done, opflow_request_result* out) {
+    if (!S) return fail(OPFLOW_E_INVALID, "null server");
+    std::unique_lock<std::mutex> lk(S->mu);
+    auto it = S->reqs.find(id);
+    if (it == S->reqs.end()) return fail(OPFLOW_E_INVALID, "unknown request %lld", id);
+    Req* r = it->second;
+    if (wait) S->cv_done.wait(lk, [&] { return r->done; });
+    if (done) *done = r->done;
+    if (r->done && out) {
+        out->id = r->id;
+        out->status = r->status;
+        out->iterations = r->iters;
+        out->solves = r->steps_done;
+        out->rel_residual = r->rel;
+        out->queue_ms = std::chrono::duration<double, std::milli>(r->t_admit - r->t_submit).count();
+        out->latency_ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
+    }
+    return OPFLOW_OK;
+}
+
+int opflow_server_drain(opflow_server S) {
+    if (!S) return fail(OPFLOW_E_INVALID, "null server");
+    std::unique_lock<std::mutex> lk(S->mu);
+    S->cv_done.wait(lk, [&] { return S->completed == S->submitted; });
+    return OPFLOW_OK;
+}
+
+int opflow_server_stats(opflow_server S, opflow_serve_stats* o) {
+    if (!S || !o) return fail(OPFLOW_E_INVALID, "null argument");
+    std::lock_guard<std::mutex> lk(S->mu);
+    std::memset(o, 0, sizeof *o);
+    o->submitted = S->submitted;
+    o->completed = S->completed;
+    o->solves = S->solves;
+    std::vector<double> l = S->lat;
+    if (!l.empty()) {
+        std::sort(l.begin(), l.end());
+        auto q = [&](double p) { return l[std::min(l.size() - 1, (size_t) std::ceil(p * l.size()) - (p > 0 ? 1 : 0))]; };
+        o->p50_ms = q(0.50);
+        o->p99_ms = q(0.99);
+        double s = 0;
+        for (double v : l) s += v;
+        o->mean_ms = s / l.size();
+        o->max_ms = l.back();
+    }
+    if (S->have_first && S->completed) {
+        o->elapsed_s = std::chrono::duration<double>(S->t_last - S->t_first).count();
+        o->solves_per_s = o->elapsed_s > 0 ? S->solves / o->elapsed_s : 0.;
+    }
+    o->max_active_seen = S->max_active_seen;
+    o->graph_launches = S->comp.graph_launches;
+    o->compositions = S->compositions;
+    return OPFLOW_OK;
+}
+
+int opflow_server_destroy(opflow_server S) {
+    if (!S) return OPFLOW_OK;
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        S->stop = true;
+    }
+    S->cv.notify_all();
+    if (S->worker.joinable()) S->worker.join();
+    for (auto& kv : S->reqs) {
+        release_req(kv.second);
+        delete kv.second;
+    }
+    if (S->comp.exec) cudaGraphExecDestroy(S->comp.exec);
+    S->comp.exec = nullptr;
+    S->comp.arena.release();
+    if (S->comp.h_active) cudaFreeHost(S->comp.h_active);
+    if (S->own_ctx.scratch) cudaFree(S->own_ctx.scratch);
+    cudaStreamDestroy(S->own_ctx.stream);
+    delete S;
+    return OPFLOW_OK;
+}
+
+}  // extern "C"

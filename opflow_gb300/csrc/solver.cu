@@ -147,7 +147,8 @@ static int gridN(opflow_ctx ctx, long long n) {
 void* Arena::alloc(size_t bytes) {
     bytes = (bytes + 255) & ~(size_t) 255;
     if (blocks.empty() || used + bytes > cap) {
-        size_t sz = std::max(bytes, (size_t) 256 << 20);
+        size_t sz = std::max(bytes, block_hint);
+        block_hint = std::min(block_hint * 2, (size_t) 256 << 20);
         void* p = nullptr;
         if (cudaMalloc(&p, sz) != cudaSuccess) return nullptr;
         blocks.push_back(p);
@@ -536,10 +537,11 @@ int mg_finalize(MGSystem* S) {
             }
             lv.push_back(D);
             const int li = base + (int) l;
-            rows(li, D, S->smooth_ch[l]);
+            if (!D.coarsest) rows(li, D, S->smooth_ch[l]);
             if (l > 0) rows(li, D, S->restrict_ch[l]);       // coarse rows of level l (restricted from l-1)
             if (!D.coarsest) rows(li, D, S->prolong_ch[l]);  // fine rows of level l (prolonged from l+1)
             if (D.coarsest && H.Ainv64) coarse_list.push_back(li);
+            if (D.coarsest && !H.Ainv64) rows(li, D, S->coarse_sm_ch);
         }
         KrylovDev K{};
         const size_t N0 = (size_t) P.levels[0].N;
@@ -595,13 +597,20 @@ int mg_finalize(MGSystem* S) {
         upload(S->restrict_ch[l], S->d_restrict[l]);
         upload(S->prolong_ch[l], S->d_prolong[l]);
     }
+    upload(S->coarse_sm_ch, S->d_coarse_sm);
     S->kd_host = kd;
+    S->lv_host = lv;
+    S->k0_host = k0;
+    S->nprob = (int) S->probs.size();
     if (!S->h_active) OPG_CUDA(cudaMallocHost(&S->h_active, sizeof(int)));
     OPG_CUDA(cudaStreamSynchronize(ctx->stream));
     return OPFLOW_OK;
 }
 
-// One V-cycle on the level-0 residuals of the active problems: z = M r.
+// One V-cycle on the level-0 residuals of the active problems: z = M r.  Each problem sees the same
+// sequence whatever else is in the batch: pre-smoothing on its levels 0..L-1, the direct solve (or,
+// without a dense inverse, pre+post smoothing) on its coarsest level L, prolongation and post-smoothing
+// back up.
 static int vcycle(MGSystem* S) {
     cudaStream_t s = S->ctx->stream;
     const int sms = S->ctx->num_sms;
@@ -611,16 +620,17 @@ static int vcycle(MGSystem* S) {
     for (int l = 0; l < S->nlevels; ++l) {
         if (l > 0) OPG_TRY(mg_launch_restrict(s, sms, f32, S->dL, S->d_restrict[l].ptr, S->d_restrict[l].n, sc));
         const ChunkList& C = S->d_smooth[l];
-        const bool last = l + 1 == S->nlevels;
-        // problems whose coarsest level is l with no dense inverse only smooth there (pre-smoothing)
         for (int it = 0; it < S->pre; ++it) {
             OPG_TRY(mg_launch_smooth(s, sms, f32, S->dL, C.ptr, C.n, 0, sc));
             OPG_TRY(mg_launch_smooth(s, sms, f32, S->dL, C.ptr, C.n, 1, sc));
         }
-        (void) last;
         if (S->d_prolong[l].n) OPG_TRY(mg_launch_residual(s, sms, f32, S->dL, S->d_prolong[l].ptr, S->d_prolong[l].n, sc));
     }
     OPG_TRY(mg_launch_coarse(s, sms, f32, S->dL, S->dcoarse, S->ncoarse, sc));
+    for (int it = 0; it < S->pre + S->post; ++it) {
+        OPG_TRY(mg_launch_smooth(s, sms, f32, S->dL, S->d_coarse_sm.ptr, S->d_coarse_sm.n, 0, sc));
+        OPG_TRY(mg_launch_smooth(s, sms, f32, S->dL, S->d_coarse_sm.ptr, S->d_coarse_sm.n, 1, sc));
+    }
     for (int l = S->nlevels - 2; l >= 0; --l) {
         OPG_TRY(mg_launch_prolong(s, sms, f32, S->dL, S->d_prolong[l].ptr, S->d_prolong[l].n, sc));
         const ChunkList& C = S->d_smooth[l];
@@ -637,7 +647,7 @@ static int iteration(MGSystem* S) {
     cudaStream_t s = S->ctx->stream;
     const int sms = S->ctx->num_sms;
     const bool f32 = S->precision == OPFLOW_PREC_MIXED;
-    const int np = (int) S->probs.size();
+    const int np = S->nprob;
     OPG_TRY(kr_launch_apply(s, sms, S->dL, S->dK, S->dk0, S->nk0, S->dS, S->partial, 1));  // q = A p
     OPG_TRY(kr_launch_reduce(s, sms, S->partial, S->dfirst, S->dcount, np, S->red));
     OPG_TRY(kr_launch_scalars(s, S->dS, S->red, np, 1, S->tol, S->max_iter, 1));
@@ -658,7 +668,7 @@ int mg_solve(MGSystem* S) {
     cudaStream_t s = S->ctx->stream;
     const int sms = S->ctx->num_sms;
     const bool f32 = S->precision == OPFLOW_PREC_MIXED;
-    const int np = (int) S->probs.size();
+    const int np = S->nprob;
     // r = b - A x; bb, rr -> active flags
     OPG_TRY(kr_launch_apply(s, sms, S->dL, S->dK, S->dk0, S->nk0, nullptr, S->partial, 0));
     OPG_TRY(kr_launch_reduce(s, sms, S->partial, S->dfirst, S->dcount, np, S->red));
@@ -671,23 +681,153 @@ int mg_solve(MGSystem* S) {
     OPG_TRY(kr_launch_count(s, S->dS, np, S->d_active));
     OPG_CUDA(cudaMemcpyAsync(S->h_active, S->d_active, sizeof(int), cudaMemcpyDeviceToHost, s));
     OPG_CUDA(cudaStreamSynchronize(s));
-    if (!S->exec) {
-        // record one iteration as a CUDA graph, replayed until every problem has converged
-        cudaGraph_t g;
-        OPG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-        int rc = iteration(S);
-        cudaError_t e = cudaStreamEndCapture(s, &g);
-        if (rc) return rc;
-        if (e != cudaSuccess) return fail(OPFLOW_E_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
-        e = cudaGraphInstantiate(&S->exec, g, 0);
-        cudaGraphDestroy(g);
-        if (e != cudaSuccess) { S->exec = nullptr; return fail(OPFLOW_E_CUDA, "graph instantiation failed: %s", cudaGetErrorString(e)); }
-    }
+    OPG_TRY(mg_iteration_graph(S));
     for (int it = 0; it < S->max_iter && *S->h_active > 0; ++it) {
         OPG_CUDA(cudaGraphLaunch(S->exec, s));
         S->graph_launches++;
         OPG_CUDA(cudaStreamSynchronize(s));
     }
+    return OPFLOW_OK;
+}
+
+// record one iteration of the whole batch as a CUDA graph (once per table layout)
+int mg_iteration_graph(MGSystem* S) {
+    if (S->exec) return OPFLOW_OK;
+    cudaStream_t s = S->ctx->stream;
+    cudaGraph_t g;
+    OPG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    int rc = iteration(S);
+    cudaError_t e = cudaStreamEndCapture(s, &g);
+    if (rc) return rc;
+    if (e != cudaSuccess) return fail(OPFLOW_E_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&S->exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) { S->exec = nullptr; return fail(OPFLOW_E_CUDA, "graph instantiation failed: %s", cudaGetErrorString(e)); }
+    return OPFLOW_OK;
+}
+
+// `iters` replays without a host synchronisation in between; the active count lands in h_active
+int mg_run_iterations(MGSystem* S, int iters) {
+    OPG_TRY(mg_iteration_graph(S));
+    for (int it = 0; it < iters; ++it) {
+        OPG_CUDA(cudaGraphLaunch(S->exec, S->ctx->stream));
+        S->graph_launches++;
+    }
+    return OPFLOW_OK;
+}
+
+__global__ void scal_seed(Scal* out, const double* red, double tol) {
+    Scal S{};
+    S.bb = red[0];
+    S.rr = red[1];
+    S.rz = 1.0;   // with p = 0 the next iteration takes alpha = 0 and only forms z = M r, p = z
+    S.alpha = 0.;
+    S.beta = 0.;
+    S.iters = -1;
+    S.active = (red[1] > tol * tol * red[0]) && red[0] > 0. ? 1 : 0;
+    *out = S;
+}
+
+int mg_prepare_problem(MGSystem* S, double tol, Scal* out_dev) {
+    cudaStream_t s = S->ctx->stream;
+    const int sms = S->ctx->num_sms;
+    const KrylovDev& K = S->kd_host[0];
+    const long long N = S->probs[0].levels[0].N;
+    OPG_TRY(kr_launch_apply(s, sms, S->dL, S->dK, S->dk0, S->nk0, nullptr, S->partial, 0));
+    OPG_TRY(kr_launch_reduce(s, sms, S->partial, S->dfirst, S->dcount, 1, S->red));
+    OPG_CUDA(cudaMemsetAsync(K.p, 0, N * sizeof(double), s));
+    scal_seed<<<1, 1, 0, s>>>(out_dev, S->red, tol);
+    OPG_LAUNCHED();
+    return check_launch("scal_seed");
+}
+
+// Composite tables over resident problems: level / problem indices are renumbered, memory is shared.
+int mg_compose(MGSystem* C, const std::vector<MGSystem*>& parts, const std::vector<Scal>& state) {
+    opflow_ctx ctx = C->ctx;
+    if (C->exec) { cudaGraphExecDestroy(C->exec); C->exec = nullptr; }
+    C->arena.release();
+    std::vector<LvlDev> lv;
+    std::vector<KrylovDev> kd;
+    std::vector<Chunk> k0;
+    std::vector<int> first, count, coarse_list;
+    C->nlevels = 0;
+    for (auto* P : parts) C->nlevels = std::max(C->nlevels, P->nlevels);
+    C->smooth_ch.assign(C->nlevels, {});
+    C->restrict_ch.assign(C->nlevels, {});
+    C->prolong_ch.assign(C->nlevels, {});
+    C->coarse_sm_ch.clear();
+    for (size_t q = 0; q < parts.size(); ++q) {
+        MGSystem* P = parts[q];
+        const int base = (int) lv.size();
+        for (size_t l = 0; l < P->lv_host.size(); ++l) {
+            LvlDev D = P->lv_host[l];
+            D.problem = (int) q;
+            if (D.coarse >= 0) D.coarse += base;
+            if (D.fine >= 0) D.fine += base;
+            lv.push_back(D);
+            if (D.coarsest && D.Ainv64) coarse_list.push_back(base + (int) l);
+        }
+        auto shift = [&](const std::vector<Chunk>& src, std::vector<Chunk>& dst) {
+            for (Chunk c : src) { c.lvl += base; dst.push_back(c); }
+        };
+        for (int l = 0; l < P->nlevels; ++l) {
+            shift(P->smooth_ch[l], C->smooth_ch[l]);
+            shift(P->restrict_ch[l], C->restrict_ch[l]);
+            shift(P->prolong_ch[l], C->prolong_ch[l]);
+        }
+        shift(P->coarse_sm_ch, C->coarse_sm_ch);
+        KrylovDev K = P->kd_host[0];
+        K.lvl0 = base;
+        kd.push_back(K);
+        first.push_back((int) k0.size());
+        shift(P->k0_host, k0);
+        count.push_back((int) P->k0_host.size());
+    }
+    C->nprob = (int) parts.size();
+    C->nlv = (int) lv.size();
+    const size_t np = std::max<size_t>(1, parts.size());
+    C->dL = (LvlDev*) C->arena.alloc(std::max<size_t>(1, lv.size()) * sizeof(LvlDev));
+    C->dK = (KrylovDev*) C->arena.alloc(np * sizeof(KrylovDev));
+    C->dS = (Scal*) C->arena.alloc(np * sizeof(Scal));
+    C->nk0 = (int) k0.size();
+    C->dk0 = (Chunk*) C->arena.alloc(std::max<size_t>(1, k0.size()) * sizeof(Chunk));
+    C->dfirst = (int*) C->arena.alloc(np * sizeof(int));
+    C->dcount = (int*) C->arena.alloc(np * sizeof(int));
+    C->partial = (double*) C->arena.alloc(std::max<size_t>(1, 2 * k0.size()) * sizeof(double));
+    C->red = (double*) C->arena.alloc(2 * np * sizeof(double));
+    C->dcoarse = (int*) C->arena.alloc(std::max<size_t>(1, coarse_list.size()) * sizeof(int));
+    C->ncoarse = (int) coarse_list.size();
+    C->d_active = (int*) C->arena.alloc(sizeof(int));
+    if (!C->dL || !C->dK || !C->dS || !C->dk0 || !C->dfirst || !C->dcount || !C->partial || !C->red || !C->dcoarse || !C->d_active)
+        return fail(OPFLOW_E_NOMEM, "batch tables");
+    cudaStream_t s = ctx->stream;
+    if (!lv.empty()) cudaMemcpyAsync(C->dL, lv.data(), lv.size() * sizeof(LvlDev), cudaMemcpyHostToDevice, s);
+    if (!kd.empty()) cudaMemcpyAsync(C->dK, kd.data(), kd.size() * sizeof(KrylovDev), cudaMemcpyHostToDevice, s);
+    if (!state.empty()) cudaMemcpyAsync(C->dS, state.data(), state.size() * sizeof(Scal), cudaMemcpyHostToDevice, s);
+    if (!k0.empty()) cudaMemcpyAsync(C->dk0, k0.data(), k0.size() * sizeof(Chunk), cudaMemcpyHostToDevice, s);
+    if (!first.empty()) cudaMemcpyAsync(C->dfirst, first.data(), first.size() * sizeof(int), cudaMemcpyHostToDevice, s);
+    if (!count.empty()) cudaMemcpyAsync(C->dcount, count.data(), count.size() * sizeof(int), cudaMemcpyHostToDevice, s);
+    if (!coarse_list.empty()) cudaMemcpyAsync(C->dcoarse, coarse_list.data(), coarse_list.size() * sizeof(int), cudaMemcpyHostToDevice, s);
+    auto upload = [&](std::vector<Chunk>& h, ChunkList& d) {
+        d.n = (int) h.size();
+        d.ptr = (Chunk*) C->arena.alloc(std::max<size_t>(1, h.size()) * sizeof(Chunk));
+        if (!h.empty()) cudaMemcpyAsync(d.ptr, h.data(), h.size() * sizeof(Chunk), cudaMemcpyHostToDevice, s);
+    };
+    C->d_smooth.assign(C->nlevels, {});
+    C->d_restrict.assign(C->nlevels, {});
+    C->d_prolong.assign(C->nlevels, {});
+    for (int l = 0; l < C->nlevels; ++l) {
+        upload(C->smooth_ch[l], C->d_smooth[l]);
+        upload(C->restrict_ch[l], C->d_restrict[l]);
+        upload(C->prolong_ch[l], C->d_prolong[l]);
+    }
+    upload(C->coarse_sm_ch, C->d_coarse_sm);
+    C->kd_host = kd;
+    C->lv_host = lv;
+    C->k0_host = k0;
+    C->composite = true;
+    if (!C->h_active) OPG_CUDA(cudaMallocHost(&C->h_active, sizeof(int)));
+    OPG_CUDA(cudaStreamSynchronize(s));  // the host vectors above must outlive their copies
     return OPFLOW_OK;
 }
 
@@ -702,6 +842,7 @@ void mg_destroy(MGSystem* S) {
     if (!S) return;
     cudaStreamSynchronize(S->ctx->stream);
     if (S->exec) cudaGraphExecDestroy(S->exec);
+    S->exec = nullptr;
     for (auto& P : S->probs)
         for (auto& L : P.levels) release_level_fields(L);
     S->arena.release();
@@ -710,7 +851,15 @@ void mg_destroy(MGSystem* S) {
 }
 
 // ================================================================================= single-problem API
-static double sum_device(opflow_ctx ctx, const double* v, long long n) {
+void mg_add_scalar(opflow_ctx ctx, double* v, long long n, double a) {
+    add_scalar<<<gridN(ctx, n), 256, 0, ctx->stream>>>(v, n, a);
+    OPG_LAUNCHED();
+}
+
+double mg_sum(opflow_ctx ctx, const double* v, long long n);
+static double sum_device(opflow_ctx ctx, const double* v, long long n) { return mg_sum(ctx, v, n); }
+
+double mg_sum(opflow_ctx ctx, const double* v, long long n) {
     double* part = (double*) ctx->scratch + 64;
     const int blocks = 256;
     sum_partials<<<blocks, 256, 0, ctx->stream>>>(v, n, part);

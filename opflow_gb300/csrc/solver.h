@@ -10,6 +10,7 @@ namespace opg {
 struct Arena {
     std::vector<void*> blocks;
     size_t cap = 0, used = 0, total = 0;
+    size_t block_hint = (size_t) 256 << 20;  // size of the next block (grows x2 up to 256 MiB)
     void* alloc(size_t bytes);
     void release();
 };
@@ -58,8 +59,12 @@ struct MGSystem {
     Arena arena;
     std::vector<ProblemHost> probs;
     int nlevels = 0, nlv = 0;
+    // smooth_ch[l]: rows of level l of the problems for which l is not the coarsest level;
+    // coarse_sm: rows of coarsest levels that have no dense inverse (they are smoothed instead)
     std::vector<std::vector<Chunk>> smooth_ch, restrict_ch, prolong_ch;
     std::vector<ChunkList> d_smooth, d_restrict, d_prolong;
+    std::vector<Chunk> coarse_sm_ch;
+    ChunkList d_coarse_sm;
     LvlDev* dL = nullptr;
     KrylovDev* dK = nullptr;
     Scal* dS = nullptr;
@@ -75,8 +80,20 @@ struct MGSystem {
     int* d_active = nullptr;  // device count of active problems (owned, so a recorded graph never dangles)
     cudaGraphExec_t exec = nullptr;
     long long graph_launches = 0;
+    int nprob = 0;                       // problems the device tables describe
+    // host copies of the device tables (for composing batches out of resident problems)
+    std::vector<LvlDev> lv_host;
+    std::vector<Chunk> k0_host;
+    bool composite = false;              // tables reference other systems' memory
 };
 
+// Device tables of a batch assembled from single-problem systems (the problems stay where they are);
+// state[i] seeds problem i's Krylov scalars.
+int mg_compose(MGSystem* C, const std::vector<MGSystem*>& parts, const std::vector<Scal>& state);
+int mg_iteration_graph(MGSystem* S);
+int mg_run_iterations(MGSystem* S, int iters);
+// r = b - A x, p = 0 and scalars for one problem so that the next batched iteration starts it
+int mg_prepare_problem(MGSystem* single, double tol, Scal* out);
 int mg_add_problem(MGSystem* S, opflow_field target, const opflow_node* nodes, int n_nodes, const opflow_field* leaves, int n_leaves, int unknown);
 int mg_finalize(MGSystem* S);
 int mg_solve(MGSystem* S);

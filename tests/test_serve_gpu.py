@@ -1,0 +1,95 @@
+"""Serving: continuous batching of independent solves and heat sessions.  A request's result must be
+bit-identical alone (one request at a time) and in the mix, and equal to the batched solve of the same
+problem; sessions equal their steps solved one after another."""
+import numpy as np
+import pytest
+
+from opflow_gb300 import _capi as capi
+from opflow_gb300 import api
+
+pytestmark = pytest.mark.gpu
+
+
+def mix(seed):
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for i in range(10):
+        if i % 3 == 2:
+            n = int(rng.integers(24, 40))
+            p = api.Problem([n, n, n], [1.0 / n] * 3, alpha=0.0, beta=1.0, loc=api.LocOnMesh.Center,
+                            bc=api.BCType.Dirc if i % 2 else api.BCType.Neum)
+            steps = 1
+        elif i % 3 == 1:
+            n = int(rng.integers(40, 200))
+            dt = 1e-3
+            p = api.Problem([n, n], [1.0 / n] * 2, alpha=1.0, beta=dt, loc=api.LocOnMesh.Center, bc=api.BCType.Dirc)
+            steps = 3
+        else:
+            n = int(rng.integers(60, 300))
+            p = api.Problem([n, n + 7], [1.0 / n, 1.0 / (n + 7)], alpha=0.0, beta=1.0, loc=api.LocOnMesh.Center,
+                            bc=api.BCType.Neum if i % 2 else api.BCType.Dirc)
+            steps = 1
+        size = int(np.prod(p.n))
+        f = rng.standard_normal(size)
+        if p.bc == api.BCType.Neum and p.alpha == 0.0:
+            f -= f.mean()
+        reqs.append((p, f, steps))
+    return reqs
+
+
+def run(server, reqs):
+    outs, ids = [], []
+    for p, f, steps in reqs:
+        out = np.zeros(f.size)
+        outs.append(out)
+        ids.append(server.submit(p, f, steps=steps, out=out))
+    res = [server.result(i) for i in ids]
+    return outs, res
+
+
+def test_server_mix_equals_alone_and_batch(ctx):
+    reqs = mix(3)
+    params = api.StructSolverParams(tol=1e-10, maxIter=100, precision="mixed")
+    s_mix = api.Server(params, max_active=8, ctx=ctx)
+    outs_mix, res_mix = run(s_mix, reqs)
+    st = s_mix.stats()
+    s_mix.close()
+    assert all(r["status"] == capi.OK for r in res_mix), res_mix
+    assert st["completed"] == len(reqs) and st["max_active_seen"] > 1
+    s_one = api.Server(params, max_active=1, ctx=ctx)
+    outs_one, res_one = run(s_one, reqs)
+    s_one.close()
+    for k in range(len(reqs)):
+        assert res_one[k]["iterations"] == res_mix[k]["iterations"], k
+        assert np.array_equal(outs_one[k], outs_mix[k]), k
+    # against the batched solve of the same problems (one-shot ones), and sessions step by step
+    for k, (p, f, steps) in enumerate(reqs):
+        B = api.Batch([p], api.StructSolverParams(tol=1e-10, maxIter=100, precision="mixed"), ctx)
+        x = np.zeros(f.size)
+        rhs = f
+        for _ in range(steps):
+            B.set(0, rhs, x)
+            s = B.solve()[0]
+            assert s.converged
+            x = B.get(0)
+            rhs = x
+        if p.bc == api.BCType.Neum and p.alpha == 0.0:
+            x = x - x[0]  # the server reports the pinned solution
+            assert outs_mix[k][0] == 0.0
+        assert np.abs(outs_mix[k] - x).max() <= 1e-9 * max(1.0, np.abs(x).max()), k
+
+
+def test_server_rejects_nan_and_respects_budget(ctx):
+    params = api.StructSolverParams(tol=1e-10, precision="mixed")
+    s = api.Server(params, hbm_budget=1, max_active=8, ctx=ctx)  # budget below one request: one at a time
+    p = api.Problem([64, 64], [1 / 64, 1 / 64], alpha=0.0, beta=1.0)
+    f = np.ones(64 * 64)
+    f[5] = np.nan
+    with pytest.raises(capi.OpflowError) as e:
+        s.submit(p, f)
+    assert e.value.code == capi.E_NAN
+    ids = [s.submit(p, np.random.default_rng(i).standard_normal(64 * 64)) for i in range(4)]
+    res = [s.result(i) for i in ids]
+    assert all(r["status"] == capi.OK for r in res)
+    assert s.stats()["max_active_seen"] == 1
+    s.close()
