@@ -290,7 +290,8 @@ def run_poisson2d(args, torch, api, capi, np, ctx, stream, world, rank, local):
     out = {}
     for prec in ("mixed", "fp64"):
         h = api.makeEqnSolveHandler(getter, p, api.StructSolverParams(tol=1e-10, maxIter=200, pinValue=True, staticMat=True,
-                                                                        precision=prec, zeroGuess=True))
+                                                                        precision=prec, zeroGuess=True, preSweeps=args.sweeps,
+                                                                        postSweeps=args.sweeps))
         for _ in range(args.warmup):
             st = h.solve()
         torch.cuda.synchronize()
@@ -363,7 +364,8 @@ def run_serve(args, torch, api, capi, np, ctx, stream, world, rank, local):
         q = lambda z: lat[min(len(lat) - 1, int(np.ceil(z * len(lat))) - 1)]
         return dict(solves_per_s=sum(r["solves"] for r in res) / wall, p50_ms=q(0.5), p99_ms=q(0.99), ok=ok, n=len(res),
                     iterations=sum(r["iterations"] for r in res), max_active_seen=st["max_active_seen"], wall_s=wall,
-                    compositions=st["compositions"])
+                    compositions=st["compositions"],
+                    worker_s={k: round(st[k], 4) for k in ("setup_s", "compose_s", "iterate_s", "retire_s")})
 
     # warm-up (allocator, graphs, kernels)
     served("mixed", 16, serve_mix(np, api, 3, 4))
@@ -415,7 +417,9 @@ def run_ours(args):
     from opflow_gb300 import api
     import numpy as np
     ctx = api.Context(local)
-    stream = torch.cuda.current_stream()
+    # a stream of its own (not the legacy default stream): kernels and events share it
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
 
     if args.workload in ("poisson2d", "serve"):
@@ -567,6 +571,7 @@ def main():
     ap.add_argument("--mode", default="fast", choices=["fast", "exact"])
     ap.add_argument("--grid", type=int, default=0, help="override the grid side (profiling a smaller case)")
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU baseline leg (profiling runs)")
+    ap.add_argument("--sweeps", type=int, default=2, help="poisson2d: red-black Gauss-Seidel sweeps before and after each coarsening")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -294,6 +294,9 @@ typedef struct {
     double elapsed_s, solves_per_s;
     int max_active_seen;
     long long graph_launches, compositions;
+    double setup_s, compose_s, iterate_s, retire_s; /* worker wall time: admitting requests (hierarchy
+                                                       setup), composing batch tables, batched iterations
+                                                       with their state read-back, retiring results     */
 } opflow_serve_stats;
 
 /* hbm_budget_bytes bounds the resident problems' memory (0: unbounded); max_active bounds the batch

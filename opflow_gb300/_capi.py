@@ -73,7 +73,8 @@ class ServeStats(C.Structure):
     _fields_ = [("submitted", C.c_longlong), ("completed", C.c_longlong), ("solves", C.c_longlong), ("p50_ms", C.c_double),
                 ("p99_ms", C.c_double), ("mean_ms", C.c_double), ("max_ms", C.c_double), ("elapsed_s", C.c_double),
                 ("solves_per_s", C.c_double), ("max_active_seen", C.c_int), ("graph_launches", C.c_longlong),
-                ("compositions", C.c_longlong)]
+                ("compositions", C.c_longlong), ("setup_s", C.c_double), ("compose_s", C.c_double), ("iterate_s", C.c_double),
+                ("retire_s", C.c_double)]
 
 
 class OpflowError(RuntimeError):

@@ -77,105 +77,79 @@ __device__ __forceinline__ bool active(const LvlDev* L, const Chunk& c, const Sc
 }
 
 // ------------------------------------------------------------------------------------ V-cycle pieces
+// Per-cell bodies, shared by the chunked kernels (large levels, a grid strides over row segments) and
+// the bottom kernel (small levels, one CTA walks every cell of a problem's level), so both give
+// bit-identical values.
+
 // r = b - A x
 template <typename T>
-__global__ void __launch_bounds__(256) mg_residual(const LvlDev* __restrict__ Ls, const Chunk* __restrict__ ch, int nch, const Scal* sc) {
-    for (int c = blockIdx.x; c < nch; c += gridDim.x) {
-        const Chunk C = ch[c];
-        if (!active(Ls, C, sc)) continue;
-        const LvlDev& L = Ls[C.lvl];
-        const T* x = Sel<T>::x(L);
-        const T* b = Sel<T>::b(L);
-        T* r = Sel<T>::r(L);
-        for (int t = threadIdx.x; t < C.cnt; t += blockDim.x) {
-            const int i = C.i0 + t;
-            const long long cell = cell_of(L, i, C.j, C.k);
-            T c0, offd;
-            stencil_parts<T>(L, x, i, C.j, C.k, cell, c0, offd);
-            r[cell] = b[cell] - (c0 * x[cell] + offd);
-        }
-    }
+__device__ __forceinline__ void cell_residual(const LvlDev& L, int i, int j, int k) {
+    const long long cell = cell_of(L, i, j, k);
+    const T* x = Sel<T>::x(L);
+    T c0, offd;
+    stencil_parts<T>(L, x, i, j, k, cell, c0, offd);
+    Sel<T>::r(L)[cell] = Sel<T>::b(L)[cell] - (c0 * x[cell] + offd);
 }
 
-// Red-black Gauss-Seidel half sweep (cells with (i+j+k)%2 == color), or for Jacobi levels:
-// color 0 computes r = b - A x, color 1 applies x += omega r / diag.
+// Gauss-Seidel update of one cell: x = (b - offd) / c0
 template <typename T>
-__global__ void __launch_bounds__(256) mg_smooth(const LvlDev* __restrict__ Ls, const Chunk* __restrict__ ch, int nch, int color, const Scal* sc) {
-    for (int c = blockIdx.x; c < nch; c += gridDim.x) {
-        const Chunk C = ch[c];
-        if (!active(Ls, C, sc)) continue;
-        const LvlDev& L = Ls[C.lvl];
-        T* x = Sel<T>::x(L);
-        const T* b = Sel<T>::b(L);
-        if (L.rbgs) {
-            const int first = (C.i0 + C.j + C.k + color) & 1;  // offset of the first cell of this color
-            for (int t = 2 * threadIdx.x + first; t < C.cnt; t += 2 * blockDim.x) {
-                const int i = C.i0 + t;
-                const long long cell = cell_of(L, i, C.j, C.k);
-                T c0, offd;
-                stencil_parts<T>(L, x, i, C.j, C.k, cell, c0, offd);
-                x[cell] = (b[cell] - offd) / c0;
-            }
-        } else {
-            T* r = Sel<T>::r(L);
-            for (int t = threadIdx.x; t < C.cnt; t += blockDim.x) {
-                const int i = C.i0 + t;
-                const long long cell = cell_of(L, i, C.j, C.k);
-                T c0, offd;
-                stencil_parts<T>(L, x, i, C.j, C.k, cell, c0, offd);
-                if (color == 0) r[cell] = b[cell] - (c0 * x[cell] + offd);
-                else x[cell] += (T) 0.8 * r[cell] / c0;
-            }
-        }
-    }
+__device__ __forceinline__ void cell_gs(const LvlDev& L, int i, int j, int k) {
+    const long long cell = cell_of(L, i, j, k);
+    T* x = Sel<T>::x(L);
+    T c0, offd;
+    stencil_parts<T>(L, x, i, j, k, cell, c0, offd);
+    x[cell] = (Sel<T>::b(L)[cell] - offd) / c0;
 }
 
-// coarse b = R r_fine, coarse x = 0; chunks are coarse rows
+// damped Jacobi in two phases: 0 forms r = b - A x, 1 applies x += 0.8 r / diag
 template <typename T>
-__global__ void __launch_bounds__(256) mg_restrict(const LvlDev* __restrict__ Ls, const Chunk* __restrict__ ch, int nch, const Scal* sc) {
-    for (int c = blockIdx.x; c < nch; c += gridDim.x) {
-        const Chunk C = ch[c];
-        if (!active(Ls, C, sc)) continue;
-        const LvlDev& Lc = Ls[C.lvl];
-        const LvlDev& Lf = Ls[Lc.fine];
-        const T* rf = Sel<T>::r(Lf);
-        T* bc = Sel<T>::b(Lc);
-        T* xc = Sel<T>::x(Lc);
-        for (int t = threadIdx.x; t < C.cnt; t += blockDim.x) {
-            const int I[3] = {C.i0 + t, C.j, C.k};
-            const long long cc = cell_of(Lc, I[0], I[1], I[2]);
-            T acc = 0;
-            if (!Lc.node) {
-                // average of the children that exist
-                int cnt = 0;
-                for (int dz = 0; dz < (Lc.ndim > 2 ? 2 : 1); ++dz)
-                    for (int dy = 0; dy < (Lc.ndim > 1 ? 2 : 1); ++dy)
-                        for (int dx = 0; dx < 2; ++dx) {
-                            const int fi = 2 * I[0] + dx, fj = 2 * I[1] + dy, fk = 2 * I[2] + dz;
-                            if (fi < Lf.n[0] && fj < Lf.n[1] && fk < Lf.n[2]) {
-                                acc += rf[cell_of(Lf, fi, fj, fk)];
-                                cnt++;
-                            }
-                        }
-                acc = acc / (T) cnt;
-            } else {
-                // full weighting on absolute node indices: coarse node I <-> fine node 2I
-                const int ga[3] = {Lc.lo[0] + I[0], Lc.lo[1] + I[1], Lc.lo[2] + I[2]};
-                const int rz = Lc.ndim > 2 ? 1 : 0, ry = Lc.ndim > 1 ? 1 : 0;
-                for (int dz = -rz; dz <= rz; ++dz)
-                    for (int dy = -ry; dy <= ry; ++dy)
-                        for (int dx = -1; dx <= 1; ++dx) {
-                            T w = dx == 0 ? (T) 0.5 : (T) 0.25;
-                            if (ry) w *= dy == 0 ? (T) 0.5 : (T) 0.25;
-                            if (rz) w *= dz == 0 ? (T) 0.5 : (T) 0.25;
-                            const int fi = 2 * ga[0] + dx - Lf.lo[0], fj = 2 * ga[1] + dy - Lf.lo[1], fk = 2 * ga[2] + dz - Lf.lo[2];
-                            if (fi >= 0 && fi < Lf.n[0] && fj >= 0 && fj < Lf.n[1] && fk >= 0 && fk < Lf.n[2]) acc += w * rf[cell_of(Lf, fi, fj, fk)];
-                        }
-            }
-            bc[cc] = acc;
-            xc[cc] = 0;
-        }
+__device__ __forceinline__ void cell_jacobi(const LvlDev& L, int i, int j, int k, int phase) {
+    const long long cell = cell_of(L, i, j, k);
+    T* x = Sel<T>::x(L);
+    T* r = Sel<T>::r(L);
+    T c0, offd;
+    stencil_parts<T>(L, x, i, j, k, cell, c0, offd);
+    if (phase == 0) r[cell] = Sel<T>::b(L)[cell] - (c0 * x[cell] + offd);
+    else x[cell] += (T) 0.8 * r[cell] / c0;
+}
+
+// coarse b = R r_fine at coarse cell I, coarse x = 0
+template <typename T>
+__device__ __forceinline__ void cell_restrict(const LvlDev* __restrict__ Ls, const LvlDev& Lc, int I0, int I1, int I2) {
+    const LvlDev& Lf = Ls[Lc.fine];
+    const T* rf = Sel<T>::r(Lf);
+    const int I[3] = {I0, I1, I2};
+    const long long cc = cell_of(Lc, I[0], I[1], I[2]);
+    T acc = 0;
+    if (!Lc.node) {
+        // average of the children that exist
+        int cnt = 0;
+        for (int dz = 0; dz < (Lc.ndim > 2 ? 2 : 1); ++dz)
+            for (int dy = 0; dy < (Lc.ndim > 1 ? 2 : 1); ++dy)
+                for (int dx = 0; dx < 2; ++dx) {
+                    const int fi = 2 * I[0] + dx, fj = 2 * I[1] + dy, fk = 2 * I[2] + dz;
+                    if (fi < Lf.n[0] && fj < Lf.n[1] && fk < Lf.n[2]) {
+                        acc += rf[cell_of(Lf, fi, fj, fk)];
+                        cnt++;
+                    }
+                }
+        acc = acc / (T) cnt;
+    } else {
+        // full weighting on absolute node indices: coarse node I <-> fine node 2I
+        const int ga[3] = {Lc.lo[0] + I[0], Lc.lo[1] + I[1], Lc.lo[2] + I[2]};
+        const int rz = Lc.ndim > 2 ? 1 : 0, ry = Lc.ndim > 1 ? 1 : 0;
+        for (int dz = -rz; dz <= rz; ++dz)
+            for (int dy = -ry; dy <= ry; ++dy)
+                for (int dx = -1; dx <= 1; ++dx) {
+                    T w = dx == 0 ? (T) 0.5 : (T) 0.25;
+                    if (ry) w *= dy == 0 ? (T) 0.5 : (T) 0.25;
+                    if (rz) w *= dz == 0 ? (T) 0.5 : (T) 0.25;
+                    const int fi = 2 * ga[0] + dx - Lf.lo[0], fj = 2 * ga[1] + dy - Lf.lo[1], fk = 2 * ga[2] + dz - Lf.lo[2];
+                    if (fi >= 0 && fi < Lf.n[0] && fj >= 0 && fj < Lf.n[1] && fk >= 0 && fk < Lf.n[2]) acc += w * rf[cell_of(Lf, fi, fj, fk)];
+                }
     }
+    Sel<T>::b(Lc)[cc] = acc;
+    Sel<T>::x(Lc)[cc] = 0;
 }
 
 // value of a coarse unknown for interpolation, with the boundary ghost rules
@@ -198,6 +172,117 @@ __device__ __forceinline__ T coarse_at(const LvlDev& Lc, const T* xc, int I0, in
     return xc[cell_of(Lc, I[0], I[1], I[2])];
 }
 
+// fine x += P x_coarse at fine cell f
+template <typename T>
+__device__ __forceinline__ void cell_prolong(const LvlDev* __restrict__ Ls, const LvlDev& Lf, int f0, int f1, int f2) {
+    const LvlDev& Lc = Ls[Lf.coarse];
+    T* xf = Sel<T>::x(Lf);
+    const T* xc = Sel<T>::x(Lc);
+    const int f[3] = {f0, f1, f2};
+    T acc = 0;
+    if (!Lc.node) {
+        // bilinear / trilinear on cell centres: 3/4 nearest coarse cell, 1/4 the next one
+        int I[3], J[3];
+        for (int d = 0; d < 3; ++d) {
+            I[d] = f[d] >> 1;
+            J[d] = (f[d] & 1) ? I[d] + 1 : I[d] - 1;
+        }
+        const int nz = Lc.ndim > 2 ? 2 : 1, ny = Lc.ndim > 1 ? 2 : 1;
+        for (int a = 0; a < nz; ++a)
+            for (int bb = 0; bb < ny; ++bb)
+                for (int e = 0; e < 2; ++e) {
+                    const T w = (e ? (T) 0.25 : (T) 0.75) * (Lc.ndim > 1 ? (bb ? (T) 0.25 : (T) 0.75) : (T) 1) *
+                                (Lc.ndim > 2 ? (a ? (T) 0.25 : (T) 0.75) : (T) 1);
+                    T s;
+                    const T v = coarse_at<T>(Lc, xc, e ? J[0] : I[0], Lc.ndim > 1 ? (bb ? J[1] : I[1]) : 0, Lc.ndim > 2 ? (a ? J[2] : I[2]) : 0, s);
+                    acc += w * s * v;
+                }
+    } else {
+        // linear interpolation on nodes: absolute fine node g <-> coarse node g/2
+        const int g[3] = {Lf.lo[0] + f[0], Lf.lo[1] + f[1], Lf.lo[2] + f[2]};
+        int c0[3], c1[3];
+        T w0[3], w1[3];
+        for (int d = 0; d < 3; ++d) {
+            if (d >= Lc.ndim) { c0[d] = c1[d] = 0; w0[d] = 1; w1[d] = 0; continue; }
+            if ((g[d] & 1) == 0) { c0[d] = c1[d] = g[d] / 2 - Lc.lo[d]; w0[d] = 1; w1[d] = 0; }
+            else { c0[d] = (g[d] - 1) / 2 - Lc.lo[d]; c1[d] = c0[d] + 1; w0[d] = w1[d] = (T) 0.5; }
+        }
+        for (int a = 0; a < 2; ++a)
+            for (int bb = 0; bb < 2; ++bb)
+                for (int e = 0; e < 2; ++e) {
+                    const T w = (e ? w1[0] : w0[0]) * (bb ? w1[1] : w0[1]) * (a ? w1[2] : w0[2]);
+                    if (w == (T) 0) continue;
+                    const int I0 = e ? c1[0] : c0[0], I1 = bb ? c1[1] : c0[1], I2 = a ? c1[2] : c0[2];
+                    bool in = I0 >= 0 && I0 < Lc.n[0] && I1 >= 0 && I1 < Lc.n[1] && I2 >= 0 && I2 < Lc.n[2];
+                    if (in) acc += w * xc[cell_of(Lc, I0, I1, I2)];
+                    else {
+                        T s;
+                        const T v = coarse_at<T>(Lc, xc, I0, I1, I2, s);
+                        // outside a Dirichlet boundary the coarse correction is 0
+                        bool zero = false;
+                        const int II[3] = {I0, I1, I2};
+                        for (int d = 0; d < Lc.ndim; ++d)
+                            if ((II[d] < 0 && Lc.gh_lo[d] == GH_ZERO) || (II[d] >= Lc.n[d] && Lc.gh_hi[d] == GH_ZERO)) zero = true;
+                        if (!zero) acc += w * s * v;
+                    }
+                }
+    }
+    xf[cell_of(Lf, f[0], f[1], f[2])] += acc;
+}
+
+// coarsest level: x = Ainv b (dense, accumulated in float64), rows t0, t0+dt, ...
+template <typename T>
+__device__ __forceinline__ void coarse_rows(const LvlDev& L, int t0, int dt) {
+    const T* b = Sel<T>::b(L);
+    T* x = Sel<T>::x(L);
+    const int N = (int) L.N;
+    for (int row = t0; row < N; row += dt) {
+        double acc = 0.;
+        const double* Ar = L.Ainv64 + (long long) row * N;
+        for (int col = 0; col < N; ++col) acc = fma(Ar[col], (double) b[col], acc);
+        x[row] = (T) acc;
+    }
+}
+
+// ---- chunked kernels (large levels)
+template <typename T>
+__global__ void __launch_bounds__(256) mg_residual(const LvlDev* __restrict__ Ls, const Chunk* __restrict__ ch, int nch, const Scal* sc) {
+    for (int c = blockIdx.x; c < nch; c += gridDim.x) {
+        const Chunk C = ch[c];
+        if (!active(Ls, C, sc)) continue;
+        const LvlDev& L = Ls[C.lvl];
+        for (int t = threadIdx.x; t < C.cnt; t += blockDim.x) cell_residual<T>(L, C.i0 + t, C.j, C.k);
+    }
+}
+
+// Red-black Gauss-Seidel half sweep (cells with (i+j+k)%2 == color), or for Jacobi levels:
+// color 0 computes r = b - A x, color 1 applies x += omega r / diag.
+template <typename T>
+__global__ void __launch_bounds__(256) mg_smooth(const LvlDev* __restrict__ Ls, const Chunk* __restrict__ ch, int nch, int color, const Scal* sc) {
+    for (int c = blockIdx.x; c < nch; c += gridDim.x) {
+        const Chunk C = ch[c];
+        if (!active(Ls, C, sc)) continue;
+        const LvlDev& L = Ls[C.lvl];
+        if (L.rbgs) {
+            const int first = (C.i0 + C.j + C.k + color) & 1;  // offset of the first cell of this color
+            for (int t = 2 * threadIdx.x + first; t < C.cnt; t += 2 * blockDim.x) cell_gs<T>(L, C.i0 + t, C.j, C.k);
+        } else {
+            for (int t = threadIdx.x; t < C.cnt; t += blockDim.x) cell_jacobi<T>(L, C.i0 + t, C.j, C.k, color);
+        }
+    }
+}
+
+// coarse b = R r_fine, coarse x = 0; chunks are coarse rows
+template <typename T>
+__global__ void __launch_bounds__(256) mg_restrict(const LvlDev* __restrict__ Ls, const Chunk* __restrict__ ch, int nch, const Scal* sc) {
+    for (int c = blockIdx.x; c < nch; c += gridDim.x) {
+        const Chunk C = ch[c];
+        if (!active(Ls, C, sc)) continue;
+        const LvlDev& Lc = Ls[C.lvl];
+        for (int t = threadIdx.x; t < C.cnt; t += blockDim.x) cell_restrict<T>(Ls, Lc, C.i0 + t, C.j, C.k);
+    }
+}
+
 // fine x += P x_coarse; chunks are fine rows
 template <typename T>
 __global__ void __launch_bounds__(256) mg_prolong(const LvlDev* __restrict__ Ls, const Chunk* __restrict__ ch, int nch, const Scal* sc) {
@@ -205,62 +290,7 @@ __global__ void __launch_bounds__(256) mg_prolong(const LvlDev* __restrict__ Ls,
         const Chunk C = ch[c];
         if (!active(Ls, C, sc)) continue;
         const LvlDev& Lf = Ls[C.lvl];
-        const LvlDev& Lc = Ls[Lf.coarse];
-        T* xf = Sel<T>::x(Lf);
-        const T* xc = Sel<T>::x(Lc);
-        for (int t = threadIdx.x; t < C.cnt; t += blockDim.x) {
-            const int f[3] = {C.i0 + t, C.j, C.k};
-            T acc = 0;
-            if (!Lc.node) {
-                // bilinear / trilinear on cell centres: 3/4 nearest coarse cell, 1/4 the next one
-                int I[3], J[3];
-                for (int d = 0; d < 3; ++d) {
-                    I[d] = f[d] >> 1;
-                    J[d] = (f[d] & 1) ? I[d] + 1 : I[d] - 1;
-                }
-                const int nz = Lc.ndim > 2 ? 2 : 1, ny = Lc.ndim > 1 ? 2 : 1;
-                for (int a = 0; a < nz; ++a)
-                    for (int bb = 0; bb < ny; ++bb)
-                        for (int e = 0; e < 2; ++e) {
-                            const T w = (e ? (T) 0.25 : (T) 0.75) * (Lc.ndim > 1 ? (bb ? (T) 0.25 : (T) 0.75) : (T) 1) *
-                                        (Lc.ndim > 2 ? (a ? (T) 0.25 : (T) 0.75) : (T) 1);
-                            T s;
-                            const T v = coarse_at<T>(Lc, xc, e ? J[0] : I[0], Lc.ndim > 1 ? (bb ? J[1] : I[1]) : 0,
-                                                     Lc.ndim > 2 ? (a ? J[2] : I[2]) : 0, s);
-                            acc += w * s * v;
-                        }
-            } else {
-                // linear interpolation on nodes: absolute fine node g <-> coarse node g/2
-                const int g[3] = {Lf.lo[0] + f[0], Lf.lo[1] + f[1], Lf.lo[2] + f[2]};
-                int c0[3], c1[3];
-                T w0[3], w1[3];
-                for (int d = 0; d < 3; ++d) {
-                    if (d >= Lc.ndim) { c0[d] = c1[d] = 0; w0[d] = 1; w1[d] = 0; continue; }
-                    if ((g[d] & 1) == 0) { c0[d] = c1[d] = g[d] / 2 - Lc.lo[d]; w0[d] = 1; w1[d] = 0; }
-                    else { c0[d] = (g[d] - 1) / 2 - Lc.lo[d]; c1[d] = c0[d] + 1; w0[d] = w1[d] = (T) 0.5; }
-                }
-                for (int a = 0; a < 2; ++a)
-                    for (int bb = 0; bb < 2; ++bb)
-                        for (int e = 0; e < 2; ++e) {
-                            const T w = (e ? w1[0] : w0[0]) * (bb ? w1[1] : w0[1]) * (a ? w1[2] : w0[2]);
-                            if (w == (T) 0) continue;
-                            const int I0 = e ? c1[0] : c0[0], I1 = bb ? c1[1] : c0[1], I2 = a ? c1[2] : c0[2];
-                            bool in = I0 >= 0 && I0 < Lc.n[0] && I1 >= 0 && I1 < Lc.n[1] && I2 >= 0 && I2 < Lc.n[2];
-                            if (in) acc += w * xc[cell_of(Lc, I0, I1, I2)];
-                            else {
-                                T s;
-                                const T v = coarse_at<T>(Lc, xc, I0, I1, I2, s);
-                                // outside a Dirichlet boundary the coarse correction is 0
-                                bool zero = false;
-                                const int II[3] = {I0, I1, I2};
-                                for (int d = 0; d < Lc.ndim; ++d)
-                                    if ((II[d] < 0 && Lc.gh_lo[d] == GH_ZERO) || (II[d] >= Lc.n[d] && Lc.gh_hi[d] == GH_ZERO)) zero = true;
-                                if (!zero) acc += w * s * v;
-                            }
-                        }
-            }
-            xf[cell_of(Lf, f[0], f[1], f[2])] += acc;
-        }
+        for (int t = threadIdx.x; t < C.cnt; t += blockDim.x) cell_prolong<T>(Ls, Lf, C.i0 + t, C.j, C.k);
     }
 }
 
@@ -270,15 +300,81 @@ __global__ void __launch_bounds__(256) mg_coarse(const LvlDev* __restrict__ Ls, 
     for (int q = blockIdx.x; q < nlv; q += gridDim.x) {
         const LvlDev& L = Ls[lv[q]];
         if (sc && !sc[L.problem].active) continue;
-        const T* b = Sel<T>::b(L);
-        T* x = Sel<T>::x(L);
-        const int N = (int) L.N;
-        for (int row = threadIdx.x; row < N; row += blockDim.x) {
-            double acc = 0.;
-            const double* Ar = L.Ainv64 + (long long) row * N;
-            for (int col = 0; col < N; ++col) acc = fma(Ar[col], (double) b[col], acc);
-            x[row] = (T) acc;
+        coarse_rows<T>(L, threadIdx.x, blockDim.x);
+    }
+}
+
+// ---- bottom kernel (small levels)
+// Walks every cell of level L in x-fastest order; for a red-black color only the cells of that color.
+template <typename T, typename F>
+__device__ __forceinline__ void for_cells(const LvlDev& L, int color, F&& f) {
+    const int n0 = L.n[0], n1 = L.n[1];
+    for (int c = threadIdx.x; c < (int) L.N; c += blockDim.x) {
+        const int i = c % n0, jk = c / n0, j = jk % n1, k = jk / n1;
+        if (color >= 0 && ((i + j + k) & 1) != color) continue;
+        f(i, j, k);
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void bottom_smooth(const LvlDev& L, int color) {
+    if (L.rbgs) for_cells<T>(L, color, [&](int i, int j, int k) { cell_gs<T>(L, i, j, k); });
+    else for_cells<T>(L, -1, [&](int i, int j, int k) { cell_jacobi<T>(L, i, j, k, color); });
+    __syncthreads();
+}
+
+// The V-cycle below (and including) a problem's first small level, one CTA per problem: the
+// restriction into that level, pre-smoothing, residuals and restrictions down to the coarsest level,
+// the coarsest solve, then prolongation and post-smoothing back up - the same operations in the same
+// order as the chunked kernels, with a CTA barrier where those have a launch boundary.
+template <typename T>
+__global__ void __launch_bounds__(512) mg_bottom(const LvlDev* __restrict__ Ls, const int* __restrict__ top, int ntop, const Scal* sc, int pre,
+                                                 int post) {
+    for (int q = blockIdx.x; q < ntop; q += gridDim.x) {
+        const int s = top[q];
+        if (sc && !sc[Ls[s].problem].active) continue;
+        if (Ls[s].fine >= 0) {
+            const LvlDev& L = Ls[s];
+            for_cells<T>(L, -1, [&](int i, int j, int k) { cell_restrict<T>(Ls, L, i, j, k); });
+            __syncthreads();
         }
+        int l = s;
+        while (!Ls[l].coarsest) {
+            const LvlDev& L = Ls[l];
+            for (int it = 0; it < pre; ++it) {
+                bottom_smooth<T>(L, 0);
+                bottom_smooth<T>(L, 1);
+            }
+            for_cells<T>(L, -1, [&](int i, int j, int k) { cell_residual<T>(L, i, j, k); });
+            __syncthreads();
+            const LvlDev& Lc = Ls[L.coarse];
+            for_cells<T>(Lc, -1, [&](int i, int j, int k) { cell_restrict<T>(Ls, Lc, i, j, k); });
+            __syncthreads();
+            l = L.coarse;
+        }
+        {
+            const LvlDev& L = Ls[l];
+            if (L.Ainv64) {
+                coarse_rows<T>(L, threadIdx.x, blockDim.x);
+                __syncthreads();
+            } else {
+                for (int it = 0; it < pre + post; ++it) {
+                    bottom_smooth<T>(L, 0);
+                    bottom_smooth<T>(L, 1);
+                }
+            }
+        }
+        while (l != s) {
+            const LvlDev& Lf = Ls[Ls[l].fine];
+            for_cells<T>(Lf, -1, [&](int i, int j, int k) { cell_prolong<T>(Ls, Lf, i, j, k); });
+            __syncthreads();
+            for (int it = 0; it < post; ++it) {
+                bottom_smooth<T>(Lf, 1);
+                bottom_smooth<T>(Lf, 0);
+            }
+            l = Ls[l].fine;
+        }
+        __syncthreads();
     }
 }
 
@@ -522,6 +618,14 @@ int mg_launch_coarse(cudaStream_t s, int sms, bool f32, const LvlDev* L, const i
     else mg_coarse<double><<<std::min(nlv, sms * 4), 256, 0, s>>>(L, lv, nlv, sc);
     OPG_LAUNCHED();
     return check_launch("mg_coarse");
+}
+int mg_launch_bottom(cudaStream_t s, int sms, bool f32, const LvlDev* L, const int* top, int ntop, const Scal* sc, int pre, int post) {
+    if (ntop <= 0) return OPFLOW_OK;
+    const int g = std::min(ntop, sms * 4);
+    if (f32) mg_bottom<float><<<g, 512, 0, s>>>(L, top, ntop, sc, pre, post);
+    else mg_bottom<double><<<g, 512, 0, s>>>(L, top, ntop, sc, pre, post);
+    OPG_LAUNCHED();
+    return check_launch("mg_bottom");
 }
 int kr_launch_apply(cudaStream_t s, int sms, const LvlDev* L, const KrylovDev* K, const Chunk* ch, int nch, const Scal* sc, double* partial, int mode) {
     if (nch <= 0) return OPFLOW_OK;

@@ -75,6 +75,7 @@ struct opflow_server_s {
     // stats
     std::vector<double> lat;
     long long submitted = 0, completed = 0, solves = 0, compositions = 0;
+    double setup_s = 0, compose_s = 0, iterate_s = 0, retire_s = 0;  // worker wall time per phase
     int max_active_seen = 0;
     Clock::time_point t_first, t_last;
     bool have_first = false;
@@ -167,6 +168,12 @@ static void worker_loop(opflow_server S) {
                 admit.push_back(r);
             }
         }
+        auto add_since = [&](double& acc, Clock::time_point t) {
+            const double d = std::chrono::duration<double>(Clock::now() - t).count();
+            std::lock_guard<std::mutex> lk(S->mu);
+            acc += d;
+        };
+        const Clock::time_point t_setup = Clock::now();
         for (Req* r : admit) {
             Scal seed{};
             r->t_admit = Clock::now();
@@ -183,7 +190,9 @@ static void worker_loop(opflow_server S) {
             S->state.push_back(seed);
             S->dirty = true;
         }
+        add_since(S->setup_s, t_setup);
         if (S->active.empty()) continue;
+        const Clock::time_point t_compose = Clock::now();
         if (S->dirty) {
             std::vector<MGSystem*> parts;
             for (Req* r : S->active) parts.push_back(r->sys);
@@ -200,7 +209,9 @@ static void worker_loop(opflow_server S) {
             retired.clear();
             S->max_active_seen = std::max(S->max_active_seen, (int) S->active.size());
         }
+        add_since(S->compose_s, t_compose);
         // a few batched iterations, then the per-request scalars
+        const Clock::time_point t_iter = Clock::now();
         if (mg_run_iterations(&S->comp, ITERS) != OPFLOW_OK) {
             S->error = opflow_last_error();
             for (Req* r : S->active) { release_req(r); finish_req(S, r, OPFLOW_E_CUDA); }
@@ -211,6 +222,8 @@ static void worker_loop(opflow_server S) {
         }
         cudaMemcpyAsync(S->state.data(), S->comp.dS, S->state.size() * sizeof(Scal), cudaMemcpyDeviceToHost, S->own_ctx.stream);
         cudaStreamSynchronize(S->own_ctx.stream);
+        add_since(S->iterate_s, t_iter);
+        const Clock::time_point t_retire = Clock::now();
         std::vector<Req*> keep;
         std::vector<Scal> keep_state;
         for (size_t i = 0; i < S->active.size(); ++i) {
@@ -244,6 +257,7 @@ static void worker_loop(opflow_server S) {
             for (Req* r : retired) release_req(r);
             retired.clear();
         }
+        add_since(S->retire_s, t_retire);
     }
     for (Req* r : retired) release_req(r);
 }
@@ -366,6 +380,10 @@ int opflow_server_stats(opflow_server S, opflow_serve_stats* o) {
     o->max_active_seen = S->max_active_seen;
     o->graph_launches = S->comp.graph_launches;
     o->compositions = S->compositions;
+    o->setup_s = S->setup_s;
+    o->compose_s = S->compose_s;
+    o->iterate_s = S->iterate_s;
+    o->retire_s = S->retire_s;
     return OPFLOW_OK;
 }
 
@@ -383,6 +401,10 @@ int opflow_server_destroy(opflow_server S) {
     }
     if (S->comp.exec) cudaGraphExecDestroy(S->comp.exec);
     S->comp.exec = nullptr;
+    if (S->comp.solve_exec) cudaGraphExecDestroy(S->comp.solve_exec);
+    S->comp.solve_exec = nullptr;
+    if (S->comp.rec_stream) cudaStreamDestroy(S->comp.rec_stream);
+    S->comp.rec_stream = nullptr;
     S->comp.arena.release();
     if (S->comp.h_active) cudaFreeHost(S->comp.h_active);
     if (S->own_ctx.scratch) cudaFree(S->own_ctx.scratch);

@@ -20,6 +20,8 @@
 // replaced by minus the sum of the others, followed by a shift that makes the pinned unknown 0.
 #include "solver.h"
 
+#include <cstdlib>
+
 #include <chrono>
 #include <cmath>
 
@@ -484,6 +486,8 @@ int mg_finalize(MGSystem* S) {
     S->smooth_ch.assign(S->nlevels, {});
     S->restrict_ch.assign(S->nlevels, {});
     S->prolong_ch.assign(S->nlevels, {});
+    S->coarse_sm_ch.clear();
+    S->bottom_host.clear();
     std::vector<int> coarse_list;
     std::vector<Chunk> k0;
     std::vector<int> first, count;
@@ -493,9 +497,14 @@ int mg_finalize(MGSystem* S) {
             for (int j = 0; j < (L.ndim > 1 ? L.n[1] : 1); ++j)
                 for (int i0 = 0; i0 < L.n[0]; i0 += CH) out.push_back(Chunk{lvl_index, j, k, i0, std::min(CH, L.n[0] - i0)});
     };
+    if (const char* e = getenv("OPFLOW_MG_BOTTOM")) S->bottom_max = atoll(e);
     for (size_t p = 0; p < S->probs.size(); ++p) {
         ProblemHost& P = S->probs[p];
         const int base = (int) lv.size();
+        // first level small enough for the one-CTA bottom kernel (levels.size(): none)
+        size_t sp = P.levels.size();
+        for (size_t l = 0; l < P.levels.size(); ++l)
+            if (P.levels[l].N <= S->bottom_max) { sp = l; break; }
         for (size_t l = 0; l < P.levels.size(); ++l) {
             LevelHost& H = P.levels[l];
             LvlDev D{};
@@ -537,6 +546,8 @@ int mg_finalize(MGSystem* S) {
             }
             lv.push_back(D);
             const int li = base + (int) l;
+            if (l == sp) S->bottom_host.push_back(li);
+            if (l >= sp) continue;                                   // inside the bottom kernel
             if (!D.coarsest) rows(li, D, S->smooth_ch[l]);
             if (l > 0) rows(li, D, S->restrict_ch[l]);       // coarse rows of level l (restricted from l-1)
             if (!D.coarsest) rows(li, D, S->prolong_ch[l]);  // fine rows of level l (prolonged from l+1)
@@ -574,8 +585,13 @@ int mg_finalize(MGSystem* S) {
     S->partial = (double*) S->arena.alloc(std::max<size_t>(1, 2 * k0.size()) * sizeof(double));
     S->red = (double*) S->arena.alloc(2 * S->probs.size() * sizeof(double));
     S->dcoarse = (int*) S->arena.alloc(std::max<size_t>(1, coarse_list.size()) * sizeof(int));
-    S->d_active = (int*) S->arena.alloc(sizeof(int));
+    S->d_active = (int*) S->arena.alloc(2 * sizeof(int));  // [0] active count, [1] solve-loop counter
     S->ncoarse = (int) coarse_list.size();
+    S->coarse_host = coarse_list;
+    S->nbottom = (int) S->bottom_host.size();
+    S->dbottom = (int*) S->arena.alloc(std::max<size_t>(1, S->bottom_host.size()) * sizeof(int));
+    if (!S->dbottom) return fail(OPFLOW_E_NOMEM, "solver tables");
+    if (S->nbottom) cudaMemcpyAsync(S->dbottom, S->bottom_host.data(), S->bottom_host.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->stream);
     if (!S->dL || !S->dK || !S->dS || !S->dk0 || !S->partial || !S->red || !S->dcoarse) return fail(OPFLOW_E_NOMEM, "solver tables");
     cudaMemcpyAsync(S->dL, lv.data(), lv.size() * sizeof(LvlDev), cudaMemcpyHostToDevice, ctx->stream);
     cudaMemcpyAsync(S->dK, kd.data(), kd.size() * sizeof(KrylovDev), cudaMemcpyHostToDevice, ctx->stream);
@@ -611,8 +627,10 @@ int mg_finalize(MGSystem* S) {
 // sequence whatever else is in the batch: pre-smoothing on its levels 0..L-1, the direct solve (or,
 // without a dense inverse, pre+post smoothing) on its coarsest level L, prolongation and post-smoothing
 // back up.
+static cudaStream_t work_stream(const MGSystem* S) { return S->recording ? S->rec_stream : S->ctx->stream; }
+
 static int vcycle(MGSystem* S) {
-    cudaStream_t s = S->ctx->stream;
+    cudaStream_t s = work_stream(S);
     const int sms = S->ctx->num_sms;
     const bool f32 = S->precision == OPFLOW_PREC_MIXED;
     const Scal* sc = S->dS;
@@ -626,6 +644,7 @@ static int vcycle(MGSystem* S) {
         }
         if (S->d_prolong[l].n) OPG_TRY(mg_launch_residual(s, sms, f32, S->dL, S->d_prolong[l].ptr, S->d_prolong[l].n, sc));
     }
+    OPG_TRY(mg_launch_bottom(s, sms, f32, S->dL, S->dbottom, S->nbottom, sc, S->pre, S->post));
     OPG_TRY(mg_launch_coarse(s, sms, f32, S->dL, S->dcoarse, S->ncoarse, sc));
     for (int it = 0; it < S->pre + S->post; ++it) {
         OPG_TRY(mg_launch_smooth(s, sms, f32, S->dL, S->d_coarse_sm.ptr, S->d_coarse_sm.n, 0, sc));
@@ -643,8 +662,9 @@ static int vcycle(MGSystem* S) {
 }
 
 // One flexible-PCG iteration (everything after the first direction), recorded into a CUDA graph.
-static int iteration(MGSystem* S) {
-    cudaStream_t s = S->ctx->stream;
+// With `readback` the active count is also copied to the host (for callers that step iterations).
+static int iteration(MGSystem* S, bool readback) {
+    cudaStream_t s = work_stream(S);
     const int sms = S->ctx->num_sms;
     const bool f32 = S->precision == OPFLOW_PREC_MIXED;
     const int np = S->nprob;
@@ -660,16 +680,16 @@ static int iteration(MGSystem* S) {
     OPG_TRY(kr_launch_scalars(s, S->dS, S->red, np, 3, S->tol, S->max_iter, 1));
     OPG_TRY(kr_launch_pupdate(s, sms, S->dL, S->dK, S->dk0, S->nk0, S->dS, 0));
     OPG_TRY(kr_launch_count(s, S->dS, np, S->d_active));
-    OPG_CUDA(cudaMemcpyAsync(S->h_active, S->d_active, sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (readback) OPG_CUDA(cudaMemcpyAsync(S->h_active, S->d_active, sizeof(int), cudaMemcpyDeviceToHost, s));
     return OPFLOW_OK;
 }
 
-int mg_solve(MGSystem* S) {
-    cudaStream_t s = S->ctx->stream;
+// r = b - A x, the first preconditioned direction and the active count
+static int first_direction(MGSystem* S) {
+    cudaStream_t s = work_stream(S);
     const int sms = S->ctx->num_sms;
     const bool f32 = S->precision == OPFLOW_PREC_MIXED;
     const int np = S->nprob;
-    // r = b - A x; bb, rr -> active flags
     OPG_TRY(kr_launch_apply(s, sms, S->dL, S->dK, S->dk0, S->nk0, nullptr, S->partial, 0));
     OPG_TRY(kr_launch_reduce(s, sms, S->partial, S->dfirst, S->dcount, np, S->red));
     OPG_TRY(kr_launch_scalars(s, S->dS, S->red, np, 0, S->tol, S->max_iter, 1));
@@ -678,27 +698,146 @@ int mg_solve(MGSystem* S) {
     OPG_TRY(kr_launch_reduce(s, sms, S->partial, S->dfirst, S->dcount, np, S->red));
     OPG_TRY(kr_launch_scalars(s, S->dS, S->red, np, 4, S->tol, S->max_iter, 1));
     OPG_TRY(kr_launch_pupdate(s, sms, S->dL, S->dK, S->dk0, S->nk0, S->dS, 1));
-    OPG_TRY(kr_launch_count(s, S->dS, np, S->d_active));
-    OPG_CUDA(cudaMemcpyAsync(S->h_active, S->d_active, sizeof(int), cudaMemcpyDeviceToHost, s));
-    OPG_CUDA(cudaStreamSynchronize(s));
-    OPG_TRY(mg_iteration_graph(S));
-    for (int it = 0; it < S->max_iter && *S->h_active > 0; ++it) {
-        OPG_CUDA(cudaGraphLaunch(S->exec, s));
-        S->graph_launches++;
-        OPG_CUDA(cudaStreamSynchronize(s));
+    return kr_launch_count(s, S->dS, np, S->d_active);
+}
+
+// Loop control of the whole-solve graph.  Before the loop (reset) the counter starts at 0; after each
+// body it advances.  The body runs again while some problem is active and fewer than `max_loops`
+// bodies have run, so the loop ends even if the active flags never clear.
+__global__ void loop_control(cudaGraphConditionalHandle h, int* active_and_counter, int max_loops, int reset) {
+    const int c = reset ? 0 : active_and_counter[1] + 1;
+    active_and_counter[1] = c;
+    cudaGraphSetConditional(h, (active_and_counter[0] > 0 && c < max_loops) ? 1u : 0u);
+}
+
+// Records the whole solve - first direction, then a device-side while loop over iterations - as one
+// graph, so a solve is one launch with no host round trip per iteration.
+static int solve_graph(MGSystem* S) {
+    if (S->solve_exec) return OPFLOW_OK;
+    if (!S->rec_stream) OPG_CUDA(cudaStreamCreateWithFlags(&S->rec_stream, cudaStreamNonBlocking));
+    cudaStream_t s = S->rec_stream;
+    const int max_loops = std::max(1, S->max_iter + 1);
+    const uint64_t c0 = g_launches.load();
+    OPG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    S->recording = true;
+    cudaGraph_t g = nullptr, body = nullptr;
+    cudaGraphConditionalHandle h{};
+    int rc = first_direction(S);
+    cudaError_t e = cudaSuccess;
+    if (!rc) {
+        cudaStreamCaptureStatus st;
+        e = cudaStreamGetCaptureInfo(s, &st, nullptr, &g, nullptr, nullptr, nullptr);
+        if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault);
+        if (e == cudaSuccess) {
+            loop_control<<<1, 1, 0, s>>>(h, S->d_active, max_loops, 1);
+            OPG_LAUNCHED();
+            e = cudaGetLastError();
+        }
+        const cudaGraphNode_t* deps = nullptr;
+        const cudaGraphEdgeData* edata = nullptr;
+        size_t ndeps = 0;
+        if (e == cudaSuccess) e = cudaStreamGetCaptureInfo(s, &st, nullptr, &g, &deps, &edata, &ndeps);
+        cudaGraphNodeParams cp = {};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t cond = nullptr;
+        if (e == cudaSuccess) e = cudaGraphAddNode(&cond, g, deps, edata, ndeps, &cp);
+        if (e == cudaSuccess) {
+            body = cp.conditional.phGraph_out[0];
+            e = cudaStreamUpdateCaptureDependencies(s, &cond, nullptr, 1, cudaStreamSetCaptureDependencies);
+        }
     }
+    S->recording = false;
+    const uint64_t c1 = g_launches.load();
+    cudaGraph_t outer = nullptr;
+    const cudaError_t e_end = cudaStreamEndCapture(s, &outer);
+    if (rc || e != cudaSuccess || e_end != cudaSuccess) {
+        if (e_end == cudaSuccess && outer) cudaGraphDestroy(outer);
+        if (rc) return rc;
+        return fail(OPFLOW_E_CUDA, "recording the solve graph failed: %s", cudaGetErrorString(e != cudaSuccess ? e : e_end));
+    }
+    // the loop body: one iteration and the loop control
+    e = cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(outer);
+        return fail(OPFLOW_E_CUDA, "recording the solve loop body failed: %s", cudaGetErrorString(e));
+    }
+    S->recording = true;
+    rc = iteration(S, false);
+    if (!rc) {
+        loop_control<<<1, 1, 0, s>>>(h, S->d_active, max_loops, 0);
+        OPG_LAUNCHED();
+        e = cudaGetLastError();
+    }
+    S->recording = false;
+    const uint64_t c2 = g_launches.load();
+    g_launches.fetch_sub(c2 - c0);
+    S->first_kernels = (long long) (c1 - c0);
+    S->body_kernels = (long long) (c2 - c1);
+    cudaGraph_t body_out = nullptr;
+    const cudaError_t e_end2 = cudaStreamEndCapture(s, &body_out);
+    if (rc || e != cudaSuccess || e_end2 != cudaSuccess) {
+        cudaGraphDestroy(outer);
+        if (rc) return rc;
+        return fail(OPFLOW_E_CUDA, "recording the solve loop body failed: %s", cudaGetErrorString(e != cudaSuccess ? e : e_end2));
+    }
+    e = cudaGraphInstantiate(&S->solve_exec, outer, 0);
+    cudaGraphDestroy(outer);
+    if (e != cudaSuccess) {
+        S->solve_exec = nullptr;
+        return fail(OPFLOW_E_CUDA, "solve graph instantiation failed: %s", cudaGetErrorString(e));
+    }
+    return OPFLOW_OK;
+}
+
+// OPFLOW_SOLVE_GRAPHS=0 issues the same kernels one by one with a host-side loop (profilers then see
+// every kernel as its own launch)
+static bool solve_graphs_enabled() {
+    const char* e = getenv("OPFLOW_SOLVE_GRAPHS");
+    return !(e && e[0] == '0');
+}
+
+// Runs the whole solve as one graph launch on the caller's stream; mg_states reads the outcome.
+int mg_solve(MGSystem* S) {
+    if (!solve_graphs_enabled()) {
+        cudaStream_t s = S->ctx->stream;
+        OPG_TRY(first_direction(S));
+        OPG_CUDA(cudaMemcpyAsync(S->h_active, S->d_active, sizeof(int), cudaMemcpyDeviceToHost, s));
+        OPG_CUDA(cudaStreamSynchronize(s));
+        for (int it = 0; it < S->max_iter && *S->h_active > 0; ++it) {
+            OPG_TRY(iteration(S, true));
+            OPG_CUDA(cudaStreamSynchronize(s));
+        }
+        return OPFLOW_OK;
+    }
+    OPG_TRY(solve_graph(S));
+    OPG_CUDA(cudaGraphLaunch(S->solve_exec, S->ctx->stream));
+    S->graph_launches++;
+    g_launches.fetch_add((uint64_t) S->first_kernels);
+    S->solve_pending = true;
     return OPFLOW_OK;
 }
 
 // record one iteration of the whole batch as a CUDA graph (once per table layout)
 int mg_iteration_graph(MGSystem* S) {
     if (S->exec) return OPFLOW_OK;
-    cudaStream_t s = S->ctx->stream;
+    if (!S->rec_stream) OPG_CUDA(cudaStreamCreateWithFlags(&S->rec_stream, cudaStreamNonBlocking));
+    cudaStream_t s = S->rec_stream;
     cudaGraph_t g;
+    const uint64_t c0 = g_launches.load();
     OPG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    int rc = iteration(S);
+    S->recording = true;
+    int rc = iteration(S, true);
+    S->recording = false;
+    S->iter_kernels = (long long) (g_launches.load() - c0);
+    g_launches.fetch_sub((uint64_t) S->iter_kernels);
     cudaError_t e = cudaStreamEndCapture(s, &g);
-    if (rc) return rc;
+    if (rc) {
+        if (e == cudaSuccess) cudaGraphDestroy(g);
+        return rc;
+    }
     if (e != cudaSuccess) return fail(OPFLOW_E_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
     e = cudaGraphInstantiate(&S->exec, g, 0);
     cudaGraphDestroy(g);
@@ -712,6 +851,7 @@ int mg_run_iterations(MGSystem* S, int iters) {
     for (int it = 0; it < iters; ++it) {
         OPG_CUDA(cudaGraphLaunch(S->exec, S->ctx->stream));
         S->graph_launches++;
+        g_launches.fetch_add((uint64_t) S->iter_kernels);
     }
     return OPFLOW_OK;
 }
@@ -745,11 +885,12 @@ int mg_prepare_problem(MGSystem* S, double tol, Scal* out_dev) {
 int mg_compose(MGSystem* C, const std::vector<MGSystem*>& parts, const std::vector<Scal>& state) {
     opflow_ctx ctx = C->ctx;
     if (C->exec) { cudaGraphExecDestroy(C->exec); C->exec = nullptr; }
+    if (C->solve_exec) { cudaGraphExecDestroy(C->solve_exec); C->solve_exec = nullptr; }
     C->arena.release();
     std::vector<LvlDev> lv;
     std::vector<KrylovDev> kd;
     std::vector<Chunk> k0;
-    std::vector<int> first, count, coarse_list;
+    std::vector<int> first, count, coarse_list, bottom_list;
     C->nlevels = 0;
     for (auto* P : parts) C->nlevels = std::max(C->nlevels, P->nlevels);
     C->smooth_ch.assign(C->nlevels, {});
@@ -765,8 +906,9 @@ int mg_compose(MGSystem* C, const std::vector<MGSystem*>& parts, const std::vect
             if (D.coarse >= 0) D.coarse += base;
             if (D.fine >= 0) D.fine += base;
             lv.push_back(D);
-            if (D.coarsest && D.Ainv64) coarse_list.push_back(base + (int) l);
         }
+        for (int c : P->coarse_host) coarse_list.push_back(base + c);
+        for (int b : P->bottom_host) bottom_list.push_back(base + b);
         auto shift = [&](const std::vector<Chunk>& src, std::vector<Chunk>& dst) {
             for (Chunk c : src) { c.lvl += base; dst.push_back(c); }
         };
@@ -797,8 +939,12 @@ int mg_compose(MGSystem* C, const std::vector<MGSystem*>& parts, const std::vect
     C->red = (double*) C->arena.alloc(2 * np * sizeof(double));
     C->dcoarse = (int*) C->arena.alloc(std::max<size_t>(1, coarse_list.size()) * sizeof(int));
     C->ncoarse = (int) coarse_list.size();
-    C->d_active = (int*) C->arena.alloc(sizeof(int));
-    if (!C->dL || !C->dK || !C->dS || !C->dk0 || !C->dfirst || !C->dcount || !C->partial || !C->red || !C->dcoarse || !C->d_active)
+    C->coarse_host = coarse_list;
+    C->bottom_host = bottom_list;
+    C->nbottom = (int) bottom_list.size();
+    C->dbottom = (int*) C->arena.alloc(std::max<size_t>(1, bottom_list.size()) * sizeof(int));
+    C->d_active = (int*) C->arena.alloc(2 * sizeof(int));
+    if (!C->dL || !C->dK || !C->dS || !C->dk0 || !C->dfirst || !C->dcount || !C->partial || !C->red || !C->dcoarse || !C->d_active || !C->dbottom)
         return fail(OPFLOW_E_NOMEM, "batch tables");
     cudaStream_t s = ctx->stream;
     if (!lv.empty()) cudaMemcpyAsync(C->dL, lv.data(), lv.size() * sizeof(LvlDev), cudaMemcpyHostToDevice, s);
@@ -808,6 +954,7 @@ int mg_compose(MGSystem* C, const std::vector<MGSystem*>& parts, const std::vect
     if (!first.empty()) cudaMemcpyAsync(C->dfirst, first.data(), first.size() * sizeof(int), cudaMemcpyHostToDevice, s);
     if (!count.empty()) cudaMemcpyAsync(C->dcount, count.data(), count.size() * sizeof(int), cudaMemcpyHostToDevice, s);
     if (!coarse_list.empty()) cudaMemcpyAsync(C->dcoarse, coarse_list.data(), coarse_list.size() * sizeof(int), cudaMemcpyHostToDevice, s);
+    if (!bottom_list.empty()) cudaMemcpyAsync(C->dbottom, bottom_list.data(), bottom_list.size() * sizeof(int), cudaMemcpyHostToDevice, s);
     auto upload = [&](std::vector<Chunk>& h, ChunkList& d) {
         d.n = (int) h.size();
         d.ptr = (Chunk*) C->arena.alloc(std::max<size_t>(1, h.size()) * sizeof(Chunk));
@@ -834,7 +981,13 @@ int mg_compose(MGSystem* C, const std::vector<MGSystem*>& parts, const std::vect
 int mg_states(MGSystem* S, std::vector<Scal>& out) {
     out.resize(S->probs.size());
     OPG_CUDA(cudaMemcpyAsync(out.data(), S->dS, out.size() * sizeof(Scal), cudaMemcpyDeviceToHost, S->ctx->stream));
+    int ac[2] = {0, 0};
+    if (S->solve_pending) OPG_CUDA(cudaMemcpyAsync(ac, S->d_active, sizeof ac, cudaMemcpyDeviceToHost, S->ctx->stream));
     OPG_CUDA(cudaStreamSynchronize(S->ctx->stream));
+    if (S->solve_pending) {
+        g_launches.fetch_add((uint64_t) ((long long) ac[1] * S->body_kernels));
+        S->solve_pending = false;
+    }
     return OPFLOW_OK;
 }
 
@@ -843,6 +996,10 @@ void mg_destroy(MGSystem* S) {
     cudaStreamSynchronize(S->ctx->stream);
     if (S->exec) cudaGraphExecDestroy(S->exec);
     S->exec = nullptr;
+    if (S->solve_exec) cudaGraphExecDestroy(S->solve_exec);
+    S->solve_exec = nullptr;
+    if (S->rec_stream) cudaStreamDestroy(S->rec_stream);
+    S->rec_stream = nullptr;
     for (auto& P : S->probs)
         for (auto& L : P.levels) release_level_fields(L);
     S->arena.release();

@@ -75,11 +75,27 @@ struct MGSystem {
     double* red = nullptr;
     int* dcoarse = nullptr;
     int ncoarse = 0;
+    // Levels of at most bottom_max cells run inside one CTA per problem (mg_bottom): bottom_host lists
+    // each problem's first such level, coarse_host the coarsest levels above that size (chunked path);
+    // both in this system's level numbering
+    long long bottom_max = 4096;
+    std::vector<int> coarse_host, bottom_host;
+    int* dbottom = nullptr;
+    int nbottom = 0;
     std::vector<KrylovDev> kd_host;
     int* h_active = nullptr;
     int* d_active = nullptr;  // device count of active problems (owned, so a recorded graph never dangles)
-    cudaGraphExec_t exec = nullptr;
+    cudaGraphExec_t exec = nullptr;        // one iteration (stepped by the request server)
+    cudaGraphExec_t solve_exec = nullptr;  // a whole solve: first direction + device-side while loop
+    // private stream the iteration graph is recorded on: the caller's stream may be the legacy default
+    // stream, which cannot be captured; the recorded graph is then launched on the caller's stream
+    cudaStream_t rec_stream = nullptr;
+    bool recording = false;
     long long graph_launches = 0;
+    // kernels per recorded graph, added to the library's launch counter on every replay (capture itself
+    // launches nothing): one stepped iteration, the whole-solve prologue, one whole-solve loop body
+    long long iter_kernels = 0, first_kernels = 0, body_kernels = 0;
+    bool solve_pending = false;   // a whole-solve launch whose loop count is not yet counted
     int nprob = 0;                       // problems the device tables describe
     // host copies of the device tables (for composing batches out of resident problems)
     std::vector<LvlDev> lv_host;

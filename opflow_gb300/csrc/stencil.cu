@@ -12,6 +12,9 @@
 //           are exact integer sums, one 64x53-bit product per weight group, one rounding back.
 #include "stencil.h"
 
+#include <cstdlib>
+#include <cstring>
+
 namespace opg {
 
 __device__ __forceinline__ double ld3(const FieldView& f, int i, int j, int k) {
@@ -32,7 +35,17 @@ __device__ __forceinline__ double d2_exact(double l, double c, double r, double 
     return tdiv(__dsub_rn(a, b), h, y, p2);
 }
 
+// x * 2^(58-E) rounded to an integer.  For moderate E the scaling is an exact exponent add and the
+// rounding is the hardware's float64 -> int64 conversion (round to nearest even); values whose scaled
+// magnitude is below 2^-1022 (zeros and subnormals) give 0.  Extreme E take the integer path below
+// (round half away from zero).
 __device__ __forceinline__ long long fx_from(double x, int E) {
+    if (E > -900 && E < 1000) {
+        const int hi = __double2hiint(x), lo = __double2loint(x);
+        const int emin = max(0, E - 58);
+        if ((hi & 0x7FF00000) <= emin * (1 << 20)) return 0;
+        return __double2ll_rn(__hiloint2double(hi + (58 - E) * (1 << 20), lo));
+    }
     const unsigned long long b = (unsigned long long) __double_as_longlong(x);
     const int e = (int) ((b >> 52) & 0x7FF);
     unsigned long long m = b & 0xFFFFFFFFFFFFFull;
@@ -47,8 +60,14 @@ __device__ __forceinline__ long long fx_from(double x, int E) {
     return (b >> 63) ? -(long long) q : (long long) q;
 }
 
+// q * 2^(E-58) rounded to float64 (nearest even): the hardware int64 -> float64 conversion, then an
+// exact exponent add; extreme E take the integer path.
 __device__ __forceinline__ double fx_to(long long q, int E) {
     if (q == 0) return 0.0;
+    if (E > -900 && E < 1000) {
+        const double d = __ll2double_rn(q);
+        return __hiloint2double(__double2hiint(d) + (E - 58) * (1 << 20), __double2loint(d));
+    }
     const unsigned long long sign = q < 0 ? 1ull : 0ull;
     const unsigned long long a = q < 0 ? (unsigned long long) (-q) : (unsigned long long) q;
     const int bl = 64 - __clzll((long long) a);
@@ -235,10 +254,138 @@ __global__ void __launch_bounds__(TX2) axis2d_kernel(FieldView in, FieldView out
     if (FAST) block_max_commit(vmax, &maxslots[(step + 1) % 3]);
 }
 
+// ------------------------------------------------------------------------- 3D, register-blocked
+// One warp covers 32 consecutive x-columns and computes the 30 inner ones (lanes 1..30; lanes 0 and 31
+// only supply the x neighbours) for RB consecutive y-rows, marching along z.  The planes z-1, z, z+1
+// of those rows stay in registers (z and z+1 with one halo row on each side), plane z+2 is loaded
+// while z is computed, and x neighbours come from warp shuffles.  No shared memory, no CTA barrier.
+constexpr int RB = 8;
+constexpr int RB_WARPS = 4;
+constexpr int RB_COLS = 30;
+
+template <bool FAST>
+__global__ void __launch_bounds__(32 * RB_WARPS, 4) axis3d_rb_kernel(FieldView in, FieldView out, Box box, AxisParams P, unsigned long long* maxslots,
+                                                                  int step, int zchunk, int tiles_x, int tiles_y) {
+    using T = typename std::conditional<FAST, long long, double>::type;
+    const int lane = threadIdx.x & 31;
+    const int warp = blockIdx.x * RB_WARPS + (threadIdx.x >> 5);
+    if (warp >= tiles_x * tiles_y) return;
+    const int tx = warp % tiles_x, ty = warp / tiles_x;
+    const int x0 = box.lo[0] + tx * RB_COLS, y0 = box.lo[1] + ty * RB;
+    const int i = x0 - 1 + lane;
+    const bool vx = lane >= 1 && lane <= RB_COLS && i < box.hi[0];
+    const int ic = min(i, box.hi[0]);
+    const int zs = box.lo[2] + blockIdx.y * zchunk;
+    const int ze = min(zs + zchunk, box.hi[2]);
+    if (zs >= ze) return;
+    int E = 0;
+    if (FAST) {
+        E = scale_exp(maxslots, step, P.bound_bits);
+        if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) maxslots[(step + 2) % 3] = 0ull;
+    }
+    auto conv = [&](double v) -> T {
+        if constexpr (FAST) return fx_from(v, E);
+        else return v;
+    };
+    // row offsets of y0-1 .. y0+RB, clamped to the box edge + 1 (the farthest row the stencil reads)
+    long long roff[RB + 2];
+#pragma unroll
+    for (int r = 0; r < RB + 2; ++r) roff[r] = (long long) (min(y0 - 1 + r, box.hi[1]) - in.off[1]) * in.sy;
+    const double* col = in.data + (ic - in.off[0]) - (long long) in.off[2] * in.sz;
+    T below[RB], cur[RB + 2], above[RB + 2];
+    double nxt[RB + 2];
+    {
+        const double* pm = col + (long long) (zs - 1) * in.sz;
+        const double* p0 = col + (long long) zs * in.sz;
+        const double* p1 = col + (long long) min(zs + 1, box.hi[2]) * in.sz;
+#pragma unroll
+        for (int r = 0; r < RB; ++r) below[r] = conv(pm[roff[r + 1]]);
+#pragma unroll
+        for (int r = 0; r < RB + 2; ++r) cur[r] = conv(p0[roff[r]]);
+#pragma unroll
+        for (int r = 0; r < RB + 2; ++r) above[r] = conv(p1[roff[r]]);
+    }
+    unsigned long long vmax = 0;
+    double* const ocol = out.data + (i - out.off[0]) - (long long) out.off[1] * out.sy - (long long) out.off[2] * out.sz;
+    for (int k = zs; k < ze; ++k) {
+        {
+            const double* pn = col + (long long) min(k + 2, box.hi[2]) * in.sz;
+#pragma unroll
+            for (int r = 0; r < RB + 2; ++r) nxt[r] = pn[roff[r]];
+        }
+#pragma unroll
+        for (int r = 0; r < RB; ++r) {
+            const T c = cur[r + 1];
+            const T l = __shfl_up_sync(0xffffffffu, c, 1);
+            const T rr = __shfl_down_sync(0xffffffffu, c, 1);
+            const int j = y0 + r;
+            if (vx && j < box.hi[1]) {
+                const T b = cur[r], t = cur[r + 2], zb = below[r], za = above[r + 1];
+                double v;
+                if constexpr (FAST) {
+                    long long q = c;
+                    if (P.iso) {
+                        const long long z = (l - c) + (rr - c) + (b - c) + (t - c) + (zb - c) + (za - c);
+                        q += fx_mul(z, P.wm[0], P.wshift[0], P.wneg[0]);
+                    } else {
+                        q += fx_mul((l - c) + (rr - c), P.wm[0], P.wshift[0], P.wneg[0]);
+                        q += fx_mul((b - c) + (t - c), P.wm[1], P.wshift[1], P.wneg[1]);
+                        q += fx_mul((zb - c) + (za - c), P.wm[2], P.wshift[2], P.wneg[2]);
+                    }
+                    v = fx_to(q, E);
+                    const unsigned long long ab = (unsigned long long) __double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
+                    vmax = ab > vmax ? ab : vmax;
+                } else {
+                    const double d0 = d2_exact(l, c, rr, P.h[0], P.inv_h[0], P.pow2[0]);
+                    const double d1 = d2_exact(b, c, t, P.h[1], P.inv_h[1], P.pow2[1]);
+                    const double d2 = d2_exact(zb, c, za, P.h[2], P.inv_h[2], P.pow2[2]);
+                    auto pick = [&](int a) { return a == 0 ? d0 : (a == 1 ? d1 : d2); };
+                    double sum = pick(P.order[0]);
+                    sum = __dadd_rn(sum, pick(P.order[1]));
+                    sum = __dadd_rn(sum, pick(P.order[2]));
+                    v = __dadd_rn(c, __dmul_rn(P.s, sum));
+                }
+                ocol[(long long) (j) * out.sy + (long long) k * out.sz] = v;
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < RB; ++r) below[r] = cur[r + 1];
+#pragma unroll
+        for (int r = 0; r < RB + 2; ++r) cur[r] = above[r];
+#pragma unroll
+        for (int r = 0; r < RB + 2; ++r) above[r] = conv(nxt[r]);
+    }
+    if (FAST) block_max_commit(vmax, &maxslots[(step + 1) % 3]);
+}
+
+// 3D tiling: register-blocked warps for the fixed-point mode (integer-issue bound, gains from the
+// absent barriers), shared-memory tiles for the exact mode (float64-pipe bound, measured slightly
+// faster); OPFLOW_AXIS_TILING=register|smem overrides, read at every launch so that one process can
+// compare the two
+static bool use_register_tiles(bool fast) {
+    const char* e = getenv("OPFLOW_AXIS_TILING");
+    if (e && strcmp(e, "smem") == 0) return false;
+    if (e && strcmp(e, "register") == 0) return true;
+    return fast;
+}
+
 int axis_launch(opflow_ctx ctx, const FieldView& in, const FieldView& out, const Box& box, const AxisParams& P, bool fast,
                 unsigned long long* maxslots, int step) {
     const int nx = box.hi[0] - box.lo[0], ny = box.hi[1] - box.lo[1], nz = box.hi[2] - box.lo[2];
     if (nx <= 0 || ny <= 0 || nz <= 0) return OPFLOW_OK;
+    if (P.ndim == 3 && use_register_tiles(fast)) {
+        const int tiles_x = (nx + RB_COLS - 1) / RB_COLS, tiles_y = (ny + RB - 1) / RB;
+        const int bx = (tiles_x * tiles_y + RB_WARPS - 1) / RB_WARPS;
+        int zchunks = (ctx->num_sms * 6 + bx - 1) / bx;
+        zchunks = std::max(1, std::min(zchunks, (nz + 15) / 16));
+        const int zchunk = (nz + zchunks - 1) / zchunks;
+        zchunks = (nz + zchunk - 1) / zchunk;
+        dim3 g(bx, zchunks), b(32 * RB_WARPS);
+        if (fast) axis3d_rb_kernel<true><<<g, b, 0, ctx->stream>>>(in, out, box, P, maxslots, step, zchunk, tiles_x, tiles_y);
+        else axis3d_rb_kernel<false><<<g, b, 0, ctx->stream>>>(in, out, box, P, maxslots, step, zchunk, tiles_x, tiles_y);
+        OPG_LAUNCHED();
+        return check_launch("axis3d_rb_kernel");
+    }
     if (P.ndim == 3) {
         const int bx = (nx + TX - 1) / TX, by = (ny + TY - 1) / TY;
         // enough CTAs for ~8 per SM, each marching at least 16 planes

@@ -208,3 +208,24 @@ def test_nonlinear_equation_is_rejected(ctx):
     with pytest.raises(capi.OpflowError) as e:
         api.Solve(lambda e: f == e * api.d2x(e), p)
     assert e.value.code == capi.E_UNSUPPORTED
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_iteration_cap_and_repeated_solves(ctx, prec):
+    """The device-side solve loop stops at maxIter without converging, reports exactly maxIter
+    iterations, and a handler solved again (graph replay) reaches the same answer as a fresh solve."""
+    mesh, fd, p, f = poisson_case(ctx, 64, capi.BC_DIRC)
+    getter = lambda e: f == api.d2x(e) + api.d2y(e)
+    p.assign(0.0)
+    st = api.Solve(getter, p, api.StructSolverParams(tol=1e-30, maxIter=3, precision=prec))
+    assert not st.converged and st.niter == 3, st
+    p.assign(0.0)
+    h = api.makeEqnSolveHandler(getter, p, api.StructSolverParams(tol=1e-10, maxIter=100, precision=prec, zeroGuess=True))
+    s1 = h.solve()
+    x1 = p.download()
+    p.assign(1.0)  # a different guess: zeroGuess overrides it
+    s2 = h.solve()
+    x2 = p.download()
+    h.close()
+    assert s1.converged and s2.converged and s1.niter == s2.niter
+    assert np.array_equal(x1, x2)
