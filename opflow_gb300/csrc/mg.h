@@ -7,6 +7,7 @@ namespace opg {
 // operator slots: centre, x-, x+, y-, y+, z-, z+
 constexpr int NSLOT = 7;
 constexpr int NCLASS = 27;  // position classes (first / interior / last cell per dim)
+constexpr int TSTRIDE = 8;  // class-table row: the NSLOT coefficients, then the inverse of the centre one
 
 enum GhostRule { GH_ZERO = 0, GH_COPY = 1, GH_WRAP = 2 };
 
@@ -23,10 +24,11 @@ struct LvlDev {
     int rbgs;            // 1: red-black Gauss-Seidel, 0: damped Jacobi
     int problem;         // owning problem
     int coarsest;        // 1 if no coarser level
+    int tiled;           // 1: smoothed by the fused tile kernels (which also restrict into the next level)
     int nslot;           // 2*ndim + 1
     const double* A64;   // [NSLOT][N]
     const float* A32;
-    const double* T64;   // [NCLASS][NSLOT]
+    const double* T64;   // [NCLASS][TSTRIDE]
     const float* T32;
     double *x64, *b64, *r64;
     float *x32, *b32, *r32;
@@ -57,6 +59,20 @@ struct Scal {
     int iters;
     int singular;
     int pad_;
+};
+
+// Per-problem reduction of chunk partials fused into the kernel that produces them: the CTA that
+// completes a problem's last chunk sums the problem's partials (the fixed order of the separate reduce
+// kernel), writes them to red[2p], red[2p+1] and applies scalar stage `stage` (none if stage < 0).
+struct Finish {
+    int* done;          // [nprob] completed-chunk counters, 0 between launches; nullptr: no fused finish
+    const int* first;   // [nprob] first chunk of each problem
+    const int* count;   // [nprob] chunks of each problem
+    Scal* sc;
+    double* red;
+    int stage;
+    int max_iter;
+    double tol;
 };
 
 }  // namespace opg

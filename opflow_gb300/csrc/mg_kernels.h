@@ -7,14 +7,25 @@ int mg_launch_residual(cudaStream_t s, int sms, bool f32, const LvlDev* L, const
 int mg_launch_smooth(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* ch, int nch, int color, const Scal* sc);
 int mg_launch_restrict(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* ch, int nch, const Scal* sc);
 int mg_launch_prolong(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* ch, int nch, const Scal* sc);
+// fused 2D tile steps of a level (mg_tiles.cu): down = pre-smoothing + residual + restriction,
+// up = prolongation + post-smoothing; tiles are Chunk{lvl, j = tile y origin, k = 0, i0 = tile x origin}
+constexpr int MG_TILE_X = 64, MG_TILE_Y = 32;
+bool mg_tiles_supported(int sweeps);
+int mg_tiles_prepare(int sweeps);
+int mg_launch_tile_down(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* tiles, int ntiles, const Scal* sc, int pre);
+int mg_launch_tile_up(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* tiles, int ntiles, const Scal* sc, int post);
 // the whole V-cycle below each listed level (a problem's first small level), one CTA per problem
 int mg_launch_bottom(cudaStream_t s, int sms, bool f32, const LvlDev* L, const int* top, int ntop, const Scal* sc, int pre, int post);
 int mg_launch_coarse(cudaStream_t s, int sms, bool f32, const LvlDev* L, const int* lv, int nlv, const Scal* sc);
-int kr_launch_apply(cudaStream_t s, int sms, const LvlDev* L, const KrylovDev* K, const Chunk* ch, int nch, const Scal* sc, double* partial, int mode);
-int kr_launch_update(cudaStream_t s, int sms, const LvlDev* L, const KrylovDev* K, const Chunk* ch, int nch, const Scal* sc, double* partial);
+// The Krylov kernels write per-chunk partial sums; with F.done set they also reduce them per problem
+// and apply a scalar stage (see Finish), otherwise kr_launch_reduce / kr_launch_scalars do that.
+int kr_launch_apply(cudaStream_t s, int sms, const LvlDev* L, const KrylovDev* K, const Chunk* ch, int nch, const Scal* sc, double* partial, int mode,
+                    const Finish& F = Finish{});
+int kr_launch_update(cudaStream_t s, int sms, const LvlDev* L, const KrylovDev* K, const Chunk* ch, int nch, const Scal* sc, double* partial,
+                     const Finish& F = Finish{});
 int kr_launch_to_vcycle(cudaStream_t s, int sms, bool f32, const LvlDev* L, const KrylovDev* K, const Chunk* ch, int nch, const Scal* sc);
 int kr_launch_from_vcycle(cudaStream_t s, int sms, bool f32, const LvlDev* L, const KrylovDev* K, const Chunk* ch, int nch, const Scal* sc,
-                          double* partial);
+                          double* partial, const Finish& F = Finish{});
 int kr_launch_pupdate(cudaStream_t s, int sms, const LvlDev* L, const KrylovDev* K, const Chunk* ch, int nch, const Scal* sc, int first);
 int kr_launch_reduce(cudaStream_t s, int sms, const double* partial, const int* first, const int* count, int nprob, double* out);
 int kr_launch_scalars(cudaStream_t s, Scal* sc, const double* red, int nprob, int stage, double tol, int max_iter, int flexible);

@@ -256,9 +256,8 @@ static int compress_level(MGSystem* S, LevelHost& L) {
                 rep[cx + 3 * cy + 9 * cz] = i + (long long) L.n[0] * (j + (long long) L.n[1] * k);
             }
     double* dtab = (double*) S->arena.alloc(NCLASS * NSLOT * sizeof(double));
-    float* dtab32 = (float*) S->arena.alloc(NCLASS * NSLOT * sizeof(float));
     long long* drep = (long long*) ((char*) ctx->scratch + 2048);
-    if (!dtab || !dtab32) return fail(OPFLOW_E_NOMEM, "class table");
+    if (!dtab) return fail(OPFLOW_E_NOMEM, "class table");
     cudaMemcpyAsync(drep, rep.data(), NCLASS * sizeof(long long), cudaMemcpyHostToDevice, ctx->stream);
     gather_classes<<<1, 256, 0, ctx->stream>>>(L.A64, N, drep, dtab);
     OPG_LAUNCHED();
@@ -271,10 +270,26 @@ static int compress_level(MGSystem* S, LevelHost& L) {
     cudaMemcpyAsync(tab.data(), dtab, tab.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
     cudaMemcpyAsync(&hb, bad, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
     OPG_CUDA(cudaStreamSynchronize(ctx->stream));
-    std::vector<float> t32(tab.begin(), tab.end());
-    cudaMemcpyAsync(dtab32, t32.data(), t32.size() * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
-    L.T64 = dtab;
-    L.T32 = dtab32;
+    // kernel tables: rows of TSTRIDE with the inverse of the centre coefficient appended
+    std::vector<double> t8(NCLASS * TSTRIDE, 0.);
+    std::vector<float> t8f(NCLASS * TSTRIDE, 0.f);
+    for (int c = 0; c < NCLASS; ++c) {
+        for (int q = 0; q < NSLOT; ++q) {
+            t8[c * TSTRIDE + q] = tab[c * NSLOT + q];
+            t8f[c * TSTRIDE + q] = (float) tab[c * NSLOT + q];
+        }
+        const double c0 = tab[c * NSLOT];
+        const float c0f = (float) c0;
+        t8[c * TSTRIDE + NSLOT] = c0 != 0. ? 1.0 / c0 : 0.;
+        t8f[c * TSTRIDE + NSLOT] = c0f != 0.f ? 1.0f / c0f : 0.f;
+    }
+    double* dt8 = (double*) S->arena.alloc(NCLASS * TSTRIDE * sizeof(double));
+    float* dt8f = (float*) S->arena.alloc(NCLASS * TSTRIDE * sizeof(float));
+    if (!dt8 || !dt8f) return fail(OPFLOW_E_NOMEM, "class table");
+    cudaMemcpyAsync(dt8, t8.data(), t8.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemcpyAsync(dt8f, t8f.data(), t8f.size() * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
+    L.T64 = dt8;
+    L.T32 = dt8f;
     L.table = hb == 0;
     L.tab = tab;
     if (!L.table) {
@@ -283,7 +298,7 @@ static int compress_level(MGSystem* S, LevelHost& L) {
         to_f32<<<gridN(ctx, NSLOT * N), 256, 0, ctx->stream>>>(L.A64, L.A32, NSLOT * N);
         OPG_LAUNCHED();
     }
-    OPG_CUDA(cudaStreamSynchronize(ctx->stream));  // t32 must outlive its copy
+    OPG_CUDA(cudaStreamSynchronize(ctx->stream));  // t8 / t8f must outlive their copies
     return OPFLOW_OK;
 }
 
@@ -486,8 +501,12 @@ int mg_finalize(MGSystem* S) {
     S->smooth_ch.assign(S->nlevels, {});
     S->restrict_ch.assign(S->nlevels, {});
     S->prolong_ch.assign(S->nlevels, {});
+    S->tile_ch.assign(S->nlevels, {});
     S->coarse_sm_ch.clear();
     S->bottom_host.clear();
+    const char* te = getenv("OPFLOW_MG_TILES");
+    bool tiles_on = !(te && te[0] == '0') && mg_tiles_supported(S->pre) && mg_tiles_supported(S->post);
+    if (tiles_on) OPG_TRY(mg_tiles_prepare(std::max(S->pre, S->post)));
     std::vector<int> coarse_list;
     std::vector<Chunk> k0;
     std::vector<int> first, count;
@@ -505,6 +524,23 @@ int mg_finalize(MGSystem* S) {
         size_t sp = P.levels.size();
         for (size_t l = 0; l < P.levels.size(); ++l)
             if (P.levels[l].N <= S->bottom_max) { sp = l; break; }
+        // 2D red-black class-table levels above the bottom whose coarse cells all have children in the
+        // level run as fused tiles
+        auto tileable = [&](size_t l) {
+            if (!tiles_on || l >= sp || l + 1 >= P.levels.size()) return false;
+            const LevelHost& F = P.levels[l];
+            const LevelHost& Cn = P.levels[l + 1];
+            if (F.ndim != 2 || !F.table) return false;
+            for (int d = 0; d < 2; ++d) {
+                if (F.per[d] && (F.n[d] & 1)) return false;  // damped Jacobi level
+                if (Cn.node) {
+                    if (2 * Cn.lo[d] - F.lo[d] < 0 || 2 * (Cn.lo[d] + Cn.n[d] - 1) - F.lo[d] > F.n[d] - 1) return false;
+                } else if (Cn.n[d] != (F.n[d] + 1) / 2) {
+                    return false;
+                }
+            }
+            return true;
+        };
         for (size_t l = 0; l < P.levels.size(); ++l) {
             LevelHost& H = P.levels[l];
             LvlDev D{};
@@ -531,6 +567,7 @@ int mg_finalize(MGSystem* S) {
             D.T32 = H.T32;
             D.coarse = D.coarsest ? -1 : base + (int) l + 1;
             D.fine = l == 0 ? -1 : base + (int) l - 1;
+            D.tiled = tileable(l) ? 1 : 0;
             D.Ainv64 = H.Ainv64;
             const size_t N = (size_t) H.N;
             if (f32) {
@@ -548,9 +585,15 @@ int mg_finalize(MGSystem* S) {
             const int li = base + (int) l;
             if (l == sp) S->bottom_host.push_back(li);
             if (l >= sp) continue;                                   // inside the bottom kernel
-            if (!D.coarsest) rows(li, D, S->smooth_ch[l]);
-            if (l > 0) rows(li, D, S->restrict_ch[l]);       // coarse rows of level l (restricted from l-1)
-            if (!D.coarsest) rows(li, D, S->prolong_ch[l]);  // fine rows of level l (prolonged from l+1)
+            const bool above_tiled = l > 0 && tileable(l - 1);      // restricted by the finer level's tiles
+            if (D.tiled) {
+                for (int j0 = 0; j0 < D.n[1]; j0 += MG_TILE_Y)
+                    for (int i0 = 0; i0 < D.n[0]; i0 += MG_TILE_X) S->tile_ch[l].push_back(Chunk{li, j0, 0, i0, 0});
+            } else {
+                if (!D.coarsest) rows(li, D, S->smooth_ch[l]);
+                if (!D.coarsest) rows(li, D, S->prolong_ch[l]);  // fine rows of level l (prolonged from l+1)
+            }
+            if (l > 0 && !above_tiled) rows(li, D, S->restrict_ch[l]);  // coarse rows of level l (restricted from l-1)
             if (D.coarsest && H.Ainv64) coarse_list.push_back(li);
             if (D.coarsest && !H.Ainv64) rows(li, D, S->coarse_sm_ch);
         }
@@ -586,6 +629,9 @@ int mg_finalize(MGSystem* S) {
     S->red = (double*) S->arena.alloc(2 * S->probs.size() * sizeof(double));
     S->dcoarse = (int*) S->arena.alloc(std::max<size_t>(1, coarse_list.size()) * sizeof(int));
     S->d_active = (int*) S->arena.alloc(2 * sizeof(int));  // [0] active count, [1] solve-loop counter
+    S->d_done = (int*) S->arena.alloc(S->probs.size() * sizeof(int));
+    if (!S->d_done) return fail(OPFLOW_E_NOMEM, "solver tables");
+    cudaMemsetAsync(S->d_done, 0, S->probs.size() * sizeof(int), ctx->stream);
     S->ncoarse = (int) coarse_list.size();
     S->coarse_host = coarse_list;
     S->nbottom = (int) S->bottom_host.size();
@@ -608,10 +654,12 @@ int mg_finalize(MGSystem* S) {
     S->d_smooth.assign(S->nlevels, {});
     S->d_restrict.assign(S->nlevels, {});
     S->d_prolong.assign(S->nlevels, {});
+    S->d_tiles.assign(S->nlevels, {});
     for (int l = 0; l < S->nlevels; ++l) {
         upload(S->smooth_ch[l], S->d_smooth[l]);
         upload(S->restrict_ch[l], S->d_restrict[l]);
         upload(S->prolong_ch[l], S->d_prolong[l]);
+        upload(S->tile_ch[l], S->d_tiles[l]);
     }
     upload(S->coarse_sm_ch, S->d_coarse_sm);
     S->kd_host = kd;
@@ -637,6 +685,7 @@ static int vcycle(MGSystem* S) {
     OPG_TRY(kr_launch_to_vcycle(s, sms, f32, S->dL, S->dK, S->dk0, S->nk0, sc));
     for (int l = 0; l < S->nlevels; ++l) {
         if (l > 0) OPG_TRY(mg_launch_restrict(s, sms, f32, S->dL, S->d_restrict[l].ptr, S->d_restrict[l].n, sc));
+        OPG_TRY(mg_launch_tile_down(s, sms, f32, S->dL, S->d_tiles[l].ptr, S->d_tiles[l].n, sc, S->pre));
         const ChunkList& C = S->d_smooth[l];
         for (int it = 0; it < S->pre; ++it) {
             OPG_TRY(mg_launch_smooth(s, sms, f32, S->dL, C.ptr, C.n, 0, sc));
@@ -651,6 +700,7 @@ static int vcycle(MGSystem* S) {
         OPG_TRY(mg_launch_smooth(s, sms, f32, S->dL, S->d_coarse_sm.ptr, S->d_coarse_sm.n, 1, sc));
     }
     for (int l = S->nlevels - 2; l >= 0; --l) {
+        OPG_TRY(mg_launch_tile_up(s, sms, f32, S->dL, S->d_tiles[l].ptr, S->d_tiles[l].n, sc, S->post));
         OPG_TRY(mg_launch_prolong(s, sms, f32, S->dL, S->d_prolong[l].ptr, S->d_prolong[l].n, sc));
         const ChunkList& C = S->d_smooth[l];
         for (int it = 0; it < S->post; ++it) {
@@ -661,6 +711,20 @@ static int vcycle(MGSystem* S) {
     return OPFLOW_OK;
 }
 
+// fused per-problem reduction + scalar stage for the Krylov kernels
+static Finish finish(MGSystem* S, int stage) {
+    Finish F{};
+    F.done = S->d_done;
+    F.first = S->dfirst;
+    F.count = S->dcount;
+    F.sc = S->dS;
+    F.red = S->red;
+    F.stage = stage;
+    F.max_iter = S->max_iter;
+    F.tol = S->tol;
+    return F;
+}
+
 // One flexible-PCG iteration (everything after the first direction), recorded into a CUDA graph.
 // With `readback` the active count is also copied to the host (for callers that step iterations).
 static int iteration(MGSystem* S, bool readback) {
@@ -668,16 +732,10 @@ static int iteration(MGSystem* S, bool readback) {
     const int sms = S->ctx->num_sms;
     const bool f32 = S->precision == OPFLOW_PREC_MIXED;
     const int np = S->nprob;
-    OPG_TRY(kr_launch_apply(s, sms, S->dL, S->dK, S->dk0, S->nk0, S->dS, S->partial, 1));  // q = A p
-    OPG_TRY(kr_launch_reduce(s, sms, S->partial, S->dfirst, S->dcount, np, S->red));
-    OPG_TRY(kr_launch_scalars(s, S->dS, S->red, np, 1, S->tol, S->max_iter, 1));
-    OPG_TRY(kr_launch_update(s, sms, S->dL, S->dK, S->dk0, S->nk0, S->dS, S->partial));
-    OPG_TRY(kr_launch_reduce(s, sms, S->partial, S->dfirst, S->dcount, np, S->red));
-    OPG_TRY(kr_launch_scalars(s, S->dS, S->red, np, 2, S->tol, S->max_iter, 1));
+    OPG_TRY(kr_launch_apply(s, sms, S->dL, S->dK, S->dk0, S->nk0, S->dS, S->partial, 1, finish(S, 1)));  // q = A p
+    OPG_TRY(kr_launch_update(s, sms, S->dL, S->dK, S->dk0, S->nk0, S->dS, S->partial, finish(S, 2)));
     OPG_TRY(vcycle(S));
-    OPG_TRY(kr_launch_from_vcycle(s, sms, f32, S->dL, S->dK, S->dk0, S->nk0, S->dS, S->partial));
-    OPG_TRY(kr_launch_reduce(s, sms, S->partial, S->dfirst, S->dcount, np, S->red));
-    OPG_TRY(kr_launch_scalars(s, S->dS, S->red, np, 3, S->tol, S->max_iter, 1));
+    OPG_TRY(kr_launch_from_vcycle(s, sms, f32, S->dL, S->dK, S->dk0, S->nk0, S->dS, S->partial, finish(S, 3)));
     OPG_TRY(kr_launch_pupdate(s, sms, S->dL, S->dK, S->dk0, S->nk0, S->dS, 0));
     OPG_TRY(kr_launch_count(s, S->dS, np, S->d_active));
     if (readback) OPG_CUDA(cudaMemcpyAsync(S->h_active, S->d_active, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -690,13 +748,9 @@ static int first_direction(MGSystem* S) {
     const int sms = S->ctx->num_sms;
     const bool f32 = S->precision == OPFLOW_PREC_MIXED;
     const int np = S->nprob;
-    OPG_TRY(kr_launch_apply(s, sms, S->dL, S->dK, S->dk0, S->nk0, nullptr, S->partial, 0));
-    OPG_TRY(kr_launch_reduce(s, sms, S->partial, S->dfirst, S->dcount, np, S->red));
-    OPG_TRY(kr_launch_scalars(s, S->dS, S->red, np, 0, S->tol, S->max_iter, 1));
+    OPG_TRY(kr_launch_apply(s, sms, S->dL, S->dK, S->dk0, S->nk0, nullptr, S->partial, 0, finish(S, 0)));
     OPG_TRY(vcycle(S));
-    OPG_TRY(kr_launch_from_vcycle(s, sms, f32, S->dL, S->dK, S->dk0, S->nk0, S->dS, S->partial));
-    OPG_TRY(kr_launch_reduce(s, sms, S->partial, S->dfirst, S->dcount, np, S->red));
-    OPG_TRY(kr_launch_scalars(s, S->dS, S->red, np, 4, S->tol, S->max_iter, 1));
+    OPG_TRY(kr_launch_from_vcycle(s, sms, f32, S->dL, S->dK, S->dk0, S->nk0, S->dS, S->partial, finish(S, 4)));
     OPG_TRY(kr_launch_pupdate(s, sms, S->dL, S->dK, S->dk0, S->nk0, S->dS, 1));
     return kr_launch_count(s, S->dS, np, S->d_active);
 }
@@ -896,6 +950,7 @@ int mg_compose(MGSystem* C, const std::vector<MGSystem*>& parts, const std::vect
     C->smooth_ch.assign(C->nlevels, {});
     C->restrict_ch.assign(C->nlevels, {});
     C->prolong_ch.assign(C->nlevels, {});
+    C->tile_ch.assign(C->nlevels, {});
     C->coarse_sm_ch.clear();
     for (size_t q = 0; q < parts.size(); ++q) {
         MGSystem* P = parts[q];
@@ -916,6 +971,7 @@ int mg_compose(MGSystem* C, const std::vector<MGSystem*>& parts, const std::vect
             shift(P->smooth_ch[l], C->smooth_ch[l]);
             shift(P->restrict_ch[l], C->restrict_ch[l]);
             shift(P->prolong_ch[l], C->prolong_ch[l]);
+            shift(P->tile_ch[l], C->tile_ch[l]);
         }
         shift(P->coarse_sm_ch, C->coarse_sm_ch);
         KrylovDev K = P->kd_host[0];
@@ -944,6 +1000,9 @@ int mg_compose(MGSystem* C, const std::vector<MGSystem*>& parts, const std::vect
     C->nbottom = (int) bottom_list.size();
     C->dbottom = (int*) C->arena.alloc(std::max<size_t>(1, bottom_list.size()) * sizeof(int));
     C->d_active = (int*) C->arena.alloc(2 * sizeof(int));
+    C->d_done = (int*) C->arena.alloc(np * sizeof(int));
+    if (!C->d_done) return fail(OPFLOW_E_NOMEM, "batch tables");
+    cudaMemsetAsync(C->d_done, 0, np * sizeof(int), ctx->stream);
     if (!C->dL || !C->dK || !C->dS || !C->dk0 || !C->dfirst || !C->dcount || !C->partial || !C->red || !C->dcoarse || !C->d_active || !C->dbottom)
         return fail(OPFLOW_E_NOMEM, "batch tables");
     cudaStream_t s = ctx->stream;
@@ -963,10 +1022,12 @@ int mg_compose(MGSystem* C, const std::vector<MGSystem*>& parts, const std::vect
     C->d_smooth.assign(C->nlevels, {});
     C->d_restrict.assign(C->nlevels, {});
     C->d_prolong.assign(C->nlevels, {});
+    C->d_tiles.assign(C->nlevels, {});
     for (int l = 0; l < C->nlevels; ++l) {
         upload(C->smooth_ch[l], C->d_smooth[l]);
         upload(C->restrict_ch[l], C->d_restrict[l]);
         upload(C->prolong_ch[l], C->d_prolong[l]);
+        upload(C->tile_ch[l], C->d_tiles[l]);
     }
     upload(C->coarse_sm_ch, C->d_coarse_sm);
     C->kd_host = kd;

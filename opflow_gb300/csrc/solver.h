@@ -63,6 +63,9 @@ struct MGSystem {
     // coarse_sm: rows of coarsest levels that have no dense inverse (they are smoothed instead)
     std::vector<std::vector<Chunk>> smooth_ch, restrict_ch, prolong_ch;
     std::vector<ChunkList> d_smooth, d_restrict, d_prolong;
+    // tiles of the levels run by the fused 2D tile kernels (such levels are in none of the lists above)
+    std::vector<std::vector<Chunk>> tile_ch;
+    std::vector<ChunkList> d_tiles;
     std::vector<Chunk> coarse_sm_ch;
     ChunkList d_coarse_sm;
     LvlDev* dL = nullptr;
@@ -85,6 +88,7 @@ struct MGSystem {
     std::vector<KrylovDev> kd_host;
     int* h_active = nullptr;
     int* d_active = nullptr;  // device count of active problems (owned, so a recorded graph never dangles)
+    int* d_done = nullptr;    // per-problem chunk counters of the fused reductions (zero between launches)
     cudaGraphExec_t exec = nullptr;        // one iteration (stepped by the request server)
     cudaGraphExec_t solve_exec = nullptr;  // a whole solve: first direction + device-side while loop
     // private stream the iteration graph is recorded on: the caller's stream may be the legacy default
