@@ -176,7 +176,7 @@ def run_reference(args):
     if rank != 0:
         return 0
     threads = os.cpu_count() or 1
-    if args.workload in ("poisson2d", "serve"):
+    if args.workload in SOLVE_WORKLOADS:
         vals = []
         for _ in range(max(1, min(args.steps, 3))):
             v, sample, used = cpu_solve_sample(threads)
@@ -187,6 +187,19 @@ def run_reference(args):
                 "dtype": "f64", "data": "synthetic", "config": {"workload": args.workload, "sample": sample},
                 "cpu_baseline": {"value": value, "unit": "solves/s", "cores": used, "kind": "port", "sample": sample},
                 "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return 0
+    if args.workload == "weno":
+        vals = []
+        for _ in range(max(1, min(args.steps, 3))):
+            v, sample, used = cpu_weno_sample(threads)
+            vals.append(v)
+        value = statistics.median(vals)
+        line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Gpts/s", "n_gpus": args.gpus, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64", "data": "synthetic", "config": {"workload": "weno", "sample": sample},
+                "cpu_baseline": {"value": value, "unit": "Gpts/s", "cores": used, "kind": "port", "sample": sample},
+                "e2e": {"value": value, "unit": "Gpts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return 0
     vals = []
@@ -208,7 +221,8 @@ def run_reference(args):
 
 
 # ------------------------------------------------------------------------------------------ solves
-ITER_BYTES_PER_CELL = 220.0  # algorithmic bytes per level-0 cell and flexible-PCG iteration (DESIGN.md)
+ITER_BYTES_PER_CELL = 220.0  # algorithmic bytes per level-0 cell and flexible-PCG iteration
+SOLVE_WORKLOADS = ("poisson2d", "serve", "batched", "poisson3d")
 
 
 def poisson_problem(api, rng, n, ndim, bc):
@@ -334,6 +348,162 @@ def run_poisson2d(args, torch, api, capi, np, ctx, stream, world, rank, local):
                 e2e={"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": a.nbytes, "d2h_bytes_per_step": a.nbytes, "steps": e2e_steps})
 
 
+def batched_problems(np_, api, seed, count):
+    """(I - k Lap) u = f on corner-loc Dirichlet grids: k ~ LogU[1e-4, 1], side ~ LogU[65, 1025] rounded to
+    2^m + 1, f ~ N(0, 1)."""
+    rng = np_.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        k = float(np_.exp(rng.uniform(np_.log(1e-4), np_.log(1.0))))
+        side = float(np_.exp(rng.uniform(np_.log(65), np_.log(1025))))
+        n = (1 << int(round(np_.log2(side - 1)))) + 1
+        h = 1.0 / (n - 1)
+        p = api.Problem([n, n], [h, h], alpha=1.0, beta=k, loc=api.LocOnMesh.Corner, bc=api.BCType.Dirc)
+        out.append((p, rng.standard_normal((n - 2) * (n - 2))))
+    return out
+
+
+def run_batched(args, torch, api, capi, np, ctx, stream, world, rank, local):
+    count = args.problems
+    probs = batched_problems(np, api, 99 + rank, count)
+    mixed = api.StructSolverParams(tol=1e-10, maxIter=200, precision="mixed", zeroGuess=True)
+    B = api.Batch([p for p, _ in probs], mixed, ctx)
+    for i, (_, f) in enumerate(probs):
+        B.set(i, f)
+    for _ in range(args.warmup):
+        B.solve()
+    torch.cuda.synchronize()
+    l0 = capi.launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        st = B.solve()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    launches = capi.launch_count() - l0
+    iters = [s.niter for s in st]
+    worst = max(s.relerr for s in st)
+    ok = sum(1 for s in st if s.converged)
+    # end to end: host f in, batched solve, every solution back to the host
+    t0 = time.perf_counter()
+    xs = []
+    for i, (_, f) in enumerate(probs):
+        B.set(i, f)
+    B.solve()
+    for i in range(count):
+        xs.append(B.get(i))
+    e2e_s = time.perf_counter() - t0
+    B.close()
+    # the same problems one at a time, plain FP64 (a loop of per-problem solves)
+    plain = api.StructSolverParams(tol=1e-10, maxIter=200, precision="fp64", zeroGuess=True)
+    nloop = min(count, args.loop_sample)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for p, f in probs[:nloop]:
+        b1 = api.Batch([p], plain, ctx)
+        b1.set(0, f)
+        b1.solve()
+        b1.close()
+    torch.cuda.synchronize()
+    loop_rate = nloop / (time.perf_counter() - t0)
+    cells = sum(int(np.prod([n - 2 for n in p.n])) for p, _ in probs)
+    bytes_per_solve = sum(ITER_BYTES_PER_CELL * int(np.prod([n - 2 for n in p.n])) * it for (p, _), it in zip(probs, iters))
+    peak, src = peak_hbm()
+    achieved = bytes_per_solve / (ms * 1e-3) / 1e9
+    hb = 8 * sum(f.size for _, f in probs)
+    return dict(value=count / (ms * 1e-3), unit="solves/s", ms=ms, launches=launches, dtype="f64 outer / f32 V-cycle",
+                config=dict(workload="batched", problems=count, operator="(I - k Lap) u = f, corner nodes, Dirichlet 0",
+                            k="LogU[1e-4,1]", side="LogU[65,1025] rounded to 2^m+1", unknowns=cells, tol=1e-10, converged=ok,
+                            worst_rel_residual=worst, iterations_min=min(iters), iterations_max=max(iters),
+                            plain_fp64_loop_solves_per_s=loop_rate, plain_fp64_loop_sample=nloop,
+                            batched_over_plain_loop=(count / (ms * 1e-3)) / loop_rate,
+                            l2="%.1f GB of level-0 vectors, streamed per iteration (> L2)" % (cells * 48 / 1e9)),
+                roofline={"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": src,
+                          "traffic": traffic_for("batched"), "kernel": "batched flexible-PCG solve (whole-solve graph)",
+                          "algorithmic_bytes_per_launch": bytes_per_solve},
+                e2e={"value": count / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": hb, "d2h_bytes_per_step": hb})
+
+
+def smooth_field(np_, rng, n, modes=6):
+    """A smooth random field on n^3 cell centres (sum of low-wavenumber Fourier modes), std 1."""
+    x = (np_.arange(n) + 0.5) / n
+    g = np_.zeros((n, n, n))
+    for _ in range(modes):
+        k = rng.integers(1, 4, 3)
+        ph = rng.uniform(0, 2 * np_.pi, 3)
+        a = rng.standard_normal()
+        g += a * (np_.cos(2 * np_.pi * k[2] * x + ph[2])[:, None, None] * np_.cos(2 * np_.pi * k[1] * x + ph[1])[None, :, None]
+                  * np_.cos(2 * np_.pi * k[0] * x + ph[0])[None, None, :])
+    return (g - g.mean()) / g.std()
+
+
+def run_poisson3d(args, torch, api, capi, np, ctx, stream, world, rank, local):
+    """3D 7-point variable-coefficient Poisson: div(K grad p) = f with K = exp(g) interpolated to faces."""
+    n = args.grid or 256
+    mesh = api.MeshBuilder().newMesh(n + 1, n + 1, n + 1)
+    for d in range(3):
+        mesh.setMeshOfDim(d, 0.0, 1.0)
+    mesh = mesh.build()
+    b = api.ExprBuilder().setMesh(mesh).setLoc(api.LocOnMesh.Center).setExt(1)
+    for d in range(3):
+        b.setBC(d, api.DimPos.start, api.BCType.Neum, 0.).setBC(d, api.DimPos.end, api.BCType.Neum, 0.)
+    p, f, K = b.build(ctx), b.build(ctx), b.build(ctx)
+    rng = np.random.default_rng(4321 + rank)
+    kk = K.download()
+    sl = K.index_slices(K.assignableRange)
+    kk[sl] = np.exp(smooth_field(np, rng, n))
+    K.upload(kk)
+    ff = f.download()
+    v = rng.standard_normal(ff[sl].shape)
+    ff[sl] = v - v.mean()
+    f.upload(ff)
+    getter = lambda e: f == (api.dx(api.d1IntpCenterToCorner(K, 0) * api.dx(e)) + api.dy(api.d1IntpCenterToCorner(K, 1) * api.dy(e))
+                             + api.dz(api.d1IntpCenterToCorner(K, 2) * api.dz(e)))
+    out = {}
+    for prec in ("mixed", "fp64"):
+        h = api.makeEqnSolveHandler(getter, p, api.StructSolverParams(tol=1e-10, maxIter=300, pinValue=True, staticMat=True,
+                                                                        precision=prec, zeroGuess=True))
+        for _ in range(args.warmup):
+            st = h.solve()
+        torch.cuda.synchronize()
+        l0 = capi.launch_count()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            st = h.solve()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        out[prec] = dict(solves_per_s=1e3 / ms, ms_per_solve=ms, iterations=st.niter, rel_residual=st.relerr, launches=capi.launch_count() - l0)
+        h.close()
+    host = ff.copy()
+    h = api.makeEqnSolveHandler(getter, p, api.StructSolverParams(tol=1e-10, maxIter=300, pinValue=True, staticMat=True,
+                                                                    precision="mixed", zeroGuess=True))
+    h.solve()
+    t0 = time.perf_counter()
+    for _ in range(2):
+        f.upload(host)
+        h.solve()
+        _ = p.download()
+    e2e = 2 / (time.perf_counter() - t0)
+    h.close()
+    m = out["mixed"]
+    N = n ** 3
+    bpc = ITER_BYTES_PER_CELL + 8.0 * 7 * 2  # + the seven float64 operator arrays read by two level-0 passes
+    achieved = bpc * N * m["iterations"] / (m["ms_per_solve"] * 1e-3) / 1e9
+    peak, src = peak_hbm()
+    return dict(value=m["solves_per_s"], unit="solves/s", ms=m["ms_per_solve"], launches=m["launches"], dtype="f64 outer / f32 V-cycle",
+                config=dict(workload="poisson3d", grid=[n, n, n], loc="cell", bc="neumann 0, pinned",
+                            coefficient="exp(g), g smooth seeded Fourier field of std 1, interpolated to faces", tol=1e-10,
+                            mixed=m, fp64=out["fp64"], mixed_over_fp64=m["solves_per_s"] / out["fp64"]["solves_per_s"],
+                            l2="level-0 vectors %.0f MB each (> L2)" % (N * 8 / 1e6)),
+                roofline={"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": src,
+                          "traffic": traffic_for("poisson3d"), "kernel": "flexible-PCG iteration (whole-solve graph)",
+                          "algorithmic_bytes_per_launch": bpc * N},
+                e2e={"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": ff.nbytes, "d2h_bytes_per_step": ff.nbytes, "steps": 2})
+
+
 def run_serve(args, torch, api, capi, np, ctx, stream, world, rank, local):
     count = args.requests
     rate = args.rate
@@ -403,6 +573,120 @@ def run_serve(args, torch, api, capi, np, ctx, stream, world, rank, local):
                      "d2h_bytes_per_step": 8 * sum(f.size for _, f, _ in reqs), "p50_ms": mixed["p50_ms"], "p99_ms": mixed["p99_ms"]})
 
 
+# ------------------------------------------------------------------------------------------- WENO
+def weno_u0(np_, seed, nx, ny):
+    """Per line: a square pulse and a sine pulse with seeded positions, widths and amplitudes."""
+    rng = np_.random.default_rng(seed)
+    x = (np_.arange(nx) + 0.5) / nx
+    c1, w1, a1 = rng.uniform(0.1, 0.4, ny), rng.uniform(0.05, 0.15, ny), rng.uniform(0.5, 1.0, ny)
+    c2, w2, a2 = rng.uniform(0.55, 0.85, ny), rng.uniform(0.05, 0.12, ny), rng.uniform(0.3, 0.8, ny)
+    u = np_.where(np_.abs(x[None, :] - c1[:, None]) < w1[:, None], a1[:, None], 0.0)
+    d = (x[None, :] - c2[:, None]) / w2[:, None]
+    u += np_.where(np_.abs(d) < 1.0, a2[:, None] * np_.cos(0.5 * np_.pi * d) ** 2, 0.0)
+    return u
+
+
+def cpu_weno_sample(threads):
+    """The oracle's three WENO5 stage assignments on 4096-cell periodic lines; returns points/s per RK3 step."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import numpy as np
+    import common as cm
+    import oracle_lib as orc
+    from opflow_gb300 import _capi as capi
+    from opflow_gb300 import api
+    used = orc.lib().or_set_threads(threads)
+    nx, ny = 4096, 256
+    mesh = cm.mesh_uniform([nx + 1, ny + 1])
+    fd = cm.field_desc(2, capi.CENTER, [(capi.BC_PERIODIC, capi.BC_PERIODIC)] * 2, ext=3)
+    h0 = orc.HostField(mesh, fd)
+    h0.data[h0.slices(h0.assignable())] = weno_u0(np, 7, nx, ny)
+    h0.update_padding()
+    h1 = orc.HostField(mesh, fd, data=h0.data.copy())
+    h2 = orc.HostField(mesh, fd, data=h0.data.copy())
+    L = [cm.Leaf("u"), cm.Leaf("u1"), cm.Leaf("u2")]
+    ns = [api.serialize(x, L)[0] for x in cm.weno_stage_exprs(L[0], L[1], L[2], 0.5 / nx)]
+    steps = 2
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        orc.assign(h1, ns[0], [h0, h1, h2])
+        orc.assign(h2, ns[1], [h0, h1, h2])
+        orc.assign(h0, ns[2], [h0, h1, h2])
+    dt = time.perf_counter() - t0
+    return nx * ny * steps / dt / 1e9, "%d x %d periodic lines, %d RK3 steps of the three stage assignments (oracle, %d threads)" % (nx, ny, steps, used), used
+
+
+def run_weno(args, torch, api, capi, np, ctx, stream, world, rank, local, dist):
+    nx = 4096
+    ny = args.grid or 65536
+    mesh = api.MeshBuilder().newMesh(nx + 1, ny + 1).setMeshOfDim(0, 0.0, 1.0).setMeshOfDim(1, 0.0, ny / nx).build()
+    b = api.ExprBuilder().setMesh(mesh).setName("u").setLoc(api.LocOnMesh.Center).setExt(3)
+    for d in range(2):
+        b.setBC(d, api.DimPos.start, api.BCType.Periodic, 0.0).setBC(d, api.DimPos.end, api.BCType.Periodic, 0.0)
+    u = b.build(ctx)
+    host = u.download()
+    host[u.index_slices(u.assignableRange)] = weno_u0(np, 2024 + rank, nx, ny)
+    u.upload(host)
+    hb = torch.from_numpy(host).pin_memory()
+    dt = 0.5 / nx
+    api.weno_rk3(u, dt, args.warmup)
+    torch.cuda.synchronize()
+    l0 = capi.launch_count()
+    if world > 1:
+        dist.barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        api.weno_rk3(u, dt, args.steps)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    launches = capi.launch_count() - l0
+    if world > 1:
+        tt = torch.tensor([ms], device=torch.device("cuda", local))
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    pts = nx * ny
+    value = pts * args.steps * world / (ms * 1e-3) / 1e9
+    ms_step = ms / args.steps
+    # end to end: host field in, one RK3 step, host field out
+    P = C.POINTER(C.c_double)
+    L = capi.lib()
+    cnt = hb.numel()
+    e2e_steps = 2
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        capi.check(L.opflow_field_upload(u.handle, C.cast(hb.data_ptr(), P), cnt))
+        api.weno_rk3(u, dt, 1)
+        capi.check(L.opflow_field_download(u.handle, C.cast(hb.data_ptr(), P), cnt))
+    e2e_s = time.perf_counter() - t0
+    peak, src = peak_hbm()
+    alg = 16.0 * pts
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            v, sample, used = cpu_weno_sample(os.cpu_count() or 1)
+            cpu = {"value": v, "unit": "Gpts/s", "cores": used, "kind": "port", "sample": sample}
+        except Exception as ex:
+            cpu = {"value": None, "unit": "Gpts/s", "cores": 0, "kind": "port", "sample": "failed: %s" % ex}
+    line = {"metric": METRIC, "value": value, "unit": "Gpts/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "weno", "lines": ny, "line_cells": nx, "scheme": "WENO5-JS (D1WENO53Downwind<0>) + Shu-Osher RK3, fused",
+                       "cfl": 0.5, "bc": "periodic", "init": "seeded square + cosine pulses per line", "unit": "cell updates per RK3 step",
+                       "l2": "field %.1f GB > L2" % (pts * 8 / 1e9), "parallelism": "replicas" if world > 1 else "single"},
+            "roofline": {"bound": "fp64", "achieved": alg / (ms_step * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": alg / (ms_step * 1e-3) / 1e9 / peak, "peak_source": src, "traffic": traffic_for("weno"),
+                         "kernel": "weno_rk3_kernel", "algorithmic_bytes_per_launch": alg},
+            "cpu_baseline": cpu,
+            "e2e": {"value": pts * e2e_steps / e2e_s / 1e9, "unit": "Gpts/s", "h2d_bytes_per_step": cnt * 8, "d2h_bytes_per_step": cnt * 8},
+            "gpu_launches": launches, "clocks": clk.summary()}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
 # ------------------------------------------------------------------------------------------- ours
 def run_ours(args):
     import torch
@@ -422,11 +706,11 @@ def run_ours(args):
     torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
 
-    if args.workload in ("poisson2d", "serve"):
+    if args.workload in SOLVE_WORKLOADS:
         if world > 1:
             dist.barrier()
         with ClockSampler(local) as clk:
-            fn = run_poisson2d if args.workload == "poisson2d" else run_serve
+            fn = {"poisson2d": run_poisson2d, "serve": run_serve, "batched": run_batched, "poisson3d": run_poisson3d}[args.workload]
             r = fn(args, torch, api, capi, np, ctx, stream, world, rank, local)
         value = r["value"]
         if world > 1:
@@ -449,6 +733,9 @@ def run_ours(args):
         if world > 1:
             dist.destroy_process_group()
         return 0
+
+    if args.workload == "weno":
+        return run_weno(args, torch, api, capi, np, ctx, stream, world, rank, local, dist)
 
     cfg = workload_cfg(args.workload)
     if args.grid:
@@ -544,7 +831,9 @@ def run_ours(args):
         "config": dict(cfg, mode=mode, parallelism="replicas" if world > 1 else "single"),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_src, "traffic": traffic_for(args.workload + "_" + mode),
-                     "kernel": "fast_stencil_kernel" if mode == "fast" else "ftcs_exact_kernel",
+                     "kernel": ("axis3d_rb_kernel<FAST>" if mode == "fast" else "axis3d_kernel<EXACT>") if D == 3
+                               else ("axis2d_kernel<FAST>" if mode == "fast" else "axis2d_kernel<EXACT>"),
+                     "timed": "whole step (stencil kernel + ghost-padding kernels), CUDA events on the launching stream",
                      "algorithmic_bytes_per_launch": alg_bytes},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_val, "unit": "GLUP/s", "h2d_bytes_per_step": cnt * 8, "d2h_bytes_per_step": cnt * 8,
@@ -565,7 +854,9 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="serve", choices=["serve", "poisson2d", "ftcs3d", "ftcs2d"])
+    ap.add_argument("--workload", default="serve", choices=["serve", "poisson2d", "poisson3d", "batched", "ftcs3d", "ftcs2d", "weno"])
+    ap.add_argument("--problems", type=int, default=512, help="batched: problems per batch")
+    ap.add_argument("--loop-sample", type=int, default=64, help="batched: problems timed in the plain FP64 one-at-a-time loop")
     ap.add_argument("--requests", type=int, default=48, help="serve: requests per measurement window")
     ap.add_argument("--rate", type=float, default=100.0, help="serve: Poisson arrival rate (requests/s)")
     ap.add_argument("--mode", default="fast", choices=["fast", "exact"])

@@ -572,9 +572,9 @@ int asm_prepare(opflow_ctx ctx, opflow_field target, const opflow_node* nodes, i
 int asm_run(opflow_ctx ctx, AsmPlan* plan, double* coef, double* rhs) {
     const long long N = plan->cells;
     if (N <= 0) return OPFLOW_OK;
-    PInstr* dprog = nullptr;
-    OPG_CUDA(cudaMalloc(&dprog, plan->prog.size() * sizeof(PInstr)));
     OPG_TRY(ensure_scratch(ctx, 64));
+    PInstr* dprog = (PInstr*) dev_alloc(ctx, plan->prog.size() * sizeof(PInstr));
+    if (!dprog) return fail(OPFLOW_E_NOMEM, "assembly program");
     int* err = (int*) ctx->scratch;
     cudaMemsetAsync(err, 0, sizeof(int), ctx->stream);
     cudaMemcpyAsync(dprog, plan->prog.data(), plan->prog.size() * sizeof(PInstr), cudaMemcpyHostToDevice, ctx->stream);
@@ -586,7 +586,7 @@ int asm_run(opflow_ctx ctx, AsmPlan* plan, double* coef, double* rhs) {
     int herr = 0;
     cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
     cudaError_t e = cudaStreamSynchronize(ctx->stream);
-    cudaFree(dprog);
+    dev_free(ctx, dprog);
     if (rc) return rc;
     if (e != cudaSuccess) return fail(OPFLOW_E_CUDA, "assembly failed: %s", cudaGetErrorString(e));
     if (herr) return fail(OPFLOW_E_RANGE, "a folded unknown leaf left the stencil offset set or the logical range");

@@ -93,6 +93,7 @@ int opflow_batch_create(opflow_ctx ctx, const opflow_problem_desc* problems, int
     B->S = new MGSystem();
     MGSystem* S = B->S;
     S->ctx = ctx;
+    S->arena.ctx = ctx;
     S->precision = B->params.precision;
     S->pre = B->params.pre_sweeps;
     S->post = B->params.post_sweeps;
@@ -151,8 +152,7 @@ int opflow_batch_solve(opflow_batch b, opflow_solve_state* states) {
     MGSystem* S = b->S;
     opflow_ctx ctx = b->ctx;
     auto t0 = std::chrono::steady_clock::now();
-    if (b->params.zero_guess)
-        for (size_t p = 0; p < S->probs.size(); ++p) cudaMemsetAsync(S->kd_host[p].x, 0, S->probs[p].levels[0].N * 8, ctx->stream);
+    if (b->params.zero_guess) OPG_TRY(kr_launch_zero_x(ctx->stream, ctx->num_sms, S->dL, S->dK, S->dk0, S->nk0));
     OPG_TRY(mg_solve(S));
     std::vector<Scal> st;
     OPG_TRY(mg_states(S, st));

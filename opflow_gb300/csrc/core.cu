@@ -29,12 +29,47 @@ int check_launch(const char* what) {
     return OPFLOW_OK;
 }
 
+static std::mutex g_pool_mu;
+static cudaMemPool_t g_pool[64] = {};
+
+static cudaMemPool_t device_pool(int dev) {
+    if (dev < 0 || dev >= 64) return nullptr;
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    if (!g_pool[dev]) {
+        cudaMemPoolProps props{};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        cudaMemPool_t p = nullptr;
+        if (cudaMemPoolCreate(&p, &props) != cudaSuccess) return nullptr;
+        uint64_t keep = ~0ull;  // never hand memory back at synchronisation points
+        cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep);
+        g_pool[dev] = p;
+    }
+    return g_pool[dev];
+}
+
+void* dev_alloc(opflow_ctx ctx, size_t bytes) {
+    void* p = nullptr;
+    cudaMemPool_t pool = device_pool(ctx->device);
+    if (!pool || cudaMallocFromPoolAsync(&p, bytes, pool, ctx->stream) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return p;
+}
+
+void dev_free(opflow_ctx ctx, void* p) {
+    if (p) cudaFreeAsync(p, ctx->stream);
+}
+
 int ensure_scratch(opflow_ctx ctx, size_t bytes) {
     if (ctx->scratch_bytes >= bytes) return OPFLOW_OK;
-    if (ctx->scratch) cudaFree(ctx->scratch);
+    if (ctx->scratch) dev_free(ctx, ctx->scratch);
     ctx->scratch = nullptr;
     ctx->scratch_bytes = 0;
-    OPG_CUDA(cudaMalloc(&ctx->scratch, bytes));
+    ctx->scratch = dev_alloc(ctx, bytes);
+    if (!ctx->scratch) return fail(OPFLOW_E_NOMEM, "cannot allocate %zu bytes of scratch", bytes);
     ctx->scratch_bytes = bytes;
     return OPFLOW_OK;
 }
@@ -356,9 +391,8 @@ int update_padding_assign(opflow_field f) {
 
 int ensure_back(opflow_field f) {
     if (f->buf[1 - f->cur]) return OPFLOW_OK;
-    double* p = nullptr;
-    if (cudaMalloc(&p, f->info.count * sizeof(double)) != cudaSuccess)
-        return fail(OPFLOW_E_NOMEM, "cannot allocate the second buffer of a field (%zu doubles)", f->info.count);
+    double* p = (double*) dev_alloc(f->ctx, f->info.count * sizeof(double));
+    if (!p) return fail(OPFLOW_E_NOMEM, "cannot allocate the second buffer of a field (%zu doubles)", f->info.count);
     OPG_CUDA(cudaMemcpyAsync(p, f->buf[f->cur], f->info.count * sizeof(double), cudaMemcpyDeviceToDevice, f->ctx->stream));
     f->buf[1 - f->cur] = p;
     f->bc_fresh[1 - f->cur] = f->bc_fresh[f->cur];
@@ -423,8 +457,8 @@ int opflow_ctx_create(int device, opflow_ctx* out) {
 
 int opflow_ctx_destroy(opflow_ctx ctx) {
     if (!ctx) return OPFLOW_OK;
+    if (ctx->scratch) dev_free(ctx, ctx->scratch);
     cudaStreamSynchronize(ctx->stream);
-    if (ctx->scratch) cudaFree(ctx->scratch);
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return OPFLOW_OK;
@@ -480,7 +514,8 @@ int opflow_field_create(opflow_ctx ctx, const opflow_mesh_desc* mesh, const opfl
     f->desc = *desc;
     f->info = info;
     f->mesh = md;
-    if (cudaMalloc(&f->buf[0], info.count * sizeof(double)) != cudaSuccess) {
+    f->buf[0] = (double*) dev_alloc(ctx, info.count * sizeof(double));
+    if (!f->buf[0]) {
         mesh_destroy(md);
         delete f;
         return fail(OPFLOW_E_NOMEM, "cannot allocate %zu doubles", info.count);
@@ -491,15 +526,17 @@ int opflow_field_create(opflow_ctx ctx, const opflow_mesh_desc* mesh, const opfl
         opflow_field_destroy(f);
         return rc;
     }
+    // the data array is usable from any stream once created
+    OPG_CUDA(cudaStreamSynchronize(ctx->stream));
     *out = f;
     return OPFLOW_OK;
 }
 
 int opflow_field_destroy(opflow_field f) {
     if (!f) return OPFLOW_OK;
-    cudaStreamSynchronize(f->ctx->stream);
+    // freed in the order of the context's stream, after the work already enqueued on it
     for (int k = 0; k < 2; ++k)
-        if (f->buf[k]) cudaFree(f->buf[k]);
+        if (f->buf[k]) dev_free(f->ctx, f->buf[k]);
     mesh_destroy(f->mesh);
     delete f;
     return OPFLOW_OK;

@@ -124,6 +124,12 @@ int update_padding_buf(opflow_field f, double* data);
 int update_padding_assign(opflow_field f);
 bool padding_self_overlaps(opflow_field f);
 int ensure_scratch(opflow_ctx ctx, size_t bytes);
+// Device memory of a context: stream-ordered allocations on the context's stream from a per-device
+// pool that keeps its memory (no device-wide synchronisation on free, cheap reuse).  Memory returned
+// by dev_alloc is usable on the context's stream at once and on other streams after that stream
+// has been synchronised.
+void* dev_alloc(opflow_ctx ctx, size_t bytes);
+void dev_free(opflow_ctx ctx, void* p);
 int compute_info(const opflow_mesh_desc* m, const opflow_field_desc* f, opflow_field_info* o);
 Box assign_box(const opflow_field_info& r);
 }  // namespace opg

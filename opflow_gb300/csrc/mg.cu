@@ -71,14 +71,19 @@ __global__ void __launch_bounds__(256) mg_coarse(const LvlDev* __restrict__ Ls, 
 }
 
 // ---- bottom kernel (small levels)
-// Walks every cell of level L in x-fastest order; for a red-black color only the cells of that color.
+// Walks every cell of level L (for a red-black color only the cells of that color): warps take rows,
+// lanes take columns, so no thread divides a cell index.
 template <typename T, typename F>
 __device__ __forceinline__ void for_cells(const LvlDev& L, int color, F&& f) {
-    const int n0 = L.n[0], n1 = L.n[1];
-    for (int c = threadIdx.x; c < (int) L.N; c += blockDim.x) {
-        const int i = c % n0, jk = c / n0, j = jk % n1, k = jk / n1;
-        if (color >= 0 && ((i + j + k) & 1) != color) continue;
-        f(i, j, k);
+    const int n0 = L.n[0], n1 = L.n[1], rows = L.n[1] * L.n[2];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int row = warp; row < rows; row += nw) {
+        const int j = row % n1, k = row / n1;
+        if (color < 0) {
+            for (int i = lane; i < n0; i += 32) f(i, j, k);
+        } else {
+            for (int i = ((j + k + color) & 1) + 2 * lane; i < n0; i += 64) f(i, j, k);
+        }
     }
 }
 
@@ -89,13 +94,32 @@ __device__ __forceinline__ void bottom_smooth(const LvlDev& L, int color) {
     __syncthreads();
 }
 
-// The V-cycle below (and including) a problem's first small level, one CTA per problem: the
-// restriction into that level, pre-smoothing, residuals and restrictions down to the coarsest level,
-// the coarsest solve, then prolongation and post-smoothing back up - the same operations in the same
-// order as the chunked kernels, with a CTA barrier where those have a launch boundary.
+// Points the level's V-cycle vectors (of precision T) at x, b, r.
+template <typename T>
+__device__ __forceinline__ void set_vectors(LvlDev& L, T* x, T* b, T* r);
+template <>
+__device__ __forceinline__ void set_vectors<float>(LvlDev& L, float* x, float* b, float* r) {
+    L.x32 = x;
+    L.b32 = b;
+    L.r32 = r;
+}
+template <>
+__device__ __forceinline__ void set_vectors<double>(LvlDev& L, double* x, double* b, double* r) {
+    L.x64 = x;
+    L.b64 = b;
+    L.r64 = r;
+}
+
+// The V-cycle below (and including) a problem's first small level, one CTA per problem, with the
+// levels' x, b and r in shared memory: the restriction into that level (unless a tiled finer level
+// did it), pre-smoothing, residuals and restrictions down to the coarsest level, the coarsest solve,
+// then prolongation and post-smoothing back up - the chunked kernels' operations in their order, with
+// a CTA barrier where those have a launch boundary - and the first level's x written back.
 template <typename T>
 __global__ void __launch_bounds__(512) mg_bottom(const LvlDev* __restrict__ Ls, const int* __restrict__ top, int ntop, const Scal* sc, int pre,
                                                  int post) {
+    extern __shared__ __align__(16) unsigned char bottom_smem[];
+    __shared__ LvlDev Lsm[MG_BOTTOM_LEVELS];
     for (int q = blockIdx.x; q < ntop; q += gridDim.x) {
         const int s = top[q];
         if (sc && !sc[Ls[s].problem].active) continue;
@@ -104,22 +128,47 @@ __global__ void __launch_bounds__(512) mg_bottom(const LvlDev* __restrict__ Ls, 
             for_cells<T>(L, -1, [&](int i, int j, int k) { cell_restrict<T>(Ls, L, i, j, k); });
             __syncthreads();
         }
-        int l = s;
-        while (!Ls[l].coarsest) {
-            const LvlDev& L = Ls[l];
+        if (threadIdx.x == 0) {
+            T* p = (T*) bottom_smem;
+            int l = s;
+            for (int i = 0; i < MG_BOTTOM_LEVELS; ++i) {
+                Lsm[i] = Ls[l];
+                Lsm[i].fine = i - 1;
+                Lsm[i].coarse = Ls[l].coarsest ? -1 : i + 1;
+                const long long N = Ls[l].N;
+                set_vectors<T>(Lsm[i], p, p + N, p + 2 * N);
+                p += 3 * N;
+                if (Ls[l].coarsest) break;
+                l = Ls[l].coarse;
+            }
+        }
+        __syncthreads();
+        {
+            const T* bg = Sel<T>::b(Ls[s]);
+            T* bs = Sel<T>::b(Lsm[0]);
+            T* xs = Sel<T>::x(Lsm[0]);
+            for (int c = threadIdx.x; c < (int) Lsm[0].N; c += blockDim.x) {
+                bs[c] = bg[c];
+                xs[c] = 0;
+            }
+        }
+        __syncthreads();
+        int l = 0;
+        while (!Lsm[l].coarsest) {
+            const LvlDev& L = Lsm[l];
             for (int it = 0; it < pre; ++it) {
                 bottom_smooth<T>(L, 0);
                 bottom_smooth<T>(L, 1);
             }
             for_cells<T>(L, -1, [&](int i, int j, int k) { cell_residual<T>(L, i, j, k); });
             __syncthreads();
-            const LvlDev& Lc = Ls[L.coarse];
-            for_cells<T>(Lc, -1, [&](int i, int j, int k) { cell_restrict<T>(Ls, Lc, i, j, k); });
+            const LvlDev& Lc = Lsm[L.coarse];
+            for_cells<T>(Lc, -1, [&](int i, int j, int k) { cell_restrict<T>(Lsm, Lc, i, j, k); });
             __syncthreads();
             l = L.coarse;
         }
         {
-            const LvlDev& L = Ls[l];
+            const LvlDev& L = Lsm[l];
             if (L.Ainv64) {
                 coarse_rows<T>(L, threadIdx.x, blockDim.x);
                 __syncthreads();
@@ -130,15 +179,20 @@ __global__ void __launch_bounds__(512) mg_bottom(const LvlDev* __restrict__ Ls, 
                 }
             }
         }
-        while (l != s) {
-            const LvlDev& Lf = Ls[Ls[l].fine];
-            for_cells<T>(Lf, -1, [&](int i, int j, int k) { cell_prolong<T>(Ls, Lf, i, j, k); });
+        while (l != 0) {
+            const LvlDev& Lf = Lsm[Lsm[l].fine];
+            for_cells<T>(Lf, -1, [&](int i, int j, int k) { cell_prolong<T>(Lsm, Lf, i, j, k); });
             __syncthreads();
             for (int it = 0; it < post; ++it) {
                 bottom_smooth<T>(Lf, 1);
                 bottom_smooth<T>(Lf, 0);
             }
-            l = Ls[l].fine;
+            l = Lsm[l].fine;
+        }
+        {
+            T* xg = Sel<T>::x(Ls[s]);
+            const T* xs = Sel<T>::x(Lsm[0]);
+            for (int c = threadIdx.x; c < (int) Lsm[0].N; c += blockDim.x) xg[c] = xs[c];
         }
         __syncthreads();
     }
@@ -217,8 +271,10 @@ __device__ __forceinline__ void chunk_finish(const Finish& F, int p, const doubl
 }
 
 // mode 0: r = b - A x, partial (b.b, r.r)        mode 1: q = A p, partial (p.q)
+// With to_vc (mode 0) the V-cycle's level-0 input is written as well: b = (T) r, x = 0.
+template <typename T>
 __global__ void __launch_bounds__(256) kr_apply(const LvlDev* __restrict__ Ls, const KrylovDev* __restrict__ K, const Chunk* __restrict__ ch, int nch,
-                                                const Scal* sc, double* partial, int mode, Finish F) {
+                                                const Scal* sc, double* partial, int mode, int to_vc, Finish F) {
     __shared__ double sh[32];
     __shared__ int flag;
     for (int c = blockIdx.x; c < nch; c += gridDim.x) {
@@ -229,23 +285,35 @@ __global__ void __launch_bounds__(256) kr_apply(const LvlDev* __restrict__ Ls, c
         const KrylovDev& Kp = K[pb];
         double s0 = 0., s1 = 0.;
         if (act) {
-            const double* in = mode == 0 ? Kp.x : Kp.p;
-            for (int t = threadIdx.x; t < C.cnt; t += blockDim.x) {
-                const int i = C.i0 + t;
-                const long long cell = cell_of(L, i, C.j, C.k);
-                double c0, offd;
-                stencil_parts<double>(L, in, i, C.j, C.k, cell, c0, offd);
-                const double ax = fma(c0, in[cell], offd);
-                if (mode == 0) {
-                    const double r = Kp.b[cell] - ax;
-                    Kp.r[cell] = r;
-                    s0 = fma(Kp.b[cell], Kp.b[cell], s0);
-                    s1 = fma(r, r, s1);
-                } else {
-                    Kp.q[cell] = ax;
-                    s0 = fma(in[cell], ax, s0);
+            const double* __restrict__ in = mode == 0 ? Kp.x : Kp.p;
+            const double* __restrict__ bp = Kp.b;
+            double* __restrict__ rp = Kp.r;
+            double* __restrict__ qp = Kp.q;
+            T* __restrict__ vb = Sel<T>::b(L);
+            T* __restrict__ vx = Sel<T>::x(L);
+            for (int rw = 0; rw < C.nrows; ++rw)
+#pragma unroll 4
+                for (int t = threadIdx.x; t < C.cnt; t += blockDim.x) {
+                    const int i = C.i0 + t, j = C.j + rw;
+                    const long long cell = cell_of(L, i, j, C.k);
+                    double c0, offd;
+                    stencil_parts<double>(L, in, i, j, C.k, cell, c0, offd);
+                    const double ax = fma(c0, in[cell], offd);
+                    if (mode == 0) {
+                        const double bv = bp[cell];
+                        const double r = bv - ax;
+                        rp[cell] = r;
+                        s0 = fma(bv, bv, s0);
+                        s1 = fma(r, r, s1);
+                        if (to_vc) {
+                            vb[cell] = (T) r;
+                            vx[cell] = 0;
+                        }
+                    } else {
+                        qp[cell] = ax;
+                        s0 = fma(in[cell], ax, s0);
+                    }
                 }
-            }
         }
         const double a = block_sum(s0, sh);
         const double b = block_sum(s1, sh);
@@ -257,7 +325,8 @@ __global__ void __launch_bounds__(256) kr_apply(const LvlDev* __restrict__ Ls, c
     }
 }
 
-// x += alpha p, r -= alpha q, partial (r.r)
+// x += alpha p, r -= alpha q, partial (r.r); the V-cycle's level-0 input b = (T) r, x = 0 alongside
+template <typename T>
 __global__ void __launch_bounds__(256) kr_update(const LvlDev* __restrict__ Ls, const KrylovDev* __restrict__ K, const Chunk* __restrict__ ch, int nch,
                                                  const Scal* sc, double* partial, Finish F) {
     __shared__ double sh[32];
@@ -271,13 +340,23 @@ __global__ void __launch_bounds__(256) kr_update(const LvlDev* __restrict__ Ls, 
         double s = 0.;
         if (act) {
             const double al = sc[pb].alpha;
-            for (int t = threadIdx.x; t < C.cnt; t += blockDim.x) {
-                const long long cell = cell_of(L, C.i0 + t, C.j, C.k);
-                Kp.x[cell] = fma(al, Kp.p[cell], Kp.x[cell]);
-                const double r = fma(-al, Kp.q[cell], Kp.r[cell]);
-                Kp.r[cell] = r;
-                s = fma(r, r, s);
-            }
+            double* __restrict__ xp = Kp.x;
+            const double* __restrict__ pp = Kp.p;
+            double* __restrict__ rp = Kp.r;
+            const double* __restrict__ qp = Kp.q;
+            T* __restrict__ vb = Sel<T>::b(L);
+            T* __restrict__ vx = Sel<T>::x(L);
+            for (int rw = 0; rw < C.nrows; ++rw)
+#pragma unroll 4
+                for (int t = threadIdx.x; t < C.cnt; t += blockDim.x) {
+                    const long long cell = cell_of(L, C.i0 + t, C.j + rw, C.k);
+                    xp[cell] = fma(al, pp[cell], xp[cell]);
+                    const double r = fma(-al, qp[cell], rp[cell]);
+                    rp[cell] = r;
+                    s = fma(r, r, s);
+                    vb[cell] = (T) r;
+                    vx[cell] = 0;
+                }
         }
         const double a = block_sum(s, sh);
         if (threadIdx.x == 0) { partial[2 * c] = act ? a : 0.; partial[2 * c + 1] = 0.; }
@@ -285,26 +364,7 @@ __global__ void __launch_bounds__(256) kr_update(const LvlDev* __restrict__ Ls, 
     }
 }
 
-// level-0 V-cycle input from r (float64 -> T) and zero initial guess
-template <typename T>
-__global__ void __launch_bounds__(256) kr_to_vcycle(const LvlDev* __restrict__ Ls, const KrylovDev* __restrict__ K, const Chunk* __restrict__ ch, int nch,
-                                                    const Scal* sc) {
-    for (int c = blockIdx.x; c < nch; c += gridDim.x) {
-        const Chunk C = ch[c];
-        const LvlDev& L = Ls[C.lvl];
-        if (sc && !sc[L.problem].active) continue;
-        const KrylovDev& Kp = K[L.problem];
-        T* b = Sel<T>::b(L);
-        T* x = Sel<T>::x(L);
-        for (int t = threadIdx.x; t < C.cnt; t += blockDim.x) {
-            const long long cell = cell_of(L, C.i0 + t, C.j, C.k);
-            b[cell] = (T) Kp.r[cell];
-            x[cell] = 0;
-        }
-    }
-}
-
-// z = V-cycle result; partial (z.r, z.q)
+// z = V-cycle result (read where it lies, never stored); partial (z.r, z.q)
 template <typename T>
 __global__ void __launch_bounds__(256) kr_from_vcycle(const LvlDev* __restrict__ Ls, const KrylovDev* __restrict__ K, const Chunk* __restrict__ ch,
                                                       int nch, const Scal* sc, double* partial, Finish F) {
@@ -315,16 +375,19 @@ __global__ void __launch_bounds__(256) kr_from_vcycle(const LvlDev* __restrict__
         const LvlDev& L = Ls[C.lvl];
         const bool act = !sc || sc[L.problem].active;
         const KrylovDev& Kp = K[L.problem];
-        const T* x = Sel<T>::x(L);
+        const T* __restrict__ x = Sel<T>::x(L);
         double s0 = 0., s1 = 0.;
         if (act) {
-            for (int t = threadIdx.x; t < C.cnt; t += blockDim.x) {
-                const long long cell = cell_of(L, C.i0 + t, C.j, C.k);
-                const double z = (double) x[cell];
-                Kp.z[cell] = z;
-                s0 = fma(z, Kp.r[cell], s0);
-                s1 = fma(z, Kp.q[cell], s1);
-            }
+            const double* __restrict__ rp = Kp.r;
+            const double* __restrict__ qp = Kp.q;
+            for (int rw = 0; rw < C.nrows; ++rw)
+#pragma unroll 4
+                for (int t = threadIdx.x; t < C.cnt; t += blockDim.x) {
+                    const long long cell = cell_of(L, C.i0 + t, C.j + rw, C.k);
+                    const double z = (double) x[cell];
+                    s0 = fma(z, rp[cell], s0);
+                    s1 = fma(z, qp[cell], s1);
+                }
         }
         const double a = block_sum(s0, sh);
         const double b = block_sum(s1, sh);
@@ -333,7 +396,19 @@ __global__ void __launch_bounds__(256) kr_from_vcycle(const LvlDev* __restrict__
     }
 }
 
-// p = z + beta p   (beta = 0 for the first direction)
+// x = 0 for every problem (zero initial guess), one launch for the whole batch
+__global__ void __launch_bounds__(256) kr_zero_x(const LvlDev* __restrict__ Ls, const KrylovDev* __restrict__ K, const Chunk* __restrict__ ch, int nch) {
+    for (int c = blockIdx.x; c < nch; c += gridDim.x) {
+        const Chunk C = ch[c];
+        const LvlDev& L = Ls[C.lvl];
+        const KrylovDev& Kp = K[L.problem];
+        for (int rw = 0; rw < C.nrows; ++rw)
+            for (int t = threadIdx.x; t < C.cnt; t += blockDim.x) Kp.x[cell_of(L, C.i0 + t, C.j + rw, C.k)] = 0.;
+    }
+}
+
+// p = z + beta p with z the V-cycle result (beta = 0 for the first direction)
+template <typename T>
 __global__ void __launch_bounds__(256) kr_pupdate(const LvlDev* __restrict__ Ls, const KrylovDev* __restrict__ K, const Chunk* __restrict__ ch, int nch,
                                                   const Scal* sc, int first) {
     for (int c = blockIdx.x; c < nch; c += gridDim.x) {
@@ -342,10 +417,15 @@ __global__ void __launch_bounds__(256) kr_pupdate(const LvlDev* __restrict__ Ls,
         if (!sc[L.problem].active) continue;
         const KrylovDev& Kp = K[L.problem];
         const double be = first ? 0. : sc[L.problem].beta;
-        for (int t = threadIdx.x; t < C.cnt; t += blockDim.x) {
-            const long long cell = cell_of(L, C.i0 + t, C.j, C.k);
-            Kp.p[cell] = first ? Kp.z[cell] : fma(be, Kp.p[cell], Kp.z[cell]);
-        }
+        const T* __restrict__ x = Sel<T>::x(L);
+        double* __restrict__ pp = Kp.p;
+        for (int rw = 0; rw < C.nrows; ++rw)
+#pragma unroll 4
+            for (int t = threadIdx.x; t < C.cnt; t += blockDim.x) {
+                const long long cell = cell_of(L, C.i0 + t, C.j + rw, C.k);
+                const double z = (double) x[cell];
+                pp[cell] = first ? z : fma(be, pp[cell], z);
+            }
     }
 }
 
@@ -421,34 +501,42 @@ int mg_launch_coarse(cudaStream_t s, int sms, bool f32, const LvlDev* L, const i
     OPG_LAUNCHED();
     return check_launch("mg_coarse");
 }
-int mg_launch_bottom(cudaStream_t s, int sms, bool f32, const LvlDev* L, const int* top, int ntop, const Scal* sc, int pre, int post) {
+int mg_bottom_prepare() {
+    const size_t need[2] = {3 * MG_BOTTOM_CELLS * sizeof(float), 3 * MG_BOTTOM_CELLS * sizeof(double)};
+    const void* fn[2] = {(const void*) mg_bottom<float>, (const void*) mg_bottom<double>};
+    for (int q = 0; q < 2; ++q) {
+        const cudaError_t e = cudaFuncSetAttribute(fn[q], cudaFuncAttributeMaxDynamicSharedMemorySize, (int) need[q]);
+        if (e != cudaSuccess) return fail(OPFLOW_E_CUDA, "bottom kernel: shared memory %zu B: %s", need[q], cudaGetErrorString(e));
+    }
+    return OPFLOW_OK;
+}
+
+int mg_launch_bottom(cudaStream_t s, int sms, bool f32, const LvlDev* L, const int* top, int ntop, const Scal* sc, int pre, int post,
+                     long long cells) {
     if (ntop <= 0) return OPFLOW_OK;
-    const int g = std::min(ntop, sms * 4);
-    if (f32) mg_bottom<float><<<g, 512, 0, s>>>(L, top, ntop, sc, pre, post);
-    else mg_bottom<double><<<g, 512, 0, s>>>(L, top, ntop, sc, pre, post);
+    if (cells > MG_BOTTOM_CELLS) return fail(OPFLOW_E_INVALID, "bottom levels hold %lld cells (limit %d)", cells, MG_BOTTOM_CELLS);
+    const int g = std::min(ntop, sms * 2);
+    const size_t smem = (size_t) (3 * cells) * (f32 ? sizeof(float) : sizeof(double));
+    if (f32) mg_bottom<float><<<g, 512, smem, s>>>(L, top, ntop, sc, pre, post);
+    else mg_bottom<double><<<g, 512, smem, s>>>(L, top, ntop, sc, pre, post);
     OPG_LAUNCHED();
     return check_launch("mg_bottom");
 }
 int kr_launch_apply(cudaStream_t s, int sms, const LvlDev* L, const KrylovDev* K, const Chunk* ch, int nch, const Scal* sc, double* partial, int mode,
-                    const Finish& F) {
+                    const Finish& F, int to_vc, bool f32) {
     if (nch <= 0) return OPFLOW_OK;
-    kr_apply<<<grid_of(nch, sms), 256, 0, s>>>(L, K, ch, nch, sc, partial, mode, F);
+    if (f32) kr_apply<float><<<grid_of(nch, sms), 256, 0, s>>>(L, K, ch, nch, sc, partial, mode, to_vc, F);
+    else kr_apply<double><<<grid_of(nch, sms), 256, 0, s>>>(L, K, ch, nch, sc, partial, mode, to_vc, F);
     OPG_LAUNCHED();
     return check_launch("kr_apply");
 }
-int kr_launch_update(cudaStream_t s, int sms, const LvlDev* L, const KrylovDev* K, const Chunk* ch, int nch, const Scal* sc, double* partial,
+int kr_launch_update(cudaStream_t s, int sms, bool f32, const LvlDev* L, const KrylovDev* K, const Chunk* ch, int nch, const Scal* sc, double* partial,
                      const Finish& F) {
     if (nch <= 0) return OPFLOW_OK;
-    kr_update<<<grid_of(nch, sms), 256, 0, s>>>(L, K, ch, nch, sc, partial, F);
+    if (f32) kr_update<float><<<grid_of(nch, sms), 256, 0, s>>>(L, K, ch, nch, sc, partial, F);
+    else kr_update<double><<<grid_of(nch, sms), 256, 0, s>>>(L, K, ch, nch, sc, partial, F);
     OPG_LAUNCHED();
     return check_launch("kr_update");
-}
-int kr_launch_to_vcycle(cudaStream_t s, int sms, bool f32, const LvlDev* L, const KrylovDev* K, const Chunk* ch, int nch, const Scal* sc) {
-    if (nch <= 0) return OPFLOW_OK;
-    if (f32) kr_to_vcycle<float><<<grid_of(nch, sms), 256, 0, s>>>(L, K, ch, nch, sc);
-    else kr_to_vcycle<double><<<grid_of(nch, sms), 256, 0, s>>>(L, K, ch, nch, sc);
-    OPG_LAUNCHED();
-    return check_launch("kr_to_vcycle");
 }
 int kr_launch_from_vcycle(cudaStream_t s, int sms, bool f32, const LvlDev* L, const KrylovDev* K, const Chunk* ch, int nch, const Scal* sc,
                           double* partial, const Finish& F) {
@@ -458,11 +546,18 @@ int kr_launch_from_vcycle(cudaStream_t s, int sms, bool f32, const LvlDev* L, co
     OPG_LAUNCHED();
     return check_launch("kr_from_vcycle");
 }
-int kr_launch_pupdate(cudaStream_t s, int sms, const LvlDev* L, const KrylovDev* K, const Chunk* ch, int nch, const Scal* sc, int first) {
+int kr_launch_pupdate(cudaStream_t s, int sms, bool f32, const LvlDev* L, const KrylovDev* K, const Chunk* ch, int nch, const Scal* sc, int first) {
     if (nch <= 0) return OPFLOW_OK;
-    kr_pupdate<<<grid_of(nch, sms), 256, 0, s>>>(L, K, ch, nch, sc, first);
+    if (f32) kr_pupdate<float><<<grid_of(nch, sms), 256, 0, s>>>(L, K, ch, nch, sc, first);
+    else kr_pupdate<double><<<grid_of(nch, sms), 256, 0, s>>>(L, K, ch, nch, sc, first);
     OPG_LAUNCHED();
     return check_launch("kr_pupdate");
+}
+int kr_launch_zero_x(cudaStream_t s, int sms, const LvlDev* L, const KrylovDev* K, const Chunk* ch, int nch) {
+    if (nch <= 0) return OPFLOW_OK;
+    kr_zero_x<<<grid_of(nch, sms), 256, 0, s>>>(L, K, ch, nch);
+    OPG_LAUNCHED();
+    return check_launch("kr_zero_x");
 }
 int kr_launch_reduce(cudaStream_t s, int sms, const double* partial, const int* first, const int* count, int nprob, double* out) {
     kr_reduce<<<std::min(nprob, sms * 8), 256, 0, s>>>(partial, first, count, nprob, out);

@@ -39,15 +39,17 @@ struct LvlDev {
 };
 
 // A row segment of one level: cells (i0 .. i0+cnt-1, j, k) of level `lvl`.
+// The Krylov kernels' chunks on level 0 span `nrows` consecutive rows (j .. j+nrows-1 of plane k).
 struct Chunk {
     int lvl;
     int j, k;
     int i0, cnt;
+    int nrows = 1;
 };
 
 // Per-problem Krylov state (FP64).
 struct KrylovDev {
-    double *x, *r, *z, *p, *q, *b;  // level-0 vectors of the problem
+    double *x, *r, *p, *q, *b;  // level-0 vectors of the problem (z is read from the V-cycle's level-0 x)
     int lvl0;                        // descriptor of level 0
     int pin;                         // pinned unknown index (-1 none)
 };

@@ -14,19 +14,27 @@ bool mg_tiles_supported(int sweeps);
 int mg_tiles_prepare(int sweeps);
 int mg_launch_tile_down(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* tiles, int ntiles, const Scal* sc, int pre);
 int mg_launch_tile_up(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* tiles, int ntiles, const Scal* sc, int post);
-// the whole V-cycle below each listed level (a problem's first small level), one CTA per problem
-int mg_launch_bottom(cudaStream_t s, int sms, bool f32, const LvlDev* L, const int* top, int ntop, const Scal* sc, int pre, int post);
+// the whole V-cycle below each listed level (a problem's first small level), one CTA per problem with
+// those levels' vectors in shared memory: at most MG_BOTTOM_LEVELS levels and MG_BOTTOM_CELLS cells
+// in all (`cells`: the largest such total of the listed problems)
+constexpr int MG_BOTTOM_LEVELS = 12;
+constexpr int MG_BOTTOM_CELLS = 8192;
+int mg_bottom_prepare();
+int mg_launch_bottom(cudaStream_t s, int sms, bool f32, const LvlDev* L, const int* top, int ntop, const Scal* sc, int pre, int post,
+                     long long cells);
 int mg_launch_coarse(cudaStream_t s, int sms, bool f32, const LvlDev* L, const int* lv, int nlv, const Scal* sc);
 // The Krylov kernels write per-chunk partial sums; with F.done set they also reduce them per problem
 // and apply a scalar stage (see Finish), otherwise kr_launch_reduce / kr_launch_scalars do that.
+// to_vc (mode 0): also write the V-cycle's level-0 input (precision f32 ? float : double) from r.
 int kr_launch_apply(cudaStream_t s, int sms, const LvlDev* L, const KrylovDev* K, const Chunk* ch, int nch, const Scal* sc, double* partial, int mode,
-                    const Finish& F = Finish{});
-int kr_launch_update(cudaStream_t s, int sms, const LvlDev* L, const KrylovDev* K, const Chunk* ch, int nch, const Scal* sc, double* partial,
+                    const Finish& F = Finish{}, int to_vc = 0, bool f32 = false);
+// x += alpha p, r -= alpha q and the V-cycle's level-0 input from the new r
+int kr_launch_update(cudaStream_t s, int sms, bool f32, const LvlDev* L, const KrylovDev* K, const Chunk* ch, int nch, const Scal* sc, double* partial,
                      const Finish& F = Finish{});
-int kr_launch_to_vcycle(cudaStream_t s, int sms, bool f32, const LvlDev* L, const KrylovDev* K, const Chunk* ch, int nch, const Scal* sc);
 int kr_launch_from_vcycle(cudaStream_t s, int sms, bool f32, const LvlDev* L, const KrylovDev* K, const Chunk* ch, int nch, const Scal* sc,
                           double* partial, const Finish& F = Finish{});
-int kr_launch_pupdate(cudaStream_t s, int sms, const LvlDev* L, const KrylovDev* K, const Chunk* ch, int nch, const Scal* sc, int first);
+int kr_launch_pupdate(cudaStream_t s, int sms, bool f32, const LvlDev* L, const KrylovDev* K, const Chunk* ch, int nch, const Scal* sc, int first);
+int kr_launch_zero_x(cudaStream_t s, int sms, const LvlDev* L, const KrylovDev* K, const Chunk* ch, int nch);
 int kr_launch_reduce(cudaStream_t s, int sms, const double* partial, const int* first, const int* count, int nprob, double* out);
 int kr_launch_scalars(cudaStream_t s, Scal* sc, const double* red, int nprob, int stage, double tol, int max_iter, int flexible);
 int kr_launch_count(cudaStream_t s, const Scal* sc, int nprob, int* out);

@@ -1,8 +1,8 @@
 // Fused 2D multigrid tile kernels for the large red-black levels with a class-table operator.
 //
 // The chunked kernels make one pass over a level per half-sweep, residual, restriction and
-// prolongation: 2*(pre+post) + 3 launches and as many HBM passes per level.  Here one CTA takes a
-// TX x TY tile plus a halo into shared memory and runs the whole down-leg step of the level in it -
+// prolongation: 2*(pre+post) + 3 launches and as many passes over memory per level.  Here one CTA takes
+// a TX x TY tile plus a halo into shared memory and runs the whole down-leg step of the level in it -
 // pre-smoothing, residual, restriction into the next level - or the whole up-leg step - prolongation
 // and post-smoothing.  Red-black Gauss-Seidel only couples a half-sweep to its neighbours' previous
 // half-sweep, so every half-sweep shrinks the region that is still exact by one cell: with a halo of
@@ -14,11 +14,17 @@
 // so a launch never writes the array it reads: the down step reads x and leaves the smoothed x in the
 // level's r array (the residual itself stays in shared memory), the up step reads that array and
 // writes x.
+//
+// Work layout: warps take rows of the tile region, lanes take columns (a colour's cells with a stride
+// of two), so no thread divides an index.  Tiles whose region lies inside the level away from its
+// boundary take the interior form: constant coefficients, no wrap-around or existence tests.  The tile
+// extent is chosen per level (Chunk.cnt x Chunk.nrows) so that small levels still spread over the SMs.
 #include "mg_device.h"
 
 namespace opg {
 
-constexpr int TILE_X = MG_TILE_X, TILE_Y = MG_TILE_Y, TILE_THREADS = 512;
+constexpr int TILE_THREADS = 256;
+constexpr int TILE_WARPS = TILE_THREADS / 32;
 
 // global index of a tile position along one dim: wrapped for a periodic dim, -1 outside otherwise
 __device__ __forceinline__ int tile_wrap(int g, int n, int per) {
@@ -33,16 +39,17 @@ struct TileView {
     T* x;        // [SY][SX] smem
     T* b;
     int SX, SY, H;
+    int TX, TY;  // tile extent (without halo)
     int i0, j0;  // global origin of the tile (without halo)
+    bool interior;
 };
 
-// One red-black update of smem cell (lx, ly) mirroring global (gi, gj) (both inside the level).
+// One red-black update of smem position s mirroring global (gi, gj), general form.
 template <typename T>
-__device__ __forceinline__ void tile_gs(const LvlDev& L, const T* __restrict__ tab, const TileView<T>& V, int lx, int ly, int gi, int gj) {
+__device__ __forceinline__ void tile_gs(const LvlDev& L, const T* __restrict__ tab, const TileView<T>& V, int s, int gi, int gj) {
     const int n0 = L.n[0], n1 = L.n[1];
     const int cls = pos_class(gi, n0) + 3 * pos_class(gj, n1);
     const T* cf = tab + cls * TSTRIDE;
-    const int s = ly * V.SX + lx;
     T acc = 0;
     if (L.per[0] || gi - 1 >= 0) acc += cf[1] * V.x[s - 1];
     if (L.per[0] || gi + 1 < n0) acc += cf[2] * V.x[s + 1];
@@ -52,11 +59,10 @@ __device__ __forceinline__ void tile_gs(const LvlDev& L, const T* __restrict__ t
 }
 
 template <typename T>
-__device__ __forceinline__ T tile_residual(const LvlDev& L, const T* __restrict__ tab, const TileView<T>& V, int lx, int ly, int gi, int gj) {
+__device__ __forceinline__ T tile_res(const LvlDev& L, const T* __restrict__ tab, const TileView<T>& V, int s, int gi, int gj) {
     const int n0 = L.n[0], n1 = L.n[1];
     const int cls = pos_class(gi, n0) + 3 * pos_class(gj, n1);
     const T* cf = tab + cls * TSTRIDE;
-    const int s = ly * V.SX + lx;
     T acc = 0;
     if (L.per[0] || gi - 1 >= 0) acc += cf[1] * V.x[s - 1];
     if (L.per[0] || gi + 1 < n0) acc += cf[2] * V.x[s + 1];
@@ -65,21 +71,54 @@ __device__ __forceinline__ T tile_residual(const LvlDev& L, const T* __restrict_
     return V.b[s] - (cf[0] * V.x[s] + acc);
 }
 
+// interior coefficients (class 1 + 3*1): the same operations as tile_gs / tile_res with every
+// neighbour present
+template <typename T>
+struct Interior {
+    T c0, c1, c2, c3, c4, inv;
+};
+
+template <typename T>
+__device__ __forceinline__ void int_gs(const Interior<T>& K, const TileView<T>& V, int s) {
+    T acc = 0;
+    acc += K.c1 * V.x[s - 1];
+    acc += K.c2 * V.x[s + 1];
+    acc += K.c3 * V.x[s - V.SX];
+    acc += K.c4 * V.x[s + V.SX];
+    V.x[s] = (V.b[s] - acc) * K.inv;
+}
+
+template <typename T>
+__device__ __forceinline__ T int_res(const Interior<T>& K, const TileView<T>& V, int s) {
+    T acc = 0;
+    acc += K.c1 * V.x[s - 1];
+    acc += K.c2 * V.x[s + 1];
+    acc += K.c3 * V.x[s - V.SX];
+    acc += K.c4 * V.x[s + V.SX];
+    return V.b[s] - (K.c0 * V.x[s] + acc);
+}
+
 // Loads x (from `x`) and b of the tile + halo (positions outside a non-periodic level hold 0 and are
 // never used).
 template <typename T>
 __device__ __forceinline__ void tile_load(const LvlDev& L, const TileView<T>& V, const T* __restrict__ x) {
     const T* b = Sel<T>::b(L);
-    for (int idx = threadIdx.x; idx < V.SX * V.SY; idx += blockDim.x) {
-        const int lx = idx % V.SX, ly = idx / V.SX;
-        const int gi = tile_wrap(V.i0 - V.H + lx, L.n[0], L.per[0]), gj = tile_wrap(V.j0 - V.H + ly, L.n[1], L.per[1]);
-        if (gi >= 0 && gj >= 0) {
-            const long long c = (long long) gj * L.n[0] + gi;
-            V.x[idx] = x[c];
-            V.b[idx] = b[c];
-        } else {
-            V.x[idx] = 0;
-            V.b[idx] = 0;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int ly = warp; ly < V.SY; ly += TILE_WARPS) {
+        const int gjr = V.j0 - V.H + ly;
+        const int gj = V.interior ? gjr : tile_wrap(gjr, L.n[1], L.per[1]);
+        for (int lx = lane; lx < V.SX; lx += 32) {
+            const int gir = V.i0 - V.H + lx;
+            const int gi = V.interior ? gir : tile_wrap(gir, L.n[0], L.per[0]);
+            const int s = ly * V.SX + lx;
+            if (gi >= 0 && gj >= 0) {
+                const long long c = (long long) gj * L.n[0] + gi;
+                V.x[s] = x[c];
+                V.b[s] = b[c];
+            } else {
+                V.x[s] = 0;
+                V.b[s] = 0;
+            }
         }
     }
     __syncthreads();
@@ -87,34 +126,72 @@ __device__ __forceinline__ void tile_load(const LvlDev& L, const TileView<T>& V,
 
 // Half-sweep of `color` over the positions at distance >= d from the region's edge.
 template <typename T>
-__device__ __forceinline__ void tile_sweep(const LvlDev& L, const T* __restrict__ tab, const TileView<T>& V, int color, int d) {
-    const int w = V.SX - 2 * d, h = V.SY - 2 * d;
-    for (int idx = threadIdx.x; idx < w * h; idx += blockDim.x) {
-        const int lx = d + idx % w, ly = d + idx / w;
-        const int gi = tile_wrap(V.i0 - V.H + lx, L.n[0], L.per[0]), gj = tile_wrap(V.j0 - V.H + ly, L.n[1], L.per[1]);
-        if (gi < 0 || gj < 0 || ((gi + gj) & 1) != color) continue;
-        tile_gs<T>(L, tab, V, lx, ly, gi, gj);
+__device__ __forceinline__ void tile_sweep(const LvlDev& L, const T* __restrict__ tab, const Interior<T>& K, const TileView<T>& V, int color, int d) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int ly = d + warp; ly < V.SY - d; ly += TILE_WARPS) {
+        const int gjr = V.j0 - V.H + ly;
+        // first position >= d of this colour: (gi + gj) & 1 == color with gi = i0 - H + lx (wrapping by an
+        // even period keeps the parity)
+        const int lx0 = d + ((color - (V.i0 - V.H + d) - gjr) & 1);
+        if (V.interior) {
+            for (int lx = lx0 + 2 * lane; lx < V.SX - d; lx += 64) int_gs<T>(K, V, ly * V.SX + lx);
+        } else {
+            const int gj = tile_wrap(gjr, L.n[1], L.per[1]);
+            if (gj < 0) continue;
+            for (int lx = lx0 + 2 * lane; lx < V.SX - d; lx += 64) {
+                const int gi = tile_wrap(V.i0 - V.H + lx, L.n[0], L.per[0]);
+                if (gi >= 0) tile_gs<T>(L, tab, V, ly * V.SX + lx, gi, gj);
+            }
+        }
     }
     __syncthreads();
 }
 
 template <typename T>
 __device__ __forceinline__ void tile_store(const LvlDev& L, const TileView<T>& V, T* __restrict__ x) {
-    for (int idx = threadIdx.x; idx < TILE_X * TILE_Y; idx += blockDim.x) {
-        const int tx = idx % TILE_X, ty = idx / TILE_X;
-        const int gi = V.i0 + tx, gj = V.j0 + ty;
-        if (gi < L.n[0] && gj < L.n[1]) x[(long long) gj * L.n[0] + gi] = V.x[(ty + V.H) * V.SX + tx + V.H];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int ty = warp; ty < V.TY; ty += TILE_WARPS) {
+        const int gj = V.j0 + ty;
+        if (gj >= L.n[1]) break;
+        for (int tx = lane; tx < V.TX; tx += 32) {
+            const int gi = V.i0 + tx;
+            if (gi < L.n[0]) x[(long long) gj * L.n[0] + gi] = V.x[(ty + V.H) * V.SX + tx + V.H];
+        }
     }
+}
+
+template <typename T>
+__device__ __forceinline__ void tile_setup(const LvlDev& L, const Chunk& C, int H, T* sm, T* tab, Interior<T>& K, TileView<T>& V) {
+    V.TX = C.cnt;
+    V.TY = C.nrows;
+    V.H = H;
+    V.SX = V.TX + 2 * H;
+    V.SY = V.TY + 2 * H;
+    V.i0 = C.i0;
+    V.j0 = C.j;
+    V.x = sm;
+    V.b = sm + V.SX * V.SY;
+    // inside the level with a cell to spare on each side: every position is an interior-class cell
+    V.interior = V.i0 - H >= 1 && V.i0 + V.TX + H <= L.n[0] - 1 && V.j0 - H >= 1 && V.j0 + V.TY + H <= L.n[1] - 1;
+    for (int q = threadIdx.x; q < NCLASS * TSTRIDE; q += blockDim.x) tab[q] = Sel<T>::Tb(L)[q];
+    const T* ti = Sel<T>::Tb(L) + 4 * TSTRIDE;
+    K.c0 = ti[0];
+    K.c1 = ti[1];
+    K.c2 = ti[2];
+    K.c3 = ti[3];
+    K.c4 = ti[4];
+    K.inv = ti[NSLOT];
 }
 
 // Down-leg step of a 2D level: `pre` red-black sweeps, residual, restriction into the next level (its
 // x set to 0).  reach = 1 for node-centred full weighting (residual needed one cell beyond the tile).
 template <typename T>
-__global__ void __launch_bounds__(TILE_THREADS) mg_tile_down(const LvlDev* __restrict__ Ls, const Chunk* __restrict__ tiles, int ntiles, const Scal* sc,
-                                                             int pre) {
+__global__ void __launch_bounds__(TILE_THREADS, 4) mg_tile_down(const LvlDev* __restrict__ Ls, const Chunk* __restrict__ tiles, int ntiles, const Scal* sc,
+                                                                int pre) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sm = (T*) smem_raw;
     __shared__ T tab[NCLASS * TSTRIDE];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const Chunk C = tiles[t];
         const LvlDev& L = Ls[C.lvl];
@@ -122,27 +199,33 @@ __global__ void __launch_bounds__(TILE_THREADS) mg_tile_down(const LvlDev* __res
         const LvlDev& Lc = Ls[L.coarse];
         const int reach = Lc.node ? 1 : 0;
         TileView<T> V;
-        V.H = 2 * pre + 1 + reach;
-        V.SX = TILE_X + 2 * V.H;
-        V.SY = TILE_Y + 2 * V.H;
-        V.i0 = C.i0;
-        V.j0 = C.j;
-        V.x = sm;
-        V.b = sm + V.SX * V.SY;
-        T* rs = V.b + V.SX * V.SY;  // residual over the tile + reach: (TILE_X + 2 reach) x (TILE_Y + 2 reach)
-        const int RX = TILE_X + 2 * reach;
-        for (int q = threadIdx.x; q < NCLASS * TSTRIDE; q += blockDim.x) tab[q] = Sel<T>::Tb(L)[q];
+        Interior<T> K;
+        tile_setup<T>(L, C, 2 * pre + 1 + reach, sm, tab, K, V);
+        T* rs = V.b + V.SX * V.SY;  // residual over the tile + reach: RX x RY
+        const int RX = V.TX + 2 * reach, RY = V.TY + 2 * reach;
         tile_load<T>(L, V, Sel<T>::x(L));
         for (int it = 0; it < pre; ++it) {
-            tile_sweep<T>(L, tab, V, 0, 2 * it + 1);
-            tile_sweep<T>(L, tab, V, 1, 2 * it + 2);
+            tile_sweep<T>(L, tab, K, V, 0, 2 * it + 1);
+            tile_sweep<T>(L, tab, K, V, 1, 2 * it + 2);
         }
         // residual over the tile + reach (positions outside the level are never read by the restriction)
         const int d = V.H - reach;
-        for (int idx = threadIdx.x; idx < RX * (TILE_Y + 2 * reach); idx += blockDim.x) {
-            const int lx = d + idx % RX, ly = d + idx / RX;
-            const int gi = tile_wrap(V.i0 - V.H + lx, L.n[0], L.per[0]), gj = tile_wrap(V.j0 - V.H + ly, L.n[1], L.per[1]);
-            rs[idx] = (gi >= 0 && gj >= 0) ? tile_residual<T>(L, tab, V, lx, ly, gi, gj) : (T) 0;
+        for (int ry = warp; ry < RY; ry += TILE_WARPS) {
+            const int ly = d + ry;
+            const int gjr = V.j0 - V.H + ly;
+            const int gj = V.interior ? gjr : tile_wrap(gjr, L.n[1], L.per[1]);
+            for (int rx = lane; rx < RX; rx += 32) {
+                const int lx = d + rx;
+                const int s = ly * V.SX + lx;
+                T r;
+                if (V.interior) {
+                    r = int_res<T>(K, V, s);
+                } else {
+                    const int gi = tile_wrap(V.i0 - V.H + lx, L.n[0], L.per[0]);
+                    r = (gi >= 0 && gj >= 0) ? tile_res<T>(L, tab, V, s, gi, gj) : (T) 0;
+                }
+                rs[ry * RX + rx] = r;
+            }
         }
         __syncthreads();
         tile_store<T>(L, V, Sel<T>::r(L));
@@ -150,46 +233,46 @@ __global__ void __launch_bounds__(TILE_THREADS) mg_tile_down(const LvlDev* __res
         T* bc = Sel<T>::b(Lc);
         T* xc = Sel<T>::x(Lc);
         int Ilo[2], Ihi[2];
-        const int o[2] = {V.i0, V.j0};
+        const int o[2] = {V.i0, V.j0}, ext[2] = {V.TX, V.TY};
         for (int q = 0; q < 2; ++q) {
             if (!Lc.node) {
                 Ilo[q] = o[q] / 2;
-                Ihi[q] = min((o[q] + (q ? TILE_Y : TILE_X)) / 2, Lc.n[q]);
+                Ihi[q] = min((o[q] + ext[q]) / 2, Lc.n[q]);
             } else {
                 // fine f <-> coarse I with f = 2 (Lc.lo + I) - L.lo
-                const int a = o[q] + L.lo[q], e = o[q] + (q ? TILE_Y : TILE_X) + L.lo[q];
+                const int a = o[q] + L.lo[q], e = o[q] + ext[q] + L.lo[q];
                 Ilo[q] = max(0, (a + 1) / 2 - Lc.lo[q]);
                 Ihi[q] = min(Lc.n[q], (e + 1) / 2 - Lc.lo[q]);
             }
         }
-        const int cw = Ihi[0] - Ilo[0], ch = Ihi[1] - Ilo[1];
-        for (int idx = threadIdx.x; idx < cw * ch; idx += blockDim.x) {
-            const int I0 = Ilo[0] + idx % cw, I1 = Ilo[1] + idx / cw;
-            T acc = 0;
-            if (!Lc.node) {
-                int cnt = 0;
-                for (int dy = 0; dy < 2; ++dy)
-                    for (int dx = 0; dx < 2; ++dx) {
-                        const int fi = 2 * I0 + dx, fj = 2 * I1 + dy;
-                        if (fi < L.n[0] && fj < L.n[1]) {
-                            acc += rs[(fj - V.j0) * RX + (fi - V.i0)];
-                            cnt++;
+        for (int I1 = Ilo[1] + warp; I1 < Ihi[1]; I1 += TILE_WARPS) {
+            for (int I0 = Ilo[0] + lane; I0 < Ihi[0]; I0 += 32) {
+                T acc = 0;
+                if (!Lc.node) {
+                    int cnt = 0;
+                    for (int dy = 0; dy < 2; ++dy)
+                        for (int dx = 0; dx < 2; ++dx) {
+                            const int fi = 2 * I0 + dx, fj = 2 * I1 + dy;
+                            if (fi < L.n[0] && fj < L.n[1]) {
+                                acc += rs[(fj - V.j0) * RX + (fi - V.i0)];
+                                cnt++;
+                            }
                         }
-                    }
-                acc = acc / (T) cnt;
-            } else {
-                const int ga0 = Lc.lo[0] + I0, ga1 = Lc.lo[1] + I1;
-                for (int dy = -1; dy <= 1; ++dy)
-                    for (int dx = -1; dx <= 1; ++dx) {
-                        T w = dx == 0 ? (T) 0.5 : (T) 0.25;
-                        w *= dy == 0 ? (T) 0.5 : (T) 0.25;
-                        const int fi = 2 * ga0 + dx - L.lo[0], fj = 2 * ga1 + dy - L.lo[1];
-                        if (fi >= 0 && fi < L.n[0] && fj >= 0 && fj < L.n[1]) acc += w * rs[(fj - V.j0 + 1) * RX + (fi - V.i0 + 1)];
-                    }
+                    acc = acc / (T) cnt;
+                } else {
+                    const int ga0 = Lc.lo[0] + I0, ga1 = Lc.lo[1] + I1;
+                    for (int dy = -1; dy <= 1; ++dy)
+                        for (int dx = -1; dx <= 1; ++dx) {
+                            T w = dx == 0 ? (T) 0.5 : (T) 0.25;
+                            w *= dy == 0 ? (T) 0.5 : (T) 0.25;
+                            const int fi = 2 * ga0 + dx - L.lo[0], fj = 2 * ga1 + dy - L.lo[1];
+                            if (fi >= 0 && fi < L.n[0] && fj >= 0 && fj < L.n[1]) acc += w * rs[(fj - V.j0 + 1) * RX + (fi - V.i0 + 1)];
+                        }
+                }
+                const long long cc = (long long) I1 * Lc.n[0] + I0;
+                bc[cc] = acc;
+                xc[cc] = 0;
             }
-            const long long cc = (long long) I1 * Lc.n[0] + I0;
-            bc[cc] = acc;
-            xc[cc] = 0;
         }
         __syncthreads();
     }
@@ -197,37 +280,59 @@ __global__ void __launch_bounds__(TILE_THREADS) mg_tile_down(const LvlDev* __res
 
 // Up-leg step of a 2D level: x += P x_coarse, then `post` red-black sweeps (color 1 first).
 template <typename T>
-__global__ void __launch_bounds__(TILE_THREADS) mg_tile_up(const LvlDev* __restrict__ Ls, const Chunk* __restrict__ tiles, int ntiles, const Scal* sc,
-                                                           int post) {
+__global__ void __launch_bounds__(TILE_THREADS, 4) mg_tile_up(const LvlDev* __restrict__ Ls, const Chunk* __restrict__ tiles, int ntiles, const Scal* sc,
+                                                              int post) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sm = (T*) smem_raw;
     __shared__ T tab[NCLASS * TSTRIDE];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const Chunk C = tiles[t];
         const LvlDev& L = Ls[C.lvl];
         if (sc && !sc[L.problem].active) continue;
         TileView<T> V;
-        V.H = 2 * post;
-        V.SX = TILE_X + 2 * V.H;
-        V.SY = TILE_Y + 2 * V.H;
-        V.i0 = C.i0;
-        V.j0 = C.j;
-        V.x = sm;
-        V.b = sm + V.SX * V.SY;
-        for (int q = threadIdx.x; q < NCLASS * TSTRIDE; q += blockDim.x) tab[q] = Sel<T>::Tb(L)[q];
+        Interior<T> K;
+        tile_setup<T>(L, C, 2 * post, sm, tab, K, V);
         tile_load<T>(L, V, Sel<T>::r(L));
-        for (int idx = threadIdx.x; idx < V.SX * V.SY; idx += blockDim.x) {
-            const int lx = idx % V.SX, ly = idx / V.SX;
-            const int gi = tile_wrap(V.i0 - V.H + lx, L.n[0], L.per[0]), gj = tile_wrap(V.j0 - V.H + ly, L.n[1], L.per[1]);
-            if (gi >= 0 && gj >= 0) {
-                const T acc = prolong_acc<T>(Ls, L, gi, gj, 0);
-                V.x[idx] += acc;
+        const LvlDev& Lc = Ls[L.coarse];
+        // cell-centred interior tile whose coarse neighbours (I = f/2 and I +- 1) all exist: bilinear
+        // interpolation without ghost rules, in the generic form's operation order
+        const bool cint = V.interior && !Lc.node && ((V.i0 - V.H) >> 1) - 1 >= 0 && ((V.i0 + V.TX + V.H - 1) >> 1) + 1 < Lc.n[0] &&
+                          ((V.j0 - V.H) >> 1) - 1 >= 0 && ((V.j0 + V.TY + V.H - 1) >> 1) + 1 < Lc.n[1];
+        const T* __restrict__ xc = Sel<T>::x(Lc);
+        const int nc0 = Lc.n[0];
+        for (int ly = warp; ly < V.SY; ly += TILE_WARPS) {
+            const int gjr = V.j0 - V.H + ly;
+            if (cint) {
+                const int I1 = gjr >> 1, J1 = (gjr & 1) ? I1 + 1 : I1 - 1;
+                const T* r0 = xc + (long long) I1 * nc0;
+                const T* r1 = xc + (long long) J1 * nc0;
+                for (int lx = lane; lx < V.SX; lx += 32) {
+                    const int gi = V.i0 - V.H + lx;
+                    const int I0 = gi >> 1, J0 = (gi & 1) ? I0 + 1 : I0 - 1;
+                    T acc = 0;
+                    acc += (T) 0.75 * (T) 0.75 * (T) 1 * __ldg(r0 + I0);
+                    acc += (T) 0.25 * (T) 0.75 * (T) 1 * __ldg(r0 + J0);
+                    acc += (T) 0.75 * (T) 0.25 * (T) 1 * __ldg(r1 + I0);
+                    acc += (T) 0.25 * (T) 0.25 * (T) 1 * __ldg(r1 + J0);
+                    V.x[ly * V.SX + lx] += acc;
+                }
+                continue;
+            }
+            const int gj = tile_wrap(gjr, L.n[1], L.per[1]);
+            if (gj < 0) continue;
+            for (int lx = lane; lx < V.SX; lx += 32) {
+                const int gi = tile_wrap(V.i0 - V.H + lx, L.n[0], L.per[0]);
+                if (gi >= 0) {
+                    const T acc = prolong_acc<T>(Ls, L, gi, gj, 0);
+                    V.x[ly * V.SX + lx] += acc;
+                }
             }
         }
         __syncthreads();
         for (int it = 0; it < post; ++it) {
-            tile_sweep<T>(L, tab, V, 1, 2 * it + 1);
-            tile_sweep<T>(L, tab, V, 0, 2 * it + 2);
+            tile_sweep<T>(L, tab, K, V, 1, 2 * it + 1);
+            tile_sweep<T>(L, tab, K, V, 0, 2 * it + 2);
         }
         tile_store<T>(L, V, Sel<T>::x(L));
         __syncthreads();
@@ -236,8 +341,8 @@ __global__ void __launch_bounds__(TILE_THREADS) mg_tile_up(const LvlDev* __restr
 
 static size_t tile_smem(bool f32, int sweeps, bool down) {
     const int H = down ? 2 * sweeps + 2 : 2 * sweeps;  // down: + residual + node reach (upper bound)
-    const size_t cells = (size_t) (TILE_X + 2 * H) * (TILE_Y + 2 * H);
-    const size_t res = down ? (size_t) (TILE_X + 2) * (TILE_Y + 2) : 0;
+    const size_t cells = (size_t) (MG_TILE_X + 2 * H) * (MG_TILE_Y + 2 * H);
+    const size_t res = down ? (size_t) (MG_TILE_X + 2) * (MG_TILE_Y + 2) : 0;
     return (2 * cells + res) * (f32 ? 4 : 8);
 }
 
@@ -260,7 +365,7 @@ int mg_tiles_prepare(int sweeps) {
 template <typename K>
 static int launch_tiles(K kernel, cudaStream_t s, int sms, size_t smem, const LvlDev* L, const Chunk* tiles, int ntiles, const Scal* sc, int sweeps,
                         const char* name) {
-    const int g = std::max(1, std::min(ntiles, sms * 2));  // 512 threads x <= 64 registers: two CTAs per SM
+    const int g = std::max(1, std::min(ntiles, sms * 4));  // 256 threads x <= 64 registers: four CTAs per SM
     kernel<<<g, TILE_THREADS, smem, s>>>(L, tiles, ntiles, sc, sweeps);
     OPG_LAUNCHED();
     return check_launch(name);

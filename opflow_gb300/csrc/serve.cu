@@ -37,6 +37,7 @@ struct Req {
     MGSystem* sys = nullptr;
     opflow_field t = nullptr, rhs = nullptr;
     size_t bytes = 0;
+    size_t admitted_bytes = 0;  // the estimate charged against the budget at admission
     int steps_done = 0;
     int iters = 0;
     double rel = 0.;
@@ -95,6 +96,7 @@ static int setup_req(opflow_server S, Req* r, Scal* seed) {
     r->sys = new MGSystem();
     MGSystem* M = r->sys;
     M->ctx = ctx;
+    M->arena.ctx = ctx;
     M->precision = S->params.precision;
     M->pre = S->params.pre_sweeps;
     M->post = S->params.post_sweeps;
@@ -164,7 +166,7 @@ static void worker_loop(opflow_server S) {
                 if (S->budget && S->used + est > S->budget && !(S->active.empty() && admit.empty())) break;
                 S->pending.pop_front();
                 S->used += est;
-                r->bytes = est;
+                r->admitted_bytes = est;
                 admit.push_back(r);
             }
         }
@@ -182,7 +184,7 @@ static void worker_loop(opflow_server S) {
                 r->status = rc;
                 S->error = opflow_last_error();
                 release_req(r);
-                { std::lock_guard<std::mutex> lk(S->mu); S->used -= std::min(S->used, r->bytes); }
+                { std::lock_guard<std::mutex> lk(S->mu); S->used -= std::min(S->used, r->admitted_bytes); }
                 finish_req(S, r, rc);
                 continue;
             }
@@ -247,7 +249,7 @@ static void worker_loop(opflow_server S) {
                 continue;
             }
             finish_req(S, r, ok ? OPFLOW_OK : OPFLOW_E_NOT_CONVERGED);
-            { std::lock_guard<std::mutex> lk(S->mu); S->used -= std::min(S->used, r->bytes); }
+            { std::lock_guard<std::mutex> lk(S->mu); S->used -= std::min(S->used, r->admitted_bytes); }
             retired.push_back(r);
             S->dirty = true;
         }
@@ -279,6 +281,7 @@ int opflow_server_create(opflow_ctx ctx, const opflow_solve_params* params, size
     S->budget = budget;
     S->max_active = max_active > 0 ? max_active : 64;
     S->comp.ctx = &S->own_ctx;
+    S->comp.arena.ctx = &S->own_ctx;
     S->comp.precision = S->params.precision;
     S->comp.pre = S->params.pre_sweeps;
     S->comp.post = S->params.post_sweeps;
@@ -407,7 +410,8 @@ int opflow_server_destroy(opflow_server S) {
     S->comp.rec_stream = nullptr;
     S->comp.arena.release();
     if (S->comp.h_active) cudaFreeHost(S->comp.h_active);
-    if (S->own_ctx.scratch) cudaFree(S->own_ctx.scratch);
+    if (S->own_ctx.scratch) dev_free(&S->own_ctx, S->own_ctx.scratch);
+    cudaStreamSynchronize(S->own_ctx.stream);
     cudaStreamDestroy(S->own_ctx.stream);
     delete S;
     return OPFLOW_OK;

@@ -152,7 +152,9 @@ void* Arena::alloc(size_t bytes) {
         size_t sz = std::max(bytes, block_hint);
         block_hint = std::min(block_hint * 2, (size_t) 256 << 20);
         void* p = nullptr;
-        if (cudaMalloc(&p, sz) != cudaSuccess) return nullptr;
+        if (ctx) p = dev_alloc(ctx, sz);
+        else if (cudaMalloc(&p, sz) != cudaSuccess) p = nullptr;
+        if (!p) return nullptr;
         blocks.push_back(p);
         cap = sz;
         used = 0;
@@ -163,7 +165,10 @@ void* Arena::alloc(size_t bytes) {
     return r;
 }
 void Arena::release() {
-    for (void* p : blocks) cudaFree(p);
+    for (void* p : blocks) {
+        if (ctx) dev_free(ctx, p);
+        else cudaFree(p);
+    }
     blocks.clear();
     cap = used = total = 0;
 }
@@ -188,8 +193,12 @@ static int assemble_level(MGSystem* S, opflow_field target, const std::vector<op
     const int nk = plan.P.nk;
     double *coef = nullptr, *tmp_rhs = nullptr;
     int* dks = nullptr;
-    if (cudaMalloc(&coef, (size_t) N * nk * sizeof(double)) != cudaSuccess) return fail(OPFLOW_E_NOMEM, "assembly buffer");
-    if (!rhs && cudaMalloc(&tmp_rhs, (size_t) N * sizeof(double)) != cudaSuccess) { cudaFree(coef); return fail(OPFLOW_E_NOMEM, "assembly buffer"); }
+    coef = (double*) dev_alloc(ctx, (size_t) N * nk * sizeof(double));
+    if (!coef) return fail(OPFLOW_E_NOMEM, "assembly buffer");
+    if (!rhs) {
+        tmp_rhs = (double*) dev_alloc(ctx, (size_t) N * sizeof(double));
+        if (!tmp_rhs) { dev_free(ctx, coef); return fail(OPFLOW_E_NOMEM, "assembly buffer"); }
+    }
     int rc = asm_run(ctx, &plan, coef, rhs ? rhs : tmp_rhs);
     std::vector<int> ks(nk, -1);
     for (int k = 0; k < nk; ++k) {
@@ -205,7 +214,8 @@ static int assemble_level(MGSystem* S, opflow_field target, const std::vector<op
         if (!L.A64) rc = fail(OPFLOW_E_NOMEM, "operator arrays");
     }
     if (rc == OPFLOW_OK) {
-        cudaMalloc(&dks, nk * sizeof(int));
+        dks = (int*) dev_alloc(ctx, nk * sizeof(int));
+        if (!dks) return fail(OPFLOW_E_NOMEM, "slot map");
         cudaMemcpyAsync(dks, ks.data(), nk * sizeof(int), cudaMemcpyHostToDevice, ctx->stream);
         int* bad = (int*) ctx->scratch;
         cudaMemsetAsync(bad, 0, sizeof(int), ctx->stream);
@@ -216,9 +226,9 @@ static int assemble_level(MGSystem* S, opflow_field target, const std::vector<op
         cudaStreamSynchronize(ctx->stream);
         if (hb) rc = fail(OPFLOW_E_UNSUPPORTED, "the equation's stencil has entries beyond the (2*dim+1)-point star the multigrid handles");
     }
-    cudaFree(coef);
-    if (tmp_rhs) cudaFree(tmp_rhs);
-    if (dks) cudaFree(dks);
+    dev_free(ctx, coef);
+    if (tmp_rhs) dev_free(ctx, tmp_rhs);
+    if (dks) dev_free(ctx, dks);
     if (rc) return rc;
     const Box b = plan.P.box;
     L.ndim = target->info.ndim;
@@ -504,8 +514,12 @@ int mg_finalize(MGSystem* S) {
     S->tile_ch.assign(S->nlevels, {});
     S->coarse_sm_ch.clear();
     S->bottom_host.clear();
+    S->bottom_cells_host.clear();
+    OPG_TRY(mg_bottom_prepare());
     const char* te = getenv("OPFLOW_MG_TILES");
-    bool tiles_on = !(te && te[0] == '0') && mg_tiles_supported(S->pre) && mg_tiles_supported(S->post);
+    // tiles for the float32 V-cycle only: the float64 one is bound by float64 issue, where the halo's
+    // repeated sweeps cost more than the saved passes over memory (measured)
+    bool tiles_on = f32 && !(te && te[0] == '0') && mg_tiles_supported(S->pre) && mg_tiles_supported(S->post);
     if (tiles_on) OPG_TRY(mg_tiles_prepare(std::max(S->pre, S->post)));
     std::vector<int> coarse_list;
     std::vector<Chunk> k0;
@@ -517,6 +531,25 @@ int mg_finalize(MGSystem* S) {
                 for (int i0 = 0; i0 < L.n[0]; i0 += CH) out.push_back(Chunk{lvl_index, j, k, i0, std::min(CH, L.n[0] - i0)});
     };
     if (const char* e = getenv("OPFLOW_MG_BOTTOM")) S->bottom_max = atoll(e);
+    // level-0 chunks of the Krylov kernels: whole rows of one plane, about KCH cells each (rows longer
+    // than KCH are split), so the per-chunk reduction and its barriers are amortised over many cells
+    const int KCH = 8192;
+    auto krylov_chunks = [&](int lvl_index, const LvlDev& L, std::vector<Chunk>& out) {
+        const int ny = L.ndim > 1 ? L.n[1] : 1, nz = L.ndim > 2 ? L.n[2] : 1;
+        if (L.n[0] >= KCH) {
+            for (int k = 0; k < nz; ++k)
+                for (int j = 0; j < ny; ++j)
+                    for (int i0 = 0; i0 < L.n[0]; i0 += KCH) out.push_back(Chunk{lvl_index, j, k, i0, std::min(KCH, L.n[0] - i0)});
+            return;
+        }
+        const int per = std::max(1, KCH / L.n[0]);
+        for (int k = 0; k < nz; ++k)
+            for (int j = 0; j < ny; j += per) {
+                Chunk c{lvl_index, j, k, 0, L.n[0]};
+                c.nrows = std::min(per, ny - j);
+                out.push_back(c);
+            }
+    };
     for (size_t p = 0; p < S->probs.size(); ++p) {
         ProblemHost& P = S->probs[p];
         const int base = (int) lv.size();
@@ -524,6 +557,9 @@ int mg_finalize(MGSystem* S) {
         size_t sp = P.levels.size();
         for (size_t l = 0; l < P.levels.size(); ++l)
             if (P.levels[l].N <= S->bottom_max) { sp = l; break; }
+        long long bcells = 0;
+        for (size_t l = sp; l < P.levels.size(); ++l) bcells += P.levels[l].N;
+        if (bcells > MG_BOTTOM_CELLS || P.levels.size() - sp > (size_t) MG_BOTTOM_LEVELS) sp = P.levels.size();  // chunked instead
         // 2D red-black class-table levels above the bottom whose coarse cells all have children in the
         // level run as fused tiles
         auto tileable = [&](size_t l) {
@@ -583,12 +619,25 @@ int mg_finalize(MGSystem* S) {
             }
             lv.push_back(D);
             const int li = base + (int) l;
-            if (l == sp) S->bottom_host.push_back(li);
+            if (l == sp) {
+                S->bottom_host.push_back(li);
+                S->bottom_cells_host.push_back(bcells);
+            }
             if (l >= sp) continue;                                   // inside the bottom kernel
             const bool above_tiled = l > 0 && tileable(l - 1);      // restricted by the finer level's tiles
             if (D.tiled) {
-                for (int j0 = 0; j0 < D.n[1]; j0 += MG_TILE_Y)
-                    for (int i0 = 0; i0 < D.n[0]; i0 += MG_TILE_X) S->tile_ch[l].push_back(Chunk{li, j0, 0, i0, 0});
+                // 64 x 32 tiles, or 32 x 16 where that would leave SMs idle (tile extent: cnt x nrows)
+                int tx = MG_TILE_X, ty = MG_TILE_Y;
+                if ((long long) ((D.n[0] + tx - 1) / tx) * ((D.n[1] + ty - 1) / ty) < 2LL * ctx->num_sms) {
+                    tx /= 2;
+                    ty /= 2;
+                }
+                for (int j0 = 0; j0 < D.n[1]; j0 += ty)
+                    for (int i0 = 0; i0 < D.n[0]; i0 += tx) {
+                        Chunk c{li, j0, 0, i0, tx};
+                        c.nrows = ty;
+                        S->tile_ch[l].push_back(c);
+                    }
             } else {
                 if (!D.coarsest) rows(li, D, S->smooth_ch[l]);
                 if (!D.coarsest) rows(li, D, S->prolong_ch[l]);  // fine rows of level l (prolonged from l+1)
@@ -602,10 +651,9 @@ int mg_finalize(MGSystem* S) {
         K.b = P.b;
         K.x = (double*) S->arena.alloc(N0 * 8);
         K.r = (double*) S->arena.alloc(N0 * 8);
-        K.z = (double*) S->arena.alloc(N0 * 8);
         K.p = (double*) S->arena.alloc(N0 * 8);
         K.q = (double*) S->arena.alloc(N0 * 8);
-        if (!K.x || !K.r || !K.z || !K.p || !K.q) return fail(OPFLOW_E_NOMEM, "Krylov vectors");
+        if (!K.x || !K.r || !K.p || !K.q) return fail(OPFLOW_E_NOMEM, "Krylov vectors");
         cudaMemsetAsync(K.x, 0, N0 * 8, ctx->stream);
         K.lvl0 = base;
         K.pin = -1;
@@ -613,7 +661,7 @@ int mg_finalize(MGSystem* S) {
         P.lvl0 = base;
         first.push_back((int) k0.size());
         std::vector<Chunk> mine;
-        rows(base, lv[base], mine);
+        krylov_chunks(base, lv[base], mine);
         k0.insert(k0.end(), mine.begin(), mine.end());
         count.push_back((int) mine.size());
     }
@@ -635,6 +683,8 @@ int mg_finalize(MGSystem* S) {
     S->ncoarse = (int) coarse_list.size();
     S->coarse_host = coarse_list;
     S->nbottom = (int) S->bottom_host.size();
+    S->bottom_cells = 0;
+    for (long long c : S->bottom_cells_host) S->bottom_cells = std::max(S->bottom_cells, c);
     S->dbottom = (int*) S->arena.alloc(std::max<size_t>(1, S->bottom_host.size()) * sizeof(int));
     if (!S->dbottom) return fail(OPFLOW_E_NOMEM, "solver tables");
     if (S->nbottom) cudaMemcpyAsync(S->dbottom, S->bottom_host.data(), S->bottom_host.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->stream);
@@ -677,12 +727,12 @@ int mg_finalize(MGSystem* S) {
 // back up.
 static cudaStream_t work_stream(const MGSystem* S) { return S->recording ? S->rec_stream : S->ctx->stream; }
 
+// (The level-0 input b = r, x = 0 is written by the Krylov kernel that forms r.)
 static int vcycle(MGSystem* S) {
     cudaStream_t s = work_stream(S);
     const int sms = S->ctx->num_sms;
     const bool f32 = S->precision == OPFLOW_PREC_MIXED;
     const Scal* sc = S->dS;
-    OPG_TRY(kr_launch_to_vcycle(s, sms, f32, S->dL, S->dK, S->dk0, S->nk0, sc));
     for (int l = 0; l < S->nlevels; ++l) {
         if (l > 0) OPG_TRY(mg_launch_restrict(s, sms, f32, S->dL, S->d_restrict[l].ptr, S->d_restrict[l].n, sc));
         OPG_TRY(mg_launch_tile_down(s, sms, f32, S->dL, S->d_tiles[l].ptr, S->d_tiles[l].n, sc, S->pre));
@@ -693,7 +743,7 @@ static int vcycle(MGSystem* S) {
         }
         if (S->d_prolong[l].n) OPG_TRY(mg_launch_residual(s, sms, f32, S->dL, S->d_prolong[l].ptr, S->d_prolong[l].n, sc));
     }
-    OPG_TRY(mg_launch_bottom(s, sms, f32, S->dL, S->dbottom, S->nbottom, sc, S->pre, S->post));
+    OPG_TRY(mg_launch_bottom(s, sms, f32, S->dL, S->dbottom, S->nbottom, sc, S->pre, S->post, S->bottom_cells));
     OPG_TRY(mg_launch_coarse(s, sms, f32, S->dL, S->dcoarse, S->ncoarse, sc));
     for (int it = 0; it < S->pre + S->post; ++it) {
         OPG_TRY(mg_launch_smooth(s, sms, f32, S->dL, S->d_coarse_sm.ptr, S->d_coarse_sm.n, 0, sc));
@@ -733,10 +783,10 @@ static int iteration(MGSystem* S, bool readback) {
     const bool f32 = S->precision == OPFLOW_PREC_MIXED;
     const int np = S->nprob;
     OPG_TRY(kr_launch_apply(s, sms, S->dL, S->dK, S->dk0, S->nk0, S->dS, S->partial, 1, finish(S, 1)));  // q = A p
-    OPG_TRY(kr_launch_update(s, sms, S->dL, S->dK, S->dk0, S->nk0, S->dS, S->partial, finish(S, 2)));
+    OPG_TRY(kr_launch_update(s, sms, f32, S->dL, S->dK, S->dk0, S->nk0, S->dS, S->partial, finish(S, 2)));
     OPG_TRY(vcycle(S));
     OPG_TRY(kr_launch_from_vcycle(s, sms, f32, S->dL, S->dK, S->dk0, S->nk0, S->dS, S->partial, finish(S, 3)));
-    OPG_TRY(kr_launch_pupdate(s, sms, S->dL, S->dK, S->dk0, S->nk0, S->dS, 0));
+    OPG_TRY(kr_launch_pupdate(s, sms, f32, S->dL, S->dK, S->dk0, S->nk0, S->dS, 0));
     OPG_TRY(kr_launch_count(s, S->dS, np, S->d_active));
     if (readback) OPG_CUDA(cudaMemcpyAsync(S->h_active, S->d_active, sizeof(int), cudaMemcpyDeviceToHost, s));
     return OPFLOW_OK;
@@ -748,10 +798,10 @@ static int first_direction(MGSystem* S) {
     const int sms = S->ctx->num_sms;
     const bool f32 = S->precision == OPFLOW_PREC_MIXED;
     const int np = S->nprob;
-    OPG_TRY(kr_launch_apply(s, sms, S->dL, S->dK, S->dk0, S->nk0, nullptr, S->partial, 0, finish(S, 0)));
+    OPG_TRY(kr_launch_apply(s, sms, S->dL, S->dK, S->dk0, S->nk0, nullptr, S->partial, 0, finish(S, 0), 1, f32));
     OPG_TRY(vcycle(S));
     OPG_TRY(kr_launch_from_vcycle(s, sms, f32, S->dL, S->dK, S->dk0, S->nk0, S->dS, S->partial, finish(S, 4)));
-    OPG_TRY(kr_launch_pupdate(s, sms, S->dL, S->dK, S->dk0, S->nk0, S->dS, 1));
+    OPG_TRY(kr_launch_pupdate(s, sms, f32, S->dL, S->dK, S->dk0, S->nk0, S->dS, 1));
     return kr_launch_count(s, S->dS, np, S->d_active);
 }
 
@@ -945,6 +995,8 @@ int mg_compose(MGSystem* C, const std::vector<MGSystem*>& parts, const std::vect
     std::vector<KrylovDev> kd;
     std::vector<Chunk> k0;
     std::vector<int> first, count, coarse_list, bottom_list;
+    std::vector<long long> bottom_cells;
+    C->bottom_cells = 0;
     C->nlevels = 0;
     for (auto* P : parts) C->nlevels = std::max(C->nlevels, P->nlevels);
     C->smooth_ch.assign(C->nlevels, {});
@@ -964,6 +1016,10 @@ int mg_compose(MGSystem* C, const std::vector<MGSystem*>& parts, const std::vect
         }
         for (int c : P->coarse_host) coarse_list.push_back(base + c);
         for (int b : P->bottom_host) bottom_list.push_back(base + b);
+        for (long long c : P->bottom_cells_host) {
+            bottom_cells.push_back(c);
+            C->bottom_cells = std::max(C->bottom_cells, c);
+        }
         auto shift = [&](const std::vector<Chunk>& src, std::vector<Chunk>& dst) {
             for (Chunk c : src) { c.lvl += base; dst.push_back(c); }
         };
@@ -997,6 +1053,7 @@ int mg_compose(MGSystem* C, const std::vector<MGSystem*>& parts, const std::vect
     C->ncoarse = (int) coarse_list.size();
     C->coarse_host = coarse_list;
     C->bottom_host = bottom_list;
+    C->bottom_cells_host = bottom_cells;
     C->nbottom = (int) bottom_list.size();
     C->dbottom = (int*) C->arena.alloc(std::max<size_t>(1, bottom_list.size()) * sizeof(int));
     C->d_active = (int*) C->arena.alloc(2 * sizeof(int));
@@ -1109,6 +1166,7 @@ static int build_system(opflow_solver s) {
     if (s->S) mg_destroy(s->S);
     s->S = new MGSystem();
     s->S->ctx = s->ctx;
+    s->S->arena.ctx = s->ctx;
     s->S->precision = s->params.precision;
     s->S->pre = s->params.pre_sweeps;
     s->S->post = s->params.post_sweeps;

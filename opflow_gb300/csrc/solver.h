@@ -8,6 +8,7 @@ namespace opg {
 
 // Bump allocator over large device blocks (one solver / batch owns one).
 struct Arena {
+    opflow_ctx ctx = nullptr;  // blocks come from the context's stream-ordered pool (cudaMalloc if null)
     std::vector<void*> blocks;
     size_t cap = 0, used = 0, total = 0;
     size_t block_hint = (size_t) 256 << 20;  // size of the next block (grows x2 up to 256 MiB)
@@ -85,6 +86,8 @@ struct MGSystem {
     std::vector<int> coarse_host, bottom_host;
     int* dbottom = nullptr;
     int nbottom = 0;
+    long long bottom_cells = 0;  // largest cell total of a problem's bottom levels (shared memory of mg_bottom)
+    std::vector<long long> bottom_cells_host;  // per entry of bottom_host
     std::vector<KrylovDev> kd_host;
     int* h_active = nullptr;
     int* d_active = nullptr;  // device count of active problems (owned, so a recorded graph never dangles)
