@@ -12,9 +12,14 @@ Workloads (seeded synthetic inputs with the configurations' shapes and value dis
           next to plain FP64 (solves/s)
   serve   (default) Poisson-process arrivals of 70% one-shot Poisson solves (2D side LogU[129,2049],
           3D side LogU[64,256], Neumann / Dirichlet 50/50) and 30% backward-Euler heat sessions of
-          10-100 steps, mixed precision to 1e-10: value = device-resident batched solves/s of the
-          window's requests, e2e = the request server's host-to-host solves/s with p50/p99, next to
-          plain FP64 serving one request at a time
+          10-100 steps, mixed precision to 1e-10, at arrival rates 50, 200 and 2000 req/s: value =
+          device-resident batched solves/s of the window's one-shot requests, e2e = the request
+          server's host-to-host solves/s with p50/p99 at the highest rate, next to plain FP64 serving
+          one request at a time (the whole sweep is in config)
+  poisson3d  div(exp(g) grad p) = f on 256^3 cells, Neumann, pinned, mixed next to plain FP64
+  batched 512 corner-node Dirichlet problems (I - k Lap) u = f of sides 65..1025 in one batched
+          solve, mixed precision, next to a loop of plain FP64 single solves
+  weno    WENO5-JS + RK3 on 65536 periodic lines of 4096 cells (one RK3 step per bench step)
 
 `--impl reference` times the reference's CPU algorithm (the C restatement under oracle/, the
 reference itself does not build on the Arm machine) on the host cores for the same metric.
@@ -505,14 +510,28 @@ def run_poisson3d(args, torch, api, capi, np, ctx, stream, world, rank, local):
 
 
 def run_serve(args, torch, api, capi, np, ctx, stream, world, rank, local):
+    """Served mixed precision (continuous batching, up to 64 resident requests) next to plain FP64
+    serving one request at a time, over a sweep of Poisson arrival rates.  The headline (value, e2e)
+    is the highest rate of the sweep, where throughput is set by the servers rather than by arrivals."""
     count = args.requests
-    rate = args.rate
+    rates = [float(r) for r in str(args.rate).split(",")]
     params = api.StructSolverParams(tol=1e-10, maxIter=200, precision="mixed", zeroGuess=True)
     reqs = serve_mix(np, api, 77 + rank, count)
     total_solves = sum(s for _, _, s in reqs)
-    cells = sum(int(np.prod(p.n)) * s for p, _, s in reqs)
 
-    def served(prec, max_active, rq):
+    def pinned(n):
+        return torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+
+    # requests' right-hand sides and result buffers in pinned host memory (the copies of e2e)
+    staged = []
+    for p, f, s in reqs:
+        buf = pinned(f.size)
+        buf[:] = f
+        staged.append((p, buf, s))
+    reqs = staged
+    outs = [pinned(f.size) for _, f, _ in reqs]
+
+    def served(prec, max_active, rq, rate, out_bufs=None):
         srv = api.Server(api.StructSolverParams(tol=1e-10, maxIter=200, precision=prec), hbm_budget=120 << 30,
                          max_active=max_active, ctx=ctx)
         rng = np.random.default_rng(5)
@@ -520,11 +539,11 @@ def run_serve(args, torch, api, capi, np, ctx, stream, world, rank, local):
         ids = []
         t0 = time.perf_counter()
         tnext = t0
-        for (p, f, steps), g in zip(rq, gaps):
+        for k, ((p, f, steps), g) in enumerate(zip(rq, gaps)):
             tnext += g
             while time.perf_counter() < tnext:
                 time.sleep(min(0.0005, max(0.0, tnext - time.perf_counter())))
-            ids.append(srv.submit(p, f, steps=steps, out=np.zeros(f.size)))
+            ids.append(srv.submit(p, f, steps=steps, out=out_bufs[k] if out_bufs is not None else np.zeros(f.size)))
         res = [srv.result(i) for i in ids]
         wall = time.perf_counter() - t0
         st = srv.stats()
@@ -537,12 +556,21 @@ def run_serve(args, torch, api, capi, np, ctx, stream, world, rank, local):
                     compositions=st["compositions"],
                     worker_s={k: round(st[k], 4) for k in ("setup_s", "compose_s", "iterate_s", "retire_s")})
 
-    # warm-up (allocator, graphs, kernels)
-    served("mixed", 16, serve_mix(np, api, 3, 4))
-    l0 = capi.launch_count()
-    mixed = served("mixed", 64, reqs)
-    launches = capi.launch_count() - l0
-    plain = served("fp64", 1, reqs)
+    # warm-up (allocator pool, graphs, kernels)
+    served("mixed", 16, serve_mix(np, api, 3, 4), 1000.0)
+    served("fp64", 1, serve_mix(np, api, 3, 2), 1000.0)
+    sweep = []
+    launches = 0
+    for rate in rates:
+        l0 = capi.launch_count()
+        mixed = served("mixed", 64, reqs, rate, outs)
+        launches = capi.launch_count() - l0
+        plain = served("fp64", 1, reqs, rate, outs)
+        sweep.append(dict(rate_per_s=rate, served_mixed=mixed, served_plain_fp64_one_at_a_time=plain,
+                          served_speedup=mixed["solves_per_s"] / plain["solves_per_s"],
+                          p99_ratio_mixed_over_plain=mixed["p99_ms"] / plain["p99_ms"]))
+    head = sweep[-1]
+    mixed = head["served_mixed"]
     # device-resident batched throughput of the same one-shot problems (inputs already in HBM)
     oneshot = [(p, f) for p, f, s in reqs if s == 1]
     B = api.Batch([p for p, _ in oneshot], params, ctx)
@@ -550,24 +578,29 @@ def run_serve(args, torch, api, capi, np, ctx, stream, world, rank, local):
         B.set(i, f)
     B.solve()
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
     st = B.solve()
+    e1.record(stream)
     torch.cuda.synchronize()
-    dev_rate = len(oneshot) / (time.perf_counter() - t0)
+    dev_ms = e0.elapsed_time(e1)
+    dev_rate = len(oneshot) / (dev_ms * 1e-3)
     B.close()
     iters = sum(s.niter for s in st)
     bcells = sum(int(np.prod(p.n)) for p, _ in oneshot)
     peak, src = peak_hbm()
-    achieved = ITER_BYTES_PER_CELL * bcells * (iters / max(1, len(oneshot))) * dev_rate / max(1, len(oneshot)) / 1e9
-    return dict(value=dev_rate, unit="solves/s", ms=1e3 / dev_rate, launches=launches, dtype="f64 outer / f32 V-cycle",
-                config=dict(workload="serve", requests=count, rate_per_s=rate, mix="70% one-shot Poisson (2D LogU[129,2049] / 3D LogU[64,256], "
+    achieved = ITER_BYTES_PER_CELL * bcells * (iters / max(1, len(oneshot))) / (dev_ms * 1e-3) / 1e9
+    return dict(value=dev_rate, unit="solves/s", ms=dev_ms, launches=launches, dtype="f64 outer / f32 V-cycle",
+                config=dict(workload="serve", requests=count, rates_per_s=rates, mix="70% one-shot Poisson (2D LogU[129,2049] / 3D LogU[64,256], "
                             "Neumann/Dirichlet 50/50), 30% heat sessions 10-100 backward-Euler steps (2D LogU[129,1025])",
-                            solves_in_window=total_solves, budget_gb=120, served_mixed=mixed, served_plain_fp64_one_at_a_time=plain,
-                            served_speedup=mixed["solves_per_s"] / plain["solves_per_s"],
-                            p99_ratio_mixed_over_plain=mixed["p99_ms"] / plain["p99_ms"],
+                            solves_in_window=total_solves, budget_gb=120, sweep=sweep, headline_rate_per_s=head["rate_per_s"],
+                            served_speedup=head["served_speedup"], p99_ratio_mixed_over_plain=head["p99_ratio_mixed_over_plain"],
+                            device_resident_batch=dict(problems=len(oneshot), solves_per_s=dev_rate, ms=dev_ms),
+                            value_is="device-resident batched solves/s of the window's one-shot problems (one batched solve per step); "
+                                     "e2e = served mixed-precision solves/s at the highest swept rate, host f in and host x out",
                             l2="problems of 2-68 MB each, streamed per iteration (> L2 in aggregate)"),
                 roofline={"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": src,
-                          "traffic": traffic_for("serve"), "kernel": "batched flexible-PCG iteration (graph) over the window's one-shot problems",
+                          "traffic": traffic_for("serve"), "kernel": "batched flexible-PCG solve of the window's one-shot problems (device-resident)",
                           "algorithmic_bytes_per_launch": ITER_BYTES_PER_CELL * bcells},
                 e2e={"value": mixed["solves_per_s"], "unit": "solves/s", "h2d_bytes_per_step": 8 * sum(f.size for _, f, _ in reqs),
                      "d2h_bytes_per_step": 8 * sum(f.size for _, f, _ in reqs), "p50_ms": mixed["p50_ms"], "p99_ms": mixed["p99_ms"]})
@@ -858,7 +891,7 @@ def main():
     ap.add_argument("--problems", type=int, default=512, help="batched: problems per batch")
     ap.add_argument("--loop-sample", type=int, default=64, help="batched: problems timed in the plain FP64 one-at-a-time loop")
     ap.add_argument("--requests", type=int, default=48, help="serve: requests per measurement window")
-    ap.add_argument("--rate", type=float, default=100.0, help="serve: Poisson arrival rate (requests/s)")
+    ap.add_argument("--rate", default="50,200,2000", help="serve: Poisson arrival rates (requests/s), comma-separated; the last is the headline")
     ap.add_argument("--mode", default="fast", choices=["fast", "exact"])
     ap.add_argument("--grid", type=int, default=0, help="override the grid side (profiling a smaller case)")
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU baseline leg (profiling runs)")

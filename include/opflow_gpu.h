@@ -275,7 +275,9 @@ typedef struct {
     opflow_problem_desc problem; /* alpha*u - beta*Lap(u) = f                                          */
     int steps;                   /* 1: one solve; k > 1: a session of k solves, each taking the previous
                                     solution as its right-hand side (backward-Euler heat steps)        */
-    const double* f;             /* host right-hand side / initial state, n unknowns (copied at submit) */
+    const double* f;             /* host right-hand side / initial state, n unknowns: read when the request
+                                    is admitted, so it must stay valid and unchanged until the request's
+                                    result is available (pinned host memory gives the fastest copy)      */
     double* x_out;               /* host buffer for the final solution, n unknowns (may be NULL)        */
 } opflow_request;
 

@@ -75,7 +75,7 @@ int ensure_scratch(opflow_ctx ctx, size_t bytes) {
 }
 
 // ---- mesh ---------------------------------------------------------------------------------------------
-int mesh_create(const opflow_mesh_desc* m, MeshDev** out) {
+int mesh_create(opflow_ctx ctx, const opflow_mesh_desc* m, MeshDev** out) {
     if (!m || m->ndim < 1 || m->ndim > 3 || m->pad_width < 0) return fail(OPFLOW_E_INVALID, "bad mesh description");
     auto* md = new MeshDev();
     md->ndim = m->ndim;
@@ -88,7 +88,7 @@ int mesh_create(const opflow_mesh_desc* m, MeshDev** out) {
     }
     for (int d = 0; d < m->ndim; ++d) {
         if (m->dims[d] < 2 || !m->x[d] || !m->dx[d]) {
-            mesh_destroy(md);
+            mesh_destroy(ctx, md);
             return fail(OPFLOW_E_INVALID, "mesh dim %d needs >= 2 nodes and coordinate arrays", d);
         }
         const int n = m->dims[d] + 2 * m->pad_width;
@@ -98,22 +98,25 @@ int mesh_create(const opflow_mesh_desc* m, MeshDev** out) {
         md->hdx[d].assign(m->dx[d], m->dx[d] + n - 1);
         md->h[d] = md->hdx[d][0];
         for (int i = 0; i < n - 1; ++i) md->uniform[d] = md->uniform[d] && md->hdx[d][i] == md->h[d];
-        if (cudaMalloc(&md->x[d], n * sizeof(double)) != cudaSuccess ||
-            cudaMalloc(&md->dx[d], n * sizeof(double)) != cudaSuccess) {
-            mesh_destroy(md);
+        md->x[d] = (double*) dev_alloc(ctx, n * sizeof(double));
+        md->dx[d] = (double*) dev_alloc(ctx, n * sizeof(double));
+        if (!md->x[d] || !md->dx[d]) {
+            cudaStreamSynchronize(ctx->stream);  // copies of earlier dims still read md's host arrays
+            mesh_destroy(ctx, md);
             return fail(OPFLOW_E_NOMEM, "mesh allocation failed");
         }
-        cudaMemcpy(md->x[d], m->x[d], n * sizeof(double), cudaMemcpyHostToDevice);
-        cudaMemcpy(md->dx[d], m->dx[d], (n - 1) * sizeof(double), cudaMemcpyHostToDevice);
+        // the host arrays live in md: the copies may complete after this call returns
+        cudaMemcpyAsync(md->x[d], md->hx[d].data(), n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
+        cudaMemcpyAsync(md->dx[d], md->hdx[d].data(), (n - 1) * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
     }
     *out = md;
     return OPFLOW_OK;
 }
-void mesh_destroy(MeshDev* m) {
+void mesh_destroy(opflow_ctx ctx, MeshDev* m) {
     if (!m) return;
     for (int d = 0; d < 3; ++d) {
-        if (m->x[d]) cudaFree(m->x[d]);
-        if (m->dx[d]) cudaFree(m->dx[d]);
+        if (m->x[d]) dev_free(ctx, m->x[d]);
+        if (m->dx[d]) dev_free(ctx, m->dx[d]);
     }
     delete m;
 }
@@ -508,7 +511,7 @@ int opflow_field_create(opflow_ctx ctx, const opflow_mesh_desc* mesh, const opfl
     OPG_TRY(compute_info(mesh, desc, &info));
     OPG_CUDA(cudaSetDevice(ctx->device));
     MeshDev* md = nullptr;
-    OPG_TRY(mesh_create(mesh, &md));
+    OPG_TRY(mesh_create(ctx, mesh, &md));
     auto* f = new opflow_field_s();
     f->ctx = ctx;
     f->desc = *desc;
@@ -516,7 +519,7 @@ int opflow_field_create(opflow_ctx ctx, const opflow_mesh_desc* mesh, const opfl
     f->mesh = md;
     f->buf[0] = (double*) dev_alloc(ctx, info.count * sizeof(double));
     if (!f->buf[0]) {
-        mesh_destroy(md);
+        mesh_destroy(ctx, md);
         delete f;
         return fail(OPFLOW_E_NOMEM, "cannot allocate %zu doubles", info.count);
     }
@@ -537,7 +540,7 @@ int opflow_field_destroy(opflow_field f) {
     // freed in the order of the context's stream, after the work already enqueued on it
     for (int k = 0; k < 2; ++k)
         if (f->buf[k]) dev_free(f->ctx, f->buf[k]);
-    mesh_destroy(f->mesh);
+    mesh_destroy(f->ctx, f->mesh);
     delete f;
     return OPFLOW_OK;
 }

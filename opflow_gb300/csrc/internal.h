@@ -114,8 +114,8 @@ struct opflow_field_s {
 };
 
 namespace opg {
-int mesh_create(const opflow_mesh_desc* m, MeshDev** out);
-void mesh_destroy(MeshDev* m);
+int mesh_create(opflow_ctx ctx, const opflow_mesh_desc* m, MeshDev** out);
+void mesh_destroy(opflow_ctx ctx, MeshDev* m);
 bool mesh_equal(const MeshDev* a, const MeshDev* b);
 int ensure_back(opflow_field f);
 int update_padding_buf(opflow_field f, double* data);

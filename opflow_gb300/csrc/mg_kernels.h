@@ -9,7 +9,9 @@ int mg_launch_restrict(cudaStream_t s, int sms, bool f32, const LvlDev* L, const
 int mg_launch_prolong(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* ch, int nch, const Scal* sc);
 // fused 2D tile steps of a level (mg_tiles.cu): down = pre-smoothing + residual + restriction,
 // up = prolongation + post-smoothing; tiles are Chunk{lvl, j = tile y origin, k = 0, i0 = tile x origin}
-constexpr int MG_TILE_X = 64, MG_TILE_Y = 32;
+// 54 columns: with the down step's 5-cell halo a region row is 64 positions, one colour of it one
+// warp-wide pass; small levels use MG_TILE_X_SMALL x MG_TILE_Y / 2 (32-position rows)
+constexpr int MG_TILE_X = 54, MG_TILE_Y = 32, MG_TILE_X_SMALL = 22;
 bool mg_tiles_supported(int sweeps);
 int mg_tiles_prepare(int sweeps);
 int mg_launch_tile_down(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* tiles, int ntiles, const Scal* sc, int pre);

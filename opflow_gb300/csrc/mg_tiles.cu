@@ -18,7 +18,8 @@
 // Work layout: warps take rows of the tile region, lanes take columns (a colour's cells with a stride
 // of two), so no thread divides an index.  Tiles whose region lies inside the level away from its
 // boundary take the interior form: constant coefficients, no wrap-around or existence tests.  The tile
-// extent is chosen per level (Chunk.cnt x Chunk.nrows) so that small levels still spread over the SMs.
+// extent is chosen per level (Chunk.cnt x Chunk.nrows, even widths) so that small levels still spread
+// over the SMs.
 #include "mg_device.h"
 
 namespace opg {
@@ -34,6 +35,9 @@ __device__ __forceinline__ int tile_wrap(int g, int n, int per) {
     return g < 0 ? g + n : g;
 }
 
+// The tile's geometry in registers.  (Kernels read level data through `const LvlDev&` into global
+// memory; inside loops that store through generic pointers the compiler must reload such fields after
+// every store, so the loops below only use these copies.)
 template <typename T>
 struct TileView {
     T* x;        // [SY][SX] smem
@@ -41,33 +45,35 @@ struct TileView {
     int SX, SY, H;
     int TX, TY;  // tile extent (without halo)
     int i0, j0;  // global origin of the tile (without halo)
+    int n0, n1;  // level extent
+    int per0, per1;
     bool interior;
 };
 
 // One red-black update of smem position s mirroring global (gi, gj), general form.
 template <typename T>
 __device__ __forceinline__ void tile_gs(const LvlDev& L, const T* __restrict__ tab, const TileView<T>& V, int s, int gi, int gj) {
-    const int n0 = L.n[0], n1 = L.n[1];
+    const int n0 = V.n0, n1 = V.n1;
     const int cls = pos_class(gi, n0) + 3 * pos_class(gj, n1);
     const T* cf = tab + cls * TSTRIDE;
     T acc = 0;
-    if (L.per[0] || gi - 1 >= 0) acc += cf[1] * V.x[s - 1];
-    if (L.per[0] || gi + 1 < n0) acc += cf[2] * V.x[s + 1];
-    if (L.per[1] || gj - 1 >= 0) acc += cf[3] * V.x[s - V.SX];
-    if (L.per[1] || gj + 1 < n1) acc += cf[4] * V.x[s + V.SX];
+    if (V.per0 || gi - 1 >= 0) acc += cf[1] * V.x[s - 1];
+    if (V.per0 || gi + 1 < n0) acc += cf[2] * V.x[s + 1];
+    if (V.per1 || gj - 1 >= 0) acc += cf[3] * V.x[s - V.SX];
+    if (V.per1 || gj + 1 < n1) acc += cf[4] * V.x[s + V.SX];
     V.x[s] = (V.b[s] - acc) * cf[NSLOT];
 }
 
 template <typename T>
 __device__ __forceinline__ T tile_res(const LvlDev& L, const T* __restrict__ tab, const TileView<T>& V, int s, int gi, int gj) {
-    const int n0 = L.n[0], n1 = L.n[1];
+    const int n0 = V.n0, n1 = V.n1;
     const int cls = pos_class(gi, n0) + 3 * pos_class(gj, n1);
     const T* cf = tab + cls * TSTRIDE;
     T acc = 0;
-    if (L.per[0] || gi - 1 >= 0) acc += cf[1] * V.x[s - 1];
-    if (L.per[0] || gi + 1 < n0) acc += cf[2] * V.x[s + 1];
-    if (L.per[1] || gj - 1 >= 0) acc += cf[3] * V.x[s - V.SX];
-    if (L.per[1] || gj + 1 < n1) acc += cf[4] * V.x[s + V.SX];
+    if (V.per0 || gi - 1 >= 0) acc += cf[1] * V.x[s - 1];
+    if (V.per0 || gi + 1 < n0) acc += cf[2] * V.x[s + 1];
+    if (V.per1 || gj - 1 >= 0) acc += cf[3] * V.x[s - V.SX];
+    if (V.per1 || gj + 1 < n1) acc += cf[4] * V.x[s + V.SX];
     return V.b[s] - (cf[0] * V.x[s] + acc);
 }
 
@@ -101,18 +107,17 @@ __device__ __forceinline__ T int_res(const Interior<T>& K, const TileView<T>& V,
 // Loads x (from `x`) and b of the tile + halo (positions outside a non-periodic level hold 0 and are
 // never used).
 template <typename T>
-__device__ __forceinline__ void tile_load(const LvlDev& L, const TileView<T>& V, const T* __restrict__ x) {
-    const T* b = Sel<T>::b(L);
+__device__ __forceinline__ void tile_load(const TileView<T>& V, const T* __restrict__ x, const T* __restrict__ b) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int ly = warp; ly < V.SY; ly += TILE_WARPS) {
         const int gjr = V.j0 - V.H + ly;
-        const int gj = V.interior ? gjr : tile_wrap(gjr, L.n[1], L.per[1]);
+        const int gj = V.interior ? gjr : tile_wrap(gjr, V.n1, V.per1);
         for (int lx = lane; lx < V.SX; lx += 32) {
             const int gir = V.i0 - V.H + lx;
-            const int gi = V.interior ? gir : tile_wrap(gir, L.n[0], L.per[0]);
+            const int gi = V.interior ? gir : tile_wrap(gir, V.n0, V.per0);
             const int s = ly * V.SX + lx;
             if (gi >= 0 && gj >= 0) {
-                const long long c = (long long) gj * L.n[0] + gi;
+                const long long c = (long long) gj * V.n0 + gi;
                 V.x[s] = x[c];
                 V.b[s] = b[c];
             } else {
@@ -136,10 +141,10 @@ __device__ __forceinline__ void tile_sweep(const LvlDev& L, const T* __restrict_
         if (V.interior) {
             for (int lx = lx0 + 2 * lane; lx < V.SX - d; lx += 64) int_gs<T>(K, V, ly * V.SX + lx);
         } else {
-            const int gj = tile_wrap(gjr, L.n[1], L.per[1]);
+            const int gj = tile_wrap(gjr, V.n1, V.per1);
             if (gj < 0) continue;
             for (int lx = lx0 + 2 * lane; lx < V.SX - d; lx += 64) {
-                const int gi = tile_wrap(V.i0 - V.H + lx, L.n[0], L.per[0]);
+                const int gi = tile_wrap(V.i0 - V.H + lx, V.n0, V.per0);
                 if (gi >= 0) tile_gs<T>(L, tab, V, ly * V.SX + lx, gi, gj);
             }
         }
@@ -148,14 +153,14 @@ __device__ __forceinline__ void tile_sweep(const LvlDev& L, const T* __restrict_
 }
 
 template <typename T>
-__device__ __forceinline__ void tile_store(const LvlDev& L, const TileView<T>& V, T* __restrict__ x) {
+__device__ __forceinline__ void tile_store(const TileView<T>& V, T* __restrict__ x) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int ty = warp; ty < V.TY; ty += TILE_WARPS) {
         const int gj = V.j0 + ty;
-        if (gj >= L.n[1]) break;
+        if (gj >= V.n1) break;
         for (int tx = lane; tx < V.TX; tx += 32) {
             const int gi = V.i0 + tx;
-            if (gi < L.n[0]) x[(long long) gj * L.n[0] + gi] = V.x[(ty + V.H) * V.SX + tx + V.H];
+            if (gi < V.n0) x[(long long) gj * V.n0 + gi] = V.x[(ty + V.H) * V.SX + tx + V.H];
         }
     }
 }
@@ -171,8 +176,12 @@ __device__ __forceinline__ void tile_setup(const LvlDev& L, const Chunk& C, int 
     V.j0 = C.j;
     V.x = sm;
     V.b = sm + V.SX * V.SY;
+    V.n0 = L.n[0];
+    V.n1 = L.n[1];
+    V.per0 = L.per[0];
+    V.per1 = L.per[1];
     // inside the level with a cell to spare on each side: every position is an interior-class cell
-    V.interior = V.i0 - H >= 1 && V.i0 + V.TX + H <= L.n[0] - 1 && V.j0 - H >= 1 && V.j0 + V.TY + H <= L.n[1] - 1;
+    V.interior = V.i0 - H >= 1 && V.i0 + V.TX + H <= V.n0 - 1 && V.j0 - H >= 1 && V.j0 + V.TY + H <= V.n1 - 1;
     for (int q = threadIdx.x; q < NCLASS * TSTRIDE; q += blockDim.x) tab[q] = Sel<T>::Tb(L)[q];
     const T* ti = Sel<T>::Tb(L) + 4 * TSTRIDE;
     K.c0 = ti[0];
@@ -203,7 +212,7 @@ __global__ void __launch_bounds__(TILE_THREADS, 4) mg_tile_down(const LvlDev* __
         tile_setup<T>(L, C, 2 * pre + 1 + reach, sm, tab, K, V);
         T* rs = V.b + V.SX * V.SY;  // residual over the tile + reach: RX x RY
         const int RX = V.TX + 2 * reach, RY = V.TY + 2 * reach;
-        tile_load<T>(L, V, Sel<T>::x(L));
+        tile_load<T>(V, Sel<T>::x(L), Sel<T>::b(L));
         for (int it = 0; it < pre; ++it) {
             tile_sweep<T>(L, tab, K, V, 0, 2 * it + 1);
             tile_sweep<T>(L, tab, K, V, 1, 2 * it + 2);
@@ -213,7 +222,7 @@ __global__ void __launch_bounds__(TILE_THREADS, 4) mg_tile_down(const LvlDev* __
         for (int ry = warp; ry < RY; ry += TILE_WARPS) {
             const int ly = d + ry;
             const int gjr = V.j0 - V.H + ly;
-            const int gj = V.interior ? gjr : tile_wrap(gjr, L.n[1], L.per[1]);
+            const int gj = V.interior ? gjr : tile_wrap(gjr, V.n1, V.per1);
             for (int rx = lane; rx < RX; rx += 32) {
                 const int lx = d + rx;
                 const int s = ly * V.SX + lx;
@@ -221,55 +230,59 @@ __global__ void __launch_bounds__(TILE_THREADS, 4) mg_tile_down(const LvlDev* __
                 if (V.interior) {
                     r = int_res<T>(K, V, s);
                 } else {
-                    const int gi = tile_wrap(V.i0 - V.H + lx, L.n[0], L.per[0]);
+                    const int gi = tile_wrap(V.i0 - V.H + lx, V.n0, V.per0);
                     r = (gi >= 0 && gj >= 0) ? tile_res<T>(L, tab, V, s, gi, gj) : (T) 0;
                 }
                 rs[ry * RX + rx] = r;
             }
         }
         __syncthreads();
-        tile_store<T>(L, V, Sel<T>::r(L));
+        tile_store<T>(V, Sel<T>::r(L));
         // restriction: the coarse cells whose children / centre node lie in this tile
-        T* bc = Sel<T>::b(Lc);
-        T* xc = Sel<T>::x(Lc);
+        T* __restrict__ bc = Sel<T>::b(Lc);
+        T* __restrict__ xc = Sel<T>::x(Lc);
+        const int cnode = Lc.node, cn0 = Lc.n[0], cn1 = Lc.n[1], clo0 = Lc.lo[0], clo1 = Lc.lo[1], flo0 = L.lo[0], flo1 = L.lo[1];
         int Ilo[2], Ihi[2];
         const int o[2] = {V.i0, V.j0}, ext[2] = {V.TX, V.TY};
-        for (int q = 0; q < 2; ++q) {
-            if (!Lc.node) {
-                Ilo[q] = o[q] / 2;
-                Ihi[q] = min((o[q] + ext[q]) / 2, Lc.n[q]);
-            } else {
-                // fine f <-> coarse I with f = 2 (Lc.lo + I) - L.lo
-                const int a = o[q] + L.lo[q], e = o[q] + ext[q] + L.lo[q];
-                Ilo[q] = max(0, (a + 1) / 2 - Lc.lo[q]);
-                Ihi[q] = min(Lc.n[q], (e + 1) / 2 - Lc.lo[q]);
+        {
+            const int cn[2] = {cn0, cn1}, clo[2] = {clo0, clo1}, flo[2] = {flo0, flo1};
+            for (int q = 0; q < 2; ++q) {
+                if (!cnode) {
+                    Ilo[q] = o[q] / 2;
+                    Ihi[q] = min((o[q] + ext[q]) / 2, cn[q]);
+                } else {
+                    // fine f <-> coarse I with f = 2 (Lc.lo + I) - L.lo
+                    const int a = o[q] + flo[q], e = o[q] + ext[q] + flo[q];
+                    Ilo[q] = max(0, (a + 1) / 2 - clo[q]);
+                    Ihi[q] = min(cn[q], (e + 1) / 2 - clo[q]);
+                }
             }
         }
         for (int I1 = Ilo[1] + warp; I1 < Ihi[1]; I1 += TILE_WARPS) {
             for (int I0 = Ilo[0] + lane; I0 < Ihi[0]; I0 += 32) {
                 T acc = 0;
-                if (!Lc.node) {
+                if (!cnode) {
                     int cnt = 0;
                     for (int dy = 0; dy < 2; ++dy)
                         for (int dx = 0; dx < 2; ++dx) {
                             const int fi = 2 * I0 + dx, fj = 2 * I1 + dy;
-                            if (fi < L.n[0] && fj < L.n[1]) {
+                            if (fi < V.n0 && fj < V.n1) {
                                 acc += rs[(fj - V.j0) * RX + (fi - V.i0)];
                                 cnt++;
                             }
                         }
                     acc = acc / (T) cnt;
                 } else {
-                    const int ga0 = Lc.lo[0] + I0, ga1 = Lc.lo[1] + I1;
+                    const int ga0 = clo0 + I0, ga1 = clo1 + I1;
                     for (int dy = -1; dy <= 1; ++dy)
                         for (int dx = -1; dx <= 1; ++dx) {
                             T w = dx == 0 ? (T) 0.5 : (T) 0.25;
                             w *= dy == 0 ? (T) 0.5 : (T) 0.25;
-                            const int fi = 2 * ga0 + dx - L.lo[0], fj = 2 * ga1 + dy - L.lo[1];
-                            if (fi >= 0 && fi < L.n[0] && fj >= 0 && fj < L.n[1]) acc += w * rs[(fj - V.j0 + 1) * RX + (fi - V.i0 + 1)];
+                            const int fi = 2 * ga0 + dx - flo0, fj = 2 * ga1 + dy - flo1;
+                            if (fi >= 0 && fi < V.n0 && fj >= 0 && fj < V.n1) acc += w * rs[(fj - V.j0 + 1) * RX + (fi - V.i0 + 1)];
                         }
                 }
-                const long long cc = (long long) I1 * Lc.n[0] + I0;
+                const long long cc = (long long) I1 * cn0 + I0;
                 bc[cc] = acc;
                 xc[cc] = 0;
             }
@@ -293,7 +306,7 @@ __global__ void __launch_bounds__(TILE_THREADS, 4) mg_tile_up(const LvlDev* __re
         TileView<T> V;
         Interior<T> K;
         tile_setup<T>(L, C, 2 * post, sm, tab, K, V);
-        tile_load<T>(L, V, Sel<T>::r(L));
+        tile_load<T>(V, Sel<T>::r(L), Sel<T>::b(L));
         const LvlDev& Lc = Ls[L.coarse];
         // cell-centred interior tile whose coarse neighbours (I = f/2 and I +- 1) all exist: bilinear
         // interpolation without ghost rules, in the generic form's operation order
@@ -319,10 +332,10 @@ __global__ void __launch_bounds__(TILE_THREADS, 4) mg_tile_up(const LvlDev* __re
                 }
                 continue;
             }
-            const int gj = tile_wrap(gjr, L.n[1], L.per[1]);
+            const int gj = tile_wrap(gjr, V.n1, V.per1);
             if (gj < 0) continue;
             for (int lx = lane; lx < V.SX; lx += 32) {
-                const int gi = tile_wrap(V.i0 - V.H + lx, L.n[0], L.per[0]);
+                const int gi = tile_wrap(V.i0 - V.H + lx, V.n0, V.per0);
                 if (gi >= 0) {
                     const T acc = prolong_acc<T>(Ls, L, gi, gj, 0);
                     V.x[ly * V.SX + lx] += acc;
@@ -334,7 +347,7 @@ __global__ void __launch_bounds__(TILE_THREADS, 4) mg_tile_up(const LvlDev* __re
             tile_sweep<T>(L, tab, K, V, 1, 2 * it + 1);
             tile_sweep<T>(L, tab, K, V, 0, 2 * it + 2);
         }
-        tile_store<T>(L, V, Sel<T>::x(L));
+        tile_store<T>(V, Sel<T>::x(L));
         __syncthreads();
     }
 }

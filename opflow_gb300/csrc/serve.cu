@@ -31,7 +31,8 @@ struct Req {
     long long id = 0;
     opflow_problem_desc pd{};
     int steps = 1;
-    std::vector<double> f;
+    const double* f = nullptr;  // the caller's right-hand side, read at admission
+    long long nf = 0;
     double* x_out = nullptr;
     Clock::time_point t_submit, t_admit, t_done;
     MGSystem* sys = nullptr;
@@ -71,6 +72,7 @@ struct opflow_server_s {
     bool stop = false;
     long long next_id = 1;
     MGSystem comp;
+    double* d_slots = nullptr;  // one float64 per request finishing at a boundary (pinned-shift values)
     bool dirty = true;
     std::vector<Scal> state;  // per active request, host copy
     // stats
@@ -109,8 +111,8 @@ static int setup_req(opflow_server S, Req* r, Scal* seed) {
     OPG_TRY(mg_add_problem(M, r->t, tree.data(), (int) tree.size(), leaves, 2, 0));
     OPG_TRY(mg_finalize(M));
     r->N = M->probs[0].levels[0].N;
-    if ((long long) r->f.size() != r->N) return fail(OPFLOW_E_INVALID, "request %lld: f has %zu values, the problem %lld unknowns", r->id, r->f.size(), r->N);
-    OPG_CUDA(cudaMemcpyAsync(M->probs[0].b, r->f.data(), r->N * 8, cudaMemcpyHostToDevice, ctx->stream));
+    if (r->nf != r->N) return fail(OPFLOW_E_INVALID, "request %lld: f has %lld values, the problem %lld unknowns", r->id, r->nf, r->N);
+    OPG_CUDA(cudaMemcpyAsync(M->probs[0].b, r->f, r->N * 8, cudaMemcpyHostToDevice, ctx->stream));
     ProblemHost& P = M->probs[0];
     r->pinned = P.singular && !P.has_dirichlet;
     if (r->pinned) {
@@ -128,16 +130,41 @@ static int setup_req(opflow_server S, Req* r, Scal* seed) {
     return OPFLOW_OK;
 }
 
+// x -= x[0], with x[0] first copied to `slot` (so no thread reads it while another rewrites it)
+__global__ void shift_by_first(double* x, long long n, const double* slot) {
+    const double a = -*slot;
+    for (long long t = blockIdx.x * (long long) blockDim.x + threadIdx.x; t < n; t += (long long) gridDim.x * blockDim.x) x[t] += a;
+}
+
+// Enqueues a finished request's result: the pinned shift and the copy to the caller's buffer
+// (completion: after the worker's next stream synchronisation).
+static void finish_enqueue(opflow_server S, Req* r, double* slot) {
+    opflow_ctx ctx = &S->own_ctx;
+    const KrylovDev& K = r->sys->kd_host[0];
+    if (r->pinned) {
+        cudaMemcpyAsync(slot, K.x, 8, cudaMemcpyDeviceToDevice, ctx->stream);
+        const long long blocks = std::min<long long>((r->N + 255) / 256, (long long) ctx->num_sms * 16);
+        shift_by_first<<<(int) std::max(1LL, blocks), 256, 0, ctx->stream>>>(K.x, r->N, slot);
+        OPG_LAUNCHED();
+    }
+    if (r->x_out) cudaMemcpyAsync(r->x_out, K.x, r->N * 8, cudaMemcpyDeviceToHost, ctx->stream);
+}
+
+static void finish_mark(opflow_server S, Req* r, int status) {
+    r->status = status;
+    r->t_done = Clock::now();
+    std::lock_guard<std::mutex> lk(S->mu);
+    r->done = true;
+    S->completed++;
+    S->lat.push_back(std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count());
+    S->t_last = r->t_done;
+    S->cv_done.notify_all();
+}
+
 static void finish_req(opflow_server S, Req* r, int status) {
     opflow_ctx ctx = &S->own_ctx;
     if (status == OPFLOW_OK && r->sys) {
-        const KrylovDev& K = r->sys->kd_host[0];
-        if (r->pinned) {
-            double x0 = 0.;
-            cudaMemcpy(&x0, K.x, 8, cudaMemcpyDeviceToHost);
-            mg_add_scalar(ctx, K.x, r->N, -x0);
-        }
-        if (r->x_out) cudaMemcpyAsync(r->x_out, K.x, r->N * 8, cudaMemcpyDeviceToHost, ctx->stream);
+        finish_enqueue(S, r, S->d_slots + S->max_active);
         cudaStreamSynchronize(ctx->stream);
     }
     r->status = status;
@@ -226,8 +253,13 @@ static void worker_loop(opflow_server S) {
         cudaStreamSynchronize(S->own_ctx.stream);
         add_since(S->iterate_s, t_iter);
         const Clock::time_point t_retire = Clock::now();
+        // Every restart and every result of this boundary is enqueued first; one synchronisation
+        // then covers them all.
         std::vector<Req*> keep;
         std::vector<Scal> keep_state;
+        std::vector<std::pair<size_t, size_t>> restarted;  // (index in keep, index in the composite)
+        std::vector<std::pair<Req*, int>> finished;
+        double* slots = S->d_slots;
         for (size_t i = 0; i < S->active.size(); ++i) {
             Req* r = S->active[i];
             Scal& st = S->state[i];
@@ -242,16 +274,23 @@ static void worker_loop(opflow_server S) {
                 const KrylovDev& K = r->sys->kd_host[0];
                 cudaMemcpyAsync(r->sys->probs[0].b, K.x, r->N * 8, cudaMemcpyDeviceToDevice, S->own_ctx.stream);
                 mg_prepare_problem(r->sys, S->params.tol, S->comp.dS + i);
-                cudaMemcpyAsync(&st, S->comp.dS + i, sizeof(Scal), cudaMemcpyDeviceToHost, S->own_ctx.stream);
-                cudaStreamSynchronize(S->own_ctx.stream);
+                restarted.emplace_back(keep.size(), i);
                 keep.push_back(r);
                 keep_state.push_back(st);
                 continue;
             }
-            finish_req(S, r, ok ? OPFLOW_OK : OPFLOW_E_NOT_CONVERGED);
-            { std::lock_guard<std::mutex> lk(S->mu); S->used -= std::min(S->used, r->admitted_bytes); }
-            retired.push_back(r);
+            if (ok) finish_enqueue(S, r, slots + finished.size());
+            finished.emplace_back(r, ok ? OPFLOW_OK : OPFLOW_E_NOT_CONVERGED);
             S->dirty = true;
+        }
+        if (!restarted.empty())
+            cudaMemcpyAsync(S->state.data(), S->comp.dS, S->state.size() * sizeof(Scal), cudaMemcpyDeviceToHost, S->own_ctx.stream);
+        if (!restarted.empty() || !finished.empty()) cudaStreamSynchronize(S->own_ctx.stream);
+        for (auto& q : restarted) keep_state[q.first] = S->state[q.second];
+        for (auto& f : finished) {
+            finish_mark(S, f.first, f.second);
+            { std::lock_guard<std::mutex> lk(S->mu); S->used -= std::min(S->used, f.first->admitted_bytes); }
+            retired.push_back(f.first);
         }
         S->active.swap(keep);
         S->state.swap(keep_state);
@@ -288,7 +327,8 @@ int opflow_server_create(opflow_ctx ctx, const opflow_solve_params* params, size
     S->comp.tol = S->params.tol;
     S->comp.max_iter = S->params.max_iter;
     S->comp.arena.block_hint = 1u << 20;
-    if (ensure_scratch(&S->own_ctx, 4096) != OPFLOW_OK) {
+    if (ensure_scratch(&S->own_ctx, 4096) != OPFLOW_OK ||
+        !(S->d_slots = (double*) dev_alloc(&S->own_ctx, (size_t) (S->max_active + 1) * sizeof(double)))) {
         cudaStreamDestroy(S->own_ctx.stream);
         delete S;
         return OPFLOW_E_NOMEM;
@@ -314,7 +354,8 @@ int opflow_server_submit(opflow_server S, const opflow_request* q, long long* id
     auto* r = new Req();
     r->pd = pd;
     r->steps = q->steps;
-    r->f.assign(q->f, q->f + n);
+    r->f = q->f;
+    r->nf = n;
     r->x_out = q->x_out;
     r->t_submit = Clock::now();
     {
@@ -411,6 +452,7 @@ int opflow_server_destroy(opflow_server S) {
     S->comp.arena.release();
     if (S->comp.h_active) cudaFreeHost(S->comp.h_active);
     if (S->own_ctx.scratch) dev_free(&S->own_ctx, S->own_ctx.scratch);
+    if (S->d_slots) dev_free(&S->own_ctx, S->d_slots);
     cudaStreamSynchronize(S->own_ctx.stream);
     cudaStreamDestroy(S->own_ctx.stream);
     delete S;

@@ -626,11 +626,11 @@ int mg_finalize(MGSystem* S) {
             if (l >= sp) continue;                                   // inside the bottom kernel
             const bool above_tiled = l > 0 && tileable(l - 1);      // restricted by the finer level's tiles
             if (D.tiled) {
-                // 64 x 32 tiles, or 32 x 16 where that would leave SMs idle (tile extent: cnt x nrows)
+                // 54 x 32 tiles, or 22 x 16 where that would leave SMs idle (tile extent: cnt x nrows)
                 int tx = MG_TILE_X, ty = MG_TILE_Y;
                 if ((long long) ((D.n[0] + tx - 1) / tx) * ((D.n[1] + ty - 1) / ty) < 2LL * ctx->num_sms) {
-                    tx /= 2;
-                    ty /= 2;
+                    tx = MG_TILE_X_SMALL;
+                    ty = MG_TILE_Y / 2;
                 }
                 for (int j0 = 0; j0 < D.n[1]; j0 += ty)
                     for (int i0 = 0; i0 < D.n[0]; i0 += tx) {
@@ -1111,7 +1111,9 @@ int mg_states(MGSystem* S, std::vector<Scal>& out) {
 
 void mg_destroy(MGSystem* S) {
     if (!S) return;
-    cudaStreamSynchronize(S->ctx->stream);
+    // memory goes back to the stream-ordered pool after the work already enqueued; only recorded
+    // graphs need the stream idle before they are destroyed
+    if (S->exec || S->solve_exec) cudaStreamSynchronize(S->ctx->stream);
     if (S->exec) cudaGraphExecDestroy(S->exec);
     S->exec = nullptr;
     if (S->solve_exec) cudaGraphExecDestroy(S->solve_exec);

@@ -21,9 +21,21 @@ __device__ __forceinline__ double ld3(const FieldView& f, int i, int j, int k) {
     return f.data[(long long) (i - f.off[0]) + (long long) (j - f.off[1]) * f.sy + (long long) (k - f.off[2]) * f.sz];
 }
 
-// correctly rounded x / h: exact multiply for a power-of-two h, else Markstein's three operations
+// x * y for y a power of two, exactly: when x and the product are normal numbers the product is x
+// with its exponent field moved, an integer add (no float64 instruction); zeros are returned as they
+// are; everything else (subnormal operand or product, infinities, NaN) takes the float64 multiply.
+__device__ __forceinline__ double mul_pow2(double x, double y) {
+    const int k = (int) ((__double_as_longlong(y) >> 52) & 0x7FF) - 1023;
+    const long long b = __double_as_longlong(x);
+    const int e = (int) ((b >> 52) & 0x7FF);
+    if (e > 0 && e < 2047 && e + k > 0 && e + k < 2047) return __longlong_as_double(b + ((long long) k << 52));
+    if ((b & 0x7FFFFFFFFFFFFFFFll) == 0) return x;
+    return __dmul_rn(x, y);
+}
+
+// correctly rounded x / h: an exact multiply for a power-of-two h, else Markstein's three operations
 __device__ __forceinline__ double tdiv(double x, double h, double y, int p2) {
-    if (p2) return __dmul_rn(x, y);
+    if (p2) return mul_pow2(x, y);
     const double q = __dmul_rn(x, y);
     const double r = __fma_rn(-q, h, x);
     return __fma_rn(r, y, q);
