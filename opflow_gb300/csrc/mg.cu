@@ -272,9 +272,9 @@ __device__ __forceinline__ void chunk_finish(const Finish& F, int p, const doubl
 
 // mode 0: r = b - A x, partial (b.b, r.r)        mode 1: q = A p, partial (p.q)
 // With to_vc (mode 0) the V-cycle's level-0 input is written as well: b = (T) r, x = 0.
-template <typename T>
-__global__ void __launch_bounds__(256) kr_apply(const LvlDev* __restrict__ Ls, const KrylovDev* __restrict__ K, const Chunk* __restrict__ ch, int nch,
-                                                const Scal* sc, double* partial, int mode, int to_vc, Finish F) {
+template <typename T, int mode>
+__global__ void __launch_bounds__(256, 4) kr_apply(const LvlDev* __restrict__ Ls, const KrylovDev* __restrict__ K, const Chunk* __restrict__ ch, int nch,
+                                                   const Scal* sc, double* partial, int to_vc, Finish F) {
     __shared__ double sh[32];
     __shared__ int flag;
     for (int c = blockIdx.x; c < nch; c += gridDim.x) {
@@ -292,14 +292,14 @@ __global__ void __launch_bounds__(256) kr_apply(const LvlDev* __restrict__ Ls, c
             T* __restrict__ vb = Sel<T>::b(L);
             T* __restrict__ vx = Sel<T>::x(L);
             for (int rw = 0; rw < C.nrows; ++rw)
-#pragma unroll 4
+#pragma unroll 2
                 for (int t = threadIdx.x; t < C.cnt; t += blockDim.x) {
                     const int i = C.i0 + t, j = C.j + rw;
                     const long long cell = cell_of(L, i, j, C.k);
                     double c0, offd;
                     stencil_parts<double>(L, in, i, j, C.k, cell, c0, offd);
                     const double ax = fma(c0, in[cell], offd);
-                    if (mode == 0) {
+                    if constexpr (mode == 0) {
                         const double bv = bp[cell];
                         const double r = bv - ax;
                         rp[cell] = r;
@@ -327,7 +327,7 @@ __global__ void __launch_bounds__(256) kr_apply(const LvlDev* __restrict__ Ls, c
 
 // x += alpha p, r -= alpha q, partial (r.r); the V-cycle's level-0 input b = (T) r, x = 0 alongside
 template <typename T>
-__global__ void __launch_bounds__(256) kr_update(const LvlDev* __restrict__ Ls, const KrylovDev* __restrict__ K, const Chunk* __restrict__ ch, int nch,
+__global__ void __launch_bounds__(256, 4) kr_update(const LvlDev* __restrict__ Ls, const KrylovDev* __restrict__ K, const Chunk* __restrict__ ch, int nch,
                                                  const Scal* sc, double* partial, Finish F) {
     __shared__ double sh[32];
     __shared__ int flag;
@@ -366,7 +366,7 @@ __global__ void __launch_bounds__(256) kr_update(const LvlDev* __restrict__ Ls, 
 
 // z = V-cycle result (read where it lies, never stored); partial (z.r, z.q)
 template <typename T>
-__global__ void __launch_bounds__(256) kr_from_vcycle(const LvlDev* __restrict__ Ls, const KrylovDev* __restrict__ K, const Chunk* __restrict__ ch,
+__global__ void __launch_bounds__(256, 4) kr_from_vcycle(const LvlDev* __restrict__ Ls, const KrylovDev* __restrict__ K, const Chunk* __restrict__ ch,
                                                       int nch, const Scal* sc, double* partial, Finish F) {
     __shared__ double sh[32];
     __shared__ int flag;
@@ -525,8 +525,9 @@ int mg_launch_bottom(cudaStream_t s, int sms, bool f32, const LvlDev* L, const i
 int kr_launch_apply(cudaStream_t s, int sms, const LvlDev* L, const KrylovDev* K, const Chunk* ch, int nch, const Scal* sc, double* partial, int mode,
                     const Finish& F, int to_vc, bool f32) {
     if (nch <= 0) return OPFLOW_OK;
-    if (f32) kr_apply<float><<<grid_of(nch, sms), 256, 0, s>>>(L, K, ch, nch, sc, partial, mode, to_vc, F);
-    else kr_apply<double><<<grid_of(nch, sms), 256, 0, s>>>(L, K, ch, nch, sc, partial, mode, to_vc, F);
+    if (mode == 0 && f32) kr_apply<float, 0><<<grid_of(nch, sms), 256, 0, s>>>(L, K, ch, nch, sc, partial, to_vc, F);
+    else if (mode == 0) kr_apply<double, 0><<<grid_of(nch, sms), 256, 0, s>>>(L, K, ch, nch, sc, partial, to_vc, F);
+    else kr_apply<double, 1><<<grid_of(nch, sms), 256, 0, s>>>(L, K, ch, nch, sc, partial, 0, F);
     OPG_LAUNCHED();
     return check_launch("kr_apply");
 }

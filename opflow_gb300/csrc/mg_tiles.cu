@@ -104,10 +104,19 @@ __device__ __forceinline__ T int_res(const Interior<T>& K, const TileView<T>& V,
     return V.b[s] - (K.c0 * V.x[s] + acc);
 }
 
-// Loads x (from `x`) and b of the tile + halo (positions outside a non-periodic level hold 0 and are
-// never used).
+// Asynchronous global -> shared copy of one element (cp.async: the copy needs no register and every
+// copy a thread issues is in flight at once); completed by async_wait_all + a CTA barrier.
 template <typename T>
-__device__ __forceinline__ void tile_load(const TileView<T>& V, const T* __restrict__ x, const T* __restrict__ b) {
+__device__ __forceinline__ void async_copy(T* smem, const T* gmem) {
+    const unsigned sa = (unsigned) __cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(sa), "l"(gmem), "n"(sizeof(T)) : "memory");
+}
+__device__ __forceinline__ void async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// Issues the copies of x (from `x`) and b of the tile + halo (positions outside a non-periodic level
+// get 0 and are never used); the caller waits (async_wait_all + __syncthreads).
+template <typename T>
+__device__ __forceinline__ void tile_load_issue(const TileView<T>& V, const T* __restrict__ x, const T* __restrict__ b) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int ly = warp; ly < V.SY; ly += TILE_WARPS) {
         const int gjr = V.j0 - V.H + ly;
@@ -118,14 +127,20 @@ __device__ __forceinline__ void tile_load(const TileView<T>& V, const T* __restr
             const int s = ly * V.SX + lx;
             if (gi >= 0 && gj >= 0) {
                 const long long c = (long long) gj * V.n0 + gi;
-                V.x[s] = x[c];
-                V.b[s] = b[c];
+                async_copy(V.x + s, x + c);
+                async_copy(V.b + s, b + c);
             } else {
                 V.x[s] = 0;
                 V.b[s] = 0;
             }
         }
     }
+}
+
+template <typename T>
+__device__ __forceinline__ void tile_load(const TileView<T>& V, const T* __restrict__ x, const T* __restrict__ b) {
+    tile_load_issue<T>(V, x, b);
+    async_wait_all();
     __syncthreads();
 }
 
@@ -306,28 +321,36 @@ __global__ void __launch_bounds__(TILE_THREADS, 4) mg_tile_up(const LvlDev* __re
         TileView<T> V;
         Interior<T> K;
         tile_setup<T>(L, C, 2 * post, sm, tab, K, V);
-        tile_load<T>(V, Sel<T>::r(L), Sel<T>::b(L));
         const LvlDev& Lc = Ls[L.coarse];
         // cell-centred interior tile whose coarse neighbours (I = f/2 and I +- 1) all exist: bilinear
-        // interpolation without ghost rules, in the generic form's operation order
-        const bool cint = V.interior && !Lc.node && ((V.i0 - V.H) >> 1) - 1 >= 0 && ((V.i0 + V.TX + V.H - 1) >> 1) + 1 < Lc.n[0] &&
-                          ((V.j0 - V.H) >> 1) - 1 >= 0 && ((V.j0 + V.TY + V.H - 1) >> 1) + 1 < Lc.n[1];
+        // interpolation without ghost rules, in the generic form's operation order, from a copy of the
+        // coarse block [cx0, cx0 + CW) x [cy0, cy0 + CH) in shared memory
+        const int cx0 = ((V.i0 - V.H) >> 1) - 1, cy0 = ((V.j0 - V.H) >> 1) - 1;
+        const int CW = ((V.i0 + V.TX + V.H - 1) >> 1) + 2 - cx0, CH = ((V.j0 + V.TY + V.H - 1) >> 1) + 2 - cy0;
+        const bool cint = V.interior && !Lc.node && cx0 >= 0 && cx0 + CW <= Lc.n[0] && cy0 >= 0 && cy0 + CH <= Lc.n[1];
         const T* __restrict__ xc = Sel<T>::x(Lc);
         const int nc0 = Lc.n[0];
+        T* cs = V.b + V.SX * V.SY;
+        tile_load_issue<T>(V, Sel<T>::r(L), Sel<T>::b(L));
+        if (cint)
+            for (int cy = warp; cy < CH; cy += TILE_WARPS)
+                for (int cx = lane; cx < CW; cx += 32) async_copy(cs + cy * CW + cx, xc + (long long) (cy0 + cy) * nc0 + cx0 + cx);
+        async_wait_all();
+        __syncthreads();
         for (int ly = warp; ly < V.SY; ly += TILE_WARPS) {
             const int gjr = V.j0 - V.H + ly;
             if (cint) {
                 const int I1 = gjr >> 1, J1 = (gjr & 1) ? I1 + 1 : I1 - 1;
-                const T* r0 = xc + (long long) I1 * nc0;
-                const T* r1 = xc + (long long) J1 * nc0;
+                const T* r0 = cs + (I1 - cy0) * CW - cx0;
+                const T* r1 = cs + (J1 - cy0) * CW - cx0;
                 for (int lx = lane; lx < V.SX; lx += 32) {
                     const int gi = V.i0 - V.H + lx;
                     const int I0 = gi >> 1, J0 = (gi & 1) ? I0 + 1 : I0 - 1;
                     T acc = 0;
-                    acc += (T) 0.75 * (T) 0.75 * (T) 1 * __ldg(r0 + I0);
-                    acc += (T) 0.25 * (T) 0.75 * (T) 1 * __ldg(r0 + J0);
-                    acc += (T) 0.75 * (T) 0.25 * (T) 1 * __ldg(r1 + I0);
-                    acc += (T) 0.25 * (T) 0.25 * (T) 1 * __ldg(r1 + J0);
+                    acc += (T) 0.75 * (T) 0.75 * (T) 1 * r0[I0];
+                    acc += (T) 0.25 * (T) 0.75 * (T) 1 * r0[J0];
+                    acc += (T) 0.75 * (T) 0.25 * (T) 1 * r1[I0];
+                    acc += (T) 0.25 * (T) 0.25 * (T) 1 * r1[J0];
                     V.x[ly * V.SX + lx] += acc;
                 }
                 continue;
@@ -355,8 +378,9 @@ __global__ void __launch_bounds__(TILE_THREADS, 4) mg_tile_up(const LvlDev* __re
 static size_t tile_smem(bool f32, int sweeps, bool down) {
     const int H = down ? 2 * sweeps + 2 : 2 * sweeps;  // down: + residual + node reach (upper bound)
     const size_t cells = (size_t) (MG_TILE_X + 2 * H) * (MG_TILE_Y + 2 * H);
-    const size_t res = down ? (size_t) (MG_TILE_X + 2) * (MG_TILE_Y + 2) : 0;
-    return (2 * cells + res) * (f32 ? 4 : 8);
+    // down: the residual over the tile + reach; up: the coarse block of the prolongation
+    const size_t extra = down ? (size_t) (MG_TILE_X + 2) * (MG_TILE_Y + 2) : (size_t) ((MG_TILE_X + 2 * H) / 2 + 4) * ((MG_TILE_Y + 2 * H) / 2 + 4);
+    return (2 * cells + extra) * (f32 ? 4 : 8);
 }
 
 bool mg_tiles_supported(int sweeps) { return sweeps >= 1 && tile_smem(false, sweeps, true) + NCLASS * TSTRIDE * 8 <= 200 * 1024; }
