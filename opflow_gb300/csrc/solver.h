@@ -82,7 +82,7 @@ struct MGSystem {
     // Levels of at most bottom_max cells run inside one CTA per problem (mg_bottom): bottom_host lists
     // each problem's first such level, coarse_host the coarsest levels above that size (chunked path);
     // both in this system's level numbering
-    long long bottom_max = 4096;
+    long long bottom_max = 1024;
     std::vector<int> coarse_host, bottom_host;
     int* dbottom = nullptr;
     int nbottom = 0;
