@@ -130,8 +130,9 @@ namespace GPU {
     using NodeP = std::shared_ptr<const Node>;
     struct Node {
         int kind = 0;
-        NodeP a, b;
+        NodeP a, b, c;  // c: the false branch of a conditional
         int dim = 0;
+        int param = 0;  // function or flux limiter id
         double value = 0.;
         std::shared_ptr<FieldHandle> field;  // leaves
     };
@@ -153,9 +154,10 @@ namespace GPU {
             o.kind = n->kind;
             o.a = n->a ? add(n->a, memo) : -1;
             o.b = n->b ? add(n->b, memo) : -1;
+            o.c = n->c ? add(n->c, memo) : -1;
             o.dim = n->dim;
             o.value = n->value;
-            o.field = n->kind == OPFLOW_NODE_FIELD ? slotOf(n->field) : 0;
+            o.field = n->kind == OPFLOW_NODE_FIELD ? slotOf(n->field) : n->param;
             nodes.push_back(o);
             return memo[n.get()] = (int) nodes.size() - 1;
         }
@@ -278,12 +280,14 @@ inline Expr toExpr(const CartesianField<R, M>& f) {
 }
 
 namespace GPU {
-    inline Expr makeNode(int kind, const Expr& a, const Expr* b = nullptr, int dim = 0) {
+    inline Expr makeNode(int kind, const Expr& a, const Expr* b = nullptr, int dim = 0, int param = 0, const Expr* c = nullptr) {
         auto n = std::make_shared<Node>();
         n->kind = kind;
         n->a = a.node;
         if (b) n->b = b->node;
+        if (c) n->c = c->node;
         n->dim = dim;
+        n->param = param;
         return Expr(n);
     }
 }// namespace GPU
@@ -313,6 +317,88 @@ Expr operator-(const A& a) {
     return GPU::makeNode(OPFLOW_NODE_NEG, toExpr(a));
 }
 
+// comparisons and logic (src/Core/Operator/Logical/Compare.hpp, Boolean.hpp): 1.0 / 0.0 valued
+#define OPFLOW_GPU_BINOP(op, kind)                                                                           \
+    template <typename A, typename B, std::enable_if_t<is_binary_v<A, B>, int> = 0>                           \
+    Expr operator op(const A& a, const B& b) {                                                                \
+        Expr y = toExpr(b);                                                                                  \
+        return GPU::makeNode(kind, toExpr(a), &y);                                                           \
+    }
+OPFLOW_GPU_BINOP(>, OPFLOW_NODE_GT)
+OPFLOW_GPU_BINOP(>=, OPFLOW_NODE_GE)
+OPFLOW_GPU_BINOP(<, OPFLOW_NODE_LT)
+OPFLOW_GPU_BINOP(<=, OPFLOW_NODE_LE)
+OPFLOW_GPU_BINOP(!=, OPFLOW_NODE_NE)
+OPFLOW_GPU_BINOP(&&, OPFLOW_NODE_AND)
+OPFLOW_GPU_BINOP(||, OPFLOW_NODE_OR)
+#undef OPFLOW_GPU_BINOP
+template <typename A, std::enable_if_t<is_operand_v<A> && !std::is_arithmetic_v<A>, int> = 0>
+Expr operator!(const A& a) {
+    return GPU::makeNode(OPFLOW_NODE_NOT, toExpr(a));
+}
+
+// conditional(c, a, b) = c ? a : b (src/Core/Operator/Conditional.hpp)
+template <typename C, typename A, typename B>
+Expr conditional(const C& c, const A& a, const B& b) {
+    Expr ya = toExpr(a), yb = toExpr(b);
+    return GPU::makeNode(OPFLOW_NODE_COND, toExpr(c), &ya, 0, 0, &yb);
+}
+
+// per-element functions (src/Core/Operator/Arithmetic/AMDS.hpp, MinMax.hpp)
+#define OPFLOW_GPU_FUNC1(name, id)                                                                           \
+    template <typename A, std::enable_if_t<is_operand_v<A> && !std::is_arithmetic_v<A>, int> = 0>             \
+    Expr name(const A& a) {                                                                                  \
+        return GPU::makeNode(OPFLOW_NODE_FUNC1, toExpr(a), nullptr, 0, id);                                  \
+    }
+OPFLOW_GPU_FUNC1(abs, OPFLOW_F_ABS)
+OPFLOW_GPU_FUNC1(sqrt, OPFLOW_F_SQRT)
+OPFLOW_GPU_FUNC1(ceil, OPFLOW_F_CEIL)
+OPFLOW_GPU_FUNC1(floor, OPFLOW_F_FLOOR)
+OPFLOW_GPU_FUNC1(trunc, OPFLOW_F_TRUNC)
+OPFLOW_GPU_FUNC1(round, OPFLOW_F_ROUND)
+OPFLOW_GPU_FUNC1(rint, OPFLOW_F_RINT)
+OPFLOW_GPU_FUNC1(exp, OPFLOW_F_EXP)
+OPFLOW_GPU_FUNC1(exp2, OPFLOW_F_EXP2)
+OPFLOW_GPU_FUNC1(expm1, OPFLOW_F_EXPM1)
+OPFLOW_GPU_FUNC1(log, OPFLOW_F_LOG)
+OPFLOW_GPU_FUNC1(log10, OPFLOW_F_LOG10)
+OPFLOW_GPU_FUNC1(log2, OPFLOW_F_LOG2)
+OPFLOW_GPU_FUNC1(log1p, OPFLOW_F_LOG1P)
+OPFLOW_GPU_FUNC1(cbrt, OPFLOW_F_CBRT)
+OPFLOW_GPU_FUNC1(sin, OPFLOW_F_SIN)
+OPFLOW_GPU_FUNC1(cos, OPFLOW_F_COS)
+OPFLOW_GPU_FUNC1(tan, OPFLOW_F_TAN)
+OPFLOW_GPU_FUNC1(asin, OPFLOW_F_ASIN)
+OPFLOW_GPU_FUNC1(acos, OPFLOW_F_ACOS)
+OPFLOW_GPU_FUNC1(atan, OPFLOW_F_ATAN)
+OPFLOW_GPU_FUNC1(sinh, OPFLOW_F_SINH)
+OPFLOW_GPU_FUNC1(cosh, OPFLOW_F_COSH)
+OPFLOW_GPU_FUNC1(tanh, OPFLOW_F_TANH)
+OPFLOW_GPU_FUNC1(asinh, OPFLOW_F_ASINH)
+OPFLOW_GPU_FUNC1(acosh, OPFLOW_F_ACOSH)
+OPFLOW_GPU_FUNC1(atanh, OPFLOW_F_ATANH)
+OPFLOW_GPU_FUNC1(erf, OPFLOW_F_ERF)
+OPFLOW_GPU_FUNC1(erfc, OPFLOW_F_ERFC)
+OPFLOW_GPU_FUNC1(tgamma, OPFLOW_F_TGAMMA)
+OPFLOW_GPU_FUNC1(lgamma, OPFLOW_F_LGAMMA)
+#undef OPFLOW_GPU_FUNC1
+#define OPFLOW_GPU_FUNC2(name, id)                                                                           \
+    template <typename A, typename B, std::enable_if_t<is_binary_v<A, B>, int> = 0>                           \
+    Expr name(const A& a, const B& b) {                                                                      \
+        Expr y = toExpr(b);                                                                                  \
+        return GPU::makeNode(OPFLOW_NODE_FUNC2, toExpr(a), &y, 0, id);                                       \
+    }
+OPFLOW_GPU_FUNC2(max, OPFLOW_F2_MAX)
+OPFLOW_GPU_FUNC2(min, OPFLOW_F2_MIN)
+OPFLOW_GPU_FUNC2(fdim, OPFLOW_F2_FDIM)
+OPFLOW_GPU_FUNC2(copysign, OPFLOW_F2_COPYSIGN)
+OPFLOW_GPU_FUNC2(fmod, OPFLOW_F2_FMOD)
+OPFLOW_GPU_FUNC2(remainder, OPFLOW_F2_REMAINDER)
+OPFLOW_GPU_FUNC2(pow, OPFLOW_F2_POW)
+OPFLOW_GPU_FUNC2(hypot, OPFLOW_F2_HYPOT)
+OPFLOW_GPU_FUNC2(atan2, OPFLOW_F2_ATAN2)
+#undef OPFLOW_GPU_FUNC2
+
 // `lhs == rhs` (src/Core/Equation/Equation.hpp:41-55); the solver works on lhs - rhs.
 struct Equation {
     Expr lhs, rhs;
@@ -339,6 +425,14 @@ struct D1WENO53Downwind {
 template <std::size_t d>
 struct D1WENO53Upwind {
     static constexpr int kind = OPFLOW_NODE_WENO53_UP, dim = (int) d;
+};
+template <std::size_t d>
+struct D1FirstOrderBiasedUpwind {
+    static constexpr int kind = OPFLOW_NODE_D1_BIASED_UP, dim = (int) d;
+};
+template <std::size_t d>
+struct D1FirstOrderBiasedDownwind {
+    static constexpr int kind = OPFLOW_NODE_D1_BIASED_DOWN, dim = (int) d;
 };
 
 // d1 / d2 / dx..dz / d2x..d2z as in src/Core/Operator/FDMOperators/DiffsInterface.hpp
@@ -367,6 +461,71 @@ OPFLOW_GPU_AXIS_OP(d2z, d2, 2)
 template <std::size_t dim, typename E>
 Expr d1IntpCenterToCorner(const E& e) {
     return GPU::makeNode(OPFLOW_NODE_INTP_C2C, toExpr(e), nullptr, (int) dim);
+}
+// d1IntpCornerToCenter<dim> with the default D1Linear kernel (IntpInterface.hpp:31-34)
+template <std::size_t dim, typename E>
+Expr d1IntpCornerToCenter(const E& e) {
+    return GPU::makeNode(OPFLOW_NODE_INTP_COR2CEN, toExpr(e), nullptr, (int) dim);
+}
+
+// Flux-limiter interpolation (Interpolator/D1FluxLimiter.hpp, FluxLimiterKernels.hpp,
+// D1FluxLimiterBasedIntpOp.hpp): d1Intp<d, IntpDirection::Cen2Cor, D1QUICK>(u, e) interpolates e to
+// the faces along d, upwinded by the sign of u at the target point.
+enum class IntpDirection { Cor2Cen, Cen2Cor };
+enum class KappaScheme { CDS, QUICK, CUI, Fromm, LUI };
+template <KappaScheme s>
+struct KappaKernel {
+    static constexpr int id = (int) s;  // OPFLOW_FL_CDS .. OPFLOW_FL_LUI
+};
+#define OPFLOW_GPU_LIMITER(name, id_)                                                                        \
+    struct name {                                                                                            \
+        static constexpr int id = id_;                                                                       \
+    };
+OPFLOW_GPU_LIMITER(MinmodKernel, OPFLOW_FL_MINMOD)
+OPFLOW_GPU_LIMITER(SuperbeeKernel, OPFLOW_FL_SUPERBEE)
+OPFLOW_GPU_LIMITER(MUSCLKernel, OPFLOW_FL_MUSCL)
+OPFLOW_GPU_LIMITER(HarmonicKernel, OPFLOW_FL_HARMONIC)
+OPFLOW_GPU_LIMITER(vanAlbadaKernel, OPFLOW_FL_VANALBADA)
+OPFLOW_GPU_LIMITER(UMISTKernel, OPFLOW_FL_UMIST)
+OPFLOW_GPU_LIMITER(SPL13Kernel, OPFLOW_FL_SPL13)
+OPFLOW_GPU_LIMITER(SPLMax12Kernel, OPFLOW_FL_SPLMAX12)
+OPFLOW_GPU_LIMITER(SPLMax13Kernel, OPFLOW_FL_SPLMAX13)
+OPFLOW_GPU_LIMITER(KorenLimitedCUIKernel, OPFLOW_FL_KOREN)
+OPFLOW_GPU_LIMITER(SMARTKernel, OPFLOW_FL_SMART)
+OPFLOW_GPU_LIMITER(BSOUKernel, OPFLOW_FL_BSOU)
+#undef OPFLOW_GPU_LIMITER
+template <typename K>
+struct D1FluxLimiterGen {
+    template <std::size_t d, IntpDirection dir>
+    struct Op {
+        static constexpr int limiter = K::id;
+    };
+};
+template <std::size_t d, IntpDirection dir> using D1Central = D1FluxLimiterGen<KappaKernel<KappaScheme::CDS>>::Op<d, dir>;
+template <std::size_t d, IntpDirection dir> using D1QUICK = D1FluxLimiterGen<KappaKernel<KappaScheme::QUICK>>::Op<d, dir>;
+template <std::size_t d, IntpDirection dir> using D1CUI = D1FluxLimiterGen<KappaKernel<KappaScheme::CUI>>::Op<d, dir>;
+template <std::size_t d, IntpDirection dir> using D1Fromm = D1FluxLimiterGen<KappaKernel<KappaScheme::Fromm>>::Op<d, dir>;
+template <std::size_t d, IntpDirection dir> using D1LinearUpwind = D1FluxLimiterGen<KappaKernel<KappaScheme::LUI>>::Op<d, dir>;
+template <std::size_t d, IntpDirection dir> using D1Minmod = D1FluxLimiterGen<MinmodKernel>::Op<d, dir>;
+template <std::size_t d, IntpDirection dir> using D1Superbee = D1FluxLimiterGen<SuperbeeKernel>::Op<d, dir>;
+template <std::size_t d, IntpDirection dir> using D1MUSCL = D1FluxLimiterGen<MUSCLKernel>::Op<d, dir>;
+template <std::size_t d, IntpDirection dir> using D1Harmonic = D1FluxLimiterGen<HarmonicKernel>::Op<d, dir>;
+template <std::size_t d, IntpDirection dir> using D1Albada = D1FluxLimiterGen<vanAlbadaKernel>::Op<d, dir>;
+// d1Intp<dim, dir, Kernel>(u, e) (IntpInterface.hpp:36-40) for the flux-limiter kernels
+template <std::size_t d, IntpDirection dir, template <std::size_t, IntpDirection> typename Kernel, typename U, typename E>
+Expr d1Intp(const U& u, const E& e) {
+    Expr ye = toExpr(e);
+    return GPU::makeNode(dir == IntpDirection::Cen2Cor ? OPFLOW_NODE_INTP_FL_CEN2COR : OPFLOW_NODE_INTP_FL_COR2CEN, toExpr(u), &ye,
+                         (int) d, Kernel<d, dir>::limiter);
+}
+// d1IntpCenterToCorner<dim, Kernel>(u, e) / d1IntpCornerToCenter<dim, Kernel>(u, e) with a flux-limiter kernel
+template <std::size_t d, template <std::size_t, IntpDirection> typename Kernel, typename U, typename E>
+Expr d1IntpCenterToCorner(const U& u, const E& e) {
+    return d1Intp<d, IntpDirection::Cen2Cor, Kernel>(u, e);
+}
+template <std::size_t d, template <std::size_t, IntpDirection> typename Kernel, typename U, typename E>
+Expr d1IntpCornerToCenter(const U& u, const E& e) {
+    return d1Intp<d, IntpDirection::Cor2Cen, Kernel>(u, e);
 }
 
 // ------------------------------------------------------------------------------------------ field
@@ -457,7 +616,7 @@ public:
             for (;;) {
                 std::array<Real, dim> X;
                 for (int q = 0; q < dim; ++q)
-                    X[q] = desc.loc[q] == OPFLOW_CENTER ? 0.5 * (mesh.x(q, i[q]) + mesh.x(q, i[q] + 1)) : mesh.x(q, i[q]);
+                    X[q] = desc.loc[q] == OPFLOW_CENTER ? mesh.x(q, i[q]) + .5 * mesh.dx(q, i[q]) : mesh.x(q, i[q]);
                 v[linear(i)] = f(X);
                 int d = 0;
                 while (d < dim && ++i[d] == r.end[d]) {

@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define OPFLOW_GPU_ABI_VERSION 1
+#define OPFLOW_GPU_ABI_VERSION 2
 
 /* ---- status codes ---------------------------------------------------------------------------- */
 enum opflow_status {
@@ -152,15 +152,74 @@ enum opflow_node_kind {
     OPFLOW_NODE_D1 = 9,         /* D1FirstOrderCentered<dim>    (D1FirstOrderCentered.hpp:31-36)    */
     OPFLOW_NODE_WENO53_DOWN = 10,/* D1WENO53Downwind<dim>       (D1WENO53Downwind.hpp:136-154)      */
     OPFLOW_NODE_WENO53_UP = 11, /* D1WENO53Upwind<dim>          (D1WENO53Upwind.hpp:133-151)        */
-    OPFLOW_NODE_INTP_C2C = 12   /* D1Linear Cen2Cor, d1IntpCenterToCorner<dim> (D1Linear.hpp:35-45) */
+    OPFLOW_NODE_INTP_C2C = 12,  /* D1Linear Cen2Cor, d1IntpCenterToCorner<dim> (D1Linear.hpp:35-45) */
+    OPFLOW_NODE_INTP_COR2CEN = 13,/* D1Linear Cor2Cen, d1IntpCornerToCenter<dim> (D1Linear.hpp:43-45) */
+    OPFLOW_NODE_D1_BIASED_UP = 14,  /* D1FirstOrderBiasedUpwind<dim>   (D1FirstOrderBiasedUpwind.hpp:53-58)   */
+    OPFLOW_NODE_D1_BIASED_DOWN = 15,/* D1FirstOrderBiasedDownwind<dim> (D1FirstOrderBiasedDownwind.hpp:52-57) */
+    /* comparisons (Logical/Compare.hpp:27-31): 1.0 when true, 0.0 when false */
+    OPFLOW_NODE_GT = 16,        /* a > b   GreaterThan                                             */
+    OPFLOW_NODE_GE = 17,        /* a >= b  GreaterThanOrEqual                                      */
+    OPFLOW_NODE_LT = 18,        /* a < b   LessThan                                                */
+    OPFLOW_NODE_LE = 19,        /* a <= b  LessThanOrEqual                                         */
+    OPFLOW_NODE_NE = 20,        /* a != b  NotEqualTo                                              */
+    /* logic (Logical/Boolean.hpp:24-26): operands are true when non-zero                           */
+    OPFLOW_NODE_AND = 21,       /* a && b                                                          */
+    OPFLOW_NODE_OR = 22,        /* a || b                                                          */
+    OPFLOW_NODE_NOT = 23,       /* !a                                                              */
+    OPFLOW_NODE_COND = 24,      /* conditional(a, b, c): a ? b : c   (Conditional.hpp:22-40)       */
+    OPFLOW_NODE_FUNC1 = 25,     /* per-element function `field` (enum opflow_func1) of a (AMDS.hpp:54-91) */
+    OPFLOW_NODE_FUNC2 = 26,     /* per-element function `field` (enum opflow_func2) of a, b (AMDS.hpp:39-50, MinMax.hpp) */
+    OPFLOW_NODE_INTP_FL_CEN2COR = 27, /* d1Intp<D1FluxLimiterGen<K>::Op, dim, Cen2Cor>(a, b): b interpolated
+                                         to faces, upwinded by the sign of a (D1FluxLimiter.hpp:36-133, 136-166);
+                                         `field` is the limiter K (enum opflow_flux_limiter) */
+    OPFLOW_NODE_INTP_FL_COR2CEN = 28  /* the same, corners to centres (D1FluxLimiter.hpp:61-150, 168-201) */
+};
+
+/* Per-element functions of OPFLOW_NODE_FUNC1 (std:: functions of the same name).  ABS .. RINT are
+ * exact in IEEE arithmetic and bit-identical to the reference; the others are CUDA's double-precision
+ * math functions (a few ulp from the host C library's). */
+enum opflow_func1 {
+    OPFLOW_F_ABS = 0, OPFLOW_F_SQRT, OPFLOW_F_CEIL, OPFLOW_F_FLOOR, OPFLOW_F_TRUNC, OPFLOW_F_ROUND, OPFLOW_F_RINT,
+    OPFLOW_F_EXP = 16, OPFLOW_F_EXP2, OPFLOW_F_EXPM1, OPFLOW_F_LOG, OPFLOW_F_LOG10, OPFLOW_F_LOG2, OPFLOW_F_LOG1P,
+    OPFLOW_F_CBRT, OPFLOW_F_SIN, OPFLOW_F_COS, OPFLOW_F_TAN, OPFLOW_F_ASIN, OPFLOW_F_ACOS, OPFLOW_F_ATAN,
+    OPFLOW_F_SINH, OPFLOW_F_COSH, OPFLOW_F_TANH, OPFLOW_F_ASINH, OPFLOW_F_ACOSH, OPFLOW_F_ATANH, OPFLOW_F_ERF,
+    OPFLOW_F_ERFC, OPFLOW_F_TGAMMA, OPFLOW_F_LGAMMA
+};
+/* Per-element functions of OPFLOW_NODE_FUNC2.  MAX, MIN (std::max / std::min: a < b ? b : a and
+ * b < a ? b : a), FDIM, COPYSIGN, FMOD and REMAINDER are exact; POW, HYPOT and ATAN2 are CUDA's. */
+enum opflow_func2 {
+    OPFLOW_F2_MAX = 0, OPFLOW_F2_MIN, OPFLOW_F2_FDIM, OPFLOW_F2_COPYSIGN, OPFLOW_F2_FMOD, OPFLOW_F2_REMAINDER,
+    OPFLOW_F2_POW = 16, OPFLOW_F2_HYPOT, OPFLOW_F2_ATAN2
+};
+/* Flux limiters K of OPFLOW_NODE_INTP_FL_* (Interpolator/FluxLimiterKernels.hpp, the aliases of
+ * D1FluxLimiterBasedIntpOp.hpp).  The kappa schemes are the linear kernels K(slope_u, slope_f). */
+enum opflow_flux_limiter {
+    OPFLOW_FL_CDS = 0,      /* D1Central:      KappaKernel<CDS>,   kappa = 1     */
+    OPFLOW_FL_QUICK = 1,    /* D1QUICK:        KappaKernel<QUICK>, kappa = 1/2   */
+    OPFLOW_FL_CUI = 2,      /* D1CUI:          KappaKernel<CUI>,   kappa = 1/3   */
+    OPFLOW_FL_FROMM = 3,    /* D1Fromm:        KappaKernel<Fromm>, kappa = 0     */
+    OPFLOW_FL_LUI = 4,      /* D1LinearUpwind: KappaKernel<LUI>,   kappa = -1    */
+    OPFLOW_FL_MINMOD = 5,   /* D1Minmod                                          */
+    OPFLOW_FL_SUPERBEE = 6, /* D1Superbee                                        */
+    OPFLOW_FL_MUSCL = 7,    /* D1MUSCL                                           */
+    OPFLOW_FL_HARMONIC = 8, /* D1Harmonic                                        */
+    OPFLOW_FL_VANALBADA = 9,/* D1Albada                                          */
+    OPFLOW_FL_UMIST = 10,   /* SPLMinKernel<2, 1/2>                              */
+    OPFLOW_FL_SPL13 = 11,   /* SPLMinKernel<2, 1/3>                              */
+    OPFLOW_FL_SPLMAX12 = 12,/* SPLMaxKernel<2, 1/2>                              */
+    OPFLOW_FL_SPLMAX13 = 13,/* SPLMaxKernel<2, 1/3>                              */
+    OPFLOW_FL_KOREN = 14,   /* GPLKappaKernel<2, 0, 1/3> (Koren's limited CUI)   */
+    OPFLOW_FL_SMART = 15,   /* GPLKappaKernel<4, 0, 1/2>                         */
+    OPFLOW_FL_BSOU = 16     /* GPLKappaKernel<1, 0, -1>                          */
 };
 
 typedef struct {
-    int kind;     /* enum opflow_node_kind               */
-    int a, b;     /* child node indices, -1 if unused    */
-    int dim;      /* operator direction                  */
-    int field;    /* leaf slot for OPFLOW_NODE_FIELD     */
-    double value; /* constant for OPFLOW_NODE_CONST      */
+    int kind;     /* enum opflow_node_kind                                                     */
+    int a, b;     /* child node indices, -1 if unused                                          */
+    int dim;      /* operator direction                                                        */
+    int field;    /* leaf slot for OPFLOW_NODE_FIELD; function for FUNC1/FUNC2; limiter for INTP_FL_* */
+    double value; /* constant for OPFLOW_NODE_CONST                                            */
+    int c;        /* third child (OPFLOW_NODE_COND's false branch), -1 if unused               */
 } opflow_node;
 
 /* Evaluation modes of the explicit path. */

@@ -15,7 +15,19 @@ CORNER, CENTER = 0, 1
 BC_UNDEFINED, BC_DIRC, BC_NEUM, BC_PERIODIC, BC_SYMM, BC_ASYMM = range(6)
 ASSIGN_EQ, ASSIGN_ADD, ASSIGN_SUB, ASSIGN_MUL, ASSIGN_DIV = range(5)
 (NODE_FIELD, NODE_CONST, NODE_ADD, NODE_SUB, NODE_MUL, NODE_DIV, NODE_NEG, NODE_D2, NODE_D1,
- NODE_WENO53_DOWN, NODE_WENO53_UP, NODE_INTP_C2C) = range(1, 13)
+ NODE_WENO53_DOWN, NODE_WENO53_UP, NODE_INTP_C2C, NODE_INTP_COR2CEN, NODE_D1_BIASED_UP,
+ NODE_D1_BIASED_DOWN, NODE_GT, NODE_GE, NODE_LT, NODE_LE, NODE_NE, NODE_AND, NODE_OR, NODE_NOT, NODE_COND,
+ NODE_FUNC1, NODE_FUNC2, NODE_INTP_FL_CEN2COR, NODE_INTP_FL_COR2CEN) = range(1, 29)
+# enum opflow_func1 / opflow_func2 / opflow_flux_limiter
+FUNC1 = {name: i for i, name in enumerate(["abs", "sqrt", "ceil", "floor", "trunc", "round", "rint"])}
+FUNC1.update({name: 16 + i for i, name in enumerate(
+    ["exp", "exp2", "expm1", "log", "log10", "log2", "log1p", "cbrt", "sin", "cos", "tan", "asin", "acos", "atan",
+     "sinh", "cosh", "tanh", "asinh", "acosh", "atanh", "erf", "erfc", "tgamma", "lgamma"])})
+FUNC1_EXACT = {"abs", "sqrt", "ceil", "floor", "trunc", "round", "rint"}
+FUNC2 = {"max": 0, "min": 1, "fdim": 2, "copysign": 3, "fmod": 4, "remainder": 5, "pow": 16, "hypot": 17, "atan2": 18}
+FUNC2_EXACT = {"max", "min", "fdim", "copysign", "fmod", "remainder"}
+(FL_CDS, FL_QUICK, FL_CUI, FL_FROMM, FL_LUI, FL_MINMOD, FL_SUPERBEE, FL_MUSCL, FL_HARMONIC, FL_VANALBADA, FL_UMIST,
+ FL_SPL13, FL_SPLMAX12, FL_SPLMAX13, FL_KOREN, FL_SMART, FL_BSOU) = range(17)
 EVAL_EXACT, EVAL_FAST = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
 
@@ -41,7 +53,7 @@ class FieldInfo(C.Structure):
 
 class Node(C.Structure):
     _fields_ = [("kind", C.c_int), ("a", C.c_int), ("b", C.c_int), ("dim", C.c_int), ("field", C.c_int),
-                ("value", C.c_double)]
+                ("value", C.c_double), ("c", C.c_int)]
 
 
 class SolveParams(C.Structure):

@@ -204,6 +204,41 @@ class Expr:
     def __eq__(self, o):  # lhs == rhs -> Equation (Equation.hpp:41-55)
         return Equation(self, _wrap(o))
 
+    # comparisons (Logical/Compare.hpp); `==` stays the equation builder, as in the reference
+    def __gt__(self, o):
+        return ExprNode(capi.NODE_GT, self, _wrap(o))
+
+    def __ge__(self, o):
+        return ExprNode(capi.NODE_GE, self, _wrap(o))
+
+    def __lt__(self, o):
+        return ExprNode(capi.NODE_LT, self, _wrap(o))
+
+    def __le__(self, o):
+        return ExprNode(capi.NODE_LE, self, _wrap(o))
+
+    def __ne__(self, o):
+        return ExprNode(capi.NODE_NE, self, _wrap(o))
+
+    # && / || / ! of Logical/Boolean.hpp, spelled & | ~ in Python
+    def __and__(self, o):
+        return ExprNode(capi.NODE_AND, self, _wrap(o))
+
+    def __rand__(self, o):
+        return ExprNode(capi.NODE_AND, _wrap(o), self)
+
+    def __or__(self, o):
+        return ExprNode(capi.NODE_OR, self, _wrap(o))
+
+    def __ror__(self, o):
+        return ExprNode(capi.NODE_OR, _wrap(o), self)
+
+    def __invert__(self):
+        return ExprNode(capi.NODE_NOT, self)
+
+    def __abs__(self):
+        return ExprNode(capi.NODE_FUNC1, self, param=capi.FUNC1["abs"])
+
     def __hash__(self):
         return id(self)
 
@@ -222,8 +257,8 @@ def _wrap(o):
 
 
 class ExprNode(Expr):
-    def __init__(self, kind, a=None, b=None, dim=0):
-        self.kind, self.a, self.b, self.dim = kind, a, b, dim
+    def __init__(self, kind, a=None, b=None, dim=0, c=None, param=0):
+        self.kind, self.a, self.b, self.dim, self.c, self.param = kind, a, b, dim, c, param
 
 
 class Equation:
@@ -242,9 +277,19 @@ def Eq(lhs, rhs):
     return Equation(_wrap(lhs), _wrap(rhs))
 
 
+# Kernel tags with the reference's names, for dx(u, D1FirstOrderBiasedDownwind) in the place of
+# dx<D1FirstOrderBiasedDownwind>(u) (DiffsInterface.hpp).
+D2SecondOrderCentered = capi.NODE_D2
+D1FirstOrderCentered = capi.NODE_D1
+D1FirstOrderBiasedUpwind = capi.NODE_D1_BIASED_UP
+D1FirstOrderBiasedDownwind = capi.NODE_D1_BIASED_DOWN
+D1WENO53Upwind = capi.NODE_WENO53_UP
+D1WENO53Downwind = capi.NODE_WENO53_DOWN
+
+
 def _diff(kind, dim):
-    def f(e):
-        return ExprNode(kind, _wrap(e), None, dim)
+    def f(e, kernel=None):
+        return ExprNode(kind if kernel is None else kernel, _wrap(e), None, dim)
     return f
 
 
@@ -273,9 +318,92 @@ def d1_weno53_upwind(e, dim=0):
     return ExprNode(capi.NODE_WENO53_UP, _wrap(e), None, dim)
 
 
+# d1<D1FirstOrderBiasedUpwind<d>> / d1<D1FirstOrderBiasedDownwind<d>>: one-sided first differences
+# (D1FirstOrderBiasedUpwind.hpp:53-58, D1FirstOrderBiasedDownwind.hpp:52-57); the reference's
+# examples/CONV1D writes the downwind one as dx<D1FirstOrderBiasedDownwind>(u).
+def d1_biased_upwind(e, dim=0):
+    return ExprNode(capi.NODE_D1_BIASED_UP, _wrap(e), None, dim)
+
+
+def d1_biased_downwind(e, dim=0):
+    return ExprNode(capi.NODE_D1_BIASED_DOWN, _wrap(e), None, dim)
+
+
 # d1IntpCenterToCorner<d> (IntpInterface.hpp:22-33, D1Linear Cen2Cor)
 def d1IntpCenterToCorner(e, dim):
     return ExprNode(capi.NODE_INTP_C2C, _wrap(e), None, dim)
+
+
+# d1IntpCornerToCenter<d> (IntpInterface.hpp:31-34, D1Linear Cor2Cen: the midpoint of e(i), e(i+1))
+def d1IntpCornerToCenter(e, dim):
+    return ExprNode(capi.NODE_INTP_COR2CEN, _wrap(e), None, dim)
+
+
+# conditional(c, a, b) = c ? a : b (Conditional.hpp)
+def conditional(c, a, b):
+    return ExprNode(capi.NODE_COND, _wrap(c), _wrap(a), c=_wrap(b))
+
+
+def logical_and(a, b):
+    return ExprNode(capi.NODE_AND, _wrap(a), _wrap(b))
+
+
+def logical_or(a, b):
+    return ExprNode(capi.NODE_OR, _wrap(a), _wrap(b))
+
+
+def logical_not(a):
+    return ExprNode(capi.NODE_NOT, _wrap(a))
+
+
+def _func1(name):
+    fid = capi.FUNC1[name]
+
+    def f(e):
+        return ExprNode(capi.NODE_FUNC1, _wrap(e), param=fid)
+    f.__name__ = name
+    f.__doc__ = "Per-element std::%s (Arithmetic/AMDS.hpp)." % name
+    return f
+
+
+def _func2(name):
+    fid = capi.FUNC2[name]
+
+    def f(a, b):
+        return ExprNode(capi.NODE_FUNC2, _wrap(a), _wrap(b), param=fid)
+    f.__name__ = name
+    f.__doc__ = "Per-element std::%s (Arithmetic/AMDS.hpp, MinMax.hpp)." % name
+    return f
+
+
+_FUNCS = {**{n: _func1(n) for n in capi.FUNC1}, **{n: _func2(n) for n in capi.FUNC2}}
+
+
+def __getattr__(name):
+    """api.max, api.sqrt, ... (module attributes only, so that this module's own code keeps Python's
+    builtin max / min / abs / round / pow)."""
+    try:
+        return _FUNCS[name]
+    except KeyError:
+        raise AttributeError("module %r has no attribute %r" % (__name__, name)) from None
+
+
+# Flux-limiter interpolators of D1FluxLimiterBasedIntpOp.hpp: d1Intp<D1QUICK, d, Cen2Cor>(u, e) is
+# d1IntpCenterToCorner(e, d, limiter="QUICK", u=u): e interpolated to the faces along d, upwinded by
+# the sign of u at the face (D1FluxLimiter.hpp:136-201).
+FLUX_LIMITERS = {"Central": capi.FL_CDS, "QUICK": capi.FL_QUICK, "CUI": capi.FL_CUI, "Fromm": capi.FL_FROMM,
+                 "LinearUpwind": capi.FL_LUI, "Minmod": capi.FL_MINMOD, "Superbee": capi.FL_SUPERBEE,
+                 "MUSCL": capi.FL_MUSCL, "Harmonic": capi.FL_HARMONIC, "Albada": capi.FL_VANALBADA,
+                 "UMIST": capi.FL_UMIST, "SPL13": capi.FL_SPL13, "SPLMax12": capi.FL_SPLMAX12,
+                 "SPLMax13": capi.FL_SPLMAX13, "KorenLimitedCUI": capi.FL_KOREN, "SMART": capi.FL_SMART,
+                 "BSOU": capi.FL_BSOU}
+
+
+def d1_flux_limiter_intp(u, e, dim, limiter, to_corner=True):
+    """d1Intp<D1FluxLimiterGen<K>::Op, dim, Cen2Cor or Cor2Cen>(u, e)."""
+    k = FLUX_LIMITERS[limiter] if isinstance(limiter, str) else int(limiter)
+    kind = capi.NODE_INTP_FL_CEN2COR if to_corner else capi.NODE_INTP_FL_COR2CEN
+    return ExprNode(kind, _wrap(u), _wrap(e), dim, param=k)
 
 
 def serialize(expr, extra_leaves=()):
@@ -297,13 +425,14 @@ def serialize(expr, extra_leaves=()):
         if key in memo and not is_leaf:
             return memo[key]
         if is_leaf:
-            n = (capi.NODE_FIELD, -1, -1, 0, leaf_slot(e), 0.0)
+            n = (capi.NODE_FIELD, -1, -1, 0, leaf_slot(e), 0.0, -1)
         elif isinstance(e, ScalarExpr):
-            n = (capi.NODE_CONST, -1, -1, 0, 0, e.value)
+            n = (capi.NODE_CONST, -1, -1, 0, 0, e.value, -1)
         elif isinstance(e, ExprNode):
             a = rec(e.a) if e.a is not None else -1
             b = rec(e.b) if e.b is not None else -1
-            n = (e.kind, a, b, e.dim, 0, 0.0)
+            c = rec(e.c) if getattr(e, "c", None) is not None else -1
+            n = (e.kind, a, b, e.dim, getattr(e, "param", 0), 0.0, c)
         else:
             raise TypeError("not an expression: %r" % (e,))
         nodes.append(n)
@@ -312,8 +441,8 @@ def serialize(expr, extra_leaves=()):
 
     rec(_wrap(expr))
     arr = (capi.Node * len(nodes))()
-    for i, (k, a, b, d, f, v) in enumerate(nodes):
-        arr[i].kind, arr[i].a, arr[i].b, arr[i].dim, arr[i].field, arr[i].value = k, a, b, d, f, v
+    for i, (k, a, b, d, f, v, c) in enumerate(nodes):
+        arr[i].kind, arr[i].a, arr[i].b, arr[i].dim, arr[i].field, arr[i].value, arr[i].c = k, a, b, d, f, v, c
     return arr, leaves
 
 

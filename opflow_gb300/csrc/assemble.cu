@@ -5,6 +5,7 @@
 // StencilField.hpp:123-350).  The device keeps each pad dense over the fixed offset set K that the
 // program can reach; "absent" and "zero" coincide there, which changes no value.
 #include "assemble.h"
+#include "pointwise.h"
 
 #include <cmath>
 #include <map>
@@ -50,14 +51,31 @@ struct PadCompiler {
                     L = loc[nd.a][0] >= 0 ? loc[nd.a] : loc[nd.b];
                     break;
                 case OPFLOW_NODE_NEG: case OPFLOW_NODE_D2: case OPFLOW_NODE_D1: case OPFLOW_NODE_INTP_C2C:
+                case OPFLOW_NODE_INTP_COR2CEN: case OPFLOW_NODE_D1_BIASED_UP: case OPFLOW_NODE_D1_BIASED_DOWN:
                     if (nd.a < 0) return fail(OPFLOW_E_INVALID, "node %d: missing operand", k);
                     L = loc[nd.a];
                     if (nd.kind != OPFLOW_NODE_NEG && (nd.dim < 0 || nd.dim >= mesh->ndim)) return fail(OPFLOW_E_INVALID, "node %d: bad dim", k);
                     if (nd.kind == OPFLOW_NODE_D1) L[nd.dim] = L[nd.dim] == OPFLOW_CENTER ? OPFLOW_CORNER : OPFLOW_CENTER;
                     if (nd.kind == OPFLOW_NODE_INTP_C2C) L[nd.dim] = OPFLOW_CORNER;
+                    if (nd.kind == OPFLOW_NODE_INTP_COR2CEN) L[nd.dim] = OPFLOW_CENTER;
                     break;
                 case OPFLOW_NODE_WENO53_DOWN: case OPFLOW_NODE_WENO53_UP:
                     return fail(OPFLOW_E_UNSUPPORTED, "WENO operators are nonlinear and have no StencilPad form");
+                case OPFLOW_NODE_GT: case OPFLOW_NODE_GE: case OPFLOW_NODE_LT: case OPFLOW_NODE_LE: case OPFLOW_NODE_NE:
+                case OPFLOW_NODE_AND: case OPFLOW_NODE_OR: case OPFLOW_NODE_FUNC2:
+                    if (nd.a < 0 || nd.b < 0) return fail(OPFLOW_E_INVALID, "node %d: missing operand", k);
+                    L = loc[nd.a][0] >= 0 ? loc[nd.a] : loc[nd.b];
+                    break;
+                case OPFLOW_NODE_NOT: case OPFLOW_NODE_FUNC1:
+                    if (nd.a < 0) return fail(OPFLOW_E_INVALID, "node %d: missing operand", k);
+                    L = loc[nd.a];
+                    break;
+                case OPFLOW_NODE_COND:
+                    if (nd.a < 0 || nd.b < 0 || nd.c < 0 || nd.c >= k) return fail(OPFLOW_E_INVALID, "node %d: bad conditional operands", k);
+                    L = loc[nd.b][0] >= 0 ? loc[nd.b] : (loc[nd.c][0] >= 0 ? loc[nd.c] : loc[nd.a]);
+                    break;
+                case OPFLOW_NODE_INTP_FL_CEN2COR: case OPFLOW_NODE_INTP_FL_COR2CEN:
+                    return fail(OPFLOW_E_UNSUPPORTED, "flux-limiter interpolation has no StencilPad form in this engine");
                 default: return fail(OPFLOW_E_UNSUPPORTED, "node %d: unknown kind", k);
             }
         }
@@ -171,8 +189,49 @@ struct PadCompiler {
                 bin(Q_DIV);
                 break;
             }
+            case OPFLOW_NODE_INTP_COR2CEN: {
+                // Math::mid(e(i), e(i + 1)) = (x1 + x2) * 0.5
+                int op_[3] = {off[0], off[1], off[2]};
+                op_[nd.dim]++;
+                emit(nd.a, off); emit(nd.a, op_); bin(Q_ADD); cst(0.5); bin(Q_MUL);
+                break;
+            }
+            case OPFLOW_NODE_D1_BIASED_UP: case OPFLOW_NODE_D1_BIASED_DOWN: {
+                const int d = nd.dim, up = nd.kind == OPFLOW_NODE_D1_BIASED_UP, o = off[d] - (up ? 0 : 1);
+                int hi[3] = {off[0], off[1], off[2]}, lo[3] = {off[0], off[1], off[2]};
+                if (up) hi[d]++; else lo[d]--;
+                emit(nd.a, hi); emit(nd.a, lo); bin(Q_SUB);
+                if (loc[nd.a][d] == OPFLOW_CORNER) dxm(d, o);
+                else { dxm(d, o); dxm(d, o + 1); bin(Q_ADD); cst(0.5); bin(Q_MUL); }
+                bin(Q_DIV);
+                break;
+            }
+            case OPFLOW_NODE_GT: case OPFLOW_NODE_GE: case OPFLOW_NODE_LT: case OPFLOW_NODE_LE: case OPFLOW_NODE_NE:
+            case OPFLOW_NODE_AND: case OPFLOW_NODE_OR: case OPFLOW_NODE_FUNC2: {
+                static const int ops[] = {Q_GT, Q_GE, Q_LT, Q_LE, Q_NE, Q_AND, Q_OR};
+                emit(nd.a, off); emit(nd.b, off);
+                scalar_op(nd.kind == OPFLOW_NODE_FUNC2 ? Q_F2 : ops[nd.kind - OPFLOW_NODE_GT], 2, nd.field);
+                break;
+            }
+            case OPFLOW_NODE_NOT: emit(nd.a, off); scalar_op(Q_NOT, 1, 0); break;
+            case OPFLOW_NODE_FUNC1: emit(nd.a, off); scalar_op(Q_F1, 1, nd.field); break;
+            case OPFLOW_NODE_COND: emit(nd.a, off); emit(nd.b, off); emit(nd.c, off); scalar_op(Q_SEL, 3, 0); break;
             default: err = fail(OPFLOW_E_UNSUPPORTED, "operator without a StencilPad form");
         }
+    }
+    // A comparison, logic operator, conditional or per-element function of values that do not depend
+    // on the unknown; applied to a StencilPad it has no linear form.
+    void scalar_op(int op, int arity, int fn) {
+        if (err) return;
+        for (int q = 0; q < arity; ++q)
+            if (kinds[kinds.size() - 1 - q]) {
+                err = fail(OPFLOW_E_UNSUPPORTED, "comparison, conditional or function of the unknown: no StencilPad form");
+                return;
+            }
+        for (int q = 0; q < arity; ++q) kinds.pop_back();
+        PInstr in{op, fn, {0, 0, 0}, 0.};
+        prog.push_back(in);
+        kinds.push_back(0);
     }
 
     int run(std::vector<std::array<int, 3>>& K) {
@@ -183,13 +242,25 @@ struct PadCompiler {
         emit(n - 1, off);
         if (err) return err;
         if (kinds.size() != 1 || !kinds[0]) return fail(OPFLOW_E_INVALID, "the equation does not depend on the unknown");
-        int sp = 0, maxsp = 0;
+        // depths of the evaluator's two stacks (StencilPads and numbers)
+        int sp = 0, psp = 0, maxsp = 0, maxpsp = 0;
         for (auto& in : prog) {
-            if (in.op == Q_LOADS || in.op == Q_LOADU || in.op == Q_CONST || in.op == Q_DX || in.op == Q_X) sp++;
-            else if (in.op != Q_NEG) sp--;
+            switch (in.op) {
+                case Q_LOADU: psp++; break;
+                case Q_LOADS: case Q_CONST: case Q_DX: case Q_X: sp++; break;
+                case Q_NEG: case Q_NOT: case Q_F1: break;
+                case Q_SEL: sp -= 2; break;
+                case Q_GT: case Q_GE: case Q_LT: case Q_LE: case Q_NE: case Q_AND: case Q_OR: case Q_F2: sp--; break;
+                default:
+                    if (in.ta && in.tb) psp--;
+                    else sp--;
+            }
             maxsp = std::max(maxsp, sp);
+            maxpsp = std::max(maxpsp, psp);
         }
-        if (maxsp > PAD_STACK) return fail(OPFLOW_E_UNSUPPORTED, "equation needs a stack of %d values (limit %d)", maxsp, PAD_STACK);
+        if (psp != 1 || sp != 0) return fail(OPFLOW_E_INVALID, "malformed equation");
+        if (maxpsp > PAD_STACK) return fail(OPFLOW_E_UNSUPPORTED, "equation needs %d StencilPads at once (limit %d)", maxpsp, PAD_STACK);
+        if (maxsp > SCAL_STACK) return fail(OPFLOW_E_UNSUPPORTED, "equation needs a stack of %d numbers (limit %d)", maxsp, SCAL_STACK);
         // K: every offset a folded unknown leaf can land on (box hull of each loaded offset)
         std::set<std::array<int, 3>> ks;
         for (auto& o : uoffs) {
@@ -333,9 +404,11 @@ __global__ void __launch_bounds__(128) assemble_kernel(const PInstr* __restrict_
     for (long long t = blockIdx.x * (long long) blockDim.x + threadIdx.x; t < total; t += (long long) gridDim.x * blockDim.x) {
         int cell[3];
         box_index(t, P.box, cell[0], cell[1], cell[2]);
+        // two stacks: StencilPad values (operands that depend on the unknown) and plain numbers; every
+        // instruction knows statically which of its operands are pads (ta, tb)
         PadVal st[PAD_STACK];
-        double sv[PAD_STACK];
-        int sp = 0;
+        double sv[SCAL_STACK];
+        int psp = 0, sp = 0;
         bool ok = true;
         for (int p = 0; p < nprog && ok; ++p) {
             const PInstr in = prog[p];
@@ -350,10 +423,10 @@ __global__ void __launch_bounds__(128) assemble_kernel(const PInstr* __restrict_
                     int ki;
                     double c, b;
                     ok = st_leaf(P, cell, in.off, &ki, &c, &b);
-                    for (int q = 0; q < P.nk; ++q) st[sp].c[q] = 0.;
-                    if (ki >= 0) st[sp].c[ki] = c;
-                    st[sp].b = b;
-                    sp++;
+                    for (int q = 0; q < P.nk; ++q) st[psp].c[q] = 0.;
+                    if (ki >= 0) st[psp].c[ki] = c;
+                    st[psp].b = b;
+                    psp++;
                     break;
                 }
                 case Q_CONST: sv[sp++] = in.v; break;
@@ -361,16 +434,25 @@ __global__ void __launch_bounds__(128) assemble_kernel(const PInstr* __restrict_
                 case Q_X: sv[sp++] = P.mx[in.slot][cell[in.slot] + in.off[0] - P.es[in.slot]]; break;
                 case Q_NEG:
                     if (in.ta) {
-                        for (int q = 0; q < P.nk; ++q) st[sp - 1].c[q] = -st[sp - 1].c[q];
-                        st[sp - 1].b = -st[sp - 1].b;
+                        for (int q = 0; q < P.nk; ++q) st[psp - 1].c[q] = -st[psp - 1].c[q];
+                        st[psp - 1].b = -st[psp - 1].b;
                     } else sv[sp - 1] = -sv[sp - 1];
                     break;
+                case Q_GT: sp--; sv[sp - 1] = sv[sp - 1] > sv[sp] ? 1. : 0.; break;
+                case Q_GE: sp--; sv[sp - 1] = sv[sp - 1] >= sv[sp] ? 1. : 0.; break;
+                case Q_LT: sp--; sv[sp - 1] = sv[sp - 1] < sv[sp] ? 1. : 0.; break;
+                case Q_LE: sp--; sv[sp - 1] = sv[sp - 1] <= sv[sp] ? 1. : 0.; break;
+                case Q_NE: sp--; sv[sp - 1] = sv[sp - 1] != sv[sp] ? 1. : 0.; break;
+                case Q_AND: sp--; sv[sp - 1] = (sv[sp - 1] != 0. && sv[sp] != 0.) ? 1. : 0.; break;
+                case Q_OR: sp--; sv[sp - 1] = (sv[sp - 1] != 0. || sv[sp] != 0.) ? 1. : 0.; break;
+                case Q_NOT: sv[sp - 1] = sv[sp - 1] == 0. ? 1. : 0.; break;
+                case Q_SEL: sp -= 2; sv[sp - 1] = sv[sp - 1] != 0. ? sv[sp] : sv[sp + 1]; break;
+                case Q_F1: sv[sp - 1] = func1_eval(in.slot, sv[sp - 1]); break;
+                case Q_F2: sp--; sv[sp - 1] = func2_eval(in.slot, sv[sp - 1], sv[sp]); break;
                 default: {
-                    sp--;
-                    PadVal& A = st[sp - 1];
-                    const PadVal& B = st[sp];
-                    const double a = sv[sp - 1], b = sv[sp];
                     if (!in.ta && !in.tb) {
+                        sp--;
+                        const double a = sv[sp - 1], b = sv[sp];
                         double r;
                         switch (in.op) {
                             case Q_ADD: r = __dadd_rn(a, b); break;
@@ -379,18 +461,29 @@ __global__ void __launch_bounds__(128) assemble_kernel(const PInstr* __restrict_
                             default: r = __ddiv_rn(a, b);
                         }
                         sv[sp - 1] = r;
-                    } else if (in.op == Q_ADD) {
+                        break;
+                    }
+                    // pad (op) pad: A = st[psp-2], B = st[psp-1]; pad (op) num: A = st[psp-1], b = sv[sp-1];
+                    // num (op) pad: a = sv[sp-1], B = st[psp-1]; the result is a pad on top of st
+                    double a = 0., b = 0.;
+                    if (in.ta && in.tb) psp--;
+                    else if (in.ta) b = sv[--sp];
+                    else a = sv[--sp];
+                    PadVal& A = st[psp - 1];
+                    const PadVal& B = st[psp - (in.ta && in.tb ? 0 : 1)];
+                    if (in.op == Q_ADD) {
                         if (in.ta && in.tb) { for (int q = 0; q < P.nk; ++q) A.c[q] = __dadd_rn(A.c[q], B.c[q]); A.b = __dadd_rn(A.b, B.b); }
                         else if (in.ta) A.b = __dadd_rn(A.b, b);
-                        else { A = B; A.b = __dadd_rn(B.b, a); }
+                        else A.b = __dadd_rn(B.b, a);
                     } else if (in.op == Q_SUB) {
                         // pad - pad = a + (b * -1.0); pad - num = a + (-b); num - pad = StencilPad(a) + (b * -1.0)
                         if (in.ta && in.tb) { for (int q = 0; q < P.nk; ++q) A.c[q] = __dadd_rn(A.c[q], __dmul_rn(B.c[q], -1.0)); A.b = __dadd_rn(A.b, __dmul_rn(B.b, -1.0)); }
                         else if (in.ta) A.b = __dadd_rn(A.b, -b);
-                        else { for (int q = 0; q < P.nk; ++q) A.c[q] = __dmul_rn(B.c[q], -1.0); A.b = __dadd_rn(a, __dmul_rn(B.b, -1.0)); }
+                        else { for (int q = 0; q < P.nk; ++q) A.c[q] = __dmul_rn(A.c[q], -1.0); A.b = __dadd_rn(a, __dmul_rn(A.b, -1.0)); }
                     } else if (in.op == Q_MUL) {
-                        if (in.ta) { for (int q = 0; q < P.nk; ++q) A.c[q] = __dmul_rn(A.c[q], b); A.b = __dmul_rn(A.b, b); }
-                        else { A = B; for (int q = 0; q < P.nk; ++q) A.c[q] = __dmul_rn(A.c[q], a); A.b = __dmul_rn(A.b, a); }
+                        const double s = in.ta ? b : a;
+                        for (int q = 0; q < P.nk; ++q) A.c[q] = __dmul_rn(A.c[q], s);
+                        A.b = __dmul_rn(A.b, s);
                     } else {  // pad / num = pad * (1. / num)
                         const double r = __ddiv_rn(1., b);
                         for (int q = 0; q < P.nk; ++q) A.c[q] = __dmul_rn(A.c[q], r);
@@ -488,6 +581,25 @@ struct KeyEval {
                 if (!y2.pad) return y1;
                 kmerge(y2, y1);
                 return y2;
+            }
+            case OPFLOW_NODE_GT: case OPFLOW_NODE_GE: case OPFLOW_NODE_LT: case OPFLOW_NODE_LE: case OPFLOW_NODE_NE:
+            case OPFLOW_NODE_AND: case OPFLOW_NODE_OR: case OPFLOW_NODE_NOT: case OPFLOW_NODE_COND:
+            case OPFLOW_NODE_FUNC1: case OPFLOW_NODE_FUNC2:
+                return r;  // scalar-valued (the compiler refuses them on the unknown)
+            case OPFLOW_NODE_INTP_COR2CEN: {
+                auto jp = sh(nd.dim, 1);
+                KeyPad a = ev(nd.a, i), b = ev(nd.a, jp.data());
+                if (!a.pad) return b;
+                kmerge(a, b);
+                return a;
+            }
+            case OPFLOW_NODE_D1_BIASED_UP: case OPFLOW_NODE_D1_BIASED_DOWN: {
+                const bool up = nd.kind == OPFLOW_NODE_D1_BIASED_UP;
+                auto j = sh(nd.dim, up ? 1 : -1);
+                KeyPad a = up ? ev(nd.a, j.data()) : ev(nd.a, i), b = up ? ev(nd.a, i) : ev(nd.a, j.data());
+                if (!a.pad) return b;
+                kmerge(a, b);
+                return a;
             }
         }
         return r;

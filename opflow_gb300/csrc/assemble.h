@@ -4,17 +4,22 @@
 
 namespace opg {
 
-enum QOp : int { Q_LOADS = 0, Q_LOADU, Q_CONST, Q_ADD, Q_SUB, Q_MUL, Q_DIV, Q_NEG, Q_DX, Q_X };
+enum QOp : int {
+    Q_LOADS = 0, Q_LOADU, Q_CONST, Q_ADD, Q_SUB, Q_MUL, Q_DIV, Q_NEG, Q_DX, Q_X,
+    // scalar-only operators (no operand depends on the unknown)
+    Q_GT, Q_GE, Q_LT, Q_LE, Q_NE, Q_AND, Q_OR, Q_NOT, Q_SEL, Q_F1, Q_F2
+};
 struct PInstr {
     int op;
-    int slot;     // Q_LOADS/Q_LOADU: leaf slot; Q_DX/Q_X: dim
+    int slot;     // Q_LOADS/Q_LOADU: leaf slot; Q_DX/Q_X: dim; Q_F1/Q_F2: function
     int off[3];   // load offset; Q_DX/Q_X: off[0]
     double v;     // Q_CONST
     int ta = 0, tb = 0;  // operand kinds (0 scalar, 1 pad) for arithmetic
 };
 
 constexpr int PAD_KMAX = 9;   // stencil entries a pad may hold (up to 3x3 in 2D / 7 in 3D)
-constexpr int PAD_STACK = 8;  // evaluation stack depth
+constexpr int PAD_STACK = 8;    // StencilPad values live at once during an evaluation
+constexpr int SCAL_STACK = 24;  // plain numbers live at once
 
 struct AsmParams {
     int ndim;

@@ -12,6 +12,7 @@
 //      tree, again in the reference's operation order.
 #include "internal.h"
 #include "stencil.h"
+#include "pointwise.h"
 
 #include <algorithm>
 #include <array>
@@ -22,10 +23,17 @@
 namespace opg {
 
 // ======================================================================================== program format
-enum POp : int { P_LOAD = 0, P_CONST, P_ADD, P_SUB, P_MUL, P_DIV, P_NEG, P_DX, P_X, P_WENO };
+enum POp : int {
+    P_LOAD = 0, P_CONST, P_ADD, P_SUB, P_MUL, P_DIV, P_NEG, P_DX, P_X, P_WENO,
+    P_GT, P_GE, P_LT, P_LE, P_NE, P_AND, P_OR, P_NOT,  // 1.0 / 0.0 results
+    P_SEL,  // c ? a : b with (c, a, b) on the stack, c true when non-zero
+    P_F1,   // slot: enum opflow_func1
+    P_F2,   // slot: enum opflow_func2
+    P_LIM   // slot: enum opflow_flux_limiter (a non-linear limiter K(r))
+};
 struct Instr {
     int op;
-    int slot;    // P_LOAD: leaf slot; P_DX/P_X: dim; P_WENO: 1 for the upwind variant
+    int slot;    // P_LOAD: leaf slot; P_DX/P_X: dim; P_WENO: 1 for the upwind variant; P_F1/P_F2/P_LIM: function
     int off[3];  // P_LOAD: offset; P_DX/P_X: off[0] = index offset along dim
     double v;    // P_CONST
 };
@@ -36,6 +44,9 @@ static bool is_pow2(double h) {
     double m = std::frexp(h, &e);
     return m == 0.5;
 }
+
+static bool func1_known(int f) { return (f >= OPFLOW_F_ABS && f <= OPFLOW_F_RINT) || (f >= OPFLOW_F_EXP && f <= OPFLOW_F_LGAMMA); }
+static bool func2_known(int f) { return (f >= OPFLOW_F2_MAX && f <= OPFLOW_F2_REMAINDER) || (f >= OPFLOW_F2_POW && f <= OPFLOW_F2_ATAN2); }
 
 // Host compiler: expands the tree into postfix with per-leaf offsets, mirroring the recursion of
 // Expression::evalAtImpl_final (Expression.hpp:51-88); operands of binary operators keep their order.
@@ -57,6 +68,7 @@ struct Compiler {
         for (int k = 0; k < n; ++k) {
             const opflow_node& nd = nodes[k];
             if (nd.a >= k || nd.b >= k) return fail(OPFLOW_E_INVALID, "node %d: children must precede parents", k);
+            if (nd.kind == OPFLOW_NODE_COND && (nd.c < 0 || nd.c >= k)) return fail(OPFLOW_E_INVALID, "node %d: bad third operand", k);
             auto& L = loc[k];
             switch (nd.kind) {
                 case OPFLOW_NODE_FIELD:
@@ -65,11 +77,40 @@ struct Compiler {
                     break;
                 case OPFLOW_NODE_CONST: break;
                 case OPFLOW_NODE_ADD: case OPFLOW_NODE_SUB: case OPFLOW_NODE_MUL: case OPFLOW_NODE_DIV:
+                case OPFLOW_NODE_GT: case OPFLOW_NODE_GE: case OPFLOW_NODE_LT: case OPFLOW_NODE_LE: case OPFLOW_NODE_NE:
+                case OPFLOW_NODE_AND: case OPFLOW_NODE_OR: case OPFLOW_NODE_FUNC2:
+                    // initPropsFrom(arg1), or arg2 when arg1 is a scalar (BinOpDefMacros.hpp.in)
                     if (nd.a < 0 || nd.b < 0) return fail(OPFLOW_E_INVALID, "node %d: missing operand", k);
+                    if (nd.kind == OPFLOW_NODE_FUNC2 && !func2_known(nd.field)) return fail(OPFLOW_E_INVALID, "node %d: unknown function %d", k, nd.field);
                     L = loc[nd.a][0] >= 0 ? loc[nd.a] : loc[nd.b];
                     break;
+                case OPFLOW_NODE_NOT: case OPFLOW_NODE_FUNC1:
+                    if (nd.a < 0) return fail(OPFLOW_E_INVALID, "node %d: missing operand", k);
+                    if (nd.kind == OPFLOW_NODE_FUNC1 && !func1_known(nd.field)) return fail(OPFLOW_E_INVALID, "node %d: unknown function %d", k, nd.field);
+                    L = loc[nd.a];
+                    break;
+                case OPFLOW_NODE_COND:
+                    // CondOp::prepare: initPropsFrom(arg2), or arg3 when arg2 is a scalar (Conditional.hpp:41-115)
+                    if (nd.a < 0 || nd.b < 0) return fail(OPFLOW_E_INVALID, "node %d: missing operand", k);
+                    L = loc[nd.b][0] >= 0 ? loc[nd.b] : (loc[nd.c][0] >= 0 ? loc[nd.c] : loc[nd.a]);
+                    break;
+                case OPFLOW_NODE_INTP_FL_CEN2COR: case OPFLOW_NODE_INTP_FL_COR2CEN: {
+                    // D1FluxLimiterImpl::prepare (D1FluxLimiter.hpp:152-166, 182-201)
+                    if (nd.a < 0 || nd.b < 0) return fail(OPFLOW_E_INVALID, "node %d: missing operand", k);
+                    if (nd.dim < 0 || nd.dim >= mesh->ndim) return fail(OPFLOW_E_INVALID, "node %d: operator dim %d", k, nd.dim);
+                    if (nd.field < OPFLOW_FL_CDS || nd.field > OPFLOW_FL_BSOU) return fail(OPFLOW_E_INVALID, "node %d: unknown flux limiter %d", k, nd.field);
+                    if (loc[nd.b][0] < 0) return fail(OPFLOW_E_INVALID, "node %d: interpolation of a scalar", k);
+                    const bool c2c = nd.kind == OPFLOW_NODE_INTP_FL_CEN2COR;
+                    if (loc[nd.b][nd.dim] != (c2c ? OPFLOW_CENTER : OPFLOW_CORNER))
+                        return fail(OPFLOW_E_INVALID, "node %d: flux-limiter interpolation of an expression located at the %s along dim %d", k,
+                                    c2c ? "corner" : "centre", nd.dim);
+                    L = loc[nd.b];
+                    L[nd.dim] = c2c ? OPFLOW_CORNER : OPFLOW_CENTER;
+                    break;
+                }
                 case OPFLOW_NODE_NEG: case OPFLOW_NODE_D2: case OPFLOW_NODE_WENO53_DOWN: case OPFLOW_NODE_WENO53_UP:
-                case OPFLOW_NODE_D1: case OPFLOW_NODE_INTP_C2C:
+                case OPFLOW_NODE_D1: case OPFLOW_NODE_INTP_C2C: case OPFLOW_NODE_INTP_COR2CEN:
+                case OPFLOW_NODE_D1_BIASED_UP: case OPFLOW_NODE_D1_BIASED_DOWN:
                     if (nd.a < 0) return fail(OPFLOW_E_INVALID, "node %d: missing operand", k);
                     L = loc[nd.a];
                     if (nd.kind != OPFLOW_NODE_NEG) {
@@ -78,6 +119,7 @@ struct Compiler {
                     }
                     if (nd.kind == OPFLOW_NODE_D1) L[nd.dim] = L[nd.dim] == OPFLOW_CENTER ? OPFLOW_CORNER : OPFLOW_CENTER;
                     if (nd.kind == OPFLOW_NODE_INTP_C2C) L[nd.dim] = OPFLOW_CORNER;
+                    if (nd.kind == OPFLOW_NODE_INTP_COR2CEN) L[nd.dim] = OPFLOW_CENTER;
                     break;
                 default: return fail(OPFLOW_E_UNSUPPORTED, "node %d: unknown kind %d", k, nd.kind);
             }
@@ -193,7 +235,89 @@ struct Compiler {
                 bin(P_DIV);
                 break;
             }
+            case OPFLOW_NODE_INTP_COR2CEN: {
+                // Math::mid(e(i), e(i + 1)) = (x1 + x2) * 0.5
+                int op_[3] = {off[0], off[1], off[2]};
+                op_[nd.dim]++;
+                emit(nd.a, off); emit(nd.a, op_); bin(P_ADD); cst(0.5); bin(P_MUL);
+                break;
+            }
+            case OPFLOW_NODE_D1_BIASED_UP: case OPFLOW_NODE_D1_BIASED_DOWN: {
+                // upwind:   (e(i+1) - e(i)) / (Corner ? dx(i)   : (dx(i)   + dx(i+1)) * 0.5)
+                // downwind: (e(i) - e(i-1)) / (Corner ? dx(i-1) : (dx(i-1) + dx(i))   * 0.5)
+                const int d = nd.dim, up = nd.kind == OPFLOW_NODE_D1_BIASED_UP, o = off[d] - (up ? 0 : 1);
+                int hi[3] = {off[0], off[1], off[2]}, lo[3] = {off[0], off[1], off[2]};
+                if (up) hi[d]++; else lo[d]--;
+                emit(nd.a, hi); emit(nd.a, lo); bin(P_SUB);
+                if (loc[nd.a][d] == OPFLOW_CORNER) mesh_dx(d, o);
+                else { mesh_dx(d, o); mesh_dx(d, o + 1); bin(P_ADD); cst(0.5); bin(P_MUL); }
+                bin(P_DIV);
+                break;
+            }
+            case OPFLOW_NODE_GT: case OPFLOW_NODE_GE: case OPFLOW_NODE_LT: case OPFLOW_NODE_LE: case OPFLOW_NODE_NE:
+            case OPFLOW_NODE_AND: case OPFLOW_NODE_OR: {
+                static const int ops[] = {P_GT, P_GE, P_LT, P_LE, P_NE, P_AND, P_OR};
+                emit(nd.a, off); emit(nd.b, off);
+                push(Instr{ops[nd.kind - OPFLOW_NODE_GT], 0, {0, 0, 0}, 0.});
+                break;
+            }
+            case OPFLOW_NODE_NOT: emit(nd.a, off); push(Instr{P_NOT, 0, {0, 0, 0}, 0.}); break;
+            case OPFLOW_NODE_FUNC1: emit(nd.a, off); push(Instr{P_F1, nd.field, {0, 0, 0}, 0.}); break;
+            case OPFLOW_NODE_FUNC2: emit(nd.a, off); emit(nd.b, off); push(Instr{P_F2, nd.field, {0, 0, 0}, 0.}); break;
+            case OPFLOW_NODE_COND:
+                // both branches are evaluated; the reference evaluates only the taken one, with the same value
+                emit(nd.a, off); emit(nd.b, off); emit(nd.c, off);
+                push(Instr{P_SEL, 0, {0, 0, 0}, 0.});
+                break;
+            case OPFLOW_NODE_INTP_FL_CEN2COR: case OPFLOW_NODE_INTP_FL_COR2CEN: {
+                // u(i) > 0. ? upwind : downwind (D1FluxLimiterImpl::eval)
+                emit(nd.a, off); cst(0.); push(Instr{P_GT, 0, {0, 0, 0}, 0.});
+                flux_side(nd, off, true);
+                flux_side(nd, off, false);
+                push(Instr{P_SEL, 0, {0, 0, 0}, 0.});
+                break;
+            }
         }
+    }
+
+    // One side of D1FluxLimiterUpwindImpl / D1FluxLimiterDownwindImpl (D1FluxLimiter.hpp:36-133).
+    // Points p1, p2, p3 along dim (offsets from i); positions are cell centres x + 0.5*dx (Cen2Cor) or
+    // nodes x (Cor2Cen); su, sf the upwind and face slopes; the value is y2 +- (dx(o)*0.5)*K(su, sf)
+    // for the kappa kernels and y2 +- ((dx(o)*0.5)*K(sf/(su + 1e-16)))*su for the limiters.
+    void flux_side(const opflow_node& nd, const int* off, bool up) {
+        const int d = nd.dim, c2c = nd.kind == OPFLOW_NODE_INTP_FL_CEN2COR;
+        int p1, hoff;  // offset of the first point and of the dx factor
+        if (c2c) { p1 = up ? -2 : -1; hoff = up ? -1 : 0; }
+        else { p1 = up ? -1 : 0; hoff = 0; }
+        auto pos = [&](int q) {
+            const int o = off[d] + p1 + q;
+            if (c2c) {
+                if (up) { mesh_x(d, o); cst(0.5); mesh_dx(d, o); bin(P_MUL); bin(P_ADD); }  // x + 0.5*dx
+                else { mesh_x(d, o); mesh_dx(d, o); cst(0.5); bin(P_MUL); bin(P_ADD); }     // x + dx*0.5
+            } else mesh_x(d, o);
+        };
+        auto val = [&](int q) { int j[3] = {off[0], off[1], off[2]}; j[d] += p1 + q; emit(nd.b, j); };
+        // slope between points q and q+1: (y(q+1) - y(q)) / (x(q+1) - x(q))
+        auto slope = [&](int q) { val(q + 1); val(q); bin(P_SUB); pos(q + 1); pos(q); bin(P_SUB); bin(P_DIV); };
+        auto su = [&] { slope(up ? 0 : 1); };
+        auto sf = [&] { slope(up ? 1 : 0); };
+        val(1);                                             // y2
+        mesh_dx(d, off[d] + hoff); cst(0.5); bin(P_MUL);    // dx*0.5
+        const int K = nd.field;
+        if (K <= OPFLOW_FL_LUI) {
+            // KappaKernel::eval(slop_u, slop_f) = (1 + kappa) / 2. * slop_f + (1 - kappa) / 2. * slop_u
+            static const double kap[] = {1., 0.5, 1. / 3., 0., -1.};
+            cst((1 + kap[K]) / 2.); sf(); bin(P_MUL);
+            cst((1 - kap[K]) / 2.); su(); bin(P_MUL);
+            bin(P_ADD);
+            bin(P_MUL);
+        } else {
+            sf(); su(); cst(1e-16); bin(P_ADD); bin(P_DIV);  // r
+            push(Instr{P_LIM, K, {0, 0, 0}, 0.});
+            bin(P_MUL);
+            su(); bin(P_MUL);
+        }
+        bin(up ? P_ADD : P_SUB);
     }
 
     int run() {
@@ -207,8 +331,9 @@ struct Compiler {
         for (auto& in : prog) {
             switch (in.op) {
                 case P_LOAD: case P_CONST: case P_DX: case P_X: sp++; break;
-                case P_NEG: break;
+                case P_NEG: case P_NOT: case P_F1: case P_LIM: break;
                 case P_WENO: sp -= 6; break;
+                case P_SEL: sp -= 2; break;
                 default: sp--; break;
             }
             maxsp = std::max(maxsp, sp);
@@ -311,6 +436,18 @@ __global__ void __launch_bounds__(128) interp_kernel(const Instr* __restrict__ p
                     st[sp - 1] = in.slot ? -w : w;
                     break;
                 }
+                case P_GT: sp--; st[sp - 1] = st[sp - 1] > st[sp] ? 1. : 0.; break;
+                case P_GE: sp--; st[sp - 1] = st[sp - 1] >= st[sp] ? 1. : 0.; break;
+                case P_LT: sp--; st[sp - 1] = st[sp - 1] < st[sp] ? 1. : 0.; break;
+                case P_LE: sp--; st[sp - 1] = st[sp - 1] <= st[sp] ? 1. : 0.; break;
+                case P_NE: sp--; st[sp - 1] = st[sp - 1] != st[sp] ? 1. : 0.; break;
+                case P_AND: sp--; st[sp - 1] = (st[sp - 1] != 0. && st[sp] != 0.) ? 1. : 0.; break;
+                case P_OR: sp--; st[sp - 1] = (st[sp - 1] != 0. || st[sp] != 0.) ? 1. : 0.; break;
+                case P_NOT: st[sp - 1] = st[sp - 1] == 0. ? 1. : 0.; break;
+                case P_SEL: sp -= 2; st[sp - 1] = st[sp - 1] != 0. ? st[sp] : st[sp + 1]; break;
+                case P_F1: st[sp - 1] = func1_eval(in.slot, st[sp - 1]); break;
+                case P_F2: sp--; st[sp - 1] = func2_eval(in.slot, st[sp - 1], st[sp]); break;
+                case P_LIM: st[sp - 1] = flux_limiter(in.slot, st[sp - 1]); break;
             }
         }
         const long long o = (i - out.off[0]) + (j - out.off[1]) * out.sy + (k - out.off[2]) * out.sz;
@@ -735,6 +872,14 @@ static Lin lin_eval(const Compiler& C, int k, const int* off) {
             Lin a = bin(bin(lin_eval(C, nd.a, op_), lin_eval(C, nd.a, off), P_SUB), cstv(h), P_DIV);
             Lin b = bin(bin(lin_eval(C, nd.a, off), lin_eval(C, nd.a, om), P_SUB), cstv(h), P_DIV);
             return bin(bin(a, b, P_SUB), cstv(h), P_DIV);
+        }
+        case OPFLOW_NODE_D1_BIASED_UP: case OPFLOW_NODE_D1_BIASED_DOWN: {
+            // on a uniform mesh both locations divide by h ((h + h) * 0.5 == h)
+            const int d = nd.dim;
+            if (!C.mesh->uniform[d]) { r.ok = false; return r; }
+            int hi[3] = {off[0], off[1], off[2]}, lo[3] = {off[0], off[1], off[2]};
+            if (nd.kind == OPFLOW_NODE_D1_BIASED_UP) hi[d]++; else lo[d]--;
+            return bin(bin(lin_eval(C, nd.a, hi), lin_eval(C, nd.a, lo), P_SUB), cstv(C.mesh->h[d]), P_DIV);
         }
         default: r.ok = false; return r;
     }

@@ -57,18 +57,36 @@ double or_u01(uint64_t seed, uint64_t k) {
 /* mesh: MeshBuilder<CartesianMesh>::set1DRange / set1DMesh(min,max) / setExtMesh (Symm)             */
 /* CartesianMesh.hpp:209-217, 219-237, 268-276, 292-303                                              */
 /* ------------------------------------------------------------------------------------------------ */
+static void ext_symm(int dims, int start, int pad, double* x, double* dx);
+
 int or_mesh_uniform(int dims, int start, int pad, double min, double max, double* x, double* dx) {
     if (dims < 2 || pad < 0) return fail(OPFLOW_E_INVALID, "mesh needs >= 2 nodes");
-    const int es = start - pad, end = start + dims, ee = end + pad;
+    const int es = start - pad, end = start + dims;
     for (int i = start; i < end; ++i) x[i - es] = (max - min) / (double) (dims - 1) * (double) (i - start) + min;
     for (int j = start; j < end - 1; ++j) dx[j - es] = (max - min) / (double) (dims - 1);
+    ext_symm(dims, start, pad, x, dx);
+    return OPFLOW_OK;
+}
+
+/* set1DMesh(const MeshSetter& f, k) (CartesianMesh.hpp:279-290): pts[i - start] = f(i) for the dims
+ * nodes, dx(j) = x(j + 1) - x(j), then the same Symm extension. */
+int or_mesh_points(int dims, int start, int pad, const double* pts, double* x, double* dx) {
+    if (dims < 2 || pad < 0) return fail(OPFLOW_E_INVALID, "mesh needs >= 2 nodes");
+    const int es = start - pad, end = start + dims;
+    for (int i = start; i < end; ++i) x[i - es] = pts[i - start];
+    for (int j = start; j < end - 1; ++j) dx[j - es] = x[j + 1 - es] - x[j - es];
+    ext_symm(dims, start, pad, x, dx);
+    return OPFLOW_OK;
+}
+
+static void ext_symm(int dims, int start, int pad, double* x, double* dx) {
+    const int es = start - pad, end = start + dims, ee = end + pad;
     /* Symm extension of dx (the default MeshExtMode) */
     for (int i = es; i < start; ++i) dx[i - es] = dx[2 * start - 1 - i - es];
     for (int i = end - 1; i < ee - 1; ++i) dx[i - es] = dx[2 * end - 3 - i - es];
     /* integrate x into the ghost extension */
     for (int i = start - 1; i >= es; --i) x[i - es] = x[i + 1 - es] - dx[i - es];
     for (int i = end; i < ee; ++i) x[i - es] = x[i - 1 - es] + dx[i - 1 - es];
-    return OPFLOW_OK;
 }
 
 typedef struct {
@@ -336,9 +354,48 @@ static int compute_locs(Ctx* c) {
                 for (int d = 0; d < 3; ++d) L[d] = c->loc[nd->a][d];
                 L[nd->dim] = OPFLOW_CORNER;
                 break;
+            case OPFLOW_NODE_INTP_COR2CEN: /* D1Linear.hpp:60-69 */
+                for (int d = 0; d < 3; ++d) L[d] = c->loc[nd->a][d];
+                L[nd->dim] = OPFLOW_CENTER;
+                break;
+            case OPFLOW_NODE_D1_BIASED_UP: case OPFLOW_NODE_D1_BIASED_DOWN:
+                /* D1FirstOrderBiasedUpwind.hpp:68-84, D1FirstOrderBiasedDownwind.hpp:67-83: loc kept */
+                for (int d = 0; d < 3; ++d) L[d] = c->loc[nd->a][d];
+                break;
+            case OPFLOW_NODE_GT: case OPFLOW_NODE_GE: case OPFLOW_NODE_LT: case OPFLOW_NODE_LE: case OPFLOW_NODE_NE:
+            case OPFLOW_NODE_AND: case OPFLOW_NODE_OR: case OPFLOW_NODE_FUNC2: {
+                /* binary operators and functions: initPropsFrom(arg1), or arg2 when arg1 is a scalar */
+                if (nd->b < 0) return fail(OPFLOW_E_INVALID, "missing operand");
+                const int* La = c->loc[nd->a];
+                const int* Lb = c->loc[nd->b];
+                for (int d = 0; d < 3; ++d) L[d] = La[0] >= 0 ? La[d] : Lb[d];
+                break;
+            }
+            case OPFLOW_NODE_NOT: case OPFLOW_NODE_FUNC1:
+                for (int d = 0; d < 3; ++d) L[d] = c->loc[nd->a][d];
+                break;
+            case OPFLOW_NODE_COND: { /* CondOp::prepare: initPropsFrom(arg2), or arg3 (Conditional.hpp:41-115) */
+                if (nd->b < 0 || nd->c < 0 || nd->c >= k) return fail(OPFLOW_E_INVALID, "bad conditional operands");
+                const int* Lt = c->loc[nd->b];
+                const int* Lf = c->loc[nd->c];
+                for (int d = 0; d < 3; ++d) L[d] = Lt[0] >= 0 ? Lt[d] : (Lf[0] >= 0 ? Lf[d] : c->loc[nd->a][d]);
+                break;
+            }
+            case OPFLOW_NODE_INTP_FL_CEN2COR: case OPFLOW_NODE_INTP_FL_COR2CEN: {
+                /* D1FluxLimiterImpl::prepare (D1FluxLimiter.hpp:152-166, 182-201): the location of arg2 */
+                const int c2c = nd->kind == OPFLOW_NODE_INTP_FL_CEN2COR;
+                if (nd->b < 0) return fail(OPFLOW_E_INVALID, "missing operand");
+                if (nd->field < OPFLOW_FL_CDS || nd->field > OPFLOW_FL_BSOU) return fail(OPFLOW_E_INVALID, "unknown flux limiter");
+                if (nd->dim < 0 || nd->dim >= c->m->ndim) return fail(OPFLOW_E_INVALID, "bad operator dim");
+                if (c->loc[nd->b][nd->dim] != (c2c ? OPFLOW_CENTER : OPFLOW_CORNER)) return fail(OPFLOW_E_INVALID, "flux-limiter operand at the wrong location");
+                for (int d = 0; d < 3; ++d) L[d] = c->loc[nd->b][d];
+                L[nd->dim] = c2c ? OPFLOW_CORNER : OPFLOW_CENTER;
+                break;
+            }
             default: return fail(OPFLOW_E_UNSUPPORTED, "unknown node kind");
         }
-        if (nd->kind >= OPFLOW_NODE_D2 && (nd->dim < 0 || nd->dim >= c->m->ndim)) return fail(OPFLOW_E_INVALID, "bad operator dim");
+        if (nd->kind >= OPFLOW_NODE_D2 && nd->kind <= OPFLOW_NODE_D1_BIASED_DOWN && (nd->dim < 0 || nd->dim >= c->m->ndim))
+            return fail(OPFLOW_E_INVALID, "bad operator dim");
         if (nd->kind != OPFLOW_NODE_FIELD && nd->kind != OPFLOW_NODE_CONST && nd->a < 0) return fail(OPFLOW_E_INVALID, "missing operand");
         if (nd->kind >= OPFLOW_NODE_ADD && nd->kind <= OPFLOW_NODE_DIV && nd->b < 0) return fail(OPFLOW_E_INVALID, "missing operand");
     }
@@ -374,6 +431,153 @@ static double weno_kernel(double pm3, double pm2, double pm1, double p0, double 
     double w2 = a2 / (a1 + a2 + a3);
     double w3 = a3 / (a1 + a2 + a3);
     return w1 * ddx1 + w2 * ddx2 + w3 * ddx3;
+}
+
+/* std::max(a, b) = (a < b) ? b : a; std::min(a, b) = (b < a) ? b : a; the initializer-list forms
+ * (std::max_element / std::min_element) keep the first extreme element. */
+static double std_max(double a, double b) { return a < b ? b : a; }
+static double std_min(double a, double b) { return b < a ? b : a; }
+
+/* FluxLimiterKernels.hpp: MinmodKernel, SuperbeeKernel, MUSCLKernel, HarmonicKernel, vanAlbadaKernel,
+ * SPLMinKernel, SPLMaxKernel and GPLKappaKernel with the aliases' parameters.  `m`, `kappa` and
+ * `alpha` are computed as the reference does, `M::num / M::den` in integer arithmetic. */
+static double ratio_int(long num, long den) { return (double) (num / den); }
+static double spl_min(double m, double kappa, double r) {
+    const double v[4] = {m * r, 0.5 * (1 + kappa) * r + 0.5 * (1 - kappa), 0.5 * (1 - kappa) * r + 0.5 * (1 + kappa), m};
+    double cur = v[0];
+    for (int q = 1; q < 4; ++q) if (v[q] < cur) cur = v[q];
+    return std_max(0., cur);
+}
+static double spl_max(double m, double kappa, double r) {
+    double mx = 0.5 * (1 + kappa) * r + 0.5 * (1 - kappa);
+    const double l2 = 0.5 * (1 - kappa) * r + 0.5 * (1 + kappa);
+    if (mx < l2) mx = l2;
+    double cur = m * r;
+    if (mx < cur) cur = mx;
+    if (m < cur) cur = m;
+    return std_max(0., cur);
+}
+static double gpl(double m, double alpha, double kappa, double r) {
+    double cur = (2 + alpha) * r;
+    const double t = 0.5 * (1 + kappa) * r + 0.5 * (1 - kappa);
+    if (t < cur) cur = t;
+    if (m < cur) cur = m;
+    return std_max(0., cur);
+}
+static double limiter(int K, double r) {
+    switch (K) {
+        case OPFLOW_FL_MINMOD: return std_max(0., std_min(r, 1.));
+        case OPFLOW_FL_SUPERBEE: {
+            double m = 0., t = std_min(2. * r, 1.);
+            if (m < t) m = t;
+            t = std_min(r, 2.);
+            if (m < t) m = t;
+            return m;
+        }
+        case OPFLOW_FL_MUSCL: {
+            double m = 2 * r, t = (r + 1) / 2.;
+            if (t < m) m = t;
+            if (2. < m) m = 2.;
+            return std_max(0., m);
+        }
+        case OPFLOW_FL_HARMONIC: return (r + fabs(r)) / (r + 1);
+        case OPFLOW_FL_VANALBADA: return r * (r + 1) / (r * r + 1);
+        case OPFLOW_FL_UMIST: return spl_min(ratio_int(2, 1), ratio_int(1, 2), r);
+        case OPFLOW_FL_SPL13: return spl_min(ratio_int(2, 1), ratio_int(1, 3), r);
+        case OPFLOW_FL_SPLMAX12: return spl_max(ratio_int(2, 1), ratio_int(1, 2), r);
+        case OPFLOW_FL_SPLMAX13: return spl_max(ratio_int(2, 1), ratio_int(1, 3), r);
+        case OPFLOW_FL_KOREN: return gpl(ratio_int(2, 1), ratio_int(0, 1), ratio_int(1, 3), r);
+        case OPFLOW_FL_SMART: return gpl(ratio_int(4, 1), ratio_int(0, 1), ratio_int(1, 2), r);
+        default: return gpl(ratio_int(1, 1), ratio_int(0, 1), ratio_int(-1, 1), r); /* BSOU */
+    }
+}
+/* KappaKernel<s>::eval(slop_u, slop_f) (FluxLimiterKernels.hpp:31-44) */
+static double kappa_kernel(int K, double su, double sf) {
+    static const double kap[] = {1., 0.5, 1. / 3., 0., -1.};
+    const double kappa = kap[K];
+    return (1 + kappa) / 2. * sf + (1 - kappa) / 2. * su;
+}
+
+static double func1(int f, double x) {
+    switch (f) {
+        case OPFLOW_F_ABS: return fabs(x);
+        case OPFLOW_F_SQRT: return sqrt(x);
+        case OPFLOW_F_CEIL: return ceil(x);
+        case OPFLOW_F_FLOOR: return floor(x);
+        case OPFLOW_F_TRUNC: return trunc(x);
+        case OPFLOW_F_ROUND: return round(x);
+        case OPFLOW_F_RINT: return rint(x);
+        case OPFLOW_F_EXP: return exp(x);
+        case OPFLOW_F_EXP2: return exp2(x);
+        case OPFLOW_F_EXPM1: return expm1(x);
+        case OPFLOW_F_LOG: return log(x);
+        case OPFLOW_F_LOG10: return log10(x);
+        case OPFLOW_F_LOG2: return log2(x);
+        case OPFLOW_F_LOG1P: return log1p(x);
+        case OPFLOW_F_CBRT: return cbrt(x);
+        case OPFLOW_F_SIN: return sin(x);
+        case OPFLOW_F_COS: return cos(x);
+        case OPFLOW_F_TAN: return tan(x);
+        case OPFLOW_F_ASIN: return asin(x);
+        case OPFLOW_F_ACOS: return acos(x);
+        case OPFLOW_F_ATAN: return atan(x);
+        case OPFLOW_F_SINH: return sinh(x);
+        case OPFLOW_F_COSH: return cosh(x);
+        case OPFLOW_F_TANH: return tanh(x);
+        case OPFLOW_F_ASINH: return asinh(x);
+        case OPFLOW_F_ACOSH: return acosh(x);
+        case OPFLOW_F_ATANH: return atanh(x);
+        case OPFLOW_F_ERF: return erf(x);
+        case OPFLOW_F_ERFC: return erfc(x);
+        case OPFLOW_F_TGAMMA: return tgamma(x);
+        case OPFLOW_F_LGAMMA: return lgamma(x);
+    }
+    return NAN;
+}
+static double func2(int f, double a, double b) {
+    switch (f) {
+        case OPFLOW_F2_MAX: return std_max(a, b);
+        case OPFLOW_F2_MIN: return std_min(a, b);
+        case OPFLOW_F2_FDIM: return fdim(a, b);
+        case OPFLOW_F2_COPYSIGN: return copysign(a, b);
+        case OPFLOW_F2_FMOD: return fmod(a, b);
+        case OPFLOW_F2_REMAINDER: return remainder(a, b);
+        case OPFLOW_F2_POW: return pow(a, b);
+        case OPFLOW_F2_HYPOT: return hypot(a, b);
+        case OPFLOW_F2_ATAN2: return atan2(a, b);
+    }
+    return NAN;
+}
+
+static double ev(Ctx* c, int k, const int* i);
+
+/* D1FluxLimiterUpwindImpl / D1FluxLimiterDownwindImpl::eval (D1FluxLimiter.hpp:36-133) */
+static double flux_side(Ctx* c, const opflow_node* nd, const int* i, int up) {
+    const opflow_mesh_desc* m = c->m;
+    const int d = nd->dim, c2c = nd->kind == OPFLOW_NODE_INTP_FL_CEN2COR;
+    double x[3], y[3];
+    int p1, hoff;
+    if (c2c) { p1 = up ? -2 : -1; hoff = up ? -1 : 0; }
+    else { p1 = up ? -1 : 0; hoff = 0; }
+    for (int q = 0; q < 3; ++q) {
+        const int o = i[d] + p1 + q;
+        if (c2c) x[q] = up ? mesh_x(m, d, o) + 0.5 * mesh_dx(m, d, o) : mesh_x(m, d, o) + mesh_dx(m, d, o) * 0.5;
+        else x[q] = mesh_x(m, d, o);
+        int j[3] = {i[0], i[1], i[2]};
+        j[d] = o;
+        y[q] = ev(c, nd->b, j);
+    }
+    double su, sf;
+    if (up) { su = (y[1] - y[0]) / (x[1] - x[0]); sf = (y[2] - y[1]) / (x[2] - x[1]); }
+    else { su = (y[2] - y[1]) / (x[2] - x[1]); sf = (y[1] - y[0]) / (x[1] - x[0]); }
+    const double h = mesh_dx(m, d, i[d] + hoff);
+    double t;
+    if (nd->field <= OPFLOW_FL_LUI) t = h * 0.5 * kappa_kernel(nd->field, su, sf);
+    else {
+        const double r = sf / (su + 1e-16);
+        t = h * 0.5 * limiter(nd->field, r) * su;
+    }
+    return up ? y[1] + t : y[1] - t;
 }
 
 static double ev(Ctx* c, int k, const int* i) {
@@ -428,6 +632,41 @@ static double ev(Ctx* c, int k, const int* i) {
             double y1 = ev(c, nd->a, im), y2 = ev(c, nd->a, i);
             return intp_d(x1, y1, x2, y2, mesh_x(c->m, d, i[d]));
         }
+        case OPFLOW_NODE_INTP_COR2CEN: { /* D1Linear<Cor2Cen>::eval: Math::mid(e(i), e(i+1)) (D1Linear.hpp:43-45) */
+            int ip[3] = {i[0], i[1], i[2]};
+            ip[nd->dim]++;
+            return (ev(c, nd->a, i) + ev(c, nd->a, ip)) * 0.5;
+        }
+        case OPFLOW_NODE_D1_BIASED_UP: { /* D1FirstOrderBiasedUpwind::eval (D1FirstOrderBiasedUpwind.hpp:53-58) */
+            const int d = nd->dim;
+            int ip[3] = {i[0], i[1], i[2]};
+            ip[d]++;
+            const double h = c->loc[nd->a][d] == OPFLOW_CORNER ? mesh_dx(c->m, d, i[d])
+                                                                : (mesh_dx(c->m, d, i[d]) + mesh_dx(c->m, d, i[d] + 1)) * 0.5;
+            return (ev(c, nd->a, ip) - ev(c, nd->a, i)) / h;
+        }
+        case OPFLOW_NODE_D1_BIASED_DOWN: { /* D1FirstOrderBiasedDownwind::eval (D1FirstOrderBiasedDownwind.hpp:52-57) */
+            const int d = nd->dim;
+            int im[3] = {i[0], i[1], i[2]};
+            im[d]--;
+            const double h = c->loc[nd->a][d] == OPFLOW_CORNER ? mesh_dx(c->m, d, i[d] - 1)
+                                                                : (mesh_dx(c->m, d, i[d] - 1) + mesh_dx(c->m, d, i[d])) * 0.5;
+            return (ev(c, nd->a, i) - ev(c, nd->a, im)) / h;
+        }
+        case OPFLOW_NODE_GT: return ev(c, nd->a, i) > ev(c, nd->b, i) ? 1. : 0.;
+        case OPFLOW_NODE_GE: return ev(c, nd->a, i) >= ev(c, nd->b, i) ? 1. : 0.;
+        case OPFLOW_NODE_LT: return ev(c, nd->a, i) < ev(c, nd->b, i) ? 1. : 0.;
+        case OPFLOW_NODE_LE: return ev(c, nd->a, i) <= ev(c, nd->b, i) ? 1. : 0.;
+        case OPFLOW_NODE_NE: return ev(c, nd->a, i) != ev(c, nd->b, i) ? 1. : 0.;
+        case OPFLOW_NODE_AND: return (ev(c, nd->a, i) != 0. && ev(c, nd->b, i) != 0.) ? 1. : 0.;
+        case OPFLOW_NODE_OR: return (ev(c, nd->a, i) != 0. || ev(c, nd->b, i) != 0.) ? 1. : 0.;
+        case OPFLOW_NODE_NOT: return ev(c, nd->a, i) == 0. ? 1. : 0.;
+        case OPFLOW_NODE_COND: /* CondOp::eval (Conditional.hpp:35-40): only the taken branch */
+            return ev(c, nd->a, i) != 0. ? ev(c, nd->b, i) : ev(c, nd->c, i);
+        case OPFLOW_NODE_FUNC1: return func1(nd->field, ev(c, nd->a, i));
+        case OPFLOW_NODE_FUNC2: { double a = ev(c, nd->a, i); return func2(nd->field, a, ev(c, nd->b, i)); }
+        case OPFLOW_NODE_INTP_FL_CEN2COR: case OPFLOW_NODE_INTP_FL_COR2CEN: /* D1FluxLimiterImpl::eval */
+            return ev(c, nd->a, i) > 0. ? flux_side(c, nd, i, 1) : flux_side(c, nd, i, 0);
     }
     return NAN;
 }
@@ -730,6 +969,43 @@ static Val evp(Ctx* c, int k, const int* i) {
             Val y1 = evp(c, nd->a, im), y2 = evp(c, nd->a, i);
             double a = x1 - x, b = x2 - x;
             return v_div(v_sub(v_scal(y2, a), v_scal(y1, b)), vnum(a - b));
+        }
+        case OPFLOW_NODE_INTP_COR2CEN: {
+            int ip[3] = {i[0], i[1], i[2]};
+            ip[nd->dim]++;
+            Val a = evp(c, nd->a, i);
+            return v_mul(v_add(a, evp(c, nd->a, ip)), vnum(0.5));
+        }
+        case OPFLOW_NODE_D1_BIASED_UP: case OPFLOW_NODE_D1_BIASED_DOWN: {
+            const int d = nd->dim, up = nd->kind == OPFLOW_NODE_D1_BIASED_UP, o = up ? i[d] : i[d] - 1;
+            int j[3] = {i[0], i[1], i[2]};
+            j[d] += up ? 1 : -1;
+            const double h = c->loc[nd->a][d] == OPFLOW_CORNER ? mesh_dx(c->m, d, o) : (mesh_dx(c->m, d, o) + mesh_dx(c->m, d, o + 1)) * 0.5;
+            Val a = up ? evp(c, nd->a, j) : evp(c, nd->a, i);
+            Val b = up ? evp(c, nd->a, i) : evp(c, nd->a, j);
+            return v_div(v_sub(a, b), vnum(h));
+        }
+        case OPFLOW_NODE_GT: case OPFLOW_NODE_GE: case OPFLOW_NODE_LT: case OPFLOW_NODE_LE: case OPFLOW_NODE_NE:
+        case OPFLOW_NODE_AND: case OPFLOW_NODE_OR: case OPFLOW_NODE_NOT: case OPFLOW_NODE_COND:
+        case OPFLOW_NODE_FUNC1: case OPFLOW_NODE_FUNC2: {
+            /* scalar-valued operators: defined on numbers only (a StencilPad operand has no linear form) */
+            Val a = evp(c, nd->a, i);
+            Val b = nd->b >= 0 ? evp(c, nd->b, i) : vnum(0.);
+            Val t = nd->kind == OPFLOW_NODE_COND ? evp(c, nd->c, i) : vnum(0.);
+            if (a.is_pad || b.is_pad || t.is_pad) { g_pad_err = 2; return vnum(NAN); }
+            switch (nd->kind) {
+                case OPFLOW_NODE_GT: return vnum(a.v > b.v ? 1. : 0.);
+                case OPFLOW_NODE_GE: return vnum(a.v >= b.v ? 1. : 0.);
+                case OPFLOW_NODE_LT: return vnum(a.v < b.v ? 1. : 0.);
+                case OPFLOW_NODE_LE: return vnum(a.v <= b.v ? 1. : 0.);
+                case OPFLOW_NODE_NE: return vnum(a.v != b.v ? 1. : 0.);
+                case OPFLOW_NODE_AND: return vnum((a.v != 0. && b.v != 0.) ? 1. : 0.);
+                case OPFLOW_NODE_OR: return vnum((a.v != 0. || b.v != 0.) ? 1. : 0.);
+                case OPFLOW_NODE_NOT: return vnum(a.v == 0. ? 1. : 0.);
+                case OPFLOW_NODE_COND: return a.v != 0. ? b : t;
+                case OPFLOW_NODE_FUNC1: return vnum(func1(nd->field, a.v));
+                default: return vnum(func2(nd->field, a.v, b.v));
+            }
         }
         default:
             /* WENO and the other nonlinear operators have no StencilPad form */

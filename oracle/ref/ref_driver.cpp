@@ -170,6 +170,196 @@ static int run_weno(int nx, int ny, int steps, uint64_t seed, int upwind_kernel)
     return 0;
 }
 
+// One-sided first differences and corner-to-centre interpolation on a stretched 2D mesh.
+static double stretched(int i, int n) {
+    const double t = (double) i / (double) (n - 1);
+    return t + 0.25 * t * (1.0 - t);
+}
+static int run_ops(int nx, int ny, uint64_t seed) {
+    using Mesh = CartesianMesh<Meta::int_<2>>;
+    using Field = CartesianField<Real, Mesh>;
+    auto mesh = MeshBuilder<Mesh>()
+                        .newMesh(nx + 1, ny + 1)
+                        .setMeshOfDim(0, [&](int i) { return stretched(i, nx + 1); })
+                        .setMeshOfDim(1, [&](int i) { return stretched(i, ny + 1) * 2.0; })
+                        .build();
+    // the mesh itself (extended range), so that the restated MeshBuilder is pinned too
+    for (int d = 0; d < 2; ++d) {
+        auto er = mesh.getExtRange();
+        std::vector<double> xs, dxs;
+        for (int i = er.start[d]; i < er.end[d]; ++i) xs.push_back(mesh.x(d, i));
+        for (int i = er.start[d]; i < er.end[d] - 1; ++i) dxs.push_back(mesh.dx(d, i));
+        fprintf(g_out, "FIELD {\"name\":\"mesh_x%d\",\"count\":%zu}\n", d, xs.size());
+        put(xs);
+        fprintf(g_out, "FIELD {\"name\":\"mesh_dx%d\",\"count\":%zu}\n", d, dxs.size());
+        put(dxs);
+    }
+    // c: cell-centred, Dirc 0.5 / Neum -1 along x, periodic along y
+    auto c = ExprBuilder<Field>()
+                     .setName("c")
+                     .setMesh(mesh)
+                     .setLoc(LocOnMesh::Center)
+                     .setBC(0, DimPos::start, BCType::Dirc, 0.5)
+                     .setBC(0, DimPos::end, BCType::Neum, -1.0)
+                     .setBC(1, DimPos::start, BCType::Periodic)
+                     .setBC(1, DimPos::end, BCType::Periodic)
+                     .setExt(1)
+                     .build();
+    rangeFor_s(c.assignableRange, [&](auto&& i) { c[i] = u01(seed, (uint64_t) i[1] * nx + i[0]); });
+    c.updatePadding();
+    // v: nodal, Dirc 0.25 / Dirc -0.75 along x, Neum 0 / Dirc 1 along y
+    auto v = ExprBuilder<Field>()
+                     .setName("v")
+                     .setMesh(mesh)
+                     .setLoc(LocOnMesh::Corner)
+                     .setBC(0, DimPos::start, BCType::Dirc, 0.25)
+                     .setBC(0, DimPos::end, BCType::Dirc, -0.75)
+                     .setBC(1, DimPos::start, BCType::Neum, 0.)
+                     .setBC(1, DimPos::end, BCType::Dirc, 1.0)
+                     .setExt(1)
+                     .build();
+    rangeFor_s(v.assignableRange, [&](auto&& i) { v[i] = u01(seed + 1, (uint64_t) i[1] * (nx + 1) + i[0]); });
+    v.updatePadding();
+    dump_field(c, "c");
+    dump_field(v, "v");
+    auto c_up0 = c, c_dn1 = c, c_mix = c;
+    c_up0 = d1<D1FirstOrderBiasedUpwind<0>>(c);
+    c_dn1 = d1<D1FirstOrderBiasedDownwind<1>>(c);
+    c_mix = c + 0.25 * d1IntpCornerToCenter<1>(d1IntpCornerToCenter<0>(v)) - 0.3 * dx<D1FirstOrderBiasedDownwind>(c);
+    dump_field(c_up0, "c_up0");
+    dump_field(c_dn1, "c_dn1");
+    dump_field(c_mix, "c_mix");
+    auto v_up1 = v, v_dn0 = v;
+    v_up1 = dy<D1FirstOrderBiasedUpwind>(v);
+    v_dn0 = dx<D1FirstOrderBiasedDownwind>(v);
+    dump_field(v_up1, "v_up1");
+    dump_field(v_dn0, "v_dn0");
+    // corner -> centre along one dim: destinations with the mixed locations
+    auto w0 = ExprBuilder<Field>()
+                      .setName("w0")
+                      .setMesh(mesh)
+                      .setLoc({LocOnMesh::Center, LocOnMesh::Corner})
+                      .setBC(0, DimPos::start, BCType::Dirc, 0.)
+                      .setBC(0, DimPos::end, BCType::Dirc, 0.)
+                      .setBC(1, DimPos::start, BCType::Neum, 0.)
+                      .setBC(1, DimPos::end, BCType::Dirc, 0.)
+                      .build();
+    auto w1 = ExprBuilder<Field>()
+                      .setName("w1")
+                      .setMesh(mesh)
+                      .setLoc({LocOnMesh::Corner, LocOnMesh::Center})
+                      .setBC(0, DimPos::start, BCType::Dirc, 0.)
+                      .setBC(0, DimPos::end, BCType::Dirc, 0.)
+                      .setBC(1, DimPos::start, BCType::Neum, 0.)
+                      .setBC(1, DimPos::end, BCType::Dirc, 0.)
+                      .build();
+    w0 = d1IntpCornerToCenter<0>(v);
+    w1 = d1IntpCornerToCenter<1>(v);
+    dump_field(w0, "w0");
+    dump_field(w1, "w1");
+    return 0;
+}
+
+// Comparisons, logic, conditionals, per-element functions and flux-limiter interpolation on the
+// stretched mesh of run_ops.
+template <typename K>
+using FL = typename D1FluxLimiterGen<K>::template Op<0, IntpDirection::Cen2Cor>;
+static int run_logic(int nx, int ny, uint64_t seed) {
+    using Mesh = CartesianMesh<Meta::int_<2>>;
+    using Field = CartesianField<Real, Mesh>;
+    auto mesh = MeshBuilder<Mesh>()
+                        .newMesh(nx + 1, ny + 1)
+                        .setMeshOfDim(0, [&](int i) { return stretched(i, nx + 1); })
+                        .setMeshOfDim(1, [&](int i) { return stretched(i, ny + 1) * 2.0; })
+                        .build();
+    // the x faces / nodes of the flux-limiter targets are Dirichlet at both ends, so that no target
+    // point needs a value beyond the operand's one-cell padding
+    auto mk = [&](const char* name, LocOnMesh l0, LocOnMesh l1, bool periodic_y) {
+        auto b = ExprBuilder<Field>().setName(name).setMesh(mesh).setLoc({l0, l1}).setExt(1);
+        b.setBC(0, DimPos::start, BCType::Dirc, 0.5);
+        if (l0 == LocOnMesh::Corner && l1 == LocOnMesh::Center) b.setBC(0, DimPos::end, BCType::Dirc, -1.0);
+        else b.setBC(0, DimPos::end, BCType::Neum, -1.0);
+        if (periodic_y) b.setBC(1, DimPos::start, BCType::Periodic).setBC(1, DimPos::end, BCType::Periodic);
+        else b.setBC(1, DimPos::start, BCType::Neum, 0.).setBC(1, DimPos::end, BCType::Dirc, 1.0);
+        return b.build();
+    };
+    auto fill = [&](auto& f, uint64_t s, double shift) {
+        auto r = f.assignableRange;
+        rangeFor_s(r, [&](auto&& i) { f[i] = u01(s, (uint64_t) i[1] * 1000 + i[0]) - shift; });
+        f.updatePadding();
+    };
+    const auto Cn = LocOnMesh::Center, Co = LocOnMesh::Corner;
+    auto c = mk("c", Cn, Cn, true), g = mk("g", Cn, Cn, true);
+    auto v = mk("v", Co, Co, false);
+    auto ux = mk("ux", Co, Cn, true);  // velocity on the x faces of the cells
+    auto uy = mk("uy", Co, Cn, false); // velocity at the y-cell centres of the x nodes
+    fill(c, seed, 0.0);
+    fill(g, seed + 1, 0.5);
+    fill(v, seed + 2, 0.25);
+    fill(ux, seed + 3, 0.5);
+    fill(uy, seed + 4, 0.5);
+    for (auto* f : {&c, &g, &v, &ux, &uy}) dump_field(*f, f->getName().c_str());
+    auto out_c = c;
+    out_c = conditional(g > 0., dx<D1FirstOrderBiasedDownwind>(c), dx<D1FirstOrderBiasedUpwind>(c));
+    dump_field(out_c, "cond");
+    out_c = (g > 0.25 && c < 0.5) || !(g >= -0.1);
+    dump_field(out_c, "logic");
+    out_c = conditional(g != c, max(c, g) - min(g, c), abs(g)) + sqrt(c) * floor(g * 4.) - ceil(c * 3.)
+            + round(g * 7.) + trunc(c * 5.) + fdim(c, g) + copysign(c, g) + fmod(c * 7., g + 1.);
+    dump_field(out_c, "exactfn");
+    out_c = exp(c) * sin(g) + log(g + 1.5) - pow(c, g + 1.) + tanh(g) + atan2(g, c) + hypot(c, g) + erf(g)
+            + cbrt(g) + log1p(c) + expm1(g) + cos(c) + sqrt(c * c + g * g);
+    dump_field(out_c, "transfn");
+    // flux-limiter interpolation: centres -> x faces (c, upwinded by ux) and nodes -> y centres
+    // (v, upwinded by uy), one dump per limiter kernel
+    auto fx = ux, fy = uy;
+    auto both = [&](auto kern, const char* name) {
+        using K = decltype(kern);
+        fx = d1Intp<0, IntpDirection::Cen2Cor, D1FluxLimiterGen<K>::template Op>(ux, c);
+        fy = d1Intp<1, IntpDirection::Cor2Cen, D1FluxLimiterGen<K>::template Op>(uy, v);
+        dump_field(fx, (std::string("fx_") + name).c_str());
+        dump_field(fy, (std::string("fy_") + name).c_str());
+    };
+    both(KappaKernel<KappaScheme::CDS> {}, "CDS");
+    both(KappaKernel<KappaScheme::QUICK> {}, "QUICK");
+    both(KappaKernel<KappaScheme::CUI> {}, "CUI");
+    both(KappaKernel<KappaScheme::Fromm> {}, "Fromm");
+    both(KappaKernel<KappaScheme::LUI> {}, "LUI");
+    both(MinmodKernel {}, "Minmod");
+    both(SuperbeeKernel {}, "Superbee");
+    both(MUSCLKernel {}, "MUSCL");
+    both(HarmonicKernel {}, "Harmonic");
+    both(vanAlbadaKernel {}, "vanAlbada");
+    both(UMISTKernel {}, "UMIST");
+    both(SPL13Kernel {}, "SPL13");
+    both(SPLMax12Kernel {}, "SPLMax12");
+    both(SPLMax13Kernel {}, "SPLMax13");
+    both(KorenLimitedCUIKernel {}, "Koren");
+    both(SMARTKernel {}, "SMART");
+    both(BSOUKernel {}, "BSOU");
+    return 0;
+}
+
+// examples/CONV1D: first-order upwind convection of a square pulse, u = u - dt*c*dx<Downwind>(u).
+static int run_conv1d(int n, int steps) {
+    using Mesh = CartesianMesh<Meta::int_<1>>;
+    using Field = CartesianField<Real, Mesh>;
+    auto mesh = MeshBuilder<Mesh>().newMesh(n).setMeshOfDim(0, 0., 1.).build();
+    auto u = ExprBuilder<Field>()
+                     .setMesh(mesh)
+                     .setName("u")
+                     .setBC(0, DimPos::start, BCType::Dirc, 0.)
+                     .setBC(0, DimPos::end, BCType::Dirc, 0.)
+                     .setLoc(LocOnMesh::Corner)
+                     .build();
+    u.initBy([](auto&& x) { return 0.2 <= x[0] && x[0] <= 0.4 ? 1.0 : 0.0; });
+    dump_field(u, "u0");
+    const Real dt = 0.5e-2, cc = 1.0;
+    for (int s = 0; s < steps; ++s) u = u - dt * cc * dx<D1FirstOrderBiasedDownwind>(u);
+    dump_field(u, "u");
+    return 0;
+}
+
 // Field construction + padding rules: one field per (loc, bc) combination, initialised by a smooth
 // function of the coordinates, dumped over its readable range.
 static int run_padding(int nx, int ny, int loc_i, int bc_lo, int bc_hi, int ext) {
@@ -322,6 +512,90 @@ static int run_assemble(const std::string& which, int n) {
                       false);
         return 0;
     }
+    if (which == "biased2d") {
+        // flux form from one-sided differences on a stretched mesh, Dirichlet cells:
+        // f == d1<Down<0>>(K * d1<Up<0>>(e)) + d1<Down<1>>(d1<Up<1>>(e)) - 0.5 * e
+        auto m = MeshBuilder<Mesh2>()
+                         .newMesh(n + 1, n + 1)
+                         .setMeshOfDim(0, [&](int i) { return stretched(i, n + 1); })
+                         .setMeshOfDim(1, [&](int i) { return stretched(i, n + 1) * 2.0; })
+                         .build();
+        auto mk = [&](double bcv) {
+            return ExprBuilder<Field2>()
+                    .setMesh(m)
+                    .setName("p")
+                    .setBC(0, DimPos::start, BCType::Dirc, bcv)
+                    .setBC(0, DimPos::end, BCType::Dirc, bcv)
+                    .setBC(1, DimPos::start, BCType::Dirc, bcv)
+                    .setBC(1, DimPos::end, BCType::Dirc, bcv)
+                    .setExt(1)
+                    .setLoc({LocOnMesh::Center, LocOnMesh::Center})
+                    .build();
+        };
+        auto p = mk(0.25);
+        auto K = mk(1.0);
+        auto f = mk(0.);
+        rangeFor_s(K.assignableRange, [&](auto&& i) { K[i] = 1.0 + u01(17, (uint64_t) i[1] * n + i[0]); });
+        K.updatePadding();
+        rangeFor_s(f.assignableRange, [&](auto&& i) { f[i] = u01(19, (uint64_t) i[1] * n + i[0]) - 0.5; });
+        f.updatePadding();
+        dump_field(K, "K");
+        dump_field(f, "f");
+        assemble_dump(p,
+                      [&](auto&& e) {
+                          return f
+                                 == d1<D1FirstOrderBiasedDownwind<0>>(K * d1<D1FirstOrderBiasedUpwind<0>>(e))
+                                            + d1<D1FirstOrderBiasedDownwind<1>>(d1<D1FirstOrderBiasedUpwind<1>>(e))
+                                            - 0.5 * e;
+                      },
+                      false);
+        return 0;
+    }
+    if (which == "funcs2d") {
+        // coefficients built from comparisons, conditionals and per-element functions of known fields:
+        // f == dx(max(intp0(K), 1.25) * dx(e)) + dy(conditional(intp1(K) > 1.5, sqrt(intp1(K)), intp1(K)) * dy(e))
+        //      - (abs(g) + 0.5) * e
+        auto m = MeshBuilder<Mesh2>().newMesh(n + 1, n + 1).setMeshOfDim(0, 0., 1.).setMeshOfDim(1, 0., 1.).build();
+        auto mk = [&](double bcv) {
+            return ExprBuilder<Field2>()
+                    .setMesh(m)
+                    .setName("p")
+                    .setBC(0, DimPos::start, BCType::Dirc, bcv)
+                    .setBC(0, DimPos::end, BCType::Dirc, bcv)
+                    .setBC(1, DimPos::start, BCType::Neum, 0.)
+                    .setBC(1, DimPos::end, BCType::Neum, 0.)
+                    .setExt(1)
+                    .setLoc({LocOnMesh::Center, LocOnMesh::Center})
+                    .build();
+        };
+        auto p = mk(0.5);
+        auto K = mk(1.0);
+        auto g = mk(0.);
+        auto f = mk(0.);
+        rangeFor_s(K.assignableRange, [&](auto&& i) { K[i] = 1.0 + u01(23, (uint64_t) i[1] * n + i[0]); });
+        K.updatePadding();
+        rangeFor_s(g.assignableRange, [&](auto&& i) { g[i] = u01(29, (uint64_t) i[1] * n + i[0]) - 0.5; });
+        g.updatePadding();
+        rangeFor_s(f.assignableRange, [&](auto&& i) { f[i] = u01(31, (uint64_t) i[1] * n + i[0]) - 0.5; });
+        f.updatePadding();
+        dump_field(K, "K");
+        dump_field(g, "g");
+        dump_field(f, "f");
+        assemble_dump(p,
+                      [&](auto&& e) {
+                          return f
+                                 == dx<D1FirstOrderCentered>(max(d1IntpCenterToCorner<0>(K), 1.25)
+                                                             * dx<D1FirstOrderCentered>(e))
+                                            + dy<D1FirstOrderCentered>(
+                                                    conditional(d1IntpCenterToCorner<1>(K) > 1.5,
+                                                                sqrt(d1IntpCenterToCorner<1>(K)),
+                                                                d1IntpCenterToCorner<1>(K))
+                                                    * dy<D1FirstOrderCentered>(e))
+                                            - (abs(g) + 0.5) * e;
+                      },
+                      false);
+        return 0;
+    }
     if (which == "helm_corner") {
         // (I - k Lap) u = f on a node grid with Dirichlet nodes: e - k*(d2x(e)+d2y(e)) == f
         auto m = MeshBuilder<Mesh2>().newMesh(n, n).setMeshOfDim(0, 0., 1.).setMeshOfDim(1, 0., 1.).build();
@@ -385,6 +659,9 @@ int main(int argc, char** argv) {
     else if (cmd == "ftcs3d") rc = run_ftcs3d(I(3), I(4), std::strtoull(argv[5], nullptr, 10), D(6));
     else if (cmd == "weno") rc = run_weno(I(3), I(4), I(5), std::strtoull(argv[6], nullptr, 10), I(7));
     else if (cmd == "padding") rc = run_padding(I(3), I(4), I(5), I(6), I(7), I(8));
+    else if (cmd == "ops") rc = run_ops(I(3), I(4), std::strtoull(argv[5], nullptr, 10));
+    else if (cmd == "conv1d") rc = run_conv1d(I(3), I(4));
+    else if (cmd == "logic") rc = run_logic(I(3), I(4), std::strtoull(argv[5], nullptr, 10));
     else if (cmd == "assemble") rc = run_assemble(argv[3], argc > 4 ? I(4) : 0);
     fclose(g_out);
     return rc;

@@ -38,6 +38,30 @@ def mesh_uniform(dims, ranges=None, pad=5):
     return api.CartesianMesh(len(dims), dims, [0] * len(dims), pad, xs, dxs)
 
 
+def mesh_points(points, pad=5):
+    """CartesianMesh from per-dim node positions (MeshBuilder::setMeshOfDim(k, f) restated by the oracle)."""
+    xs, dxs = [], []
+    for p in points:
+        p = np.ascontiguousarray(p, dtype=np.float64)
+        n = len(p)
+        x = np.zeros(n + 2 * pad)
+        dx = np.zeros(n + 2 * pad - 1)
+        orc.lib().or_mesh_points(n, 0, pad, orc.dptr(p), orc.dptr(x), orc.dptr(dx))
+        xs.append(x)
+        dxs.append(dx)
+    return api.CartesianMesh(len(points), [len(p) for p in points], [0] * len(points), pad, xs, dxs)
+
+
+def stretched_points(n, scale=1.0):
+    """Node positions t + 0.25*t*(1 - t), t = i/(n - 1), times scale: the nonuniform mesh of the
+    reference driver's operator cases, evaluated in the same IEEE operation order."""
+    out = np.empty(n)
+    for i in range(n):
+        t = float(i) / float(n - 1)
+        out[i] = (t + 0.25 * t * (1.0 - t)) * scale
+    return out
+
+
 def field_desc(ndim, loc, bcs, values=None, ext=0, padding=0):
     """bcs: list per dim of (lo, hi) BC types; values likewise (default 0)."""
     fd = capi.FieldDesc()

@@ -5,7 +5,7 @@ sources) on small cases and stores every dump as a .npz next to this script.  Ne
 (present only where the fixtures are generated); the fixtures themselves are committed so the tests
 run anywhere.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case ...]     (all cases when none is named)
 """
 import json
 import os
@@ -42,6 +42,16 @@ CASES = {
     "asm_var2d_n16": ["assemble", "var2d", "16"],
     "asm_helm_corner_n9": ["assemble", "helm_corner", "9"],
     "asm_var3d_n6": ["assemble", "var3d", "6"],
+    "asm_biased2d_n12": ["assemble", "biased2d", "12"],
+    "asm_funcs2d_n10": ["assemble", "funcs2d", "10"],
+    # one-sided differences and corner-to-centre interpolation on a stretched mesh: nx, ny, seed
+    "ops_12x9": ["ops", "12", "9", "21"],
+    "ops_16x20": ["ops", "16", "20", "22"],
+    # comparisons, logic, conditionals, per-element functions, flux-limiter interpolation: nx, ny, seed
+    "logic_12x9": ["logic", "12", "9", "31"],
+    "logic_16x20": ["logic", "16", "20", "32"],
+    # examples/CONV1D: nodes, steps
+    "conv1d_n101": ["conv1d", "101", "100"],
 }
 # field construction + padding: nx, ny, loc (0 corner / 1 centre), bc_lo, bc_hi, ext
 # bc codes: 0 Dirc, 1 Neum, 2 Periodic, 3 Symm, 4 ASymm
@@ -77,7 +87,10 @@ def parse(path):
 def main():
     if not os.path.exists(DRIVER):
         subprocess.check_call([os.path.join(ROOT, "oracle", "build_ref.sh")])
+    wanted = set(sys.argv[1:]) or set(CASES)
     for name, args in sorted(CASES.items()):
+        if name not in wanted:
+            continue
         with tempfile.TemporaryDirectory() as td:
             out = os.path.join(td, "o.bin")
             subprocess.check_call([DRIVER, out] + args)

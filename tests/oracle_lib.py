@@ -25,6 +25,7 @@ def lib():
         L = C.CDLL(SO)
         P = C.POINTER
         L.or_mesh_uniform.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, P(C.c_double), P(C.c_double)]
+        L.or_mesh_points.argtypes = [C.c_int, C.c_int, C.c_int, P(C.c_double), P(C.c_double), P(C.c_double)]
         L.or_field_info.argtypes = [P(capi.MeshDesc), P(capi.FieldDesc), P(capi.FieldInfo)]
         L.or_update_padding.argtypes = [P(capi.MeshDesc), P(capi.FieldDesc), P(C.c_double)]
         L.or_assign.argtypes = [P(capi.MeshDesc), P(capi.FieldDesc), P(P(C.c_double)), C.c_int, C.c_int, C.c_int,

@@ -17,7 +17,7 @@ def test_library_exports_every_declared_symbol():
     assert len(syms) >= 30
     missing = [s for s in syms if not hasattr(L, s)]
     assert not missing, missing
-    assert L.opflow_abi_version() == 1
+    assert L.opflow_abi_version() == 2
 
 
 @pytest.mark.parametrize("n,lo,hi,pad", [(1025, 0.0, 1.0, 5), (512, 0.0, 1.0, 5), (20, -1.0, 3.0, 3), (2049, 0.0, 1.0, 5)])
@@ -69,3 +69,13 @@ def test_serialize_keeps_operand_order_and_shares_leaves():
     sub = [nodes[i] for i in range(len(nodes)) if nodes[i].kind == capi.NODE_SUB][0]
     assert nodes[sub.a].kind == capi.NODE_CONST and nodes[sub.a].value == 2.0
     assert nodes[sub.b].kind == capi.NODE_DIV
+
+
+def test_expression_functions_do_not_shadow_builtins():
+    """api.max / api.abs / ... are expression builders, reachable as module attributes, while the
+    module's own code keeps Python's builtins of the same names."""
+    from opflow_gb300 import api
+    for name in ("max", "min", "abs", "round", "pow"):
+        assert name not in vars(api)
+        assert callable(getattr(api, name))
+    assert isinstance(api.max(api.ScalarExpr(1.0), 2.0), api.ExprNode)

@@ -25,7 +25,7 @@ def build_example(name, outdir):
     return exe
 
 
-@pytest.mark.parametrize("name", ["ftcs2d", "poisson"])
+@pytest.mark.parametrize("name", ["ftcs2d", "poisson", "conv1d"])
 def test_examples_compile_and_link(tmp_path, name):
     build_example(name, str(tmp_path))
 
@@ -59,3 +59,48 @@ def test_poisson_program_recovers_manufactured_solution(ctx, tmp_path, prec):
     r = subprocess.run([exe, "64", prec], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "converged 1" in r.stdout
+
+
+def _conv1d_oracle(n, steps, scheme):
+    """The conv1d program's fields and updates, run by the oracle."""
+    mesh = cm.mesh_uniform([n])
+    fu = cm.field_desc(1, capi.CORNER, [(capi.BC_DIRC, capi.BC_DIRC)], ext=2)
+    fc = cm.field_desc(1, capi.CENTER, [(capi.BC_NEUM, capi.BC_NEUM)], ext=1)
+    u, c = orc.HostField(mesh, fu), orc.HostField(mesh, fc)
+    rng = u.assignable()
+    x = np.array([mesh.x_at(0, i) for i in range(*rng[0])])
+    u.data[u.slices(rng)] = np.where((0.2 <= x) & (x <= 0.4), 1.0, 0.0)
+    u.update_padding()
+    c.data[c.slices(c.assignable())] = 1.0
+    c.update_padding()
+    U, Cf = cm.Leaf("u"), cm.Leaf("c")
+    dt, cv = 0.5e-2, 1.0
+    if scheme == "upwind":
+        e = U - dt * cv * api.dx(U, api.D1FirstOrderBiasedDownwind)
+    elif scheme == "cond":
+        e = U - dt * cv * api.conditional(1.0, api.dx(U, api.D1FirstOrderBiasedDownwind), api.dx(U, api.D1FirstOrderBiasedUpwind))
+    else:
+        e = U - dt * api.dx(Cf * api.d1_flux_limiter_intp(Cf, U, 0, "Minmod", to_corner=False))
+    nodes, _ = api.serialize(e, [U, Cf])
+    for _ in range(steps):
+        orc.assign(u, nodes, [u, c])
+    return u
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("scheme", ["upwind", "cond", "minmod"])
+def test_conv1d_program_matches_oracle_and_reference(ctx, tmp_path, scheme):
+    """examples/CONV1D through the C++ front end: bit-identical to the oracle; the upwind scheme also to
+    the reference's own run of the example (fixture conv1d_n101)."""
+    n, steps = 101, 100
+    exe = build_example("conv1d", str(tmp_path))
+    out = str(tmp_path / "u.bin")
+    r = subprocess.run([exe, str(n), str(steps), scheme, out], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    h = _conv1d_oracle(n, steps, scheme)
+    got = np.fromfile(out, dtype=np.float64)
+    assert got.size == h.data.size
+    assert np.array_equal(got.reshape(h.data.shape), h.data)
+    if scheme != "minmod":
+        _, arr = cm.golden("conv1d_n101")
+        assert np.array_equal(h.data[h.slices([(0, n)])], arr["u__data"])

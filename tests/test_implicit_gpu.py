@@ -210,6 +210,19 @@ def test_nonlinear_equation_is_rejected(ctx):
     assert e.value.code == capi.E_UNSUPPORTED
 
 
+def test_logic_of_the_unknown_has_no_stencil_form(ctx):
+    """Comparisons, conditionals and functions assemble only on values that do not depend on the
+    unknown, and flux-limiter interpolation not at all: anything else is refused with E_UNSUPPORTED
+    instead of being mis-assembled."""
+    mesh, fd, p, f = poisson_case(ctx, 16, capi.BC_DIRC)
+    for eq in (lambda e: f == api.d2x(e) + api.conditional(f > 0., e, 2. * e),
+               lambda e: f == api.d2x(e) + api.abs(e),
+               lambda e: f == api.d2x(e) + api.d1_flux_limiter_intp(f, e, 0, "QUICK")):
+        with pytest.raises(capi.OpflowError) as err:
+            api.Solve(eq, p)
+        assert err.value.code == capi.E_UNSUPPORTED
+
+
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
 def test_iteration_cap_and_repeated_solves(ctx, prec):
     """The device-side solve loop stops at maxIter without converging, reports exactly maxIter

@@ -178,6 +178,33 @@ def _assemble_case(name, arr, meta):
         rhs = (api.dx(api.d1IntpCenterToCorner(KK, 0) * api.dx(e)) + api.dy(api.d1IntpCenterToCorner(KK, 1) * api.dy(e))
                + api.dz(api.d1IntpCenterToCorner(KK, 2) * api.dz(e)))
         return p, {"p": p, "K": K, "f": f}, api.Eq(F, rhs), True
+    if which == "biased2d":
+        mesh = cm.mesh_points([cm.stretched_points(n + 1), cm.stretched_points(n + 1, 2.0)])
+        mk = lambda v: cm.field_desc(2, capi.CENTER, [(capi.BC_DIRC, capi.BC_DIRC)] * 2, [(v, v)] * 2, ext=1)
+        p = orc.HostField(mesh, mk(0.25))
+        K = orc.HostField(mesh, mk(1.0))
+        f = orc.HostField(mesh, mk(0.0))
+        for h, key in ((K, "K"), (f, "f")):
+            h.data[h.slices(cm.readable(h.info))] = arr[key + "__data"].reshape(h.data[h.slices(cm.readable(h.info))].shape)
+        e, KK, F = cm.Leaf("p"), cm.Leaf("K"), cm.Leaf("f")
+        rhs = (api.d1_biased_downwind(KK * api.d1_biased_upwind(e, 0), 0)
+               + api.d1_biased_downwind(api.d1_biased_upwind(e, 1), 1) - 0.5 * e)
+        return p, {"p": p, "K": K, "f": f}, api.Eq(F, rhs), False
+    if which == "funcs2d":
+        mesh = cm.mesh_uniform([n + 1, n + 1])
+        mk = lambda v: cm.field_desc(2, capi.CENTER, [(capi.BC_DIRC, capi.BC_DIRC), (capi.BC_NEUM, capi.BC_NEUM)],
+                                     [(v, v), (0.0, 0.0)], ext=1)
+        p = orc.HostField(mesh, mk(0.5))
+        fields = {"p": p}
+        for key, v in (("K", 1.0), ("g", 0.0), ("f", 0.0)):
+            h = orc.HostField(mesh, mk(v))
+            h.data[h.slices(cm.readable(h.info))] = arr[key + "__data"].reshape(h.data[h.slices(cm.readable(h.info))].shape)
+            fields[key] = h
+        e, KK, G, F = cm.Leaf("p"), cm.Leaf("K"), cm.Leaf("g"), cm.Leaf("f")
+        k0, k1 = api.d1IntpCenterToCorner(KK, 0), api.d1IntpCenterToCorner(KK, 1)
+        rhs = (api.dx(api.max(k0, 1.25) * api.dx(e)) + api.dy(api.conditional(k1 > 1.5, api.sqrt(k1), k1) * api.dy(e))
+               - (api.abs(G) + 0.5) * e)
+        return p, fields, api.Eq(F, rhs), False
     raise KeyError(which)
 
 
