@@ -733,7 +733,9 @@ struct StructSolverParams {
     std::string dumpPath;
     int printLevel = 0, logging = 0;
     int rapType = 0, relaxType = 1, numPreRelax = 1, numPostRelax = 1, skipRelax = 0;
-    bool gpuMixedPrecision = false;  // FP32 V-cycle inside the FP64 flexible-PCG outer iteration
+    int kDim = 5;                    // GMRES restart length (StructSolverGMRES.hpp:20-23)
+    Real absTol = 0.;
+    bool gpuMixedPrecision = false;  // FP32 V-cycle inside the FP64 flexible outer iteration
 };
 
 template <StructSolverType Solver, StructSolverType Precond = StructSolverType::None>
@@ -807,6 +809,25 @@ namespace GPU {
         o.pin_value = p.pinValue ? 1 : 0;
         o.zero_guess = p.useZeroGuess ? 1 : 0;
         o.precision = (p.gpuMixedPrecision || pp.gpuMixedPrecision) ? OPFLOW_PREC_MIXED : OPFLOW_PREC_FP64;
+        o.kdim = p.kDim;
+        o.abs_tol = p.absTol;
+        // PrecondStructSolver<T, P>: T the outer iteration, P its preconditioner; a preconditioner type
+        // as T without P (StructSolver<PFMG> etc.) iterates it alone
+        auto pre = [](StructSolverType t) {
+            switch (t) {
+                case StructSolverType::PFMG: case StructSolverType::SMG: case StructSolverType::CYCRED: return (int) OPFLOW_PRECOND_MG;
+                case StructSolverType::Jacobi: return (int) OPFLOW_PRECOND_JACOBI;
+                default: return (int) OPFLOW_PRECOND_NONE;
+            }
+        };
+        switch (T) {
+            case StructSolverType::PCG: o.krylov = OPFLOW_KRYLOV_PCG; o.precond = pre(P); break;
+            case StructSolverType::GMRES: o.krylov = OPFLOW_KRYLOV_GMRES; o.precond = pre(P); break;
+            case StructSolverType::FlexGMRES: o.krylov = OPFLOW_KRYLOV_FGMRES; o.precond = pre(P); break;
+            case StructSolverType::LGMRES: o.krylov = OPFLOW_KRYLOV_LGMRES; o.precond = pre(P); break;
+            case StructSolverType::BICGSTAB: o.krylov = OPFLOW_KRYLOV_BICGSTAB; o.precond = pre(P); break;
+            default: o.krylov = OPFLOW_KRYLOV_NONE; o.precond = pre(T); break;
+        }
         return o;
     }
 }// namespace GPU

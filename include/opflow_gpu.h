@@ -268,6 +268,22 @@ int opflow_assemble(opflow_ctx ctx, opflow_field target, const opflow_node* node
 /* Solver parameters: StructSolverParamsBase (src/Core/Solvers/Struct/StructSolver.hpp:39-51) plus the
  * PFMG preconditioner knobs (StructSolverPFMG.hpp:23-33) and the GPU extensions. */
 enum opflow_precision { OPFLOW_PREC_FP64 = 0, OPFLOW_PREC_MIXED = 1 };
+/* Outer iterations (src/Core/Solvers/Struct/StructSolver.hpp:23-34).  PCG with the multigrid
+ * preconditioner is the fused device-side flexible PCG; every other combination runs host-driven
+ * (one host read of the step's scalars per step).  GMRES, FGMRES and LGMRES all run as restarted
+ * flexible GMRES(kdim); NONE iterates the preconditioner alone (PFMG, SMG or Jacobi as the solver). */
+enum opflow_krylov {
+    OPFLOW_KRYLOV_PCG = 0,
+    OPFLOW_KRYLOV_GMRES = 1,
+    OPFLOW_KRYLOV_FGMRES = 2,
+    OPFLOW_KRYLOV_LGMRES = 3,
+    OPFLOW_KRYLOV_BICGSTAB = 4,
+    OPFLOW_KRYLOV_NONE = 5
+};
+/* Preconditioners: the geometric multigrid V-cycle stands in for PFMG, SMG and CycRed; JACOBI is one
+ * diagonal step z = D^-1 v; NONE the identity. */
+enum opflow_precond { OPFLOW_PRECOND_MG = 0, OPFLOW_PRECOND_JACOBI = 1, OPFLOW_PRECOND_NONE = 2 };
+
 typedef struct {
     double tol;           /* relative residual ||b-Ax||_2/||b||_2 target (reference: tol)        */
     int max_iter;         /* reference: maxIter                                                  */
@@ -278,6 +294,10 @@ typedef struct {
     int post_sweeps;      /* default 2                                                           */
     int coarse_max;       /* coarsest level size bound for the dense direct solve, default 64    */
     int zero_guess;       /* 1: start from x = 0 instead of the target's values                  */
+    int krylov;           /* enum opflow_krylov: the outer iteration (reference: StructSolverType) */
+    int precond;          /* enum opflow_precond: its preconditioner                             */
+    int kdim;             /* GMRES restart length (reference: kDim, HYPRE's default 5)           */
+    double abs_tol;       /* also stop once ||b - A x||_2 <= abs_tol (reference: absTol); 0 off  */
 } opflow_solve_params;
 
 typedef struct {

@@ -59,7 +59,12 @@ class Node(C.Structure):
 class SolveParams(C.Structure):
     _fields_ = [("tol", C.c_double), ("max_iter", C.c_int), ("static_mat", C.c_int), ("pin_value", C.c_int),
                 ("precision", C.c_int), ("pre_sweeps", C.c_int), ("post_sweeps", C.c_int), ("coarse_max", C.c_int),
-                ("zero_guess", C.c_int)]
+                ("zero_guess", C.c_int), ("krylov", C.c_int), ("precond", C.c_int), ("kdim", C.c_int), ("abs_tol", C.c_double)]
+
+
+# enum opflow_krylov / opflow_precond
+KRYLOV_PCG, KRYLOV_GMRES, KRYLOV_FGMRES, KRYLOV_LGMRES, KRYLOV_BICGSTAB, KRYLOV_NONE = range(6)
+PRECOND_MG, PRECOND_JACOBI, PRECOND_NONE = range(3)
 
 
 class SolveState(C.Structure):

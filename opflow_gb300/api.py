@@ -660,15 +660,33 @@ def describe(mesh, desc):
 
 
 # ------------------------------------------------------------------------------------------ implicit path
+# StructSolverType (src/Core/Solvers/Struct/StructSolver.hpp:23-34) -> (outer iteration, preconditioner)
+STRUCT_SOLVERS = {"PCG": capi.KRYLOV_PCG, "GMRES": capi.KRYLOV_GMRES, "FGMRES": capi.KRYLOV_FGMRES,
+                  "LGMRES": capi.KRYLOV_LGMRES, "BICGSTAB": capi.KRYLOV_BICGSTAB}
+STRUCT_PRECONDS = {"PFMG": capi.PRECOND_MG, "SMG": capi.PRECOND_MG, "CYCRED": capi.PRECOND_MG,
+                   "Jacobi": capi.PRECOND_JACOBI, "None": capi.PRECOND_NONE}
+
+
 class StructSolverParams:
     """StructSolverParamsBase (src/Core/Solvers/Struct/StructSolver.hpp:39-51) with the PFMG knobs
-    (StructSolverPFMG.hpp:23-33) and the GPU extensions (precision form, coarse size)."""
+    (StructSolverPFMG.hpp:23-33), the GMRES ones (kDim, absTol) and the GPU extensions (precision form,
+    coarse size).  `solver` / `precond` name the StructSolverType pair of
+    PrecondStructSolver<solver, precond>; a preconditioner type as `solver` (PFMG, SMG, Jacobi) with
+    precond "None" iterates it alone."""
 
     def __init__(self, tol=1e-10, maxIter=200, staticMat=False, pinValue=False, precision="fp64", preSweeps=2,
-                 postSweeps=2, coarseMax=64, zeroGuess=False):
+                 postSweeps=2, coarseMax=64, zeroGuess=False, solver="PCG", precond="PFMG", kDim=5, absTol=0.0):
         self.tol, self.maxIter, self.staticMat, self.pinValue = tol, maxIter, staticMat, pinValue
         self.precision, self.preSweeps, self.postSweeps, self.coarseMax, self.zeroGuess = (precision, preSweeps, postSweeps,
                                                                                            coarseMax, zeroGuess)
+        self.solver, self.precond, self.kDim, self.absTol = solver, precond, kDim, absTol
+
+    def krylov_and_precond(self):
+        if self.solver in STRUCT_SOLVERS:
+            return STRUCT_SOLVERS[self.solver], STRUCT_PRECONDS[self.precond]
+        if self.solver in STRUCT_PRECONDS and self.precond == "None":
+            return capi.KRYLOV_NONE, STRUCT_PRECONDS[self.solver]
+        raise ValueError("unsupported solver combination %s + %s" % (self.solver, self.precond))
 
     def to_c(self):
         p = capi.SolveParams()
@@ -680,6 +698,9 @@ class StructSolverParams:
         p.pre_sweeps, p.post_sweeps = int(self.preSweeps), int(self.postSweeps)
         p.coarse_max = int(self.coarseMax)
         p.zero_guess = int(bool(self.zeroGuess))
+        p.krylov, p.precond = self.krylov_and_precond()
+        p.kdim = int(self.kDim)
+        p.abs_tol = float(self.absTol)
         return p
 
 

@@ -555,6 +555,7 @@ int opflow_field_upload(opflow_field f, const double* host, size_t count) {
     if (!f || !host) return fail(OPFLOW_E_INVALID, "null argument");
     if (count != f->info.count) return fail(OPFLOW_E_INVALID, "upload of %zu values into a field of %zu", count, f->info.count);
     f->bc_fresh[0] = f->bc_fresh[1] = false;
+    f->version++;
     OPG_CUDA(cudaMemcpyAsync(f->buf[f->cur], host, count * sizeof(double), cudaMemcpyHostToDevice, f->ctx->stream));
     if (f->buf[1 - f->cur])
         OPG_CUDA(cudaMemcpyAsync(f->buf[1 - f->cur], f->buf[f->cur], count * sizeof(double), cudaMemcpyDeviceToDevice, f->ctx->stream));
@@ -574,6 +575,7 @@ int opflow_field_device_ptr(opflow_field f, double** p) {
     if (!f || !p) return fail(OPFLOW_E_INVALID, "null argument");
     *p = f->buf[f->cur];
     f->bc_fresh[0] = f->bc_fresh[1] = false;  // the caller may write through the pointer
+    f->version++;
     return OPFLOW_OK;
 }
 

@@ -1062,12 +1062,8 @@ static int run_plan(opflow_ctx ctx, opflow_field dst, int arith, const opflow_fi
             }
         }
     }
-    if (oop) {
-        if (arith != OPFLOW_ASSIGN_EQ && plan->kind == PLAN_INTERP) {
-            // the interpreter already applied `cur op value` while writing the back buffer
-        }
-        dst->cur = 1 - dst->cur;
-    }
+    if (oop) dst->cur = 1 - dst->cur;  // (the interpreter applied `cur op value` while writing the back buffer)
+    dst->version++;
     return update_padding_assign(dst);
 }
 
@@ -1112,6 +1108,7 @@ int opflow_assign(opflow_ctx ctx, opflow_field dst, int arith, const opflow_node
 
 int opflow_field_fill(opflow_field f, int arith, double c) {
     if (!f) return fail(OPFLOW_E_INVALID, "null field");
+    f->version++;
     Box b = assign_box(f->info);
     if (b.count() > 0) {
         fill_kernel<<<grid_for(f->ctx, b.count(), 256), 256, 0, f->ctx->stream>>>(f->view(), b, arith, c);
@@ -1127,6 +1124,7 @@ int opflow_field_copy(opflow_field dst, opflow_field src) {
     if (!dst || !src) return fail(OPFLOW_E_INVALID, "null field");
     if (dst->info.count != src->info.count) return fail(OPFLOW_E_INVALID, "field shapes differ");
     dst->bc_fresh[0] = dst->bc_fresh[1] = false;
+    dst->version++;
     OPG_CUDA(cudaMemcpyAsync(dst->buf[dst->cur], src->buf[src->cur], src->info.count * sizeof(double), cudaMemcpyDeviceToDevice, dst->ctx->stream));
     OPG_TRY(update_padding_buf(dst, dst->buf[dst->cur]));
     OPG_CUDA(cudaStreamSynchronize(dst->ctx->stream));

@@ -108,6 +108,9 @@ struct opflow_field_s {
     // the caller may have written the buffer); lets a padding update that can only rewrite constant
     // Dirichlet nodes be skipped
     bool bc_fresh[2] = {false, false};
+    // bumped by every write of the values (assign, fill, copy, upload, device pointer, solve, WENO
+    // step): a solve handler compares it to decide whether its assembled system is still current
+    unsigned long long version = 0;
     bool padding_is_step0_only() const;
     opg::FieldView view() const;
     opg::FieldView view_back() const;

@@ -761,6 +761,8 @@ static int vcycle(MGSystem* S) {
     return OPFLOW_OK;
 }
 
+int mg_vcycle(MGSystem* S) { return vcycle(S); }
+
 // fused per-problem reduction + scalar stage for the Krylov kernels
 static Finish finish(MGSystem* S, int stage) {
     Finish F{};
@@ -1122,6 +1124,7 @@ void mg_destroy(MGSystem* S) {
     S->rec_stream = nullptr;
     for (auto& P : S->probs)
         for (auto& L : P.levels) release_level_fields(L);
+    krylov_release(S);
     S->arena.release();
     if (S->h_active) cudaFreeHost(S->h_active);
     delete S;
@@ -1162,7 +1165,16 @@ struct opflow_solver_s {
     opflow_solve_params params;
     MGSystem* S = nullptr;
     bool first = true;
+    // write counters of the leaves when the system was last assembled (the target's after its solve)
+    std::vector<unsigned long long> assembled_versions;
 };
+
+// (the unknown's own values only seed the iteration, so its slot is left out)
+static std::vector<unsigned long long> leaf_versions(opflow_solver s) {
+    std::vector<unsigned long long> v;
+    for (size_t k = 0; k < s->leaves.size(); ++k) v.push_back((int) k == s->unknown ? 0ull : s->leaves[k]->version);
+    return v;
+}
 
 static int build_system(opflow_solver s) {
     if (s->S) mg_destroy(s->S);
@@ -1192,6 +1204,10 @@ void opflow_solve_params_default(opflow_solve_params* p) {
     p->post_sweeps = 2;
     p->coarse_max = 64;
     p->zero_guess = 0;
+    p->krylov = OPFLOW_KRYLOV_PCG;
+    p->precond = OPFLOW_PRECOND_MG;
+    p->kdim = 5;
+    p->abs_tol = 0.;
 }
 
 int opflow_solver_create(opflow_ctx ctx, opflow_field target, const opflow_node* nodes, int n_nodes, const opflow_field* leaves, int n_leaves,
@@ -1202,6 +1218,12 @@ int opflow_solver_create(opflow_ctx ctx, opflow_field target, const opflow_node*
     else opflow_solve_params_default(&p);
     if (!(p.tol > 0) || p.max_iter < 0 || p.pre_sweeps < 0 || p.post_sweeps < 0) return fail(OPFLOW_E_INVALID, "bad solver parameters");
     if (p.precision != OPFLOW_PREC_FP64 && p.precision != OPFLOW_PREC_MIXED) return fail(OPFLOW_E_INVALID, "bad precision");
+    if (p.krylov < OPFLOW_KRYLOV_PCG || p.krylov > OPFLOW_KRYLOV_NONE) return fail(OPFLOW_E_INVALID, "bad Krylov method %d", p.krylov);
+    if (p.precond < OPFLOW_PRECOND_MG || p.precond > OPFLOW_PRECOND_NONE) return fail(OPFLOW_E_INVALID, "bad preconditioner %d", p.precond);
+    if (p.krylov == OPFLOW_KRYLOV_NONE && p.precond == OPFLOW_PRECOND_NONE) return fail(OPFLOW_E_INVALID, "no solver: neither a Krylov method nor a preconditioner");
+    if (p.kdim <= 0) p.kdim = 5;
+    if (p.kdim > 60) return fail(OPFLOW_E_INVALID, "kdim must be at most 60");
+    if (p.abs_tol < 0) return fail(OPFLOW_E_INVALID, "negative abs_tol");
     if (p.coarse_max <= 0) p.coarse_max = 64;
     auto* s = new opflow_solver_s();
     s->ctx = ctx;
@@ -1211,6 +1233,7 @@ int opflow_solver_create(opflow_ctx ctx, opflow_field target, const opflow_node*
     s->unknown = unknown_slot;
     s->params = p;
     int rc = build_system(s);
+    s->assembled_versions = leaf_versions(s);
     if (rc) {
         if (s->S) mg_destroy(s->S);
         delete s;
@@ -1225,8 +1248,11 @@ int opflow_solver_solve(opflow_solver s, opflow_solve_state* state) {
     using clk = std::chrono::steady_clock;
     auto t0 = clk::now();
     opflow_ctx ctx = s->ctx;
-    // generateAb on every solve, generateb only when staticMat (HYPREEqnSolveHandler.hpp:190-209)
-    if (!s->first) {
+    // generateAb on the first solve and on every later one, generateb only when staticMat
+    // (HYPREEqnSolveHandler.hpp:190-209).  The first solve reuses the system assembled at creation
+    // unless a field of the equation was written since.
+    if (s->first && leaf_versions(s) != s->assembled_versions) OPG_TRY(build_system(s));
+    else if (!s->first) {
         if (s->params.static_mat) {
             AsmPlan plan;
             OPG_TRY(asm_prepare(ctx, s->target, s->tree.data(), (int) s->tree.size(), s->leaves.data(), (int) s->leaves.size(), s->unknown, 0,
@@ -1267,9 +1293,22 @@ int opflow_solver_solve(opflow_solver s, opflow_solve_state* state) {
         }
     }
     auto t1 = clk::now();
-    OPG_TRY(mg_solve(S));
-    std::vector<Scal> st;
-    OPG_TRY(mg_states(S, st));
+    int iters = 0;
+    if (s->params.krylov == OPFLOW_KRYLOV_PCG && s->params.precond == OPFLOW_PRECOND_MG) {
+        OPG_TRY(mg_solve(S));
+        std::vector<Scal> st;
+        OPG_TRY(mg_states(S, st));
+        iters = st[0].iters;
+    } else {
+        KrylovParams kp;
+        kp.method = s->params.krylov;
+        kp.precond = s->params.precond;
+        kp.kdim = s->params.kdim;
+        kp.max_iter = s->params.max_iter;
+        kp.tol = s->params.tol;
+        kp.abs_tol = s->params.abs_tol;
+        OPG_TRY(krylov_solve(S, kp, &iters));
+    }
     double shift = 0.;
     if (pinned) {
         OPG_CUDA(cudaMemcpy(&shift, K.x, 8, cudaMemcpyDeviceToHost));
@@ -1292,19 +1331,21 @@ int opflow_solver_solve(opflow_solver s, opflow_solve_state* state) {
     scatter_box<<<gridN(ctx, N), 256, 0, ctx->stream>>>(s->target->view(), box, K.x, 0.);
     OPG_LAUNCHED();
     s->target->bc_fresh[s->target->cur] = false;
+    s->target->version++;
+    s->assembled_versions = leaf_versions(s);
     OPG_TRY(update_padding_buf(s->target, s->target->buf[s->target->cur]));
     OPG_CUDA(cudaStreamSynchronize(ctx->stream));
     auto t2 = clk::now();
     if (state) {
-        state->iterations = st[0].iters;
+        state->iterations = iters;
         state->abs_residual = std::sqrt(rr);
         state->rel_residual = bb > 0 ? std::sqrt(rr / bb) : std::sqrt(rr);
-        state->converged = state->rel_residual <= s->params.tol;
+        state->converged = state->rel_residual <= s->params.tol || (s->params.abs_tol > 0 && state->abs_residual <= s->params.abs_tol);
         state->setup_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
         state->solve_ms = std::chrono::duration<double, std::milli>(t2 - t1).count();
     }
-    if (state && !state->converged && st[0].iters >= s->params.max_iter)
-        return fail(OPFLOW_E_NOT_CONVERGED, "not converged after %d iterations (relative residual %g)", st[0].iters, state->rel_residual);
+    if (state && !state->converged && iters >= s->params.max_iter)
+        return fail(OPFLOW_E_NOT_CONVERGED, "not converged after %d iterations (relative residual %g)", iters, state->rel_residual);
     return OPFLOW_OK;
 }
 

@@ -6,6 +6,8 @@
 
 namespace opg {
 
+struct KrylovWork;  // krylov.cu
+
 // Bump allocator over large device blocks (one solver / batch owns one).
 struct Arena {
     opflow_ctx ctx = nullptr;  // blocks come from the context's stream-ordered pool (cudaMalloc if null)
@@ -108,7 +110,23 @@ struct MGSystem {
     std::vector<LvlDev> lv_host;
     std::vector<Chunk> k0_host;
     bool composite = false;              // tables reference other systems' memory
+    KrylovWork* kwork = nullptr;         // workspace of the host-driven Krylov methods (arena memory)
 };
+
+// The host-driven Krylov methods of krylov.cu (every method but the fused flexible PCG with the
+// multigrid preconditioner).
+struct KrylovParams {
+    int method = OPFLOW_KRYLOV_GMRES;  // enum opflow_krylov
+    int precond = OPFLOW_PRECOND_MG;   // enum opflow_precond
+    int kdim = 5;
+    int max_iter = 100;
+    double tol = 1e-10, abs_tol = 0.;
+};
+// Solves the single problem of S in place (K.x holds the initial guess, K.b the right-hand side).
+int krylov_solve(MGSystem* S, const KrylovParams& P, int* iters);
+void krylov_release(MGSystem* S);
+// one V-cycle on the level-0 input already written (b, x = 0)
+int mg_vcycle(MGSystem* S);
 
 // Device tables of a batch assembled from single-problem systems (the problems stay where they are);
 // state[i] seeds problem i's Krylov scalars.

@@ -181,10 +181,13 @@ extern "C" int opflow_weno_rk3(opflow_ctx ctx, opflow_field u, opflow_field u1, 
     weno_rk3_kernel<<<blocks, threads, smem, ctx->stream>>>(u->view(), v1, v2, stages ? 1 : 0, lines, P, steps);
     OPG_LAUNCHED();
     OPG_TRY(check_launch("weno_rk3_kernel"));
+    u->version++;
     OPG_TRY(update_padding_assign(u));
     if (stages) {
         u1->bc_fresh[0] = u1->bc_fresh[1] = false;
         u2->bc_fresh[0] = u2->bc_fresh[1] = false;
+        u1->version++;
+        u2->version++;
         OPG_TRY(update_padding_assign(u1));
         OPG_TRY(update_padding_assign(u2));
     }
