@@ -542,6 +542,7 @@ public:
 
     CartesianField() = default;
     CartesianField(const CartesianField& o) : name(o.name), mesh(o.mesh), desc(o.desc) {
+        if (!o.h) return;  // a copy of a field that was never built is unbuilt too
         create();
         GPU::check(opflow_field_copy(h->f, o.h->f), "CartesianField copy");
     }
@@ -551,6 +552,7 @@ public:
     // the reference's value assignment between fields
     CartesianField& operator=(const CartesianField& o) {
         if (this == &o) return *this;
+        if (!o.h) GPU::check(OPFLOW_E_INVALID, "assignment from a field that was never built");
         if (!h) {
             name = o.name;
             mesh = o.mesh;
@@ -670,51 +672,59 @@ template <typename R, typename Mesh>
 struct ExprBuilder<CartesianField<R, Mesh>> {
     static constexpr int dim = Mesh::dim;
     using Field = CartesianField<R, Mesh>;
-    Field f;
+    // plain settings (copying a builder copies no device data); one builder makes several fields,
+    // as OpFlow's does
+    std::string name;
+    Mesh mesh;
+    opflow_field_desc desc {};
     bool ext_set = false;
 
     ExprBuilder() {
-        f.desc.ndim = dim;
-        for (int d = 0; d < dim; ++d) f.desc.loc[d] = OPFLOW_CORNER;
+        desc.ndim = dim;
+        for (int d = 0; d < dim; ++d) desc.loc[d] = OPFLOW_CORNER;
     }
     ExprBuilder& setName(const std::string& n) {
-        f.name = n;
+        name = n;
         return *this;
     }
     ExprBuilder& setMesh(const Mesh& m) {
-        f.mesh = m;
+        mesh = m;
         return *this;
     }
     ExprBuilder& setLoc(const std::array<LocOnMesh, dim>& loc) {
-        for (int d = 0; d < dim; ++d) f.desc.loc[d] = (int) loc[d];
+        for (int d = 0; d < dim; ++d) desc.loc[d] = (int) loc[d];
         return *this;
     }
     ExprBuilder& setLoc(LocOnMesh loc) {
-        for (int d = 0; d < dim; ++d) f.desc.loc[d] = (int) loc;
+        for (int d = 0; d < dim; ++d) desc.loc[d] = (int) loc;
         return *this;
     }
     ExprBuilder& setBC(int d, DimPos pos, BCType type, Real value = 0.) {
-        f.desc.bc_type[d][(int) pos] = (int) type;
-        f.desc.bc_value[d][(int) pos] = value;
+        desc.bc_type[d][(int) pos] = (int) type;
+        desc.bc_value[d][(int) pos] = value;
         return *this;
     }
     ExprBuilder& setExt(int e) {
-        for (int d = 0; d < dim; ++d) f.desc.ext[d][0] = f.desc.ext[d][1] = e;
+        for (int d = 0; d < dim; ++d) desc.ext[d][0] = desc.ext[d][1] = e;
         ext_set = true;
         return *this;
     }
     ExprBuilder& setExt(int d, DimPos pos, int e) {
-        f.desc.ext[d][(int) pos] = e;
+        desc.ext[d][(int) pos] = e;
         ext_set = true;
         return *this;
     }
     ExprBuilder& setPadding(int p) {
-        f.desc.padding = p;
+        desc.padding = p;
         return *this;
     }
-    Field build() {
-        f.create();
-        return std::move(f);
+    Field build() const {
+        Field out;
+        out.name = name;
+        out.mesh = mesh;
+        out.desc = desc;
+        out.create();
+        return out;
     }
 };
 

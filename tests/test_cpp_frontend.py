@@ -25,7 +25,7 @@ def build_example(name, outdir):
     return exe
 
 
-@pytest.mark.parametrize("name", ["ftcs2d", "poisson", "conv1d"])
+@pytest.mark.parametrize("name", ["ftcs2d", "poisson", "conv1d", "lid_driven"])
 def test_examples_compile_and_link(tmp_path, name):
     build_example(name, str(tmp_path))
 
@@ -104,3 +104,24 @@ def test_conv1d_program_matches_oracle_and_reference(ctx, tmp_path, scheme):
     if scheme != "minmod":
         _, arr = cm.golden("conv1d_n101")
         assert np.array_equal(h.data[h.slices([(0, n)])], arr["u__data"])
+
+
+@pytest.mark.gpu
+def test_lid_driven_program_matches_the_python_run(ctx, tmp_path):
+    """examples/LidDriven through the C++ front end (GMRES + PFMG solves, staticMat / pinValue pressure
+    equation): every solve converges, the divergence stays at solver-tolerance level, and u, v, p are
+    bit-identical to the same steps taken through the Python API (whose solves the oracle checks in
+    test_lid_driven_gpu.py)."""
+    from test_lid_driven_gpu import run_cavity
+    n, steps = 33, 3
+    exe = build_example("lid_driven", str(tmp_path))
+    out = str(tmp_path / "uvp.bin")
+    r = subprocess.run([exe, str(n), str(steps), out], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    for line in r.stdout.splitlines():
+        assert float(line.split("div")[1]) <= 1e-6, line
+    u, v, p = run_cavity(ctx, n, steps, check=False)
+    got = np.fromfile(out, dtype=np.float64)
+    want = np.concatenate([f.download().reshape(-1) for f in (u, v, p)])
+    assert got.size == want.size
+    assert np.array_equal(got, want)

@@ -56,8 +56,9 @@ def _ops():
     return conv_xx, conv_xy, conv_yx, conv_yy, lap
 
 
-def test_lid_driven_cavity_steps(ctx):
-    n, steps = 33, 4
+def run_cavity(ctx, n, steps, check=True):
+    """The cavity's time steps; with `check`, every solve is verified against the oracle and the
+    divergence after each projection is bounded.  Returns the final u, v, p fields."""
     dt, nu = 0.5e-2, 1.0e-2
     u, du, v, dv, p, dp = _fields(ctx, n)
     conv_xx, conv_xy, conv_yx, conv_yy, lap = _ops()
@@ -82,21 +83,29 @@ def test_lid_driven_cavity_steps(ctx):
         for h, eq, tgt, pin in ((hu, u_eq, du, False), (hv, v_eq, dv, False)):
             st = h.solve()
             assert st.converged and st.relerr <= 1e-10, (step, st)
-            rel, _ = oracle_check(tgt, eq, tgt, pin, 1e-10)
-            assert rel <= 2e-10, (step, rel)
+            if check:
+                rel, _ = oracle_check(tgt, eq, tgt, pin, 1e-10)
+                assert rel <= 2e-10, (step, rel)
         du.assign(du - 0.5 * dt * conv_xy(u, dv))
         u.assign(u + du)
         v.assign(v + dv)
         st = hp.solve()
         assert st.converged and st.relerr <= 1e-10, (step, st)
-        rel, _ = oracle_check(dp, p_eq, dp, True, 1e-10)
-        assert rel <= 2e-10, (step, rel)
+        if check:
+            rel, _ = oracle_check(dp, p_eq, dp, True, 1e-10)
+            assert rel <= 2e-10, (step, rel)
         u.assign(u - dt * api.dx(dp, D1C))
         v.assign(v - dt * api.dy(dp, D1C))
         p.assign(p + dp)
-        div.assign(api.dx(u, D1C) + api.dy(v, D1C))
-        d = div.download()[div.index_slices([tuple(div.info.assignable[q]) for q in range(2)])]
-        assert np.abs(d).max() <= 1e-6, (step, np.abs(d).max())
+        if check:
+            div.assign(api.dx(u, D1C) + api.dy(v, D1C))
+            d = div.download()[div.index_slices([tuple(div.info.assignable[q]) for q in range(2)])]
+            assert np.abs(d).max() <= 1e-6, (step, np.abs(d).max())
+    return u, v, p
+
+
+def test_lid_driven_cavity_steps(ctx):
+    u, v, p = run_cavity(ctx, 33, 4)
     # the lid drags the fluid: the top row moves along +x, a return flow develops below
     U = u.download()[u.index_slices([tuple(u.info.assignable[q]) for q in range(2)])]
     assert U[-1].mean() > 0.05 and U.min() < 0
