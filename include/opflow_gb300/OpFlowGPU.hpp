@@ -12,9 +12,11 @@
 //     templates; they are lowered to device kernels when assigned.
 //   - Field data lives in device memory.  Host reads (evalAt, operator[], data()) download a host
 //     mirror on demand; host writes go through initBy / setData / operator[] + upload().
-//   - The implicit solve is the engine's flexible PCG with a geometric-multigrid V-cycle whatever
-//     Krylov / preconditioner pair is requested; tol, maxIter, staticMat and pinValue keep their
-//     meaning.  `gpuMixedPrecision` selects the FP32 V-cycle inside the FP64 outer iteration.
+//   - The implicit solve runs the requested PrecondStructSolver<Solver, Precond> pair on the GPU:
+//     PCG, GMRES / FlexGMRES / LGMRES (restarted flexible GMRES with kDim), BICGSTAB, or the
+//     preconditioner alone, with the engine's geometric-multigrid V-cycle standing in for PFMG, SMG and
+//     CycRed, or Jacobi, or none.  tol, absTol, maxIter, kDim, staticMat and pinValue keep their
+//     meaning; `gpuMixedPrecision` selects the FP32 V-cycle inside the FP64 outer iteration.
 //   - Failures print the engine's message and exit(1), the reference's OP_ABORT behaviour
 //     (src/Core/Macros.hpp:146-151); set OpFlow::GPU::throwOnError(true) to get exceptions instead.
 #ifndef OPFLOW_GB300_OPFLOWGPU_HPP
