@@ -867,6 +867,58 @@ EqnSolveState Solve(F&& getter, Target& target) {
     return Solve<S, P>(std::forward<F>(getter), target, StructSolverParams<S> {}, StructSolverParams<P> {});
 }
 
+// ------------------------------------------------------------------------------------ snapshots
+namespace Utils {
+    // TimeStamp (src/Utils/Writers/Streams.hpp:31-45)
+    struct TimeStamp {
+        double time {};
+        TimeStamp() = default;
+        explicit TimeStamp(double t) : time(t) {}
+        explicit operator double() const { return time; }
+    };
+    // the directory part of a stream path (std::filesystem::path::parent_path of a plain path)
+    inline std::string parentDir(const std::string& p) {
+        const auto k = p.find_last_of('/');
+        return k == std::string::npos ? std::string(".") : (k == 0 ? std::string("/") : p.substr(0, k));
+    }
+    // RawBinaryOStream (src/Utils/Writers/RawBinaryStream.hpp:42-62, 97-150): `s << TimeStamp(t) << u`
+    // writes <dir>/<name>_<count>.cart and advances the counter
+    struct RawBinaryOStream {
+        std::string dir = ".";
+        double time = 0.;
+        int count = 0;
+        RawBinaryOStream() = default;
+        explicit RawBinaryOStream(const std::string& path) : dir(parentDir(path)) {}
+        void setCounterTo(int c) { count = c; }
+        RawBinaryOStream& operator<<(const TimeStamp& t) {
+            time = t.time;
+            return *this;
+        }
+        template <typename R, typename M>
+        RawBinaryOStream& operator<<(const CartesianField<R, M>& f) {
+            GPU::check(opflow_field_write_raw(f.handle(), dir.c_str(), f.name.c_str(), count, time), "RawBinaryOStream");
+            ++count;
+            return *this;
+        }
+    };
+    // RawBinaryIStream (RawBinaryStream.hpp:64-77, 152-224): `s >> u` reads <dir>/<name>_<count>.cart
+    struct RawBinaryIStream {
+        std::string dir = ".";
+        int count = 0;
+        double time = 0.;
+        RawBinaryIStream() = default;
+        explicit RawBinaryIStream(const std::string& path) : dir(parentDir(path)) {}
+        void setCounterTo(int c) { count = c; }
+        template <typename R, typename M>
+        RawBinaryIStream& operator>>(CartesianField<R, M>& f) {
+            GPU::check(opflow_field_read_raw(f.handle(), dir.c_str(), f.name.c_str(), count, &time), "RawBinaryIStream");
+            f.h->host_valid = false;
+            ++count;
+            return *this;
+        }
+    };
+}// namespace Utils
+
 // EnvironmentGardian (src/Core/Environment.hpp): brings the engine up and releases it at scope exit.
 struct EnvironmentGardian {
     EnvironmentGardian() { GPU::context(); }

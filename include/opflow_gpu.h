@@ -131,6 +131,13 @@ int opflow_field_download(opflow_field f, double* host, size_t count);
 int opflow_field_device_ptr(opflow_field f, double** dptr);
 /* CartesianField::updatePaddingImpl_final (CartesianField.hpp:349-629), single-rank branch. */
 int opflow_field_update_padding(opflow_field f);
+/* Field snapshots in OpFlow's raw binary format: Utils::RawBinaryOStream << field
+ * (src/Utils/Writers/RawBinaryStream.hpp:97-150) writes <dir>/<name>_<count>.cart with the time stamp,
+ * the mesh range and coordinates, the field's accessible and local ranges and the local-range values;
+ * RawBinaryIStream >> field (RawBinaryStream.hpp:152-224) reads one back after checking the mesh and
+ * ranges against the field's, then updates the padding.  The streams' counters live in the caller. */
+int opflow_field_write_raw(opflow_field f, const char* dir, const char* name, int count, double time);
+int opflow_field_read_raw(opflow_field f, const char* dir, const char* name, int count, double* time_out);
 /* `f = c` for a constant (CartesianField::assignImpl_final(const D&), CartesianField.hpp:236-280). */
 int opflow_field_fill(opflow_field f, int arith, double c);
 /* `dst = src` between two fields of identical shape (data copy, then padding). */

@@ -118,6 +118,8 @@ _SIGS = {
     "opflow_field_download": [C.c_void_p, C.POINTER(C.c_double), C.c_size_t],
     "opflow_field_device_ptr": [C.c_void_p, C.POINTER(C.c_void_p)],
     "opflow_field_update_padding": [C.c_void_p],
+    "opflow_field_write_raw": [C.c_void_p, C.c_char_p, C.c_char_p, C.c_int, C.c_double],
+    "opflow_field_read_raw": [C.c_void_p, C.c_char_p, C.c_char_p, C.c_int, C.POINTER(C.c_double)],
     "opflow_field_fill": [C.c_void_p, C.c_int, C.c_double],
     "opflow_field_copy": [C.c_void_p, C.c_void_p],
     "opflow_assign": [C.c_void_p, C.c_void_p, C.c_int, C.POINTER(Node), C.c_int, C.POINTER(C.c_void_p), C.c_int, C.c_int],

@@ -16,6 +16,7 @@ Python cannot overload `=`, so `u = expr` is spelled `u.assign(expr)` (and `u +=
 """
 import atexit
 import ctypes as C
+import os
 import threading
 
 import numpy as np
@@ -649,6 +650,57 @@ class ExprBuilder:
 
     def build(self, ctx=None):
         return CartesianField(self._mesh, self.desc(), ctx or default_context(), self._name)
+
+
+# ------------------------------------------------------------------------------------------ snapshots
+class TimeStamp:
+    """Utils::TimeStamp (src/Utils/Writers/Streams.hpp:31-45)."""
+
+    def __init__(self, time=0.0, step=None):
+        self.time, self.step = float(time), step
+
+
+class RawBinaryOStream:
+    """Utils::RawBinaryOStream (src/Utils/Writers/RawBinaryStream.hpp:42-62, 97-150): `stream << TimeStamp(t)`
+    sets the time, `stream << field` writes <dir>/<name>_<count>.cart and advances the counter.  As in
+    the reference, the files go to the directory part of `path` (its parent)."""
+
+    def __init__(self, path):
+        self.dir = os.path.dirname(os.fspath(path)) or "."
+        self.time = 0.0
+        self.count = 0
+
+    def setCounterTo(self, c):
+        self.count = int(c)
+
+    def __lshift__(self, x):
+        if isinstance(x, TimeStamp):
+            self.time = x.time
+            return self
+        check(lib().opflow_field_write_raw(x.handle, self.dir.encode(), x.name.encode(), self.count, self.time))
+        self.count += 1
+        return self
+
+
+class RawBinaryIStream:
+    """Utils::RawBinaryIStream (RawBinaryStream.hpp:64-77, 152-224): `stream >> field` reads
+    <dir>/<name>_<count>.cart into the field (mesh and ranges checked) and advances the counter; the
+    time stamp read is kept in `time`."""
+
+    def __init__(self, path):
+        self.dir = os.path.dirname(os.fspath(path)) or "."
+        self.count = 0
+        self.time = 0.0
+
+    def setCounterTo(self, c):
+        self.count = int(c)
+
+    def __rshift__(self, f):
+        t = C.c_double(0.0)
+        check(lib().opflow_field_read_raw(f.handle, self.dir.encode(), f.name.encode(), self.count, C.byref(t)))
+        self.time = t.value
+        self.count += 1
+        return self
 
 
 def describe(mesh, desc):

@@ -79,6 +79,7 @@ int mesh_create(opflow_ctx ctx, const opflow_mesh_desc* m, MeshDev** out) {
     if (!m || m->ndim < 1 || m->ndim > 3 || m->pad_width < 0) return fail(OPFLOW_E_INVALID, "bad mesh description");
     auto* md = new MeshDev();
     md->ndim = m->ndim;
+    md->pad = m->pad_width;
     for (int d = 0; d < 3; ++d) {
         md->x[d] = md->dx[d] = nullptr;
         md->uniform[d] = true;

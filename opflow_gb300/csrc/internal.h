@@ -58,6 +58,7 @@ struct MeshDev {
     int ndim;
     int es[3];          // first index of the extended mesh range (start - pad_width)
     int n[3];           // number of nodes in the extended range
+    int pad = 0;        // pad_width: the mesh range is [es + pad, es + n - pad)
     double* x[3];       // device arrays
     double* dx[3];
     // host copies
