@@ -61,6 +61,7 @@ typedef struct opflow_field_s* opflow_field;
 typedef struct opflow_solver_s* opflow_solver;
 typedef struct opflow_batch_s* opflow_batch;
 typedef struct opflow_server_s* opflow_server;
+typedef struct opflow_eqnset_s* opflow_eqnset;
 
 /* ---- context --------------------------------------------------------------------------------- */
 /* Replaces EnvironmentGardian / the global ParallelPlan (src/Core/Environment.hpp:41-62): one context
@@ -326,6 +327,24 @@ int opflow_solver_create(opflow_ctx ctx, opflow_field target, const opflow_node*
  * static_mat), solves, writes the solution into the target field and updates its padding. */
 int opflow_solver_solve(opflow_solver s, opflow_solve_state* state);
 int opflow_solver_destroy(opflow_solver s);
+
+/* ---- coupled equation sets (the reference's SolveEqns / AMGCL path) ------------------------------
+ * SolveEqns(getter_0, ..., getter_{n-1}, targets..., mapper, params) (src/Core/Equation/UnifiedSolve.hpp:69-100,
+ * AMGCLEqnSolveHandler.hpp:53-190): equation k (the tree trees[k], the lhs - rhs of getter k) is solved
+ * for targets[k] jointly with the others.  All trees index one leaf list in which every target
+ * appears; pin[k] pins equation k's last unknown (CSRMatrixGenerator.hpp:57-75); params (one set for
+ * the whole system) choose the outer iteration and the block-diagonal preconditioner (each equation's
+ * multigrid, Jacobi, none).  The first solve assembles the matrix; later ones re-assemble it unless
+ * static_mat, in which case only the right-hand side is regenerated.  x starts at 0 on the first solve
+ * and from the previous solution afterwards; the solution is written back into the targets. */
+int opflow_eqnset_create(opflow_ctx ctx, int n_eqn, const opflow_field* targets, const opflow_node* const* trees, const int* n_nodes,
+                         const opflow_field* leaves, int n_leaves, const int* pin, const opflow_solve_params* params, opflow_eqnset* out);
+int opflow_eqnset_solve(opflow_eqnset s, opflow_solve_state* state);
+/* The assembled system as CSR (CSRMatrixGenerator::generate): rows and columns numbered equation after
+ * equation, x fastest within each target's assignable range; columns ascending within a row; exact
+ * zeros left out.  Call with null arrays to get n_rows and nnz; row_ptr has n_rows + 1 entries. */
+int opflow_eqnset_csr(opflow_eqnset s, long long* n_rows, long long* nnz, long long* row_ptr, long long* cols, double* vals, double* rhs);
+int opflow_eqnset_destroy(opflow_eqnset s);
 
 /* ---- batched uneven solves ------------------------------------------------------------------- */
 /* Many independent 2D/3D problems of different sizes in one persistent launch per multigrid

@@ -119,6 +119,11 @@ _SIGS = {
     "opflow_field_device_ptr": [C.c_void_p, C.POINTER(C.c_void_p)],
     "opflow_field_update_padding": [C.c_void_p],
     "opflow_field_write_raw": [C.c_void_p, C.c_char_p, C.c_char_p, C.c_int, C.c_double],
+    "opflow_eqnset_create": [C.c_void_p, C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_int), C.POINTER(C.c_void_p),
+                             C.c_int, C.POINTER(C.c_int), C.c_void_p, C.POINTER(C.c_void_p)],
+    "opflow_eqnset_solve": [C.c_void_p, C.c_void_p],
+    "opflow_eqnset_csr": [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p],
+    "opflow_eqnset_destroy": [C.c_void_p],
     "opflow_field_read_raw": [C.c_void_p, C.c_char_p, C.c_char_p, C.c_int, C.POINTER(C.c_double)],
     "opflow_field_fill": [C.c_void_p, C.c_int, C.c_double],
     "opflow_field_copy": [C.c_void_p, C.c_void_p],

@@ -817,6 +817,75 @@ def Solve(getter, target, params=None, pparams=None):
     return EqnSolveHandler(getter, target, params).solve()
 
 
+class EqnSetSolveHandler:
+    """makeEqnSolveHandler over an equation set / SolveEqns (src/Core/Equation/UnifiedSolve.hpp:69-100,
+    AMGCLEqnSolveHandler.hpp:53-190): getters[k](*targets) returns equation k, solved for targets[k]
+    jointly with the others.  `params` (one StructSolverParams) picks the outer iteration and the
+    block-diagonal preconditioner; `pins[k]` pins equation k's last unknown (CSRMatrixGenerator)."""
+
+    def __init__(self, getters, targets, params=None, pins=None):
+        if len(getters) != len(targets):
+            raise ValueError("one getter per target")
+        self.targets = list(targets)
+        self.params = params or StructSolverParams(solver="BICGSTAB", precond="PFMG")
+        leaves = list(targets)
+        node_lists = []
+        for g in getters:
+            eq = g(*targets)
+            if not isinstance(eq, Equation):
+                raise TypeError("each getter must return `lhs == rhs`")
+            nodes, leaves = serialize(eq.residual_expr(), leaves)
+            node_lists.append(nodes)
+        self._nodes = node_lists
+        self._leaves = leaves
+        n = len(targets)
+        tg = (C.c_void_p * n)(*[t.handle.value for t in targets])
+        trees = (C.c_void_p * n)(*[C.cast(nl, C.c_void_p).value for nl in node_lists])
+        counts = (C.c_int * n)(*[len(nl) for nl in node_lists])
+        lv = (C.c_void_p * len(leaves))(*[f.handle.value for f in leaves])
+        pins = pins or [False] * n
+        pn = (C.c_int * n)(*[int(bool(p)) for p in pins])
+        p = self.params.to_c()
+        h = C.c_void_p()
+        check(lib().opflow_eqnset_create(targets[0].ctx.handle, n, tg, trees, counts, lv, len(leaves), pn, C.byref(p), C.byref(h)))
+        self.handle = h
+
+    def solve(self):
+        st = capi.SolveState()
+        rc = lib().opflow_eqnset_solve(self.handle, C.byref(st))
+        if rc not in (capi.OK, capi.E_NOT_CONVERGED):
+            check(rc)
+        return EqnSolveState(st)
+
+    def csr(self):
+        """The assembled coupled system (CSRMatrixGenerator's numbering): (row_ptr, cols, vals, rhs)."""
+        nr, nnz = C.c_longlong(0), C.c_longlong(0)
+        check(lib().opflow_eqnset_csr(self.handle, C.byref(nr), C.byref(nnz), None, None, None, None))
+        rp = np.zeros(nr.value + 1, dtype=np.int64)
+        cols = np.zeros(nnz.value, dtype=np.int64)
+        vals = np.zeros(nnz.value)
+        rhs = np.zeros(nr.value)
+        check(lib().opflow_eqnset_csr(self.handle, C.byref(nr), C.byref(nnz), rp.ctypes.data, cols.ctypes.data, vals.ctypes.data,
+                                      rhs.ctypes.data))
+        return rp, cols, vals, rhs
+
+    def close(self):
+        if getattr(self, "handle", None) and not _exiting[0]:
+            lib().opflow_eqnset_destroy(self.handle)
+        self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def SolveEqns(getters, targets, params=None, pins=None):
+    """SolveEqns(getter_0, ..., targets..., mapper, params): one solve of the coupled set."""
+    return EqnSetSolveHandler(getters, targets, params, pins).solve()
+
+
 def assemble(getter, target, pin=False):
     """The coefficients and right-hand side HYPREEqnSolveHandler::generateAb would hand to HYPRE
     (opflow_assemble): (offsets[n_entries, D], coef[cells, n_entries], rhs[cells])."""

@@ -608,7 +608,7 @@ struct KeyEval {
 
 // ================================================================================== public helpers
 int asm_prepare(opflow_ctx ctx, opflow_field target, const opflow_node* nodes, int n, const opflow_field* leaves, int nleaves, int unknown,
-                int pin, AsmPlan* plan) {
+                int pin, AsmPlan* plan, opflow_field rows) {
     if (!ctx || !target || !nodes || n < 1 || nleaves < 1 || nleaves > 8) return fail(OPFLOW_E_INVALID, "bad assembly arguments (1..8 leaves)");
     for (int s = 0; s < nleaves; ++s) {
         if (!leaves[s]) return fail(OPFLOW_E_INVALID, "null leaf %d", s);
@@ -641,7 +641,8 @@ int asm_prepare(opflow_ctx ctx, opflow_field target, const opflow_node* nodes, i
         P.mdx[d] = target->mesh->dx[d];
         P.es[d] = target->mesh->es[d];
     }
-    P.box = assign_box(R);
+    P.box = assign_box(rows ? rows->info : R);
+    if (rows && (rows->info.ndim != R.ndim || !mesh_equal(rows->mesh, target->mesh))) return fail(OPFLOW_E_INVALID, "row field on another mesh");
     P.nk = (int) K.size();
     for (int k = 0; k < P.nk; ++k)
         for (int d = 0; d < 3; ++d) P.K[k][d] = K[k][d];

@@ -44,8 +44,10 @@ struct AsmPlan {
     long long cells = 0;
 };
 
+// `rows`: the field whose assignable cells are the equations' rows when they are not the unknown's own
+// (a coupled system's off-diagonal block); the unknown's StencilField rules still come from `target`.
 int asm_prepare(opflow_ctx ctx, opflow_field target, const opflow_node* nodes, int n, const opflow_field* leaves, int nleaves, int unknown,
-                int pin, AsmPlan* plan);
+                int pin, AsmPlan* plan, opflow_field rows = nullptr);
 // coef: [nk][cells] (SoA over the plan's K order), rhs: [cells] = -bias
 int asm_run(opflow_ctx ctx, AsmPlan* plan, double* coef, double* rhs);
 

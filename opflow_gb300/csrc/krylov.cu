@@ -161,50 +161,18 @@ struct KrylovWork {
 namespace {
 
 struct Ctx {
-    MGSystem* S;
+    KrylovOp* op;
     KrylovWork* W;
-    LvlDev L0;
     cudaStream_t s;
     int grid;
     long long N;
-    int precond;
-    bool f32;
 };
 
 int launch_ok(const char* what) { return check_launch(what); }
 
-int matvec(Ctx& c, const double* x, double* y) {
-    kv_matvec<<<c.grid, KV_THREADS, 0, c.s>>>(c.L0, x, y);
-    OPG_LAUNCHED();
-    return launch_ok("kv_matvec");
-}
-
-int residual(Ctx& c, const double* b, const double* x, double* r) {
-    kv_residual<<<c.grid, KV_THREADS, 0, c.s>>>(c.L0, b, x, r);
-    OPG_LAUNCHED();
-    return launch_ok("kv_residual");
-}
-
-// z = M v
-int precond(Ctx& c, const double* v, double* z) {
-    if (c.precond == OPFLOW_PRECOND_NONE) {
-        OPG_CUDA(cudaMemcpyAsync(z, v, c.N * 8, cudaMemcpyDeviceToDevice, c.s));
-        return OPFLOW_OK;
-    }
-    if (c.precond == OPFLOW_PRECOND_JACOBI) {
-        kv_jacobi<<<c.grid, KV_THREADS, 0, c.s>>>(c.L0, v, z);
-        OPG_LAUNCHED();
-        return launch_ok("kv_jacobi");
-    }
-    if (c.f32) kv_to_vcycle<float><<<c.grid, KV_THREADS, 0, c.s>>>(c.N, v, c.L0.b32, c.L0.x32);
-    else kv_to_vcycle<double><<<c.grid, KV_THREADS, 0, c.s>>>(c.N, v, c.L0.b64, c.L0.x64);
-    OPG_LAUNCHED();
-    OPG_TRY(mg_vcycle(c.S));
-    if (c.f32) kv_from_vcycle<float><<<c.grid, KV_THREADS, 0, c.s>>>(c.N, c.L0.x32, z);
-    else kv_from_vcycle<double><<<c.grid, KV_THREADS, 0, c.s>>>(c.N, c.L0.x64, z);
-    OPG_LAUNCHED();
-    return launch_ok("kv_from_vcycle");
-}
+int matvec(Ctx& c, const double* x, double* y) { return c.op->matvec(x, y); }
+int residual(Ctx& c, const double* b, const double* x, double* r) { return c.op->residual(b, x, r); }
+int precond(Ctx& c, const double* v, double* z) { return c.op->precond(v, z); }
 
 // dred[0..nv) = <w, v_{q0..q0+nv}> (device only)
 int dots_dev(Ctx& c, const double* base, long long stride, int q0, int nv, const double* w) {
@@ -443,7 +411,119 @@ int stationary(Ctx& c, const KrylovParams& P, double* b, double* x, int* iters) 
     return OPFLOW_OK;
 }
 
+// The operator of one multigrid system's level 0 with its preconditioners.
+struct MgOp : KrylovOp {
+    MGSystem* S;
+    LvlDev L0;
+    cudaStream_t s;
+    int grid;
+    long long N;
+    int pc;
+    bool f32;
+    int matvec(const double* x, double* y) override {
+        kv_matvec<<<grid, KV_THREADS, 0, s>>>(L0, x, y);
+        OPG_LAUNCHED();
+        return launch_ok("kv_matvec");
+    }
+    int residual(const double* b, const double* x, double* r) override {
+        kv_residual<<<grid, KV_THREADS, 0, s>>>(L0, b, x, r);
+        OPG_LAUNCHED();
+        return launch_ok("kv_residual");
+    }
+    int precond(const double* v, double* z) override {
+        if (pc == OPFLOW_PRECOND_NONE) {
+            OPG_CUDA(cudaMemcpyAsync(z, v, N * 8, cudaMemcpyDeviceToDevice, s));
+            return OPFLOW_OK;
+        }
+        if (pc == OPFLOW_PRECOND_JACOBI) {
+            kv_jacobi<<<grid, KV_THREADS, 0, s>>>(L0, v, z);
+            OPG_LAUNCHED();
+            return launch_ok("kv_jacobi");
+        }
+        return mg_precond_level0(S, v, z);
+    }
+};
+
 }  // namespace
+
+int KrylovOp::residual(const double* b, const double* x, double* r) {
+    OPG_TRY(matvec(x, r));
+    kv_axpby<<<grid_hint, KV_THREADS, 0, stream>>>(n, 1., b, -1., r, 0., nullptr);  // r = b - A x
+    OPG_LAUNCHED();
+    return launch_ok("kv_axpby");
+}
+
+// z = V-cycle(v) on S's level 0 (its single problem must be active)
+int mg_precond_level0(MGSystem* S, const double* v, double* z) {
+    const ProblemHost& Pr = S->probs[0];
+    const LvlDev& L0 = S->lv_host[Pr.lvl0];
+    const long long N = Pr.levels[0].N;
+    cudaStream_t s = S->ctx->stream;
+    const int grid = (int) std::max<long long>(1, std::min<long long>((N + KV_THREADS - 1) / KV_THREADS, (long long) S->ctx->num_sms * 8));
+    if (S->precision == OPFLOW_PREC_MIXED) kv_to_vcycle<float><<<grid, KV_THREADS, 0, s>>>(N, v, L0.b32, L0.x32);
+    else kv_to_vcycle<double><<<grid, KV_THREADS, 0, s>>>(N, v, L0.b64, L0.x64);
+    OPG_LAUNCHED();
+    OPG_TRY(mg_vcycle(S));
+    if (S->precision == OPFLOW_PREC_MIXED) kv_from_vcycle<float><<<grid, KV_THREADS, 0, s>>>(N, L0.x32, z);
+    else kv_from_vcycle<double><<<grid, KV_THREADS, 0, s>>>(N, L0.x64, z);
+    OPG_LAUNCHED();
+    return launch_ok("kv_from_vcycle");
+}
+
+// marks S's single problem active for the V-cycle kernels (they skip inactive problems)
+int mg_activate(MGSystem* S) {
+    Scal sc{};
+    sc.active = 1;
+    OPG_CUDA(cudaMemcpyAsync(S->dS, &sc, sizeof sc, cudaMemcpyHostToDevice, S->ctx->stream));
+    return OPFLOW_OK;
+}
+
+int krylov_vectors(const KrylovParams& P) {
+    return (P.method == OPFLOW_KRYLOV_GMRES || P.method == OPFLOW_KRYLOV_FGMRES || P.method == OPFLOW_KRYLOV_LGMRES) ? 2 * P.kdim + 2 : 8;
+}
+
+KrylovWork* krylov_work(Arena& arena, opflow_ctx ctx, long long N, const KrylovParams& P) {
+    auto* W = new KrylovWork();
+    W->N = N;
+    W->nvec = krylov_vectors(P);
+    W->kdim = P.kdim;
+    W->blocks = std::max(1, ctx->num_sms * KV_BLOCKS_PER_SM);
+    W->vec = (double*) arena.alloc((size_t) W->nvec * N * 8);
+    W->part = (double*) arena.alloc((size_t) W->blocks * KV_MAXDOT * 8);
+    W->dred = (double*) arena.alloc(64 * 8);
+    W->dcoef = (double*) arena.alloc(64 * 8);
+    if (!W->vec || !W->part || !W->dred || !W->dcoef) {
+        delete W;
+        return nullptr;
+    }
+    return W;
+}
+
+void krylov_work_free(KrylovWork* W) { delete W; }
+
+bool krylov_work_fits(const KrylovWork* W, long long N, const KrylovParams& P) {
+    return W && W->N == N && W->nvec >= krylov_vectors(P) && W->kdim == P.kdim;
+}
+
+int krylov_run(KrylovOp& op, KrylovWork& W, opflow_ctx ctx, long long N, const KrylovParams& P, double* b, double* x, int* iters) {
+    if (P.kdim < 1 || P.kdim > 60) return fail(OPFLOW_E_INVALID, "GMRES restart length must be 1..60");
+    Ctx c{};
+    c.op = &op;
+    c.W = &W;
+    c.s = ctx->stream;
+    c.N = N;
+    c.grid = (int) std::max<long long>(1, std::min<long long>((N + KV_THREADS - 1) / KV_THREADS, (long long) ctx->num_sms * 8));
+    op.stream = c.s;
+    op.grid_hint = c.grid;
+    op.n = N;
+    switch (P.method) {
+        case OPFLOW_KRYLOV_GMRES: case OPFLOW_KRYLOV_FGMRES: case OPFLOW_KRYLOV_LGMRES: return fgmres(c, P, b, x, iters);
+        case OPFLOW_KRYLOV_BICGSTAB: return bicgstab(c, P, b, x, iters);
+        case OPFLOW_KRYLOV_PCG: return pcg(c, P, b, x, iters);
+        case OPFLOW_KRYLOV_NONE: return stationary(c, P, b, x, iters);
+    }
+    return fail(OPFLOW_E_INVALID, "unknown Krylov method %d", P.method);
+}
 
 void krylov_release(MGSystem* S) {
     delete S->kwork;
@@ -452,52 +532,25 @@ void krylov_release(MGSystem* S) {
 
 int krylov_solve(MGSystem* S, const KrylovParams& P, int* iters) {
     if (S->probs.size() != 1) return fail(OPFLOW_E_INVALID, "the host-driven Krylov methods solve one problem");
-    if (P.kdim < 1 || P.kdim > 60) return fail(OPFLOW_E_INVALID, "GMRES restart length must be 1..60");
     opflow_ctx ctx = S->ctx;
     const ProblemHost& Pr = S->probs[0];
     const KrylovDev& K = S->kd_host[0];
     const long long N = Pr.levels[0].N;
-    int nvec = 8;
-    if (P.method == OPFLOW_KRYLOV_GMRES || P.method == OPFLOW_KRYLOV_FGMRES || P.method == OPFLOW_KRYLOV_LGMRES) nvec = 2 * P.kdim + 2;
-    KrylovWork*& W = S->kwork;
-    if (W && (W->N != N || W->nvec < nvec || W->kdim != P.kdim)) krylov_release(S);
-    if (!W) {
-        W = new KrylovWork();
-        W->N = N;
-        W->nvec = nvec;
-        W->kdim = P.kdim;
-        W->blocks = std::max(1, ctx->num_sms * KV_BLOCKS_PER_SM);
-        W->vec = (double*) S->arena.alloc((size_t) nvec * N * 8);
-        W->part = (double*) S->arena.alloc((size_t) W->blocks * KV_MAXDOT * 8);
-        W->dred = (double*) S->arena.alloc(64 * 8);
-        W->dcoef = (double*) S->arena.alloc(64 * 8);
-        if (!W->vec || !W->part || !W->dred || !W->dcoef) {
-            krylov_release(S);
-            return fail(OPFLOW_E_NOMEM, "Krylov workspace");
-        }
+    if (!krylov_work_fits(S->kwork, N, P)) {
+        krylov_release(S);
+        S->kwork = krylov_work(S->arena, ctx, N, P);
+        if (!S->kwork) return fail(OPFLOW_E_NOMEM, "Krylov workspace");
     }
-    Ctx c{};
-    c.S = S;
-    c.W = W;
-    c.L0 = S->lv_host[Pr.lvl0];
-    c.s = ctx->stream;
-    c.N = N;
-    c.grid = (int) std::max<long long>(1, std::min<long long>((N + KV_THREADS - 1) / KV_THREADS, (long long) ctx->num_sms * 8));
-    c.precond = P.precond;
-    c.f32 = S->precision == OPFLOW_PREC_MIXED;
-    if (c.precond == OPFLOW_PRECOND_MG) {
-        // the V-cycle kernels skip problems whose Krylov state is inactive
-        Scal sc{};
-        sc.active = 1;
-        OPG_CUDA(cudaMemcpyAsync(S->dS, &sc, sizeof sc, cudaMemcpyHostToDevice, c.s));
-    }
-    switch (P.method) {
-        case OPFLOW_KRYLOV_GMRES: case OPFLOW_KRYLOV_FGMRES: case OPFLOW_KRYLOV_LGMRES: return fgmres(c, P, K.b, K.x, iters);
-        case OPFLOW_KRYLOV_BICGSTAB: return bicgstab(c, P, K.b, K.x, iters);
-        case OPFLOW_KRYLOV_PCG: return pcg(c, P, K.b, K.x, iters);
-        case OPFLOW_KRYLOV_NONE: return stationary(c, P, K.b, K.x, iters);
-    }
-    return fail(OPFLOW_E_INVALID, "unknown Krylov method %d", P.method);
+    MgOp op;
+    op.S = S;
+    op.L0 = S->lv_host[Pr.lvl0];
+    op.s = ctx->stream;
+    op.N = N;
+    op.grid = (int) std::max<long long>(1, std::min<long long>((N + KV_THREADS - 1) / KV_THREADS, (long long) ctx->num_sms * 8));
+    op.pc = P.precond;
+    op.f32 = S->precision == OPFLOW_PREC_MIXED;
+    if (op.pc == OPFLOW_PRECOND_MG) OPG_TRY(mg_activate(S));
+    return krylov_run(op, *S->kwork, ctx, N, P, K.b, K.x, iters);
 }
 
 }  // namespace opg

@@ -122,9 +122,30 @@ struct KrylovParams {
     int max_iter = 100;
     double tol = 1e-10, abs_tol = 0.;
 };
+// A linear operator with its preconditioner for the host-driven methods.  `residual` defaults to
+// matvec + r = b - A x; stream / grid_hint / n are set by krylov_run.
+struct KrylovOp {
+    cudaStream_t stream = nullptr;
+    int grid_hint = 1;
+    long long n = 0;
+    virtual ~KrylovOp() = default;
+    virtual int matvec(const double* x, double* y) = 0;
+    virtual int residual(const double* b, const double* x, double* r);
+    virtual int precond(const double* v, double* z) = 0;
+};
+// Workspace sized for P's method (carved from `arena`), and the method itself: x holds the initial
+// guess and receives the solution of A x = b.
+KrylovWork* krylov_work(Arena& arena, opflow_ctx ctx, long long N, const KrylovParams& P);
+bool krylov_work_fits(const KrylovWork* W, long long N, const KrylovParams& P);
+void krylov_work_free(KrylovWork* W);
+int krylov_run(KrylovOp& op, KrylovWork& W, opflow_ctx ctx, long long N, const KrylovParams& P, double* b, double* x, int* iters);
 // Solves the single problem of S in place (K.x holds the initial guess, K.b the right-hand side).
 int krylov_solve(MGSystem* S, const KrylovParams& P, int* iters);
 void krylov_release(MGSystem* S);
+// z = one V-cycle of S's single problem applied to v (level-0 vectors); mg_activate marks the
+// problem active for the V-cycle kernels first
+int mg_precond_level0(MGSystem* S, const double* v, double* z);
+int mg_activate(MGSystem* S);
 // one V-cycle on the level-0 input already written (b, x = 0)
 int mg_vcycle(MGSystem* S);
 

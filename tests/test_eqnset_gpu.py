@@ -1,0 +1,165 @@
+"""Coupled equation sets (the reference's SolveEqns / AMGCL path, eqnset.cu).
+
+- EqnSetTest's cases (src test/Core/Equation/EqnSetTest.cpp): copies of `1.0 == d2x(e) + d2y(e)` solved
+  as one system agree with the single-equation solve (Dirichlet) and with each other (pinned Neumann,
+  the CSR generator's last-row pin).
+- A genuinely coupled pair u, v: the engine's assembled CSR equals the oracle's StencilPad assembly of
+  every block, and the solution meets 1e-10 on that system.
+"""
+import numpy as np
+import pytest
+
+import common as cm
+import oracle_lib as orc
+from opflow_gb300 import _capi as capi
+from opflow_gb300 import api
+
+pytestmark = pytest.mark.gpu
+
+
+def _center_field(ctx, n, bc, name, value=0.0):
+    mesh = cm.mesh_uniform([n + 1, n + 1])
+    fd = cm.field_desc(2, capi.CENTER, [(bc, bc)] * 2, [(value, value)] * 2, ext=1)
+    f = api.CartesianField(mesh, fd, ctx, name)
+    f.assign(0.)
+    return f
+
+
+def _interior(f):
+    return f.download()[f.index_slices([tuple(f.info.assignable[d]) for d in range(2)])]
+
+
+@pytest.mark.parametrize("solver,precond", [("BICGSTAB", "PFMG"), ("GMRES", "PFMG"), ("PCG", "PFMG"), ("GMRES", "Jacobi")])
+def test_two_copies_of_a_dirichlet_poisson_equation(ctx, solver, precond):
+    n = 32
+    p, p2, pt = (_center_field(ctx, n, capi.BC_DIRC, nm) for nm in ("p", "p2", "pt"))
+    prm = api.StructSolverParams(tol=1e-12, maxIter=2000, solver=solver, precond=precond, kDim=30)
+    lap = lambda e: api.d2x(e) + api.d2y(e)
+    st = api.SolveEqns([lambda e, e2: api.Eq(1.0, lap(e)), lambda e, e2: api.Eq(1.0, lap(e2))], [p, p2], prm)
+    assert st.converged and st.relerr <= 1e-12, st
+    st1 = api.Solve(lambda e: api.Eq(1.0, lap(e)), pt, api.StructSolverParams(tol=1e-13, maxIter=200))
+    assert st1.converged
+    a, a2, at = _interior(p), _interior(p2), _interior(pt)
+    assert np.abs(a - at).max() <= 1e-9 * np.abs(at).max()
+    assert np.abs(a2 - at).max() <= 1e-9 * np.abs(at).max()
+
+
+def test_pinned_neumann_copies_agree_and_pin_the_last_cell(ctx):
+    n = 24
+    p, p2 = (_center_field(ctx, n, capi.BC_NEUM, nm) for nm in ("p", "p2"))
+    prm = api.StructSolverParams(tol=1e-12, maxIter=500, solver="BICGSTAB", precond="PFMG")
+    lap = lambda e: api.d2x(e) + api.d2y(e)
+    h = api.EqnSetSolveHandler([lambda e, e2: api.Eq(1.0, lap(e)), lambda e, e2: api.Eq(1.0, lap(e2))], [p, p2], prm, pins=[True, True])
+    st = h.solve()
+    assert st.converged, st
+    a, a2 = _interior(p), _interior(p2)
+    assert np.array_equal(a, a2)
+    assert a[-1, -1] == 0.0
+    # every other row of the (unpinned) reference system holds: assembled by the oracle
+    rp, cols, vals, rhs = h.csr()
+    N = n * n
+    assert rp[N] - rp[N - 1] == 1 and cols[rp[N - 1]] == N - 1 and vals[rp[N - 1]] == 1.0 and rhs[N - 1] == 0.0
+    hf = orc.HostField(p.mesh, p.desc, data=p.download())
+    L = cm.Leaf("p")
+    nodes, _ = api.serialize(api.Eq(1.0, lap(L)).residual_expr(), [L])
+    off, coef, b = orc.assemble(hf, nodes, [hf], 0, 0)
+    x = a.reshape(-1)
+    r = b.copy()
+    for e in range(off.shape[0]):
+        di, dj = int(off[e, 0]), int(off[e, 1])
+        xs = np.zeros((n, n))
+        src = a[max(0, dj):n + min(0, dj), max(0, di):n + min(0, di)]
+        xs[max(0, -dj):n - max(0, dj), max(0, -di):n - max(0, di)] = src
+        r -= coef[:, e] * xs.reshape(-1)
+    r[N - 1] = 0.
+    assert np.linalg.norm(r) <= 1e-10 * np.linalg.norm(b), np.linalg.norm(r) / np.linalg.norm(b)
+    del x
+
+
+def _oracle_blocks(fields, getters):
+    """Every block (k, j) of the coupled system assembled by the oracle (the other unknowns as zero
+    fields) as a dense matrix over the unknowns' cells, and each equation's right-hand side."""
+    n_eq = len(fields)
+    hosts = [orc.HostField(f.mesh, f.desc, data=f.download()) for f in fields]
+    zeros = []
+    for f in fields:
+        z = orc.HostField(f.mesh, f.desc)
+        z.update_padding()
+        zeros.append(z)
+    leaves = [cm.Leaf("u%d" % k) for k in range(n_eq)]
+    sizes = [int(np.prod([f.info.assignable[d][1] - f.info.assignable[d][0] for d in range(2)])) for f in fields]
+    N = sum(sizes)
+    A = np.zeros((N, N))
+    b = np.zeros(N)
+    offs = np.cumsum([0] + sizes)
+    for k in range(n_eq):
+        nodes, lv = api.serialize(getters[k](*leaves).residual_expr(), leaves)
+        known = [orc.HostField(g.mesh, g.desc, data=g.download()) for g in lv[n_eq:]]  # fields the equation reads
+        for j in range(n_eq):
+            if not any(nd.kind == capi.NODE_FIELD and nd.field == j for nd in nodes):
+                continue  # equation k does not involve unknown j
+            slots = [hosts[q] if q == j else zeros[q] for q in range(n_eq)] + known
+            off, coef, rhs = orc.assemble(hosts[j], nodes, slots, j, 0)
+            b[offs[k]:offs[k + 1]] = rhs
+            rng = hosts[j].assignable()
+            nx, ny = rng[0][1] - rng[0][0], rng[1][1] - rng[1][0]
+            for r in range(sizes[k]):
+                i, jj = r % nx, r // nx
+                for e in range(off.shape[0]):
+                    ci, cj = i + int(off[e, 0]), jj + int(off[e, 1])
+                    if coef[r, e] != 0.0:
+                        assert 0 <= ci < nx and 0 <= cj < ny
+                        A[offs[k] + r, offs[j] + cj * nx + ci] += coef[r, e]
+    return A, b
+
+
+def test_coupled_pair_matches_oracle_assembly_and_solves(ctx):
+    n = 16
+    u = _center_field(ctx, n, capi.BC_DIRC, "u", 0.5)
+    v = _center_field(ctx, n, capi.BC_DIRC, "v", -0.25)
+    f = _center_field(ctx, n, capi.BC_DIRC, "f")
+    rng = np.random.default_rng(4)
+    a = f.download()
+    sl = f.index_slices([tuple(f.info.assignable[d]) for d in range(2)])
+    a[sl] = rng.standard_normal(a[sl].shape)
+    f.upload(a)
+    lap = lambda e: api.d2x(e) + api.d2y(e)
+    getters = [lambda uu, vv: uu - 0.1 * lap(uu) + 0.3 * vv == f, lambda uu, vv: vv - 0.1 * lap(vv) - 0.3 * uu == 2.0 * f]
+    prm = api.StructSolverParams(tol=1e-12, maxIter=300, solver="GMRES", precond="PFMG", kDim=10)
+    h = api.EqnSetSolveHandler(getters, [u, v], prm)
+    st = h.solve()
+    assert st.converged and st.relerr <= 1e-12, st
+    A, b = _oracle_blocks([u, v], getters)
+    rp, cols, vals, rhs = h.csr()
+    dense = np.zeros_like(A)
+    for r in range(A.shape[0]):
+        for q in range(rp[r], rp[r + 1]):
+            dense[r, cols[q]] += vals[q]
+    assert np.array_equal(dense, A)
+    assert np.array_equal(rhs, b)
+    x = np.concatenate([_interior(u).reshape(-1), _interior(v).reshape(-1)])
+    assert np.linalg.norm(b - A @ x) <= 1e-10 * np.linalg.norm(b)
+    # a second solve with a new right-hand side re-assembles (the matrix is not static)
+    f.assign(f * 3.0)
+    st2 = h.solve()
+    assert st2.converged
+    A2, b2 = _oracle_blocks([u, v], getters)
+    x2 = np.concatenate([_interior(u).reshape(-1), _interior(v).reshape(-1)])
+    assert np.linalg.norm(b2 - A2 @ x2) <= 1e-10 * np.linalg.norm(b2)
+
+
+def test_three_equations_with_jacobi_and_static_matrix(ctx):
+    n = 12
+    fs = [_center_field(ctx, n, capi.BC_DIRC, "p%d" % k, 0.1 * k) for k in range(3)]
+    lap = lambda e: api.d2x(e) + api.d2y(e)
+    getters = [lambda a, b, c: a - 0.05 * lap(a) + 0.1 * b == 1.0,
+               lambda a, b, c: b - 0.05 * lap(b) + 0.1 * c - 0.1 * a == 2.0,
+               lambda a, b, c: c - 0.05 * lap(c) - 0.1 * b == 3.0]
+    prm = api.StructSolverParams(tol=1e-12, maxIter=500, solver="BICGSTAB", precond="Jacobi", staticMat=True)
+    h = api.EqnSetSolveHandler(getters, fs, prm)
+    for _ in range(2):
+        st = h.solve()
+        assert st.converged, st
+        A, b = _oracle_blocks(fs, getters)
+        x = np.concatenate([_interior(f).reshape(-1) for f in fs])
+        assert np.linalg.norm(b - A @ x) <= 1e-10 * np.linalg.norm(b)
