@@ -11,30 +11,52 @@
 namespace opg {
 
 // ---- chunked kernels (large levels)
+// A chunk is one row segment (nrows == 1: the CTA's threads stride along it) or several whole rows of
+// one plane (one warp per row, lanes along the row), so short rows still fill the CTA.  `color` >= 0
+// visits only the cells of that red-black color.
+template <typename F>
+__device__ __forceinline__ void chunk_cells(const Chunk& C, int color, F&& f) {
+    if (C.nrows == 1) {
+        if (color < 0) {
+            for (int t = threadIdx.x; t < C.cnt; t += blockDim.x) f(C.i0 + t, C.j);
+        } else {
+            const int first = (C.i0 + C.j + C.k + color) & 1;
+            for (int t = 2 * threadIdx.x + first; t < C.cnt; t += 2 * blockDim.x) f(C.i0 + t, C.j);
+        }
+        return;
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int r = warp; r < C.nrows; r += nw) {
+        const int j = C.j + r;
+        if (color < 0) {
+            for (int t = lane; t < C.cnt; t += 32) f(C.i0 + t, j);
+        } else {
+            const int first = (C.i0 + j + C.k + color) & 1;
+            for (int t = first + 2 * lane; t < C.cnt; t += 64) f(C.i0 + t, j);
+        }
+    }
+}
+
 template <typename T>
-__global__ void __launch_bounds__(256) mg_residual(const LvlDev* __restrict__ Ls, const Chunk* __restrict__ ch, int nch, const Scal* sc) {
+__global__ void __launch_bounds__(256, 4) mg_residual(const LvlDev* __restrict__ Ls, const Chunk* __restrict__ ch, int nch, const Scal* sc) {
     for (int c = blockIdx.x; c < nch; c += gridDim.x) {
         const Chunk C = ch[c];
         if (!active(Ls, C, sc)) continue;
         const LvlDev& L = Ls[C.lvl];
-        for (int t = threadIdx.x; t < C.cnt; t += blockDim.x) cell_residual<T>(L, C.i0 + t, C.j, C.k);
+        chunk_cells(C, -1, [&](int i, int j) { cell_residual<T>(L, i, j, C.k); });
     }
 }
 
 // Red-black Gauss-Seidel half sweep (cells with (i+j+k)%2 == color), or for Jacobi levels:
 // color 0 computes r = b - A x, color 1 applies x += omega r / diag.
 template <typename T>
-__global__ void __launch_bounds__(256) mg_smooth(const LvlDev* __restrict__ Ls, const Chunk* __restrict__ ch, int nch, int color, const Scal* sc) {
+__global__ void __launch_bounds__(256, 4) mg_smooth(const LvlDev* __restrict__ Ls, const Chunk* __restrict__ ch, int nch, int color, const Scal* sc) {
     for (int c = blockIdx.x; c < nch; c += gridDim.x) {
         const Chunk C = ch[c];
         if (!active(Ls, C, sc)) continue;
         const LvlDev& L = Ls[C.lvl];
-        if (L.rbgs) {
-            const int first = (C.i0 + C.j + C.k + color) & 1;  // offset of the first cell of this color
-            for (int t = 2 * threadIdx.x + first; t < C.cnt; t += 2 * blockDim.x) cell_gs<T>(L, C.i0 + t, C.j, C.k);
-        } else {
-            for (int t = threadIdx.x; t < C.cnt; t += blockDim.x) cell_jacobi<T>(L, C.i0 + t, C.j, C.k, color);
-        }
+        if (L.rbgs) chunk_cells(C, color, [&](int i, int j) { cell_gs<T>(L, i, j, C.k); });
+        else chunk_cells(C, -1, [&](int i, int j) { cell_jacobi<T>(L, i, j, C.k, color); });
     }
 }
 
@@ -45,7 +67,7 @@ __global__ void __launch_bounds__(256) mg_restrict(const LvlDev* __restrict__ Ls
         const Chunk C = ch[c];
         if (!active(Ls, C, sc)) continue;
         const LvlDev& Lc = Ls[C.lvl];
-        for (int t = threadIdx.x; t < C.cnt; t += blockDim.x) cell_restrict<T>(Ls, Lc, C.i0 + t, C.j, C.k);
+        chunk_cells(C, -1, [&](int i, int j) { cell_restrict<T>(Ls, Lc, i, j, C.k); });
     }
 }
 
@@ -56,7 +78,7 @@ __global__ void __launch_bounds__(256) mg_prolong(const LvlDev* __restrict__ Ls,
         const Chunk C = ch[c];
         if (!active(Ls, C, sc)) continue;
         const LvlDev& Lf = Ls[C.lvl];
-        for (int t = threadIdx.x; t < C.cnt; t += blockDim.x) cell_prolong<T>(Ls, Lf, C.i0 + t, C.j, C.k);
+        chunk_cells(C, -1, [&](int i, int j) { cell_prolong<T>(Ls, Lf, i, j, C.k); });
     }
 }
 

@@ -524,11 +524,26 @@ int mg_finalize(MGSystem* S) {
     std::vector<int> coarse_list;
     std::vector<Chunk> k0;
     std::vector<int> first, count;
-    const int CH = 1024;
+    // V-cycle chunks: rows of at least CH cells are split into segments of CH; shorter rows are grouped,
+    // whole rows of one plane, into chunks of about CH2 cells (one warp per row in the kernels), as far
+    // as the level still has two chunks per SM (a level of few rows keeps one row per chunk)
+    const int CH = 1024, CH2 = 2048;
     auto rows = [&](int lvl_index, const LvlDev& L, std::vector<Chunk>& out) {
-        for (int k = 0; k < (L.ndim > 2 ? L.n[2] : 1); ++k)
-            for (int j = 0; j < (L.ndim > 1 ? L.n[1] : 1); ++j)
-                for (int i0 = 0; i0 < L.n[0]; i0 += CH) out.push_back(Chunk{lvl_index, j, k, i0, std::min(CH, L.n[0] - i0)});
+        const int ny = L.ndim > 1 ? L.n[1] : 1, nz = L.ndim > 2 ? L.n[2] : 1;
+        if (L.n[0] >= CH) {
+            for (int k = 0; k < nz; ++k)
+                for (int j = 0; j < ny; ++j)
+                    for (int i0 = 0; i0 < L.n[0]; i0 += CH) out.push_back(Chunk{lvl_index, j, k, i0, std::min(CH, L.n[0] - i0)});
+            return;
+        }
+        const long long all_rows = (long long) ny * nz;
+        const int per = (int) std::max<long long>(1, std::min<long long>(CH2 / L.n[0], all_rows / (2LL * ctx->num_sms)));
+        for (int k = 0; k < nz; ++k)
+            for (int j = 0; j < ny; j += per) {
+                Chunk c{lvl_index, j, k, 0, L.n[0]};
+                c.nrows = std::min(per, ny - j);
+                out.push_back(c);
+            }
     };
     if (const char* e = getenv("OPFLOW_MG_BOTTOM")) S->bottom_max = atoll(e);
     // level-0 chunks of the Krylov kernels: whole rows of one plane, about KCH cells each (rows longer
