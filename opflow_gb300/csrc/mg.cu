@@ -8,6 +8,8 @@
 // the Krylov vectors, their updates and all inner products are float64.
 #include "mg_device.h"
 
+#include <type_traits>
+
 namespace opg {
 
 // ---- chunked kernels (large levels)
@@ -60,6 +62,61 @@ __global__ void __launch_bounds__(256, 4) mg_smooth(const LvlDev* __restrict__ L
     }
 }
 
+// Red-black Gauss-Seidel half sweep of a 3D class-table level, marching along z: a CTA owns a tile of
+// MG_ZT_X computed x-columns (lanes 1..30 of each warp; lanes 0 and 31 only hold the neighbouring
+// columns) by MG_ZT_Y rows (one warp each) and a run of planes.  Each thread keeps its column's x at
+// planes k-1, k, k+1 in registers, takes the x-neighbours from the adjacent lanes and the y-neighbours
+// from the cache, so x is streamed once per half sweep.  The cells of one colour only read cells of
+// the other, so the in-place update needs no barrier.  Interior cells use the interior class's
+// coefficients with the chunked kernel's operations in its order (bit-identical results); boundary
+// cells take the general per-cell path.  (Levels with coefficient arrays stay on the chunked kernel:
+// with seven more streams per cell the march was measured slower.)  Tiles: Chunk{lvl, j = y origin, k = first plane,
+// i0 = x origin, cnt = MG_ZT_X, nrows = planes}.
+template <typename T>
+__global__ void __launch_bounds__(32 * MG_ZT_Y) mg_smooth_z(const LvlDev* __restrict__ Ls, const Chunk* __restrict__ ch, int nch, int color,
+                                                           const Scal* sc) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int c = blockIdx.x; c < nch; c += gridDim.x) {
+        const Chunk C = ch[c];
+        if (!active(Ls, C, sc)) continue;
+        const LvlDev& L = Ls[C.lvl];
+        const int n0 = L.n[0], n1 = L.n[1], n2 = L.n[2];
+        const long long sy = n0, sz = (long long) n0 * n1;
+        const int i = C.i0 - 1 + lane, j = C.j + warp;
+        const bool col_ok = i >= 0 && i < n0 && j < n1;
+        const bool computes = col_ok && lane >= 1 && lane <= MG_ZT_X;
+        T* x = Sel<T>::x(L);
+        const T* b = Sel<T>::b(L);
+        const T* t = Sel<T>::Tb(L) + 13 * TSTRIDE;  // the interior class (1 + 3 + 9)
+        const T c1 = t[1], c2 = t[2], c3 = t[3], c4 = t[4], c5 = t[5], c6 = t[6], cinv = t[NSLOT];
+        const long long col = col_ok ? (long long) i + sy * j : 0;
+        const int k0 = C.k, k1 = min(C.k + C.nrows, n2);
+        T xm = (col_ok && k0 > 0) ? x[col + sz * (k0 - 1)] : (T) 0;
+        T xc = col_ok ? x[col + sz * k0] : (T) 0;
+        for (int k = k0; k < k1; ++k) {
+            const T xp = (col_ok && k + 1 < n2) ? x[col + sz * (k + 1)] : (T) 0;
+            const T xw = __shfl_up_sync(0xffffffffu, xc, 1), xe = __shfl_down_sync(0xffffffffu, xc, 1);
+            if (computes && ((i + j + k + color) & 1) == 0) {
+                const long long cell = col + sz * k;
+                if (i > 0 && i < n0 - 1 && j > 0 && j < n1 - 1 && k > 0 && k < n2 - 1) {
+                    T acc = 0;
+                    acc += c1 * xw;
+                    acc += c2 * xe;
+                    acc += c3 * x[cell - sy];
+                    acc += c4 * x[cell + sy];
+                    acc += c5 * xm;
+                    acc += c6 * xp;
+                    x[cell] = (b[cell] - acc) * cinv;
+                } else {
+                    cell_gs<T>(L, i, j, k);
+                }
+            }
+            xm = xc;
+            xc = xp;
+        }
+    }
+}
+
 // coarse b = R r_fine, coarse x = 0; chunks are coarse rows
 template <typename T>
 __global__ void __launch_bounds__(256) mg_restrict(const LvlDev* __restrict__ Ls, const Chunk* __restrict__ ch, int nch, const Scal* sc) {
@@ -78,7 +135,7 @@ __global__ void __launch_bounds__(256) mg_prolong(const LvlDev* __restrict__ Ls,
         const Chunk C = ch[c];
         if (!active(Ls, C, sc)) continue;
         const LvlDev& Lf = Ls[C.lvl];
-        chunk_cells(C, -1, [&](int i, int j) { cell_prolong<T>(Ls, Lf, i, j, C.k); });
+        chunk_cells(C, -1, [&](int i, int j) { cell_prolong<T, std::is_same<T, float>::value>(Ls, Lf, i, j, C.k); });
     }
 }
 
@@ -501,6 +558,13 @@ int mg_launch_smooth(cudaStream_t s, int sms, bool f32, const LvlDev* L, const C
     else mg_smooth<double><<<grid_of(nch, sms), 256, 0, s>>>(L, ch, nch, color, sc);
     OPG_LAUNCHED();
     return check_launch("mg_smooth");
+}
+int mg_launch_smooth_z(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* ch, int nch, int color, const Scal* sc) {
+    if (nch <= 0) return OPFLOW_OK;
+    if (f32) mg_smooth_z<float><<<grid_of(nch, sms), 32 * MG_ZT_Y, 0, s>>>(L, ch, nch, color, sc);
+    else mg_smooth_z<double><<<grid_of(nch, sms), 32 * MG_ZT_Y, 0, s>>>(L, ch, nch, color, sc);
+    OPG_LAUNCHED();
+    return check_launch("mg_smooth_z");
 }
 int mg_launch_restrict(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* ch, int nch, const Scal* sc) {
     if (nch <= 0) return OPFLOW_OK;

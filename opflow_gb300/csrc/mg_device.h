@@ -173,8 +173,10 @@ __device__ __forceinline__ T coarse_at(const LvlDev& Lc, const T* xc, int I0, in
     return xc[cell_of(Lc, I[0], I[1], I[2])];
 }
 
-// fine x += P x_coarse at fine cell f
-template <typename T>
+// fine x += P x_coarse at fine cell f.  FAST adds a path for cell-centred fine cells whose coarse
+// neighbours are all inside the box (the same terms in the same order, sign 1); the chunked
+// float32 prolongation uses it, the tile and bottom kernels (tight on registers) do not.
+template <typename T, bool FAST = false>
 __device__ __forceinline__ T prolong_acc(const LvlDev* __restrict__ Ls, const LvlDev& Lf, int f0, int f1, int f2) {
     const LvlDev& Lc = Ls[Lf.coarse];
     const T* xc = Sel<T>::x(Lc);
@@ -188,6 +190,20 @@ __device__ __forceinline__ T prolong_acc(const LvlDev* __restrict__ Ls, const Lv
             J[d] = (f[d] & 1) ? I[d] + 1 : I[d] - 1;
         }
         const int nz = Lc.ndim > 2 ? 2 : 1, ny = Lc.ndim > 1 ? 2 : 1;
+        bool inside = FAST;
+        for (int d = 0; FAST && d < Lc.ndim; ++d) inside = inside && I[d] >= 0 && I[d] < Lc.n[d] && J[d] >= 0 && J[d] < Lc.n[d];
+        if (FAST && inside) {
+            // every coarse neighbour inside the box: the terms below with sign 1, in their order
+            for (int a = 0; a < nz; ++a)
+                for (int bb = 0; bb < ny; ++bb)
+                    for (int e = 0; e < 2; ++e) {
+                        const T w = (e ? (T) 0.25 : (T) 0.75) * (Lc.ndim > 1 ? (bb ? (T) 0.25 : (T) 0.75) : (T) 1) *
+                                    (Lc.ndim > 2 ? (a ? (T) 0.25 : (T) 0.75) : (T) 1);
+                        const T v = xc[cell_of(Lc, e ? J[0] : I[0], Lc.ndim > 1 ? (bb ? J[1] : I[1]) : 0, Lc.ndim > 2 ? (a ? J[2] : I[2]) : 0)];
+                        acc += w * (T) 1 * v;
+                    }
+            return acc;
+        }
         for (int a = 0; a < nz; ++a)
             for (int bb = 0; bb < ny; ++bb)
                 for (int e = 0; e < 2; ++e) {
@@ -230,9 +246,9 @@ __device__ __forceinline__ T prolong_acc(const LvlDev* __restrict__ Ls, const Lv
     return acc;
 }
 
-template <typename T>
+template <typename T, bool FAST = false>
 __device__ __forceinline__ void cell_prolong(const LvlDev* __restrict__ Ls, const LvlDev& Lf, int f0, int f1, int f2) {
-    const T acc = prolong_acc<T>(Ls, Lf, f0, f1, f2);
+    const T acc = prolong_acc<T, FAST>(Ls, Lf, f0, f1, f2);
     Sel<T>::x(Lf)[cell_of(Lf, f0, f1, f2)] += acc;
 }
 

@@ -5,6 +5,12 @@
 namespace opg {
 int mg_launch_residual(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* ch, int nch, const Scal* sc);
 int mg_launch_smooth(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* ch, int nch, int color, const Scal* sc);
+// red-black half sweep of 3D class-table levels marching along z (tiles: Chunk{lvl, j = y origin,
+// k = first plane, i0 = x origin, cnt = MG_ZT_X, nrows = planes}); used for 3D levels of at least
+// MG_ZT_MIN cells with at least 3 cells along every dim
+constexpr int MG_ZT_X = 30, MG_ZT_Y = 8, MG_ZT_Z = 32;
+constexpr long long MG_ZT_MIN = 32768;
+int mg_launch_smooth_z(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* ch, int nch, int color, const Scal* sc);
 int mg_launch_restrict(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* ch, int nch, const Scal* sc);
 int mg_launch_prolong(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* ch, int nch, const Scal* sc);
 // fused 2D tile steps of a level (mg_tiles.cu): down = pre-smoothing + residual + restriction,

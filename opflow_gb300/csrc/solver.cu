@@ -512,6 +512,7 @@ int mg_finalize(MGSystem* S) {
     S->restrict_ch.assign(S->nlevels, {});
     S->prolong_ch.assign(S->nlevels, {});
     S->tile_ch.assign(S->nlevels, {});
+    S->zsm_ch.assign(S->nlevels, {});
     S->coarse_sm_ch.clear();
     S->bottom_host.clear();
     S->bottom_cells_host.clear();
@@ -521,6 +522,8 @@ int mg_finalize(MGSystem* S) {
     // repeated sweeps cost more than the saved passes over memory (measured)
     bool tiles_on = f32 && !(te && te[0] == '0') && mg_tiles_supported(S->pre) && mg_tiles_supported(S->post);
     if (tiles_on) OPG_TRY(mg_tiles_prepare(std::max(S->pre, S->post)));
+    const char* ze = getenv("OPFLOW_MG_ZMARCH");
+    const bool zoff = ze && ze[0] == '0';
     std::vector<int> coarse_list;
     std::vector<Chunk> k0;
     std::vector<int> first, count;
@@ -654,7 +657,23 @@ int mg_finalize(MGSystem* S) {
                         S->tile_ch[l].push_back(c);
                     }
             } else {
-                if (!D.coarsest) rows(li, D, S->smooth_ch[l]);
+                const bool zmarch = !zoff && D.ndim == 3 && D.table && D.rbgs && !D.coarsest && D.N >= MG_ZT_MIN && D.n[0] >= 3 && D.n[1] >= 3 &&
+                                    D.n[2] >= 3;
+                // planes per tile: up to MG_ZT_Z, fewer where the level would otherwise have fewer than
+                // four tiles per SM (a short march leaves SMs idle); below 4 planes the chunked kernel
+                const long long txy = (long long) ((D.n[0] + MG_ZT_X - 1) / MG_ZT_X) * ((D.n[1] + MG_ZT_Y - 1) / MG_ZT_Y);
+                const int zz = (int) std::min<long long>(MG_ZT_Z, (long long) D.n[2] * txy / (4LL * ctx->num_sms));
+                if (zmarch && zz >= 4) {
+                    for (int k0 = 0; k0 < D.n[2]; k0 += zz)
+                        for (int j0 = 0; j0 < D.n[1]; j0 += MG_ZT_Y)
+                            for (int i0 = 0; i0 < D.n[0]; i0 += MG_ZT_X) {
+                                Chunk c{li, j0, k0, i0, MG_ZT_X};
+                                c.nrows = std::min(zz, D.n[2] - k0);
+                                S->zsm_ch[l].push_back(c);
+                            }
+                } else if (!D.coarsest) {
+                    rows(li, D, S->smooth_ch[l]);
+                }
                 if (!D.coarsest) rows(li, D, S->prolong_ch[l]);  // fine rows of level l (prolonged from l+1)
             }
             if (l > 0 && !above_tiled) rows(li, D, S->restrict_ch[l]);  // coarse rows of level l (restricted from l-1)
@@ -720,11 +739,13 @@ int mg_finalize(MGSystem* S) {
     S->d_restrict.assign(S->nlevels, {});
     S->d_prolong.assign(S->nlevels, {});
     S->d_tiles.assign(S->nlevels, {});
+    S->d_zsm.assign(S->nlevels, {});
     for (int l = 0; l < S->nlevels; ++l) {
         upload(S->smooth_ch[l], S->d_smooth[l]);
         upload(S->restrict_ch[l], S->d_restrict[l]);
         upload(S->prolong_ch[l], S->d_prolong[l]);
         upload(S->tile_ch[l], S->d_tiles[l]);
+        upload(S->zsm_ch[l], S->d_zsm[l]);
     }
     upload(S->coarse_sm_ch, S->d_coarse_sm);
     S->kd_host = kd;
@@ -752,9 +773,12 @@ static int vcycle(MGSystem* S) {
         if (l > 0) OPG_TRY(mg_launch_restrict(s, sms, f32, S->dL, S->d_restrict[l].ptr, S->d_restrict[l].n, sc));
         OPG_TRY(mg_launch_tile_down(s, sms, f32, S->dL, S->d_tiles[l].ptr, S->d_tiles[l].n, sc, S->pre));
         const ChunkList& C = S->d_smooth[l];
+        const ChunkList& Z = S->d_zsm[l];
         for (int it = 0; it < S->pre; ++it) {
             OPG_TRY(mg_launch_smooth(s, sms, f32, S->dL, C.ptr, C.n, 0, sc));
+            OPG_TRY(mg_launch_smooth_z(s, sms, f32, S->dL, Z.ptr, Z.n, 0, sc));
             OPG_TRY(mg_launch_smooth(s, sms, f32, S->dL, C.ptr, C.n, 1, sc));
+            OPG_TRY(mg_launch_smooth_z(s, sms, f32, S->dL, Z.ptr, Z.n, 1, sc));
         }
         if (S->d_prolong[l].n) OPG_TRY(mg_launch_residual(s, sms, f32, S->dL, S->d_prolong[l].ptr, S->d_prolong[l].n, sc));
     }
@@ -768,9 +792,12 @@ static int vcycle(MGSystem* S) {
         OPG_TRY(mg_launch_tile_up(s, sms, f32, S->dL, S->d_tiles[l].ptr, S->d_tiles[l].n, sc, S->post));
         OPG_TRY(mg_launch_prolong(s, sms, f32, S->dL, S->d_prolong[l].ptr, S->d_prolong[l].n, sc));
         const ChunkList& C = S->d_smooth[l];
+        const ChunkList& Z = S->d_zsm[l];
         for (int it = 0; it < S->post; ++it) {
             OPG_TRY(mg_launch_smooth(s, sms, f32, S->dL, C.ptr, C.n, 1, sc));
+            OPG_TRY(mg_launch_smooth_z(s, sms, f32, S->dL, Z.ptr, Z.n, 1, sc));
             OPG_TRY(mg_launch_smooth(s, sms, f32, S->dL, C.ptr, C.n, 0, sc));
+            OPG_TRY(mg_launch_smooth_z(s, sms, f32, S->dL, Z.ptr, Z.n, 0, sc));
         }
     }
     return OPFLOW_OK;
@@ -1020,6 +1047,7 @@ int mg_compose(MGSystem* C, const std::vector<MGSystem*>& parts, const std::vect
     C->restrict_ch.assign(C->nlevels, {});
     C->prolong_ch.assign(C->nlevels, {});
     C->tile_ch.assign(C->nlevels, {});
+    C->zsm_ch.assign(C->nlevels, {});
     C->coarse_sm_ch.clear();
     for (size_t q = 0; q < parts.size(); ++q) {
         MGSystem* P = parts[q];
@@ -1045,6 +1073,7 @@ int mg_compose(MGSystem* C, const std::vector<MGSystem*>& parts, const std::vect
             shift(P->restrict_ch[l], C->restrict_ch[l]);
             shift(P->prolong_ch[l], C->prolong_ch[l]);
             shift(P->tile_ch[l], C->tile_ch[l]);
+            shift(P->zsm_ch[l], C->zsm_ch[l]);
         }
         shift(P->coarse_sm_ch, C->coarse_sm_ch);
         KrylovDev K = P->kd_host[0];
@@ -1097,11 +1126,13 @@ int mg_compose(MGSystem* C, const std::vector<MGSystem*>& parts, const std::vect
     C->d_restrict.assign(C->nlevels, {});
     C->d_prolong.assign(C->nlevels, {});
     C->d_tiles.assign(C->nlevels, {});
+    C->d_zsm.assign(C->nlevels, {});
     for (int l = 0; l < C->nlevels; ++l) {
         upload(C->smooth_ch[l], C->d_smooth[l]);
         upload(C->restrict_ch[l], C->d_restrict[l]);
         upload(C->prolong_ch[l], C->d_prolong[l]);
         upload(C->tile_ch[l], C->d_tiles[l]);
+        upload(C->zsm_ch[l], C->d_zsm[l]);
     }
     upload(C->coarse_sm_ch, C->d_coarse_sm);
     C->kd_host = kd;

@@ -69,6 +69,9 @@ struct MGSystem {
     // tiles of the levels run by the fused 2D tile kernels (such levels are in none of the lists above)
     std::vector<std::vector<Chunk>> tile_ch;
     std::vector<ChunkList> d_tiles;
+    // tiles of the 3D levels smoothed by the z-marching kernel (such levels are not in smooth_ch)
+    std::vector<std::vector<Chunk>> zsm_ch;
+    std::vector<ChunkList> d_zsm;
     std::vector<Chunk> coarse_sm_ch;
     ChunkList d_coarse_sm;
     LvlDev* dL = nullptr;
