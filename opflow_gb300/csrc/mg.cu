@@ -91,28 +91,34 @@ __global__ void __launch_bounds__(32 * MG_ZT_Y) mg_smooth_z(const LvlDev* __rest
         const T c1 = t[1], c2 = t[2], c3 = t[3], c4 = t[4], c5 = t[5], c6 = t[6], cinv = t[NSLOT];
         const long long col = col_ok ? (long long) i + sy * j : 0;
         const int k0 = C.k, k1 = min(C.k + C.nrows, n2);
-        T xm = (col_ok && k0 > 0) ? x[col + sz * (k0 - 1)] : (T) 0;
-        T xc = col_ok ? x[col + sz * k0] : (T) 0;
+        const bool ij_inner = i > 0 && i < n0 - 1 && j > 0 && j < n1 - 1;
+        T* xk = x + col + sz * k0;  // this column at plane k (dereferenced only where col_ok)
+        const T* bk = b + col + sz * k0;
+        T xm = (col_ok && k0 > 0) ? xk[-sz] : (T) 0;
+        T xc = col_ok ? *xk : (T) 0;
+        int parity = (i + j + k0 + color) & 1;
         for (int k = k0; k < k1; ++k) {
-            const T xp = (col_ok && k + 1 < n2) ? x[col + sz * (k + 1)] : (T) 0;
+            const T xp = (col_ok && k + 1 < n2) ? xk[sz] : (T) 0;
             const T xw = __shfl_up_sync(0xffffffffu, xc, 1), xe = __shfl_down_sync(0xffffffffu, xc, 1);
-            if (computes && ((i + j + k + color) & 1) == 0) {
-                const long long cell = col + sz * k;
-                if (i > 0 && i < n0 - 1 && j > 0 && j < n1 - 1 && k > 0 && k < n2 - 1) {
+            if (computes && parity == 0) {
+                if (ij_inner && k > 0 && k < n2 - 1) {
                     T acc = 0;
                     acc += c1 * xw;
                     acc += c2 * xe;
-                    acc += c3 * x[cell - sy];
-                    acc += c4 * x[cell + sy];
+                    acc += c3 * xk[-sy];
+                    acc += c4 * xk[sy];
                     acc += c5 * xm;
                     acc += c6 * xp;
-                    x[cell] = (b[cell] - acc) * cinv;
+                    *xk = (*bk - acc) * cinv;
                 } else {
                     cell_gs<T>(L, i, j, k);
                 }
             }
             xm = xc;
             xc = xp;
+            xk += sz;
+            bk += sz;
+            parity ^= 1;
         }
     }
 }
