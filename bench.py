@@ -17,6 +17,7 @@ Workloads (seeded synthetic inputs with the configurations' shapes and value dis
           server's host-to-host solves/s with p50/p99 at the highest rate, next to plain FP64 serving
           one request at a time (the whole sweep is in config)
   poisson3d  div(exp(g) grad p) = f on 256^3 cells, Neumann, pinned, mixed next to plain FP64
+          (--const-coef: d2x + d2y + d2z instead, the serving workload's 3D operator)
   batched 512 corner-node Dirichlet problems (I - k Lap) u = f of sides 65..1025 in one batched
           solve, mixed precision, next to a loop of plain FP64 single solves
   weno    WENO5-JS + RK3 on 65536 periodic lines of 4096 cells (one RK3 step per bench step)
@@ -465,6 +466,8 @@ def run_poisson3d(args, torch, api, capi, np, ctx, stream, world, rank, local):
     f.upload(ff)
     getter = lambda e: f == (api.dx(api.d1IntpCenterToCorner(K, 0) * api.dx(e)) + api.dy(api.d1IntpCenterToCorner(K, 1) * api.dy(e))
                              + api.dz(api.d1IntpCenterToCorner(K, 2) * api.dz(e)))
+    if args.const_coef:
+        getter = lambda e: f == api.d2x(e) + api.d2y(e) + api.d2z(e)
     out = {}
     for prec in ("mixed", "fp64"):
         h = api.makeEqnSolveHandler(getter, p, api.StructSolverParams(tol=1e-10, maxIter=300, pinValue=True, staticMat=True,
@@ -495,12 +498,13 @@ def run_poisson3d(args, torch, api, capi, np, ctx, stream, world, rank, local):
     h.close()
     m = out["mixed"]
     N = n ** 3
-    bpc = ITER_BYTES_PER_CELL + 8.0 * 7 * 2  # + the seven float64 operator arrays read by two level-0 passes
+    bpc = ITER_BYTES_PER_CELL + (0.0 if args.const_coef else 8.0 * 7 * 2)  # + the seven float64 operator arrays read by two level-0 passes
     achieved = bpc * N * m["iterations"] / (m["ms_per_solve"] * 1e-3) / 1e9
     peak, src = peak_hbm()
     return dict(value=m["solves_per_s"], unit="solves/s", ms=m["ms_per_solve"], launches=m["launches"], dtype="f64 outer / f32 V-cycle",
                 config=dict(workload="poisson3d", grid=[n, n, n], loc="cell", bc="neumann 0, pinned",
-                            coefficient="exp(g), g smooth seeded Fourier field of std 1, interpolated to faces", tol=1e-10,
+                            coefficient="1 (d2x + d2y + d2z)" if args.const_coef else "exp(g), g smooth seeded Fourier field of std 1, interpolated to faces",
+                            tol=1e-10,
                             mixed=m, fp64=out["fp64"], mixed_over_fp64=m["solves_per_s"] / out["fp64"]["solves_per_s"],
                             l2="level-0 vectors %.0f MB each (> L2)" % (N * 8 / 1e6)),
                 roofline={"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": src,
@@ -896,6 +900,7 @@ def main():
     ap.add_argument("--grid", type=int, default=0, help="override the grid side (profiling a smaller case)")
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU baseline leg (profiling runs)")
     ap.add_argument("--sweeps", type=int, default=2, help="poisson2d: red-black Gauss-Seidel sweeps before and after each coarsening")
+    ap.add_argument("--const-coef", action="store_true", help="poisson3d: constant coefficient (the serving workload's 3D operator)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
