@@ -8,6 +8,7 @@
 // the Krylov vectors, their updates and all inner products are float64.
 #include "mg_device.h"
 
+#include <cstdlib>
 #include <type_traits>
 
 namespace opg {
@@ -62,20 +63,56 @@ __global__ void __launch_bounds__(256, 4) mg_smooth(const LvlDev* __restrict__ L
     }
 }
 
+// Cells of a z tile that take the general per-cell path (boundary faces), queued during the march and
+// updated by the whole CTA after it: a boundary column would otherwise hold its warp for every plane
+// of the tile.  Deferring them is exact for the three z kernels: a half sweep's cells only read cells
+// of the other colour, and the residual and prolongation write nothing they read.
+struct ZQueue {
+    unsigned n;
+    unsigned short cell[MG_ZT_X * MG_ZT_Y * MG_ZT_Z];  // (plane offset << 8) | (row << 5) | lane
+};
+static_assert(MG_ZT_Y <= 8 && MG_ZT_Z <= 256, "queue entries hold the row in 3 bits and the plane offset in 8");
+
+__device__ __forceinline__ void zq_push(ZQueue& Q, unsigned planes, int koff, int warp, int lane) {
+    if (!planes) return;
+    unsigned slot = atomicAdd(&Q.n, (unsigned) __popc(planes));
+    for (; planes; planes &= planes - 1) Q.cell[slot++] = (unsigned short) (((koff + __ffs(planes) - 1) << 8) | (warp << 5) | lane);
+}
+
+// after the march: every thread of the CTA takes queued cells; leaves the queue empty
+template <typename F>
+__device__ __forceinline__ void zq_drain(ZQueue& Q, const Chunk& C, F&& fn) {
+    __syncthreads();
+    const unsigned n = Q.n;
+    __syncthreads();
+    if (threadIdx.x == 0) Q.n = 0;
+    for (unsigned e = threadIdx.x; e < n; e += blockDim.x) {
+        const unsigned v = Q.cell[e];
+        fn(C.i0 - 1 + (int) (v & 31), C.j + (int) ((v >> 5) & 7), C.k + (int) (v >> 8));
+    }
+    __syncthreads();
+}
+
 // Red-black Gauss-Seidel half sweep of a 3D class-table level, marching along z: a CTA owns a tile of
 // MG_ZT_X computed x-columns (lanes 1..30 of each warp; lanes 0 and 31 only hold the neighbouring
-// columns) by MG_ZT_Y rows (one warp each) and a run of planes.  Each thread keeps its column's x at
-// planes k-1, k, k+1 in registers, takes the x-neighbours from the adjacent lanes and the y-neighbours
-// from the cache, so x is streamed once per half sweep.  The cells of one colour only read cells of
-// the other, so the in-place update needs no barrier.  Interior cells use the interior class's
+// columns) by MG_ZT_Y rows (one warp each) and a run of planes.  Each thread walks its column upward
+// in batches of ZB planes: it first issues every load of the batch (x at the next ZB planes, and b and
+// the two y-neighbours of the cells it updates), then updates the batch's cells with the x-neighbours
+// taken from the adjacent lanes, so x is streamed once per half sweep with ZB planes of loads in
+// flight per thread.  The cells of one colour only read cells of the other, so values loaded ahead
+// are never stale and the in-place update needs no barrier.  Interior cells use the interior class's
 // coefficients with the chunked kernel's operations in its order (bit-identical results); boundary
-// cells take the general per-cell path.  (Levels with coefficient arrays stay on the chunked kernel:
-// with seven more streams per cell the march was measured slower.)  Tiles: Chunk{lvl, j = y origin, k = first plane,
-// i0 = x origin, cnt = MG_ZT_X, nrows = planes}.
-template <typename T>
+// cells take the general per-cell path, queued (ZQueue).  (Levels with coefficient arrays stay on the chunked kernel:
+// with seven more streams per cell the march was measured slower.)  Tiles: Chunk{lvl, j = y origin,
+// k = first plane, i0 = x origin, cnt = MG_ZT_X, nrows = planes}.
+template <typename T, int ZB>
 __global__ void __launch_bounds__(32 * MG_ZT_Y) mg_smooth_z(const LvlDev* __restrict__ Ls, const Chunk* __restrict__ ch, int nch, int color,
                                                            const Scal* sc) {
+    static_assert(ZB % 2 == 0, "every batch starts on the same colour");
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __shared__ ZQueue Q;
+    if (threadIdx.x == 0) Q.n = 0;
+    __syncthreads();
     for (int c = blockIdx.x; c < nch; c += gridDim.x) {
         const Chunk C = ch[c];
         if (!active(Ls, C, sc)) continue;
@@ -92,34 +129,214 @@ __global__ void __launch_bounds__(32 * MG_ZT_Y) mg_smooth_z(const LvlDev* __rest
         const long long col = col_ok ? (long long) i + sy * j : 0;
         const int k0 = C.k, k1 = min(C.k + C.nrows, n2);
         const bool ij_inner = i > 0 && i < n0 - 1 && j > 0 && j < n1 - 1;
-        T* xk = x + col + sz * k0;  // this column at plane k (dereferenced only where col_ok)
+        const int p0 = (i + j + k0 + color) & 1;  // 0: the cells at planes k0, k0 + 2, ... are updated
+        T* xk = x + col + sz * k0;                // this column at the batch's first plane (dereferenced only where col_ok)
         const T* bk = b + col + sz * k0;
         T xm = (col_ok && k0 > 0) ? xk[-sz] : (T) 0;
         T xc = col_ok ? *xk : (T) 0;
-        int parity = (i + j + k0 + color) & 1;
-        for (int k = k0; k < k1; ++k) {
-            const T xp = (col_ok && k + 1 < n2) ? xk[sz] : (T) 0;
-            const T xw = __shfl_up_sync(0xffffffffu, xc, 1), xe = __shfl_down_sync(0xffffffffu, xc, 1);
-            if (computes && parity == 0) {
-                if (ij_inner && k > 0 && k < n2 - 1) {
-                    T acc = 0;
-                    acc += c1 * xw;
-                    acc += c2 * xe;
-                    acc += c3 * xk[-sy];
-                    acc += c4 * xk[sy];
-                    acc += c5 * xm;
-                    acc += c6 * xp;
-                    *xk = (*bk - acc) * cinv;
-                } else {
-                    cell_gs<T>(L, i, j, k);
+        for (int kb = k0; kb < k1; kb += ZB) {
+            T xs[ZB + 2], bv[ZB], ys[ZB], yn[ZB];  // xs[q + 1]: x at plane kb + q
+            unsigned general = 0;                  // planes of the batch whose cell takes the per-cell path
+            xs[0] = xm;
+            xs[1] = xc;
+#pragma unroll
+            for (int q = 0; q < ZB; ++q) {
+                const int k = kb + q;
+                const bool upd = computes && k < k1 && ((q + p0) & 1) == 0;
+                xs[q + 2] = (col_ok && k + 1 < n2) ? xk[(q + 1) * sz] : (T) 0;
+                bv[q] = upd ? bk[q * sz] : (T) 0;
+                ys[q] = (upd && ij_inner) ? xk[q * sz - sy] : (T) 0;
+                yn[q] = (upd && ij_inner) ? xk[q * sz + sy] : (T) 0;
+            }
+#pragma unroll
+            for (int q = 0; q < ZB; ++q) {
+                const int k = kb + q;
+                const T xw = __shfl_up_sync(0xffffffffu, xs[q + 1], 1), xe = __shfl_down_sync(0xffffffffu, xs[q + 1], 1);
+                if (computes && k < k1 && ((q + p0) & 1) == 0) {
+                    if (ij_inner && k > 0 && k < n2 - 1) {
+                        T acc = 0;
+                        acc += c1 * xw;
+                        acc += c2 * xe;
+                        acc += c3 * ys[q];
+                        acc += c4 * yn[q];
+                        acc += c5 * xs[q];
+                        acc += c6 * xs[q + 2];
+                        xk[q * sz] = (bv[q] - acc) * cinv;
+                    } else {
+                        general |= 1u << q;
+                    }
                 }
             }
-            xm = xc;
-            xc = xp;
-            xk += sz;
-            bk += sz;
-            parity ^= 1;
+            zq_push(Q, general, kb - k0, warp, lane);
+            xm = xs[ZB];
+            xc = xs[ZB + 1];
+            xk += ZB * sz;
+            bk += ZB * sz;
         }
+        zq_drain(Q, C, [&](int ci, int cj, int ck) { cell_gs<T>(L, ci, cj, ck); });
+    }
+}
+
+// r = b - A x over the z-marching tiles of a 3D class-table level (every cell; the same batches,
+// register window and lane shuffles as mg_smooth_z, and cell_residual's operations in its order)
+template <typename T, int ZB>
+__global__ void __launch_bounds__(32 * MG_ZT_Y) mg_residual_z(const LvlDev* __restrict__ Ls, const Chunk* __restrict__ ch, int nch, const Scal* sc) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __shared__ ZQueue Q;
+    if (threadIdx.x == 0) Q.n = 0;
+    __syncthreads();
+    for (int c = blockIdx.x; c < nch; c += gridDim.x) {
+        const Chunk C = ch[c];
+        if (!active(Ls, C, sc)) continue;
+        const LvlDev& L = Ls[C.lvl];
+        const int n0 = L.n[0], n1 = L.n[1], n2 = L.n[2];
+        const long long sy = n0, sz = (long long) n0 * n1;
+        const int i = C.i0 - 1 + lane, j = C.j + warp;
+        const bool col_ok = i >= 0 && i < n0 && j < n1;
+        const bool computes = col_ok && lane >= 1 && lane <= MG_ZT_X;
+        const T* t = Sel<T>::Tb(L) + 13 * TSTRIDE;
+        const T c0 = t[0], c1 = t[1], c2 = t[2], c3 = t[3], c4 = t[4], c5 = t[5], c6 = t[6];
+        const long long col = col_ok ? (long long) i + sy * j : 0;
+        const int k0 = C.k, k1 = min(C.k + C.nrows, n2);
+        const bool ij_inner = i > 0 && i < n0 - 1 && j > 0 && j < n1 - 1;
+        const T* xk = Sel<T>::x(L) + col + sz * k0;
+        const T* bk = Sel<T>::b(L) + col + sz * k0;
+        T* rk = Sel<T>::r(L) + col + sz * k0;
+        T xm = (col_ok && k0 > 0) ? xk[-sz] : (T) 0;
+        T xc = col_ok ? *xk : (T) 0;
+        for (int kb = k0; kb < k1; kb += ZB) {
+            T xs[ZB + 2], bv[ZB], ys[ZB], yn[ZB];
+            unsigned general = 0;
+            xs[0] = xm;
+            xs[1] = xc;
+#pragma unroll
+            for (int q = 0; q < ZB; ++q) {
+                const int k = kb + q;
+                const bool in = computes && k < k1;
+                xs[q + 2] = (col_ok && k + 1 < n2) ? xk[(q + 1) * sz] : (T) 0;
+                bv[q] = in ? bk[q * sz] : (T) 0;
+                ys[q] = (in && ij_inner) ? xk[q * sz - sy] : (T) 0;
+                yn[q] = (in && ij_inner) ? xk[q * sz + sy] : (T) 0;
+            }
+#pragma unroll
+            for (int q = 0; q < ZB; ++q) {
+                const int k = kb + q;
+                const T xw = __shfl_up_sync(0xffffffffu, xs[q + 1], 1), xe = __shfl_down_sync(0xffffffffu, xs[q + 1], 1);
+                if (computes && k < k1) {
+                    if (ij_inner && k > 0 && k < n2 - 1) {
+                        T acc = 0;
+                        acc += c1 * xw;
+                        acc += c2 * xe;
+                        acc += c3 * ys[q];
+                        acc += c4 * yn[q];
+                        acc += c5 * xs[q];
+                        acc += c6 * xs[q + 2];
+                        rk[q * sz] = bv[q] - (c0 * xs[q + 1] + acc);
+                    } else {
+                        general |= 1u << q;
+                    }
+                }
+            }
+            zq_push(Q, general, kb - k0, warp, lane);
+            xm = xs[ZB];
+            xc = xs[ZB + 1];
+            xk += ZB * sz;
+            bk += ZB * sz;
+            rk += ZB * sz;
+        }
+        zq_drain(Q, C, [&](int ci, int cj, int ck) { cell_residual<T>(L, ci, cj, ck); });
+    }
+}
+
+// x += P x_coarse over the z-marching tiles of a 3D level whose coarse level is cell-centred: each
+// thread walks its fine column upward, ZB fine planes (ZB / 2 coarse planes) per batch.  Fine plane
+// 2K + e interpolates coarse planes K and K - 1 + 2e, so a batch reads coarse planes K0 - 1 .. K0 + ZB/2
+// of which the first two come from the previous batch: each coarse value a thread needs is loaded once
+// per tile instead of once per fine cell.  Interior cells sum the eight trilinear terms in
+// prolong_acc's order and weights (bit-identical to the chunked kernel); cells with a coarse
+// neighbour outside the box take cell_prolong (queued).  Levels whose coarse level is node-centred are
+// skipped here (they stay on the chunked kernel).  Tiles start at even planes.
+template <typename T, int ZB>
+__global__ void __launch_bounds__(32 * MG_ZT_Y) mg_prolong_z(const LvlDev* __restrict__ Ls, const Chunk* __restrict__ ch, int nch, const Scal* sc) {
+    static_assert(ZB % 2 == 0, "whole coarse planes per batch");
+    constexpr bool FAST = std::is_same<T, float>::value;  // the chunked kernel's instance
+    constexpr int NP = ZB / 2 + 2;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __shared__ ZQueue Q;
+    if (threadIdx.x == 0) Q.n = 0;
+    __syncthreads();
+    for (int c = blockIdx.x; c < nch; c += gridDim.x) {
+        const Chunk C = ch[c];
+        if (!active(Ls, C, sc)) continue;
+        const LvlDev& L = Ls[C.lvl];
+        const LvlDev& Lc = Ls[L.coarse];
+        const int n0 = L.n[0], n1 = L.n[1], n2 = L.n[2];
+        const long long sy = n0, sz = (long long) n0 * n1;
+        const int i = C.i0 - 1 + lane, j = C.j + warp;
+        const bool computes = i >= 0 && i < n0 && j < n1 && lane >= 1 && lane <= MG_ZT_X;
+        const int k0 = C.k, k1 = min(C.k + C.nrows, n2);
+        if (Lc.node || (k0 & 1)) continue;  // node-centred levels take the chunked kernel; tiles start at even planes
+        const int nc0 = Lc.n[0], nc1 = Lc.n[1], nc2 = Lc.n[2];
+        const int I0 = i >> 1, J0 = (i & 1) ? I0 + 1 : I0 - 1;
+        const int I1 = j >> 1, J1 = (j & 1) ? I1 + 1 : I1 - 1;
+        const bool in_xy = computes && I0 < nc0 && J0 >= 0 && J0 < nc0 && I1 < nc1 && J1 >= 0 && J1 < nc1;
+        const long long csz = (long long) nc0 * nc1;
+        // the four coarse columns, in prolong_acc's order (x fastest, then y)
+        const long long o0 = in_xy ? I0 + (long long) nc0 * I1 : 0, o1 = in_xy ? J0 + (long long) nc0 * I1 : 0;
+        const long long o2 = in_xy ? I0 + (long long) nc0 * J1 : 0, o3 = in_xy ? J0 + (long long) nc0 * J1 : 0;
+        const T* xcr = Sel<T>::x(Lc);
+        T cv[NP][4];  // cv[p]: coarse plane K0 - 1 + p of the current batch
+        auto load_plane = [&](int K, T* v) {
+            const bool ok = in_xy && K >= 0 && K < nc2;
+            const T* pl = xcr + csz * (ok ? K : 0);
+            v[0] = ok ? pl[o0] : (T) 0;
+            v[1] = ok ? pl[o1] : (T) 0;
+            v[2] = ok ? pl[o2] : (T) 0;
+            v[3] = ok ? pl[o3] : (T) 0;
+        };
+        load_plane((k0 >> 1) - 1, cv[0]);
+        load_plane(k0 >> 1, cv[1]);
+        T* xf = Sel<T>::x(L) + (computes ? (long long) i + sy * j : 0) + sz * k0;
+        const T w[2] = {(T) 0.75, (T) 0.25};
+        for (int kb = k0; kb < k1; kb += ZB) {
+            const int K0 = kb >> 1;
+#pragma unroll
+            for (int p = 2; p < NP; ++p) load_plane(K0 + p - 1, cv[p]);
+            T xv[ZB];
+            unsigned general = 0;
+#pragma unroll
+            for (int q = 0; q < ZB; ++q) xv[q] = (computes && kb + q < k1) ? xf[q * sz] : (T) 0;
+#pragma unroll
+            for (int q = 0; q < ZB; ++q) {
+                const int k = kb + q;
+                if (!computes || k >= k1) continue;
+                const int KI = K0 + q / 2, KJ = (q & 1) ? KI + 1 : KI - 1;
+                if (in_xy && KI < nc2 && KJ >= 0 && KJ < nc2) {
+                    const int pI = q / 2 + 1, pJ = (q & 1) ? pI + 1 : pI - 1;
+                    T acc = 0;
+#pragma unroll
+                    for (int a = 0; a < 2; ++a)
+#pragma unroll
+                        for (int bb = 0; bb < 2; ++bb)
+#pragma unroll
+                            for (int e = 0; e < 2; ++e) {
+                                const T wt = w[e] * w[bb] * w[a];
+                                acc += wt * (T) 1 * cv[a ? pJ : pI][2 * bb + e];
+                            }
+                    xf[q * sz] = xv[q] + acc;
+                } else {
+                    general |= 1u << q;
+                }
+            }
+            zq_push(Q, general, kb - k0, warp, lane);
+#pragma unroll
+            for (int v = 0; v < 4; ++v) {
+                cv[0][v] = cv[NP - 2][v];
+                cv[1][v] = cv[NP - 1][v];
+            }
+            xf += ZB * sz;
+        }
+        zq_drain(Q, C, [&](int ci, int cj, int ck) { cell_prolong<T, FAST>(Ls, L, ci, cj, ck); });
     }
 }
 
@@ -565,12 +782,41 @@ int mg_launch_smooth(cudaStream_t s, int sms, bool f32, const LvlDev* L, const C
     OPG_LAUNCHED();
     return check_launch("mg_smooth");
 }
+// planes per batch of the z-marching kernels (OPFLOW_MG_ZB = 2, 4 or 8; default 4)
+static int z_batch() {
+    static const int zb = [] {
+        const char* e = getenv("OPFLOW_MG_ZB");
+        const int v = e ? atoi(e) : 4;
+        return v == 2 || v == 8 ? v : 4;
+    }();
+    return zb;
+}
+#define OPG_ZB_LAUNCH(KERNEL, T, ...)                                                                   \
+    switch (z_batch()) {                                                                               \
+        case 2: KERNEL<T, 2><<<grid_of(nch, sms), 32 * MG_ZT_Y, 0, s>>>(__VA_ARGS__); break;           \
+        case 8: KERNEL<T, 8><<<grid_of(nch, sms), 32 * MG_ZT_Y, 0, s>>>(__VA_ARGS__); break;           \
+        default: KERNEL<T, 4><<<grid_of(nch, sms), 32 * MG_ZT_Y, 0, s>>>(__VA_ARGS__); break;          \
+    }
 int mg_launch_smooth_z(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* ch, int nch, int color, const Scal* sc) {
     if (nch <= 0) return OPFLOW_OK;
-    if (f32) mg_smooth_z<float><<<grid_of(nch, sms), 32 * MG_ZT_Y, 0, s>>>(L, ch, nch, color, sc);
-    else mg_smooth_z<double><<<grid_of(nch, sms), 32 * MG_ZT_Y, 0, s>>>(L, ch, nch, color, sc);
+    if (f32) { OPG_ZB_LAUNCH(mg_smooth_z, float, L, ch, nch, color, sc) }
+    else { OPG_ZB_LAUNCH(mg_smooth_z, double, L, ch, nch, color, sc) }
     OPG_LAUNCHED();
     return check_launch("mg_smooth_z");
+}
+int mg_launch_residual_z(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* ch, int nch, const Scal* sc) {
+    if (nch <= 0) return OPFLOW_OK;
+    if (f32) { OPG_ZB_LAUNCH(mg_residual_z, float, L, ch, nch, sc) }
+    else { OPG_ZB_LAUNCH(mg_residual_z, double, L, ch, nch, sc) }
+    OPG_LAUNCHED();
+    return check_launch("mg_residual_z");
+}
+int mg_launch_prolong_z(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* ch, int nch, const Scal* sc) {
+    if (nch <= 0) return OPFLOW_OK;
+    if (f32) { OPG_ZB_LAUNCH(mg_prolong_z, float, L, ch, nch, sc) }
+    else { OPG_ZB_LAUNCH(mg_prolong_z, double, L, ch, nch, sc) }
+    OPG_LAUNCHED();
+    return check_launch("mg_prolong_z");
 }
 int mg_launch_restrict(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* ch, int nch, const Scal* sc) {
     if (nch <= 0) return OPFLOW_OK;

@@ -662,8 +662,10 @@ int mg_finalize(MGSystem* S) {
                 // planes per tile: up to MG_ZT_Z, fewer where the level would otherwise have fewer than
                 // four tiles per SM (a short march leaves SMs idle); below 4 planes the chunked kernel
                 const long long txy = (long long) ((D.n[0] + MG_ZT_X - 1) / MG_ZT_X) * ((D.n[1] + MG_ZT_Y - 1) / MG_ZT_Y);
-                const int zz = (int) std::min<long long>(MG_ZT_Z, (long long) D.n[2] * txy / (4LL * ctx->num_sms));
-                if (zmarch && zz >= 4) {
+                // (even, so that the prolongation's tiles start on whole coarse planes)
+                const int zz = (int) std::min<long long>(MG_ZT_Z, (long long) D.n[2] * txy / (4LL * ctx->num_sms)) & ~1;
+                const bool ztiles = zmarch && zz >= 4;
+                if (ztiles) {
                     for (int k0 = 0; k0 < D.n[2]; k0 += zz)
                         for (int j0 = 0; j0 < D.n[1]; j0 += MG_ZT_Y)
                             for (int i0 = 0; i0 < D.n[0]; i0 += MG_ZT_X) {
@@ -672,9 +674,11 @@ int mg_finalize(MGSystem* S) {
                                 S->zsm_ch[l].push_back(c);
                             }
                 } else if (!D.coarsest) {
-                    rows(li, D, S->smooth_ch[l]);
+                    rows(li, D, S->smooth_ch[l]);  // (also the rows of the residual before restriction)
                 }
-                if (!D.coarsest) rows(li, D, S->prolong_ch[l]);  // fine rows of level l (prolonged from l+1)
+                // fine rows of level l prolonged from l+1 by the chunked kernel (z levels of cell-centred
+                // problems take mg_prolong_z over their tiles)
+                if (!D.coarsest && (!ztiles || D.node)) rows(li, D, S->prolong_ch[l]);
             }
             if (l > 0 && !above_tiled) rows(li, D, S->restrict_ch[l]);  // coarse rows of level l (restricted from l-1)
             if (D.coarsest && H.Ainv64) coarse_list.push_back(li);
@@ -780,7 +784,8 @@ static int vcycle(MGSystem* S) {
             OPG_TRY(mg_launch_smooth(s, sms, f32, S->dL, C.ptr, C.n, 1, sc));
             OPG_TRY(mg_launch_smooth_z(s, sms, f32, S->dL, Z.ptr, Z.n, 1, sc));
         }
-        if (S->d_prolong[l].n) OPG_TRY(mg_launch_residual(s, sms, f32, S->dL, S->d_prolong[l].ptr, S->d_prolong[l].n, sc));
+        OPG_TRY(mg_launch_residual(s, sms, f32, S->dL, C.ptr, C.n, sc));
+        OPG_TRY(mg_launch_residual_z(s, sms, f32, S->dL, Z.ptr, Z.n, sc));
     }
     OPG_TRY(mg_launch_bottom(s, sms, f32, S->dL, S->dbottom, S->nbottom, sc, S->pre, S->post, S->bottom_cells));
     OPG_TRY(mg_launch_coarse(s, sms, f32, S->dL, S->dcoarse, S->ncoarse, sc));
@@ -790,9 +795,10 @@ static int vcycle(MGSystem* S) {
     }
     for (int l = S->nlevels - 2; l >= 0; --l) {
         OPG_TRY(mg_launch_tile_up(s, sms, f32, S->dL, S->d_tiles[l].ptr, S->d_tiles[l].n, sc, S->post));
-        OPG_TRY(mg_launch_prolong(s, sms, f32, S->dL, S->d_prolong[l].ptr, S->d_prolong[l].n, sc));
         const ChunkList& C = S->d_smooth[l];
         const ChunkList& Z = S->d_zsm[l];
+        OPG_TRY(mg_launch_prolong(s, sms, f32, S->dL, S->d_prolong[l].ptr, S->d_prolong[l].n, sc));
+        OPG_TRY(mg_launch_prolong_z(s, sms, f32, S->dL, Z.ptr, Z.n, sc));
         for (int it = 0; it < S->post; ++it) {
             OPG_TRY(mg_launch_smooth(s, sms, f32, S->dL, C.ptr, C.n, 1, sc));
             OPG_TRY(mg_launch_smooth_z(s, sms, f32, S->dL, Z.ptr, Z.n, 1, sc));
