@@ -7,6 +7,10 @@
 // z = M r and p = z) and leaves as soon as it converges, so requests of different sizes that arrive at
 // different times share every launch while they overlap.  A heat session restarts in place after each
 // step (b := x, no recomposition).  Admission is bounded by an HBM budget and a batch size.
+//
+// Two threads: the admission thread builds each admitted request's system (host-side hierarchy,
+// uploads, the seed) on a stream of its own and hands it over ready; the worker only composes and
+// iterates, so set-up overlaps the batched iterations instead of stalling them.
 #include "solver.h"
 
 #include <algorithm>
@@ -46,6 +50,7 @@ struct Req {
     bool pinned = false;
     bool done = false;
     long long N = 0;
+    Scal seed{};  // the Krylov scalars after set-up
 };
 
 static size_t estimate_bytes(const opflow_problem_desc& pd) {
@@ -59,14 +64,18 @@ static size_t estimate_bytes(const opflow_problem_desc& pd) {
 using namespace opg;
 
 struct opflow_server_s {
-    opflow_ctx_s own_ctx;  // private stream and scratch on the caller's device
+    opflow_ctx_s own_ctx;    // the worker's stream and scratch on the caller's device
+    opflow_ctx_s setup_ctx;  // the admission thread's
     opflow_solve_params params;
     size_t budget = 0, used = 0;
     int max_active = 64;
-    std::thread worker;
+    std::thread worker, admitter;
     std::mutex mu;
-    std::condition_variable cv, cv_done;
+    std::condition_variable cv, cv_done, cv_admit;
     std::deque<Req*> pending;
+    std::deque<Req*> ready;  // set up, joining at the worker's next iteration boundary
+    int resident = 0;        // admitted and not finished (in set-up, ready or active)
+    int in_setup = 0;
     std::vector<Req*> active;
     std::unordered_map<long long, Req*> reqs;
     bool stop = false;
@@ -93,7 +102,7 @@ static void release_req(Req* r) {
 
 // hierarchy, right-hand side, pinning, and the seed of the Krylov scalars
 static int setup_req(opflow_server S, Req* r, Scal* seed) {
-    opflow_ctx ctx = &S->own_ctx;
+    opflow_ctx ctx = &S->setup_ctx;
     OPG_TRY(batch_problem_fields(ctx, r->pd, &r->t, &r->rhs));
     r->sys = new MGSystem();
     MGSystem* M = r->sys;
@@ -156,6 +165,9 @@ static void finish_mark(opflow_server S, Req* r, int status) {
     std::lock_guard<std::mutex> lk(S->mu);
     r->done = true;
     S->completed++;
+    S->resident--;
+    S->used -= std::min(S->used, r->admitted_bytes);
+    S->cv_admit.notify_one();
     S->lat.push_back(std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count());
     S->t_last = r->t_done;
     S->cv_done.notify_all();
@@ -172,9 +184,65 @@ static void finish_req(opflow_server S, Req* r, int status) {
     std::lock_guard<std::mutex> lk(S->mu);
     r->done = true;
     S->completed++;
+    S->resident--;
+    S->used -= std::min(S->used, r->admitted_bytes);
+    S->cv_admit.notify_one();
     S->lat.push_back(std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count());
     S->t_last = r->t_done;
     S->cv_done.notify_all();
+}
+
+// true when the next pending request fits the batch size and the HBM budget (a request alone is
+// always admitted); called with the lock held
+static bool can_admit(opflow_server S) {
+    if (S->pending.empty() || S->resident >= S->max_active) return false;
+    const size_t est = estimate_bytes(S->pending.front()->pd);
+    return !S->budget || S->used + est <= S->budget || S->resident == 0;
+}
+
+// The admission thread: set-up on its own stream, then the system, its fields and their memory are
+// handed to the worker's stream (the set-up stream is synchronised by setup_req).
+static void admit_loop(opflow_server S) {
+    cudaSetDevice(S->setup_ctx.device);
+    for (;;) {
+        Req* r = nullptr;
+        {
+            std::unique_lock<std::mutex> lk(S->mu);
+            S->cv_admit.wait(lk, [&] { return (S->stop && S->pending.empty()) || can_admit(S); });
+            if (!can_admit(S)) break;  // stopping, nothing left to admit
+            r = S->pending.front();
+            S->pending.pop_front();
+            r->admitted_bytes = estimate_bytes(r->pd);
+            S->used += r->admitted_bytes;
+            S->resident++;
+            S->in_setup++;
+        }
+        const Clock::time_point t0 = Clock::now();
+        r->t_admit = t0;
+        const int rc = setup_req(S, r, &r->seed);
+        if (rc) {
+            const std::string err = opflow_last_error();
+            release_req(r);
+            finish_req(S, r, rc);
+            std::lock_guard<std::mutex> lk(S->mu);
+            S->error = err;
+            S->in_setup--;
+            S->setup_s += std::chrono::duration<double>(Clock::now() - t0).count();
+            S->cv.notify_one();
+            continue;
+        }
+        r->sys->ctx = &S->own_ctx;
+        r->sys->arena.ctx = &S->own_ctx;
+        r->t->ctx = &S->own_ctx;
+        r->rhs->ctx = &S->own_ctx;
+        {
+            std::lock_guard<std::mutex> lk(S->mu);
+            S->ready.push_back(r);
+            S->in_setup--;
+            S->setup_s += std::chrono::duration<double>(Clock::now() - t0).count();
+        }
+        S->cv.notify_one();
+    }
 }
 
 static void worker_loop(opflow_server S) {
@@ -185,16 +253,12 @@ static void worker_loop(opflow_server S) {
         std::vector<Req*> admit;
         {
             std::unique_lock<std::mutex> lk(S->mu);
-            S->cv.wait(lk, [&] { return S->stop || !S->pending.empty() || !S->active.empty(); });
-            if (S->stop && S->pending.empty() && S->active.empty()) break;
-            while (!S->pending.empty() && (int) (S->active.size() + admit.size()) < S->max_active) {
-                Req* r = S->pending.front();
-                const size_t est = estimate_bytes(r->pd);
-                if (S->budget && S->used + est > S->budget && !(S->active.empty() && admit.empty())) break;
-                S->pending.pop_front();
-                S->used += est;
-                r->admitted_bytes = est;
-                admit.push_back(r);
+            const auto drained = [&] { return S->stop && S->pending.empty() && S->in_setup == 0 && S->ready.empty(); };
+            S->cv.wait(lk, [&] { return drained() || !S->ready.empty() || !S->active.empty(); });
+            if (drained() && S->active.empty()) break;
+            while (!S->ready.empty()) {
+                admit.push_back(S->ready.front());
+                S->ready.pop_front();
             }
         }
         auto add_since = [&](double& acc, Clock::time_point t) {
@@ -202,31 +266,18 @@ static void worker_loop(opflow_server S) {
             std::lock_guard<std::mutex> lk(S->mu);
             acc += d;
         };
-        const Clock::time_point t_setup = Clock::now();
         for (Req* r : admit) {
-            Scal seed{};
-            r->t_admit = Clock::now();
-            const int rc = setup_req(S, r, &seed);
-            if (rc) {
-                r->status = rc;
-                S->error = opflow_last_error();
-                release_req(r);
-                { std::lock_guard<std::mutex> lk(S->mu); S->used -= std::min(S->used, r->admitted_bytes); }
-                finish_req(S, r, rc);
-                continue;
-            }
             S->active.push_back(r);
-            S->state.push_back(seed);
+            S->state.push_back(r->seed);
             S->dirty = true;
         }
-        add_since(S->setup_s, t_setup);
         if (S->active.empty()) continue;
         const Clock::time_point t_compose = Clock::now();
         if (S->dirty) {
             std::vector<MGSystem*> parts;
             for (Req* r : S->active) parts.push_back(r->sys);
             if (mg_compose(&S->comp, parts, S->state) != OPFLOW_OK) {
-                S->error = opflow_last_error();
+                { std::lock_guard<std::mutex> lk(S->mu); S->error = opflow_last_error(); }
                 for (Req* r : S->active) { release_req(r); finish_req(S, r, OPFLOW_E_CUDA); }
                 S->active.clear();
                 S->state.clear();
@@ -242,7 +293,7 @@ static void worker_loop(opflow_server S) {
         // a few batched iterations, then the per-request scalars
         const Clock::time_point t_iter = Clock::now();
         if (mg_run_iterations(&S->comp, ITERS) != OPFLOW_OK) {
-            S->error = opflow_last_error();
+            { std::lock_guard<std::mutex> lk(S->mu); S->error = opflow_last_error(); }
             for (Req* r : S->active) { release_req(r); finish_req(S, r, OPFLOW_E_CUDA); }
             S->active.clear();
             S->state.clear();
@@ -289,7 +340,6 @@ static void worker_loop(opflow_server S) {
         for (auto& q : restarted) keep_state[q.first] = S->state[q.second];
         for (auto& f : finished) {
             finish_mark(S, f.first, f.second);
-            { std::lock_guard<std::mutex> lk(S->mu); S->used -= std::min(S->used, f.first->admitted_bytes); }
             retired.push_back(f.first);
         }
         S->active.swap(keep);
@@ -315,6 +365,14 @@ int opflow_server_create(opflow_ctx ctx, const opflow_solve_params* params, size
         return fail(OPFLOW_E_CUDA, "stream creation failed");
     }
     S->own_ctx.own_stream = true;
+    S->setup_ctx.device = ctx->device;
+    S->setup_ctx.num_sms = ctx->num_sms;
+    if (cudaStreamCreateWithFlags(&S->setup_ctx.stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaStreamDestroy(S->own_ctx.stream);
+        delete S;
+        return fail(OPFLOW_E_CUDA, "stream creation failed");
+    }
+    S->setup_ctx.own_stream = true;
     if (params) S->params = *params;
     else opflow_solve_params_default(&S->params);
     S->budget = budget;
@@ -327,13 +385,17 @@ int opflow_server_create(opflow_ctx ctx, const opflow_solve_params* params, size
     S->comp.tol = S->params.tol;
     S->comp.max_iter = S->params.max_iter;
     S->comp.arena.block_hint = 1u << 20;
-    if (ensure_scratch(&S->own_ctx, 4096) != OPFLOW_OK ||
+    if (ensure_scratch(&S->own_ctx, 4096) != OPFLOW_OK || ensure_scratch(&S->setup_ctx, 4096) != OPFLOW_OK ||
         !(S->d_slots = (double*) dev_alloc(&S->own_ctx, (size_t) (S->max_active + 1) * sizeof(double)))) {
+        cudaStreamSynchronize(S->own_ctx.stream);
+        cudaStreamSynchronize(S->setup_ctx.stream);
         cudaStreamDestroy(S->own_ctx.stream);
+        cudaStreamDestroy(S->setup_ctx.stream);
         delete S;
         return OPFLOW_E_NOMEM;
     }
     S->worker = std::thread(worker_loop, S);
+    S->admitter = std::thread(admit_loop, S);
     *out = S;
     return OPFLOW_OK;
 }
@@ -367,7 +429,7 @@ int opflow_server_submit(opflow_server S, const opflow_request* q, long long* id
         S->submitted++;
         if (!S->have_first) { S->t_first = r->t_submit; S->have_first = true; }
     }
-    S->cv.notify_one();
+    S->cv_admit.notify_one();
     if (id) *id = r->id;
     return OPFLOW_OK;
 }
@@ -437,6 +499,9 @@ int opflow_server_destroy(opflow_server S) {
         std::lock_guard<std::mutex> lk(S->mu);
         S->stop = true;
     }
+    S->cv_admit.notify_all();
+    S->cv.notify_all();
+    if (S->admitter.joinable()) S->admitter.join();
     S->cv.notify_all();
     if (S->worker.joinable()) S->worker.join();
     for (auto& kv : S->reqs) {
@@ -455,6 +520,9 @@ int opflow_server_destroy(opflow_server S) {
     if (S->d_slots) dev_free(&S->own_ctx, S->d_slots);
     cudaStreamSynchronize(S->own_ctx.stream);
     cudaStreamDestroy(S->own_ctx.stream);
+    if (S->setup_ctx.scratch) dev_free(&S->setup_ctx, S->setup_ctx.scratch);
+    cudaStreamSynchronize(S->setup_ctx.stream);
+    cudaStreamDestroy(S->setup_ctx.stream);
     delete S;
     return OPFLOW_OK;
 }

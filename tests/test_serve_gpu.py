@@ -93,3 +93,40 @@ def test_server_rejects_nan_and_respects_budget(ctx):
     assert all(r["status"] == capi.OK for r in res)
     assert s.stats()["max_active_seen"] == 1
     s.close()
+
+
+def test_failed_setup_leaves_the_others_served(ctx):
+    """A request whose set-up fails (a boundary condition the problem form does not take) finishes with
+    its error while the requests around it are served as usual."""
+    params = api.StructSolverParams(tol=1e-10, maxIter=100, precision="mixed")
+    s = api.Server(params, max_active=4, ctx=ctx)
+    good = api.Problem([48, 40], [1 / 48, 1 / 40], alpha=1.0, beta=1e-3)
+    bad = api.Problem([48, 40], [1 / 48, 1 / 40], alpha=1.0, beta=1e-3, bc=api.BCType.Periodic)
+    rng = np.random.default_rng(7)
+    fs = [rng.standard_normal(48 * 40) for _ in range(5)]
+    ids = [s.submit(bad if k == 2 else good, fs[k]) for k in range(5)]
+    res = [s.result(i) for i in ids]
+    assert res[2]["status"] == capi.E_INVALID
+    assert all(res[k]["status"] == capi.OK and res[k]["rel_residual"] <= 1e-10 for k in (0, 1, 3, 4)), res
+    st = s.stats()
+    assert st["completed"] == 5
+    s.close()
+
+
+def test_close_serves_what_was_submitted(ctx):
+    """Closing a server with requests still queued or in set-up serves them all before it returns."""
+    reqs = mix(11)
+    params = api.StructSolverParams(tol=1e-10, maxIter=100, precision="mixed")
+    s = api.Server(params, max_active=3, ctx=ctx)
+    outs = []
+    for p, f, steps in reqs:
+        out = np.full(f.size, np.nan)
+        outs.append(out)
+        s.submit(p, f, steps=steps, out=out)
+    s.close()
+    ref = api.Server(params, max_active=8, ctx=ctx)
+    outs_ref, res_ref = run(ref, reqs)
+    ref.close()
+    assert all(r["status"] == capi.OK for r in res_ref)
+    for k in range(len(reqs)):
+        assert np.array_equal(outs[k], outs_ref[k]), k
