@@ -416,6 +416,22 @@ int opflow_server_drain(opflow_server s);
 int opflow_server_stats(opflow_server s, opflow_serve_stats* out);
 int opflow_server_destroy(opflow_server s);
 
+/* ---- autotuner ---------------------------------------------------------------------------------- */
+/* No counterpart in the reference (HYPRE and the OpenMP evaluators have no launch configurations).
+ * Where a kernel has equivalent launch configurations - the z-marching 3D multigrid kernels' plane
+ * batch, the 2D tile shape of the fused multigrid tile kernels, the 3D explicit kernels' tiling - the
+ * engine times them on the device the first time a (kernel, shape, stencil) key is met and keeps the
+ * fastest; results are identical whichever is chosen.  OPFLOW_TUNE=0 turns tuning off (the measured
+ * defaults); the explicit OPFLOW_MG_ZB / OPFLOW_AXIS_TILING switches override it.
+ * set_cache: choices are loaded from `path` (when it exists) and new ones appended to it; NULL keeps
+ * them in memory only (the default; OPFLOW_TUNE_CACHE names a file for the process instead).
+ * lookup: the cached choice for a key (OPFLOW_E_INVALID when there is none).  stats: choices measured
+ * by this process, cache hits, and entries held.  clear: forget every choice (the file is kept). */
+int opflow_tune_set_cache(const char* path);
+int opflow_tune_lookup(const char* key, int* value);
+int opflow_tune_stats(long long* tuned, long long* hits, long long* entries);
+int opflow_tune_clear(void);
+
 /* ---- residual norms without device allocation ------------------------------------------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device memory where they need the
  * answer - code running inside a CUDA stream capture (cudaMalloc/cudaFree cannot be captured), hosts

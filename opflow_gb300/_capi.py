@@ -119,6 +119,10 @@ _SIGS = {
     "opflow_field_device_ptr": [C.c_void_p, C.POINTER(C.c_void_p)],
     "opflow_field_update_padding": [C.c_void_p],
     "opflow_field_write_raw": [C.c_void_p, C.c_char_p, C.c_char_p, C.c_int, C.c_double],
+    "opflow_tune_set_cache": [C.c_char_p],
+    "opflow_tune_lookup": [C.c_char_p, C.POINTER(C.c_int)],
+    "opflow_tune_stats": [C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)],
+    "opflow_tune_clear": [],
     "opflow_eqnset_create": [C.c_void_p, C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_int), C.POINTER(C.c_void_p),
                              C.c_int, C.POINTER(C.c_int), C.c_void_p, C.POINTER(C.c_void_p)],
     "opflow_eqnset_solve": [C.c_void_p, C.c_void_p],

@@ -984,6 +984,31 @@ class Batch:
 
 
 # ------------------------------------------------------------------------------------------------ serving
+def tune_set_cache(path):
+    """Autotuner cache file (opflow_tune_set_cache): choices are loaded from `path` and new ones appended;
+    None keeps them in memory only."""
+    check(lib().opflow_tune_set_cache(None if path is None else str(path).encode()))
+
+
+def tune_lookup(key):
+    """The tuned choice for `key`, or None."""
+    v = C.c_int(0)
+    if lib().opflow_tune_lookup(key.encode(), C.byref(v)) != capi.OK:
+        return None
+    return v.value
+
+
+def tune_stats():
+    """(choices measured by this process, cache hits, entries held)."""
+    t, h, n = C.c_longlong(0), C.c_longlong(0), C.c_longlong(0)
+    check(lib().opflow_tune_stats(C.byref(t), C.byref(h), C.byref(n)))
+    return t.value, h.value, n.value
+
+
+def tune_clear():
+    check(lib().opflow_tune_clear())
+
+
 class Server:
     """Request loop with continuous batching (opflow_server_*): requests of any size join the running
     batch at the next iteration boundary and leave when they converge; heat sessions (steps > 1) stay

@@ -782,36 +782,36 @@ int mg_launch_smooth(cudaStream_t s, int sms, bool f32, const LvlDev* L, const C
     OPG_LAUNCHED();
     return check_launch("mg_smooth");
 }
-// planes per batch of the z-marching kernels (OPFLOW_MG_ZB = 2, 4 or 8; default 4)
-static int z_batch() {
-    static const int zb = [] {
+// planes per batch of the z-marching kernels: the system's (tuned) choice unless OPFLOW_MG_ZB = 2, 4 or 8
+static int z_batch(int zb) {
+    static const int forced = [] {
         const char* e = getenv("OPFLOW_MG_ZB");
-        const int v = e ? atoi(e) : 4;
-        return v == 2 || v == 8 ? v : 4;
+        const int v = e ? atoi(e) : 0;
+        return v == 2 || v == 4 || v == 8 ? v : 0;
     }();
-    return zb;
+    return forced ? forced : (zb == 2 || zb == 8 ? zb : 4);
 }
 #define OPG_ZB_LAUNCH(KERNEL, T, ...)                                                                   \
-    switch (z_batch()) {                                                                               \
+    switch (z_batch(zb)) {                                                                             \
         case 2: KERNEL<T, 2><<<grid_of(nch, sms), 32 * MG_ZT_Y, 0, s>>>(__VA_ARGS__); break;           \
         case 8: KERNEL<T, 8><<<grid_of(nch, sms), 32 * MG_ZT_Y, 0, s>>>(__VA_ARGS__); break;           \
         default: KERNEL<T, 4><<<grid_of(nch, sms), 32 * MG_ZT_Y, 0, s>>>(__VA_ARGS__); break;          \
     }
-int mg_launch_smooth_z(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* ch, int nch, int color, const Scal* sc) {
+int mg_launch_smooth_z(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* ch, int nch, int color, const Scal* sc, int zb) {
     if (nch <= 0) return OPFLOW_OK;
     if (f32) { OPG_ZB_LAUNCH(mg_smooth_z, float, L, ch, nch, color, sc) }
     else { OPG_ZB_LAUNCH(mg_smooth_z, double, L, ch, nch, color, sc) }
     OPG_LAUNCHED();
     return check_launch("mg_smooth_z");
 }
-int mg_launch_residual_z(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* ch, int nch, const Scal* sc) {
+int mg_launch_residual_z(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* ch, int nch, const Scal* sc, int zb) {
     if (nch <= 0) return OPFLOW_OK;
     if (f32) { OPG_ZB_LAUNCH(mg_residual_z, float, L, ch, nch, sc) }
     else { OPG_ZB_LAUNCH(mg_residual_z, double, L, ch, nch, sc) }
     OPG_LAUNCHED();
     return check_launch("mg_residual_z");
 }
-int mg_launch_prolong_z(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* ch, int nch, const Scal* sc) {
+int mg_launch_prolong_z(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* ch, int nch, const Scal* sc, int zb) {
     if (nch <= 0) return OPFLOW_OK;
     if (f32) { OPG_ZB_LAUNCH(mg_prolong_z, float, L, ch, nch, sc) }
     else { OPG_ZB_LAUNCH(mg_prolong_z, double, L, ch, nch, sc) }

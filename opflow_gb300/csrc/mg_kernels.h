@@ -10,11 +10,12 @@ int mg_launch_smooth(cudaStream_t s, int sms, bool f32, const LvlDev* L, const C
 // MG_ZT_MIN cells with at least 3 cells along every dim
 constexpr int MG_ZT_X = 30, MG_ZT_Y = 8, MG_ZT_Z = 32;
 constexpr long long MG_ZT_MIN = 32768;
-int mg_launch_smooth_z(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* ch, int nch, int color, const Scal* sc);
+// (zb: planes per load batch, 2, 4 or 8; OPFLOW_MG_ZB overrides)
+int mg_launch_smooth_z(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* ch, int nch, int color, const Scal* sc, int zb);
 // r = b - A x over the same tiles
-int mg_launch_residual_z(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* ch, int nch, const Scal* sc);
+int mg_launch_residual_z(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* ch, int nch, const Scal* sc, int zb);
 // x += P x_coarse over the same tiles (the tiles' first planes are even)
-int mg_launch_prolong_z(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* ch, int nch, const Scal* sc);
+int mg_launch_prolong_z(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* ch, int nch, const Scal* sc, int zb);
 int mg_launch_restrict(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* ch, int nch, const Scal* sc);
 int mg_launch_prolong(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* ch, int nch, const Scal* sc);
 // fused 2D tile steps of a level (mg_tiles.cu): down = pre-smoothing + residual + restriction,

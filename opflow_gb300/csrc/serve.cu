@@ -115,6 +115,9 @@ static int setup_req(opflow_server S, Req* r, Scal* seed) {
     M->tol = S->params.tol;
     M->max_iter = S->params.max_iter;
     M->arena.block_hint = 4u << 20;
+    // requests take the tuner's cached choices (from earlier solves of the shape or a cache file): timing
+    // here would add to the request's latency and run beside the batch, which would skew it
+    M->tune_measure = false;
     std::vector<opflow_node> tree = helmholtz_tree(r->pd.ndim, r->pd.alpha, r->pd.beta);
     opflow_field leaves[2] = {r->t, r->rhs};
     OPG_TRY(mg_add_problem(M, r->t, tree.data(), (int) tree.size(), leaves, 2, 0));

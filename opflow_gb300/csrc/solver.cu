@@ -19,11 +19,15 @@
 // poses it: the pinned system equals the consistent singular system whose pinned-row right-hand side is
 // replaced by minus the sum of the others, followed by a shift that makes the pinned unknown 0.
 #include "solver.h"
+#include "tune.h"
 
+#include <cstdio>
 #include <cstdlib>
 
 #include <chrono>
 #include <cmath>
+#include <functional>
+#include <string>
 
 namespace opg {
 
@@ -501,6 +505,102 @@ int mg_add_problem(MGSystem* S, opflow_field target, const opflow_node* nodes, i
 }
 
 // Vectors, device descriptors and chunk lists for every problem added.
+// Device time (ms) of `launch`, run once to warm up and once timed on the system's stream; negative
+// when a launch fails.
+static float time_launch(MGSystem* S, const std::function<int()>& launch) {
+    cudaStream_t s = S->ctx->stream;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    float ms = -1.f;
+    if (cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess && launch() == OPFLOW_OK &&
+        cudaEventRecord(e0, s) == cudaSuccess && launch() == OPFLOW_OK && cudaEventRecord(e1, s) == cudaSuccess &&
+        cudaEventSynchronize(e1) == cudaSuccess)
+        cudaEventElapsedTime(&ms, e0, e1);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    return ms;
+}
+
+static std::string level_key(const char* kernel, const MGSystem* S, int l) {
+    char buf[160];
+    const bool f32 = S->precision == OPFLOW_PREC_MIXED;
+    if (S->probs.size() == 1) {
+        const LevelHost& H = S->probs[0].levels[l];
+        std::snprintf(buf, sizeof buf, "%s/%s/%dx%dx%d/%s/%d,%d", kernel, f32 ? "f32" : "f64", H.n[0], H.ndim > 1 ? H.n[1] : 1,
+                      H.ndim > 2 ? H.n[2] : 1, H.node ? "node" : "cell", S->pre, S->post);
+    } else {
+        long long cells = 0;
+        for (const auto& P : S->probs)
+            if (l < (int) P.levels.size()) cells += P.levels[l].N;
+        std::snprintf(buf, sizeof buf, "%s/%s/batch%zu/%lld/%d/%d,%d", kernel, f32 ? "f32" : "f64", S->probs.size(), cells,
+                      (int) S->zsm_ch[l].size(), S->pre, S->post);
+    }
+    return buf;
+}
+
+// The tuner's choices for a finalized system (tune.h): the plane batch of every z-marching level and,
+// on single-problem systems, the 2D tile shape of every tiled level, each timed on the level itself.
+// The level vectors are zeroed first; every V-cycle rewrites them before reading them.
+static int tune_levels(MGSystem* S) {
+    if (!tune_enabled()) return OPFLOW_OK;
+    bool any = false;
+    for (int l = 0; l < S->nlevels; ++l) any = any || S->d_zsm[l].n > 0 || !S->tile_alt[l].empty();
+    if (!any) return OPFLOW_OK;
+    opflow_ctx ctx = S->ctx;
+    const int sms = ctx->num_sms;
+    const bool f32 = S->precision == OPFLOW_PREC_MIXED;
+    const size_t es = f32 ? 4 : 8;
+    auto choose = [&](const std::string& key, const std::vector<int>& cands, const std::function<float(int)>& time_ms) {
+        return S->tune_measure ? tune_pick(key, cands, time_ms) : tune_cached(key, cands);
+    };
+    for (const LvlDev& D : S->lv_host) {
+        if (!S->tune_measure) break;
+        void* v[3] = {f32 ? (void*) D.x32 : (void*) D.x64, f32 ? (void*) D.b32 : (void*) D.b64, f32 ? (void*) D.r32 : (void*) D.r64};
+        for (void* p : v)
+            if (p) OPG_CUDA(cudaMemsetAsync(p, 0, (size_t) D.N * es, ctx->stream));
+    }
+    for (int l = 0; l < S->nlevels; ++l) {
+        const ChunkList& Z = S->d_zsm[l];
+        if (Z.n > 0) {
+            S->zb[l] = choose(level_key("mg_smooth_z", S, l), {4, 2, 8}, [&](int zb) {
+                return time_launch(S, [&] {
+                    OPG_TRY(mg_launch_smooth_z(ctx->stream, sms, f32, S->dL, Z.ptr, Z.n, 0, nullptr, zb));
+                    return mg_launch_smooth_z(ctx->stream, sms, f32, S->dL, Z.ptr, Z.n, 1, nullptr, zb);
+                });
+            });
+        }
+        if (!S->tile_alt[l].empty()) {
+            // candidate 0: the list built (the shape the SM-fill rule picked), 1: the other shape
+            ChunkList alt{};
+            const int pick = choose(level_key("mg_tile", S, l), {0, 1}, [&](int cand) {
+                if (cand == 1 && !alt.ptr) {
+                    alt.n = (int) S->tile_alt[l].size();
+                    alt.ptr = (Chunk*) S->arena.alloc(S->tile_alt[l].size() * sizeof(Chunk));
+                    if (!alt.ptr) return -1.f;
+                    cudaMemcpyAsync(alt.ptr, S->tile_alt[l].data(), S->tile_alt[l].size() * sizeof(Chunk), cudaMemcpyHostToDevice, ctx->stream);
+                }
+                const ChunkList& T = cand ? alt : S->d_tiles[l];
+                return time_launch(S, [&] {
+                    OPG_TRY(mg_launch_tile_down(ctx->stream, sms, f32, S->dL, T.ptr, T.n, nullptr, S->pre));
+                    return mg_launch_tile_up(ctx->stream, sms, f32, S->dL, T.ptr, T.n, nullptr, S->post);
+                });
+            });
+            if (pick == 1) {
+                if (!alt.ptr) {  // a cached choice: the list is uploaded now
+                    alt.n = (int) S->tile_alt[l].size();
+                    alt.ptr = (Chunk*) S->arena.alloc(S->tile_alt[l].size() * sizeof(Chunk));
+                    if (!alt.ptr) return fail(OPFLOW_E_NOMEM, "tile list");
+                    OPG_CUDA(cudaMemcpyAsync(alt.ptr, S->tile_alt[l].data(), S->tile_alt[l].size() * sizeof(Chunk), cudaMemcpyHostToDevice, ctx->stream));
+                }
+                S->tile_ch[l].swap(S->tile_alt[l]);
+                S->d_tiles[l] = alt;
+            }
+            S->tile_alt[l].clear();
+        }
+    }
+    OPG_CUDA(cudaStreamSynchronize(ctx->stream));
+    return OPFLOW_OK;
+}
+
 int mg_finalize(MGSystem* S) {
     opflow_ctx ctx = S->ctx;
     const bool f32 = S->precision == OPFLOW_PREC_MIXED;
@@ -513,6 +613,8 @@ int mg_finalize(MGSystem* S) {
     S->prolong_ch.assign(S->nlevels, {});
     S->tile_ch.assign(S->nlevels, {});
     S->zsm_ch.assign(S->nlevels, {});
+    S->zb.assign(S->nlevels, 4);
+    S->tile_alt.assign(S->nlevels, {});
     S->coarse_sm_ch.clear();
     S->bottom_host.clear();
     S->bottom_cells_host.clear();
@@ -644,18 +746,20 @@ int mg_finalize(MGSystem* S) {
             if (l >= sp) continue;                                   // inside the bottom kernel
             const bool above_tiled = l > 0 && tileable(l - 1);      // restricted by the finer level's tiles
             if (D.tiled) {
-                // 54 x 32 tiles, or 22 x 16 where that would leave SMs idle (tile extent: cnt x nrows)
-                int tx = MG_TILE_X, ty = MG_TILE_Y;
-                if ((long long) ((D.n[0] + tx - 1) / tx) * ((D.n[1] + ty - 1) / ty) < 2LL * ctx->num_sms) {
-                    tx = MG_TILE_X_SMALL;
-                    ty = MG_TILE_Y / 2;
-                }
-                for (int j0 = 0; j0 < D.n[1]; j0 += ty)
-                    for (int i0 = 0; i0 < D.n[0]; i0 += tx) {
-                        Chunk c{li, j0, 0, i0, tx};
-                        c.nrows = ty;
-                        S->tile_ch[l].push_back(c);
-                    }
+                // 54 x 32 tiles, or 22 x 16 where that would leave SMs idle (tile extent: cnt x nrows);
+                // a single-problem system also keeps the other shape for the tuner
+                const bool small = (long long) ((D.n[0] + MG_TILE_X - 1) / MG_TILE_X) * ((D.n[1] + MG_TILE_Y - 1) / MG_TILE_Y) < 2LL * ctx->num_sms;
+                auto tiles = [&](bool sm, std::vector<Chunk>& out) {
+                    const int tx = sm ? MG_TILE_X_SMALL : MG_TILE_X, ty = sm ? MG_TILE_Y / 2 : MG_TILE_Y;
+                    for (int j0 = 0; j0 < D.n[1]; j0 += ty)
+                        for (int i0 = 0; i0 < D.n[0]; i0 += tx) {
+                            Chunk c{li, j0, 0, i0, tx};
+                            c.nrows = ty;
+                            out.push_back(c);
+                        }
+                };
+                tiles(small, S->tile_ch[l]);
+                if (S->probs.size() == 1 && tune_enabled()) tiles(!small, S->tile_alt[l]);
             } else {
                 const bool zmarch = !zoff && D.ndim == 3 && D.table && D.rbgs && !D.coarsest && D.N >= MG_ZT_MIN && D.n[0] >= 3 && D.n[1] >= 3 &&
                                     D.n[2] >= 3;
@@ -758,7 +862,7 @@ int mg_finalize(MGSystem* S) {
     S->nprob = (int) S->probs.size();
     if (!S->h_active) OPG_CUDA(cudaMallocHost(&S->h_active, sizeof(int)));
     OPG_CUDA(cudaStreamSynchronize(ctx->stream));
-    return OPFLOW_OK;
+    return tune_levels(S);
 }
 
 // One V-cycle on the level-0 residuals of the active problems: z = M r.  Each problem sees the same
@@ -780,12 +884,12 @@ static int vcycle(MGSystem* S) {
         const ChunkList& Z = S->d_zsm[l];
         for (int it = 0; it < S->pre; ++it) {
             OPG_TRY(mg_launch_smooth(s, sms, f32, S->dL, C.ptr, C.n, 0, sc));
-            OPG_TRY(mg_launch_smooth_z(s, sms, f32, S->dL, Z.ptr, Z.n, 0, sc));
+            OPG_TRY(mg_launch_smooth_z(s, sms, f32, S->dL, Z.ptr, Z.n, 0, sc, S->zb[l]));
             OPG_TRY(mg_launch_smooth(s, sms, f32, S->dL, C.ptr, C.n, 1, sc));
-            OPG_TRY(mg_launch_smooth_z(s, sms, f32, S->dL, Z.ptr, Z.n, 1, sc));
+            OPG_TRY(mg_launch_smooth_z(s, sms, f32, S->dL, Z.ptr, Z.n, 1, sc, S->zb[l]));
         }
         OPG_TRY(mg_launch_residual(s, sms, f32, S->dL, C.ptr, C.n, sc));
-        OPG_TRY(mg_launch_residual_z(s, sms, f32, S->dL, Z.ptr, Z.n, sc));
+        OPG_TRY(mg_launch_residual_z(s, sms, f32, S->dL, Z.ptr, Z.n, sc, S->zb[l]));
     }
     OPG_TRY(mg_launch_bottom(s, sms, f32, S->dL, S->dbottom, S->nbottom, sc, S->pre, S->post, S->bottom_cells));
     OPG_TRY(mg_launch_coarse(s, sms, f32, S->dL, S->dcoarse, S->ncoarse, sc));
@@ -798,12 +902,12 @@ static int vcycle(MGSystem* S) {
         const ChunkList& C = S->d_smooth[l];
         const ChunkList& Z = S->d_zsm[l];
         OPG_TRY(mg_launch_prolong(s, sms, f32, S->dL, S->d_prolong[l].ptr, S->d_prolong[l].n, sc));
-        OPG_TRY(mg_launch_prolong_z(s, sms, f32, S->dL, Z.ptr, Z.n, sc));
+        OPG_TRY(mg_launch_prolong_z(s, sms, f32, S->dL, Z.ptr, Z.n, sc, S->zb[l]));
         for (int it = 0; it < S->post; ++it) {
             OPG_TRY(mg_launch_smooth(s, sms, f32, S->dL, C.ptr, C.n, 1, sc));
-            OPG_TRY(mg_launch_smooth_z(s, sms, f32, S->dL, Z.ptr, Z.n, 1, sc));
+            OPG_TRY(mg_launch_smooth_z(s, sms, f32, S->dL, Z.ptr, Z.n, 1, sc, S->zb[l]));
             OPG_TRY(mg_launch_smooth(s, sms, f32, S->dL, C.ptr, C.n, 0, sc));
-            OPG_TRY(mg_launch_smooth_z(s, sms, f32, S->dL, Z.ptr, Z.n, 0, sc));
+            OPG_TRY(mg_launch_smooth_z(s, sms, f32, S->dL, Z.ptr, Z.n, 0, sc, S->zb[l]));
         }
     }
     return OPFLOW_OK;
@@ -1054,6 +1158,9 @@ int mg_compose(MGSystem* C, const std::vector<MGSystem*>& parts, const std::vect
     C->prolong_ch.assign(C->nlevels, {});
     C->tile_ch.assign(C->nlevels, {});
     C->zsm_ch.assign(C->nlevels, {});
+    C->zb.assign(C->nlevels, 4);
+    C->tile_alt.assign(C->nlevels, {});
+    std::vector<size_t> zb_tiles(C->nlevels, 0);  // each level takes the batch of the part with most tiles there
     C->coarse_sm_ch.clear();
     for (size_t q = 0; q < parts.size(); ++q) {
         MGSystem* P = parts[q];
@@ -1080,6 +1187,10 @@ int mg_compose(MGSystem* C, const std::vector<MGSystem*>& parts, const std::vect
             shift(P->prolong_ch[l], C->prolong_ch[l]);
             shift(P->tile_ch[l], C->tile_ch[l]);
             shift(P->zsm_ch[l], C->zsm_ch[l]);
+            if (P->zsm_ch[l].size() > zb_tiles[l]) {
+                zb_tiles[l] = P->zsm_ch[l].size();
+                C->zb[l] = P->zb[l];
+            }
         }
         shift(P->coarse_sm_ch, C->coarse_sm_ch);
         KrylovDev K = P->kd_host[0];

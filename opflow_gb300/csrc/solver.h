@@ -72,6 +72,10 @@ struct MGSystem {
     // tiles of the 3D levels smoothed by the z-marching kernel (such levels are not in smooth_ch)
     std::vector<std::vector<Chunk>> zsm_ch;
     std::vector<ChunkList> d_zsm;
+    std::vector<int> zb;  // planes per load batch of the z-marching kernels, per level (tuned)
+    bool tune_measure = true;  // false: cached tuner choices only, nothing timed (the request server)
+    // the other 2D tile shape of a tiled level, when the tuner is to time it against tile_ch
+    std::vector<std::vector<Chunk>> tile_alt;
     std::vector<Chunk> coarse_sm_ch;
     ChunkList d_coarse_sm;
     LvlDev* dL = nullptr;

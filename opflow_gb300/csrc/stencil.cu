@@ -11,9 +11,12 @@
 //   FAST  - exact 64-bit fixed point: values are converted once when staged, the second differences
 //           are exact integer sums, one 64x53-bit product per weight group, one rounding back.
 #include "stencil.h"
+#include "tune.h"
 
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <vector>
 
 namespace opg {
 
@@ -370,22 +373,63 @@ __global__ void __launch_bounds__(32 * RB_WARPS, 4) axis3d_rb_kernel(FieldView i
     if (FAST) block_max_commit(vmax, &maxslots[(step + 1) % 3]);
 }
 
-// 3D tiling: register-blocked warps for the fixed-point mode (integer-issue bound, gains from the
-// absent barriers), shared-memory tiles for the exact mode (float64-pipe bound, measured slightly
-// faster); OPFLOW_AXIS_TILING=register|smem overrides, read at every launch so that one process can
-// compare the two
-static bool use_register_tiles(bool fast) {
+// 3D tiling: register-blocked warps (the measured default for the fixed-point mode: integer-issue
+// bound, gains from the absent barriers) or shared-memory tiles (the default for the exact mode:
+// float64-pipe bound).  Both give the same values; the tuner times the two on the first launch of a
+// (mode, box, stencil) key (a repeated launch rewrites `out` and the max slot with the same values),
+// and OPFLOW_AXIS_TILING=register|smem overrides it, read at every launch.
+static int axis_launch_tiling(opflow_ctx ctx, const FieldView& in, const FieldView& out, const Box& box, const AxisParams& P, bool fast,
+                              unsigned long long* maxslots, int step, bool reg);
+
+static bool use_register_tiles(opflow_ctx ctx, const FieldView& in, const FieldView& out, const Box& box, const AxisParams& P, bool fast,
+                               unsigned long long* maxslots, int step) {
     const char* e = getenv("OPFLOW_AXIS_TILING");
     if (e && strcmp(e, "smem") == 0) return false;
     if (e && strcmp(e, "register") == 0) return true;
-    return fast;
+    if (!tune_enabled()) return fast;
+    unsigned long long h = tune_hash(&P.ndim, sizeof P.ndim);
+    h = tune_hash(P.h, sizeof P.h, h);
+    h = tune_hash(P.inv_h, sizeof P.inv_h, h);
+    h = tune_hash(P.pow2, sizeof P.pow2, h);
+    h = tune_hash(P.order, sizeof P.order, h);
+    h = tune_hash(&P.s, sizeof P.s, h);
+    h = tune_hash(&P.iso, sizeof P.iso, h);
+    h = tune_hash(P.wm, sizeof P.wm, h);
+    h = tune_hash(P.wshift, sizeof P.wshift, h);
+    h = tune_hash(P.wneg, sizeof P.wneg, h);
+    h = tune_hash(&P.bound_bits, sizeof P.bound_bits, h);
+    char key[160];
+    std::snprintf(key, sizeof key, "axis3d/%s/%dx%dx%d/%016llx", fast ? "fixed" : "exact", box.hi[0] - box.lo[0], box.hi[1] - box.lo[1],
+                  box.hi[2] - box.lo[2], h);
+    const std::vector<int> cands = fast ? std::vector<int>{1, 0} : std::vector<int>{0, 1};
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(ctx->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return tune_cached(key, cands) == 1;
+    return tune_pick(key, cands, [&](int reg) {
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        float ms = -1.f;
+        if (cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess &&
+            axis_launch_tiling(ctx, in, out, box, P, fast, maxslots, step, reg) == OPFLOW_OK && cudaEventRecord(e0, ctx->stream) == cudaSuccess &&
+            axis_launch_tiling(ctx, in, out, box, P, fast, maxslots, step, reg) == OPFLOW_OK && cudaEventRecord(e1, ctx->stream) == cudaSuccess &&
+            cudaEventSynchronize(e1) == cudaSuccess)
+            cudaEventElapsedTime(&ms, e0, e1);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        return ms;
+    }) == 1;
 }
 
 int axis_launch(opflow_ctx ctx, const FieldView& in, const FieldView& out, const Box& box, const AxisParams& P, bool fast,
                 unsigned long long* maxslots, int step) {
     const int nx = box.hi[0] - box.lo[0], ny = box.hi[1] - box.lo[1], nz = box.hi[2] - box.lo[2];
     if (nx <= 0 || ny <= 0 || nz <= 0) return OPFLOW_OK;
-    if (P.ndim == 3 && use_register_tiles(fast)) {
+    const bool reg = P.ndim == 3 && use_register_tiles(ctx, in, out, box, P, fast, maxslots, step);
+    return axis_launch_tiling(ctx, in, out, box, P, fast, maxslots, step, reg);
+}
+
+static int axis_launch_tiling(opflow_ctx ctx, const FieldView& in, const FieldView& out, const Box& box, const AxisParams& P, bool fast,
+                              unsigned long long* maxslots, int step, bool reg) {
+    const int nx = box.hi[0] - box.lo[0], ny = box.hi[1] - box.lo[1], nz = box.hi[2] - box.lo[2];
+    if (P.ndim == 3 && reg) {
         const int tiles_x = (nx + RB_COLS - 1) / RB_COLS, tiles_y = (ny + RB - 1) / RB;
         const int bx = (tiles_x * tiles_y + RB_WARPS - 1) / RB_WARPS;
         int zchunks = (ctx->num_sms * 6 + bx - 1) / bx;
