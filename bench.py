@@ -21,6 +21,8 @@ Workloads (seeded synthetic inputs with the configurations' shapes and value dis
   batched 512 corner-node Dirichlet problems (I - k Lap) u = f of sides 65..1025 in one batched
           solve, mixed precision, next to a loop of plain FP64 single solves
   weno    WENO5-JS + RK3 on 65536 periodic lines of 4096 cells (one RK3 step per bench step)
+  ftcs_batch  explicit steps of 256 uneven 2D grids (side LogU[65,513]) in one launch per step
+          (opflow_assign_batch), next to the same grids stepped one after another
 
 `--impl reference` times the reference's CPU algorithm (the C restatement under oracle/, the
 reference itself does not build on the Arm machine) on the host cores for the same metric.
@@ -140,6 +142,9 @@ def workload_cfg(name):
     if name == "ftcs2d":
         return dict(workload="ftcs2d", grid=[1025, 1025], loc="node", bc="dirichlet 0", dt="0.2*h^2", init="U[0,1) seeded",
                     expression="u = u + dt*alpha*(d2x(u)+d2y(u))", l2="field 8.4 MB fits in L2: L2-resident")
+    if name == "ftcs_batch":
+        return dict(workload="ftcs_batch", grids=256, side="LogU[65,513] nodes", mode="exact",
+                    sample="the host port steps one 1025^2 grid (the same update, one grid at a time)")
     raise SystemExit("unknown workload " + name)
 
 
@@ -725,6 +730,92 @@ def run_weno(args, torch, api, capi, np, ctx, stream, world, rank, local, dist):
 
 
 # ------------------------------------------------------------------------------------------- ours
+def run_ftcs_batch(args, torch, api, capi, np, ctx, stream, world, rank, local, dist):
+    """Explicit steps of many uneven grids in one launch per step: 256 2D node grids of side LogU[65,513]
+    (seeded), Dirichlet 0, u = u + 0.2 h^2 (d2x(u) + d2y(u)) in exact mode, batched (opflow_assign_batch)
+    next to the same assignments run one grid after another."""
+    rng = np.random.default_rng(4242 + rank)
+    sides = [int(round(np.exp(rng.uniform(np.log(65), np.log(513))))) for _ in range(256)]
+    fields, exprs, hosts = [], [], []
+    for k, n in enumerate(sides):
+        mesh = api.MeshBuilder().newMesh(n, n).setMeshOfDim(0, 0.0, 1.0).setMeshOfDim(1, 0.0, 1.0).build()
+        b = api.ExprBuilder().setMesh(mesh).setName("u%d" % k).setLoc(api.LocOnMesh.Corner)
+        for d in range(2):
+            b.setBC(d, api.DimPos.start, api.BCType.Dirc, 0.0).setBC(d, api.DimPos.end, api.BCType.Dirc, 0.0)
+        u = b.build(ctx)
+        a = u.download()
+        a[...] = 0.0
+        sl = u.index_slices([tuple(u.info.assignable[d]) for d in range(2)])
+        a[sl] = rng.random(a[sl].shape)
+        u.upload(a)
+        host = torch.empty(a.size, dtype=torch.float64, pin_memory=True)
+        host.numpy()[:] = a.reshape(-1)
+        hosts.append(host)
+        h = 1.0 / (n - 1)
+        fields.append(u)
+        exprs.append(u + 0.2 * h * h * (api.d2x(u) + api.d2y(u)))
+    pts = sum((n - 2) ** 2 for n in sides)
+    pairs = list(zip(fields, exprs))
+    api.assign_batch(pairs, steps=max(1, args.warmup))
+    for u, e in pairs:
+        u.assign(e, mode="exact", steps=1)
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    launches0 = capi.launch_count()
+    with ClockSampler(local) as clk:
+        ev[0].record(stream)
+        api.assign_batch(pairs, steps=args.steps)
+        ev[1].record(stream)
+        torch.cuda.synchronize()
+    launches = capi.launch_count() - launches0
+    ms = ev[0].elapsed_time(ev[1])
+    ev[2].record(stream)
+    for u, e in pairs:
+        u.assign(e, mode="exact", steps=args.steps)
+    ev[3].record(stream)
+    torch.cuda.synchronize()
+    ms_loop = ev[2].elapsed_time(ev[3])
+    value = pts * args.steps / (ms * 1e-3) / 1e9
+    # end to end with host buffers: every field uploaded, one batched step, every field downloaded
+    P = C.POINTER(C.c_double)
+    L = capi.lib()
+    e2e_steps = max(1, min(args.steps, 5))
+    t0 = time.perf_counter()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        for u, host in zip(fields, hosts):
+            capi.check(L.opflow_field_upload(u.handle, C.cast(host.data_ptr(), P), host.numel()))
+        api.assign_batch(pairs, steps=1)
+        for u, host in zip(fields, hosts):
+            capi.check(L.opflow_field_download(u.handle, C.cast(host.data_ptr(), P), host.numel()))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = max(e0.elapsed_time(e1), (time.perf_counter() - t0) * 1e3)
+    nbytes = sum(h.numel() for h in hosts) * 8
+    peak, peak_src = peak_hbm()
+    achieved = 16.0 * pts / (ms / args.steps * 1e-3) / 1e9
+    line = {"metric": METRIC, "value": value, "unit": "GLUP/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": "ftcs_batch", "grids": len(sides), "side": "LogU[65,513] nodes", "points": pts, "mode": "exact",
+                       "one_grid_at_a_time_glups": pts * args.steps / (ms_loop * 1e-3) / 1e9, "batched_over_loop": ms_loop / ms,
+                       "l2": "%.1f MB of fields in total (L2-resident across steps)" % (nbytes / 1e6),
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_src,
+                         "traffic": None, "kernel": "interp_batch_kernel (whole step: every grid's tiles from one work queue)",
+                         "algorithmic_bytes_per_launch": 16.0 * pts},
+            "cpu_baseline": None,
+            "e2e": {"value": pts * e2e_steps / (e2e_ms * 1e-3) / 1e9, "unit": "GLUP/s", "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+                    "steps": e2e_steps},
+            "gpu_launches": launches, "clocks": clk.summary()}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -773,6 +864,8 @@ def run_ours(args):
 
     if args.workload == "weno":
         return run_weno(args, torch, api, capi, np, ctx, stream, world, rank, local, dist)
+    if args.workload == "ftcs_batch":
+        return run_ftcs_batch(args, torch, api, capi, np, ctx, stream, world, rank, local, dist)
 
     cfg = workload_cfg(args.workload)
     if args.grid:
@@ -891,7 +984,8 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="serve", choices=["serve", "poisson2d", "poisson3d", "batched", "ftcs3d", "ftcs2d", "weno"])
+    ap.add_argument("--workload", default="serve", choices=["serve", "poisson2d", "poisson3d", "batched", "ftcs3d", "ftcs2d", "weno",
+                                                            "ftcs_batch"])
     ap.add_argument("--problems", type=int, default=512, help="batched: problems per batch")
     ap.add_argument("--loop-sample", type=int, default=64, help="batched: problems timed in the plain FP64 one-at-a-time loop")
     ap.add_argument("--requests", type=int, default=48, help="serve: requests per measurement window")

@@ -245,9 +245,19 @@ enum opflow_eval_mode {
  * An expression that reads dst itself is evaluated out of place, as the reference does. */
 int opflow_assign(opflow_ctx ctx, opflow_field dst, int arith, const opflow_node* nodes, int n_nodes,
                   const opflow_field* leaves, int n_leaves, int mode);
+/* Many explicit assignments in one launch, each `dsts[i] <arith[i]>= expr_i` over its own field and
+ * grid (sizes may differ), `steps` times: a persistent grid takes tiles of every assignment's box from
+ * one work queue.  Each expression is evaluated in exact mode (the FTCS update where it has that
+ * shape, else the interpreter), so the values equal
+ * opflow_assign_repeat's in OPFLOW_EVAL_EXACT mode, step for step.  The destinations must differ and no
+ * assignment may read another one's destination (they run concurrently); an assignment may read its own
+ * destination (u = u + ...), as in opflow_assign.  No counterpart in the reference, which evaluates one
+ * field per FieldAssigner::assign call. */
+int opflow_assign_batch(opflow_ctx ctx, int n, const opflow_field* dsts, const int* arith, const opflow_node* const* nodes, const int* n_nodes,
+                        const opflow_field* const* leaves, const int* n_leaves, int steps);
 
 /* Runs `steps` repetitions of the same assignment (one fused kernel per step where the expression has
- * a specialised kernel; the launches are recorded once into a CUDA graph and replayed). */
+ * a specialised kernel). */
 int opflow_assign_repeat(opflow_ctx ctx, opflow_field dst, int arith, const opflow_node* nodes, int n_nodes,
                          const opflow_field* leaves, int n_leaves, int mode, int steps);
 

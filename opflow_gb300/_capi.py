@@ -119,6 +119,8 @@ _SIGS = {
     "opflow_field_device_ptr": [C.c_void_p, C.POINTER(C.c_void_p)],
     "opflow_field_update_padding": [C.c_void_p],
     "opflow_field_write_raw": [C.c_void_p, C.c_char_p, C.c_char_p, C.c_int, C.c_double],
+    "opflow_assign_batch": [C.c_void_p, C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_int), C.POINTER(C.c_void_p), C.POINTER(C.c_int),
+                            C.POINTER(C.c_void_p), C.POINTER(C.c_int), C.c_int],
     "opflow_tune_set_cache": [C.c_char_p],
     "opflow_tune_lookup": [C.c_char_p, C.POINTER(C.c_int)],
     "opflow_tune_stats": [C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)],

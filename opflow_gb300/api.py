@@ -984,6 +984,33 @@ class Batch:
 
 
 # ------------------------------------------------------------------------------------------------ serving
+def assign_batch(assignments, steps=1):
+    """Many explicit assignments in one launch per step (opflow_assign_batch): `assignments` holds
+    (dst, expr) or (dst, expr, op) with op one of "=", "+", "-", "*", "/" (as in CartesianField.assign),
+    over fields of any sizes; the values equal
+    dst.assign(expr, op, mode="exact", steps=steps) for each, step for step.  No assignment may read
+    another one's destination."""
+    n = len(assignments)
+    if n == 0:
+        return
+    keep = []
+    dsts, ariths, nn, nl = (C.c_void_p * n)(), (C.c_int * n)(), (C.c_int * n)(), (C.c_int * n)()
+    nodes_p, leaves_p = (C.c_void_p * n)(), (C.c_void_p * n)()
+    for i, a in enumerate(assignments):
+        dst, expr = a[0], a[1]
+        op = a[2] if len(a) > 2 else "="
+        nodes, leaves = serialize(expr)
+        hs = (C.c_void_p * max(1, len(leaves)))(*[f.handle.value for f in leaves])
+        keep += [nodes, hs]
+        dsts[i] = dst.handle.value
+        ariths[i] = _ARITH[op]
+        nodes_p[i] = C.cast(nodes, C.c_void_p)
+        nn[i] = len(nodes)
+        leaves_p[i] = C.cast(hs, C.c_void_p)
+        nl[i] = len(leaves)
+    check(lib().opflow_assign_batch(assignments[0][0].ctx.handle, n, dsts, ariths, nodes_p, nn, leaves_p, nl, int(steps)))
+
+
 def tune_set_cache(path):
     """Autotuner cache file (opflow_tune_set_cache): choices are loaded from `path` and new ones appended;
     None keeps them in memory only."""

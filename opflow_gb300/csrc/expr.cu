@@ -405,54 +405,59 @@ __device__ __forceinline__ double apply_arith(int arith, double o, double v) {
 
 // ======================================================================================== generic kernel
 #define STACK_MAX 24
+// one cell (box-relative index t) of the postfix program: out = value, or cur op value
+__device__ __forceinline__ void interp_cell(const Instr* __restrict__ prog, int nprog, const LeafViews& leaves, const MeshPtrs& mesh,
+                                            const Box& box, const FieldView& out, const FieldView& cur, int arith, long long t) {
+    int i, j, k;
+    box_index(t, box, i, j, k);
+    const int idx[3] = {i, j, k};
+    double st[STACK_MAX];
+    int sp = 0;
+    for (int p = 0; p < nprog; ++p) {
+        const Instr in = prog[p];
+        switch (in.op) {
+            case P_LOAD: st[sp++] = ld(leaves.v[in.slot], i + in.off[0], j + in.off[1], k + in.off[2]); break;
+            case P_CONST: st[sp++] = in.v; break;
+            case P_ADD: sp--; st[sp - 1] = __dadd_rn(st[sp - 1], st[sp]); break;
+            case P_SUB: sp--; st[sp - 1] = __dsub_rn(st[sp - 1], st[sp]); break;
+            case P_MUL: sp--; st[sp - 1] = __dmul_rn(st[sp - 1], st[sp]); break;
+            case P_DIV: sp--; st[sp - 1] = __ddiv_rn(st[sp - 1], st[sp]); break;
+            case P_NEG: st[sp - 1] = -st[sp - 1]; break;
+            case P_DX: st[sp++] = mesh.dx[in.slot][idx[in.slot] + in.off[0] - mesh.es[in.slot]]; break;
+            case P_X: st[sp++] = mesh.x[in.slot][idx[in.slot] + in.off[0] - mesh.es[in.slot]]; break;
+            case P_WENO: {
+                sp -= 6;
+                const double* a = &st[sp - 1];
+                const double h = st[sp + 5];
+                const double w = weno_kernel(a[0], a[1], a[2], a[3], a[4], a[5], h);
+                // D1WENO53Upwind: the mirrored stencil's result, negated (exact)
+                st[sp - 1] = in.slot ? -w : w;
+                break;
+            }
+            case P_GT: sp--; st[sp - 1] = st[sp - 1] > st[sp] ? 1. : 0.; break;
+            case P_GE: sp--; st[sp - 1] = st[sp - 1] >= st[sp] ? 1. : 0.; break;
+            case P_LT: sp--; st[sp - 1] = st[sp - 1] < st[sp] ? 1. : 0.; break;
+            case P_LE: sp--; st[sp - 1] = st[sp - 1] <= st[sp] ? 1. : 0.; break;
+            case P_NE: sp--; st[sp - 1] = st[sp - 1] != st[sp] ? 1. : 0.; break;
+            case P_AND: sp--; st[sp - 1] = (st[sp - 1] != 0. && st[sp] != 0.) ? 1. : 0.; break;
+            case P_OR: sp--; st[sp - 1] = (st[sp - 1] != 0. || st[sp] != 0.) ? 1. : 0.; break;
+            case P_NOT: st[sp - 1] = st[sp - 1] == 0. ? 1. : 0.; break;
+            case P_SEL: sp -= 2; st[sp - 1] = st[sp - 1] != 0. ? st[sp] : st[sp + 1]; break;
+            case P_F1: st[sp - 1] = func1_eval(in.slot, st[sp - 1]); break;
+            case P_F2: sp--; st[sp - 1] = func2_eval(in.slot, st[sp - 1], st[sp]); break;
+            case P_LIM: st[sp - 1] = flux_limiter(in.slot, st[sp - 1]); break;
+        }
+    }
+    const long long o = (i - out.off[0]) + (j - out.off[1]) * out.sy + (k - out.off[2]) * out.sz;
+    out.data[o] = arith == OPFLOW_ASSIGN_EQ ? st[0] : apply_arith(arith, cur.data[o], st[0]);
+}
+
 __global__ void __launch_bounds__(128) interp_kernel(const Instr* __restrict__ prog, int nprog, LeafViews leaves, MeshPtrs mesh,
                                                      Box box, FieldView out, FieldView cur, int arith) {
     const long long nx = box.hi[0] - box.lo[0], ny = box.hi[1] - box.lo[1], nz = box.hi[2] - box.lo[2];
     const long long total = nx * ny * nz;
-    for (long long t = blockIdx.x * (long long) blockDim.x + threadIdx.x; t < total; t += (long long) gridDim.x * blockDim.x) {
-        int i, j, k;
-        box_index(t, box, i, j, k);
-        const int idx[3] = {i, j, k};
-        double st[STACK_MAX];
-        int sp = 0;
-        for (int p = 0; p < nprog; ++p) {
-            const Instr in = prog[p];
-            switch (in.op) {
-                case P_LOAD: st[sp++] = ld(leaves.v[in.slot], i + in.off[0], j + in.off[1], k + in.off[2]); break;
-                case P_CONST: st[sp++] = in.v; break;
-                case P_ADD: sp--; st[sp - 1] = __dadd_rn(st[sp - 1], st[sp]); break;
-                case P_SUB: sp--; st[sp - 1] = __dsub_rn(st[sp - 1], st[sp]); break;
-                case P_MUL: sp--; st[sp - 1] = __dmul_rn(st[sp - 1], st[sp]); break;
-                case P_DIV: sp--; st[sp - 1] = __ddiv_rn(st[sp - 1], st[sp]); break;
-                case P_NEG: st[sp - 1] = -st[sp - 1]; break;
-                case P_DX: st[sp++] = mesh.dx[in.slot][idx[in.slot] + in.off[0] - mesh.es[in.slot]]; break;
-                case P_X: st[sp++] = mesh.x[in.slot][idx[in.slot] + in.off[0] - mesh.es[in.slot]]; break;
-                case P_WENO: {
-                    sp -= 6;
-                    const double* a = &st[sp - 1];
-                    const double h = st[sp + 5];
-                    const double w = weno_kernel(a[0], a[1], a[2], a[3], a[4], a[5], h);
-                    // D1WENO53Upwind: the mirrored stencil's result, negated (exact)
-                    st[sp - 1] = in.slot ? -w : w;
-                    break;
-                }
-                case P_GT: sp--; st[sp - 1] = st[sp - 1] > st[sp] ? 1. : 0.; break;
-                case P_GE: sp--; st[sp - 1] = st[sp - 1] >= st[sp] ? 1. : 0.; break;
-                case P_LT: sp--; st[sp - 1] = st[sp - 1] < st[sp] ? 1. : 0.; break;
-                case P_LE: sp--; st[sp - 1] = st[sp - 1] <= st[sp] ? 1. : 0.; break;
-                case P_NE: sp--; st[sp - 1] = st[sp - 1] != st[sp] ? 1. : 0.; break;
-                case P_AND: sp--; st[sp - 1] = (st[sp - 1] != 0. && st[sp] != 0.) ? 1. : 0.; break;
-                case P_OR: sp--; st[sp - 1] = (st[sp - 1] != 0. || st[sp] != 0.) ? 1. : 0.; break;
-                case P_NOT: st[sp - 1] = st[sp - 1] == 0. ? 1. : 0.; break;
-                case P_SEL: sp -= 2; st[sp - 1] = st[sp - 1] != 0. ? st[sp] : st[sp + 1]; break;
-                case P_F1: st[sp - 1] = func1_eval(in.slot, st[sp - 1]); break;
-                case P_F2: sp--; st[sp - 1] = func2_eval(in.slot, st[sp - 1], st[sp]); break;
-                case P_LIM: st[sp - 1] = flux_limiter(in.slot, st[sp - 1]); break;
-            }
-        }
-        const long long o = (i - out.off[0]) + (j - out.off[1]) * out.sy + (k - out.off[2]) * out.sz;
-        out.data[o] = arith == OPFLOW_ASSIGN_EQ ? st[0] : apply_arith(arith, cur.data[o], st[0]);
-    }
+    for (long long t = blockIdx.x * (long long) blockDim.x + threadIdx.x; t < total; t += (long long) gridDim.x * blockDim.x)
+        interp_cell(prog, nprog, leaves, mesh, box, out, cur, arith, t);
 }
 
 // ======================================================================================== exact FTCS kernel
@@ -478,30 +483,77 @@ __device__ __forceinline__ double div_h(double x, double h, double y, int p2) {
     return __fma_rn(r, y, q);
 }
 
+// one cell (box-relative index t) of the exact FTCS update, D terms (D <= 3; a compile-time D unrolls)
+__device__ __forceinline__ void ftcs_cell(const FieldView& in, const FieldView& out, const Box& box, const FtcsParams& P, long long t, int D) {
+    int i, j, k;
+    box_index(t, box, i, j, k);
+    const long long o = (i - in.off[0]) + (j - in.off[1]) * in.sy + (k - in.off[2]) * in.sz;
+    const double c = in.data[o];
+    double sum = 0.;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        if (q >= D) break;
+        const int d = P.dims_order[q];
+        const long long st = d == 0 ? 1 : (d == 1 ? in.sy : in.sz);
+        const double l = in.data[o - st], r = in.data[o + st];
+        const double h = P.h[d], y = P.inv_h[d];
+        const int p2 = P.pow2[d];
+        const double a = div_h(__dsub_rn(r, c), h, y, p2);
+        const double b = div_h(__dsub_rn(c, l), h, y, p2);
+        const double d2 = div_h(__dsub_rn(a, b), h, y, p2);
+        sum = q == 0 ? d2 : __dadd_rn(sum, d2);
+    }
+    const long long oo = (i - out.off[0]) + (j - out.off[1]) * out.sy + (k - out.off[2]) * out.sz;
+    out.data[oo] = __dadd_rn(c, __dmul_rn(P.s, sum));
+}
+
 template <int D>
 __global__ void __launch_bounds__(256) ftcs_exact_kernel(FieldView in, FieldView out, Box box, FtcsParams P) {
     const long long nx = box.hi[0] - box.lo[0], ny = box.hi[1] - box.lo[1], nz = box.hi[2] - box.lo[2];
     const long long total = nx * ny * nz;
-    for (long long t = blockIdx.x * (long long) blockDim.x + threadIdx.x; t < total; t += (long long) gridDim.x * blockDim.x) {
-        int i, j, k;
-        box_index(t, box, i, j, k);
-        const long long o = (i - in.off[0]) + (j - in.off[1]) * in.sy + (k - in.off[2]) * in.sz;
-        const double c = in.data[o];
-        double sum = 0.;
-#pragma unroll
-        for (int q = 0; q < D; ++q) {
-            const int d = P.dims_order[q];
-            const long long st = d == 0 ? 1 : (d == 1 ? in.sy : in.sz);
-            const double l = in.data[o - st], r = in.data[o + st];
-            const double h = P.h[d], y = P.inv_h[d];
-            const int p2 = P.pow2[d];
-            const double a = div_h(__dsub_rn(r, c), h, y, p2);
-            const double b = div_h(__dsub_rn(c, l), h, y, p2);
-            const double d2 = div_h(__dsub_rn(a, b), h, y, p2);
-            sum = q == 0 ? d2 : __dadd_rn(sum, d2);
+    for (long long t = blockIdx.x * (long long) blockDim.x + threadIdx.x; t < total; t += (long long) gridDim.x * blockDim.x)
+        ftcs_cell(in, out, box, P, t, D);
+}
+
+// Many assignments in one launch (opflow_assign_batch): a persistent grid takes tiles of every
+// assignment's box from one work queue (an atomic counter over the tile table), so grids of uneven
+// sizes and expressions of uneven cost share the launch.  An FTCS-shaped item takes the exact FTCS
+// cell (the values of the specialised kernels), any other the interpreter.
+struct BatchItem {
+    const Instr* prog;
+    int nprog, arith;
+    int ftcs;          // 1: the exact FTCS update of `src`
+    FtcsParams fp;
+    FieldView src;
+    LeafViews leaves;
+    MeshPtrs mesh;
+    Box box;
+    FieldView out, cur;
+};
+struct BatchTile {
+    int item;
+    int n;           // cells
+    long long t0;    // first box-relative cell
+};
+constexpr int BATCH_TILE = 4096;
+
+__global__ void __launch_bounds__(128) interp_batch_kernel(const BatchItem* __restrict__ items, const BatchTile* __restrict__ tiles, int ntiles,
+                                                           int* next) {
+    __shared__ int tile;
+    for (;;) {
+        if (threadIdx.x == 0) tile = atomicAdd(next, 1);
+        __syncthreads();
+        const int c = tile;
+        __syncthreads();  // every thread has read `tile` before thread 0 takes the next one
+        if (c >= ntiles) return;
+        const BatchTile T = tiles[c];
+        const BatchItem& I = items[T.item];
+        if (I.ftcs) {
+            for (long long t = T.t0 + threadIdx.x; t < T.t0 + T.n; t += blockDim.x) ftcs_cell(I.src, I.out, I.box, I.fp, t, I.fp.ndim);
+        } else {
+            for (long long t = T.t0 + threadIdx.x; t < T.t0 + T.n; t += blockDim.x)
+                interp_cell(I.prog, I.nprog, I.leaves, I.mesh, I.box, I.out, I.cur, I.arith, t);
         }
-        const long long oo = (i - out.off[0]) + (j - out.off[1]) * out.sy + (k - out.off[2]) * out.sz;
-        out.data[oo] = __dadd_rn(c, __dmul_rn(P.s, sum));
     }
 }
 
@@ -1104,6 +1156,95 @@ int opflow_assign_repeat(opflow_ctx ctx, opflow_field dst, int arith, const opfl
 int opflow_assign(opflow_ctx ctx, opflow_field dst, int arith, const opflow_node* nodes, int n_nodes, const opflow_field* leaves, int n_leaves,
                   int mode) {
     return opflow_assign_repeat(ctx, dst, arith, nodes, n_nodes, leaves, n_leaves, mode, 1);
+}
+
+int opflow_assign_batch(opflow_ctx ctx, int n, const opflow_field* dsts, const int* arith, const opflow_node* const* nodes, const int* n_nodes,
+                        const opflow_field* const* leaves, const int* n_leaves, int steps) {
+    if (!ctx || n < 0 || (n > 0 && (!dsts || !arith || !nodes || !n_nodes || !leaves || !n_leaves))) return fail(OPFLOW_E_INVALID, "bad batch arguments");
+    if (steps < 0) return fail(OPFLOW_E_INVALID, "negative step count");
+    if (n == 0 || steps == 0) return OPFLOW_OK;
+    for (int i = 0; i < n; ++i) {
+        if (!dsts[i]) return fail(OPFLOW_E_INVALID, "null destination %d", i);
+        if (dsts[i]->ctx != ctx) return fail(OPFLOW_E_INVALID, "destination %d belongs to another context", i);
+        for (int q = 0; q < i; ++q)
+            if (dsts[q] == dsts[i]) return fail(OPFLOW_E_INVALID, "destinations %d and %d are the same field", q, i);
+    }
+    // the assignments run concurrently: none may read another one's destination
+    for (int i = 0; i < n; ++i)
+        for (int s = 0; s < n_leaves[i]; ++s)
+            for (int q = 0; q < n; ++q)
+                if (q != i && leaves[i][s] == dsts[q]) return fail(OPFLOW_E_INVALID, "assignment %d reads the destination of assignment %d", i, q);
+    std::vector<Plan> plans(n);
+    std::vector<int> prog_at(n);
+    std::vector<Instr> progs;
+    int rc = OPFLOW_OK;
+    for (int i = 0; i < n && rc == OPFLOW_OK; ++i) {
+        // exact mode for every item: the FTCS cell where the expression has that shape, else the interpreter
+        rc = build_plan(ctx, dsts[i], arith[i], nodes[i], n_nodes[i], leaves[i], n_leaves[i], OPFLOW_EVAL_EXACT, &plans[i]);
+        free_plan(&plans[i]);
+        if (rc == OPFLOW_OK && plans[i].aliased) rc = ensure_back(dsts[i]);
+        prog_at[i] = (int) progs.size();
+        progs.insert(progs.end(), plans[i].prog.begin(), plans[i].prog.end());
+    }
+    if (rc) return rc;
+    // tiles of every box; items for even and odd steps (aliased destinations swap buffers every step)
+    std::vector<BatchTile> tiles;
+    for (int i = 0; i < n; ++i) {
+        const long long total = plans[i].box.count();
+        for (long long t0 = 0; t0 < total; t0 += BATCH_TILE) tiles.push_back(BatchTile{i, (int) std::min<long long>(BATCH_TILE, total - t0), t0});
+    }
+    if (tiles.size() > (size_t) 0x7fffffff) return fail(OPFLOW_E_INVALID, "too many tiles");
+    std::vector<BatchItem> items(2 * (size_t) n);
+    for (int par = 0; par < 2; ++par)
+        for (int i = 0; i < n; ++i) {
+            opflow_field d = dsts[i];
+            const bool flip = par == 1 && plans[i].aliased;
+            const FieldView front = flip ? d->view_back() : d->view(), back = flip ? d->view() : d->view_back();
+            BatchItem& I = items[(size_t) par * n + i];
+            I.nprog = (int) plans[i].prog.size();
+            I.arith = arith[i];
+            I.leaves = plans[i].leaves;
+            for (int s = 0; s < n_leaves[i]; ++s) I.leaves.v[s] = leaves[i][s] == d ? front : leaves[i][s]->view();
+            I.mesh = plans[i].mesh;
+            I.box = plans[i].box;
+            I.out = plans[i].aliased ? back : front;
+            I.cur = front;
+            I.ftcs = plans[i].kind == PLAN_FTCS_EXACT || plans[i].kind == PLAN_AXIS_EXACT;
+            I.fp = plans[i].ftcs;
+            if (I.ftcs) I.src = I.leaves.v[plans[i].src_slot];
+        }
+    const size_t bytes_items = items.size() * sizeof(BatchItem), bytes_tiles = std::max<size_t>(1, tiles.size()) * sizeof(BatchTile);
+    const size_t bytes_prog = std::max<size_t>(1, progs.size()) * sizeof(Instr);
+    char* blob = (char*) dev_alloc(ctx, bytes_items + bytes_tiles + bytes_prog + 256);
+    if (!blob) return fail(OPFLOW_E_NOMEM, "batch tables");
+    auto align = [](size_t v) { return (v + 15) & ~(size_t) 15; };
+    BatchItem* d_items = (BatchItem*) blob;
+    BatchTile* d_tiles = (BatchTile*) (blob + align(bytes_items));
+    Instr* d_prog = (Instr*) (blob + align(bytes_items) + align(bytes_tiles));
+    int* d_next = (int*) (blob + align(bytes_items) + align(bytes_tiles) + align(bytes_prog));
+    for (size_t q = 0; q < items.size(); ++q) items[q].prog = d_prog + prog_at[q % n];
+    rc = OPFLOW_OK;
+    if (cudaMemcpyAsync(d_items, items.data(), bytes_items, cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess ||
+        (!tiles.empty() && cudaMemcpyAsync(d_tiles, tiles.data(), tiles.size() * sizeof(BatchTile), cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess) ||
+        (!progs.empty() && cudaMemcpyAsync(d_prog, progs.data(), progs.size() * sizeof(Instr), cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess))
+        rc = fail(OPFLOW_E_CUDA, "batch tables upload failed");
+    const int grid = (int) std::max<long long>(1, std::min<long long>((long long) tiles.size(), (long long) ctx->num_sms * 8));
+    for (int s = 0; s < steps && rc == OPFLOW_OK; ++s) {
+        if (!tiles.empty()) {
+            if (cudaMemsetAsync(d_next, 0, sizeof(int), ctx->stream) != cudaSuccess) { rc = fail(OPFLOW_E_CUDA, "batch queue reset failed"); break; }
+            interp_batch_kernel<<<grid, 128, 0, ctx->stream>>>(d_items + (size_t) (s & 1) * n, d_tiles, (int) tiles.size(), d_next);
+            OPG_LAUNCHED();
+            rc = check_launch("interp_batch_kernel");
+        }
+        for (int i = 0; i < n && rc == OPFLOW_OK; ++i) {
+            if (plans[i].aliased) dsts[i]->cur = 1 - dsts[i]->cur;
+            dsts[i]->version++;
+            rc = update_padding_assign(dsts[i]);
+        }
+    }
+    dev_free(ctx, blob);
+    if (rc == OPFLOW_OK && cudaStreamSynchronize(ctx->stream) != cudaSuccess) rc = fail(OPFLOW_E_CUDA, "batched assign failed: %s", cudaGetErrorString(cudaGetLastError()));
+    return rc;
 }
 
 int opflow_field_fill(opflow_field f, int arith, double c) {
