@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define OPFLOW_GPU_ABI_VERSION 2
+#define OPFLOW_GPU_ABI_VERSION 3
 
 /* ---- status codes ---------------------------------------------------------------------------- */
 enum opflow_status {
@@ -394,6 +394,8 @@ typedef struct {
                                     is admitted, so it must stay valid and unchanged until the request's
                                     result is available (pinned host memory gives the fastest copy)      */
     double* x_out;               /* host buffer for the final solution, n unknowns (may be NULL)        */
+    const double* x0;            /* host initial guess of the first solve, n unknowns (NULL: zero); a
+                                    session restored from a checkpoint passes the checkpoint here and as f */
 } opflow_request;
 
 typedef struct {
@@ -423,6 +425,12 @@ int opflow_server_submit(opflow_server s, const opflow_request* req, long long* 
 /* wait != 0 blocks until the request is done; otherwise *done tells whether `out` was filled */
 int opflow_server_result(opflow_server s, long long id, int wait, int* done, opflow_request_result* out);
 int opflow_server_drain(opflow_server s);
+/* Checkpoint of a running session (steps > 1) at its next step boundary: x_out (n values) receives the
+ * solver state after *steps_done steps (for a pinned problem, before the final shift).  Submitting the
+ * same problem with f = x0 = that state and steps - *steps_done steps continues the session bit for bit
+ * (the state can go to disk through a field and opflow_field_write_raw).  OPFLOW_E_INVALID for an
+ * unknown request, a single solve, a wrong n, or a session that finishes before its next boundary. */
+int opflow_server_checkpoint(opflow_server s, long long id, double* x_out, size_t n, int* steps_done);
 int opflow_server_stats(opflow_server s, opflow_serve_stats* out);
 int opflow_server_destroy(opflow_server s);
 

@@ -78,7 +78,8 @@ class ProblemDesc(C.Structure):
 
 
 class Request(C.Structure):
-    _fields_ = [("problem", ProblemDesc), ("steps", C.c_int), ("f", C.POINTER(C.c_double)), ("x_out", C.POINTER(C.c_double))]
+    _fields_ = [("problem", ProblemDesc), ("steps", C.c_int), ("f", C.POINTER(C.c_double)), ("x_out", C.POINTER(C.c_double)),
+                ("x0", C.POINTER(C.c_double))]
 
 
 class RequestResult(C.Structure):
@@ -155,6 +156,7 @@ _SIGS = {
     "opflow_server_submit": [C.c_void_p, C.POINTER(Request), C.POINTER(C.c_longlong)],
     "opflow_server_result": [C.c_void_p, C.c_longlong, C.c_int, C.POINTER(C.c_int), C.POINTER(RequestResult)],
     "opflow_server_drain": [C.c_void_p],
+    "opflow_server_checkpoint": [C.c_void_p, C.c_longlong, C.POINTER(C.c_double), C.c_size_t, C.POINTER(C.c_int)],
     "opflow_server_stats": [C.c_void_p, C.POINTER(ServeStats)],
     "opflow_server_destroy": [C.c_void_p],
     "opflow_residual_norms_noalloc": [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_void_p, C.c_void_p, C.c_void_p,

@@ -1050,19 +1050,30 @@ class Server:
         self.handle = h
         self._keep = {}
 
-    def submit(self, problem, f, steps=1, out=None):
+    def submit(self, problem, f, steps=1, out=None, x0=None):
+        """Queues a request; x0 is the first solve's initial guess (a restored session's checkpoint)."""
         f = np.ascontiguousarray(f, dtype=np.float64).reshape(-1)
         req = capi.Request()
         req.problem = problem.to_c()
         req.steps = int(steps)
         req.f = f.ctypes.data_as(C.POINTER(C.c_double))
+        if x0 is not None:
+            x0 = np.ascontiguousarray(x0, dtype=np.float64).reshape(-1)
+            req.x0 = x0.ctypes.data_as(C.POINTER(C.c_double))
         if out is not None:
             assert out.dtype == np.float64 and out.flags["C_CONTIGUOUS"]
             req.x_out = out.ctypes.data_as(C.POINTER(C.c_double))
         rid = C.c_longlong(0)
         check(lib().opflow_server_submit(self.handle, C.byref(req), C.byref(rid)))
-        self._keep[rid.value] = (f, out)
+        self._keep[rid.value] = (f, out, x0)
         return rid.value
+
+    def checkpoint(self, rid, n):
+        """(state, steps done) of a running session at its next step boundary (opflow_server_checkpoint)."""
+        x = np.empty(int(n))
+        k = C.c_int(0)
+        check(lib().opflow_server_checkpoint(self.handle, rid, x.ctypes.data_as(C.POINTER(C.c_double)), x.size, C.byref(k)))
+        return x, k.value
 
     def result(self, rid, wait=True):
         res = capi.RequestResult()

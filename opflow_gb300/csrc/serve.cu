@@ -36,8 +36,12 @@ struct Req {
     opflow_problem_desc pd{};
     int steps = 1;
     const double* f = nullptr;  // the caller's right-hand side, read at admission
+    const double* x0 = nullptr;  // the caller's initial guess (or null), read at admission
     long long nf = 0;
     double* x_out = nullptr;
+    double* ckpt_out = nullptr;  // a requested checkpoint's buffer
+    int ckpt_state = 0;          // 0 none, 1 requested, 2 written (steps in ckpt_steps)
+    int ckpt_steps = 0;
     Clock::time_point t_submit, t_admit, t_done;
     MGSystem* sys = nullptr;
     opflow_field t = nullptr, rhs = nullptr;
@@ -125,6 +129,7 @@ static int setup_req(opflow_server S, Req* r, Scal* seed) {
     r->N = M->probs[0].levels[0].N;
     if (r->nf != r->N) return fail(OPFLOW_E_INVALID, "request %lld: f has %lld values, the problem %lld unknowns", r->id, r->nf, r->N);
     OPG_CUDA(cudaMemcpyAsync(M->probs[0].b, r->f, r->N * 8, cudaMemcpyHostToDevice, ctx->stream));
+    if (r->x0) OPG_CUDA(cudaMemcpyAsync(M->kd_host[0].x, r->x0, r->N * 8, cudaMemcpyHostToDevice, ctx->stream));
     ProblemHost& P = M->probs[0];
     r->pinned = P.singular && !P.has_dirichlet;
     if (r->pinned) {
@@ -313,6 +318,7 @@ static void worker_loop(opflow_server S) {
         std::vector<Scal> keep_state;
         std::vector<std::pair<size_t, size_t>> restarted;  // (index in keep, index in the composite)
         std::vector<std::pair<Req*, int>> finished;
+        std::vector<Req*> checkpointed;
         double* slots = S->d_slots;
         for (size_t i = 0; i < S->active.size(); ++i) {
             Req* r = S->active[i];
@@ -326,6 +332,15 @@ static void worker_loop(opflow_server S) {
             if (ok && r->steps_done < r->steps) {
                 // next backward-Euler step: the solution becomes the right-hand side, same operator
                 const KrylovDev& K = r->sys->kd_host[0];
+                bool want = false;
+                {
+                    std::lock_guard<std::mutex> lk(S->mu);
+                    want = r->ckpt_state == 1;
+                }
+                if (want) {  // the state after this step, before the next one changes it
+                    cudaMemcpyAsync(r->ckpt_out, K.x, r->N * 8, cudaMemcpyDeviceToHost, S->own_ctx.stream);
+                    checkpointed.push_back(r);
+                }
                 cudaMemcpyAsync(r->sys->probs[0].b, K.x, r->N * 8, cudaMemcpyDeviceToDevice, S->own_ctx.stream);
                 mg_prepare_problem(r->sys, S->params.tol, S->comp.dS + i);
                 restarted.emplace_back(keep.size(), i);
@@ -341,6 +356,14 @@ static void worker_loop(opflow_server S) {
             cudaMemcpyAsync(S->state.data(), S->comp.dS, S->state.size() * sizeof(Scal), cudaMemcpyDeviceToHost, S->own_ctx.stream);
         if (!restarted.empty() || !finished.empty()) cudaStreamSynchronize(S->own_ctx.stream);
         for (auto& q : restarted) keep_state[q.first] = S->state[q.second];
+        if (!checkpointed.empty()) {
+            std::lock_guard<std::mutex> lk(S->mu);
+            for (Req* r : checkpointed) {
+                r->ckpt_state = 2;
+                r->ckpt_steps = r->steps_done;
+            }
+            S->cv_done.notify_all();
+        }
         for (auto& f : finished) {
             finish_mark(S, f.first, f.second);
             retired.push_back(f.first);
@@ -420,6 +443,7 @@ int opflow_server_submit(opflow_server S, const opflow_request* q, long long* id
     r->pd = pd;
     r->steps = q->steps;
     r->f = q->f;
+    r->x0 = q->x0;
     r->nf = n;
     r->x_out = q->x_out;
     r->t_submit = Clock::now();
@@ -454,6 +478,27 @@ int opflow_server_result(opflow_server S, long long id, int wait, int* done, opf
         out->queue_ms = std::chrono::duration<double, std::milli>(r->t_admit - r->t_submit).count();
         out->latency_ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
     }
+    return OPFLOW_OK;
+}
+
+int opflow_server_checkpoint(opflow_server S, long long id, double* x_out, size_t n, int* steps_done) {
+    if (!S || !x_out) return fail(OPFLOW_E_INVALID, "null argument");
+    std::unique_lock<std::mutex> lk(S->mu);
+    auto it = S->reqs.find(id);
+    if (it == S->reqs.end()) return fail(OPFLOW_E_INVALID, "unknown request %lld", id);
+    Req* r = it->second;
+    if (r->steps <= 1) return fail(OPFLOW_E_INVALID, "request %lld is a single solve, not a session", id);
+    if ((long long) n != r->nf) return fail(OPFLOW_E_INVALID, "request %lld has %lld unknowns, not %zu", id, r->nf, n);
+    if (r->done) return fail(OPFLOW_E_INVALID, "request %lld has finished", id);
+    if (r->ckpt_state != 0) return fail(OPFLOW_E_INVALID, "request %lld: a checkpoint is already pending", id);
+    r->ckpt_out = x_out;
+    r->ckpt_state = 1;
+    S->cv_done.wait(lk, [&] { return r->ckpt_state == 2 || r->done; });
+    const bool taken = r->ckpt_state == 2;
+    r->ckpt_state = 0;
+    r->ckpt_out = nullptr;
+    if (!taken) return fail(OPFLOW_E_INVALID, "request %lld finished before its next step boundary", id);
+    if (steps_done) *steps_done = r->ckpt_steps;
     return OPFLOW_OK;
 }
 

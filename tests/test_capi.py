@@ -17,7 +17,7 @@ def test_library_exports_every_declared_symbol():
     assert len(syms) >= 30
     missing = [s for s in syms if not hasattr(L, s)]
     assert not missing, missing
-    assert L.opflow_abi_version() == 2
+    assert L.opflow_abi_version() == 3
 
 
 @pytest.mark.parametrize("n,lo,hi,pad", [(1025, 0.0, 1.0, 5), (512, 0.0, 1.0, 5), (20, -1.0, 3.0, 3), (2049, 0.0, 1.0, 5)])

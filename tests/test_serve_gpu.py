@@ -4,6 +4,7 @@ problem; sessions equal their steps solved one after another."""
 import numpy as np
 import pytest
 
+import common as cm
 from opflow_gb300 import _capi as capi
 from opflow_gb300 import api
 
@@ -130,3 +131,65 @@ def test_close_serves_what_was_submitted(ctx):
     assert all(r["status"] == capi.OK for r in res_ref)
     for k in range(len(reqs)):
         assert np.array_equal(outs[k], outs_ref[k]), k
+
+
+def test_session_checkpoint_to_disk_and_restore(ctx, tmp_path):
+    """A heat session checkpointed at a step boundary, written to disk as a RawBinary field snapshot,
+    read back and resubmitted (f = x0 = the state, the remaining steps) ends bit for bit where the
+    uninterrupted session ends."""
+    n, steps = 257, 30
+    p = api.Problem([n, n], [1.0 / n] * 2, alpha=1.0, beta=1.0 / n, loc=api.LocOnMesh.Center, bc=api.BCType.Dirc)
+    f = np.random.default_rng(21).standard_normal(n * n)
+    params = api.StructSolverParams(tol=1e-10, maxIter=100, precision="mixed")
+    ref = api.Server(params, ctx=ctx)
+    whole = np.zeros(n * n)
+    rid = ref.submit(p, f, steps=steps, out=whole)
+    assert ref.result(rid)["status"] == capi.OK
+    ref.close()
+    s = api.Server(params, ctx=ctx)
+    out = np.zeros(n * n)
+    rid = s.submit(p, f, steps=steps, out=out)
+    state, k = s.checkpoint(rid, n * n)
+    assert 1 <= k < steps
+    assert s.result(rid)["status"] == capi.OK
+    s.close()
+    assert np.array_equal(out, whole)  # the checkpoint did not disturb the session
+    # to disk and back through a cell-centred field of the problem's shape
+    mesh = cm.mesh_uniform([n + 1, n + 1])
+    fd = cm.field_desc(2, capi.CENTER, [(capi.BC_DIRC, capi.BC_DIRC)] * 2, ext=1)
+    fld = api.CartesianField(mesh, fd, ctx, "session")
+    a = fld.download()
+    sl = fld.index_slices([tuple(fld.info.assignable[d]) for d in range(2)])
+    a[sl] = state.reshape(n, n)
+    fld.upload(a)
+    api.RawBinaryOStream(str(tmp_path / "ckpt")) << api.TimeStamp(float(k)) << fld
+    back = api.CartesianField(mesh, fd, ctx, "session")
+    ist = api.RawBinaryIStream(str(tmp_path / "ckpt"))
+    ist >> back
+    assert ist.time == float(k)
+    restored = back.download()[sl].reshape(-1).copy()
+    assert np.array_equal(restored, state)
+    s2 = api.Server(params, ctx=ctx)
+    out2 = np.zeros(n * n)
+    rid2 = s2.submit(p, restored, steps=steps - k, out=out2, x0=restored)
+    assert s2.result(rid2)["status"] == capi.OK
+    s2.close()
+    assert np.array_equal(out2, whole)
+
+
+def test_checkpoint_refusals(ctx):
+    params = api.StructSolverParams(tol=1e-10, precision="mixed")
+    s = api.Server(params, ctx=ctx)
+    p = api.Problem([64, 64], [1 / 64, 1 / 64], alpha=1.0, beta=1e-3)
+    rid = s.submit(p, np.ones(64 * 64))
+    with pytest.raises(capi.OpflowError) as e:
+        s.checkpoint(rid, 64 * 64)
+    assert e.value.code == capi.E_INVALID and "single solve" in str(e.value)
+    rid = s.submit(p, np.ones(64 * 64), steps=3)
+    with pytest.raises(capi.OpflowError):
+        s.checkpoint(rid, 10)
+    s.result(rid)
+    with pytest.raises(capi.OpflowError) as e:
+        s.checkpoint(rid, 64 * 64)
+    assert "finished" in str(e.value)
+    s.close()
