@@ -79,16 +79,17 @@ __device__ __forceinline__ void zq_push(ZQueue& Q, unsigned planes, int koff, in
     for (; planes; planes &= planes - 1) Q.cell[slot++] = (unsigned short) (((koff + __ffs(planes) - 1) << 8) | (warp << 5) | lane);
 }
 
-// after the march: every thread of the CTA takes queued cells; leaves the queue empty
+// after the march: every thread of the CTA takes queued cells; leaves the queue empty (x of lane 0 of a
+// queued cell: C.i0 + x0)
 template <typename F>
-__device__ __forceinline__ void zq_drain(ZQueue& Q, const Chunk& C, F&& fn) {
+__device__ __forceinline__ void zq_drain(ZQueue& Q, const Chunk& C, F&& fn, int x0 = -1) {
     __syncthreads();
     const unsigned n = Q.n;
     __syncthreads();
     if (threadIdx.x == 0) Q.n = 0;
     for (unsigned e = threadIdx.x; e < n; e += blockDim.x) {
         const unsigned v = Q.cell[e];
-        fn(C.i0 - 1 + (int) (v & 31), C.j + (int) ((v >> 5) & 7), C.k + (int) (v >> 8));
+        fn(C.i0 + x0 + (int) (v & 31), C.j + (int) ((v >> 5) & 7), C.k + (int) (v >> 8));
     }
     __syncthreads();
 }
@@ -337,6 +338,163 @@ __global__ void __launch_bounds__(32 * MG_ZT_Y) mg_prolong_z(const LvlDev* __res
             xf += ZB * sz;
         }
         zq_drain(Q, C, [&](int ci, int cj, int ck) { cell_prolong<T, FAST>(Ls, L, ci, cj, ck); });
+    }
+}
+
+// ---------------------------------------------------------------- TMA-staged z-marching smoother
+// Bulk asynchronous copies (cp.async.bulk, global -> shared, completing on an mbarrier) and bounded
+// mbarrier waits.  Every wait gives up after MBAR_SPINS polls; the kernel then records the failure in
+// g_mg_err, waits (bounded again) for the copies it issued and returns.
+__device__ int g_mg_err;
+constexpr int MBAR_SPINS = 1 << 24;
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned) __cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void mbar_arrive_expect(unsigned long long* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_test(unsigned long long* bar, unsigned parity) {
+    unsigned done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+    for (int it = 0; it < MBAR_SPINS; ++it)
+        if (mbar_test(bar, parity)) return true;
+    return false;
+}
+// global -> shared bulk copy of `bytes` (a multiple of 16; both addresses 16-byte aligned)
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(dst)), "l"(src),
+                 "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+
+// Red-black half sweep of a float32 class-table 3D level whose rows hold a multiple of 4 cells, the
+// planes staged in shared memory by bulk copies: a CTA owns 32 x-columns (one lane each, x origin a
+// multiple of 32) by MG_ZT_Y rows (one warp each) and a run of planes.  Warp 0 streams planes of x
+// (MG_ZT_Y + 2 rows of 40 cells from x origin - 4: the halo, 16-byte aligned) and of b (MG_ZT_Y rows of
+// 32) into a ring of ZT_RING slots, ZT_AHEAD planes ahead of the plane being updated; each slot's
+// mbarrier counts the bytes.  Rows and planes outside the level are not copied: only boundary cells,
+// which take the general path from global memory (queued), would read them.  Updates go straight to
+// global memory: a half sweep reads only the other colour, which it never writes.  Interior cells use
+// the interior class's coefficients in the other kernels' operation order (bit-identical).
+constexpr int ZT_RING = 8, ZT_AHEAD = 4, ZT_W = 40, ZT_H = MG_ZT_Y + 2;
+struct ZtStage {
+    float x[ZT_RING][ZT_H][ZT_W];
+    float b[ZT_RING][MG_ZT_Y][32];
+    unsigned long long bar[ZT_RING];
+};
+static_assert(ZT_AHEAD + 3 <= ZT_RING, "a slot is refilled only after its plane is no longer read");
+static_assert(ZT_H + MG_ZT_Y <= 32, "one lane of warp 0 per copied row");
+
+__global__ void __launch_bounds__(32 * MG_ZT_Y) mg_smooth_zt(const LvlDev* __restrict__ Ls, const Chunk* __restrict__ ch, int nch, int color,
+                                                            const Scal* sc) {
+    __shared__ __align__(128) ZtStage St;
+    __shared__ ZQueue Q;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < ZT_RING; ++s) mbar_init(&St.bar[s], 1);
+        Q.n = 0;
+        mbar_fence_init();
+    }
+    __syncthreads();
+    unsigned seq = 0;  // planes issued by this CTA so far: plane number q uses slot q % ZT_RING, phase (q / ZT_RING) & 1
+    for (int c = blockIdx.x; c < nch; c += gridDim.x) {
+        const Chunk C = ch[c];
+        if (!active(Ls, C, sc)) continue;
+        const LvlDev& L = Ls[C.lvl];
+        const int n0 = L.n[0], n1 = L.n[1], n2 = L.n[2];
+        const int i0 = C.i0, j0 = C.j, k0 = C.k, k1 = min(C.k + C.nrows, n2);
+        float* x = L.x32;
+        const float* b = L.b32;
+        const float* t = L.T32 + 13 * TSTRIDE;
+        const float c1 = t[1], c2 = t[2], c3 = t[3], c4 = t[4], c5 = t[5], c6 = t[6], cinv = t[NSLOT];
+        const unsigned base = seq;  // plane k0 - 1 is plane number base
+        const int last = k1;        // planes k0 - 1 .. k1 are read
+        auto slot_of = [&](int p) { return (int) ((base + (unsigned) (p - k0 + 1)) % ZT_RING); };
+        auto phase_of = [&](int p) { return ((base + (unsigned) (p - k0 + 1)) / ZT_RING) & 1u; };
+        // warp 0: plane p's rows into its slot (rows outside the level: no bytes)
+        auto issue = [&](int p) {
+            const int s = slot_of(p);
+            unsigned bytes = 0;
+            const float* src = nullptr;
+            float* dst = nullptr;
+            if (p >= 0 && p < n2) {
+                if (lane < ZT_H) {
+                    const int j = j0 - 1 + lane;
+                    if (j >= 0 && j < n1) {
+                        const int xs = max(i0 - 4, 0), xe = min(i0 + ZT_W - 4, n0);
+                        src = x + ((long long) p * n1 + j) * n0 + xs;
+                        dst = &St.x[s][lane][xs - (i0 - 4)];
+                        bytes = (unsigned) (xe - xs) * 4u;
+                    }
+                } else if (lane < ZT_H + MG_ZT_Y) {
+                    const int r = lane - ZT_H, j = j0 + r;
+                    if (j < n1) {
+                        const int xe = min(i0 + 32, n0);
+                        src = b + ((long long) p * n1 + j) * n0 + i0;
+                        dst = &St.b[s][r][0];
+                        bytes = (unsigned) (xe - i0) * 4u;
+                    }
+                }
+            }
+            const unsigned total = __reduce_add_sync(0xffffffffu, bytes);
+            if (lane == 0) mbar_arrive_expect(&St.bar[s], total);
+            __syncwarp();
+            if (bytes) bulk_load(dst, src, bytes, &St.bar[s]);
+        };
+        int issued = min(k0 - 1 + ZT_AHEAD, last);  // the last plane issued
+        if (warp == 0)
+            for (int p = k0 - 1; p <= issued; ++p) issue(p);
+        int waited = k0 - 2;  // the last plane waited for
+        bool ok = true, failed = false;
+        for (int k = k0; k < k1; ++k) {
+            for (int p = waited + 1; p <= k + 1; ++p) ok = ok && mbar_wait(&St.bar[slot_of(p)], phase_of(p));
+            waited = k + 1;
+            if (__syncthreads_or(!ok)) {  // (the same answer in every thread)
+                failed = true;
+                break;
+            }
+            const int i = i0 + lane, j = j0 + warp;
+            if (i < n0 && j < n1 && ((i + j + k + color) & 1) == 0) {
+                if (i > 0 && i < n0 - 1 && j > 0 && j < n1 - 1 && k > 0 && k < n2 - 1) {
+                    const float* xc = &St.x[slot_of(k)][warp + 1][lane + 4];
+                    float acc = 0;
+                    acc += c1 * xc[-1];
+                    acc += c2 * xc[1];
+                    acc += c3 * xc[-ZT_W];
+                    acc += c4 * xc[ZT_W];
+                    acc += c5 * St.x[slot_of(k - 1)][warp + 1][lane + 4];
+                    acc += c6 * St.x[slot_of(k + 1)][warp + 1][lane + 4];
+                    x[((long long) k * n1 + j) * n0 + i] = (St.b[slot_of(k)][warp][lane] - acc) * cinv;
+                } else {
+                    zq_push(Q, 1u, k - k0, warp, lane);
+                }
+            }
+            __syncthreads();  // plane k - 1's slot is free from here on
+            if (issued < last) {
+                ++issued;
+                if (warp == 0) issue(issued);
+            }
+        }
+        seq = base + (unsigned) (last - k0 + 2);
+        if (failed) {
+            // a copy never completed: record it, wait (bounded) for every copy this tile issued, stop
+            for (int p = k0 - 1; p <= issued; ++p) mbar_wait(&St.bar[slot_of(p)], phase_of(p));
+            if (threadIdx.x == 0) atomicExch(&g_mg_err, 1);
+            return;
+        }
+        zq_drain(Q, C, [&](int ci, int cj, int ck) { cell_gs<float>(L, ci, cj, ck); }, 0);
     }
 }
 
@@ -782,14 +940,20 @@ int mg_launch_smooth(cudaStream_t s, int sms, bool f32, const LvlDev* L, const C
     OPG_LAUNCHED();
     return check_launch("mg_smooth");
 }
-// planes per batch of the z-marching kernels: the system's (tuned) choice unless OPFLOW_MG_ZB = 2, 4 or 8
-static int z_batch(int zb) {
+// the z-marching variant: the system's (tuned) choice unless OPFLOW_MG_ZB = 2, 4, 8 (plane batch of the
+// register kernels) or 16 (the TMA-staged smoother where a level has its tiles)
+int mg_z_batch(int zb) {
     static const int forced = [] {
         const char* e = getenv("OPFLOW_MG_ZB");
         const int v = e ? atoi(e) : 0;
-        return v == 2 || v == 4 || v == 8 ? v : 0;
+        return v == 2 || v == 4 || v == 8 || v == MG_ZB_TMA ? v : 0;
     }();
-    return forced ? forced : (zb == 2 || zb == 8 ? zb : 4);
+    return forced ? forced : zb;
+}
+// the register kernels' plane batch
+static int z_batch(int zb) {
+    const int v = mg_z_batch(zb);
+    return v == 2 || v == 8 ? v : 4;
 }
 #define OPG_ZB_LAUNCH(KERNEL, T, ...)                                                                   \
     switch (z_batch(zb)) {                                                                             \
@@ -810,6 +974,19 @@ int mg_launch_residual_z(cudaStream_t s, int sms, bool f32, const LvlDev* L, con
     else { OPG_ZB_LAUNCH(mg_residual_z, double, L, ch, nch, sc) }
     OPG_LAUNCHED();
     return check_launch("mg_residual_z");
+}
+int mg_launch_smooth_zt(cudaStream_t s, int sms, const LvlDev* L, const Chunk* ch, int nch, int color, const Scal* sc) {
+    if (nch <= 0) return OPFLOW_OK;
+    mg_smooth_zt<<<grid_of(nch, sms), 32 * MG_ZT_Y, 0, s>>>(L, ch, nch, color, sc);
+    OPG_LAUNCHED();
+    return check_launch("mg_smooth_zt");
+}
+int mg_take_error(cudaStream_t s, int* err) {
+    int zero = 0;
+    OPG_CUDA(cudaMemcpyFromSymbolAsync(err, g_mg_err, sizeof(int), 0, cudaMemcpyDeviceToHost, s));
+    OPG_CUDA(cudaStreamSynchronize(s));
+    if (*err) OPG_CUDA(cudaMemcpyToSymbolAsync(g_mg_err, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, s));
+    return OPFLOW_OK;
 }
 int mg_launch_prolong_z(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* ch, int nch, const Scal* sc, int zb) {
     if (nch <= 0) return OPFLOW_OK;

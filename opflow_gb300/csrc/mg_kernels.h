@@ -14,6 +14,14 @@ constexpr long long MG_ZT_MIN = 32768;
 int mg_launch_smooth_z(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* ch, int nch, int color, const Scal* sc, int zb);
 // r = b - A x over the same tiles
 int mg_launch_residual_z(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* ch, int nch, const Scal* sc, int zb);
+// the TMA-staged float32 smoother over its own tiles (Chunk{lvl, j, k, i0 = a multiple of 32, 32, planes})
+int mg_launch_smooth_zt(cudaStream_t s, int sms, const LvlDev* L, const Chunk* ch, int nch, int color, const Scal* sc);
+// reads (and clears) the kernels' failure flag: 1 after a bounded wait of mg_smooth_zt gave up
+int mg_take_error(cudaStream_t s, int* err);
+// plane-batch value that selects mg_smooth_zt in the tuner and OPFLOW_MG_ZB
+constexpr int MG_ZB_TMA = 16;
+// a level's z-marching choice after the OPFLOW_MG_ZB override
+int mg_z_batch(int zb);
 // x += P x_coarse over the same tiles (the tiles' first planes are even)
 int mg_launch_prolong_z(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* ch, int nch, const Scal* sc, int zb);
 int mg_launch_restrict(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* ch, int nch, const Scal* sc);

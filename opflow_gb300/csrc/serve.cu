@@ -310,6 +310,14 @@ static void worker_loop(opflow_server S) {
         }
         cudaMemcpyAsync(S->state.data(), S->comp.dS, S->state.size() * sizeof(Scal), cudaMemcpyDeviceToHost, S->own_ctx.stream);
         cudaStreamSynchronize(S->own_ctx.stream);
+        if (mg_check_error(&S->comp) != OPFLOW_OK) {
+            { std::lock_guard<std::mutex> lk(S->mu); S->error = opflow_last_error(); }
+            for (Req* r : S->active) { release_req(r); finish_req(S, r, OPFLOW_E_CUDA); }
+            S->active.clear();
+            S->state.clear();
+            S->dirty = true;
+            continue;
+        }
         add_since(S->iterate_s, t_iter);
         const Clock::time_point t_retire = Clock::now();
         // Every restart and every result of this boundary is enqueued first; one synchronisation

@@ -21,6 +21,7 @@
 #include "solver.h"
 #include "tune.h"
 
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 
@@ -505,6 +506,9 @@ int mg_add_problem(MGSystem* S, opflow_field target, const opflow_node* nodes, i
 }
 
 // Vectors, device descriptors and chunk lists for every problem added.
+static int smooth_z_level(MGSystem* S, int l, int color, const Scal* sc, int zb);
+int mg_check_error(MGSystem* S);
+
 // Device time (ms) of `launch`, run once to warm up and once timed on the system's stream; negative
 // when a launch fails.
 static float time_launch(MGSystem* S, const std::function<int()>& launch) {
@@ -561,10 +565,12 @@ static int tune_levels(MGSystem* S) {
     for (int l = 0; l < S->nlevels; ++l) {
         const ChunkList& Z = S->d_zsm[l];
         if (Z.n > 0) {
-            S->zb[l] = choose(level_key("mg_smooth_z", S, l), {4, 2, 8}, [&](int zb) {
+            std::vector<int> cands = {4, 2, 8};
+            if (S->d_zt[l].n > 0) cands.push_back(MG_ZB_TMA);
+            S->zb[l] = choose(level_key("mg_smooth_z", S, l), cands, [&](int zb) {
                 return time_launch(S, [&] {
-                    OPG_TRY(mg_launch_smooth_z(ctx->stream, sms, f32, S->dL, Z.ptr, Z.n, 0, nullptr, zb));
-                    return mg_launch_smooth_z(ctx->stream, sms, f32, S->dL, Z.ptr, Z.n, 1, nullptr, zb);
+                    OPG_TRY(smooth_z_level(S, l, 0, nullptr, zb));
+                    return smooth_z_level(S, l, 1, nullptr, zb);
                 });
             });
         }
@@ -615,6 +621,7 @@ int mg_finalize(MGSystem* S) {
     S->zsm_ch.assign(S->nlevels, {});
     S->zb.assign(S->nlevels, 4);
     S->tile_alt.assign(S->nlevels, {});
+    S->zt_ch.assign(S->nlevels, {});
     S->coarse_sm_ch.clear();
     S->bottom_host.clear();
     S->bottom_cells_host.clear();
@@ -777,6 +784,15 @@ int mg_finalize(MGSystem* S) {
                                 c.nrows = std::min(zz, D.n[2] - k0);
                                 S->zsm_ch[l].push_back(c);
                             }
+                    // the TMA-staged smoother's tiles: 16-byte aligned rows (float32, a multiple of 4 cells)
+                    if (f32 && D.n[0] % 4 == 0 && (reinterpret_cast<uintptr_t>(D.x32) & 15) == 0 && (reinterpret_cast<uintptr_t>(D.b32) & 15) == 0)
+                        for (int k0 = 0; k0 < D.n[2]; k0 += zz)
+                            for (int j0 = 0; j0 < D.n[1]; j0 += MG_ZT_Y)
+                                for (int i0 = 0; i0 < D.n[0]; i0 += 32) {
+                                    Chunk c{li, j0, k0, i0, 32};
+                                    c.nrows = std::min(zz, D.n[2] - k0);
+                                    S->zt_ch[l].push_back(c);
+                                }
                 } else if (!D.coarsest) {
                     rows(li, D, S->smooth_ch[l]);  // (also the rows of the residual before restriction)
                 }
@@ -848,12 +864,14 @@ int mg_finalize(MGSystem* S) {
     S->d_prolong.assign(S->nlevels, {});
     S->d_tiles.assign(S->nlevels, {});
     S->d_zsm.assign(S->nlevels, {});
+    S->d_zt.assign(S->nlevels, {});
     for (int l = 0; l < S->nlevels; ++l) {
         upload(S->smooth_ch[l], S->d_smooth[l]);
         upload(S->restrict_ch[l], S->d_restrict[l]);
         upload(S->prolong_ch[l], S->d_prolong[l]);
         upload(S->tile_ch[l], S->d_tiles[l]);
         upload(S->zsm_ch[l], S->d_zsm[l]);
+        upload(S->zt_ch[l], S->d_zt[l]);
     }
     upload(S->coarse_sm_ch, S->d_coarse_sm);
     S->kd_host = kd;
@@ -872,6 +890,16 @@ int mg_finalize(MGSystem* S) {
 static cudaStream_t work_stream(const MGSystem* S) { return S->recording ? S->rec_stream : S->ctx->stream; }
 
 // (The level-0 input b = r, x = 0 is written by the Krylov kernel that forms r.)
+// one half sweep of level l's z-marching tiles: the TMA-staged smoother where chosen and available,
+// else the register kernel with the level's plane batch
+static int smooth_z_level(MGSystem* S, int l, int color, const Scal* sc, int zb) {
+    cudaStream_t s = work_stream(S);
+    const int sms = S->ctx->num_sms;
+    if (mg_z_batch(zb) == MG_ZB_TMA && S->d_zt[l].n > 0) return mg_launch_smooth_zt(s, sms, S->dL, S->d_zt[l].ptr, S->d_zt[l].n, color, sc);
+    return mg_launch_smooth_z(s, sms, S->precision == OPFLOW_PREC_MIXED, S->dL, S->d_zsm[l].ptr, S->d_zsm[l].n, color, sc, zb);
+}
+static int smooth_z_level(MGSystem* S, int l, int color) { return smooth_z_level(S, l, color, S->dS, S->zb[l]); }
+
 static int vcycle(MGSystem* S) {
     cudaStream_t s = work_stream(S);
     const int sms = S->ctx->num_sms;
@@ -884,9 +912,9 @@ static int vcycle(MGSystem* S) {
         const ChunkList& Z = S->d_zsm[l];
         for (int it = 0; it < S->pre; ++it) {
             OPG_TRY(mg_launch_smooth(s, sms, f32, S->dL, C.ptr, C.n, 0, sc));
-            OPG_TRY(mg_launch_smooth_z(s, sms, f32, S->dL, Z.ptr, Z.n, 0, sc, S->zb[l]));
+            OPG_TRY(smooth_z_level(S, l, 0));
             OPG_TRY(mg_launch_smooth(s, sms, f32, S->dL, C.ptr, C.n, 1, sc));
-            OPG_TRY(mg_launch_smooth_z(s, sms, f32, S->dL, Z.ptr, Z.n, 1, sc, S->zb[l]));
+            OPG_TRY(smooth_z_level(S, l, 1));
         }
         OPG_TRY(mg_launch_residual(s, sms, f32, S->dL, C.ptr, C.n, sc));
         OPG_TRY(mg_launch_residual_z(s, sms, f32, S->dL, Z.ptr, Z.n, sc, S->zb[l]));
@@ -905,9 +933,9 @@ static int vcycle(MGSystem* S) {
         OPG_TRY(mg_launch_prolong_z(s, sms, f32, S->dL, Z.ptr, Z.n, sc, S->zb[l]));
         for (int it = 0; it < S->post; ++it) {
             OPG_TRY(mg_launch_smooth(s, sms, f32, S->dL, C.ptr, C.n, 1, sc));
-            OPG_TRY(mg_launch_smooth_z(s, sms, f32, S->dL, Z.ptr, Z.n, 1, sc, S->zb[l]));
+            OPG_TRY(smooth_z_level(S, l, 1));
             OPG_TRY(mg_launch_smooth(s, sms, f32, S->dL, C.ptr, C.n, 0, sc));
-            OPG_TRY(mg_launch_smooth_z(s, sms, f32, S->dL, Z.ptr, Z.n, 0, sc, S->zb[l]));
+            OPG_TRY(smooth_z_level(S, l, 0));
         }
     }
     return OPFLOW_OK;
@@ -1160,6 +1188,7 @@ int mg_compose(MGSystem* C, const std::vector<MGSystem*>& parts, const std::vect
     C->zsm_ch.assign(C->nlevels, {});
     C->zb.assign(C->nlevels, 4);
     C->tile_alt.assign(C->nlevels, {});
+    C->zt_ch.assign(C->nlevels, {});
     std::vector<size_t> zb_tiles(C->nlevels, 0);  // each level takes the batch of the part with most tiles there
     C->coarse_sm_ch.clear();
     for (size_t q = 0; q < parts.size(); ++q) {
@@ -1187,6 +1216,7 @@ int mg_compose(MGSystem* C, const std::vector<MGSystem*>& parts, const std::vect
             shift(P->prolong_ch[l], C->prolong_ch[l]);
             shift(P->tile_ch[l], C->tile_ch[l]);
             shift(P->zsm_ch[l], C->zsm_ch[l]);
+            shift(P->zt_ch[l], C->zt_ch[l]);
             if (P->zsm_ch[l].size() > zb_tiles[l]) {
                 zb_tiles[l] = P->zsm_ch[l].size();
                 C->zb[l] = P->zb[l];
@@ -1244,12 +1274,14 @@ int mg_compose(MGSystem* C, const std::vector<MGSystem*>& parts, const std::vect
     C->d_prolong.assign(C->nlevels, {});
     C->d_tiles.assign(C->nlevels, {});
     C->d_zsm.assign(C->nlevels, {});
+    C->d_zt.assign(C->nlevels, {});
     for (int l = 0; l < C->nlevels; ++l) {
         upload(C->smooth_ch[l], C->d_smooth[l]);
         upload(C->restrict_ch[l], C->d_restrict[l]);
         upload(C->prolong_ch[l], C->d_prolong[l]);
         upload(C->tile_ch[l], C->d_tiles[l]);
         upload(C->zsm_ch[l], C->d_zsm[l]);
+        upload(C->zt_ch[l], C->d_zt[l]);
     }
     upload(C->coarse_sm_ch, C->d_coarse_sm);
     C->kd_host = kd;
@@ -1271,6 +1303,17 @@ int mg_states(MGSystem* S, std::vector<Scal>& out) {
         g_launches.fetch_add((uint64_t) ((long long) ac[1] * S->body_kernels));
         S->solve_pending = false;
     }
+    return mg_check_error(S);
+}
+
+// the TMA-staged smoother's failure flag (a bounded wait that gave up), for systems that use it
+int mg_check_error(MGSystem* S) {
+    bool uses = false;
+    for (const ChunkList& z : S->d_zt) uses = uses || z.n > 0;
+    if (!uses) return OPFLOW_OK;
+    int err = 0;
+    OPG_TRY(mg_take_error(S->ctx->stream, &err));
+    if (err) return fail(OPFLOW_E_CUDA, "the staged 3D smoother gave up waiting for an asynchronous copy; results are invalid");
     return OPFLOW_OK;
 }
 

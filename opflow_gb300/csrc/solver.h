@@ -72,7 +72,10 @@ struct MGSystem {
     // tiles of the 3D levels smoothed by the z-marching kernel (such levels are not in smooth_ch)
     std::vector<std::vector<Chunk>> zsm_ch;
     std::vector<ChunkList> d_zsm;
-    std::vector<int> zb;  // planes per load batch of the z-marching kernels, per level (tuned)
+    std::vector<int> zb;  // planes per load batch of the z-marching kernels, per level (tuned; MG_ZB_TMA: mg_smooth_zt)
+    // tiles of the TMA-staged smoother (float32 levels whose rows hold a multiple of 4 cells)
+    std::vector<std::vector<Chunk>> zt_ch;
+    std::vector<ChunkList> d_zt;
     bool tune_measure = true;  // false: cached tuner choices only, nothing timed (the request server)
     // the other 2D tile shape of a tiled level, when the tuner is to time it against tile_ch
     std::vector<std::vector<Chunk>> tile_alt;
@@ -167,6 +170,8 @@ int mg_add_problem(MGSystem* S, opflow_field target, const opflow_node* nodes, i
 int mg_finalize(MGSystem* S);
 int mg_solve(MGSystem* S);
 int mg_states(MGSystem* S, std::vector<Scal>& out);
+// OPFLOW_E_CUDA when a bounded wait of the staged 3D smoother gave up since the last check
+int mg_check_error(MGSystem* S);
 void mg_destroy(MGSystem* S);
 
 }  // namespace opg

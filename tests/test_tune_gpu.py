@@ -49,7 +49,8 @@ def _same(a, b):
 
 def test_solver_choices_are_cached_and_change_no_bit(ctx, fresh, monkeypatch, tmp_path):
     cache = tmp_path / "tune.txt"
-    solves = [_poisson(ctx, [130, 100, 96]), _poisson(ctx, [600, 450])]  # (3D: enough planes for z tiles)
+    # (3D: enough planes for z tiles, rows of a multiple of 4 cells for the staged smoother)
+    solves = [_poisson(ctx, [128, 100, 96]), _poisson(ctx, [600, 450])]
     monkeypatch.setenv("OPFLOW_TUNE", "0")
     plain = [s() for s in solves]
     monkeypatch.delenv("OPFLOW_TUNE")
@@ -62,7 +63,7 @@ def test_solver_choices_are_cached_and_change_no_bit(ctx, fresh, monkeypatch, tm
     zkeys = [k for k in keys if k.startswith("mg_smooth_z/f32/")]
     tkeys = [k for k in keys if k.startswith("mg_tile/f32/")]
     assert zkeys and tkeys, keys
-    assert all(keys[k] in (2, 4, 8) for k in zkeys) and all(keys[k] in (0, 1) for k in tkeys)
+    assert all(keys[k] in (2, 4, 8, 16) for k in zkeys) and all(keys[k] in (0, 1) for k in tkeys)
     n_tuned, hits, entries = api.tune_stats()
     assert n_tuned == len(keys) == entries
     # the same shapes again: cache hits only
@@ -70,9 +71,9 @@ def test_solver_choices_are_cached_and_change_no_bit(ctx, fresh, monkeypatch, tm
         s()
     assert api.tune_stats()[0] == n_tuned and api.tune_stats()[1] > hits
     # every other choice, forced through a cache file: the same bits
-    for alt in range(2):
+    for alt in range(3):  # plane batches 2 and 8, then the staged smoother (16)
         forced = tmp_path / ("forced%d.txt" % alt)
-        forced.write_text("".join("%s %d 0\n" % (k, [2, 8][alt] if k in zkeys else 1 - keys[k]) for k in keys))
+        forced.write_text("".join("%s %d 0\n" % (k, [2, 8, 16][alt] if k in zkeys else (1 - keys[k] if alt < 2 else keys[k])) for k in keys))
         api.tune_clear()
         api.tune_set_cache(forced)
         for a, s in zip(plain, solves):
