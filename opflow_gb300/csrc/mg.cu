@@ -8,6 +8,9 @@
 // the Krylov vectors, their updates and all inner products are float64.
 #include "mg_device.h"
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <cstdlib>
 #include <type_traits>
 
@@ -342,8 +345,7 @@ __global__ void __launch_bounds__(32 * MG_ZT_Y) mg_prolong_z(const LvlDev* __res
 }
 
 // ---------------------------------------------------------------- TMA-staged z-marching smoother
-// Bulk asynchronous copies (cp.async.bulk, global -> shared, completing on an mbarrier) and bounded
-// mbarrier waits.  Every wait gives up after MBAR_SPINS polls; the kernel then records the failure in
+// TMA copies (global -> shared, completing on an mbarrier) and bounded mbarrier waits.  Every wait gives up after MBAR_SPINS polls; the kernel then records the failure in
 // g_mg_err, waits (bounded again) for the copies it issued and returns.
 __device__ int g_mg_err;
 constexpr int MBAR_SPINS = 1 << 24;
@@ -372,33 +374,40 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned pari
         if (mbar_test(bar, parity)) return true;
     return false;
 }
-// global -> shared bulk copy of `bytes` (a multiple of 16; both addresses 16-byte aligned)
-__device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(dst)), "l"(src),
-                 "r"(bytes), "r"(smem_addr(bar))
+
+// 3D tiled copy of a tensor map's box at (x, y, z) into shared memory, completing on `bar`
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z, unsigned long long* bar) {
+    asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_addr(dst)),
+                 "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_addr(bar))
                  : "memory");
+}
+__device__ __forceinline__ void tensormap_acquire(const CUtensorMap* map) {
+    asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(map) : "memory");
 }
 
 // Red-black half sweep of a float32 class-table 3D level whose rows hold a multiple of 4 cells, the
-// planes staged in shared memory by bulk copies: a CTA owns 32 x-columns (one lane each, x origin a
-// multiple of 32) by MG_ZT_Y rows (one warp each) and a run of planes.  Warp 0 streams planes of x
-// (MG_ZT_Y + 2 rows of 40 cells from x origin - 4: the halo, 16-byte aligned) and of b (MG_ZT_Y rows of
-// 32) into a ring of ZT_RING slots, ZT_AHEAD planes ahead of the plane being updated; each slot's
-// mbarrier counts the bytes.  Rows and planes outside the level are not copied: only boundary cells,
-// which take the general path from global memory (queued), would read them.  Updates go straight to
-// global memory: a half sweep reads only the other colour, which it never writes.  Interior cells use
-// the interior class's coefficients in the other kernels' operation order (bit-identical).
+// planes staged in shared memory by TMA: a CTA owns 32 x-columns (one lane each, x origin a multiple
+// of 32) by MG_ZT_Y rows (one warp each) and a run of planes.  One thread streams each plane as two
+// tensor-map boxes - x: 40 x (MG_ZT_Y + 2) cells from (x origin - 4, y origin - 1), the halo, its x
+// coordinate on a 16-byte boundary; b: 32 x MG_ZT_Y - into a ring of ZT_RING slots, ZT_AHEAD planes
+// ahead of the plane being updated; each slot's mbarrier counts the bytes.  Cells outside the level
+// arrive as zeros: only boundary cells, which take the general path from global memory (queued), would
+// read them.  Updates go straight to global memory: a half sweep reads only the other colour, which it
+// never writes.  Interior cells use the interior class's coefficients in the other kernels' operation
+// order (bit-identical).  maps[2 * level] and maps[2 * level + 1] are the level's x and b maps.
 constexpr int ZT_RING = 8, ZT_AHEAD = 4, ZT_W = 40, ZT_H = MG_ZT_Y + 2;
+constexpr int ZT_XSLOT = ((ZT_W * ZT_H * 4 + 127) / 128) * 32;  // floats per x slot (128-byte multiple)
+constexpr unsigned ZT_BYTES = (ZT_W * ZT_H + 32 * MG_ZT_Y) * 4;   // bytes per plane (both boxes)
 struct ZtStage {
-    float x[ZT_RING][ZT_H][ZT_W];
-    float b[ZT_RING][MG_ZT_Y][32];
+    float x[ZT_RING][ZT_XSLOT];
+    float b[ZT_RING][MG_ZT_Y * 32];
     unsigned long long bar[ZT_RING];
 };
 static_assert(ZT_AHEAD + 3 <= ZT_RING, "a slot is refilled only after its plane is no longer read");
-static_assert(ZT_H + MG_ZT_Y <= 32, "one lane of warp 0 per copied row");
+static_assert((MG_ZT_Y * 32 * 4) % 128 == 0, "b slots on 128-byte boundaries");
 
 __global__ void __launch_bounds__(32 * MG_ZT_Y) mg_smooth_zt(const LvlDev* __restrict__ Ls, const Chunk* __restrict__ ch, int nch, int color,
-                                                            const Scal* sc) {
+                                                            const Scal* sc, const CUtensorMap* __restrict__ maps) {
     __shared__ __align__(128) ZtStage St;
     __shared__ ZQueue Q;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -416,46 +425,27 @@ __global__ void __launch_bounds__(32 * MG_ZT_Y) mg_smooth_zt(const LvlDev* __res
         const int n0 = L.n[0], n1 = L.n[1], n2 = L.n[2];
         const int i0 = C.i0, j0 = C.j, k0 = C.k, k1 = min(C.k + C.nrows, n2);
         float* x = L.x32;
-        const float* b = L.b32;
         const float* t = L.T32 + 13 * TSTRIDE;
         const float c1 = t[1], c2 = t[2], c3 = t[3], c4 = t[4], c5 = t[5], c6 = t[6], cinv = t[NSLOT];
+        const CUtensorMap* mx = maps + 2 * C.lvl;
+        const CUtensorMap* mb = mx + 1;
         const unsigned base = seq;  // plane k0 - 1 is plane number base
         const int last = k1;        // planes k0 - 1 .. k1 are read
         auto slot_of = [&](int p) { return (int) ((base + (unsigned) (p - k0 + 1)) % ZT_RING); };
         auto phase_of = [&](int p) { return ((base + (unsigned) (p - k0 + 1)) / ZT_RING) & 1u; };
-        // warp 0: plane p's rows into its slot (rows outside the level: no bytes)
-        auto issue = [&](int p) {
+        const bool producer = threadIdx.x == 0;
+        auto issue = [&](int p) {  // the producer thread: plane p's two boxes into its slot
             const int s = slot_of(p);
-            unsigned bytes = 0;
-            const float* src = nullptr;
-            float* dst = nullptr;
-            if (p >= 0 && p < n2) {
-                if (lane < ZT_H) {
-                    const int j = j0 - 1 + lane;
-                    if (j >= 0 && j < n1) {
-                        const int xs = max(i0 - 4, 0), xe = min(i0 + ZT_W - 4, n0);
-                        src = x + ((long long) p * n1 + j) * n0 + xs;
-                        dst = &St.x[s][lane][xs - (i0 - 4)];
-                        bytes = (unsigned) (xe - xs) * 4u;
-                    }
-                } else if (lane < ZT_H + MG_ZT_Y) {
-                    const int r = lane - ZT_H, j = j0 + r;
-                    if (j < n1) {
-                        const int xe = min(i0 + 32, n0);
-                        src = b + ((long long) p * n1 + j) * n0 + i0;
-                        dst = &St.b[s][r][0];
-                        bytes = (unsigned) (xe - i0) * 4u;
-                    }
-                }
-            }
-            const unsigned total = __reduce_add_sync(0xffffffffu, bytes);
-            if (lane == 0) mbar_arrive_expect(&St.bar[s], total);
-            __syncwarp();
-            if (bytes) bulk_load(dst, src, bytes, &St.bar[s]);
+            mbar_arrive_expect(&St.bar[s], ZT_BYTES);
+            tma_load_3d(&St.x[s][0], mx, i0 - 4, j0 - 1, p, &St.bar[s]);
+            tma_load_3d(&St.b[s][0], mb, i0, j0, p, &St.bar[s]);
         };
         int issued = min(k0 - 1 + ZT_AHEAD, last);  // the last plane issued
-        if (warp == 0)
+        if (producer) {
+            tensormap_acquire(mx);
+            tensormap_acquire(mb);
             for (int p = k0 - 1; p <= issued; ++p) issue(p);
+        }
         int waited = k0 - 2;  // the last plane waited for
         bool ok = true, failed = false;
         for (int k = k0; k < k1; ++k) {
@@ -468,15 +458,16 @@ __global__ void __launch_bounds__(32 * MG_ZT_Y) mg_smooth_zt(const LvlDev* __res
             const int i = i0 + lane, j = j0 + warp;
             if (i < n0 && j < n1 && ((i + j + k + color) & 1) == 0) {
                 if (i > 0 && i < n0 - 1 && j > 0 && j < n1 - 1 && k > 0 && k < n2 - 1) {
-                    const float* xc = &St.x[slot_of(k)][warp + 1][lane + 4];
+                    const int at = (warp + 1) * ZT_W + lane + 4;
+                    const float* xc = &St.x[slot_of(k)][at];
                     float acc = 0;
                     acc += c1 * xc[-1];
                     acc += c2 * xc[1];
                     acc += c3 * xc[-ZT_W];
                     acc += c4 * xc[ZT_W];
-                    acc += c5 * St.x[slot_of(k - 1)][warp + 1][lane + 4];
-                    acc += c6 * St.x[slot_of(k + 1)][warp + 1][lane + 4];
-                    x[((long long) k * n1 + j) * n0 + i] = (St.b[slot_of(k)][warp][lane] - acc) * cinv;
+                    acc += c5 * St.x[slot_of(k - 1)][at];
+                    acc += c6 * St.x[slot_of(k + 1)][at];
+                    x[((long long) k * n1 + j) * n0 + i] = (St.b[slot_of(k)][warp * 32 + lane] - acc) * cinv;
                 } else {
                     zq_push(Q, 1u, k - k0, warp, lane);
                 }
@@ -484,7 +475,7 @@ __global__ void __launch_bounds__(32 * MG_ZT_Y) mg_smooth_zt(const LvlDev* __res
             __syncthreads();  // plane k - 1's slot is free from here on
             if (issued < last) {
                 ++issued;
-                if (warp == 0) issue(issued);
+                if (producer) issue(issued);
             }
         }
         seq = base + (unsigned) (last - k0 + 2);
@@ -975,11 +966,34 @@ int mg_launch_residual_z(cudaStream_t s, int sms, bool f32, const LvlDev* L, con
     OPG_LAUNCHED();
     return check_launch("mg_residual_z");
 }
-int mg_launch_smooth_zt(cudaStream_t s, int sms, const LvlDev* L, const Chunk* ch, int nch, int color, const Scal* sc) {
+int mg_launch_smooth_zt(cudaStream_t s, int sms, const LvlDev* L, const Chunk* ch, int nch, int color, const Scal* sc, const CUtensorMap* maps) {
     if (nch <= 0) return OPFLOW_OK;
-    mg_smooth_zt<<<grid_of(nch, sms), 32 * MG_ZT_Y, 0, s>>>(L, ch, nch, color, sc);
+    mg_smooth_zt<<<grid_of(nch, sms), 32 * MG_ZT_Y, 0, s>>>(L, ch, nch, color, sc, maps);
     OPG_LAUNCHED();
     return check_launch("mg_smooth_zt");
+}
+int mg_encode_zt_maps(const LvlDev& D, CUtensorMap* two) {
+    static const PFN_cuTensorMapEncodeTiled_v12000 enc = [] {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            fn = nullptr;
+        }
+        return (PFN_cuTensorMapEncodeTiled_v12000) fn;
+    }();
+    if (!enc) return fail(OPFLOW_E_UNSUPPORTED, "cuTensorMapEncodeTiled is not available");
+    const cuuint64_t dims[3] = {(cuuint64_t) D.n[0], (cuuint64_t) D.n[1], (cuuint64_t) D.n[2]};
+    const cuuint64_t strides[2] = {(cuuint64_t) D.n[0] * 4, (cuuint64_t) D.n[0] * D.n[1] * 4};
+    const cuuint32_t box_x[3] = {ZT_W, ZT_H, 1}, box_b[3] = {32, MG_ZT_Y, 1}, ones[3] = {1, 1, 1};
+    for (int q = 0; q < 2; ++q) {
+        const CUresult r = enc(&two[q], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, q == 0 ? (void*) D.x32 : (void*) D.b32, dims, strides,
+                               q == 0 ? box_x : box_b, ones, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                               CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) return fail(OPFLOW_E_UNSUPPORTED, "tensor map of a %dx%dx%d level: error %d", D.n[0], D.n[1], D.n[2], (int) r);
+    }
+    return OPFLOW_OK;
 }
 int mg_take_error(cudaStream_t s, int* err) {
     int zero = 0;

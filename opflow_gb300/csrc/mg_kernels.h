@@ -1,5 +1,7 @@
 // Launchers of the multigrid / Krylov kernels (mg.cu).
 #pragma once
+
+#include <cuda.h>
 #include "mg.h"
 
 namespace opg {
@@ -14,8 +16,11 @@ constexpr long long MG_ZT_MIN = 32768;
 int mg_launch_smooth_z(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* ch, int nch, int color, const Scal* sc, int zb);
 // r = b - A x over the same tiles
 int mg_launch_residual_z(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* ch, int nch, const Scal* sc, int zb);
-// the TMA-staged float32 smoother over its own tiles (Chunk{lvl, j, k, i0 = a multiple of 32, 32, planes})
-int mg_launch_smooth_zt(cudaStream_t s, int sms, const LvlDev* L, const Chunk* ch, int nch, int color, const Scal* sc);
+// the TMA-staged float32 smoother over its own tiles (Chunk{lvl, j, k, i0 = a multiple of 32, 32, planes});
+// maps: device array, the x and b tensor maps of level index l at [2 l] and [2 l + 1]
+int mg_launch_smooth_zt(cudaStream_t s, int sms, const LvlDev* L, const Chunk* ch, int nch, int color, const Scal* sc, const CUtensorMap* maps);
+// encodes the x and b tensor maps of a float32 level for mg_smooth_zt (boxes 40 x (MG_ZT_Y + 2) and 32 x MG_ZT_Y)
+int mg_encode_zt_maps(const LvlDev& D, CUtensorMap* two);
 // reads (and clears) the kernels' failure flag: 1 after a bounded wait of mg_smooth_zt gave up
 int mg_take_error(cudaStream_t s, int* err);
 // plane-batch value that selects mg_smooth_zt in the tuner and OPFLOW_MG_ZB

@@ -27,7 +27,9 @@
 
 #include <chrono>
 #include <cmath>
+#include <array>
 #include <functional>
+#include <map>
 #include <string>
 
 namespace opg {
@@ -622,6 +624,7 @@ int mg_finalize(MGSystem* S) {
     S->zb.assign(S->nlevels, 4);
     S->tile_alt.assign(S->nlevels, {});
     S->zt_ch.assign(S->nlevels, {});
+    std::map<int, std::array<CUtensorMap, 2>> zt_maps;  // by level index
     S->coarse_sm_ch.clear();
     S->bottom_host.clear();
     S->bottom_cells_host.clear();
@@ -785,7 +788,10 @@ int mg_finalize(MGSystem* S) {
                                 S->zsm_ch[l].push_back(c);
                             }
                     // the TMA-staged smoother's tiles: 16-byte aligned rows (float32, a multiple of 4 cells)
-                    if (f32 && D.n[0] % 4 == 0 && (reinterpret_cast<uintptr_t>(D.x32) & 15) == 0 && (reinterpret_cast<uintptr_t>(D.b32) & 15) == 0)
+                    CUtensorMap two[2];
+                    if (f32 && D.n[0] % 4 == 0 && (reinterpret_cast<uintptr_t>(D.x32) & 15) == 0 && (reinterpret_cast<uintptr_t>(D.b32) & 15) == 0 &&
+                        mg_encode_zt_maps(D, two) == OPFLOW_OK) {
+                        zt_maps[li] = {two[0], two[1]};
                         for (int k0 = 0; k0 < D.n[2]; k0 += zz)
                             for (int j0 = 0; j0 < D.n[1]; j0 += MG_ZT_Y)
                                 for (int i0 = 0; i0 < D.n[0]; i0 += 32) {
@@ -793,6 +799,7 @@ int mg_finalize(MGSystem* S) {
                                     c.nrows = std::min(zz, D.n[2] - k0);
                                     S->zt_ch[l].push_back(c);
                                 }
+                    }
                 } else if (!D.coarsest) {
                     rows(li, D, S->smooth_ch[l]);  // (also the rows of the residual before restriction)
                 }
@@ -874,6 +881,17 @@ int mg_finalize(MGSystem* S) {
         upload(S->zt_ch[l], S->d_zt[l]);
     }
     upload(S->coarse_sm_ch, S->d_coarse_sm);
+    S->zt_maps.assign(2 * lv.size(), CUtensorMap{});
+    for (auto& m : zt_maps) {
+        S->zt_maps[2 * m.first] = m.second[0];
+        S->zt_maps[2 * m.first + 1] = m.second[1];
+    }
+    S->d_zt_maps = nullptr;
+    if (!zt_maps.empty()) {
+        S->d_zt_maps = (CUtensorMap*) S->arena.alloc(S->zt_maps.size() * sizeof(CUtensorMap));
+        if (!S->d_zt_maps) return fail(OPFLOW_E_NOMEM, "tensor maps");
+        OPG_CUDA(cudaMemcpyAsync(S->d_zt_maps, S->zt_maps.data(), S->zt_maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice, ctx->stream));
+    }
     S->kd_host = kd;
     S->lv_host = lv;
     S->k0_host = k0;
@@ -895,7 +913,8 @@ static cudaStream_t work_stream(const MGSystem* S) { return S->recording ? S->re
 static int smooth_z_level(MGSystem* S, int l, int color, const Scal* sc, int zb) {
     cudaStream_t s = work_stream(S);
     const int sms = S->ctx->num_sms;
-    if (mg_z_batch(zb) == MG_ZB_TMA && S->d_zt[l].n > 0) return mg_launch_smooth_zt(s, sms, S->dL, S->d_zt[l].ptr, S->d_zt[l].n, color, sc);
+    if (mg_z_batch(zb) == MG_ZB_TMA && S->d_zt[l].n > 0)
+        return mg_launch_smooth_zt(s, sms, S->dL, S->d_zt[l].ptr, S->d_zt[l].n, color, sc, S->d_zt_maps);
     return mg_launch_smooth_z(s, sms, S->precision == OPFLOW_PREC_MIXED, S->dL, S->d_zsm[l].ptr, S->d_zsm[l].n, color, sc, zb);
 }
 static int smooth_z_level(MGSystem* S, int l, int color) { return smooth_z_level(S, l, color, S->dS, S->zb[l]); }
@@ -1189,6 +1208,8 @@ int mg_compose(MGSystem* C, const std::vector<MGSystem*>& parts, const std::vect
     C->zb.assign(C->nlevels, 4);
     C->tile_alt.assign(C->nlevels, {});
     C->zt_ch.assign(C->nlevels, {});
+    C->zt_maps.clear();
+    bool any_maps = false;
     std::vector<size_t> zb_tiles(C->nlevels, 0);  // each level takes the batch of the part with most tiles there
     C->coarse_sm_ch.clear();
     for (size_t q = 0; q < parts.size(); ++q) {
@@ -1196,6 +1217,11 @@ int mg_compose(MGSystem* C, const std::vector<MGSystem*>& parts, const std::vect
         const int base = (int) lv.size();
         for (size_t l = 0; l < P->lv_host.size(); ++l) {
             LvlDev D = P->lv_host[l];
+            // the part's tensor maps move with its level (they address the part's own vectors)
+            const bool has_maps = 2 * l + 1 < P->zt_maps.size();
+            C->zt_maps.push_back(has_maps ? P->zt_maps[2 * l] : CUtensorMap{});
+            C->zt_maps.push_back(has_maps ? P->zt_maps[2 * l + 1] : CUtensorMap{});
+            any_maps = any_maps || (has_maps && P->d_zt_maps);
             D.problem = (int) q;
             if (D.coarse >= 0) D.coarse += base;
             if (D.fine >= 0) D.fine += base;
@@ -1282,6 +1308,15 @@ int mg_compose(MGSystem* C, const std::vector<MGSystem*>& parts, const std::vect
         upload(C->tile_ch[l], C->d_tiles[l]);
         upload(C->zsm_ch[l], C->d_zsm[l]);
         upload(C->zt_ch[l], C->d_zt[l]);
+    }
+    C->d_zt_maps = nullptr;
+    if (any_maps) {
+        C->d_zt_maps = (CUtensorMap*) C->arena.alloc(C->zt_maps.size() * sizeof(CUtensorMap));
+        if (!C->d_zt_maps) return fail(OPFLOW_E_NOMEM, "tensor maps");
+        OPG_CUDA(cudaMemcpyAsync(C->d_zt_maps, C->zt_maps.data(), C->zt_maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice, ctx->stream));
+    } else {
+        for (auto& z : C->zt_ch) z.clear();
+        for (auto& z : C->d_zt) z.n = 0;
     }
     upload(C->coarse_sm_ch, C->d_coarse_sm);
     C->kd_host = kd;

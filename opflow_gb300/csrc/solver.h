@@ -76,6 +76,8 @@ struct MGSystem {
     // tiles of the TMA-staged smoother (float32 levels whose rows hold a multiple of 4 cells)
     std::vector<std::vector<Chunk>> zt_ch;
     std::vector<ChunkList> d_zt;
+    std::vector<CUtensorMap> zt_maps;  // the x and b maps of level index l at [2 l], [2 l + 1] (levels with zt tiles)
+    CUtensorMap* d_zt_maps = nullptr;
     bool tune_measure = true;  // false: cached tuner choices only, nothing timed (the request server)
     // the other 2D tile shape of a tiled level, when the tuner is to time it against tile_ch
     std::vector<std::vector<Chunk>> tile_alt;
