@@ -395,7 +395,7 @@ __device__ __forceinline__ void tensormap_acquire(const CUtensorMap* map) {
 // read them.  Updates go straight to global memory: a half sweep reads only the other colour, which it
 // never writes.  Interior cells use the interior class's coefficients in the other kernels' operation
 // order (bit-identical).  maps[2 * level] and maps[2 * level + 1] are the level's x and b maps.
-constexpr int ZT_RING = 8, ZT_AHEAD = 4, ZT_W = 40, ZT_H = MG_ZT_Y + 2;
+constexpr int ZT_RING = 8, ZT_AHEAD = 5, ZT_W = 40, ZT_H = MG_ZT_Y + 2;
 constexpr int ZT_XSLOT = ((ZT_W * ZT_H * 4 + 127) / 128) * 32;  // floats per x slot (128-byte multiple)
 constexpr unsigned ZT_BYTES = (ZT_W * ZT_H + 32 * MG_ZT_Y) * 4;   // bytes per plane (both boxes)
 struct ZtStage {
@@ -403,7 +403,9 @@ struct ZtStage {
     float b[ZT_RING][MG_ZT_Y * 32];
     unsigned long long bar[ZT_RING];
 };
-static_assert(ZT_AHEAD + 3 <= ZT_RING, "a slot is refilled only after its plane is no longer read");
+// the slot refilled at step k held plane k + ZT_AHEAD - ZT_RING, last read at step k + ZT_AHEAD - ZT_RING + 1,
+// which every thread has left once it passes step k's first barrier
+static_assert(ZT_AHEAD + 2 <= ZT_RING, "a slot is refilled only after its plane is no longer read");
 static_assert((MG_ZT_Y * 32 * 4) % 128 == 0, "b slots on 128-byte boundaries");
 
 __global__ void __launch_bounds__(32 * MG_ZT_Y) mg_smooth_zt(const LvlDev* __restrict__ Ls, const Chunk* __restrict__ ch, int nch, int color,
@@ -455,6 +457,10 @@ __global__ void __launch_bounds__(32 * MG_ZT_Y) mg_smooth_zt(const LvlDev* __res
                 failed = true;
                 break;
             }
+            if (issued < last) {  // every thread is past step k - 1: the refilled slot is no longer read
+                ++issued;
+                if (producer) issue(issued);
+            }
             const int i = i0 + lane, j = j0 + warp;
             if (i < n0 && j < n1 && ((i + j + k + color) & 1) == 0) {
                 if (i > 0 && i < n0 - 1 && j > 0 && j < n1 - 1 && k > 0 && k < n2 - 1) {
@@ -471,11 +477,6 @@ __global__ void __launch_bounds__(32 * MG_ZT_Y) mg_smooth_zt(const LvlDev* __res
                 } else {
                     zq_push(Q, 1u, k - k0, warp, lane);
                 }
-            }
-            __syncthreads();  // plane k - 1's slot is free from here on
-            if (issued < last) {
-                ++issued;
-                if (producer) issue(issued);
             }
         }
         seq = base + (unsigned) (last - k0 + 2);
