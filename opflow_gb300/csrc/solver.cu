@@ -27,6 +27,7 @@
 
 #include <chrono>
 #include <cmath>
+#include <algorithm>
 #include <array>
 #include <functional>
 #include <map>
@@ -511,6 +512,22 @@ int mg_add_problem(MGSystem* S, opflow_field target, const opflow_node* nodes, i
 static int smooth_z_level(MGSystem* S, int l, int color, const Scal* sc, int zb);
 int mg_check_error(MGSystem* S);
 
+// zt_full: per level, whether the staged smoother's tiles cover every level index the z tiles cover
+static void zt_coverage(MGSystem* S) {
+    S->zt_full.assign(S->nlevels, 0);
+    for (int l = 0; l < S->nlevels; ++l) {
+        if (S->zt_ch[l].empty()) continue;
+        std::vector<int> a, b;
+        for (const Chunk& c : S->zsm_ch[l]) a.push_back(c.lvl);
+        for (const Chunk& c : S->zt_ch[l]) b.push_back(c.lvl);
+        std::sort(a.begin(), a.end());
+        a.erase(std::unique(a.begin(), a.end()), a.end());
+        std::sort(b.begin(), b.end());
+        b.erase(std::unique(b.begin(), b.end()), b.end());
+        S->zt_full[l] = a == b;
+    }
+}
+
 // Device time (ms) of `launch`, run once to warm up and once timed on the system's stream; negative
 // when a launch fails.
 static float time_launch(MGSystem* S, const std::function<int()>& launch) {
@@ -568,7 +585,7 @@ static int tune_levels(MGSystem* S) {
         const ChunkList& Z = S->d_zsm[l];
         if (Z.n > 0) {
             std::vector<int> cands = {4, 2, 8};
-            if (S->d_zt[l].n > 0) cands.push_back(MG_ZB_TMA);
+            if (S->d_zt[l].n > 0 && S->zt_full[l]) cands.push_back(MG_ZB_TMA);
             S->zb[l] = choose(level_key("mg_smooth_z", S, l), cands, [&](int zb) {
                 return time_launch(S, [&] {
                     OPG_TRY(smooth_z_level(S, l, 0, nullptr, zb));
@@ -886,6 +903,7 @@ int mg_finalize(MGSystem* S) {
         S->zt_maps[2 * m.first] = m.second[0];
         S->zt_maps[2 * m.first + 1] = m.second[1];
     }
+    zt_coverage(S);
     S->d_zt_maps = nullptr;
     if (!zt_maps.empty()) {
         S->d_zt_maps = (CUtensorMap*) S->arena.alloc(S->zt_maps.size() * sizeof(CUtensorMap));
@@ -913,7 +931,7 @@ static cudaStream_t work_stream(const MGSystem* S) { return S->recording ? S->re
 static int smooth_z_level(MGSystem* S, int l, int color, const Scal* sc, int zb) {
     cudaStream_t s = work_stream(S);
     const int sms = S->ctx->num_sms;
-    if (mg_z_batch(zb) == MG_ZB_TMA && S->d_zt[l].n > 0)
+    if (mg_z_batch(zb) == MG_ZB_TMA && S->d_zt[l].n > 0 && S->zt_full[l])
         return mg_launch_smooth_zt(s, sms, S->dL, S->d_zt[l].ptr, S->d_zt[l].n, color, sc, S->d_zt_maps);
     return mg_launch_smooth_z(s, sms, S->precision == OPFLOW_PREC_MIXED, S->dL, S->d_zsm[l].ptr, S->d_zsm[l].n, color, sc, zb);
 }
@@ -1309,6 +1327,7 @@ int mg_compose(MGSystem* C, const std::vector<MGSystem*>& parts, const std::vect
         upload(C->zsm_ch[l], C->d_zsm[l]);
         upload(C->zt_ch[l], C->d_zt[l]);
     }
+    zt_coverage(C);
     C->d_zt_maps = nullptr;
     if (any_maps) {
         C->d_zt_maps = (CUtensorMap*) C->arena.alloc(C->zt_maps.size() * sizeof(CUtensorMap));

@@ -77,6 +77,9 @@ struct MGSystem {
     std::vector<std::vector<Chunk>> zt_ch;
     std::vector<ChunkList> d_zt;
     std::vector<CUtensorMap> zt_maps;  // the x and b maps of level index l at [2 l], [2 l + 1] (levels with zt tiles)
+    // per level: every problem with z tiles there also has zt tiles (only then may the level take the
+    // staged smoother, which visits nothing else)
+    std::vector<char> zt_full;
     CUtensorMap* d_zt_maps = nullptr;
     bool tune_measure = true;  // false: cached tuner choices only, nothing timed (the request server)
     // the other 2D tile shape of a tiled level, when the tuner is to time it against tile_ch
