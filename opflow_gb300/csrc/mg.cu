@@ -348,7 +348,9 @@ __global__ void __launch_bounds__(32 * MG_ZT_Y) mg_prolong_z(const LvlDev* __res
 // TMA copies (global -> shared, completing on an mbarrier) and bounded mbarrier waits.  Every wait gives up after MBAR_SPINS polls; the kernel then records the failure in
 // g_mg_err, waits (bounded again) for the copies it issued and returns.
 __device__ int g_mg_err;
-constexpr int MBAR_SPINS = 1 << 24;
+// polls of a wait (each suspends the thread for up to MBAR_SUSPEND_NS): about a second in all
+constexpr int MBAR_SPINS = 1 << 20;
+constexpr unsigned MBAR_SUSPEND_NS = 1000;
 
 __device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned) __cvta_generic_to_shared(p); }
 __device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
@@ -358,14 +360,16 @@ __device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier
 __device__ __forceinline__ void mbar_arrive_expect(unsigned long long* bar, unsigned bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
 }
+// true once the phase of the given parity has completed; the thread is suspended (not spinning) while it
+// waits, for at most MBAR_SUSPEND_NS
 __device__ __forceinline__ bool mbar_test(unsigned long long* bar, unsigned parity) {
     unsigned done;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
-        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(done)
-        : "r"(smem_addr(bar)), "r"(parity)
+        : "r"(smem_addr(bar)), "r"(parity), "r"(MBAR_SUSPEND_NS)
         : "memory");
     return done != 0;
 }
