@@ -113,3 +113,39 @@ def test_explicit_tiling_choice_changes_no_bit(ctx, fresh, monkeypatch, tmp_path
     api.tune_set_cache(forced)
     assert np.array_equal(run(), plain)
     assert api.tune_stats()[0] == 0
+
+
+def test_batch_level_mixing_row_lengths_keeps_every_problem_smoothed(ctx, fresh, monkeypatch, tmp_path):
+    """A batched level holding a problem with rows of 128 cells (staged tiles) and one with rows of 130
+    (none): forcing the staged smoother there must still smooth both, so the results stay those of the
+    untuned batch, bit for bit."""
+    probs = [api.Problem([n, 96, 80], [1.0 / n, 1.0 / 96, 1.0 / 80], alpha=0.0, beta=1.0, loc=api.LocOnMesh.Center, bc=api.BCType.Neum)
+             for n in (128, 130)]
+    rng = np.random.default_rng(8)
+    fs = []
+    for p in probs:
+        f = rng.standard_normal(int(np.prod(p.n)))
+        fs.append(f - f.mean())
+
+    def run():
+        B = api.Batch(probs, api.StructSolverParams(tol=1e-10, maxIter=100, precision="mixed"), ctx)
+        for i, f in enumerate(fs):
+            B.set(i, f, np.zeros(f.size))
+        st = B.solve()
+        return [(s.niter, s.relerr) for s in st], [B.get(i) for i in range(len(probs))]
+    monkeypatch.setenv("OPFLOW_TUNE", "0")
+    plain = run()
+    monkeypatch.delenv("OPFLOW_TUNE")
+    cache = tmp_path / "tune.txt"
+    api.tune_set_cache(cache)
+    run()
+    zkeys = [ln.split()[0] for ln in cache.read_text().splitlines() if ln.startswith("mg_smooth_z/f32/batch2/")]
+    assert zkeys, cache.read_text()
+    forced = tmp_path / "forced.txt"
+    forced.write_text("".join("%s 16 0\n" % k for k in zkeys))
+    api.tune_clear()
+    api.tune_set_cache(forced)
+    got = run()
+    assert got[0] == plain[0]
+    for a, b in zip(got[1], plain[1]):
+        assert np.array_equal(a, b)
