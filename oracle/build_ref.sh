@@ -1,7 +1,11 @@
 #!/bin/sh
-# Compiles OpFlow's own CPU path (header-only C++ under the reference tree) together with
-# oracle/ref/ref_driver.cpp into oracle/_ref/ref_driver.  Used only to generate and re-check the
-# golden fixtures under tests/golden/; nothing in the package links it.
+# Compiles OpFlow's own CPU path (header-only C++ under the reference tree named by $OPFLOW_REFERENCE)
+# into oracle/_ref/:
+#   ref_driver  (oracle/ref/ref_driver.cpp): explicit evaluation, padding and StencilPad assembly dumps;
+#   ref_solve   (oracle/ref/ref_solve.cpp):  HYPREEqnSolveHandler + PrecondStructSolver<PCG, PFMG>
+#               over the vendored HYPRE struct solvers (built by oracle/build_hypre.sh).
+# Used only to generate and re-check the golden fixtures under tests/golden/; nothing in the package
+# links either binary.
 #
 # The reference needs C++26 and several external pieces that this toolchain (g++ 13) and image lack.
 # The recipe bridges them without running the reference's build system:
@@ -10,12 +14,15 @@
 #     stand-in for the slice of oneTBB used by rangeFor (scheduling only; OpFlow's results do not depend
 #     on the thread count).
 #   * oracle/_ref/gen/OpFlowCoreNoSolvers.hpp : the reference's include/Core umbrella minus its HYPRE /
-#     AMGCL solver headers (the driver emulates HYPREEqnSolveHandler::generateAb without HYPRE).
+#     AMGCL solver headers (ref_driver emulates HYPREEqnSolveHandler::generateAb without HYPRE).
+#   * oracle/_ref/gen/OpFlowCoreHYPRE.hpp : the same umbrella plus the HYPRE handler and the Struct
+#     solver wrappers, still without AMGCL (which needs Boost) and UnifiedSolve.hpp (which includes it).
 #   * oracle/_ref/gen/Core/Meta.hpp : the reference's Meta.hpp with its two C++26 pack-indexing
 #     aliases (`T...[0]`, `T...[sizeof...(T) - 1]`) rewritten as std::tuple_element_t, generated by sed
 #     at build time and never committed.
 set -e
-REF=${OPFLOW_REFERENCE:-/root/reference}
+if [ -z "$OPFLOW_REFERENCE" ]; then echo "set OPFLOW_REFERENCE to the OpFlow source tree" >&2; exit 1; fi
+REF="$OPFLOW_REFERENCE"
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 if [ ! -d "$REF/src/Core" ]; then echo "reference tree not found at $REF" >&2; exit 1; fi
@@ -23,11 +30,14 @@ mkdir -p "$OUT/gen/Core"
 sed -e 's/T\.\.\.\[0\]/std::tuple_element_t<0, std::tuple<T...>>/' \
     -e 's/T\.\.\.\[sizeof\.\.\.(T) - 1\]/std::tuple_element_t<sizeof...(T) - 1, std::tuple<T...>>/' \
     "$REF/src/Core/Meta.hpp" > "$OUT/gen/Core/Meta.hpp"
-# Umbrella of the reference's Core headers without the HYPRE / AMGCL solver layer (those need the
-# vendored HYPRE and Boost builds, which this recipe does not perform).
 grep -v -E 'HYPRE|AMGCL|Solvers/|UnifiedSolve|CSRMatrixGenerator|EquationHolder|StencilHolder' \
     "$REF/include/Core" > "$OUT/gen/OpFlowCoreNoSolvers.hpp"
-${CXX:-g++} -std=c++23 -O2 -ffp-contract=off -fopenmp -w -include numeric \
-    -I"$OUT/gen" -I"$HERE/ref/shim" -I"$REF/src" -I"$REF/include" \
-    -o "$OUT/ref_driver" "$HERE/ref/ref_driver.cpp"
-echo "built $OUT/ref_driver"
+grep -v -E 'AMGCL|UnifiedSolve|CSRMatrixGenerator|EquationHolder|StencilHolder|Solvers/SemiStruct/SemiStructSolverFAC|Solvers/IJ' \
+    "$REF/include/Core" > "$OUT/gen/OpFlowCoreHYPRE.hpp"
+CXXFLAGS="-std=c++23 -O2 -ffp-contract=off -w -include numeric -I$OUT/gen -I$HERE/ref/shim -I$HERE/ref -I$REF/src -I$REF/include"
+${CXX:-g++} $CXXFLAGS -fopenmp -o "$OUT/ref_driver" "$HERE/ref/ref_driver.cpp" &
+"$HERE/build_hypre.sh" > /dev/null
+${CXX:-g++} $CXXFLAGS $(cat "$OUT/hypre/include_flags.txt") -o "$OUT/ref_solve" "$HERE/ref/ref_solve.cpp" \
+    "$OUT/hypre/libHYPRE_struct.a" -lm
+wait
+echo "built $OUT/ref_driver $OUT/ref_solve"

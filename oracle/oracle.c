@@ -1062,20 +1062,32 @@ int or_assemble(const opflow_mesh_desc* m, const opflow_field_desc* descs, doubl
     if (offsets)
         for (int e = 0; e < comm.n; ++e)
             for (int d = 0; d < D; ++d) offsets[e * D + d] = comm.key[e][d];
-    size_t cell = 0;
-    BOX_FOR(D, lo, hi, idx) {
-        Val v = evp(&c, n - 1, idx);
-        Pad cur = v.p;
-        for (int e = 0; e < cur.n; ++e)
-            for (int d = 0; d < 3; ++d) cur.key[e][d] -= idx[d];
-        for (int e = 0; e < comm.n; ++e) {
-            int f = pad_find(&cur, comm.key[e]);
-            double x = f >= 0 ? cur.val[f] : 0.;
-            coef[cell * comm.n + e] = x == 0. ? 0. : x; /* +0 for -0 */
+    /* cells are independent: the outermost dimension's slabs run on several host threads (the values
+     * do not depend on the thread count; each slab writes its own rows of coef and rhs) */
+    const int outer = D - 1;
+    size_t slab = 1;
+    for (int d = 0; d < outer; ++d) slab *= (size_t) (hi[d] - lo[d]);
+#pragma omp parallel for schedule(static)
+    for (int o = lo[outer]; o < hi[outer]; ++o) {
+        int l2[3] = {lo[0], lo[1], lo[2]}, h2[3] = {hi[0], hi[1], hi[2]}, ix[3];
+        l2[outer] = o;
+        h2[outer] = o + 1;
+        size_t cell = (size_t) (o - lo[outer]) * slab;
+        BOX_FOR(D, l2, h2, ix) {
+            Val v = evp(&c, n - 1, ix);
+            Pad cur = v.p;
+            for (int e = 0; e < cur.n; ++e)
+                for (int d = 0; d < 3; ++d) cur.key[e][d] -= ix[d];
+            for (int e = 0; e < comm.n; ++e) {
+                int f = pad_find(&cur, comm.key[e]);
+                double x = f >= 0 ? cur.val[f] : 0.;
+                coef[cell * comm.n + e] = x == 0. ? 0. : x; /* +0 for -0 */
+            }
+            rhs[cell] = -cur.bias;
+            ++cell;
         }
-        rhs[cell] = -cur.bias;
-        ++cell;
     }
+    (void) idx;
     if (pin) {
         /* the first unknown's row: identity, rhs 0 (lines 145-163) */
         for (int e = 0; e < comm.n; ++e) {

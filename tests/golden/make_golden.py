@@ -1,11 +1,12 @@
 """Regenerates the golden fixtures in this directory from the reference itself.
 
-Runs oracle/_ref/ref_driver (OpFlow's own CPU code, built by oracle/build_ref.sh from the reference
+Runs oracle/_ref/ref_driver and oracle/_ref/ref_solve (OpFlow's own CPU code and, for the solves, its
+HYPREEqnSolveHandler over the vendored HYPRE PCG + PFMG, built by oracle/build_ref.sh from the reference
 sources) on small cases and stores every dump as a .npz next to this script.  Needs the reference tree
-(present only where the fixtures are generated); the fixtures themselves are committed so the tests
-run anywhere.
+(named by $OPFLOW_REFERENCE, present only where the fixtures are generated); the fixtures themselves are
+committed so the tests run anywhere.
 
-    python tests/golden/make_golden.py [case ...]     (all cases when none is named)
+    OPFLOW_REFERENCE=<OpFlow tree> python tests/golden/make_golden.py [case ...]   (all cases when none is named)
 """
 import json
 import os
@@ -18,6 +19,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
+SOLVER = os.path.join(ROOT, "oracle", "_ref", "ref_solve")
 
 CASES = {
     # FTCS2D (Corner, Dirichlet all sides): n, steps, seed, bc value, dt/h^2
@@ -53,6 +55,17 @@ CASES = {
     # examples/CONV1D: nodes, steps
     "conv1d_n101": ["conv1d", "101", "100"],
 }
+# HYPREEqnSolveHandler + PrecondStructSolver<PCG, PFMG> (tol 1e-10, maxIter 100, twoNorm): case, cells per
+# side, seed.  The solution stored is the one PFMG with HYPRE's default parameters gives (the reference
+# tests' usage, NeumEqnTest.cpp:204-216); a second run with one PFMG V-cycle per PCG iteration (the CPU
+# baseline's setting) contributes only its iteration count and residual.  The right-hand side f is not
+# stored: the tests regenerate it from the seed and check it against the stored SHA-256 of its bytes.
+HYPRE_CASES = {
+    "hypre_neum2d_n256": ["neum2d", "256", "7"],
+    "hypre_dirc2d_n256": ["dirc2d", "256", "8"],
+    "hypre_var3d_n32": ["var3d", "32", "9"],
+}
+
 # field construction + padding: nx, ny, loc (0 corner / 1 centre), bc_lo, bc_hi, ext
 # bc codes: 0 Dirc, 1 Neum, 2 Periodic, 3 Symm, 4 ASymm
 for loc in (0, 1):
@@ -69,6 +82,9 @@ def parse(path):
         kind, js = raw[pos:nl].decode().split(" ", 1)
         meta = json.loads(js)
         pos = nl + 1
+        if kind == "SOLVE":
+            out.append((kind, meta, {}))
+            continue
         if kind == "FIELD":
             n = meta["count"]
             arr = np.frombuffer(raw[pos:pos + 8 * n], dtype="<f8").copy()
@@ -84,10 +100,38 @@ def parse(path):
     return out
 
 
+def hypre_case(name, args):
+    import hashlib
+    arrays, metas = {}, []
+    with tempfile.TemporaryDirectory() as td:
+        out = os.path.join(td, "o.bin")
+        subprocess.check_call([SOLVER, out] + args + ["1e-10", "100", "1", "0"])
+        recs = parse(out)
+        subprocess.check_call([SOLVER, out] + args + ["1e-10", "100", "1", "1"])
+        one_cycle = [m for k, m, _ in parse(out) if k == "SOLVE"][0]
+    for kind, meta, arrs in recs:
+        if kind == "SOLVE":
+            metas.append({"kind": kind, "key": "solve", "meta": meta})
+            metas.append({"kind": kind, "key": "solve_pfmg1", "meta": one_cycle})
+            continue
+        key = meta["name"]
+        if key == "f":
+            meta = dict(meta, sha256=hashlib.sha256(arrs["data"].astype("<f8").tobytes()).hexdigest())
+        else:
+            arrays["%s__data" % key] = arrs["data"]
+        metas.append({"kind": kind, "key": key, "meta": meta})
+    arrays["meta"] = np.array(json.dumps({"args": args, "records": metas}))
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrays)
+    print(name, [m["key"] for m in metas], metas[-1]["meta"] if metas else None)
+
+
 def main():
-    if not os.path.exists(DRIVER):
+    if not (os.path.exists(DRIVER) and os.path.exists(SOLVER)):
         subprocess.check_call([os.path.join(ROOT, "oracle", "build_ref.sh")])
-    wanted = set(sys.argv[1:]) or set(CASES)
+    wanted = set(sys.argv[1:]) or (set(CASES) | set(HYPRE_CASES))
+    for name, args in sorted(HYPRE_CASES.items()):
+        if name in wanted:
+            hypre_case(name, args)
     for name, args in sorted(CASES.items()):
         if name not in wanted:
             continue
