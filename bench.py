@@ -43,6 +43,7 @@ import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+from opflow_gb300 import workloads as wl  # noqa: E402  (numpy-only seeded inputs)
 
 METRIC = "served mixed-prec vs plain FP64 GPU: solves/s, p99 @1e-10 resid; GLUP/s %HBM"
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -236,42 +237,6 @@ ITER_BYTES_PER_CELL = 220.0  # algorithmic bytes per level-0 cell and flexible-P
 SOLVE_WORKLOADS = ("poisson2d", "serve", "batched", "poisson3d")
 
 
-def poisson_problem(api, rng, n, ndim, bc):
-    return api.Problem([n] * ndim, [1.0 / n] * ndim, alpha=0.0, beta=1.0, loc=api.LocOnMesh.Center, bc=bc)
-
-
-def rhs_for(np_, rng, p):
-    f = rng.standard_normal(int(np_.prod(p.n)))
-    if p.alpha == 0.0 and p.bc != 1:
-        f -= f.mean()
-    return f
-
-
-def serve_mix(np_, api, seed, count):
-    """Requests of the serving configuration, seeded."""
-    rng = np_.random.default_rng(seed)
-    reqs = []
-    for _ in range(count):
-        u = rng.random()
-        if u < 0.7:
-            if rng.random() < 0.5:
-                n = int(round(np_.exp(rng.uniform(np_.log(129), np_.log(2049)))))
-                ndim = 2
-            else:
-                n = int(round(np_.exp(rng.uniform(np_.log(64), np_.log(256)))))
-                ndim = 3
-            bc = api.BCType.Neum if rng.random() < 0.5 else api.BCType.Dirc
-            p = poisson_problem(api, rng, n, ndim, bc)
-            steps = 1
-        else:
-            n = int(round(np_.exp(rng.uniform(np_.log(129), np_.log(1025)))))
-            dt = 1.0 / n
-            p = api.Problem([n, n], [1.0 / n] * 2, alpha=1.0, beta=dt, loc=api.LocOnMesh.Center, bc=api.BCType.Dirc)
-            steps = int(rng.integers(10, 101))
-        reqs.append((p, rhs_for(np_, rng, p), steps))
-    return reqs
-
-
 def cpu_solve_sample(threads):
     """The oracle's FP64 CG (Jacobi) on a 256^2 Neumann Poisson sample: solves/s on the host cores."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
@@ -359,24 +324,9 @@ def run_poisson2d(args, torch, api, capi, np, ctx, stream, world, rank, local):
                 e2e={"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": a.nbytes, "d2h_bytes_per_step": a.nbytes, "steps": e2e_steps})
 
 
-def batched_problems(np_, api, seed, count):
-    """(I - k Lap) u = f on corner-loc Dirichlet grids: k ~ LogU[1e-4, 1], side ~ LogU[65, 1025] rounded to
-    2^m + 1, f ~ N(0, 1)."""
-    rng = np_.random.default_rng(seed)
-    out = []
-    for _ in range(count):
-        k = float(np_.exp(rng.uniform(np_.log(1e-4), np_.log(1.0))))
-        side = float(np_.exp(rng.uniform(np_.log(65), np_.log(1025))))
-        n = (1 << int(round(np_.log2(side - 1)))) + 1
-        h = 1.0 / (n - 1)
-        p = api.Problem([n, n], [h, h], alpha=1.0, beta=k, loc=api.LocOnMesh.Corner, bc=api.BCType.Dirc)
-        out.append((p, rng.standard_normal((n - 2) * (n - 2))))
-    return out
-
-
 def run_batched(args, torch, api, capi, np, ctx, stream, world, rank, local):
     count = args.problems
-    probs = batched_problems(np, api, 99 + rank, count)
+    probs = wl.batched_problems(api, 99 + rank, count)
     mixed = api.StructSolverParams(tol=1e-10, maxIter=200, precision="mixed", zeroGuess=True)
     B = api.Batch([p for p, _ in probs], mixed, ctx)
     for i, (_, f) in enumerate(probs):
@@ -436,19 +386,6 @@ def run_batched(args, torch, api, capi, np, ctx, stream, world, rank, local):
                 e2e={"value": count / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": hb, "d2h_bytes_per_step": hb})
 
 
-def smooth_field(np_, rng, n, modes=6):
-    """A smooth random field on n^3 cell centres (sum of low-wavenumber Fourier modes), std 1."""
-    x = (np_.arange(n) + 0.5) / n
-    g = np_.zeros((n, n, n))
-    for _ in range(modes):
-        k = rng.integers(1, 4, 3)
-        ph = rng.uniform(0, 2 * np_.pi, 3)
-        a = rng.standard_normal()
-        g += a * (np_.cos(2 * np_.pi * k[2] * x + ph[2])[:, None, None] * np_.cos(2 * np_.pi * k[1] * x + ph[1])[None, :, None]
-                  * np_.cos(2 * np_.pi * k[0] * x + ph[0])[None, None, :])
-    return (g - g.mean()) / g.std()
-
-
 def run_poisson3d(args, torch, api, capi, np, ctx, stream, world, rank, local):
     """3D 7-point variable-coefficient Poisson: div(K grad p) = f with K = exp(g) interpolated to faces."""
     n = args.grid or 256
@@ -463,7 +400,7 @@ def run_poisson3d(args, torch, api, capi, np, ctx, stream, world, rank, local):
     rng = np.random.default_rng(4321 + rank)
     kk = K.download()
     sl = K.index_slices(K.assignableRange)
-    kk[sl] = np.exp(smooth_field(np, rng, n))
+    kk[sl] = np.exp(wl.smooth_field(rng, n))
     K.upload(kk)
     ff = f.download()
     v = rng.standard_normal(ff[sl].shape)
@@ -525,7 +462,7 @@ def run_serve(args, torch, api, capi, np, ctx, stream, world, rank, local):
     count = args.requests
     rates = [float(r) for r in str(args.rate).split(",")]
     params = api.StructSolverParams(tol=1e-10, maxIter=200, precision="mixed", zeroGuess=True)
-    reqs = serve_mix(np, api, 77 + rank, count)
+    reqs = wl.serve_mix(api, 77 + rank, count)
     total_solves = sum(s for _, _, s in reqs)
 
     def pinned(n):
@@ -566,8 +503,8 @@ def run_serve(args, torch, api, capi, np, ctx, stream, world, rank, local):
                     worker_s={k: round(st[k], 4) for k in ("setup_s", "compose_s", "iterate_s", "retire_s")})
 
     # warm-up (allocator pool, graphs, kernels)
-    served("mixed", 16, serve_mix(np, api, 3, 4), 1000.0)
-    served("fp64", 1, serve_mix(np, api, 3, 2), 1000.0)
+    served("mixed", 16, wl.serve_mix(api, 3, 4), 1000.0)
+    served("fp64", 1, wl.serve_mix(api, 3, 2), 1000.0)
     sweep = []
     launches = 0
     for rate in rates:
@@ -616,18 +553,6 @@ def run_serve(args, torch, api, capi, np, ctx, stream, world, rank, local):
 
 
 # ------------------------------------------------------------------------------------------- WENO
-def weno_u0(np_, seed, nx, ny):
-    """Per line: a square pulse and a sine pulse with seeded positions, widths and amplitudes."""
-    rng = np_.random.default_rng(seed)
-    x = (np_.arange(nx) + 0.5) / nx
-    c1, w1, a1 = rng.uniform(0.1, 0.4, ny), rng.uniform(0.05, 0.15, ny), rng.uniform(0.5, 1.0, ny)
-    c2, w2, a2 = rng.uniform(0.55, 0.85, ny), rng.uniform(0.05, 0.12, ny), rng.uniform(0.3, 0.8, ny)
-    u = np_.where(np_.abs(x[None, :] - c1[:, None]) < w1[:, None], a1[:, None], 0.0)
-    d = (x[None, :] - c2[:, None]) / w2[:, None]
-    u += np_.where(np_.abs(d) < 1.0, a2[:, None] * np_.cos(0.5 * np_.pi * d) ** 2, 0.0)
-    return u
-
-
 def cpu_weno_sample(threads):
     """The oracle's three WENO5 stage assignments on 4096-cell periodic lines; returns points/s per RK3 step."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
@@ -641,7 +566,7 @@ def cpu_weno_sample(threads):
     mesh = cm.mesh_uniform([nx + 1, ny + 1])
     fd = cm.field_desc(2, capi.CENTER, [(capi.BC_PERIODIC, capi.BC_PERIODIC)] * 2, ext=3)
     h0 = orc.HostField(mesh, fd)
-    h0.data[h0.slices(h0.assignable())] = weno_u0(np, 7, nx, ny)
+    h0.data[h0.slices(h0.assignable())] = wl.weno_u0(7, nx, ny)
     h0.update_padding()
     h1 = orc.HostField(mesh, fd, data=h0.data.copy())
     h2 = orc.HostField(mesh, fd, data=h0.data.copy())
@@ -666,7 +591,7 @@ def run_weno(args, torch, api, capi, np, ctx, stream, world, rank, local, dist):
         b.setBC(d, api.DimPos.start, api.BCType.Periodic, 0.0).setBC(d, api.DimPos.end, api.BCType.Periodic, 0.0)
     u = b.build(ctx)
     host = u.download()
-    host[u.index_slices(u.assignableRange)] = weno_u0(np, 2024 + rank, nx, ny)
+    host[u.index_slices(u.assignableRange)] = wl.weno_u0(2024 + rank, nx, ny)
     u.upload(host)
     hb = torch.from_numpy(host).pin_memory()
     dt = 0.5 / nx

@@ -454,15 +454,19 @@ int opflow_tune_clear(void);
 /* No counterpart in the reference.  For callers that cannot allocate device memory where they need the
  * answer - code running inside a CUDA stream capture (cudaMalloc/cudaFree cannot be captured), hosts
  * whose device memory belongs to their own pool allocator, latency-critical loops that must not
- * synchronise the device: computes r = b - A x and norms[0] = ||b||_2, norms[1] = ||b - A x||_2 (the
- * residual the solvers report as EqnSolveState::relerr = norms[1]/norms[0]) with no allocation at all.
+ * synchronise the device: computes r = b - A x and norms[0] = ||b||_2, norms[1] = ||b - A x||_2 with no
+ * allocation at all.  For a system with nonzero b, norms[1]/norms[0] is the residual the solvers report
+ * as EqnSolveState::relerr (with b = 0 they report norms[1]).  For a pinned system (pinValue) pass the
+ * reference's system: the first unknown's row the identity (centre 1, other slots 0) with b[0] = 0 and
+ * the solution with x[0] = 0, as the solvers return it; that row's residual is then exactly 0.
  * Every pointer is device memory the caller owns: coef is the (2*ndim+1)-point operator as seven
  * float64 slot arrays [7][N] (centre, x-, x+, y-, y+, z-, z+; unused slots ignored), b/x/r hold N
  * values x fastest, norms two values.  Work is enqueued on `stream` (results valid after it completes).
  * The partial sums live in one static 1 MiB device array per device: grids needing more than 65536
  * chunks (one per 1024 cells of every x-row) are rejected with OPFLOW_E_INVALID; calls that overlap on
  * the GPU race on that array.  The first call on a device looks up the array's address with that
- * device current: make it before any stream capture begins. */
+ * device current and keeps it: make it before any stream capture begins, and do not use the entry point
+ * across a cudaDeviceReset of that device in the same process (the kept address would be stale). */
 int opflow_residual_norms_noalloc(void* stream, int ndim, const int* n, const int* periodic, const double* coef, const double* b,
                                   const double* x, double* r, double* norms);
 

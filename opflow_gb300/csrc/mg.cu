@@ -728,9 +728,11 @@ __device__ __forceinline__ void chunk_finish(const Finish& F, int p, const doubl
 
 // mode 0: r = b - A x, partial (b.b, r.r)        mode 1: q = A p, partial (p.q)
 // With to_vc (mode 0) the V-cycle's level-0 input is written as well: b = (T) r, x = 0.
+// With skip0 (mode 0) the first unknown's r is left out of r.r: the true residual of a pinned system,
+// whose first row is the identity with b = 0 (satisfied exactly once the solution is shifted to x[0] = 0).
 template <typename T, int mode>
 __global__ void __launch_bounds__(256, 4) kr_apply(const LvlDev* __restrict__ Ls, const KrylovDev* __restrict__ K, const Chunk* __restrict__ ch, int nch,
-                                                   const Scal* sc, double* partial, int to_vc, Finish F) {
+                                                   const Scal* sc, double* partial, int to_vc, Finish F, int skip0) {
     __shared__ double sh[32];
     __shared__ int flag;
     for (int c = blockIdx.x; c < nch; c += gridDim.x) {
@@ -760,7 +762,7 @@ __global__ void __launch_bounds__(256, 4) kr_apply(const LvlDev* __restrict__ Ls
                         const double r = bv - ax;
                         rp[cell] = r;
                         s0 = fma(bv, bv, s0);
-                        s1 = fma(r, r, s1);
+                        if (!(skip0 && cell == 0)) s1 = fma(r, r, s1);
                         if (to_vc) {
                             vb[cell] = (T) r;
                             vx[cell] = 0;
@@ -1057,11 +1059,12 @@ int mg_launch_bottom(cudaStream_t s, int sms, bool f32, const LvlDev* L, const i
     return check_launch("mg_bottom");
 }
 int kr_launch_apply(cudaStream_t s, int sms, const LvlDev* L, const KrylovDev* K, const Chunk* ch, int nch, const Scal* sc, double* partial, int mode,
-                    const Finish& F, int to_vc, bool f32) {
+                    const Finish& F, int to_vc, bool f32, bool skip_first) {
     if (nch <= 0) return OPFLOW_OK;
-    if (mode == 0 && f32) kr_apply<float, 0><<<grid_of(nch, sms), 256, 0, s>>>(L, K, ch, nch, sc, partial, to_vc, F);
-    else if (mode == 0) kr_apply<double, 0><<<grid_of(nch, sms), 256, 0, s>>>(L, K, ch, nch, sc, partial, to_vc, F);
-    else kr_apply<double, 1><<<grid_of(nch, sms), 256, 0, s>>>(L, K, ch, nch, sc, partial, 0, F);
+    const int sk = skip_first ? 1 : 0;
+    if (mode == 0 && f32) kr_apply<float, 0><<<grid_of(nch, sms), 256, 0, s>>>(L, K, ch, nch, sc, partial, to_vc, F, sk);
+    else if (mode == 0) kr_apply<double, 0><<<grid_of(nch, sms), 256, 0, s>>>(L, K, ch, nch, sc, partial, to_vc, F, sk);
+    else kr_apply<double, 1><<<grid_of(nch, sms), 256, 0, s>>>(L, K, ch, nch, sc, partial, 0, F, 0);
     OPG_LAUNCHED();
     return check_launch("kr_apply");
 }

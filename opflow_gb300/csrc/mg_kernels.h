@@ -53,7 +53,7 @@ int mg_launch_coarse(cudaStream_t s, int sms, bool f32, const LvlDev* L, const i
 // and apply a scalar stage (see Finish), otherwise kr_launch_reduce / kr_launch_scalars do that.
 // to_vc (mode 0): also write the V-cycle's level-0 input (precision f32 ? float : double) from r.
 int kr_launch_apply(cudaStream_t s, int sms, const LvlDev* L, const KrylovDev* K, const Chunk* ch, int nch, const Scal* sc, double* partial, int mode,
-                    const Finish& F = Finish{}, int to_vc = 0, bool f32 = false);
+                    const Finish& F = Finish{}, int to_vc = 0, bool f32 = false, bool skip_first = false);
 // x += alpha p, r -= alpha q and the V-cycle's level-0 input from the new r
 int kr_launch_update(cudaStream_t s, int sms, bool f32, const LvlDev* L, const KrylovDev* K, const Chunk* ch, int nch, const Scal* sc, double* partial,
                      const Finish& F = Finish{});

@@ -17,7 +17,9 @@
 //     entry has to start at zero; but calls whose kernels overlap on the GPU (different streams, or
 //     different host threads) race on the array: serialise them.
 //   - The first call on each device looks up the array's device address (cudaGetSymbolAddress) with
-//     that device current; make that first call before any stream capture begins.
+//     that device current and keeps it; make that first call before any stream capture begins.  The
+//     kept address belongs to the device's context of that moment: after a cudaDeviceReset of the
+//     device the module is loaded again elsewhere, so the entry point must not be used across a reset.
 #include "internal.h"
 
 #include <mutex>

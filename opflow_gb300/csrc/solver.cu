@@ -1578,16 +1578,15 @@ int opflow_solver_solve(opflow_solver s, opflow_solve_state* state) {
         add_scalar<<<gridN(ctx, N), 256, 0, ctx->stream>>>(K.x, N, -shift);
         OPG_LAUNCHED();
     }
-    // true residual of the reference's system
-    OPG_TRY(kr_launch_apply(ctx->stream, ctx->num_sms, S->dL, S->dK, S->dk0, S->nk0, nullptr, S->partial, 0));
+    // true residual of the reference's system (a pinned system's first row, the identity with b = 0, is
+    // satisfied exactly after the shift and is left out of r.r instead of being subtracted afterwards,
+    // which would cancel catastrophically: that row's residual in the singular operator is O(||b||))
+    OPG_TRY(kr_launch_apply(ctx->stream, ctx->num_sms, S->dL, S->dK, S->dk0, S->nk0, nullptr, S->partial, 0, Finish{}, 0, false, pinned));
     OPG_TRY(kr_launch_reduce(ctx->stream, ctx->num_sms, S->partial, S->dfirst, S->dcount, 1, S->red));
     double red[2];
     OPG_CUDA(cudaMemcpyAsync(red, S->red, sizeof red, cudaMemcpyDeviceToHost, ctx->stream));
-    double r0 = 0.;
-    if (pinned) OPG_CUDA(cudaMemcpyAsync(&r0, K.r, 8, cudaMemcpyDeviceToHost, ctx->stream));
     OPG_CUDA(cudaStreamSynchronize(ctx->stream));
-    double rr = red[1] - (pinned ? r0 * r0 : 0.), bb = red[0];
-    if (rr < 0) rr = 0;
+    const double rr = red[1], bb = red[0];
     scatter_box<<<gridN(ctx, N), 256, 0, ctx->stream>>>(s->target->view(), box, K.x, 0.);
     OPG_LAUNCHED();
     s->target->bc_fresh[s->target->cur] = false;

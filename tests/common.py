@@ -113,3 +113,29 @@ def seeded_interior(hf, seed, n_line):
         hf.data[hf.slices(rng)] = orc.u01(seed, (j.astype(np.uint64) * np.uint64(n_line) + i.astype(np.uint64)))
     else:
         raise NotImplementedError
+
+
+def problem_residual(p, f, x):
+    """||b - A x||_2 / ||b||_2 of a problem-form system (api.Problem: alpha*u - beta*Lap(u) = f, the
+    equation `alpha*e - beta*(d2x(e) + d2y(e) [+ d2z(e)]) == f` on its own mesh) assembled by the
+    oracle, with f and x over the unknowns (x fastest).  A pure Neumann Poisson problem is the singular
+    consistent system (no pinned row), so a solution shifted by a constant has the same residual."""
+    nd = len(p.n)
+    nodes_per_dim = [n + 1 if p.loc == capi.CENTER else n for n in p.n]
+    mesh = mesh_uniform(nodes_per_dim, [(0.0, p.h[d] * (nodes_per_dim[d] - 1)) for d in range(nd)])
+    ext = 1 if (p.loc == capi.CENTER or p.bc == capi.BC_NEUM) else 0
+    fd = field_desc(nd, p.loc, [(p.bc, p.bc)] * nd, ext=ext)
+    u, F = orc.HostField(mesh, fd), orc.HostField(mesh, fd)
+    rng = F.assignable()
+    F.data[F.slices(rng)] = np.asarray(f, dtype=np.float64).reshape(F.data[F.slices(rng)].shape)
+    F.update_padding()
+    L = [Leaf("u"), Leaf("f")]
+    lap = api.d2x(L[0]) + api.d2y(L[0]) if nd >= 2 else api.d2x(L[0])
+    if nd == 3:
+        lap = lap + api.d2z(L[0])
+    eq = api.Eq(float(p.alpha) * L[0] - float(p.beta) * lap, L[1])
+    nodes, _ = api.serialize(eq.residual_expr(), L)
+    off, coef, rhs = orc.assemble(u, nodes, [u, F], 0, 0)
+    dims = [r[1] - r[0] for r in rng]
+    r, bn = orc.residual(dims, [0] * nd, off, coef, rhs, np.asarray(x, dtype=np.float64).reshape(-1))
+    return r / bn if bn > 0 else r

@@ -3,7 +3,7 @@ csr_generator_test.json (row pointers, columns, values and right-hand sides of
 `1.0 == d2x(e) + d2y(e)` on a 4x4-cell grid with h = 1 for Dirichlet, Neumann and periodic
 boundaries; the Neumann and periodic systems pin the last row).  Reads the test file as text.
 
-    python tests/golden/extract_csr_golden.py [path/to/OpFlow]
+    python tests/golden/extract_csr_golden.py [path/to/OpFlow]    (default: $OPFLOW_REFERENCE)
 """
 import json
 import os
@@ -14,7 +14,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("OPFLOW_REFERENCE")
+    if not ref:
+        sys.exit("name the OpFlow source tree (argument or $OPFLOW_REFERENCE)")
     src = open(os.path.join(ref, "test/Core/Equation/CSRMatrixGeneratorTest.cpp")).read()
     out = {}
     for name, bc in (("SimplePoisson", "dirc"), ("SimplePoisson_Neum", "neum"), ("SimplePoisson_Periodic", "periodic")):
