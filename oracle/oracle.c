@@ -1185,3 +1185,566 @@ int or_pcg(int D, const int* dims_in, const int* periodic, int ne, const int* of
     free(r); free(z); free(p); free(q);
     return OPFLOW_OK;
 }
+
+/* ------------------------------------------------------------------------------------------------ */
+/* The reference's CPU solve of an assembled structured system, restated: HYPRE Struct PCG           */
+/* (external/hypre/src/krylov/pcg.c:318-830, two-norm stopping test) preconditioned by PFMG          */
+/* (struct_ls/pfmg_setup.c:63-720, pfmg_setup_interp.c:290-410, pfmg_setup_rap.c (Galerkin R A P    */
+/* with R = P^T, pfmg_setup.c:416-427), pfmg_solve.c:31-340, pfmg_relax.c (weighted Jacobi),        */
+/* semi_restrict.c, semi_interp.c).  It is the CPU baseline the benchmark times when the reference    */
+/* itself (OpFlow + vendored HYPRE) is not built on the host, and the tests check it against the      */
+/* fixtures HYPRE produced (iteration counts, residuals, solutions).                                  */
+/*                                                                                                    */
+/* PFMG as restated: semicoarsening by 2 in one direction per level (coarse points at even indices),  */
+/* the direction with the smallest "dxyz" (from the operator's mean off-diagonal couplings,           */
+/* pfmg_setup.c:765-895), dxyz doubled in that direction per level, until every extent is 1;         */
+/* operator-dependent 1D interpolation at the fine (odd) points, P = -(A_left|A_right collapsed) /    */
+/* (A collapsed centre), set to 0 where the direct neighbour coefficient is 0; restriction P^T;      */
+/* coarse operator P^T A P; weighted Jacobi with the weight 2/(3 - beta/alpha) (2/3 when the          */
+/* coefficients vary by more than 10 % or in 1D), one pre- and one post-sweep, relaxation skipped on */
+/* levels not coarsened before in the same direction (skip_relax = 1); the coarsest level: plain     */
+/* Jacobi, min(4 * levels, extent) sweeps.  Stencils of radius 1 only; no periodic directions.       */
+/* Reentrant (no globals): the benchmark runs independent solves on several host threads.            */
+/* ------------------------------------------------------------------------------------------------ */
+typedef struct {
+    int n[3];          /* points per dim (1 beyond ndim)                                  */
+    int g[3];          /* ghosted extents n + 2 (dims < ndim), 1 otherwise                */
+    size_t G;          /* ghosted vector length                                           */
+    int ne;            /* stencil entries                                                 */
+    int off[27][3];    /* their offsets                                                   */
+    long long lo[27];  /* their linear offsets in the ghosted layout                      */
+    double* A;         /* [interior cell][ne], interior cells x fastest                   */
+    double* diag;      /* centre coefficient per interior cell                            */
+    double *x, *b, *r; /* ghosted vectors (ghosts stay 0)                                 */
+    double *p0, *p1;   /* interpolation weights per interior cell (used at odd cdir index) */
+    int cdir, active;
+    double w;
+} PfLvl;
+
+typedef struct {
+    int D, nl;
+    PfLvl L[64];
+    double* t; /* scratch for Jacobi, ghosted, level 0 size */
+} Pfmg;
+
+static inline long long pf_lin(const PfLvl* l, int i, int j, int k) {
+    return ((long long) (k + (l->g[2] > 1)) * l->g[1] + (j + (l->g[1] > 1))) * l->g[0] + (i + 1);
+}
+
+static void pf_geom(PfLvl* l, int D, const int* n) {
+    l->G = 1;
+    for (int d = 0; d < 3; ++d) {
+        l->n[d] = d < D ? n[d] : 1;
+        l->g[d] = d < D ? n[d] + 2 : 1;
+        l->G *= (size_t) l->g[d];
+    }
+}
+
+static void pf_set_offsets(PfLvl* l) {
+    for (int e = 0; e < l->ne; ++e)
+        l->lo[e] = ((long long) l->off[e][2] * l->g[1] + l->off[e][1]) * l->g[0] + l->off[e][0];
+}
+
+/* y = A x over the interior (ghost x are 0, so boundary rows need no test) */
+static void pf_matvec(const PfLvl* l, const double* x, double* y) {
+    size_t c = 0;
+    for (int k = 0; k < l->n[2]; ++k)
+        for (int j = 0; j < l->n[1]; ++j) {
+            long long q = pf_lin(l, 0, j, k);
+            for (int i = 0; i < l->n[0]; ++i, ++q, ++c) {
+                const double* a = l->A + c * l->ne;
+                double s = 0.;
+                for (int e = 0; e < l->ne; ++e) s += a[e] * x[q + l->lo[e]];
+                y[q] = s;
+            }
+        }
+}
+
+/* r = b - A x */
+static void pf_residual(const PfLvl* l, const double* x, const double* b, double* r) {
+    size_t c = 0;
+    for (int k = 0; k < l->n[2]; ++k)
+        for (int j = 0; j < l->n[1]; ++j) {
+            long long q = pf_lin(l, 0, j, k);
+            for (int i = 0; i < l->n[0]; ++i, ++q, ++c) {
+                const double* a = l->A + c * l->ne;
+                double s = 0.;
+                for (int e = 0; e < l->ne; ++e) s += a[e] * x[q + l->lo[e]];
+                r[q] = b[q] - s;
+            }
+        }
+}
+
+/* weighted Jacobi (pfmg_relax.c / point_relax.c): x += w D^-1 (b - A x); zero guess: x = w D^-1 b */
+static void pf_relax(const PfLvl* l, double* x, const double* b, double* t, double w, int sweeps, int zero_guess) {
+    for (int s = 0; s < sweeps; ++s) {
+        if (zero_guess && s == 0) {
+            size_t c = 0;
+            for (int k = 0; k < l->n[2]; ++k)
+                for (int j = 0; j < l->n[1]; ++j) {
+                    long long q = pf_lin(l, 0, j, k);
+                    for (int i = 0; i < l->n[0]; ++i, ++q, ++c) x[q] = l->diag[c] != 0. ? w * b[q] / l->diag[c] : 0.;
+                }
+            continue;
+        }
+        pf_residual(l, x, b, t);
+        size_t c = 0;
+        for (int k = 0; k < l->n[2]; ++k)
+            for (int j = 0; j < l->n[1]; ++j) {
+                long long q = pf_lin(l, 0, j, k);
+                for (int i = 0; i < l->n[0]; ++i, ++q, ++c)
+                    if (l->diag[c] != 0.) x[q] += w * t[q] / l->diag[c];
+            }
+    }
+}
+
+static int pf_find(const PfLvl* l, int ox, int oy, int oz) {
+    for (int e = 0; e < l->ne; ++e)
+        if (l->off[e][0] == ox && l->off[e][1] == oy && l->off[e][2] == oz) return e;
+    return -1;
+}
+
+/* interpolation weights at every point (pfmg_setup_interp.c:325-410): collapse the stencil onto the
+ * coarsening direction; p0 weighs the coarse point below, p1 the one above */
+static void pf_interp_weights(PfLvl* l, int cdir) {
+    int dn[3] = {0, 0, 0}, up[3] = {0, 0, 0};
+    dn[cdir] = -1;
+    up[cdir] = 1;
+    const int s0 = pf_find(l, dn[0], dn[1], dn[2]), s1 = pf_find(l, up[0], up[1], up[2]);
+    const size_t N = (size_t) l->n[0] * l->n[1] * l->n[2];
+    for (size_t c = 0; c < N; ++c) {
+        const double* a = l->A + c * l->ne;
+        double center = 0., w0 = 0., w1 = 0.;
+        for (int e = 0; e < l->ne; ++e) {
+            const int o = l->off[e][cdir];
+            if (o == 0) center += a[e];
+            else if (o == -1) w0 -= a[e];
+            else w1 -= a[e];
+        }
+        if (center == 0.) w0 = w1 = 0.;
+        else {
+            w0 /= center;
+            w1 /= center;
+        }
+        if (s0 < 0 || a[s0] == 0.) w0 = 0.;
+        if (s1 < 0 || a[s1] == 0.) w1 = 0.;
+        l->p0[c] = w0;
+        l->p1[c] = w1;
+    }
+}
+
+static inline size_t pf_cell(const PfLvl* l, int i, int j, int k) { return ((size_t) k * l->n[1] + j) * l->n[0] + i; }
+
+/* coarse operator R A P with R = P^T (the Galerkin product of pfmg_setup_rap.c for rap_type 0) */
+static int pf_rap(const PfLvl* f, PfLvl* c, int cdir, int D) {
+    /* the coarse pattern: offsets reachable through R (cdir -1..1), A (f's offsets) and P */
+    int mark[27] = {0};
+    for (int a = -1; a <= 1; ++a)
+        for (int e = 0; e < f->ne; ++e) {
+            const int t = a + f->off[e][cdir];
+            int ks[2], nk = 0;
+            if ((t & 1) == 0) ks[nk++] = t / 2;
+            else {
+                ks[nk++] = (t - 1) / 2;
+                ks[nk++] = (t + 1) / 2;
+            }
+            for (int q = 0; q < nk; ++q) {
+                int o[3] = {f->off[e][0], f->off[e][1], f->off[e][2]};
+                o[cdir] = ks[q];
+                if (o[cdir] < -1 || o[cdir] > 1) continue;
+                mark[((o[2] + 1) * 3 + (o[1] + 1)) * 3 + (o[0] + 1)] = 1;
+            }
+        }
+    c->ne = 0;
+    int slot[27];
+    for (int m = 0; m < 27; ++m) {
+        slot[m] = -1;
+        if (!mark[m]) continue;
+        const int ox = m % 3 - 1, oy = (m / 3) % 3 - 1, oz = m / 9 - 1;
+        if ((D < 2 && oy) || (D < 3 && oz)) continue;
+        slot[m] = c->ne;
+        c->off[c->ne][0] = ox;
+        c->off[c->ne][1] = oy;
+        c->off[c->ne][2] = oz;
+        c->ne++;
+    }
+    pf_set_offsets(c);
+    const size_t Nc = (size_t) c->n[0] * c->n[1] * c->n[2];
+    c->A = (double*) calloc(Nc * c->ne, sizeof(double));
+    if (!c->A) return 1;
+    int I[3];
+    for (I[2] = 0; I[2] < c->n[2]; ++I[2])
+        for (I[1] = 0; I[1] < c->n[1]; ++I[1])
+            for (I[0] = 0; I[0] < c->n[0]; ++I[0]) {
+                double* ac = c->A + pf_cell(c, I[0], I[1], I[2]) * c->ne;
+                for (int a = -1; a <= 1; ++a) {
+                    int f1[3] = {I[0], I[1], I[2]};
+                    f1[cdir] = 2 * I[cdir] + a;
+                    if (f1[cdir] < 0 || f1[cdir] >= f->n[cdir]) continue;
+                    const size_t c1 = pf_cell(f, f1[0], f1[1], f1[2]);
+                    /* R(I, f1): 1 at the coarse point; the F point's weight towards I otherwise */
+                    const double ra = a == 0 ? 1. : (a == 1 ? f->p0[c1] : f->p1[c1]);
+                    if (ra == 0.) continue;
+                    const double* af = f->A + c1 * f->ne;
+                    for (int e = 0; e < f->ne; ++e) {
+                        if (af[e] == 0.) continue;
+                        int f2[3] = {f1[0] + f->off[e][0], f1[1] + f->off[e][1], f1[2] + f->off[e][2]};
+                        int out = 0;
+                        for (int d = 0; d < 3; ++d) out |= f2[d] < 0 || f2[d] >= f->n[d];
+                        if (out) continue;
+                        const int t = f2[cdir];
+                        int ks[2], nk = 0;
+                        double wk[2];
+                        if ((t & 1) == 0) {
+                            ks[nk] = t / 2;
+                            wk[nk++] = 1.;
+                        } else {
+                            const size_t c2 = pf_cell(f, f2[0], f2[1], f2[2]);
+                            ks[nk] = (t - 1) / 2;
+                            wk[nk++] = f->p0[c2];
+                            ks[nk] = (t + 1) / 2;
+                            wk[nk++] = f->p1[c2];
+                        }
+                        for (int q = 0; q < nk; ++q) {
+                            if (wk[q] == 0.) continue;
+                            int o[3] = {f2[0] - I[0], f2[1] - I[1], f2[2] - I[2]};
+                            o[cdir] = ks[q] - I[cdir];
+                            const int m = ((o[2] + 1) * 3 + (o[1] + 1)) * 3 + (o[0] + 1);
+                            ac[slot[m]] += ra * af[e] * wk[q];
+                        }
+                    }
+                }
+            }
+    return 0;
+}
+
+static void pf_free(Pfmg* P) {
+    for (int l = 0; l < P->nl; ++l) {
+        free(P->L[l].A);
+        free(P->L[l].diag);
+        free(P->L[l].x);
+        free(P->L[l].b);
+        free(P->L[l].r);
+        free(P->L[l].p0);
+        free(P->L[l].p1);
+    }
+    free(P->t);
+}
+
+static int pf_alloc_vectors(PfLvl* l) {
+    const size_t N = (size_t) l->n[0] * l->n[1] * l->n[2];
+    l->x = (double*) calloc(l->G, 8);
+    l->b = (double*) calloc(l->G, 8);
+    l->r = (double*) calloc(l->G, 8);
+    l->p0 = (double*) calloc(N, 8);
+    l->p1 = (double*) calloc(N, 8);
+    l->diag = (double*) calloc(N, 8);
+    if (!l->x || !l->b || !l->r || !l->p0 || !l->p1 || !l->diag) return 1;
+    const int ce = pf_find(l, 0, 0, 0);
+    for (size_t c = 0; c < N; ++c) l->diag[c] = ce >= 0 ? l->A[c * l->ne + ce] : 0.;
+    return 0;
+}
+
+/* hypre_PFMGComputeDxyz (pfmg_setup.c:765-895, the 5/7-point branches generalised to any radius-1
+ * stencil): per direction the mean and mean square of -sign(diag) * (sum of the couplings along it) */
+static int pf_dxyz(const PfLvl* l, int D, double* dxyz) {
+    double cx[3] = {0, 0, 0}, sq[3] = {0, 0, 0};
+    const size_t N = (size_t) l->n[0] * l->n[1] * l->n[2];
+    for (size_t c = 0; c < N; ++c) {
+        const double* a = l->A + c * l->ne;
+        const double sg = l->diag[c] < 0. ? -1. : 1.;
+        for (int d = 0; d < D; ++d) {
+            double t = 0.;
+            for (int e = 0; e < l->ne; ++e) {
+                int only = l->off[e][d] != 0;
+                for (int q = 0; q < 3; ++q)
+                    if (q != d && l->off[e][q] != 0) only = 0;
+                if (only) t += a[e];
+            }
+            t = -sg * t;
+            cx[d] += t;
+            sq[d] += t * t;
+        }
+    }
+    int flag = 0;
+    for (int d = 0; d < D; ++d) {
+        const double mean = cx[d] / (double) N, dev = sq[d] / (double) N - mean * mean;
+        if (dev > 0.1 * mean * mean) flag = 1;
+    }
+    double mx = 0.;
+    for (int d = 0; d < D; ++d) mx = cx[d] > mx ? cx[d] : mx;
+    if (mx == 0.) {
+        for (int d = 0; d < D; ++d) cx[d] = 1.;
+        mx = 1.;
+    }
+    for (int d = 0; d < 3; ++d) {
+        if (d >= D) {
+            dxyz[d] = 1.;
+            continue;
+        }
+        const double maxan = 1.7976931348623157e308 / 1000.;
+        if (cx[d] > mx / maxan) dxyz[d] = sqrt(1. / (cx[d] / mx));
+        else dxyz[d] = sqrt(maxan);
+    }
+    return flag;
+}
+
+static int pf_setup(Pfmg* P, int D, const int* dims, int ne, const int* off, const double* coef) {
+    memset(P, 0, sizeof *P);
+    P->D = D;
+    PfLvl* l0 = &P->L[0];
+    pf_geom(l0, D, dims);
+    l0->ne = ne;
+    for (int e = 0; e < ne; ++e)
+        for (int d = 0; d < 3; ++d) {
+            l0->off[e][d] = d < D ? off[e * D + d] : 0;
+            if (l0->off[e][d] < -1 || l0->off[e][d] > 1) return 2;
+        }
+    pf_set_offsets(l0);
+    const size_t N0 = (size_t) l0->n[0] * l0->n[1] * l0->n[2];
+    l0->A = (double*) malloc(N0 * ne * 8);
+    if (!l0->A) return 1;
+    memcpy(l0->A, coef, N0 * ne * 8);
+    P->nl = 1;
+    if (pf_alloc_vectors(l0)) return 1;
+    P->t = (double*) calloc(l0->G, 8);
+    if (!P->t) return 1;
+    double dxyz[3];
+    const int dflag = pf_dxyz(l0, D, dxyz);
+    int coarsen[3] = {1, 1, 1};
+    for (int l = 0;; ++l) {
+        PfLvl* L = &P->L[l];
+        double mn = dxyz[0] + dxyz[1] + dxyz[2] + 1, alpha = 0., beta = 0.;
+        int cdir = -1;
+        for (int d = 0; d < D; ++d) {
+            if (L->n[d] > 1 && dxyz[d] < mn) {
+                mn = dxyz[d];
+                cdir = d;
+            }
+            alpha += 1. / (dxyz[d] * dxyz[d]);
+        }
+        L->w = 1.;
+        if (cdir != -1) {
+            if (dflag) L->w = 2. / 3.;
+            else {
+                for (int d = 0; d < D; ++d)
+                    if (d != cdir) beta += 1. / (dxyz[d] * dxyz[d]);
+                alpha = beta == alpha ? 0. : beta / alpha;
+                L->w = D > 1 ? 2. / (3. - alpha) : 2. / 3.;
+            }
+        }
+        if (cdir != -1 && l == 63) cdir = -1;
+        if (cdir == -1) {
+            L->active = 1;
+            L->cdir = -1;
+            break;
+        }
+        L->cdir = cdir;
+        if (coarsen[cdir]) {
+            L->active = 1;
+            coarsen[0] = coarsen[1] = coarsen[2] = 0;
+            coarsen[cdir] = 1;
+        } else {
+            L->active = 0;
+            coarsen[cdir] = 1;
+        }
+        dxyz[cdir] *= 2;
+        pf_interp_weights(L, cdir);
+        PfLvl* C = &P->L[l + 1];
+        int nc[3] = {L->n[0], L->n[1], L->n[2]};
+        nc[cdir] = (L->n[cdir] + 1) / 2;
+        pf_geom(C, D, nc);
+        P->nl = l + 2;
+        if (pf_rap(L, C, cdir, D)) return 1;
+        if (pf_alloc_vectors(C)) return 1;
+    }
+    return 0;
+}
+
+/* semi_restrict.c: b_c(I) = r(2I) + p0(2I+1) r(2I+1) + p1(2I-1) r(2I-1) along cdir */
+static void pf_restrict(const PfLvl* f, PfLvl* c, int cdir) {
+    int I[3];
+    for (I[2] = 0; I[2] < c->n[2]; ++I[2])
+        for (I[1] = 0; I[1] < c->n[1]; ++I[1])
+            for (I[0] = 0; I[0] < c->n[0]; ++I[0]) {
+                int F[3] = {I[0], I[1], I[2]};
+                F[cdir] = 2 * I[cdir];
+                double s = f->r[pf_lin(f, F[0], F[1], F[2])];
+                if (F[cdir] + 1 < f->n[cdir]) {
+                    int G[3] = {F[0], F[1], F[2]};
+                    G[cdir] += 1;
+                    s += f->p0[pf_cell(f, G[0], G[1], G[2])] * f->r[pf_lin(f, G[0], G[1], G[2])];
+                }
+                if (F[cdir] - 1 >= 0) {
+                    int G[3] = {F[0], F[1], F[2]};
+                    G[cdir] -= 1;
+                    s += f->p1[pf_cell(f, G[0], G[1], G[2])] * f->r[pf_lin(f, G[0], G[1], G[2])];
+                }
+                c->b[pf_lin(c, I[0], I[1], I[2])] = s;
+            }
+}
+
+/* semi_interp.c + the correction: x(2I) += x_c(I); x(2I+1) += p0 x_c(I) + p1 x_c(I+1) */
+static void pf_interp_add(PfLvl* f, const PfLvl* c, int cdir) {
+    int F[3];
+    for (F[2] = 0; F[2] < f->n[2]; ++F[2])
+        for (F[1] = 0; F[1] < f->n[1]; ++F[1])
+            for (F[0] = 0; F[0] < f->n[0]; ++F[0]) {
+                int I[3] = {F[0], F[1], F[2]};
+                const int t = F[cdir];
+                double e;
+                if ((t & 1) == 0) {
+                    I[cdir] = t / 2;
+                    e = c->x[pf_lin(c, I[0], I[1], I[2])];
+                } else {
+                    const size_t cf = pf_cell(f, F[0], F[1], F[2]);
+                    I[cdir] = (t - 1) / 2;
+                    e = f->p0[cf] * c->x[pf_lin(c, I[0], I[1], I[2])];
+                    if ((t + 1) / 2 < c->n[cdir]) {
+                        I[cdir] = (t + 1) / 2;
+                        e += f->p1[cf] * c->x[pf_lin(c, I[0], I[1], I[2])];
+                    }
+                }
+                f->x[pf_lin(f, F[0], F[1], F[2])] += e;
+            }
+}
+
+static double pf_dot(const PfLvl* l, const double* u, const double* v) {
+    double s = 0.;
+    for (int k = 0; k < l->n[2]; ++k)
+        for (int j = 0; j < l->n[1]; ++j) {
+            long long q = pf_lin(l, 0, j, k);
+            for (int i = 0; i < l->n[0]; ++i, ++q) s += u[q] * v[q];
+        }
+    return s;
+}
+
+static void pf_zero(const PfLvl* l, double* v) { memset(v, 0, l->G * 8); }
+
+/* one PFMG V-cycle from x = 0 on level 0 (pfmg_solve.c:120-330) */
+static void pf_vcycle(Pfmg* P) {
+    PfLvl* L = P->L;
+    const int nl = P->nl;
+    pf_zero(&L[0], L[0].x);
+    pf_relax(&L[0], L[0].x, L[0].b, P->t, L[0].w, 1, 1);
+    if (nl == 1) return;
+    pf_residual(&L[0], L[0].x, L[0].b, L[0].r);
+    pf_restrict(&L[0], &L[1], L[0].cdir);
+    int l = 1;
+    for (; l <= nl - 2; ++l) {
+        if (L[l].active) {
+            pf_relax(&L[l], L[l].x, L[l].b, P->t, L[l].w, 1, 1);
+            pf_residual(&L[l], L[l].x, L[l].b, L[l].r);
+        } else {
+            pf_zero(&L[l], L[l].x);
+            memcpy(L[l].r, L[l].b, L[l].G * 8);
+        }
+        pf_restrict(&L[l], &L[l + 1], L[l].cdir);
+    }
+    /* the coarsest level: Jacobi (weight 1), min(4 * levels, largest extent) sweeps */
+    {
+        int mx = 1;
+        for (int d = 0; d < 3; ++d) mx = L[l].n[d] > mx ? L[l].n[d] : mx;
+        const int sweeps = 4 * nl < mx ? 4 * nl : mx;
+        pf_relax(&L[l], L[l].x, L[l].b, P->t, 1.0, sweeps, 1);
+    }
+    for (l = nl - 2; l >= 1; --l) {
+        pf_interp_add(&L[l], &L[l + 1], L[l].cdir);
+        if (L[l].active) pf_relax(&L[l], L[l].x, L[l].b, P->t, L[l].w, 1, 0);
+    }
+    pf_interp_add(&L[0], &L[1], L[0].cdir);
+    pf_relax(&L[0], L[0].x, L[0].b, P->t, L[0].w, 1, 0);
+}
+
+/* z = M r: `cycles` V-cycles (0: PFMG's defaults, V-cycles until ||b - A z|| < 1e-6 ||b||, at most
+ * 200, always at least one) */
+static void pf_precond(Pfmg* P, const double* r, double* z, int cycles, double* tmp) {
+    PfLvl* L0 = &P->L[0];
+    memcpy(L0->b, r, L0->G * 8);
+    if (cycles > 0 && cycles == 1) {
+        pf_vcycle(P);
+        memcpy(z, L0->x, L0->G * 8);
+        return;
+    }
+    /* iterate x += V(b - A x) */
+    const int maxc = cycles > 0 ? cycles : 200;
+    const double bb = pf_dot(L0, r, r);
+    memset(z, 0, L0->G * 8);
+    for (int it = 0; it < maxc; ++it) {
+        if (it == 0) memcpy(L0->b, r, L0->G * 8);
+        else {
+            pf_residual(L0, z, r, tmp);
+            if (cycles == 0 && pf_dot(L0, tmp, tmp) < 1e-12 * bb) break;
+            memcpy(L0->b, tmp, L0->G * 8);
+        }
+        pf_vcycle(P);
+        for (size_t q = 0; q < L0->G; ++q) z[q] += L0->x[q];
+    }
+}
+
+int or_pfmg_pcg(int D, const int* dims_in, int ne, const int* off, const double* coef, const double* rhs, double* x_out, double tol,
+                int maxit, int precond_cycles, int* iters, double* relres, int* levels) {
+    Pfmg* P = (Pfmg*) calloc(1, sizeof(Pfmg));
+    if (!P) return OPFLOW_E_NOMEM;
+    int rc = pf_setup(P, D, dims_in, ne, off, coef);
+    if (rc) {
+        pf_free(P);
+        free(P);
+        return rc == 2 ? OPFLOW_E_UNSUPPORTED : OPFLOW_E_NOMEM;
+    }
+    PfLvl* L0 = &P->L[0];
+    const size_t G = L0->G;
+    double *x = calloc(G, 8), *b = calloc(G, 8), *r = calloc(G, 8), *p = calloc(G, 8), *s = calloc(G, 8), *tmp = calloc(G, 8);
+    if (!x || !b || !r || !p || !s || !tmp) {
+        free(x); free(b); free(r); free(p); free(s); free(tmp);
+        pf_free(P);
+        free(P);
+        return OPFLOW_E_NOMEM;
+    }
+    size_t c = 0;
+    for (int k = 0; k < L0->n[2]; ++k)
+        for (int j = 0; j < L0->n[1]; ++j) {
+            long long q = pf_lin(L0, 0, j, k);
+            for (int i = 0; i < L0->n[0]; ++i, ++q, ++c) b[q] = rhs[c];
+        }
+    /* PCG (pcg.c), x0 = 0, two-norm test <r,r>/<b,b> < tol^2 */
+    const double bi = pf_dot(L0, b, b);
+    int it = 0;
+    if (bi > 0.) {
+        const double eps = tol * tol;
+        memcpy(r, b, G * 8);
+        pf_precond(P, r, p, precond_cycles, tmp);
+        double gamma = pf_dot(L0, r, p);
+        while (it < maxit) {
+            ++it;
+            pf_matvec(L0, p, s);
+            const double alpha = gamma / pf_dot(L0, s, p);
+            for (size_t q = 0; q < G; ++q) {
+                x[q] += alpha * p[q];
+                r[q] -= alpha * s[q];
+            }
+            pf_precond(P, r, s, precond_cycles, tmp);
+            const double gold = gamma;
+            gamma = pf_dot(L0, r, s);
+            const double ip = pf_dot(L0, r, r);
+            if (ip / bi < eps) break;
+            const double beta = gamma / gold;
+            for (size_t q = 0; q < G; ++q) p[q] = s[q] + beta * p[q];
+        }
+    }
+    c = 0;
+    for (int k = 0; k < L0->n[2]; ++k)
+        for (int j = 0; j < L0->n[1]; ++j) {
+            long long q = pf_lin(L0, 0, j, k);
+            for (int i = 0; i < L0->n[0]; ++i, ++q, ++c) x_out[c] = x[q];
+        }
+    pf_residual(L0, x, b, r);
+    const double rr = pf_dot(L0, r, r);
+    if (iters) *iters = it;
+    if (relres) *relres = bi > 0. ? sqrt(rr / bi) : sqrt(rr);
+    if (levels) *levels = P->nl;
+    free(x); free(b); free(r); free(p); free(s); free(tmp);
+    pf_free(P);
+    free(P);
+    return OPFLOW_OK;
+}

@@ -106,6 +106,29 @@ def test_hypre_solution_solves_the_oracles_system(name):
     assert cm.record(c["meta"], "solve_pfmg1")["relres"] <= 1e-10
 
 
+@pytest.mark.parametrize("cycles", [1, 0])
+@pytest.mark.parametrize("name", CASES)
+def test_restated_pcg_pfmg_reproduces_hypre(name, cycles):
+    """The oracle's restatement of PCG + PFMG (or_pfmg_pcg, the CPU baseline of the benchmark) takes
+    HYPRE's iteration count and ends at HYPRE's final residual, with one PFMG V-cycle per PCG iteration
+    (cycles = 1) and with PFMG's default parameters (cycles = 0, V-cycles to 1e-6 per application)."""
+    c = host_case(name)
+    dims, off, coef, rhs, _ = oracle_system(c, c["x"])
+    x, it, rel, levels = orc.pfmg_pcg(dims, off, coef, rhs, tol=1e-10, maxit=100, cycles=cycles)
+    h = cm.record(c["meta"], "solve_pfmg1" if cycles == 1 else "solve")
+    assert it == h["niter"], (it, h)
+    if cycles == 1:
+        assert abs(rel - h["relres"]) <= 0.01 * h["relres"], (rel, h)
+    else:
+        assert rel <= 1e-10 and h["relres"] <= 1e-10
+    a = x.copy()
+    b = c["x"].data[c["x"].slices(c["x"].assignable())].reshape(-1).copy()
+    if c["pin"]:
+        a -= a.mean()
+        b -= b.mean()
+    assert np.abs(a - b).max() <= 1e-9 * np.abs(b).max()
+
+
 def gpu_solve(ctx, c, prec):
     p = api.CartesianField(c["mesh"], c["fd"], ctx)
     g = {k: api.CartesianField(c["mesh"], c["fd"], ctx) for k in c["fields"]}
