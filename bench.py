@@ -41,6 +41,8 @@ import sys
 import threading
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 from opflow_gb300 import workloads as wl  # noqa: E402  (numpy-only seeded inputs)
@@ -183,24 +185,53 @@ def cpu_ftcs_sample(workload, threads, reps):
     return pts / dt / 1e9, "%s: %d^%d nodes x %d steps on %d host threads (oracle port, %.1f s)" % (workload, n, D, reps, used, dt), used
 
 
+def reference_requests(args):
+    """The systems of the workload in problem form, as (problem, f, steps), without a GPU."""
+    from opflow_gb300 import api
+    import numpy as np
+    if args.workload == "serve":
+        return wl.serve_mix(api, 77, args.requests)
+    if args.workload == "batched":
+        return [(p, f, 1) for p, f in wl.batched_problems(api, 99, args.problems)]
+    if args.workload == "poisson2d":
+        n = args.grid or 2048
+        v = np.random.default_rng(1234).standard_normal((n, n))
+        return [(wl.poisson_problem(api, n, 2, api.BCType.Neum), (v - v.mean()).reshape(-1), 1)]
+    raise SystemExit("the reference arm restates problem-form systems only (serve, batched, poisson2d)")
+
+
+def run_reference_solves(args, threads):
+    """The reference's CPU path for the solve workloads: every timed step solves one system of the
+    workload's window, picked by systematic sampling over the window sorted by size (so --steps K
+    systems cover its size distribution), with the restated HYPRE PCG + PFMG on all host threads,
+    assembly and set-up included as in HYPREEqnSolveHandler::solve.  value = systems / total seconds."""
+    reqs = reference_requests(args)
+    # warm-up: the smallest systems (page in the oracle, the thread pool)
+    small = sorted(reqs, key=lambda r: int(np.prod(r[0].n)))[:max(1, args.warmup)]
+    cpu_pfmg_sample(small, len(small), threads)
+    v, secs, its, used, desc = cpu_pfmg_sample(reqs, max(1, args.steps), threads)
+    one, _, _, _, desc1 = cpu_pfmg_sample(reqs, 3, 1)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * sum(secs) / len(secs), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "requests": len(reqs), "sample": desc, "iterations": its,
+                       "seconds_per_system": secs, "one_core": {"value": one, "unit": "solves/s", "sample": desc1},
+                       "unit_is": "one linear system solved to ||b-Ax||/||b|| <= 1e-10 (a one-shot request or one session step)",
+                       "note": "the reference (OpFlow + vendored HYPRE) is not built on this host; its PCG + PFMG is restated by the "
+                               "oracle, which reproduces HYPRE's iteration counts and residuals on the committed fixtures"},
+            "cpu_baseline": {"value": v, "unit": "solves/s", "cores": used, "kind": "port", "sample": desc},
+            "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
     threads = os.cpu_count() or 1
     if args.workload in SOLVE_WORKLOADS:
-        vals = []
-        for _ in range(max(1, min(args.steps, 3))):
-            v, sample, used = cpu_solve_sample(threads)
-            vals.append(v)
-        value = statistics.median(vals)
-        line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": args.gpus, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": 1e3 / value, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                "dtype": "f64", "data": "synthetic", "config": {"workload": args.workload, "sample": sample},
-                "cpu_baseline": {"value": value, "unit": "solves/s", "cores": used, "kind": "port", "sample": sample},
-                "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        print(json.dumps(line), flush=True)
-        return 0
+        return run_reference_solves(args, threads)
     if args.workload == "weno":
         vals = []
         for _ in range(max(1, min(args.steps, 3))):
@@ -233,33 +264,56 @@ def run_reference(args):
 
 
 # ------------------------------------------------------------------------------------------ solves
-ITER_BYTES_PER_CELL = 220.0  # algorithmic bytes per level-0 cell and flexible-PCG iteration
 SOLVE_WORKLOADS = ("poisson2d", "serve", "batched", "poisson3d")
 
 
-def cpu_solve_sample(threads):
-    """The oracle's FP64 CG (Jacobi) on a 256^2 Neumann Poisson sample: solves/s on the host cores."""
+def iter_bytes_per_cell(ndim, precision="mixed", var_coef=False):
+    """Algorithmic bytes per level-0 cell and flexible-PCG iteration (the measurement table's figures):
+    the float64 Krylov step (SpMV 16 B, vector updates 56 B, dot products 16 B: ~100 B with the
+    preconditioned-vector read) plus one V-cycle at the level precision, (4/3 in 2D, 8/7 in 3D) x
+    (smoother 2 x (16 + 8) + residual 24 + restriction 10 + prolongation 16 = 98 B at float64, half at
+    float32).  Variable coefficients add the (2 ndim + 1) coefficient arrays read by the float64 SpMV
+    and by the two level-0 smoother sweeps at the level precision, over the hierarchy."""
+    h = 4.0 / 3.0 if ndim == 2 else 8.0 / 7.0
+    lvl = 0.5 if precision == "mixed" else 1.0
+    b = 100.0 + h * 98.0 * lvl
+    if var_coef:
+        b += (2 * ndim + 1) * (8.0 + 2 * 8.0 * lvl * h)
+    return b
+
+
+def cpu_pfmg_sample(reqs, nsample, threads, order_key=None):
+    """The reference's CPU solve restated (oracle: assembly as in HYPREEqnSolveHandler::generateAb, then
+    HYPRE PCG + PFMG with one V-cycle per iteration, two-norm test at 1e-10) on a systematic sample of
+    the window's linear systems: sorted by size, every (len/nsample)-th, so the sample covers the
+    window's size distribution.  One-shot requests are timed with their assembly and set-up (a fresh
+    handler's solve()); a session's step without the matrix assembly (staticMat: generateb + setup +
+    solve), the b generation left out.  Returns (solves/s, per-system seconds, iterations, threads, desc)."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import numpy as np
     import common as cm
     import oracle_lib as orc
-    from opflow_gb300 import _capi as capi
     from opflow_gb300 import api
     used = orc.lib().or_set_threads(threads)
-    n = 256
-    mesh = cm.mesh_uniform([n + 1, n + 1])
-    fd = cm.field_desc(2, capi.CENTER, [(capi.BC_NEUM, capi.BC_NEUM)] * 2, ext=1)
-    p, f = orc.HostField(mesh, fd), orc.HostField(mesh, fd)
-    rng = np.random.default_rng(0)
-    v = rng.standard_normal((n, n))
-    f.data[f.slices(f.assignable())] = v - v.mean()
-    L = [cm.Leaf("p"), cm.Leaf("f")]
-    nodes, _ = api.serialize(api.Eq(L[1], api.d2x(L[0]) + api.d2y(L[0])).residual_expr(), L)
-    t0 = time.perf_counter()
-    off, coef, rhs = orc.assemble(p, nodes, [p, f], 0, 1)
-    x, it, rr = orc.pcg([n, n], [0, 0], off, coef, rhs, tol=1e-10, maxit=100000)
-    dt = time.perf_counter() - t0
-    return 1.0 / dt, "256^2 Neumann Poisson, oracle assembly + FP64 Jacobi-PCG to 1e-10 (%d it, %.2f s; HYPRE PFMG is not built here)" % (it, dt), 1
+    order = sorted(range(len(reqs)), key=lambda i: int(np.prod(reqs[i][0].n)))
+    idx = [order[min(len(order) - 1, int((k + 0.5) * len(order) / nsample))] for k in range(nsample)]
+    secs, its = [], []
+    for i in idx:
+        p, f, steps = reqs[i]
+        pin = p.alpha == 0.0 and p.bc == api.BCType.Neum
+        t0 = time.perf_counter()
+        dims, off, coef, rhs = cm.problem_system(p, np.asarray(f), pin)
+        t1 = time.perf_counter()
+        x, it, rel, nl = orc.pfmg_pcg(dims, off, coef, rhs, tol=1e-10, maxit=200, cycles=1, threads=used)
+        t2 = time.perf_counter()
+        if rel > 1e-10:
+            raise RuntimeError("restated PCG+PFMG did not reach 1e-10 on system %d (%g)" % (i, rel))
+        secs.append((t2 - t0) if steps == 1 else (t2 - t1))
+        its.append(it)
+    desc = ("restated HYPRE PCG+PFMG(1 V-cycle), tol 1e-10 two-norm, incl. assembly + setup per one-shot solve; %d systems "
+            "sampled by size from the window (%s unknowns), %d host threads" %
+            (nsample, ",".join(str(int(np.prod(reqs[i][0].n))) for i in idx), used))
+    return nsample / sum(secs), secs, its, used, desc
 
 
 def run_poisson2d(args, torch, api, capi, np, ctx, stream, world, rank, local):
@@ -312,7 +366,8 @@ def run_poisson2d(args, torch, api, capi, np, ctx, stream, world, rank, local):
     h.close()
     N = n * n
     m = out["mixed"]
-    achieved = ITER_BYTES_PER_CELL * N * m["iterations"] / (m["ms_per_solve"] * 1e-3) / 1e9
+    bpc = iter_bytes_per_cell(2, "mixed")
+    achieved = bpc * N * m["iterations"] / (m["ms_per_solve"] * 1e-3) / 1e9
     peak, src = peak_hbm()
     return dict(value=m["solves_per_s"], unit="solves/s", ms=m["ms_per_solve"], launches=m["launches"], dtype="f64 outer / f32 V-cycle",
                 config=dict(workload="poisson2d", grid=[n, n], loc="cell", bc="neumann 0, pinned", rhs="N(0,1) zero mean", tol=1e-10,
@@ -320,7 +375,7 @@ def run_poisson2d(args, torch, api, capi, np, ctx, stream, world, rank, local):
                             l2="level-0 vectors 33.5 MB each; the solve streams several of them per iteration (> L2)"),
                 roofline={"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": src,
                           "traffic": traffic_for("poisson2d"), "kernel": "flexible-PCG iteration (graph: FP32 V-cycle + FP64 Krylov)",
-                          "algorithmic_bytes_per_launch": ITER_BYTES_PER_CELL * N},
+                          "algorithmic_bytes_per_launch": bpc * N * m["iterations"], "bytes_per_cell_iteration": bpc},
                 e2e={"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": a.nbytes, "d2h_bytes_per_step": a.nbytes, "steps": e2e_steps})
 
 
@@ -369,7 +424,7 @@ def run_batched(args, torch, api, capi, np, ctx, stream, world, rank, local):
     torch.cuda.synchronize()
     loop_rate = nloop / (time.perf_counter() - t0)
     cells = sum(int(np.prod([n - 2 for n in p.n])) for p, _ in probs)
-    bytes_per_solve = sum(ITER_BYTES_PER_CELL * int(np.prod([n - 2 for n in p.n])) * it for (p, _), it in zip(probs, iters))
+    bytes_per_solve = sum(iter_bytes_per_cell(2, "mixed") * int(np.prod([n - 2 for n in p.n])) * it for (p, _), it in zip(probs, iters))
     peak, src = peak_hbm()
     achieved = bytes_per_solve / (ms * 1e-3) / 1e9
     hb = 8 * sum(f.size for _, f in probs)
@@ -440,7 +495,7 @@ def run_poisson3d(args, torch, api, capi, np, ctx, stream, world, rank, local):
     h.close()
     m = out["mixed"]
     N = n ** 3
-    bpc = ITER_BYTES_PER_CELL + (0.0 if args.const_coef else 8.0 * 7 * 2)  # + the seven float64 operator arrays read by two level-0 passes
+    bpc = iter_bytes_per_cell(3, "mixed", var_coef=not args.const_coef)
     achieved = bpc * N * m["iterations"] / (m["ms_per_solve"] * 1e-3) / 1e9
     peak, src = peak_hbm()
     return dict(value=m["solves_per_s"], unit="solves/s", ms=m["ms_per_solve"], launches=m["launches"], dtype="f64 outer / f32 V-cycle",
@@ -451,31 +506,63 @@ def run_poisson3d(args, torch, api, capi, np, ctx, stream, world, rank, local):
                             l2="level-0 vectors %.0f MB each (> L2)" % (N * 8 / 1e6)),
                 roofline={"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": src,
                           "traffic": traffic_for("poisson3d"), "kernel": "flexible-PCG iteration (whole-solve graph)",
-                          "algorithmic_bytes_per_launch": bpc * N},
+                          "algorithmic_bytes_per_launch": bpc * N * m["iterations"], "bytes_per_cell_iteration": bpc},
                 e2e={"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": ff.nbytes, "d2h_bytes_per_step": ff.nbytes, "steps": 2})
 
 
 def run_serve(args, torch, api, capi, np, ctx, stream, world, rank, local):
-    """Served mixed precision (continuous batching, up to 64 resident requests) next to plain FP64
-    serving one request at a time, over a sweep of Poisson arrival rates.  The headline (value, e2e)
-    is the highest rate of the sweep, where throughput is set by the servers rather than by arrivals."""
+    """The serving configuration.  One unit throughout is a linear system solved to 1e-10: a one-shot
+    request, or one backward-Euler step of a session.
+
+    value: device-resident throughput of the window's systems (every one-shot request and one step of
+           every session, inputs already in HBM), one batched mixed-precision solve per step, median
+           over the timed steps (CUDA events on the launching stream);
+    e2e:   the request server (continuous batching, mixed precision) at the highest swept arrival rate,
+           host right-hand sides in and host solutions out, every session step counted;
+    next to plain FP64 serving one request at a time on the same stream of requests."""
     count = args.requests
     rates = [float(r) for r in str(args.rate).split(",")]
     params = api.StructSolverParams(tol=1e-10, maxIter=200, precision="mixed", zeroGuess=True)
     reqs = wl.serve_mix(api, 77 + rank, count)
-    total_solves = sum(s for _, _, s in reqs)
+    total_systems = sum(s for _, _, s in reqs)
 
+    # (1) device-resident batched solve of the window's systems
+    B = api.Batch([p for p, _, _ in reqs], params, ctx)
+    for i, (_, f, _) in enumerate(reqs):
+        B.set(i, f)
+    for _ in range(args.warmup):
+        B.solve()
+    torch.cuda.synchronize()
+    l0 = capi.launch_count()
+    ms_steps, iters = [], None
+    for _ in range(args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        st = B.solve()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms_steps.append(e0.elapsed_time(e1))
+        iters = [s.niter for s in st]
+        assert all(s.converged for s in st)
+    launches = capi.launch_count() - l0
+    worst = max(s.relerr for s in st)
+    B.close()
+    dev_ms = statistics.median(ms_steps)
+    value = len(reqs) / (dev_ms * 1e-3)
+    alg = sum(iter_bytes_per_cell(len(p.n), "mixed") * int(np.prod(p.n)) * it for (p, _, _), it in zip(reqs, iters))
+    peak, src = peak_hbm()
+    achieved = alg / (dev_ms * 1e-3) / 1e9
+
+    # (2) the request server: pinned host buffers for the right-hand sides and the results
     def pinned(n):
         return torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
 
-    # requests' right-hand sides and result buffers in pinned host memory (the copies of e2e)
     staged = []
-    for p, f, s in reqs:
+    for p, f, st_ in reqs:
         buf = pinned(f.size)
         buf[:] = f
-        staged.append((p, buf, s))
-    reqs = staged
-    outs = [pinned(f.size) for _, f, _ in reqs]
+        staged.append((p, buf, st_))
+    outs = [pinned(f.size) for _, f, _ in staged]
 
     def served(prec, max_active, rq, rate, out_bufs=None):
         srv = api.Server(api.StructSolverParams(tol=1e-10, maxIter=200, precision=prec), hbm_budget=120 << 30,
@@ -498,58 +585,48 @@ def run_serve(args, torch, api, capi, np, ctx, stream, world, rank, local):
         lat = sorted(r["latency_ms"] for r in res)
         q = lambda z: lat[min(len(lat) - 1, int(np.ceil(z * len(lat))) - 1)]
         return dict(solves_per_s=sum(r["solves"] for r in res) / wall, p50_ms=q(0.5), p99_ms=q(0.99), ok=ok, n=len(res),
-                    iterations=sum(r["iterations"] for r in res), max_active_seen=st["max_active_seen"], wall_s=wall,
-                    compositions=st["compositions"],
+                    systems=sum(r["solves"] for r in res), iterations=sum(r["iterations"] for r in res),
+                    max_active_seen=st["max_active_seen"], wall_s=wall, compositions=st["compositions"],
                     worker_s={k: round(st[k], 4) for k in ("setup_s", "compose_s", "iterate_s", "retire_s")})
 
     # warm-up (allocator pool, graphs, kernels)
     served("mixed", 16, wl.serve_mix(api, 3, 4), 1000.0)
     served("fp64", 1, wl.serve_mix(api, 3, 2), 1000.0)
     sweep = []
-    launches = 0
     for rate in rates:
-        l0 = capi.launch_count()
-        mixed = served("mixed", 64, reqs, rate, outs)
-        launches = capi.launch_count() - l0
-        plain = served("fp64", 1, reqs, rate, outs)
-        sweep.append(dict(rate_per_s=rate, served_mixed=mixed, served_plain_fp64_one_at_a_time=plain,
-                          served_speedup=mixed["solves_per_s"] / plain["solves_per_s"],
-                          p99_ratio_mixed_over_plain=mixed["p99_ms"] / plain["p99_ms"]))
+        sweep.append(dict(rate_per_s=rate, served_mixed=served("mixed", 64, staged, rate, outs)))
     head = sweep[-1]
+    plain = served("fp64", 1, staged, head["rate_per_s"], outs)
+    head["served_plain_fp64_one_at_a_time"] = plain
+    head["served_speedup"] = head["served_mixed"]["solves_per_s"] / plain["solves_per_s"]
+    head["p99_ratio_mixed_over_plain"] = head["served_mixed"]["p99_ms"] / plain["p99_ms"]
     mixed = head["served_mixed"]
-    # device-resident batched throughput of the same one-shot problems (inputs already in HBM)
-    oneshot = [(p, f) for p, f, s in reqs if s == 1]
-    B = api.Batch([p for p, _ in oneshot], params, ctx)
-    for i, (_, f) in enumerate(oneshot):
-        B.set(i, f)
-    B.solve()
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    st = B.solve()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    dev_ms = e0.elapsed_time(e1)
-    dev_rate = len(oneshot) / (dev_ms * 1e-3)
-    B.close()
-    iters = sum(s.niter for s in st)
-    bcells = sum(int(np.prod(p.n)) for p, _ in oneshot)
-    peak, src = peak_hbm()
-    achieved = ITER_BYTES_PER_CELL * bcells * (iters / max(1, len(oneshot))) / (dev_ms * 1e-3) / 1e9
-    return dict(value=dev_rate, unit="solves/s", ms=dev_ms, launches=launches, dtype="f64 outer / f32 V-cycle",
-                config=dict(workload="serve", requests=count, rates_per_s=rates, mix="70% one-shot Poisson (2D LogU[129,2049] / 3D LogU[64,256], "
-                            "Neumann/Dirichlet 50/50), 30% heat sessions 10-100 backward-Euler steps (2D LogU[129,1025])",
-                            solves_in_window=total_solves, budget_gb=120, sweep=sweep, headline_rate_per_s=head["rate_per_s"],
-                            served_speedup=head["served_speedup"], p99_ratio_mixed_over_plain=head["p99_ratio_mixed_over_plain"],
-                            device_resident_batch=dict(problems=len(oneshot), solves_per_s=dev_rate, ms=dev_ms),
-                            value_is="device-resident batched solves/s of the window's one-shot problems (one batched solve per step); "
-                                     "e2e = served mixed-precision solves/s at the highest swept rate, host f in and host x out",
-                            l2="problems of 2-68 MB each, streamed per iteration (> L2 in aggregate)"),
+    hb = 8 * sum(f.size for _, f, _ in staged)
+    return dict(value=value, unit="solves/s", ms=dev_ms, ms_steps=ms_steps, launches=launches, dtype="f64 outer / f32 V-cycle",
+                config=dict(workload="serve", requests=count, rates_per_s=rates,
+                            mix="70% one-shot Poisson (2D side LogU[129,2049] / 3D side LogU[64,256], Neumann/Dirichlet 50/50), "
+                                "30% heat sessions of 10-100 backward-Euler steps (2D side LogU[129,1025])",
+                            unit_is="one linear system solved to ||b-Ax||/||b|| <= 1e-10 (a one-shot request or one session step)",
+                            systems_in_window=len(reqs), systems_served=total_systems, budget_gb=120, sweep=sweep,
+                            headline_rate_per_s=head["rate_per_s"], served_speedup=head["served_speedup"],
+                            p99_ratio_mixed_over_plain=head["p99_ratio_mixed_over_plain"],
+                            device_resident_batch=dict(systems=len(reqs), unknowns=int(sum(int(np.prod(p.n)) for p, _, _ in reqs)),
+                                                       ms_median=dev_ms, ms_min=min(ms_steps), ms_max=max(ms_steps),
+                                                       iterations_min=min(iters), iterations_max=max(iters), worst_rel_residual=worst),
+                            value_is="median over the timed steps of one batched mixed-precision solve of the window's %d systems "
+                                     "(inputs resident in HBM)" % len(reqs),
+                            e2e_is="request server, mixed precision, at %g req/s: %d requests = %d systems, host f in and host x out"
+                                   % (head["rate_per_s"], count, total_systems),
+                            l2="%.1f GB of level-0 vectors per batched solve (> L2): no flush needed" % (
+                                sum(int(np.prod(p.n)) for p, _, _ in reqs) * 48 / 1e9)),
                 roofline={"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": src,
-                          "traffic": traffic_for("serve"), "kernel": "batched flexible-PCG solve of the window's one-shot problems (device-resident)",
-                          "algorithmic_bytes_per_launch": ITER_BYTES_PER_CELL * bcells},
-                e2e={"value": mixed["solves_per_s"], "unit": "solves/s", "h2d_bytes_per_step": 8 * sum(f.size for _, f, _ in reqs),
-                     "d2h_bytes_per_step": 8 * sum(f.size for _, f, _ in reqs), "p50_ms": mixed["p50_ms"], "p99_ms": mixed["p99_ms"]})
+                          "traffic": traffic_for("serve"),
+                          "kernel": "batched flexible-PCG solve of the window's systems (FP32 V-cycle + FP64 Krylov kernels, one launch each per operation)",
+                          "algorithmic_bytes_per_launch": alg,
+                          "bytes_per_cell_iteration": {"2d": iter_bytes_per_cell(2), "3d": iter_bytes_per_cell(3)}},
+                e2e={"value": mixed["solves_per_s"], "unit": "solves/s", "h2d_bytes_per_step": hb, "d2h_bytes_per_step": hb,
+                     "p50_ms": mixed["p50_ms"], "p99_ms": mixed["p99_ms"]},
+                reqs=reqs)
 
 
 # ------------------------------------------------------------------------------------------- WENO
@@ -652,6 +729,74 @@ def run_weno(args, torch, api, capi, np, ctx, stream, world, rank, local, dist):
     if world > 1:
         dist.destroy_process_group()
     return 0
+
+
+def explicit_record(torch, api, capi, np, ctx, stream, local, rank, steps=20, warmup=3):
+    """Path E measured beside the default (solve) line: the 512^3 FTCS3D configuration (fixed-point
+    mode, and the bit-exact IEEE mode) and WENO5-RK3 on 65536 x 4096 periodic lines, each timed with
+    CUDA events on the launching stream over `steps` steps after `warmup`, with its own clock record."""
+    out = {}
+    peak, src = peak_hbm()
+    n = 512
+    mesh = api.MeshBuilder().newMesh(n, n, n)
+    for d in range(3):
+        mesh.setMeshOfDim(d, 0.0, 1.0)
+    mesh = mesh.build()
+    b = api.ExprBuilder().setMesh(mesh).setName("u").setLoc(api.LocOnMesh.Corner)
+    for d in range(3):
+        b.setBC(d, api.DimPos.start, api.BCType.Dirc, 0.0).setBC(d, api.DimPos.end, api.BCType.Dirc, 0.0)
+    u = b.build(ctx)
+    u0 = gaussians_u0(torch, n, 1234 + rank, torch.device("cuda", local)).cpu().numpy()
+    host = u.download()
+    host[...] = u0
+    u.upload(host)
+    h = 1.0 / (n - 1)
+    expr = u + (0.1 * h * h) * (api.d2x(u) + api.d2y(u) + api.d2z(u))
+    pts = (n - 2) ** 3
+    for mode, k in (("fast", steps), ("exact", max(2, steps // 10))):
+        u.assign(expr, mode=mode, steps=warmup)
+        torch.cuda.synchronize()
+        l0 = capi.launch_count()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with ClockSampler(local) as clk:
+            ev0.record(stream)
+            u.assign(expr, mode=mode, steps=k)
+            ev1.record(stream)
+            torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1) / k
+        glups = pts / (ms * 1e-3) / 1e9
+        out["ftcs3d_512_" + mode] = {"glup_per_s": glups, "ms_per_step": ms, "steps": k, "launches": capi.launch_count() - l0,
+                                     "achieved_gbs": 16.0 * glups, "frac": 16.0 * glups / peak, "peak": peak, "peak_source": src,
+                                     "bytes_per_update": 16, "clocks": clk.summary()}
+    del u
+    nx, ny = 4096, 65536
+    mesh = api.MeshBuilder().newMesh(nx + 1, ny + 1).setMeshOfDim(0, 0.0, 1.0).setMeshOfDim(1, 0.0, ny / nx).build()
+    b = api.ExprBuilder().setMesh(mesh).setName("u").setLoc(api.LocOnMesh.Center).setExt(3)
+    for d in range(2):
+        b.setBC(d, api.DimPos.start, api.BCType.Periodic, 0.0).setBC(d, api.DimPos.end, api.BCType.Periodic, 0.0)
+    w = b.build(ctx)
+    host = w.download()
+    host[w.index_slices(w.assignableRange)] = wl.weno_u0(2024 + rank, nx, ny)
+    w.upload(host)
+    del host
+    dt = 0.5 / nx
+    api.weno_rk3(w, dt, warmup)
+    torch.cuda.synchronize()
+    k = max(2, steps // 4)
+    l0 = capi.launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        api.weno_rk3(w, dt, k)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / k
+    rate = nx * ny / (ms * 1e-3) / 1e9
+    out["weno_65536x4096"] = {"gpts_per_s": rate, "ms_per_rk3_step": ms, "steps": k, "launches": capi.launch_count() - l0,
+                              "achieved_gbs": 16.0 * rate, "frac": 16.0 * rate / peak, "bytes_per_point_rk3_step": 16,
+                              "clocks": clk.summary()}
+    del w
+    return out
 
 
 # ------------------------------------------------------------------------------------------- ours
@@ -771,12 +916,16 @@ def run_ours(args):
             dist.all_reduce(tt, op=dist.ReduceOp.MIN)  # every replica does the same work: slowest rank * N
             value = float(tt.item()) * world
         cpu = None
-        if rank == 0 and not args.no_cpu_baseline:
+        if rank == 0 and not args.no_cpu_baseline and args.workload != "poisson3d":
             try:
-                v, sample, used = cpu_solve_sample(os.cpu_count() or 1)
-                cpu = {"value": v, "unit": "solves/s", "cores": used, "kind": "port", "sample": sample}
+                v, secs, its, used, desc = cpu_pfmg_sample(r.get("reqs") or reference_requests(args), 6 if args.workload == "serve" else 2,
+                                                           os.cpu_count() or 1)
+                cpu = {"value": v, "unit": "solves/s", "cores": used, "kind": "port", "sample": desc}
             except Exception as ex:
                 cpu = {"value": None, "unit": "solves/s", "cores": 0, "kind": "port", "sample": "failed: %s" % ex}
+        r.pop("reqs", None)
+        if args.workload == "serve" and not args.no_explicit:
+            r["config"]["explicit"] = explicit_record(torch, api, capi, np, ctx, stream, local, rank)
         line = {"metric": METRIC, "value": value, "unit": r["unit"], "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
                 "ms_per_step": r["ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": r["dtype"],
                 "data": "synthetic", "config": dict(r["config"], parallelism="replicas" if world > 1 else "single"),
@@ -913,11 +1062,12 @@ def main():
                                                             "ftcs_batch"])
     ap.add_argument("--problems", type=int, default=512, help="batched: problems per batch")
     ap.add_argument("--loop-sample", type=int, default=64, help="batched: problems timed in the plain FP64 one-at-a-time loop")
-    ap.add_argument("--requests", type=int, default=48, help="serve: requests per measurement window")
+    ap.add_argument("--requests", type=int, default=500, help="serve: requests per measurement window")
     ap.add_argument("--rate", default="50,200,2000", help="serve: Poisson arrival rates (requests/s), comma-separated; the last is the headline")
     ap.add_argument("--mode", default="fast", choices=["fast", "exact"])
     ap.add_argument("--grid", type=int, default=0, help="override the grid side (profiling a smaller case)")
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU baseline leg (profiling runs)")
+    ap.add_argument("--no-explicit", action="store_true", help="serve: skip the explicit-path record (profiling runs)")
     ap.add_argument("--sweeps", type=int, default=2, help="poisson2d: red-black Gauss-Seidel sweeps before and after each coarsening")
     ap.add_argument("--const-coef", action="store_true", help="poisson3d: constant coefficient (the serving workload's 3D operator)")
     args = ap.parse_args()

@@ -1204,7 +1204,8 @@ int or_pcg(int D, const int* dims_in, const int* periodic, int ne, const int* of
 /* coefficients vary by more than 10 % or in 1D), one pre- and one post-sweep, relaxation skipped on */
 /* levels not coarsened before in the same direction (skip_relax = 1); the coarsest level: plain     */
 /* Jacobi, min(4 * levels, extent) sweeps.  Stencils of radius 1 only; no periodic directions.       */
-/* Reentrant (no globals): the benchmark runs independent solves on several host threads.            */
+/* Reentrant (no globals); `threads` host threads share each loop (the sums of a dot product are     */
+/* then split by thread, so the last bits may depend on the thread count, as in HYPRE with OpenMP).   */
 /* ------------------------------------------------------------------------------------------------ */
 typedef struct {
     int n[3];          /* points per dim (1 beyond ndim)                                  */
@@ -1219,6 +1220,7 @@ typedef struct {
     double *p0, *p1;   /* interpolation weights per interior cell (used at odd cdir index) */
     int cdir, active;
     double w;
+    int nt;            /* host threads for this level's loops                             */
 } PfLvl;
 
 typedef struct {
@@ -1247,54 +1249,61 @@ static void pf_set_offsets(PfLvl* l) {
 
 /* y = A x over the interior (ghost x are 0, so boundary rows need no test) */
 static void pf_matvec(const PfLvl* l, const double* x, double* y) {
-    size_t c = 0;
-    for (int k = 0; k < l->n[2]; ++k)
-        for (int j = 0; j < l->n[1]; ++j) {
-            long long q = pf_lin(l, 0, j, k);
-            for (int i = 0; i < l->n[0]; ++i, ++q, ++c) {
-                const double* a = l->A + c * l->ne;
-                double s = 0.;
-                for (int e = 0; e < l->ne; ++e) s += a[e] * x[q + l->lo[e]];
-                y[q] = s;
-            }
+    const long long rows = (long long) l->n[1] * l->n[2];
+#pragma omp parallel for schedule(static) num_threads(l->nt) if (l->nt > 1)
+    for (long long row = 0; row < rows; ++row) {
+        const int j = (int) (row % l->n[1]), k = (int) (row / l->n[1]);
+        size_t c = (size_t) row * l->n[0];
+        long long q = pf_lin(l, 0, j, k);
+        for (int i = 0; i < l->n[0]; ++i, ++q, ++c) {
+            const double* a = l->A + c * l->ne;
+            double s = 0.;
+            for (int e = 0; e < l->ne; ++e) s += a[e] * x[q + l->lo[e]];
+            y[q] = s;
         }
+    }
 }
 
 /* r = b - A x */
 static void pf_residual(const PfLvl* l, const double* x, const double* b, double* r) {
-    size_t c = 0;
-    for (int k = 0; k < l->n[2]; ++k)
-        for (int j = 0; j < l->n[1]; ++j) {
-            long long q = pf_lin(l, 0, j, k);
-            for (int i = 0; i < l->n[0]; ++i, ++q, ++c) {
-                const double* a = l->A + c * l->ne;
-                double s = 0.;
-                for (int e = 0; e < l->ne; ++e) s += a[e] * x[q + l->lo[e]];
-                r[q] = b[q] - s;
-            }
+    const long long rows = (long long) l->n[1] * l->n[2];
+#pragma omp parallel for schedule(static) num_threads(l->nt) if (l->nt > 1)
+    for (long long row = 0; row < rows; ++row) {
+        const int j = (int) (row % l->n[1]), k = (int) (row / l->n[1]);
+        size_t c = (size_t) row * l->n[0];
+        long long q = pf_lin(l, 0, j, k);
+        for (int i = 0; i < l->n[0]; ++i, ++q, ++c) {
+            const double* a = l->A + c * l->ne;
+            double s = 0.;
+            for (int e = 0; e < l->ne; ++e) s += a[e] * x[q + l->lo[e]];
+            r[q] = b[q] - s;
         }
+    }
 }
 
 /* weighted Jacobi (pfmg_relax.c / point_relax.c): x += w D^-1 (b - A x); zero guess: x = w D^-1 b */
 static void pf_relax(const PfLvl* l, double* x, const double* b, double* t, double w, int sweeps, int zero_guess) {
+    const long long rows = (long long) l->n[1] * l->n[2];
     for (int s = 0; s < sweeps; ++s) {
         if (zero_guess && s == 0) {
-            size_t c = 0;
-            for (int k = 0; k < l->n[2]; ++k)
-                for (int j = 0; j < l->n[1]; ++j) {
-                    long long q = pf_lin(l, 0, j, k);
-                    for (int i = 0; i < l->n[0]; ++i, ++q, ++c) x[q] = l->diag[c] != 0. ? w * b[q] / l->diag[c] : 0.;
-                }
+#pragma omp parallel for schedule(static) num_threads(l->nt) if (l->nt > 1)
+            for (long long row = 0; row < rows; ++row) {
+                const int j = (int) (row % l->n[1]), k = (int) (row / l->n[1]);
+                size_t c = (size_t) row * l->n[0];
+                long long q = pf_lin(l, 0, j, k);
+                for (int i = 0; i < l->n[0]; ++i, ++q, ++c) x[q] = l->diag[c] != 0. ? w * b[q] / l->diag[c] : 0.;
+            }
             continue;
         }
         pf_residual(l, x, b, t);
-        size_t c = 0;
-        for (int k = 0; k < l->n[2]; ++k)
-            for (int j = 0; j < l->n[1]; ++j) {
-                long long q = pf_lin(l, 0, j, k);
-                for (int i = 0; i < l->n[0]; ++i, ++q, ++c)
-                    if (l->diag[c] != 0.) x[q] += w * t[q] / l->diag[c];
-            }
+#pragma omp parallel for schedule(static) num_threads(l->nt) if (l->nt > 1)
+        for (long long row = 0; row < rows; ++row) {
+            const int j = (int) (row % l->n[1]), k = (int) (row / l->n[1]);
+            size_t c = (size_t) row * l->n[0];
+            long long q = pf_lin(l, 0, j, k);
+            for (int i = 0; i < l->n[0]; ++i, ++q, ++c)
+                if (l->diag[c] != 0.) x[q] += w * t[q] / l->diag[c];
+        }
     }
 }
 
@@ -1311,8 +1320,9 @@ static void pf_interp_weights(PfLvl* l, int cdir) {
     dn[cdir] = -1;
     up[cdir] = 1;
     const int s0 = pf_find(l, dn[0], dn[1], dn[2]), s1 = pf_find(l, up[0], up[1], up[2]);
-    const size_t N = (size_t) l->n[0] * l->n[1] * l->n[2];
-    for (size_t c = 0; c < N; ++c) {
+    const long long N = (long long) l->n[0] * l->n[1] * l->n[2];
+#pragma omp parallel for schedule(static) num_threads(l->nt) if (l->nt > 1)
+    for (long long c = 0; c < N; ++c) {
         const double* a = l->A + c * l->ne;
         double center = 0., w0 = 0., w1 = 0.;
         for (int e = 0; e < l->ne; ++e) {
@@ -1372,10 +1382,11 @@ static int pf_rap(const PfLvl* f, PfLvl* c, int cdir, int D) {
     const size_t Nc = (size_t) c->n[0] * c->n[1] * c->n[2];
     c->A = (double*) calloc(Nc * c->ne, sizeof(double));
     if (!c->A) return 1;
-    int I[3];
-    for (I[2] = 0; I[2] < c->n[2]; ++I[2])
-        for (I[1] = 0; I[1] < c->n[1]; ++I[1])
-            for (I[0] = 0; I[0] < c->n[0]; ++I[0]) {
+    const long long crows = (long long) c->n[1] * c->n[2];
+#pragma omp parallel for schedule(static) num_threads(f->nt) if (f->nt > 1)
+    for (long long row = 0; row < crows; ++row)
+        for (int i0 = 0; i0 < c->n[0]; ++i0) {
+                const int I[3] = {i0, (int) (row % c->n[1]), (int) (row / c->n[1])};
                 double* ac = c->A + pf_cell(c, I[0], I[1], I[2]) * c->ne;
                 for (int a = -1; a <= 1; ++a) {
                     int f1[3] = {I[0], I[1], I[2]};
@@ -1489,9 +1500,10 @@ static int pf_dxyz(const PfLvl* l, int D, double* dxyz) {
     return flag;
 }
 
-static int pf_setup(Pfmg* P, int D, const int* dims, int ne, const int* off, const double* coef) {
+static int pf_setup(Pfmg* P, int D, const int* dims, int ne, const int* off, const double* coef, int nt) {
     memset(P, 0, sizeof *P);
     P->D = D;
+    for (int l = 0; l < 64; ++l) P->L[l].nt = nt;
     PfLvl* l0 = &P->L[0];
     pf_geom(l0, D, dims);
     l0->ne = ne;
@@ -1563,10 +1575,11 @@ static int pf_setup(Pfmg* P, int D, const int* dims, int ne, const int* off, con
 
 /* semi_restrict.c: b_c(I) = r(2I) + p0(2I+1) r(2I+1) + p1(2I-1) r(2I-1) along cdir */
 static void pf_restrict(const PfLvl* f, PfLvl* c, int cdir) {
-    int I[3];
-    for (I[2] = 0; I[2] < c->n[2]; ++I[2])
-        for (I[1] = 0; I[1] < c->n[1]; ++I[1])
-            for (I[0] = 0; I[0] < c->n[0]; ++I[0]) {
+    const long long crows = (long long) c->n[1] * c->n[2];
+#pragma omp parallel for schedule(static) num_threads(f->nt) if (f->nt > 1)
+    for (long long row = 0; row < crows; ++row)
+        for (int i0 = 0; i0 < c->n[0]; ++i0) {
+                const int I[3] = {i0, (int) (row % c->n[1]), (int) (row / c->n[1])};
                 int F[3] = {I[0], I[1], I[2]};
                 F[cdir] = 2 * I[cdir];
                 double s = f->r[pf_lin(f, F[0], F[1], F[2])];
@@ -1586,10 +1599,11 @@ static void pf_restrict(const PfLvl* f, PfLvl* c, int cdir) {
 
 /* semi_interp.c + the correction: x(2I) += x_c(I); x(2I+1) += p0 x_c(I) + p1 x_c(I+1) */
 static void pf_interp_add(PfLvl* f, const PfLvl* c, int cdir) {
-    int F[3];
-    for (F[2] = 0; F[2] < f->n[2]; ++F[2])
-        for (F[1] = 0; F[1] < f->n[1]; ++F[1])
-            for (F[0] = 0; F[0] < f->n[0]; ++F[0]) {
+    const long long frows = (long long) f->n[1] * f->n[2];
+#pragma omp parallel for schedule(static) num_threads(f->nt) if (f->nt > 1)
+    for (long long row = 0; row < frows; ++row)
+        for (int i0 = 0; i0 < f->n[0]; ++i0) {
+                const int F[3] = {i0, (int) (row % f->n[1]), (int) (row / f->n[1])};
                 int I[3] = {F[0], F[1], F[2]};
                 const int t = F[cdir];
                 double e;
@@ -1611,11 +1625,13 @@ static void pf_interp_add(PfLvl* f, const PfLvl* c, int cdir) {
 
 static double pf_dot(const PfLvl* l, const double* u, const double* v) {
     double s = 0.;
-    for (int k = 0; k < l->n[2]; ++k)
-        for (int j = 0; j < l->n[1]; ++j) {
-            long long q = pf_lin(l, 0, j, k);
-            for (int i = 0; i < l->n[0]; ++i, ++q) s += u[q] * v[q];
-        }
+    const long long rows = (long long) l->n[1] * l->n[2];
+#pragma omp parallel for schedule(static) reduction(+ : s) num_threads(l->nt) if (l->nt > 1)
+    for (long long row = 0; row < rows; ++row) {
+        const int j = (int) (row % l->n[1]), k = (int) (row / l->n[1]);
+        long long q = pf_lin(l, 0, j, k);
+        for (int i = 0; i < l->n[0]; ++i, ++q) s += u[q] * v[q];
+    }
     return s;
 }
 
@@ -1683,10 +1699,11 @@ static void pf_precond(Pfmg* P, const double* r, double* z, int cycles, double* 
 }
 
 int or_pfmg_pcg(int D, const int* dims_in, int ne, const int* off, const double* coef, const double* rhs, double* x_out, double tol,
-                int maxit, int precond_cycles, int* iters, double* relres, int* levels) {
+                int maxit, int precond_cycles, int threads, int* iters, double* relres, int* levels) {
     Pfmg* P = (Pfmg*) calloc(1, sizeof(Pfmg));
     if (!P) return OPFLOW_E_NOMEM;
-    int rc = pf_setup(P, D, dims_in, ne, off, coef);
+    const int nt = threads > 0 ? threads : 1;
+    int rc = pf_setup(P, D, dims_in, ne, off, coef, nt);
     if (rc) {
         pf_free(P);
         free(P);
@@ -1719,6 +1736,7 @@ int or_pfmg_pcg(int D, const int* dims_in, int ne, const int* off, const double*
             ++it;
             pf_matvec(L0, p, s);
             const double alpha = gamma / pf_dot(L0, s, p);
+#pragma omp parallel for schedule(static) num_threads(nt) if (nt > 1)
             for (size_t q = 0; q < G; ++q) {
                 x[q] += alpha * p[q];
                 r[q] -= alpha * s[q];
@@ -1729,6 +1747,7 @@ int or_pfmg_pcg(int D, const int* dims_in, int ne, const int* off, const double*
             const double ip = pf_dot(L0, r, r);
             if (ip / bi < eps) break;
             const double beta = gamma / gold;
+#pragma omp parallel for schedule(static) num_threads(nt) if (nt > 1)
             for (size_t q = 0; q < G; ++q) p[q] = s[q] + beta * p[q];
         }
     }

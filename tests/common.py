@@ -115,11 +115,11 @@ def seeded_interior(hf, seed, n_line):
         raise NotImplementedError
 
 
-def problem_residual(p, f, x):
-    """||b - A x||_2 / ||b||_2 of a problem-form system (api.Problem: alpha*u - beta*Lap(u) = f, the
-    equation `alpha*e - beta*(d2x(e) + d2y(e) [+ d2z(e)]) == f` on its own mesh) assembled by the
-    oracle, with f and x over the unknowns (x fastest).  A pure Neumann Poisson problem is the singular
-    consistent system (no pinned row), so a solution shifted by a constant has the same residual."""
+def problem_system(p, f, pin=False):
+    """The oracle's assembly of a problem-form system (api.Problem: alpha*u - beta*Lap(u) = f, the
+    equation `alpha*e - beta*(d2x(e) + d2y(e) [+ d2z(e)]) == f` on its own mesh) with f over the
+    unknowns (x fastest): (dims, offsets, coef, rhs).  pin: the reference's pinned form (pinValue) of
+    a singular system."""
     nd = len(p.n)
     nodes_per_dim = [n + 1 if p.loc == capi.CENTER else n for n in p.n]
     mesh = mesh_uniform(nodes_per_dim, [(0.0, p.h[d] * (nodes_per_dim[d] - 1)) for d in range(nd)])
@@ -135,7 +135,14 @@ def problem_residual(p, f, x):
         lap = lap + api.d2z(L[0])
     eq = api.Eq(float(p.alpha) * L[0] - float(p.beta) * lap, L[1])
     nodes, _ = api.serialize(eq.residual_expr(), L)
-    off, coef, rhs = orc.assemble(u, nodes, [u, F], 0, 0)
-    dims = [r[1] - r[0] for r in rng]
-    r, bn = orc.residual(dims, [0] * nd, off, coef, rhs, np.asarray(x, dtype=np.float64).reshape(-1))
+    off, coef, rhs = orc.assemble(u, nodes, [u, F], 0, int(pin))
+    return [r[1] - r[0] for r in rng], off, coef, rhs
+
+
+def problem_residual(p, f, x):
+    """||b - A x||_2 / ||b||_2 of a problem-form system (see problem_system) assembled by the oracle,
+    with f and x over the unknowns (x fastest).  A pure Neumann Poisson problem is the singular
+    consistent system (no pinned row), so a solution shifted by a constant has the same residual."""
+    dims, off, coef, rhs = problem_system(p, f)
+    r, bn = orc.residual(dims, [0] * len(dims), off, coef, rhs, np.asarray(x, dtype=np.float64).reshape(-1))
     return r / bn if bn > 0 else r

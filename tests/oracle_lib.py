@@ -165,11 +165,11 @@ def u01(seed, k):
     return (z >> np.uint64(11)).astype(np.float64) * 2.0 ** -53
 
 
-def pfmg_pcg(dims, offsets, coef, rhs, tol=1e-10, maxit=200, cycles=1):
+def pfmg_pcg(dims, offsets, coef, rhs, tol=1e-10, maxit=200, cycles=1, threads=1):
     """or_pfmg_pcg: the restated HYPRE PCG + PFMG solve of an assembled system (x0 = 0, two-norm test).
-    cycles: PFMG V-cycles per preconditioner application (0: PFMG's defaults).  Returns
-    (x, iterations, final relative residual, levels).  Single-threaded and reentrant: independent
-    solves may run on several host threads at once (ctypes releases the GIL)."""
+    cycles: PFMG V-cycles per preconditioner application (0: PFMG's defaults); threads: host threads
+    sharing each loop.  Returns (x, iterations, final relative residual, levels).  Reentrant:
+    independent solves may also run on several host threads at once (ctypes releases the GIL)."""
     D = len(dims)
     d3 = (C.c_int * 3)(*(list(dims) + [1] * (3 - D)))
     off = np.ascontiguousarray(offsets, dtype=np.int32).reshape(-1)
@@ -178,5 +178,5 @@ def pfmg_pcg(dims, offsets, coef, rhs, tol=1e-10, maxit=200, cycles=1):
     x = np.zeros(rhs.size)
     it, rr, nl = C.c_int(0), C.c_double(0), C.c_int(0)
     _chk(lib().or_pfmg_pcg(D, d3, offsets.shape[0], off.ctypes.data_as(C.POINTER(C.c_int)), dptr(coef), dptr(rhs), dptr(x),
-                           C.c_double(tol), maxit, cycles, C.byref(it), C.byref(rr), C.byref(nl)))
+                           C.c_double(tol), maxit, cycles, threads, C.byref(it), C.byref(rr), C.byref(nl)))
     return x, it.value, rr.value, nl.value
