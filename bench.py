@@ -185,12 +185,20 @@ def cpu_ftcs_sample(workload, threads, reps):
     return pts / dt / 1e9, "%s: %d^%d nodes x %d steps on %d host threads (oracle port, %.1f s)" % (workload, n, D, reps, used, dt), used
 
 
+def served_population(reqs):
+    """Every linear system a served window solves: a one-shot request once, a session once per step
+    (each step re-solves the session's operator with a new right-hand side)."""
+    out = []
+    for p, f, steps in reqs:
+        out.extend([(p, f, steps)] * steps)
+    return out
+
+
 def reference_requests(args):
     """The systems of the workload in problem form, as (problem, f, steps), without a GPU."""
     from opflow_gb300 import api
-    import numpy as np
     if args.workload == "serve":
-        return wl.serve_mix(api, 77, args.requests)
+        return served_population(wl.serve_mix(api, 77, args.requests))
     if args.workload == "batched":
         return [(p, f, 1) for p, f in wl.batched_problems(api, 99, args.problems)]
     if args.workload == "poisson2d":
@@ -205,7 +213,7 @@ def run_reference_solves(args, threads):
     workload's window, picked by systematic sampling over the window sorted by size (so --steps K
     systems cover its size distribution), with the restated HYPRE PCG + PFMG on all host threads,
     assembly and set-up included as in HYPREEqnSolveHandler::solve.  value = systems / total seconds."""
-    reqs = reference_requests(args)
+    reqs = reference_requests(args)  # the served window's systems, session steps included
     # warm-up: the smallest systems (page in the oracle, the thread pool)
     small = sorted(reqs, key=lambda r: int(np.prod(r[0].n)))[:max(1, args.warmup)]
     cpu_pfmg_sample(small, len(small), threads)
@@ -310,9 +318,9 @@ def cpu_pfmg_sample(reqs, nsample, threads, order_key=None):
             raise RuntimeError("restated PCG+PFMG did not reach 1e-10 on system %d (%g)" % (i, rel))
         secs.append((t2 - t0) if steps == 1 else (t2 - t1))
         its.append(it)
-    desc = ("restated HYPRE PCG+PFMG(1 V-cycle), tol 1e-10 two-norm, incl. assembly + setup per one-shot solve; %d systems "
-            "sampled by size from the window (%s unknowns), %d host threads" %
-            (nsample, ",".join(str(int(np.prod(reqs[i][0].n))) for i in idx), used))
+    desc = ("restated HYPRE PCG+PFMG(1 V-cycle), tol 1e-10 two-norm, incl. assembly + setup per one-shot solve (setup + solve per "
+            "session step); %d of the window's %d systems sampled by size (%s unknowns), %d host threads" %
+            (nsample, len(reqs), ",".join(str(int(np.prod(reqs[i][0].n))) for i in idx), used))
     return nsample / sum(secs), secs, its, used, desc
 
 
@@ -512,223 +520,144 @@ def run_poisson3d(args, torch, api, capi, np, ctx, stream, world, rank, local):
 
 def run_serve(args, torch, api, capi, np, ctx, stream, world, rank, local):
     """The serving configuration.  One unit throughout is a linear system solved to 1e-10: a one-shot
-    request, or one backward-Euler step of a session.
+    request or one backward-Euler step of a session.  A window of --requests requests (Poisson
+    arrivals) is served by the request server (continuous batching, mixed precision):
 
-    value: device-resident throughput of the window's systems (every one-shot request and one step of
-           every session, inputs already in HBM), one batched mixed-precision solve per step, median
-           over the timed steps (CUDA events on the launching stream);
-    e2e:   the request server (continuous batching, mixed precision) at the highest swept arrival rate,
-           host right-hand sides in and host solutions out, every session step counted;
-    next to plain FP64 serving one request at a time on the same stream of requests."""
+    value: the window served with right-hand sides and result buffers already in HBM (device tensors),
+           at the highest swept arrival rate; the window is one continuous run, timed as --steps
+           consecutive steps (step k ends when the k-th group of requests, in submission order, has
+           its results: CUDA events on the caller's stream), value = systems / total time;
+    e2e:   the same window and rate with host right-hand sides in and host solutions out (pinned);
+    next to plain FP64 serving one request at a time on the same window (host buffers)."""
     count = args.requests
     rates = [float(r) for r in str(args.rate).split(",")]
     params = api.StructSolverParams(tol=1e-10, maxIter=200, precision="mixed", zeroGuess=True)
     reqs = wl.serve_mix(api, 77 + rank, count)
     total_systems = sum(s for _, _, s in reqs)
+    peak, src = peak_hbm()
 
-    # (1) device-resident batched solve of the window's systems
+    # the window's distinct systems (one per request) in one batched solve, inputs resident: the kernel
+    # time of the solver itself, against the roofline
     B = api.Batch([p for p, _, _ in reqs], params, ctx)
     for i, (_, f, _) in enumerate(reqs):
         B.set(i, f)
-    for _ in range(args.warmup):
-        B.solve()
+    B.solve()
     torch.cuda.synchronize()
-    l0 = capi.launch_count()
-    ms_steps, iters = [], None
-    for _ in range(args.steps):
+    bms = []
+    for _ in range(max(1, min(args.steps, 3))):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         st = B.solve()
         e1.record(stream)
         torch.cuda.synchronize()
-        ms_steps.append(e0.elapsed_time(e1))
-        iters = [s.niter for s in st]
-        assert all(s.converged for s in st)
-    launches = capi.launch_count() - l0
-    worst = max(s.relerr for s in st)
+        bms.append(e0.elapsed_time(e1))
+    iters = [s_.niter for s_ in st]
+    worst = max(s_.relerr for s_ in st)
     B.close()
-    dev_ms = statistics.median(ms_steps)
-    value = len(reqs) / (dev_ms * 1e-3)
+    batch_ms = statistics.median(bms)
     alg = sum(iter_bytes_per_cell(len(p.n), "mixed") * int(np.prod(p.n)) * it for (p, _, _), it in zip(reqs, iters))
-    peak, src = peak_hbm()
-    achieved = alg / (dev_ms * 1e-3) / 1e9
+    achieved = alg / (batch_ms * 1e-3) / 1e9
 
-    # (2) the request server: pinned host buffers for the right-hand sides and the results
     def pinned(n):
         return torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
 
-    staged = []
-    for p, f, st_ in reqs:
-        buf = pinned(f.size)
-        buf[:] = f
-        staged.append((p, buf, st_))
-    outs = [pinned(f.size) for _, f, _ in staged]
+    dev = torch.device("cuda", local)
+    host_in, host_out, dev_in, dev_out = [], [], [], []
+    for _, f, _ in reqs:
+        hb = pinned(f.size)
+        hb[:] = f
+        host_in.append(hb)
+        host_out.append(pinned(f.size))
+        dev_in.append(torch.from_numpy(f).to(dev))
+        dev_out.append(torch.empty(f.size, dtype=torch.float64, device=dev))
+    torch.cuda.synchronize()
 
-    def served(prec, max_active, rq, rate, out_bufs=None):
+    def served(prec, max_active, rate, fin, fout, nsteps=1, rq=None):
+        rq = rq if rq is not None else [(p, f, s_) for (p, _, s_), f in zip(reqs, fin)]
         srv = api.Server(api.StructSolverParams(tol=1e-10, maxIter=200, precision=prec), hbm_budget=120 << 30,
                          max_active=max_active, ctx=ctx)
         rng = np.random.default_rng(5)
         gaps = rng.exponential(1.0 / rate, len(rq))
         ids = []
+        l0 = capi.launch_count()
+        torch.cuda.synchronize()
+        evs = [torch.cuda.Event(enable_timing=True)]
+        evs[0].record(stream)
         t0 = time.perf_counter()
         tnext = t0
         for k, ((p, f, steps), g) in enumerate(zip(rq, gaps)):
             tnext += g
             while time.perf_counter() < tnext:
                 time.sleep(min(0.0005, max(0.0, tnext - time.perf_counter())))
-            ids.append(srv.submit(p, f, steps=steps, out=out_bufs[k] if out_bufs is not None else np.zeros(f.size)))
-        res = [srv.result(i) for i in ids]
+            ids.append(srv.submit(p, f, steps=steps, out=fout[k] if fout is not None else np.zeros(np.size(f))))
+        res = []
+        bounds = [int(round((g + 1) * len(ids) / nsteps)) for g in range(nsteps)]
+        for k, i in enumerate(ids):
+            res.append(srv.result(i))
+            if k + 1 in bounds:
+                ev = torch.cuda.Event(enable_timing=True)
+                ev.record(stream)
+                evs.append(ev)
         wall = time.perf_counter() - t0
+        torch.cuda.synchronize()
+        launches = capi.launch_count() - l0
+        step_ms = [evs[k].elapsed_time(evs[k + 1]) for k in range(len(evs) - 1)]
         st = srv.stats()
         srv.close()
         ok = sum(1 for r in res if r["status"] == capi.OK)
         lat = sorted(r["latency_ms"] for r in res)
         q = lambda z: lat[min(len(lat) - 1, int(np.ceil(z * len(lat))) - 1)]
-        return dict(solves_per_s=sum(r["solves"] for r in res) / wall, p50_ms=q(0.5), p99_ms=q(0.99), ok=ok, n=len(res),
-                    systems=sum(r["solves"] for r in res), iterations=sum(r["iterations"] for r in res),
-                    max_active_seen=st["max_active_seen"], wall_s=wall, compositions=st["compositions"],
+        systems = sum(r["solves"] for r in res)
+        tot_ms = sum(step_ms)
+        return dict(solves_per_s=systems / (tot_ms * 1e-3), p50_ms=q(0.5), p99_ms=q(0.99), ok=ok, n=len(res), systems=systems,
+                    iterations=sum(r["iterations"] for r in res), max_active_seen=st["max_active_seen"], wall_s=wall,
+                    event_s=tot_ms * 1e-3, step_ms=step_ms, launches=launches, compositions=st["compositions"],
                     worker_s={k: round(st[k], 4) for k in ("setup_s", "compose_s", "iterate_s", "retire_s")})
 
     # warm-up (allocator pool, graphs, kernels)
-    served("mixed", 16, wl.serve_mix(api, 3, 4), 1000.0)
-    served("fp64", 1, wl.serve_mix(api, 3, 2), 1000.0)
+    for _ in range(max(1, min(args.warmup, 2))):
+        served("mixed", 16, 1000.0, None, None, rq=wl.serve_mix(api, 3, 6))
+    served("fp64", 1, 1000.0, None, None, rq=wl.serve_mix(api, 3, 2))
+    head_rate = max(rates)
+    with ClockSampler(local) as clk:
+        dres = served("mixed", 64, head_rate, dev_in, dev_out, nsteps=args.steps)
     sweep = []
     for rate in rates:
-        sweep.append(dict(rate_per_s=rate, served_mixed=served("mixed", 64, staged, rate, outs)))
-    head = sweep[-1]
-    plain = served("fp64", 1, staged, head["rate_per_s"], outs)
+        sweep.append(dict(rate_per_s=rate, served_mixed=served("mixed", 64, rate, host_in, host_out)))
+    head = [w for w in sweep if w["rate_per_s"] == head_rate][0]
+    plain = served("fp64", 1, head_rate, host_in, host_out)
     head["served_plain_fp64_one_at_a_time"] = plain
     head["served_speedup"] = head["served_mixed"]["solves_per_s"] / plain["solves_per_s"]
     head["p99_ratio_mixed_over_plain"] = head["served_mixed"]["p99_ms"] / plain["p99_ms"]
     mixed = head["served_mixed"]
-    hb = 8 * sum(f.size for _, f, _ in staged)
-    return dict(value=value, unit="solves/s", ms=dev_ms, ms_steps=ms_steps, launches=launches, dtype="f64 outer / f32 V-cycle",
+    hb = 8 * sum(f.size for _, f, _ in reqs)
+    value = dres["solves_per_s"]
+    return dict(value=value, unit="solves/s", ms=statistics.mean(dres["step_ms"]), launches=dres["launches"], clocks=clk.summary(),
+                dtype="f64 outer / f32 V-cycle",
                 config=dict(workload="serve", requests=count, rates_per_s=rates,
                             mix="70% one-shot Poisson (2D side LogU[129,2049] / 3D side LogU[64,256], Neumann/Dirichlet 50/50), "
                                 "30% heat sessions of 10-100 backward-Euler steps (2D side LogU[129,1025])",
                             unit_is="one linear system solved to ||b-Ax||/||b|| <= 1e-10 (a one-shot request or one session step)",
-                            systems_in_window=len(reqs), systems_served=total_systems, budget_gb=120, sweep=sweep,
-                            headline_rate_per_s=head["rate_per_s"], served_speedup=head["served_speedup"],
-                            p99_ratio_mixed_over_plain=head["p99_ratio_mixed_over_plain"],
+                            systems_in_window=total_systems, budget_gb=120, headline_rate_per_s=head_rate,
+                            value_is="the window served at %g req/s with device-resident f and x (one continuous run timed as %d steps "
+                                     "of consecutive request groups)" % (head_rate, args.steps),
+                            device_resident_served=dres, sweep=sweep,
+                            served_speedup=head["served_speedup"], p99_ratio_mixed_over_plain=head["p99_ratio_mixed_over_plain"],
                             device_resident_batch=dict(systems=len(reqs), unknowns=int(sum(int(np.prod(p.n)) for p, _, _ in reqs)),
-                                                       ms_median=dev_ms, ms_min=min(ms_steps), ms_max=max(ms_steps),
-                                                       iterations_min=min(iters), iterations_max=max(iters), worst_rel_residual=worst),
-                            value_is="median over the timed steps of one batched mixed-precision solve of the window's %d systems "
-                                     "(inputs resident in HBM)" % len(reqs),
-                            e2e_is="request server, mixed precision, at %g req/s: %d requests = %d systems, host f in and host x out"
-                                   % (head["rate_per_s"], count, total_systems),
+                                                       ms_median=batch_ms, ms_all=bms, iterations_min=min(iters), iterations_max=max(iters),
+                                                       worst_rel_residual=worst,
+                                                       what="one batched mixed-precision solve of the window's distinct systems (one per request)"),
+                            e2e_is="the same window served at %g req/s with pinned host f in and host x out" % head_rate,
                             l2="%.1f GB of level-0 vectors per batched solve (> L2): no flush needed" % (
                                 sum(int(np.prod(p.n)) for p, _, _ in reqs) * 48 / 1e9)),
                 roofline={"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": src,
                           "traffic": traffic_for("serve"),
-                          "kernel": "batched flexible-PCG solve of the window's systems (FP32 V-cycle + FP64 Krylov kernels, one launch each per operation)",
-                          "algorithmic_bytes_per_launch": alg,
+                          "kernel": "batched flexible-PCG solve of the window's distinct systems (FP32 V-cycle + FP64 Krylov kernels)",
+                          "algorithmic_bytes_per_launch": alg, "launch_ms": batch_ms,
                           "bytes_per_cell_iteration": {"2d": iter_bytes_per_cell(2), "3d": iter_bytes_per_cell(3)}},
                 e2e={"value": mixed["solves_per_s"], "unit": "solves/s", "h2d_bytes_per_step": hb, "d2h_bytes_per_step": hb,
-                     "p50_ms": mixed["p50_ms"], "p99_ms": mixed["p99_ms"]},
+                     "p50_ms": mixed["p50_ms"], "p99_ms": mixed["p99_ms"], "note": "bytes per window (all requests' f and x)"},
                 reqs=reqs)
-
-
-# ------------------------------------------------------------------------------------------- WENO
-def cpu_weno_sample(threads):
-    """The oracle's three WENO5 stage assignments on 4096-cell periodic lines; returns points/s per RK3 step."""
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
-    import numpy as np
-    import common as cm
-    import oracle_lib as orc
-    from opflow_gb300 import _capi as capi
-    from opflow_gb300 import api
-    used = orc.lib().or_set_threads(threads)
-    nx, ny = 4096, 256
-    mesh = cm.mesh_uniform([nx + 1, ny + 1])
-    fd = cm.field_desc(2, capi.CENTER, [(capi.BC_PERIODIC, capi.BC_PERIODIC)] * 2, ext=3)
-    h0 = orc.HostField(mesh, fd)
-    h0.data[h0.slices(h0.assignable())] = wl.weno_u0(7, nx, ny)
-    h0.update_padding()
-    h1 = orc.HostField(mesh, fd, data=h0.data.copy())
-    h2 = orc.HostField(mesh, fd, data=h0.data.copy())
-    L = [cm.Leaf("u"), cm.Leaf("u1"), cm.Leaf("u2")]
-    ns = [api.serialize(x, L)[0] for x in cm.weno_stage_exprs(L[0], L[1], L[2], 0.5 / nx)]
-    steps = 2
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        orc.assign(h1, ns[0], [h0, h1, h2])
-        orc.assign(h2, ns[1], [h0, h1, h2])
-        orc.assign(h0, ns[2], [h0, h1, h2])
-    dt = time.perf_counter() - t0
-    return nx * ny * steps / dt / 1e9, "%d x %d periodic lines, %d RK3 steps of the three stage assignments (oracle, %d threads)" % (nx, ny, steps, used), used
-
-
-def run_weno(args, torch, api, capi, np, ctx, stream, world, rank, local, dist):
-    nx = 4096
-    ny = args.grid or 65536
-    mesh = api.MeshBuilder().newMesh(nx + 1, ny + 1).setMeshOfDim(0, 0.0, 1.0).setMeshOfDim(1, 0.0, ny / nx).build()
-    b = api.ExprBuilder().setMesh(mesh).setName("u").setLoc(api.LocOnMesh.Center).setExt(3)
-    for d in range(2):
-        b.setBC(d, api.DimPos.start, api.BCType.Periodic, 0.0).setBC(d, api.DimPos.end, api.BCType.Periodic, 0.0)
-    u = b.build(ctx)
-    host = u.download()
-    host[u.index_slices(u.assignableRange)] = wl.weno_u0(2024 + rank, nx, ny)
-    u.upload(host)
-    hb = torch.from_numpy(host).pin_memory()
-    dt = 0.5 / nx
-    api.weno_rk3(u, dt, args.warmup)
-    torch.cuda.synchronize()
-    l0 = capi.launch_count()
-    if world > 1:
-        dist.barrier()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clk:
-        ev0.record(stream)
-        api.weno_rk3(u, dt, args.steps)
-        ev1.record(stream)
-        torch.cuda.synchronize()
-    ms = ev0.elapsed_time(ev1)
-    launches = capi.launch_count() - l0
-    if world > 1:
-        tt = torch.tensor([ms], device=torch.device("cuda", local))
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
-    pts = nx * ny
-    value = pts * args.steps * world / (ms * 1e-3) / 1e9
-    ms_step = ms / args.steps
-    # end to end: host field in, one RK3 step, host field out
-    P = C.POINTER(C.c_double)
-    L = capi.lib()
-    cnt = hb.numel()
-    e2e_steps = 2
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        capi.check(L.opflow_field_upload(u.handle, C.cast(hb.data_ptr(), P), cnt))
-        api.weno_rk3(u, dt, 1)
-        capi.check(L.opflow_field_download(u.handle, C.cast(hb.data_ptr(), P), cnt))
-    e2e_s = time.perf_counter() - t0
-    peak, src = peak_hbm()
-    alg = 16.0 * pts
-    cpu = None
-    if rank == 0 and not args.no_cpu_baseline:
-        try:
-            v, sample, used = cpu_weno_sample(os.cpu_count() or 1)
-            cpu = {"value": v, "unit": "Gpts/s", "cores": used, "kind": "port", "sample": sample}
-        except Exception as ex:
-            cpu = {"value": None, "unit": "Gpts/s", "cores": 0, "kind": "port", "sample": "failed: %s" % ex}
-    line = {"metric": METRIC, "value": value, "unit": "Gpts/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "weno", "lines": ny, "line_cells": nx, "scheme": "WENO5-JS (D1WENO53Downwind<0>) + Shu-Osher RK3, fused",
-                       "cfl": 0.5, "bc": "periodic", "init": "seeded square + cosine pulses per line", "unit": "cell updates per RK3 step",
-                       "l2": "field %.1f GB > L2" % (pts * 8 / 1e9), "parallelism": "replicas" if world > 1 else "single"},
-            "roofline": {"bound": "fp64", "achieved": alg / (ms_step * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
-                         "frac": alg / (ms_step * 1e-3) / 1e9 / peak, "peak_source": src, "traffic": traffic_for("weno"),
-                         "kernel": "weno_rk3_kernel", "algorithmic_bytes_per_launch": alg},
-            "cpu_baseline": cpu,
-            "e2e": {"value": pts * e2e_steps / e2e_s / 1e9, "unit": "Gpts/s", "h2d_bytes_per_step": cnt * 8, "d2h_bytes_per_step": cnt * 8},
-            "gpu_launches": launches, "clocks": clk.summary()}
-    if rank == 0:
-        print(json.dumps(line), flush=True)
-    if world > 1:
-        dist.destroy_process_group()
-    return 0
 
 
 def explicit_record(torch, api, capi, np, ctx, stream, local, rank, steps=20, warmup=3):
@@ -918,8 +847,8 @@ def run_ours(args):
         cpu = None
         if rank == 0 and not args.no_cpu_baseline and args.workload != "poisson3d":
             try:
-                v, secs, its, used, desc = cpu_pfmg_sample(r.get("reqs") or reference_requests(args), 6 if args.workload == "serve" else 2,
-                                                           os.cpu_count() or 1)
+                pop = served_population(r["reqs"]) if r.get("reqs") else reference_requests(args)
+                v, secs, its, used, desc = cpu_pfmg_sample(pop, 8 if args.workload == "serve" else 2, os.cpu_count() or 1)
                 cpu = {"value": v, "unit": "solves/s", "cores": used, "kind": "port", "sample": desc}
             except Exception as ex:
                 cpu = {"value": None, "unit": "solves/s", "cores": 0, "kind": "port", "sample": "failed: %s" % ex}
@@ -929,7 +858,8 @@ def run_ours(args):
         line = {"metric": METRIC, "value": value, "unit": r["unit"], "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
                 "ms_per_step": r["ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": r["dtype"],
                 "data": "synthetic", "config": dict(r["config"], parallelism="replicas" if world > 1 else "single"),
-                "roofline": r["roofline"], "cpu_baseline": cpu, "e2e": r["e2e"], "gpu_launches": r["launches"], "clocks": clk.summary()}
+                "roofline": r["roofline"], "cpu_baseline": cpu, "e2e": r["e2e"], "gpu_launches": r["launches"],
+                "clocks": r.get("clocks") or clk.summary()}
         if rank == 0:
             print(json.dumps(line), flush=True)
         if world > 1:

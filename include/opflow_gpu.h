@@ -390,12 +390,15 @@ typedef struct {
     opflow_problem_desc problem; /* alpha*u - beta*Lap(u) = f                                          */
     int steps;                   /* 1: one solve; k > 1: a session of k solves, each taking the previous
                                     solution as its right-hand side (backward-Euler heat steps)        */
-    const double* f;             /* host right-hand side / initial state, n unknowns: read when the request
-                                    is admitted, so it must stay valid and unchanged until the request's
-                                    result is available (pinned host memory gives the fastest copy)      */
-    double* x_out;               /* host buffer for the final solution, n unknowns (may be NULL)        */
-    const double* x0;            /* host initial guess of the first solve, n unknowns (NULL: zero); a
-                                    session restored from a checkpoint passes the checkpoint here and as f */
+    const double* f;             /* right-hand side / initial state, n unknowns, in host or device memory
+                                    (unified addressing): read when the request is admitted, so it must
+                                    stay valid and unchanged until the request's result is available
+                                    (pinned host memory gives the fastest host copy).  Non-finite values
+                                    are refused with OPFLOW_E_NAN: by submit for host memory, as the
+                                    request's result status for device memory (checked at admission)   */
+    double* x_out;               /* buffer for the final solution, n unknowns, host or device (may be NULL) */
+    const double* x0;            /* initial guess of the first solve, n unknowns, host or device (NULL: zero);
+                                    a session restored from a checkpoint passes the checkpoint here and as f */
 } opflow_request;
 
 typedef struct {

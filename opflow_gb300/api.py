@@ -1050,19 +1050,32 @@ class Server:
         self.handle = h
         self._keep = {}
 
+    @staticmethod
+    def _ptr(a):
+        """Address of a float64 buffer: a numpy array (host) or any object with a CUDA device pointer
+        (a contiguous float64 torch tensor on the GPU: device-resident requests)."""
+        if hasattr(a, "data_ptr") and getattr(a, "is_cuda", False):
+            assert a.is_contiguous() and str(a.dtype) == "torch.float64"
+            return a, C.cast(C.c_void_p(a.data_ptr()), C.POINTER(C.c_double))
+        a = np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
+        return a, a.ctypes.data_as(C.POINTER(C.c_double))
+
     def submit(self, problem, f, steps=1, out=None, x0=None):
-        """Queues a request; x0 is the first solve's initial guess (a restored session's checkpoint)."""
-        f = np.ascontiguousarray(f, dtype=np.float64).reshape(-1)
+        """Queues a request; x0 is the first solve's initial guess (a restored session's checkpoint).
+        f, out and x0 are host arrays or device tensors (the library copies with unified addressing)."""
+        f, fp = self._ptr(f)
         req = capi.Request()
         req.problem = problem.to_c()
         req.steps = int(steps)
-        req.f = f.ctypes.data_as(C.POINTER(C.c_double))
+        req.f = fp
         if x0 is not None:
-            x0 = np.ascontiguousarray(x0, dtype=np.float64).reshape(-1)
-            req.x0 = x0.ctypes.data_as(C.POINTER(C.c_double))
+            x0, req.x0 = self._ptr(x0)
         if out is not None:
-            assert out.dtype == np.float64 and out.flags["C_CONTIGUOUS"]
-            req.x_out = out.ctypes.data_as(C.POINTER(C.c_double))
+            if hasattr(out, "data_ptr") and getattr(out, "is_cuda", False):
+                out, req.x_out = self._ptr(out)
+            else:
+                assert out.dtype == np.float64 and out.flags["C_CONTIGUOUS"]
+                req.x_out = out.ctypes.data_as(C.POINTER(C.c_double))
         rid = C.c_longlong(0)
         check(lib().opflow_server_submit(self.handle, C.byref(req), C.byref(rid)))
         self._keep[rid.value] = (f, out, x0)

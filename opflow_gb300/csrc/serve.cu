@@ -36,6 +36,7 @@ struct Req {
     opflow_problem_desc pd{};
     int steps = 1;
     const double* f = nullptr;  // the caller's right-hand side, read at admission
+    bool f_dev = false;         // f is device memory: checked for non-finite values on the device at admission
     const double* x0 = nullptr;  // the caller's initial guess (or null), read at admission
     long long nf = 0;
     double* x_out = nullptr;
@@ -104,6 +105,12 @@ static void release_req(Req* r) {
     if (r->rhs) { opflow_field_destroy(r->rhs); r->rhs = nullptr; }
 }
 
+// flag = 1 when any of the n values is not finite (every offending thread writes the same 1)
+__global__ void flag_nonfinite(const double* __restrict__ v, long long n, int* flag) {
+    for (long long i = (long long) blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x)
+        if (!isfinite(v[i])) *flag = 1;
+}
+
 // hierarchy, right-hand side, pinning, and the seed of the Krylov scalars
 static int setup_req(opflow_server S, Req* r, Scal* seed) {
     opflow_ctx ctx = &S->setup_ctx;
@@ -128,8 +135,21 @@ static int setup_req(opflow_server S, Req* r, Scal* seed) {
     OPG_TRY(mg_finalize(M));
     r->N = M->probs[0].levels[0].N;
     if (r->nf != r->N) return fail(OPFLOW_E_INVALID, "request %lld: f has %lld values, the problem %lld unknowns", r->id, r->nf, r->N);
-    OPG_CUDA(cudaMemcpyAsync(M->probs[0].b, r->f, r->N * 8, cudaMemcpyHostToDevice, ctx->stream));
-    if (r->x0) OPG_CUDA(cudaMemcpyAsync(M->kd_host[0].x, r->x0, r->N * 8, cudaMemcpyHostToDevice, ctx->stream));
+    // f, x0: host or device memory (unified addressing picks the direction)
+    OPG_CUDA(cudaMemcpyAsync(M->probs[0].b, r->f, r->N * 8, cudaMemcpyDefault, ctx->stream));
+    if (r->x0) OPG_CUDA(cudaMemcpyAsync(M->kd_host[0].x, r->x0, r->N * 8, cudaMemcpyDefault, ctx->stream));
+    if (r->f_dev) {
+        // a host f was checked at submission; a device f is checked here, before the request joins a batch
+        int* flag = (int*) ctx->scratch;
+        int h_flag = 0;
+        OPG_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), ctx->stream));
+        const long long blk = std::min<long long>((r->N + 255) / 256, (long long) std::max(1, ctx->num_sms) * 8);
+        flag_nonfinite<<<(int) std::max<long long>(1, blk), 256, 0, ctx->stream>>>(M->probs[0].b, r->N, flag);
+        OPG_LAUNCHED();
+        OPG_CUDA(cudaMemcpyAsync(&h_flag, flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        OPG_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (h_flag) return fail(OPFLOW_E_NAN, "request %lld: non-finite value in the (device) right-hand side", r->id);
+    }
     ProblemHost& P = M->probs[0];
     r->pinned = P.singular && !P.has_dirichlet;
     if (r->pinned) {
@@ -164,7 +184,7 @@ static void finish_enqueue(opflow_server S, Req* r, double* slot) {
         shift_by_first<<<(int) std::max(1LL, blocks), 256, 0, ctx->stream>>>(K.x, r->N, slot);
         OPG_LAUNCHED();
     }
-    if (r->x_out) cudaMemcpyAsync(r->x_out, K.x, r->N * 8, cudaMemcpyDeviceToHost, ctx->stream);
+    if (r->x_out) cudaMemcpyAsync(r->x_out, K.x, r->N * 8, cudaMemcpyDefault, ctx->stream);  // host or device buffer
 }
 
 static void finish_mark(opflow_server S, Req* r, int status) {
@@ -445,9 +465,15 @@ int opflow_server_submit(opflow_server S, const opflow_request* q, long long* id
         const int unk = pd.loc == OPFLOW_CENTER ? pd.n[d] : (pd.bc == OPFLOW_BC_DIRC ? pd.n[d] - 2 : pd.n[d]);
         n *= unk;
     }
-    for (long long i = 0; i < n; ++i)
-        if (!std::isfinite(q->f[i])) return fail(OPFLOW_E_NAN, "non-finite value in the right-hand side at %lld", i);
+    // f in device memory is checked on the device at admission; host (or managed) memory here
+    cudaPointerAttributes pa{};
+    const bool f_dev = cudaPointerGetAttributes(&pa, q->f) == cudaSuccess && pa.type == cudaMemoryTypeDevice;
+    cudaGetLastError();  // an unregistered host pointer is not an error for this query
+    if (!f_dev)
+        for (long long i = 0; i < n; ++i)
+            if (!std::isfinite(q->f[i])) return fail(OPFLOW_E_NAN, "non-finite value in the right-hand side at %lld", i);
     auto* r = new Req();
+    r->f_dev = f_dev;
     r->pd = pd;
     r->steps = q->steps;
     r->f = q->f;

@@ -193,3 +193,29 @@ def test_checkpoint_refusals(ctx):
         s.checkpoint(rid, 64 * 64)
     assert "finished" in str(e.value)
     s.close()
+
+
+def test_device_resident_requests_equal_host_requests(ctx):
+    """Right-hand sides and result buffers in device memory (unified addressing) give the host
+    requests' results bit for bit; a non-finite device right-hand side finishes with OPFLOW_E_NAN."""
+    torch = pytest.importorskip("torch")
+    reqs = mix(5)
+    params = api.StructSolverParams(tol=1e-10, maxIter=100, precision="mixed")
+    s = api.Server(params, max_active=8, ctx=ctx)
+    outs_h, res_h = run(s, reqs)
+    dev = torch.device("cuda", 0)
+    fd = [torch.from_numpy(f.copy()).to(dev) for _, f, _ in reqs]
+    od = [torch.zeros(f.size, dtype=torch.float64, device=dev) for _, f, _ in reqs]
+    torch.cuda.synchronize()
+    ids = [s.submit(p, fd[k], steps=steps, out=od[k]) for k, (p, f, steps) in enumerate(reqs)]
+    res_d = [s.result(i) for i in ids]
+    bad = fd[0].clone()
+    bad[7] = float("nan")
+    torch.cuda.synchronize()
+    rb = s.result(s.submit(reqs[0][0], bad, steps=1))
+    s.close()
+    assert all(r["status"] == capi.OK for r in res_d), res_d
+    for k in range(len(reqs)):
+        assert res_d[k]["iterations"] == res_h[k]["iterations"], k
+        assert np.array_equal(od[k].cpu().numpy(), outs_h[k]), k
+    assert rb["status"] == capi.E_NAN
