@@ -98,7 +98,8 @@ def test_noalloc_3d_periodic_and_long_rows_twice(ctx):
     longer than one chunk (1280 cells: two chunks per row, the second starting at i0 = 1024)."""
     torch = pytest.importorskip("torch")
     n0, n1, n2 = 1280, 8, 8
-    mesh = cm.mesh_uniform([n0 + 1, n1 + 1, n2 + 1])
+    # equal spacing in every dimension (an isotropic operator, which the multigrid solver converges on)
+    mesh = cm.mesh_uniform([n0 + 1, n1 + 1, n2 + 1], [(0.0, n0 / 64.0), (0.0, n1 / 64.0), (0.0, n2 / 64.0)])
     fd = cm.field_desc(3, capi.CENTER, [(capi.BC_DIRC, capi.BC_DIRC), (capi.BC_DIRC, capi.BC_DIRC), (capi.BC_PERIODIC, capi.BC_PERIODIC)], ext=1)
     p, f = api.CartesianField(mesh, fd, ctx), api.CartesianField(mesh, fd, ctx)
     a = f.download()
