@@ -1072,6 +1072,28 @@ static void free_plan(Plan* p) {
     p->dprog = nullptr;
 }
 
+// A run of fixed-point steps can keep the field in fixed point between its steps when the update reads
+// only the destination (u = u + sum_d w_d (u(i-e_d) + u(i+e_d) - 2u), 3D), the values outside the
+// update box are constants (node-centred Dirichlet on every side, no ghost layer: updatePadding rewrites
+// only those constants) and the weights obey the maximum principle (w_d >= 0, 1 - 2 sum w_d >= 0), so
+// that the initial bound on |u| holds for every step.  OPFLOW_FX_RESIDENT=0 turns it off.
+static bool resident_eligible(const Plan& plan, opflow_field dst, const opflow_field* leaves, int steps) {
+    if (plan.kind != PLAN_AXIS_FAST || !plan.aliased || steps < 2 || plan.axis.ndim != 3) return false;
+    if (leaves[plan.src_slot] != dst || !dst->padding_is_step0_only()) return false;
+    const char* e = getenv("OPFLOW_FX_RESIDENT");
+    if (e && e[0] == '0') return false;
+    for (int d = 0; d < 3; ++d)
+        for (int sd = 0; sd < 2; ++sd)
+            if (dst->desc.loc[d] != OPFLOW_CORNER || dst->desc.bc_type[d][sd] != OPFLOW_BC_DIRC) return false;
+    double sum = 0.;
+    for (int d = 0; d < 3; ++d) {
+        const int g = plan.axis.iso ? 0 : d;
+        if (plan.axis.wneg[g]) return false;
+        sum += std::ldexp((double) plan.axis.wm[g], -plan.axis.wshift[g]);
+    }
+    return 1.0 - 2.0 * sum >= 0.0;
+}
+
 // One assignment step: evaluates into the back buffer when the expression reads dst (out-of-place, as
 // FieldAssigner does through its temporary copy), otherwise into dst directly; then the padding.
 static int run_plan(opflow_ctx ctx, opflow_field dst, int arith, const opflow_field* leaves, Plan* plan, unsigned long long* maxslots, int step) {
@@ -1147,7 +1169,18 @@ int opflow_assign_repeat(opflow_ctx ctx, opflow_field dst, int arith, const opfl
         rc = check_launch("maxabs_kernel");
         if (rc) { free_plan(&plan); return rc; }
     }
-    for (int s = 0; s < steps && rc == OPFLOW_OK; ++s) rc = run_plan(ctx, dst, arith, leaves, &plan, maxslots, s);
+    if (resident_eligible(plan, dst, leaves, steps)) {
+        // fixed point kept in the field's buffers between the steps of the run (axis3d_fxres_kernel)
+        OPG_TRY(ensure_back(dst));
+        for (int s = 0; s < steps && rc == OPFLOW_OK; ++s) {
+            rc = axis_launch_resident(ctx, dst->view(), dst->view_back(), plan.box, plan.axis, maxslots, s == 0, s == steps - 1);
+            dst->cur = 1 - dst->cur;
+            dst->version++;
+            if (rc == OPFLOW_OK) rc = update_padding_assign(dst);
+        }
+    } else {
+        for (int s = 0; s < steps && rc == OPFLOW_OK; ++s) rc = run_plan(ctx, dst, arith, leaves, &plan, maxslots, s);
+    }
     if (rc == OPFLOW_OK && cudaStreamSynchronize(ctx->stream) != cudaSuccess) rc = fail(OPFLOW_E_CUDA, "assign failed: %s", cudaGetErrorString(cudaGetLastError()));
     free_plan(&plan);
     return rc;

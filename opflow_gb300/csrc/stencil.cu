@@ -373,6 +373,141 @@ __global__ void __launch_bounds__(32 * RB_WARPS, 4) axis3d_rb_kernel(FieldView i
     if (FAST) block_max_commit(vmax, &maxslots[(step + 1) % 3]);
 }
 
+// ------------------------------------------------------------- 3D, fixed point kept between steps
+// A run of K >= 2 fixed-point steps of a field whose update box is surrounded by constant boundary
+// nodes (node-centred Dirichlet, no ghost layer) and whose weights obey the maximum principle
+// (w_d >= 0, 1 - 2 sum_d w_d >= 0): then |u| never exceeds its initial bound 2^E, one scale serves every
+// step, and the box's values stay in the field's two buffers as 64-bit fixed-point integers between
+// steps instead of being rounded to float64 and converted back at every step.  The first step reads
+// float64 (MODE bit 0), the last writes float64 (MODE bit 1); values outside the box (the boundary
+// nodes) stay float64 in both buffers throughout and are converted as they are read.  Per update: the
+// six neighbours' sum minus six times the centre (exact), one signed 64x54-bit product rounded to the
+// fixed grid, one add - no float64 instruction and no per-value conversion between the first and the
+// last step.  Same register blocking as axis3d_rb_kernel.
+
+// (z * w + 2^(sh-1)) >> sh, arithmetic, on the 128-bit signed product: w carries the weight's sign
+__device__ __forceinline__ long long fx_mul_signed(long long z, long long w, int sh) {
+    const unsigned long long lo = (unsigned long long) z * (unsigned long long) w;
+    long long hi = __mul64hi(z, w);
+    if (sh == 0) return (long long) lo;
+    if (sh < 64) {
+        const unsigned long long lo2 = lo + (1ull << (sh - 1));
+        hi += (lo2 < lo) ? 1 : 0;
+        return (long long) ((lo2 >> sh) | ((unsigned long long) hi << (64 - sh)));
+    }
+    if (sh == 64) return hi + (long long) (lo >> 63);
+    return (hi + (1ll << (sh - 65))) >> (sh - 64);
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(32 * RB_WARPS, 4) axis3d_fxres_kernel(FieldView in, FieldView out, Box box, AxisParams P,
+                                                                     const unsigned long long* maxslots, int zchunk, int tiles_x, int tiles_y) {
+    constexpr bool IN_F64 = (MODE & 1) != 0, OUT_F64 = (MODE & 2) != 0;
+    const int lane = threadIdx.x & 31;
+    const int warp = blockIdx.x * RB_WARPS + (threadIdx.x >> 5);
+    if (warp >= tiles_x * tiles_y) return;
+    const int tx = warp % tiles_x, ty = warp / tiles_x;
+    const int x0 = box.lo[0] + tx * RB_COLS, y0 = box.lo[1] + ty * RB;
+    const int i = x0 - 1 + lane;
+    const bool vx = lane >= 1 && lane <= RB_COLS && i < box.hi[0];
+    const int ic = min(i, box.hi[0]);
+    const bool in_i = ic >= box.lo[0] && ic < box.hi[0];
+    const int zs = box.lo[2] + blockIdx.y * zchunk;
+    const int ze = min(zs + zchunk, box.hi[2]);
+    if (zs >= ze) return;
+    const int E = scale_exp(maxslots, 0, P.bound_bits);
+    long long roff[RB + 2];
+    bool in_row[RB + 2];
+#pragma unroll
+    for (int r = 0; r < RB + 2; ++r) {
+        const int jr = min(y0 - 1 + r, box.hi[1]);
+        roff[r] = (long long) (jr - in.off[1]) * in.sy;
+        in_row[r] = in_i && jr >= box.lo[1] && jr < box.hi[1];
+    }
+    const long long w0 = P.wneg[0] ? -(long long) P.wm[0] : (long long) P.wm[0];
+    const long long w1 = P.wneg[1] ? -(long long) P.wm[1] : (long long) P.wm[1];
+    const long long w2 = P.wneg[2] ? -(long long) P.wm[2] : (long long) P.wm[2];
+    const double* col = in.data + (ic - in.off[0]) - (long long) in.off[2] * in.sz;
+    // a value as fixed point: the box holds fixed point after the first step, everything else float64
+    auto ldq = [&](double v, bool inside) -> long long {
+        if (IN_F64 || !inside) return fx_from(v, E);
+        return __double_as_longlong(v);
+    };
+    long long below[RB], cur[RB + 2], above[RB + 2];
+    double nxt[RB + 2];
+    {
+        const int km = zs - 1, kp = min(zs + 1, box.hi[2]);
+        const bool im = km >= box.lo[2], ip = kp < box.hi[2];
+        const double* pm = col + (long long) km * in.sz;
+        const double* p0 = col + (long long) zs * in.sz;
+        const double* p1 = col + (long long) kp * in.sz;
+#pragma unroll
+        for (int r = 0; r < RB; ++r) below[r] = ldq(pm[roff[r + 1]], im && in_row[r + 1]);
+#pragma unroll
+        for (int r = 0; r < RB + 2; ++r) cur[r] = ldq(p0[roff[r]], in_row[r]);
+#pragma unroll
+        for (int r = 0; r < RB + 2; ++r) above[r] = ldq(p1[roff[r]], ip && in_row[r]);
+    }
+    double* const ocol = out.data + (i - out.off[0]) - (long long) out.off[1] * out.sy - (long long) out.off[2] * out.sz;
+    for (int k = zs; k < ze; ++k) {
+        const int kn = min(k + 2, box.hi[2]);
+        {
+            const double* pn = col + (long long) kn * in.sz;
+#pragma unroll
+            for (int r = 0; r < RB + 2; ++r) nxt[r] = pn[roff[r]];
+        }
+#pragma unroll
+        for (int r = 0; r < RB; ++r) {
+            const long long c = cur[r + 1];
+            const long long l = __shfl_up_sync(0xffffffffu, c, 1);
+            const long long rr = __shfl_down_sync(0xffffffffu, c, 1);
+            const int j = y0 + r;
+            if (vx && j < box.hi[1]) {
+                const long long b = cur[r], t = cur[r + 2], zb = below[r], za = above[r + 1];
+                long long q = c;
+                if (P.iso) {
+                    q += fx_mul_signed(((l + rr) + (b + t)) + (zb + za) - 6 * c, w0, P.wshift[0]);
+                } else {
+                    q += fx_mul_signed((l + rr) - 2 * c, w0, P.wshift[0]);
+                    q += fx_mul_signed((b + t) - 2 * c, w1, P.wshift[1]);
+                    q += fx_mul_signed((zb + za) - 2 * c, w2, P.wshift[2]);
+                }
+                ocol[(long long) j * out.sy + (long long) k * out.sz] = OUT_F64 ? fx_to(q, E) : __longlong_as_double(q);
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < RB; ++r) below[r] = cur[r + 1];
+#pragma unroll
+        for (int r = 0; r < RB + 2; ++r) cur[r] = above[r];
+        const bool in_k = kn < box.hi[2];
+#pragma unroll
+        for (int r = 0; r < RB + 2; ++r) above[r] = ldq(nxt[r], in_k && in_row[r]);
+    }
+}
+
+int axis_launch_resident(opflow_ctx ctx, const FieldView& in, const FieldView& out, const Box& box, const AxisParams& P,
+                         const unsigned long long* maxslots, bool first, bool last) {
+    const int nx = box.hi[0] - box.lo[0], ny = box.hi[1] - box.lo[1], nz = box.hi[2] - box.lo[2];
+    if (nx <= 0 || ny <= 0 || nz <= 0) return OPFLOW_OK;
+    if (P.ndim != 3) return fail(OPFLOW_E_UNSUPPORTED, "the resident fixed-point kernel covers 3D grids");
+    const int tiles_x = (nx + RB_COLS - 1) / RB_COLS, tiles_y = (ny + RB - 1) / RB;
+    const int bx = (tiles_x * tiles_y + RB_WARPS - 1) / RB_WARPS;
+    int zchunks = (ctx->num_sms * 6 + bx - 1) / bx;
+    zchunks = std::max(1, std::min(zchunks, (nz + 15) / 16));
+    const int zchunk = (nz + zchunks - 1) / zchunks;
+    zchunks = (nz + zchunk - 1) / zchunk;
+    dim3 g(bx, zchunks), b(32 * RB_WARPS);
+    const int mode = (first ? 1 : 0) | (last ? 2 : 0);
+    switch (mode) {
+        case 0: axis3d_fxres_kernel<0><<<g, b, 0, ctx->stream>>>(in, out, box, P, maxslots, zchunk, tiles_x, tiles_y); break;
+        case 1: axis3d_fxres_kernel<1><<<g, b, 0, ctx->stream>>>(in, out, box, P, maxslots, zchunk, tiles_x, tiles_y); break;
+        case 2: axis3d_fxres_kernel<2><<<g, b, 0, ctx->stream>>>(in, out, box, P, maxslots, zchunk, tiles_x, tiles_y); break;
+        default: axis3d_fxres_kernel<3><<<g, b, 0, ctx->stream>>>(in, out, box, P, maxslots, zchunk, tiles_x, tiles_y); break;
+    }
+    OPG_LAUNCHED();
+    return check_launch("axis3d_fxres_kernel");
+}
+
 // 3D tiling: register-blocked warps (the measured default for the fixed-point mode: integer-issue
 // bound, gains from the absent barriers) or shared-memory tiles (the default for the exact mode:
 // float64-pipe bound).  Both give the same values; the tuner times the two on the first launch of a

@@ -259,3 +259,50 @@ def test_ftcs3d_ragged_tiles_match_oracle(ctx, monkeypatch, tiling, mode):
     else:
         rel = np.abs(got - h0.data).max() / np.abs(h0.data).max()
         assert rel <= 1e-14, rel
+
+
+def test_fast_resident_run_at_the_512_config_within_1e14_of_exact(ctx, monkeypatch):
+    """The 512^3 x 200-step FTCS3D configuration (8 seeded Gaussians, Dirichlet 0, dt = 0.1 h^2): the
+    fixed-point run that keeps the field in fixed point between steps is within 1e-14 (normwise
+    relative) of the bit-exact IEEE run, and so is the per-step form it replaces."""
+    torch = pytest.importorskip("torch")
+    import bench
+    n, steps = 512, 200
+    mesh = cm.mesh_uniform([n] * 3)
+    fd = cm.field_desc(3, capi.CORNER, [(capi.BC_DIRC, capi.BC_DIRC)] * 3)
+    u0 = bench.gaussians_u0(torch, n, 1234, torch.device("cuda", 0)).cpu().numpy()
+    h = 1.0 / (n - 1)
+    s = 0.1 * h * h
+    out = {}
+    for name, mode, env in (("exact", "exact", "1"), ("resident", "fast", "1"), ("per_step", "fast", "0")):
+        monkeypatch.setenv("OPFLOW_FX_RESIDENT", env)
+        u = api.CartesianField(mesh, fd, ctx)
+        u.upload(u0)
+        u.assign(cm.ftcs_expr(u, s, 3), steps=steps, mode=mode)
+        out[name] = u.download()
+        del u
+    e = out["exact"]
+    for name in ("resident", "per_step"):
+        rel = np.abs(out[name] - e).max() / np.abs(e).max()
+        print("\n512^3 x %d FTCS3D: %s fixed point vs exact: %.2e" % (steps, name, rel))
+        assert rel <= 1e-14, (name, rel)
+
+
+def test_fast_resident_falls_back_when_weights_break_the_maximum_principle(ctx, monkeypatch):
+    """dt = 0.4 hx^2 on a grid with hx > hy > hz (1 - 2 sum_d w_d < 0): no resident run, the per-step
+    form runs (bit-identical with and without the switch)."""
+    dims, steps = (40, 36, 33), 3
+    mesh = cm.mesh_uniform(list(dims))
+    fd = cm.field_desc(3, capi.CORNER, [(capi.BC_DIRC, capi.BC_DIRC)] * 3, [(0.5, 0.5)] * 3)
+    a = np.random.default_rng(4).random([d for d in reversed(dims)])
+    res = {}
+    for env in ("1", "0"):
+        monkeypatch.setenv("OPFLOW_FX_RESIDENT", env)
+        u = api.CartesianField(mesh, fd, ctx)
+        b = u.download()
+        b[1:-1, 1:-1, 1:-1] = a[1:-1, 1:-1, 1:-1]
+        u.upload(b)
+        hx = 1.0 / (dims[0] - 1)
+        u.assign(cm.ftcs_expr(u, 0.4 * hx * hx, 3), steps=steps, mode="fast")
+        res[env] = u.download()
+    assert np.array_equal(res["1"], res["0"])
