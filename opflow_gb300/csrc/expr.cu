@@ -1091,7 +1091,7 @@ static bool resident_eligible(const Plan& plan, opflow_field dst, const opflow_f
         if (plan.axis.wneg[g]) return false;
         sum += std::ldexp((double) plan.axis.wm[g], -plan.axis.wshift[g]);
     }
-    return 1.0 - 2.0 * sum >= 0.0;
+    return 1.0 - 2.0 * sum >= 0.0 && axis_resident_ok(plan.axis);
 }
 
 // One assignment step: evaluates into the back buffer when the expression reads dst (out-of-place, as

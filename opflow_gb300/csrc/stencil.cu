@@ -385,29 +385,24 @@ __global__ void __launch_bounds__(32 * RB_WARPS, 4) axis3d_rb_kernel(FieldView i
 // fixed grid, one add - no float64 instruction and no per-value conversion between the first and the
 // last step.  Same register blocking as axis3d_rb_kernel.
 
-// (z * w + 2^(sh-1)) >> sh, arithmetic, on the 128-bit signed product: w carries the weight's sign
-__device__ __forceinline__ long long fx_mul_signed(long long z, long long w, int sh) {
-    const unsigned long long lo = (unsigned long long) z * (unsigned long long) w;
-    long long hi = __mul64hi(z, w);
-    if (sh == 0) return (long long) lo;
-    if (sh < 64) {
-        const unsigned long long lo2 = lo + (1ull << (sh - 1));
-        hi += (lo2 < lo) ? 1 : 0;
-        return (long long) ((lo2 >> sh) | ((unsigned long long) hi << (64 - sh)));
-    }
-    if (sh == 64) return hi + (long long) (lo >> 63);
-    return (hi + (1ll << (sh - 65))) >> (sh - 64);
+// (z * w + 2^(sh-1)) >> sh (floor, on the exact 128-bit product) for a weight 0 <= w < 2^53 given as
+// ws = w * 2^(64 - sh) (exact, ws < 2^63, so 54 <= sh <= 64): the product's high word plus the carry of
+// adding 2^63 to its low word.
+__device__ __forceinline__ long long fx_mul_hi(long long z, long long ws) {
+    const unsigned long long lo = (unsigned long long) z * (unsigned long long) ws;
+    return __mul64hi(z, ws) + (long long) (lo >> 63);
 }
 
-template <int MODE>
-__global__ void __launch_bounds__(32 * RB_WARPS, 4) axis3d_fxres_kernel(FieldView in, FieldView out, Box box, AxisParams P,
-                                                                     const unsigned long long* maxslots, int zchunk, int tiles_x, int tiles_y) {
+template <int MODE, int RBX>
+__global__ void __launch_bounds__(32 * RB_WARPS, RBX <= 4 ? 6 : (RBX <= 6 ? 5 : 4)) axis3d_fxres_kernel(FieldView in, FieldView out, Box box, AxisParams P, long long ws0,
+                                                                     long long ws1, long long ws2, const unsigned long long* maxslots,
+                                                                     int zchunk, int tiles_x, int tiles_y) {
     constexpr bool IN_F64 = (MODE & 1) != 0, OUT_F64 = (MODE & 2) != 0;
     const int lane = threadIdx.x & 31;
     const int warp = blockIdx.x * RB_WARPS + (threadIdx.x >> 5);
     if (warp >= tiles_x * tiles_y) return;
     const int tx = warp % tiles_x, ty = warp / tiles_x;
-    const int x0 = box.lo[0] + tx * RB_COLS, y0 = box.lo[1] + ty * RB;
+    const int x0 = box.lo[0] + tx * RB_COLS, y0 = box.lo[1] + ty * RBX;
     const int i = x0 - 1 + lane;
     const bool vx = lane >= 1 && lane <= RB_COLS && i < box.hi[0];
     const int ic = min(i, box.hi[0]);
@@ -416,37 +411,48 @@ __global__ void __launch_bounds__(32 * RB_WARPS, 4) axis3d_fxres_kernel(FieldVie
     const int ze = min(zs + zchunk, box.hi[2]);
     if (zs >= ze) return;
     const int E = scale_exp(maxslots, 0, P.bound_bits);
-    long long roff[RB + 2];
-    bool in_row[RB + 2];
+    long long roff[RBX + 2];
+    bool in_row[RBX + 2];
+    bool rows_in = true;  // every row of the warp's tile (with its halo rows) lies in the box
 #pragma unroll
-    for (int r = 0; r < RB + 2; ++r) {
+    for (int r = 0; r < RBX + 2; ++r) {
         const int jr = min(y0 - 1 + r, box.hi[1]);
         roff[r] = (long long) (jr - in.off[1]) * in.sy;
         in_row[r] = in_i && jr >= box.lo[1] && jr < box.hi[1];
+        rows_in = rows_in && jr >= box.lo[1] && jr < box.hi[1];
     }
-    const long long w0 = P.wneg[0] ? -(long long) P.wm[0] : (long long) P.wm[0];
-    const long long w1 = P.wneg[1] ? -(long long) P.wm[1] : (long long) P.wm[1];
-    const long long w2 = P.wneg[2] ? -(long long) P.wm[2] : (long long) P.wm[2];
+    // warp-uniform: no lane of this warp reads a value outside the box in x or y
+    const bool plane_in = __all_sync(0xffffffffu, in_i) && rows_in;
     const double* col = in.data + (ic - in.off[0]) - (long long) in.off[2] * in.sz;
-    // a value as fixed point: the box holds fixed point after the first step, everything else float64
-    auto ldq = [&](double v, bool inside) -> long long {
-        if (IN_F64 || !inside) return fx_from(v, E);
-        return __double_as_longlong(v);
+    // a plane of the warp's rows as fixed point: the box holds fixed point after the first step,
+    // everything outside it float64 (converted here, on warps that touch the box's edge only)
+    auto load_plane = [&](const double* v, bool kin, long long* dst, int r0, int nr) {
+        if (!IN_F64 && plane_in && kin) {
+#pragma unroll
+            for (int r = 0; r < RBX + 2; ++r)
+                if (r >= r0 && r < r0 + nr) dst[r - r0] = __double_as_longlong(v[r]);
+        } else {
+#pragma unroll
+            for (int r = 0; r < RBX + 2; ++r)
+                if (r >= r0 && r < r0 + nr) dst[r - r0] = (IN_F64 || !(kin && in_row[r])) ? fx_from(v[r], E) : __double_as_longlong(v[r]);
+        }
     };
-    long long below[RB], cur[RB + 2], above[RB + 2];
-    double nxt[RB + 2];
+    long long below[RBX], cur[RBX + 2], above[RBX + 2];
+    double nxt[RBX + 2];
     {
         const int km = zs - 1, kp = min(zs + 1, box.hi[2]);
-        const bool im = km >= box.lo[2], ip = kp < box.hi[2];
         const double* pm = col + (long long) km * in.sz;
         const double* p0 = col + (long long) zs * in.sz;
         const double* p1 = col + (long long) kp * in.sz;
 #pragma unroll
-        for (int r = 0; r < RB; ++r) below[r] = ldq(pm[roff[r + 1]], im && in_row[r + 1]);
+        for (int r = 0; r < RBX + 2; ++r) nxt[r] = pm[roff[r]];
+        load_plane(nxt, km >= box.lo[2], below, 1, RBX);
 #pragma unroll
-        for (int r = 0; r < RB + 2; ++r) cur[r] = ldq(p0[roff[r]], in_row[r]);
+        for (int r = 0; r < RBX + 2; ++r) nxt[r] = p0[roff[r]];
+        load_plane(nxt, true, cur, 0, RBX + 2);
 #pragma unroll
-        for (int r = 0; r < RB + 2; ++r) above[r] = ldq(p1[roff[r]], ip && in_row[r]);
+        for (int r = 0; r < RBX + 2; ++r) nxt[r] = p1[roff[r]];
+        load_plane(nxt, kp < box.hi[2], above, 0, RBX + 2);
     }
     double* const ocol = out.data + (i - out.off[0]) - (long long) out.off[1] * out.sy - (long long) out.off[2] * out.sz;
     for (int k = zs; k < ze; ++k) {
@@ -454,10 +460,10 @@ __global__ void __launch_bounds__(32 * RB_WARPS, 4) axis3d_fxres_kernel(FieldVie
         {
             const double* pn = col + (long long) kn * in.sz;
 #pragma unroll
-            for (int r = 0; r < RB + 2; ++r) nxt[r] = pn[roff[r]];
+            for (int r = 0; r < RBX + 2; ++r) nxt[r] = pn[roff[r]];
         }
 #pragma unroll
-        for (int r = 0; r < RB; ++r) {
+        for (int r = 0; r < RBX; ++r) {
             const long long c = cur[r + 1];
             const long long l = __shfl_up_sync(0xffffffffu, c, 1);
             const long long rr = __shfl_down_sync(0xffffffffu, c, 1);
@@ -466,44 +472,69 @@ __global__ void __launch_bounds__(32 * RB_WARPS, 4) axis3d_fxres_kernel(FieldVie
                 const long long b = cur[r], t = cur[r + 2], zb = below[r], za = above[r + 1];
                 long long q = c;
                 if (P.iso) {
-                    q += fx_mul_signed(((l + rr) + (b + t)) + (zb + za) - 6 * c, w0, P.wshift[0]);
+                    q += fx_mul_hi(((l + rr) + (b + t)) + ((zb + za) - 6 * c), ws0);
                 } else {
-                    q += fx_mul_signed((l + rr) - 2 * c, w0, P.wshift[0]);
-                    q += fx_mul_signed((b + t) - 2 * c, w1, P.wshift[1]);
-                    q += fx_mul_signed((zb + za) - 2 * c, w2, P.wshift[2]);
+                    q += fx_mul_hi((l + rr) - 2 * c, ws0);
+                    q += fx_mul_hi((b + t) - 2 * c, ws1);
+                    q += fx_mul_hi((zb + za) - 2 * c, ws2);
                 }
                 ocol[(long long) j * out.sy + (long long) k * out.sz] = OUT_F64 ? fx_to(q, E) : __longlong_as_double(q);
             }
         }
 #pragma unroll
-        for (int r = 0; r < RB; ++r) below[r] = cur[r + 1];
+        for (int r = 0; r < RBX; ++r) below[r] = cur[r + 1];
 #pragma unroll
-        for (int r = 0; r < RB + 2; ++r) cur[r] = above[r];
-        const bool in_k = kn < box.hi[2];
-#pragma unroll
-        for (int r = 0; r < RB + 2; ++r) above[r] = ldq(nxt[r], in_k && in_row[r]);
+        for (int r = 0; r < RBX + 2; ++r) cur[r] = above[r];
+        load_plane(nxt, kn < box.hi[2], above, 0, RBX + 2);
     }
+}
+
+bool axis_resident_ok(const AxisParams& P) {
+    for (int d = 0; d < P.ndim; ++d) {
+        const int g = P.iso ? 0 : d;
+        if (P.wneg[g] || P.wshift[g] < 54 || P.wshift[g] > 64) return false;
+        if (P.wm[g] >= (1ull << 53)) return false;
+        if (P.wshift[g] < 64 && (P.wm[g] >> (P.wshift[g] - 1)) != 0) return false;  // w * 2^(64 - sh) < 2^63
+    }
+    return true;
 }
 
 int axis_launch_resident(opflow_ctx ctx, const FieldView& in, const FieldView& out, const Box& box, const AxisParams& P,
                          const unsigned long long* maxslots, bool first, bool last) {
+    if (!axis_resident_ok(P)) return fail(OPFLOW_E_UNSUPPORTED, "weights outside the resident fixed-point kernel's range");
     const int nx = box.hi[0] - box.lo[0], ny = box.hi[1] - box.lo[1], nz = box.hi[2] - box.lo[2];
     if (nx <= 0 || ny <= 0 || nz <= 0) return OPFLOW_OK;
     if (P.ndim != 3) return fail(OPFLOW_E_UNSUPPORTED, "the resident fixed-point kernel covers 3D grids");
-    const int tiles_x = (nx + RB_COLS - 1) / RB_COLS, tiles_y = (ny + RB - 1) / RB;
+    // rows per warp: 6 (the measured best at 512^3); OPFLOW_FXRES_RB=4|6|8 for sweeps
+    int rbx = 6;
+    if (const char* e = getenv("OPFLOW_FXRES_RB")) rbx = atoi(e) == 4 ? 4 : (atoi(e) == 8 ? 8 : 6);
+    const int tiles_x = (nx + RB_COLS - 1) / RB_COLS, tiles_y = (ny + rbx - 1) / rbx;
     const int bx = (tiles_x * tiles_y + RB_WARPS - 1) / RB_WARPS;
-    int zchunks = (ctx->num_sms * 6 + bx - 1) / bx;
+    const int per_sm = rbx == 4 ? 6 : (rbx == 6 ? 5 : 4);
+    int zchunks = (ctx->num_sms * per_sm * 3 / 2 + bx - 1) / bx;
     zchunks = std::max(1, std::min(zchunks, (nz + 15) / 16));
     const int zchunk = (nz + zchunks - 1) / zchunks;
     zchunks = (nz + zchunk - 1) / zchunk;
     dim3 g(bx, zchunks), b(32 * RB_WARPS);
-    const int mode = (first ? 1 : 0) | (last ? 2 : 0);
-    switch (mode) {
-        case 0: axis3d_fxres_kernel<0><<<g, b, 0, ctx->stream>>>(in, out, box, P, maxslots, zchunk, tiles_x, tiles_y); break;
-        case 1: axis3d_fxres_kernel<1><<<g, b, 0, ctx->stream>>>(in, out, box, P, maxslots, zchunk, tiles_x, tiles_y); break;
-        case 2: axis3d_fxres_kernel<2><<<g, b, 0, ctx->stream>>>(in, out, box, P, maxslots, zchunk, tiles_x, tiles_y); break;
-        default: axis3d_fxres_kernel<3><<<g, b, 0, ctx->stream>>>(in, out, box, P, maxslots, zchunk, tiles_x, tiles_y); break;
+    // the weights as w * 2^(64 - wshift), exact and below 2^63 (checked by axis_resident_ok)
+    long long ws[3];
+    for (int d = 0; d < 3; ++d) {
+        const int gi = P.iso ? 0 : d;
+        ws[d] = (long long) (P.wm[gi] << (64 - P.wshift[gi]));
     }
+    const int mode = (first ? 1 : 0) | (last ? 2 : 0);
+    auto go = [&](auto rb_tag) {
+        constexpr int R = decltype(rb_tag)::value;
+        switch (mode) {
+            case 0: axis3d_fxres_kernel<0, R><<<g, b, 0, ctx->stream>>>(in, out, box, P, ws[0], ws[1], ws[2], maxslots, zchunk, tiles_x, tiles_y); break;
+            case 1: axis3d_fxres_kernel<1, R><<<g, b, 0, ctx->stream>>>(in, out, box, P, ws[0], ws[1], ws[2], maxslots, zchunk, tiles_x, tiles_y); break;
+            case 2: axis3d_fxres_kernel<2, R><<<g, b, 0, ctx->stream>>>(in, out, box, P, ws[0], ws[1], ws[2], maxslots, zchunk, tiles_x, tiles_y); break;
+            default: axis3d_fxres_kernel<3, R><<<g, b, 0, ctx->stream>>>(in, out, box, P, ws[0], ws[1], ws[2], maxslots, zchunk, tiles_x, tiles_y); break;
+        }
+    };
+    if (rbx == 4) go(std::integral_constant<int, 4>{});
+    else if (rbx == 8) go(std::integral_constant<int, 8>{});
+    else go(std::integral_constant<int, 6>{});
     OPG_LAUNCHED();
     return check_launch("axis3d_fxres_kernel");
 }
