@@ -313,6 +313,30 @@ int update_padding_buf(opflow_field f, double* data) {
     return OPFLOW_OK;
 }
 
+// The corner-located Dirichlet boundary nodes of `data` (the writes updatePadding makes for a field
+// without a ghost layer, in its order) filled with values[d][side] instead of the boundary values: a
+// resident fixed-point run stores the boundary constants there as fixed-point bit patterns between its
+// steps, and update_padding_full puts the float64 constants back afterwards.
+int fill_dirichlet_nodes(opflow_field f, double* data, const double values[3][2]) {
+    const opflow_field_info& R = f->info;
+    const opflow_field_desc& F = f->desc;
+    for (int i = 0; i < R.ndim; ++i)
+        for (int side = 0; side < 2; ++side) {
+            const bool at = side == 0 ? R.local[i][0] == R.accessible[i][0] : R.local[i][1] == R.accessible[i][1];
+            if (at && F.bc_type[i][side] == OPFLOW_BC_DIRC && F.loc[i] == OPFLOW_CORNER) {
+                PadOp op{};
+                op.kind = PAD_FILL;
+                op.dim = i;
+                op.bcv = values[i][side];
+                for (int k = 0; k < 3; ++k) { op.lo[k] = R.local[k][0]; op.hi[k] = R.local[k][1]; }
+                op.lo[i] = side == 0 ? R.local[i][0] : R.local[i][1] - 1;
+                op.hi[i] = op.lo[i] + 1;
+                OPG_TRY(launch_pad(f, data, op));
+            }
+        }
+    return OPFLOW_OK;
+}
+
 int update_padding_full(opflow_field f, double* data) {
     const opflow_field_info& R = f->info;
     const opflow_field_desc& F = f->desc;

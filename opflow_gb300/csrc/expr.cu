@@ -1094,6 +1094,48 @@ static bool resident_eligible(const Plan& plan, opflow_field dst, const opflow_f
     return 1.0 - 2.0 * sum >= 0.0 && axis_resident_ok(plan.axis);
 }
 
+// The scale of a fixed-point run (the exponent scale_exp gives on the device) and a float64 constant in
+// that fixed point, rounded as fx_from rounds (to nearest even; half away from zero at extreme scales).
+static int host_scale_exp(unsigned long long mx, unsigned long long bound_bits) {
+    const unsigned long long m = mx > bound_bits ? mx : bound_bits;
+    if (m == 0) return -1000;
+    return (int) ((m >> 52) & 0x7FF) - 1023 + 1;
+}
+static long long host_fx(double v, int E) {
+    const double x = std::ldexp(v, 58 - E);
+    if (E > -900 && E < 1000) return (long long) std::nearbyint(x);
+    return (long long) std::round(x);
+}
+
+// K >= 2 steps with the field in fixed point between them: step 1 reads float64; then the boundary
+// nodes of both buffers take their constants' fixed-point bit patterns; the last step writes float64
+// and the boundary constants are written back as float64 into both buffers.
+static int run_resident(opflow_ctx ctx, opflow_field dst, Plan& plan, unsigned long long* maxslots, int steps) {
+    OPG_TRY(ensure_back(dst));
+    unsigned long long mx = 0;
+    OPG_CUDA(cudaMemcpyAsync(&mx, maxslots, sizeof mx, cudaMemcpyDeviceToHost, ctx->stream));
+    OPG_CUDA(cudaStreamSynchronize(ctx->stream));
+    const int E = host_scale_exp(mx, plan.axis.bound_bits);
+    double fxv[3][2] = {{0., 0.}, {0., 0.}, {0., 0.}};
+    for (int d = 0; d < dst->info.ndim; ++d)
+        for (int sd = 0; sd < 2; ++sd) fxv[d][sd] = __builtin_bit_cast(double, host_fx(dst->desc.bc_value[d][sd], E));
+    int rc = OPFLOW_OK;
+    for (int s = 0; s < steps && rc == OPFLOW_OK; ++s) {
+        rc = axis_launch_resident(ctx, dst->view(), dst->view_back(), plan.box, plan.axis, maxslots, s == 0, s == steps - 1);
+        dst->cur = 1 - dst->cur;
+        dst->version++;
+        if (rc == OPFLOW_OK && s == 0) {
+            dst->bc_fresh[0] = dst->bc_fresh[1] = false;
+            rc = fill_dirichlet_nodes(dst, dst->buf[0], fxv);
+            if (rc == OPFLOW_OK) rc = fill_dirichlet_nodes(dst, dst->buf[1], fxv);
+        }
+    }
+    if (rc == OPFLOW_OK) rc = update_padding_full(dst, dst->buf[0]);
+    if (rc == OPFLOW_OK) rc = update_padding_full(dst, dst->buf[1]);
+    if (rc == OPFLOW_OK) dst->bc_fresh[0] = dst->bc_fresh[1] = true;
+    return rc;
+}
+
 // One assignment step: evaluates into the back buffer when the expression reads dst (out-of-place, as
 // FieldAssigner does through its temporary copy), otherwise into dst directly; then the padding.
 static int run_plan(opflow_ctx ctx, opflow_field dst, int arith, const opflow_field* leaves, Plan* plan, unsigned long long* maxslots, int step) {
@@ -1171,13 +1213,7 @@ int opflow_assign_repeat(opflow_ctx ctx, opflow_field dst, int arith, const opfl
     }
     if (resident_eligible(plan, dst, leaves, steps)) {
         // fixed point kept in the field's buffers between the steps of the run (axis3d_fxres_kernel)
-        OPG_TRY(ensure_back(dst));
-        for (int s = 0; s < steps && rc == OPFLOW_OK; ++s) {
-            rc = axis_launch_resident(ctx, dst->view(), dst->view_back(), plan.box, plan.axis, maxslots, s == 0, s == steps - 1);
-            dst->cur = 1 - dst->cur;
-            dst->version++;
-            if (rc == OPFLOW_OK) rc = update_padding_assign(dst);
-        }
+        rc = run_resident(ctx, dst, plan, maxslots, steps);
     } else {
         for (int s = 0; s < steps && rc == OPFLOW_OK; ++s) rc = run_plan(ctx, dst, arith, leaves, &plan, maxslots, s);
     }

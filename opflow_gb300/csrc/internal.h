@@ -123,6 +123,8 @@ void mesh_destroy(opflow_ctx ctx, MeshDev* m);
 bool mesh_equal(const MeshDev* a, const MeshDev* b);
 int ensure_back(opflow_field f);
 int update_padding_buf(opflow_field f, double* data);
+int update_padding_full(opflow_field f, double* data);
+int fill_dirichlet_nodes(opflow_field f, double* data, const double values[3][2]);
 // updatePadding as an assignment does it (assign_impl and assignImpl_final each run one pass; a second
 // pass only changes a periodic zone wider than its period)
 int update_padding_assign(opflow_field f);
