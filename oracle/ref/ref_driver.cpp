@@ -8,6 +8,11 @@
 #include "OpFlowCoreNoSolvers.hpp"
 #include "DataStructures/StencilPad.hpp"
 #include "Math/Function/Numeric.hpp"
+// The reference's raw binary writer calls CartesianField::evalSafeAt, which its CartesianField no
+// longer declares; for the indices it visits (the local range) evalAt returns the same stored value.
+#define evalSafeAt evalAt
+#include "Utils/Writers/RawBinaryStream.hpp"
+#undef evalSafeAt
 
 #include <cmath>
 #include <cstdint>
@@ -324,6 +329,49 @@ static int run_conv1d(int n, int steps) {
     return 0;
 }
 
+// Utils::RawBinaryOStream (src/Utils/Writers/RawBinaryStream.hpp:80-152): the two fields of the raw binary
+// tests (a cell-centred and a nodal field on a stretched 7 x 6-node mesh) written as
+// << TimeStamp(0.25) << c << v << TimeStamp(1.5) << c into <dir>/c_0.cart, v_1.cart, c_2.cart.
+static int run_rawbinary(const char* dir, uint64_t seed) {
+    using Mesh = CartesianMesh<Meta::int_<2>>;
+    using Field = CartesianField<Real, Mesh>;
+    const int nx = 6, ny = 5;
+    auto mesh = MeshBuilder<Mesh>()
+                        .newMesh(nx + 1, ny + 1)
+                        .setMeshOfDim(0, [&](int i) { return stretched(i, nx + 1); })
+                        .setMeshOfDim(1, [&](int i) { return stretched(i, ny + 1) * 2.0; })
+                        .build();
+    auto c = ExprBuilder<Field>()
+                     .setName("c")
+                     .setMesh(mesh)
+                     .setLoc(LocOnMesh::Center)
+                     .setBC(0, DimPos::start, BCType::Dirc, 0.5)
+                     .setBC(0, DimPos::end, BCType::Neum, -1.0)
+                     .setBC(1, DimPos::start, BCType::Periodic)
+                     .setBC(1, DimPos::end, BCType::Periodic)
+                     .setExt(1)
+                     .build();
+    rangeFor_s(c.assignableRange, [&](auto&& i) { c[i] = u01(seed, (uint64_t) i[1] * (nx + 1) + i[0]); });
+    c.updatePadding();
+    auto v = ExprBuilder<Field>()
+                     .setName("v")
+                     .setMesh(mesh)
+                     .setLoc(LocOnMesh::Corner)
+                     .setBC(0, DimPos::start, BCType::Dirc, 0.25)
+                     .setBC(0, DimPos::end, BCType::Dirc, -0.75)
+                     .setBC(1, DimPos::start, BCType::Neum, 0.)
+                     .setBC(1, DimPos::end, BCType::Dirc, 1.0)
+                     .build();
+    rangeFor_s(v.assignableRange, [&](auto&& i) { v[i] = u01(seed + 1, (uint64_t) i[1] * (nx + 1) + i[0]); });
+    v.updatePadding();
+    dump_field(c, "c");
+    dump_field(v, "v");
+    Utils::RawBinaryOStream os(std::string(dir) + "/snap");
+    os << Utils::TimeStamp(0.25) << c << v;
+    os << Utils::TimeStamp(1.5) << c;
+    return 0;
+}
+
 // Field construction + padding rules: one field per (loc, bc) combination, initialised by a smooth
 // function of the coordinates, dumped over its readable range.
 static int run_padding(int nx, int ny, int loc_i, int bc_lo, int bc_hi, int ext) {
@@ -624,6 +672,7 @@ int main(int argc, char** argv) {
     else if (cmd == "weno") rc = run_weno(I(3), I(4), I(5), std::strtoull(argv[6], nullptr, 10), I(7));
     else if (cmd == "padding") rc = run_padding(I(3), I(4), I(5), I(6), I(7), I(8));
     else if (cmd == "ops") rc = run_ops(I(3), I(4), std::strtoull(argv[5], nullptr, 10));
+    else if (cmd == "rawbinary") rc = run_rawbinary(argv[3], std::strtoull(argv[4], nullptr, 10));
     else if (cmd == "conv1d") rc = run_conv1d(I(3), I(4));
     else if (cmd == "logic") rc = run_logic(I(3), I(4), std::strtoull(argv[5], nullptr, 10));
     else if (cmd == "assemble") rc = run_assemble(argv[3], argc > 4 ? I(4) : 0);

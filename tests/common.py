@@ -2,6 +2,7 @@
 import ctypes as C
 import json
 import os
+import struct
 
 import numpy as np
 
@@ -146,3 +147,31 @@ def problem_residual(p, f, x):
     dims, off, coef, rhs = problem_system(p, f)
     r, bn = orc.residual(dims, [0] * len(dims), off, coef, rhs, np.asarray(x, dtype=np.float64).reshape(-1))
     return r / bn if bn > 0 else r
+
+
+def parse_cart(path=None, raw=None):
+    """The layout RawBinaryOStream::operator<< writes (RawBinaryStream.hpp:97-150), read from a file or
+    from its bytes."""
+    raw = open(path, "rb").read() if raw is None else raw
+    pos = 0
+
+    def take(fmt):
+        nonlocal pos
+        v = struct.unpack_from("<" + fmt, raw, pos)
+        pos += struct.calcsize("<" + fmt)
+        return v
+
+    (nlen,) = take("i")
+    name = raw[pos:pos + nlen].decode()
+    pos += nlen
+    dim, nproc = take("ii")
+    (time,) = take("d")
+    mesh_range = [take("ii") for _ in range(dim)]
+    coords = [np.array(take("%dd" % (e - s))) for s, e in mesh_range]
+    acc = [take("ii") for _ in range(dim)]
+    loc = [take("ii") for _ in range(dim)]
+    n = int(np.prod([e - s for s, e in loc]))
+    vals = np.array(take("%dd" % n))
+    assert pos == len(raw)
+    return dict(name=name, dim=dim, nproc=nproc, time=time, mesh_range=mesh_range, coords=coords, accessible=acc, local=loc,
+                values=vals)

@@ -125,6 +125,23 @@ def hypre_case(name, args):
     print(name, [m["key"] for m in metas], metas[-1]["meta"] if metas else None)
 
 
+def rawbinary_case(name, seed):
+    """Files written by the reference's Utils::RawBinaryOStream, stored byte for byte."""
+    arrays, metas = {}, []
+    with tempfile.TemporaryDirectory() as td:
+        out = os.path.join(td, "o.bin")
+        subprocess.check_call([DRIVER, out, "rawbinary", td, str(seed)])
+        for kind, meta, arrs in parse(out):
+            arrays["%s__data" % meta["name"]] = arrs["data"]
+            metas.append({"kind": kind, "key": meta["name"], "meta": meta})
+        files = sorted(f for f in os.listdir(td) if f.endswith(".cart"))
+        for f in files:
+            arrays["file__" + f[:-5]] = np.frombuffer(open(os.path.join(td, f), "rb").read(), dtype=np.uint8)
+    arrays["meta"] = np.array(json.dumps({"args": ["rawbinary", str(seed)], "records": metas, "files": files}))
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrays)
+    print(name, files)
+
+
 def main():
     if not (os.path.exists(DRIVER) and os.path.exists(SOLVER)):
         subprocess.check_call([os.path.join(ROOT, "oracle", "build_ref.sh")])
@@ -132,6 +149,8 @@ def main():
     for name, args in sorted(HYPRE_CASES.items()):
         if name in wanted:
             hypre_case(name, args)
+    if "rawbinary_ref" in wanted or not sys.argv[1:]:
+        rawbinary_case("rawbinary_ref", 51)
     for name, args in sorted(CASES.items()):
         if name not in wanted:
             continue

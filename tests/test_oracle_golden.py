@@ -262,3 +262,21 @@ def test_assembly_matches_csr_generator_test_literals():
         for r in rows:
             assert np.array_equal(A[r], G[r]), (bc_name, r, A[r], G[r])
             assert rhs[r] == g["rhs"][r]
+
+
+def test_reference_raw_binary_files_hold_the_dumped_fields():
+    """The .cart files the reference's RawBinaryOStream wrote (rawbinary_ref fixture) parse with the
+    independent reader and hold the fields' local-range values, with the stream's time stamps and file
+    counter."""
+    meta, arr = cm.golden("rawbinary_ref")
+    assert meta["files"] == ["c_0.cart", "c_2.cart", "v_1.cart"]
+    for f, name, t in (("c_0", "c", 0.25), ("v_1", "v", 0.25), ("c_2", "c", 1.5)):
+        rec = cm.parse_cart(raw=arr["file__" + f].tobytes())
+        fm = cm.record(meta, name)
+        assert rec["name"] == name and rec["dim"] == 2 and rec["nproc"] == 1 and rec["time"] == t
+        assert [list(r) for r in rec["local"]] == fm["local"] and [list(r) for r in rec["accessible"]] == fm["accessible"]
+        rd = fm["readable"]
+        full = arr[name + "__data"].reshape(rd[1][1] - rd[1][0], rd[0][1] - rd[0][0])
+        lo = fm["local"]
+        want = full[lo[1][0] - rd[1][0]:lo[1][1] - rd[1][0], lo[0][0] - rd[0][0]:lo[0][1] - rd[0][0]].reshape(-1)
+        assert np.array_equal(rec["values"], want)

@@ -1,10 +1,11 @@
 """Field snapshots in OpFlow's raw binary format (Utils::RawBinaryOStream / RawBinaryIStream,
 src/Utils/Writers/RawBinaryStream.hpp:80-224).
 
-The reference's own stream does not compile against its current CartesianField (its writer calls the
-removed `evalSafeAt`), so no file written by the reference exists.  The layout is checked here against
-the reference's source, field by field, with an independent Python reader, and the engine's reader
-is checked by round trips and by its refusals of mismatched files.
+Pinned to files the reference's own writer produced (tests/golden/rawbinary_ref.npz: the reference
+driver compiles RawBinaryStream.hpp with its call to the removed CartesianField::evalSafeAt renamed
+to evalAt): the engine writes the same fields byte for byte and reads the reference's files back into
+the same values.  The layout is also checked field by field with an independent Python reader, and
+the engine's reader by round trips and by its refusals of mismatched files.
 """
 import os
 import struct
@@ -14,37 +15,11 @@ import pytest
 
 import common as cm
 import oracle_lib as orc
+from common import parse_cart
 from opflow_gb300 import _capi as capi
 from opflow_gb300 import api
 
 pytestmark = pytest.mark.gpu
-
-
-def parse_cart(path):
-    """The layout RawBinaryOStream::operator<< writes (RawBinaryStream.hpp:97-150)."""
-    raw = open(path, "rb").read()
-    pos = 0
-
-    def take(fmt):
-        nonlocal pos
-        v = struct.unpack_from("<" + fmt, raw, pos)
-        pos += struct.calcsize("<" + fmt)
-        return v
-
-    (nlen,) = take("i")
-    name = raw[pos:pos + nlen].decode()
-    pos += nlen
-    dim, nproc = take("ii")
-    (time,) = take("d")
-    mesh_range = [take("ii") for _ in range(dim)]
-    coords = [np.array(take("%dd" % (e - s))) for s, e in mesh_range]
-    acc = [take("ii") for _ in range(dim)]
-    loc = [take("ii") for _ in range(dim)]
-    n = int(np.prod([e - s for s, e in loc]))
-    vals = np.array(take("%dd" % n))
-    assert pos == len(raw)
-    return dict(name=name, dim=dim, nproc=nproc, time=time, mesh_range=mesh_range, coords=coords, accessible=acc, local=loc,
-                values=vals)
 
 
 def _fields(ctx, seed=51):
@@ -113,3 +88,32 @@ def test_mismatched_files_are_refused(ctx, tmp_path):
     missing = api.CartesianField(mesh, c.desc, ctx, "nothere")
     with pytest.raises(capi.OpflowError):
         api.RawBinaryIStream(str(tmp_path / "x")) >> missing
+
+
+def test_engine_writes_the_reference_files_byte_for_byte(ctx, tmp_path):
+    meta, arr = cm.golden("rawbinary_ref")
+    mesh, (c, v) = _fields(ctx, seed=int(meta["args"][1]))
+    os_ = api.RawBinaryOStream(str(tmp_path / "snap"))
+    os_ << api.TimeStamp(0.25) << c << v
+    os_ << api.TimeStamp(1.5) << c
+    for f in meta["files"]:
+        mine = open(str(tmp_path / f), "rb").read()
+        assert mine == arr["file__" + f[:-5]].tobytes(), f
+
+
+def test_engine_reads_the_reference_files(ctx, tmp_path):
+    meta, arr = cm.golden("rawbinary_ref")
+    for f in meta["files"]:
+        (tmp_path / f).write_bytes(arr["file__" + f[:-5]].tobytes())
+    mesh, (c, v) = _fields(ctx, seed=int(meta["args"][1]))
+    c2 = api.CartesianField(c.mesh, c.desc, ctx, "c")
+    v2 = api.CartesianField(v.mesh, v.desc, ctx, "v")
+    c2.assign(0.)
+    v2.assign(0.)
+    is_ = api.RawBinaryIStream(str(tmp_path / "snap"))
+    is_ >> c2
+    assert is_.time == 0.25
+    is_ >> v2
+    for g, ref in ((c2, c), (v2, v)):
+        sl = g.index_slices([tuple(g.info.local[d]) for d in range(2)])
+        assert np.array_equal(g.download()[sl], ref.download()[sl])
