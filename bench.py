@@ -964,8 +964,12 @@ def run_ours(args):
         "dtype": "f64" if mode == "exact" else "i64 fixed point (f64 storage)", "data": "synthetic",
         "config": dict(cfg, mode=mode, parallelism="replicas" if world > 1 else "single"),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": peak_src, "traffic": traffic_for(args.workload + "_" + mode),
-                     "kernel": ("axis3d_rb_kernel<FAST>" if mode == "fast" else "axis3d_kernel<EXACT>") if D == 3
+                     "peak_source": peak_src,
+                     "traffic": traffic_for(args.workload + "_" + mode + ("_resident" if D == 3 and mode == "fast" and args.steps >= 2 and
+                                                                          os.environ.get("OPFLOW_FX_RESIDENT", "1") != "0" else "")),
+                     "kernel": (("axis3d_fxres_kernel<0, 6> (resident fixed-point run; its first step converts float64 in, its last "
+                                 "float64 out)" if args.steps >= 2 and os.environ.get("OPFLOW_FX_RESIDENT", "1") != "0"
+                                 else "axis3d_rb_kernel<FAST>") if mode == "fast" else "axis3d_kernel<EXACT>") if D == 3
                                else ("axis2d_kernel<FAST>" if mode == "fast" else "axis2d_kernel<EXACT>"),
                      "timed": "whole step (stencil kernel + ghost-padding kernels), CUDA events on the launching stream",
                      "algorithmic_bytes_per_launch": alg_bytes},
