@@ -389,7 +389,134 @@ D& assign(const S& src, D& dst) {
     return dst;
 }
 
+// ---- the implicit path: makeEqnSolveHandler / Solve over the engine's solver ----------------------
+// makeEqnSolveHandler(getter, target, solver) (HYPREEqnSolveHandler.hpp:44-48) with a Struct solver
+// (StructSolver<T> or PrecondStructSolver<T, P>) and a CartesianField target returns this handler
+// instead of OpFlow's HYPREEqnSolveHandler: the overload below has the reference's signature and a
+// constraint, so overload resolution prefers it.  The getter is called with the target itself; the
+// equation's lhs - rhs is lowered like an assignment's expression, with the target as the unknown,
+// and opflow_solver_create assembles it with StencilPad semantics (the reference's generateAb).
+// solve() uploads the fields the equation reads and the target (initial guess), solves on the device
+// (re-assembling only b under staticMat) and downloads the solution (HYPREEqnSolveHandler::solve,
+// returnValues).  The solver parameters map onto the engine's: tol, maxIter, staticMat, pinValue,
+// absTol, kDim; the outer iteration (PCG, GMRES, FGMRES, LGMRES, BiCGSTAB, or the preconditioner
+// alone) and the preconditioner (PFMG / SMG / CycRed: the engine's multigrid V-cycle; Jacobi; none).
+template <typename S>
+struct struct_solver : std::false_type {};
+template <OpFlow::StructSolverType T>
+struct struct_solver<OpFlow::StructSolver<T>> : std::true_type {
+    static constexpr OpFlow::StructSolverType outer = T, pre = OpFlow::StructSolverType::None;
+};
+template <OpFlow::StructSolverType T, OpFlow::StructSolverType P>
+struct struct_solver<OpFlow::PrecondStructSolver<T, P>> : std::true_type {
+    static constexpr OpFlow::StructSolverType outer = T, pre = P;
+};
+
+inline int krylov_code(OpFlow::StructSolverType t) {
+    using ST = OpFlow::StructSolverType;
+    switch (t) {
+        case ST::PCG: return OPFLOW_KRYLOV_PCG;
+        case ST::GMRES: return OPFLOW_KRYLOV_GMRES;
+        case ST::FGMRES: return OPFLOW_KRYLOV_FGMRES;
+        case ST::LGMRES: return OPFLOW_KRYLOV_LGMRES;
+        case ST::BICGSTAB: return OPFLOW_KRYLOV_BICGSTAB;
+        default: return OPFLOW_KRYLOV_NONE;  // a preconditioner used as the solver
+    }
+}
+inline int precond_code(OpFlow::StructSolverType t) {
+    using ST = OpFlow::StructSolverType;
+    switch (t) {
+        case ST::PFMG: case ST::SMG: case ST::CYCRED: return OPFLOW_PRECOND_MG;
+        case ST::Jacobi: return OPFLOW_PRECOND_JACOBI;
+        default: return OPFLOW_PRECOND_NONE;
+    }
+}
+
+template <typename Getter, typename T, typename S>
+struct GpuEqnSolveHandler : virtual public OpFlow::EqnSolveHandler {
+    GpuEqnSolveHandler(const Getter& g, T& target, const S& s) : getter(g), target(&target), solver(s) { this->init(); }
+    ~GpuEqnSolveHandler() override {
+        if (h) opflow_solver_destroy(h);
+    }
+    void init() override {
+        auto eqn = getter(*target);
+        const int l = L.lower(eqn.lhs);
+        const int r = L.lower(eqn.rhs);
+        L.add(OPFLOW_NODE_SUB, l, r, 0, 0, 0.);
+        unknown = L.slot(*target);
+        opflow_solve_params_default(&p);
+        using K = struct_solver<S>;
+        const auto& sp = solver.params;
+        if (sp.tol) p.tol = sp.tol.value();
+        if (sp.maxIter) p.max_iter = sp.maxIter.value();
+        p.static_mat = sp.staticMat ? 1 : 0;
+        p.pin_value = sp.pinValue ? 1 : 0;
+        if constexpr (requires { sp.absTol; })
+            if (sp.absTol) p.abs_tol = sp.absTol.value();
+        if constexpr (requires { sp.kDim; })
+            if (sp.kDim) p.kdim = sp.kDim.value();
+        if constexpr (K::pre == OpFlow::StructSolverType::None) {
+            // a solver alone: a preconditioner type iterates itself, a Krylov method runs unpreconditioned
+            const int kc = krylov_code(K::outer);
+            p.krylov = kc;
+            p.precond = kc == OPFLOW_KRYLOV_NONE ? precond_code(K::outer) : OPFLOW_PRECOND_NONE;
+        } else {
+            p.krylov = krylov_code(K::outer);
+            p.precond = precond_code(K::pre);
+        }
+        if (const char* e = std::getenv("OPFLOW_GB300_PRECISION")) p.precision = std::strcmp(e, "mixed") == 0 ? OPFLOW_PREC_MIXED : p.precision;
+    }
+    OpFlow::EqnSolveState solve() override {
+        for (size_t i = 0; i < L.leaf_keys.size(); ++i) {
+            const Mirror& m = registry().at(L.leaf_keys[i]);
+            check(opflow_field_upload(m.f, const_cast<double*>(static_cast<const double*>(m.data0)), m.info.count), "opflow_field_upload");
+        }
+        if (!h) check(opflow_solver_create(context(), L.leaves[unknown], L.nodes.data(), (int) L.nodes.size(), L.leaves.data(),
+                                           (int) L.leaves.size(), unknown, &p, &h),
+                      "opflow_solver_create");
+        opflow_solve_state st{};
+        const int rc = opflow_solver_solve(h, &st);
+        if (rc != 0 && rc != OPFLOW_E_NOT_CONVERGED) die("opflow_solver_solve");
+        const Mirror& mt = registry().at(L.leaf_keys[unknown]);
+        check(opflow_field_download(mt.f, host_data(*target, mt.info), mt.info.count), "opflow_field_download");
+        return OpFlow::EqnSolveState(st.iterations, st.rel_residual, st.abs_residual);
+    }
+    void generateAb() override {}
+
+private:
+    Getter getter;
+    T* target;
+    S solver;
+    Lowering L;
+    int unknown = 0;
+    opflow_solve_params p{};
+    opflow_solver h = nullptr;
+};
+
+template <typename T, typename S>
+concept GpuSolvable = is_cfield<std::remove_cvref_t<T>>::value && struct_solver<std::remove_cvref_t<S>>::value;
+
 }  // namespace opflow_gb300::adapter
+
+namespace OpFlow {
+template <typename F, typename T, typename S>
+    requires opflow_gb300::adapter::GpuSolvable<T, S>
+std::unique_ptr<EqnSolveHandler> makeEqnSolveHandler(F&& f, T&& t, S&& s) {
+    return std::make_unique<opflow_gb300::adapter::GpuEqnSolveHandler<std::remove_cvref_t<F>, std::remove_cvref_t<T>, std::remove_cvref_t<S>>>(
+            f, t, s);
+}
+
+// Solve (UnifiedSolve.hpp:36-43, left out with the AMGCL back end it includes): one handler, one solve.
+template <StructSolverType type = StructSolverType::GMRES, StructSolverType pType = StructSolverType::None, typename F,
+          StructuredFieldExprType T>
+auto Solve(const F& func, T&& target, StructSolverParams<type> params = StructSolverParams<type> {},
+           StructSolverParams<pType> precParams = StructSolverParams<pType> {}) {
+    auto solver = PrecondStructSolver<type, pType>(params, precParams);
+    auto handler = makeEqnSolveHandler(func, target, solver);
+    return handler->solve();
+}
+}  // namespace OpFlow
+
 
 // ---- Utils::H5Stream stand-in (OpFlow's HDF5 writer needs libhdf5) -----------------------------------
 namespace OpFlow::Utils {

@@ -196,3 +196,128 @@ int opflow_assign(opflow_ctx ctx, opflow_field dst, int arith, const opflow_node
     if (rc) return failm(rc, or_last_error());
     return OPFLOW_OK;
 }
+
+/* ---- the implicit path: the oracle's assembly (generateAb restated) and its restated PCG + PFMG ---- */
+int or_assemble(const opflow_mesh_desc* m, const opflow_field_desc* descs, double** datas, int nf, int target, const opflow_node* nodes,
+                int n, int pin, int* n_entries, int* offsets, double* coef, double* rhs, size_t* n_cells);
+int or_pfmg_pcg_x0(int D, const int* dims_in, int ne, const int* off, const double* coef, const double* rhs, const double* x0,
+                   double* x_out, double tol, int maxit, int precond_cycles, int threads, int* iters, double* relres, int* levels);
+
+/* the data index of the c-th assignable cell (x fastest) */
+static size_t assignable_index(const opflow_field_info* R, const int* dims, size_t c) {
+    const int D = R->ndim;
+    const long long i = (long long) (c % dims[0]), j = (long long) ((c / dims[0]) % dims[1]), k = (long long) (c / ((size_t) dims[0] * dims[1]));
+    const long long ii = R->assignable[0][0] + i - R->data_offset[0];
+    const long long jj = D > 1 ? R->assignable[1][0] + j - R->data_offset[1] : 0;
+    const long long kk = D > 2 ? R->assignable[2][0] + k - R->data_offset[2] : 0;
+    return (size_t) ((kk * (D > 1 ? R->data_dims[1] : 1) + jj) * R->data_dims[0] + ii);
+}
+
+void opflow_solve_params_default(opflow_solve_params* p) {
+    memset(p, 0, sizeof *p);
+    p->tol = 1e-8;
+    p->max_iter = 100;
+    p->pre_sweeps = p->post_sweeps = 2;
+    p->coarse_max = 64;
+    p->kdim = 5;
+}
+
+struct opflow_solver_s {
+    opflow_field target;
+    opflow_node* nodes;
+    int n_nodes;
+    opflow_field leaves[16];
+    int n_leaves, unknown;
+    opflow_solve_params params;
+};
+
+int opflow_solver_create(opflow_ctx ctx, opflow_field target, const opflow_node* nodes, int n_nodes, const opflow_field* leaves, int n_leaves,
+                         int unknown_slot, const opflow_solve_params* params, opflow_solver* out) {
+    (void) ctx;
+    if (!target || !nodes || n_nodes <= 0 || n_leaves <= 0 || n_leaves > 16 || unknown_slot < 0 || unknown_slot >= n_leaves || !params || !out)
+        return failm(OPFLOW_E_INVALID, "bad solver arguments");
+    struct opflow_solver_s* s = (struct opflow_solver_s*) calloc(1, sizeof *s);
+    s->target = target;
+    s->nodes = (opflow_node*) malloc(n_nodes * sizeof(opflow_node));
+    memcpy(s->nodes, nodes, n_nodes * sizeof(opflow_node));
+    s->n_nodes = n_nodes;
+    memcpy(s->leaves, leaves, n_leaves * sizeof(opflow_field));
+    s->n_leaves = n_leaves;
+    s->unknown = unknown_slot;
+    s->params = *params;
+    FILE* r = rec();
+    if (r) {
+        fprintf(r, "{\"op\":\"solver\",\"target\":%d,\"unknown\":%d,\"leaves\":[", target->id, unknown_slot);
+        for (int i = 0; i < n_leaves; ++i) fprintf(r, "%s%d", i ? "," : "", leaves[i]->id);
+        fprintf(r, "],\"params\":{\"tol\":%.17g,\"max_iter\":%d,\"static_mat\":%d,\"pin_value\":%d,\"precision\":%d,\"krylov\":%d,"
+                   "\"precond\":%d,\"kdim\":%d,\"abs_tol\":%.17g,\"zero_guess\":%d},\"nodes\":[",
+                params->tol, params->max_iter, params->static_mat, params->pin_value, params->precision, params->krylov, params->precond,
+                params->kdim, params->abs_tol, params->zero_guess);
+        for (int k = 0; k < n_nodes; ++k)
+            fprintf(r, "%s[%d,%d,%d,%d,%d,%.17g,%d]", k ? "," : "", nodes[k].kind, nodes[k].a, nodes[k].b, nodes[k].dim, nodes[k].field,
+                    nodes[k].value, nodes[k].c);
+        fputs("]}\n", r);
+        fflush(r);
+    }
+    *out = s;
+    return OPFLOW_OK;
+}
+
+int opflow_solver_solve(opflow_solver s, opflow_solve_state* state) {
+    if (!s) return failm(OPFLOW_E_INVALID, "null solver");
+    FILE* r = rec();
+    if (r) {
+        fprintf(r, "{\"op\":\"solve\",\"target\":%d}\n", s->target->id);
+        fflush(r);
+    }
+    opflow_field_desc descs[16];
+    double* datas[16];
+    for (int i = 0; i < s->n_leaves; ++i) {
+        descs[i] = s->leaves[i]->desc;
+        datas[i] = s->leaves[i]->data;
+    }
+    opflow_field t = s->leaves[s->unknown];
+    int ne = 0;
+    size_t nc = 0;
+    int rc = or_assemble(&t->mesh, descs, datas, s->n_leaves, s->unknown, s->nodes, s->n_nodes, s->params.pin_value, &ne, NULL, NULL, NULL, &nc);
+    if (rc) return failm(rc, or_last_error());
+    const int D = t->info.ndim;
+    int* off = (int*) malloc((size_t) ne * D * sizeof(int));
+    double* coef = (double*) malloc(nc * ne * sizeof(double));
+    double* rhs = (double*) malloc(nc * sizeof(double));
+    double* x = (double*) calloc(nc, sizeof(double));
+    rc = or_assemble(&t->mesh, descs, datas, s->n_leaves, s->unknown, s->nodes, s->n_nodes, s->params.pin_value, &ne, off, coef, rhs, &nc);
+    int dims[3] = {1, 1, 1}, it = 0, nl = 0;
+    double rel = 0.;
+    for (int d = 0; d < D; ++d) dims[d] = t->info.assignable[d][1] - t->info.assignable[d][0];
+    /* initial guess: the target's values (HYPREEqnSolveHandler::initx), unless zero_guess */
+    double* x0 = s->params.zero_guess ? NULL : (double*) malloc(nc * sizeof(double));
+    if (x0)
+        for (size_t c = 0; c < nc; ++c) x0[c] = t->data[assignable_index(&t->info, dims, c)];
+    if (!rc) rc = or_pfmg_pcg_x0(D, dims, ne, off, coef, rhs, x0, x, s->params.tol, s->params.max_iter, 1, 1, &it, &rel, &nl);
+    free(x0);
+    if (!rc) {
+        /* the solution into the target's assignable cells, then its padding */
+        for (size_t c = 0; c < nc; ++c) t->data[assignable_index(&t->info, dims, c)] = x[c];
+        rc = or_update_padding(&t->mesh, &t->desc, t->data);
+    }
+    free(off);
+    free(coef);
+    free(rhs);
+    free(x);
+    if (rc) return failm(rc, or_last_error());
+    if (state) {
+        memset(state, 0, sizeof *state);
+        state->iterations = it;
+        state->rel_residual = rel;
+        state->converged = rel <= s->params.tol;
+    }
+    return OPFLOW_OK;
+}
+
+int opflow_solver_destroy(opflow_solver s) {
+    if (!s) return OPFLOW_OK;
+    free(s->nodes);
+    free(s);
+    return OPFLOW_OK;
+}

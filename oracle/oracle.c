@@ -1698,8 +1698,20 @@ static void pf_precond(Pfmg* P, const double* r, double* z, int cycles, double* 
     }
 }
 
+int or_pfmg_pcg_x0(int D, const int* dims_in, int ne, const int* off, const double* coef, const double* rhs, const double* x0,
+                   double* x_out, double tol, int maxit, int precond_cycles, int threads, int* iters, double* relres, int* levels);
+
 int or_pfmg_pcg(int D, const int* dims_in, int ne, const int* off, const double* coef, const double* rhs, double* x_out, double tol,
                 int maxit, int precond_cycles, int threads, int* iters, double* relres, int* levels) {
+    return or_pfmg_pcg_x0(D, dims_in, ne, off, coef, rhs, NULL, x_out, tol, maxit, precond_cycles, threads, iters, relres, levels);
+}
+
+/* As or_pfmg_pcg, from the initial guess x0 (NULL: zero).  HYPREEqnSolveHandler::initx
+ * (src/Core/Equation/HYPREEqnSolveHandler.hpp:119) loads the target's values into x before every
+ * solve; hypre_PCGSolve (external/hypre/src/krylov/pcg.c) then starts from r = b - A x0 and runs at
+ * least one iteration before its first convergence test. */
+int or_pfmg_pcg_x0(int D, const int* dims_in, int ne, const int* off, const double* coef, const double* rhs, const double* x0,
+                   double* x_out, double tol, int maxit, int precond_cycles, int threads, int* iters, double* relres, int* levels) {
     Pfmg* P = (Pfmg*) calloc(1, sizeof(Pfmg));
     if (!P) return OPFLOW_E_NOMEM;
     const int nt = threads > 0 ? threads : 1;
@@ -1722,14 +1734,18 @@ int or_pfmg_pcg(int D, const int* dims_in, int ne, const int* off, const double*
     for (int k = 0; k < L0->n[2]; ++k)
         for (int j = 0; j < L0->n[1]; ++j) {
             long long q = pf_lin(L0, 0, j, k);
-            for (int i = 0; i < L0->n[0]; ++i, ++q, ++c) b[q] = rhs[c];
+            for (int i = 0; i < L0->n[0]; ++i, ++q, ++c) {
+                b[q] = rhs[c];
+                if (x0) x[q] = x0[c];
+            }
         }
-    /* PCG (pcg.c), x0 = 0, two-norm test <r,r>/<b,b> < tol^2 */
+    /* PCG (pcg.c), two-norm test <r,r>/<b,b> < tol^2 */
     const double bi = pf_dot(L0, b, b);
     int it = 0;
     if (bi > 0.) {
         const double eps = tol * tol;
-        memcpy(r, b, G * 8);
+        if (x0) pf_residual(L0, x, b, r);
+        else memcpy(r, b, G * 8);
         pf_precond(P, r, p, precond_cycles, tmp);
         double gamma = pf_dot(L0, r, p);
         while (it < maxit) {

@@ -309,6 +309,27 @@ static int run_logic(int nx, int ny, uint64_t seed) {
     return 0;
 }
 
+// examples/FTCS2D/FTCS-OMP.cpp's computation: n x n nodes on [0,1]^2, Dirichlet 1 on every side, u = 0,
+// dt = 0.1 / (n-1)^2, alpha = 1, `steps` updates u = u + dt*alpha*(d2x(u) + d2y(u)).
+static int run_ftcs_omp(int n, int steps) {
+    using Mesh = CartesianMesh<Meta::int_<2>>;
+    using Field = CartesianField<Real, Mesh>;
+    auto mesh = MeshBuilder<Mesh>().newMesh(n, n).setMeshOfDim(0, 0., 1.).setMeshOfDim(1, 0., 1.).build();
+    auto u = ExprBuilder<Field>()
+                     .setName("u")
+                     .setMesh(mesh)
+                     .setBC(0, DimPos::start, BCType::Dirc, 1.)
+                     .setBC(0, DimPos::end, BCType::Dirc, 1.)
+                     .setBC(1, DimPos::start, BCType::Dirc, 1.)
+                     .setBC(1, DimPos::end, BCType::Dirc, 1.)
+                     .build();
+    u = 0;
+    const Real dt = 0.1 / Math::pow2(n - 1), alpha = 1.0;
+    for (int i = 1; i <= steps; ++i) u = u + dt * alpha * (d2x<D2SecondOrderCentered>(u) + d2y<D2SecondOrderCentered>(u));
+    dump_field(u, "u");
+    return 0;
+}
+
 // examples/CONV1D: first-order upwind convection of a square pulse, u = u - dt*c*dx<Downwind>(u).
 static int run_conv1d(int n, int steps) {
     using Mesh = CartesianMesh<Meta::int_<1>>;
@@ -673,6 +694,7 @@ int main(int argc, char** argv) {
     else if (cmd == "padding") rc = run_padding(I(3), I(4), I(5), I(6), I(7), I(8));
     else if (cmd == "ops") rc = run_ops(I(3), I(4), std::strtoull(argv[5], nullptr, 10));
     else if (cmd == "rawbinary") rc = run_rawbinary(argv[3], std::strtoull(argv[4], nullptr, 10));
+    else if (cmd == "ftcs_omp") rc = run_ftcs_omp(I(3), I(4));
     else if (cmd == "conv1d") rc = run_conv1d(I(3), I(4));
     else if (cmd == "logic") rc = run_logic(I(3), I(4), std::strtoull(argv[5], nullptr, 10));
     else if (cmd == "assemble") rc = run_assemble(argv[3], argc > 4 ? I(4) : 0);

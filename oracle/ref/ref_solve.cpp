@@ -125,10 +125,47 @@ static int run_var3d(int n, uint64_t seed, const SolveOpts& o) {
             true, o);
 }
 
+// The program tests/adapter/poisson_solve.cpp (OpFlow's own API) on the reference itself: -Lap(p) = f,
+// f = sin(3x) cos(2y), on n x n cells, Dirichlet 0, PCG (tol, maxIter; HYPRE's default norm) + PFMG with
+// its defaults; one Solve (UnifiedSolve.hpp:36-43: a handler and one solve), then one handler solved
+// twice.  Each solve starts from p's current values (HYPREEqnSolveHandler::initx).
+static int run_program2d(int n, const SolveOpts& o) {
+    using Mesh = CartesianMesh<Meta::int_<2>>;
+    using Field = CartesianField<Real, Mesh>;
+    auto m = MeshBuilder<Mesh>().newMesh(n + 1, n + 1).setMeshOfDim(0, 0., 1.).setMeshOfDim(1, 0., 1.).build();
+    auto b = ExprBuilder<Field>().setMesh(m).setName("p").setLoc(LocOnMesh::Center).setExt(1);
+    for (int d = 0; d < 2; ++d) {
+        b.setBC(d, DimPos::start, BCType::Dirc, 0.);
+        b.setBC(d, DimPos::end, BCType::Dirc, 0.);
+    }
+    auto p = b.build();
+    auto f = p;
+    f.initBy([](auto&& x) { return std::sin(3.0 * x[0]) * std::cos(2.0 * x[1]); });
+    p = 0.;
+    StructSolverParams<StructSolverType::PCG> params;
+    params.tol = o.tol;
+    params.maxIter = o.max_iter;
+    StructSolverParams<StructSolverType::PFMG> pp;
+    auto eqn = [&](auto&& e) { return f == d2x<D2SecondOrderCentered>(e) + d2y<D2SecondOrderCentered>(e); };
+    auto record = [&](const EqnSolveState& st) {
+        fprintf(g_out, "SOLVE {\"niter\":%d,\"relres\":%.17g}\n", st.niter, st.relerr);
+    };
+    {
+        auto solver = PrecondStructSolver<StructSolverType::PCG, StructSolverType::PFMG>(params, pp);
+        record(makeEqnSolveHandler(eqn, p, solver)->solve());
+    }
+    dump_field(p, "x_solve");
+    auto solver = PrecondStructSolver<StructSolverType::PCG, StructSolverType::PFMG>(params, pp);
+    auto handler = makeEqnSolveHandler(eqn, p, solver);
+    for (int k = 0; k < 2; ++k) record(handler->solve());
+    dump_field(p, "x");
+    return 0;
+}
+
 int main(int argc, char** argv) {
     if (argc < 5) {
         fprintf(stderr,
-                "usage: ref_solve <out.bin> neum2d|dirc2d|var3d <n> <seed> [tol] [maxIter] [twoNorm] [pfmgCycles]\n");
+                "usage: ref_solve <out.bin> neum2d|dirc2d|var3d|program2d <n> <seed> [tol] [maxIter] [twoNorm] [pfmgCycles]\n");
         return 2;
     }
     g_out = fopen(argv[1], "wb");
@@ -145,6 +182,7 @@ int main(int argc, char** argv) {
     if (cmd == "neum2d") rc = run_poisson2d("neum", n, seed, o);
     else if (cmd == "dirc2d") rc = run_poisson2d("dirc", n, seed, o);
     else if (cmd == "var3d") rc = run_var3d(n, seed, o);
+    else if (cmd == "program2d") rc = run_program2d(n, o);
     else {
         fprintf(stderr, "unknown case %s\n", cmd.c_str());
         rc = 2;
