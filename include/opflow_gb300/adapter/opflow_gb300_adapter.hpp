@@ -21,6 +21,12 @@
 // values after every assignment, exactly as with the CPU loop (evaluation mode EXACT: bit-identical to
 // the reference; OPFLOW_GB300_EVAL=fast selects the fixed-point mode).
 //
+// What a solve does here.  makeEqnSolveHandler(getter, target, solver) with a Struct solver and a
+// CartesianField target, and Solve(...), return a handler whose solve() runs on the engine's Krylov +
+// multigrid solver (the section "the implicit path" below); the equation is lowered like an
+// assignment's expression.  The relative tolerance is tested on ||b - Ax||_2 / ||b||_2 (HYPRE PCG's
+// default test is the preconditioned norm unless twoNorm is set).
+//
 // Pieces of OpFlow that need libraries this engine does not use are left out by defining their include
 // guards first: the AMGCL back end and UnifiedSolve.hpp (Boost), the CSR matrix generation of the
 // AMGCL path (CSRMatrixGenerator, EquationHolder, StencilHolder, DS::CSRMatrix: oneTBB's parallel
