@@ -185,6 +185,38 @@ def cpu_ftcs_sample(workload, threads, reps):
     return pts / dt / 1e9, "%s: %d^%d nodes x %d steps on %d host threads (oracle port, %.1f s)" % (workload, n, D, reps, used, dt), used
 
 
+def cpu_weno_sample(threads, lines=16384, reps=1):
+    """The oracle's three WENO5-RK3 stage assignments (the reference's operation order) on a bounded
+    sample of the workload: `lines` periodic lines of 4096 cells with the benchmark's pulses, `reps` RK3
+    steps, on all host threads; returns (G cell-updates per RK3 step / s, sample description, threads)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import common as cm
+    import oracle_lib as orc
+    from opflow_gb300 import _capi as capi
+    from opflow_gb300 import api
+    used = orc.lib().or_set_threads(threads)
+    nx = 4096
+    mesh = cm.mesh_uniform([nx + 1, lines + 1])
+    fd = cm.field_desc(2, capi.CENTER, [(capi.BC_PERIODIC, capi.BC_PERIODIC)] * 2, ext=3)
+    h0 = orc.HostField(mesh, fd)
+    rng = h0.assignable()
+    h0.data[h0.slices(rng)] = wl.weno_u0(2024, nx, lines)
+    h0.update_padding()
+    h1 = orc.HostField(mesh, fd, data=h0.data.copy())
+    h2 = orc.HostField(mesh, fd, data=h0.data.copy())
+    L = [cm.Leaf("u"), cm.Leaf("u1"), cm.Leaf("u2")]
+    ns = [api.serialize(x, L)[0] for x in cm.weno_stage_exprs(L[0], L[1], L[2], 0.5 / nx)]
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        orc.assign(h1, ns[0], [h0, h1, h2])
+        orc.assign(h2, ns[1], [h0, h1, h2])
+        orc.assign(h0, ns[2], [h0, h1, h2])
+    dt = time.perf_counter() - t0
+    return (nx * lines * reps / dt / 1e9,
+            "weno: %d lines x 4096 cells x %d RK3 step(s) on %d host threads (oracle port of the three stage assignments, %.1f s)"
+            % (lines, reps, used, dt), used)
+
+
 def served_population(reqs):
     """Every linear system a served window solves: a one-shot request once, a session once per step
     (each step re-solves the session's operator with a new right-hand side)."""
@@ -709,26 +741,111 @@ def explicit_record(torch, api, capi, np, ctx, stream, local, rank, steps=20, wa
     w.upload(host)
     del host
     dt = 0.5 / nx
-    api.weno_rk3(w, dt, warmup)
-    torch.cuda.synchronize()
-    k = max(2, steps // 4)
-    l0 = capi.launch_count()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clk:
-        ev0.record(stream)
-        api.weno_rk3(w, dt, k)
-        ev1.record(stream)
+    for mode, k in (("exact", max(2, steps // 4)), ("fast", max(2, steps // 2))):
+        m = capi.EVAL_FAST if mode == "fast" else capi.EVAL_EXACT
+        api.weno_rk3(w, dt, warmup, mode=m)
         torch.cuda.synchronize()
-    ms = ev0.elapsed_time(ev1) / k
-    rate = nx * ny / (ms * 1e-3) / 1e9
-    out["weno_65536x4096"] = {"gpts_per_s": rate, "ms_per_rk3_step": ms, "steps": k, "launches": capi.launch_count() - l0,
-                              "achieved_gbs": 16.0 * rate, "frac": 16.0 * rate / peak, "bytes_per_point_rk3_step": 16,
-                              "clocks": clk.summary()}
+        l0 = capi.launch_count()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with ClockSampler(local) as clk:
+            ev0.record(stream)
+            api.weno_rk3(w, dt, k, mode=m)
+            ev1.record(stream)
+            torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1) / k
+        rate = nx * ny / (ms * 1e-3) / 1e9
+        out["weno_65536x4096_" + mode] = {"gpts_per_s": rate, "ms_per_rk3_step": ms, "steps": k, "launches": capi.launch_count() - l0,
+                                          "achieved_gbs": 16.0 * rate, "frac": 16.0 * rate / peak, "bytes_per_point_rk3_step": 16,
+                                          "bound": "float64 issue", "clocks": clk.summary()}
     del w
     return out
 
 
 # ------------------------------------------------------------------------------------------- ours
+def run_weno(args, torch, api, capi, np, ctx, stream, world, rank, local, dist):
+    """WENO5-JS + Shu-Osher RK3 advection on 65536 periodic lines of 4096 cells (square and cosine
+    pulses, dt = 0.5 h): one bench step is one RK3 step of every line (opflow_weno_rk3_mode, all stages
+    in shared memory).  `value` runs `--steps` steps in one launch with the field resident; `e2e` uploads
+    the field from pinned host memory, takes one RK3 step and downloads it, per step."""
+    nx, ny = 4096, args.lines or 65536
+    mesh = api.MeshBuilder().newMesh(nx + 1, ny + 1).setMeshOfDim(0, 0.0, 1.0).setMeshOfDim(1, 0.0, ny / nx).build()
+    b = api.ExprBuilder().setMesh(mesh).setName("u").setLoc(api.LocOnMesh.Center).setExt(3)
+    for d in range(2):
+        b.setBC(d, api.DimPos.start, api.BCType.Periodic, 0.0).setBC(d, api.DimPos.end, api.BCType.Periodic, 0.0)
+    w = b.build(ctx)
+    a = w.download()
+    a[w.index_slices(w.assignableRange)] = wl.weno_u0(2024 + rank, nx, ny)
+    host = torch.empty(a.size, dtype=torch.float64, pin_memory=True)
+    host.numpy()[:] = a.reshape(-1)
+    del a
+    cnt = host.numel()
+    P = C.POINTER(C.c_double)
+    L = capi.lib()
+    capi.check(L.opflow_field_upload(w.handle, C.cast(host.data_ptr(), P), cnt))
+    dt = 0.5 / nx
+    m = capi.EVAL_FAST if args.mode == "fast" else capi.EVAL_EXACT
+    api.weno_rk3(w, dt, max(3, args.warmup), mode=m)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    l0 = capi.launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        api.weno_rk3(w, dt, args.steps, mode=m)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    launches = capi.launch_count() - l0
+    ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        dist.barrier()
+        tt = torch.tensor([ms], device=torch.device("cuda", local))
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    pts = nx * ny
+    value = pts * args.steps * world / (ms * 1e-3) / 1e9
+    # end to end: upload, one RK3 step, download, per step
+    e2e_steps = max(1, min(args.steps, 3))
+    t0 = time.perf_counter()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        capi.check(L.opflow_field_upload(w.handle, C.cast(host.data_ptr(), P), cnt))
+        api.weno_rk3(w, dt, 1, mode=m)
+        capi.check(L.opflow_field_download(w.handle, C.cast(host.data_ptr(), P), cnt))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = max(e0.elapsed_time(e1), (time.perf_counter() - t0) * 1e3)
+    peak, peak_src = peak_hbm()
+    ms_step = ms / args.steps
+    achieved = 16.0 * pts / (ms_step * 1e-3) / 1e9
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            v, sample, used = cpu_weno_sample(os.cpu_count() or 1)
+            cpu = {"value": v, "unit": "Gpts/s", "cores": used, "kind": "port", "sample": sample}
+        except Exception as ex:  # the baseline is reported, never required
+            cpu = {"value": None, "unit": "Gpts/s", "cores": 0, "kind": "port", "sample": "failed: %s" % ex}
+    line = {"metric": METRIC, "value": value, "unit": "Gpts/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "weno", "lines": ny, "cells_per_line": nx, "mode": args.mode, "dt": "0.5 h", "init": "seeded square + cosine pulses",
+                       "l2": "field 2.1 GB > L2; the run keeps each line in shared memory across its steps",
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_src,
+                         "traffic": None, "kernel": "weno_rk3_kernel<16, false, %s, 2>" % ("true" if m == capi.EVAL_FAST else "false"),
+                         "algorithmic_bytes_per_launch": 16.0 * pts,
+                         "note": "float64-issue-bound: HBM carries 16 B per point per launch of --steps RK3 steps"},
+            "cpu_baseline": cpu,
+            "e2e": {"value": pts * e2e_steps / (e2e_ms * 1e-3) / 1e9, "unit": "Gpts/s", "h2d_bytes_per_step": cnt * 8,
+                    "d2h_bytes_per_step": cnt * 8, "steps": e2e_steps},
+            "gpu_launches": launches, "clocks": clk.summary()}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
 def run_ftcs_batch(args, torch, api, capi, np, ctx, stream, world, rank, local, dist):
     """Explicit steps of many uneven grids in one launch per step: 256 2D node grids of side LogU[65,513]
     (seeded), Dirichlet 0, u = u + 0.2 h^2 (d2x(u) + d2y(u)) in exact mode, batched (opflow_assign_batch)
@@ -1000,6 +1117,7 @@ def main():
     ap.add_argument("--rate", default="50,200,2000", help="serve: Poisson arrival rates (requests/s), comma-separated; the last is the headline")
     ap.add_argument("--mode", default="fast", choices=["fast", "exact"])
     ap.add_argument("--grid", type=int, default=0, help="override the grid side (profiling a smaller case)")
+    ap.add_argument("--lines", type=int, default=0, help="weno: override the number of lines (profiling a smaller case)")
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU baseline leg (profiling runs)")
     ap.add_argument("--no-explicit", action="store_true", help="serve: skip the explicit-path record (profiling runs)")
     ap.add_argument("--sweeps", type=int, default=2, help="poisson2d: red-black Gauss-Seidel sweeps before and after each coarsening")

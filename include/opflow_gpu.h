@@ -267,6 +267,16 @@ int opflow_assign_repeat(opflow_ctx ctx, opflow_field dst, int arith, const opfl
  * `kind` is OPFLOW_NODE_WENO53_DOWN or OPFLOW_NODE_WENO53_UP.  u1 and u2 receive the stage fields. */
 int opflow_weno_rk3(opflow_ctx ctx, opflow_field u, opflow_field u1, opflow_field u2, int kind, int dim, double dt, int steps);
 
+/* opflow_weno_rk3 with an evaluation mode.  OPFLOW_EVAL_EXACT is opflow_weno_rk3.  OPFLOW_EVAL_FAST
+ * evaluates the same scheme with contracted (fused multiply-add) arithmetic and the nonlinear weights
+ * w_k = (c_k / q_k^2) / sum_j (c_j / q_j^2) through one reciprocal instead of six divisions; it is not
+ * bit-identical: max |u_fast - u_exact| <= 4 ulps of max |u| after one RK3 step and <= 1e-14 * max |u|
+ * after 20 on periodic lines with square and cosine pulses (the tested bounds).  Over longer runs the
+ * scheme's own sensitivity dominates: WENO5-JS moves the exact result by up to 1e-8 after 100 steps
+ * when its input moves by one ulp, and FAST stays within that spread. */
+int opflow_weno_rk3_mode(opflow_ctx ctx, opflow_field u, opflow_field u1, opflow_field u2, int kind, int dim, double dt, int steps,
+                         int mode);
+
 /* ---- implicit path (path I) -------------------------------------------------------------------- */
 /* The equation `lhs == rhs` is given as the tree of `lhs - rhs` (Equation.hpp:41-55) in which the
  * unknown appears as the leaf slot `unknown_slot`; the other leaves are known fields.  This replaces

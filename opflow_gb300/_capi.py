@@ -138,6 +138,7 @@ _SIGS = {
     "opflow_assign_repeat": [C.c_void_p, C.c_void_p, C.c_int, C.POINTER(Node), C.c_int, C.POINTER(C.c_void_p), C.c_int,
                              C.c_int, C.c_int],
     "opflow_weno_rk3": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_int],
+    "opflow_weno_rk3_mode": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int],
     "opflow_assemble": [C.c_void_p, C.c_void_p, C.POINTER(Node), C.c_int, C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_int,
                         C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_double),
                         C.POINTER(C.c_size_t)],

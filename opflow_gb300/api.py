@@ -906,13 +906,15 @@ def assemble(getter, target, pin=False):
     return off.reshape(ne.value, D), coef.reshape(nc.value, ne.value), rhs
 
 
-def weno_rk3(u, dt, steps=1, upwind=False, dim=0, u1=None, u2=None):
+def weno_rk3(u, dt, steps=1, upwind=False, dim=0, u1=None, u2=None, mode=None):
     """One or more Shu-Osher RK3 steps of u_t + d1<WENO53>(u) = 0 along a periodic dim, fused
-    (opflow_weno_rk3); identical to the three assignments
-        u1 = u - dt*d1<W>(u); u2 = 0.75*u + 0.25*(u1 - dt*d1<W>(u1)); u = 1/3*u + 2/3*(u2 - dt*d1<W>(u2))."""
+    (opflow_weno_rk3_mode); in EXACT mode (the default) identical to the three assignments
+        u1 = u - dt*d1<W>(u); u2 = 0.75*u + 0.25*(u1 - dt*d1<W>(u1)); u = 1/3*u + 2/3*(u2 - dt*d1<W>(u2)).
+    mode=EvalMode.FAST: contracted arithmetic and one reciprocal for the weights (not bit-identical)."""
     kind = capi.NODE_WENO53_UP if upwind else capi.NODE_WENO53_DOWN
-    check(lib().opflow_weno_rk3(u.ctx.handle, u.handle, u1.handle if u1 else None, u2.handle if u2 else None, kind, dim, float(dt),
-                                int(steps)))
+    m = capi.EVAL_EXACT if mode is None else int(mode)
+    check(lib().opflow_weno_rk3_mode(u.ctx.handle, u.handle, u1.handle if u1 else None, u2.handle if u2 else None, kind, dim, float(dt),
+                                     int(steps), m))
 
 
 # ---------------------------------------------------------------------------------------------- batches

@@ -119,6 +119,64 @@ def test_weno_rk3_fused_4096_lines_matches_oracle(ctx):
     assert np.array_equal(u.download(), h0.data)
 
 
+def _weno_lines(ctx, nx, ny, seed):
+    from opflow_gb300 import workloads as wl
+    mesh = api.MeshBuilder().newMesh(nx + 1, ny + 1).setMeshOfDim(0, 0.0, 1.0).setMeshOfDim(1, 0.0, ny / nx).build()
+    b = api.ExprBuilder().setMesh(mesh).setLoc(api.LocOnMesh.Center).setExt(3)
+    for d in range(2):
+        b.setBC(d, api.DimPos.start, api.BCType.Periodic, 0.0).setBC(d, api.DimPos.end, api.BCType.Periodic, 0.0)
+    fields = [b.setName(nm).build(ctx) for nm in ("exact", "fast")]
+    host = fields[0].download()
+    host[fields[0].index_slices(fields[0].assignableRange)] = wl.weno_u0(seed, nx, ny)
+    for f in fields:
+        f.upload(host)
+    return fields, float(np.abs(host).max())
+
+
+@pytest.mark.parametrize("ny,steps,upwind", [(65536, 1, False), (65536, 20, False), (1024, 1, True)])
+def test_weno_rk3_fast_mode_within_1e14_of_exact(ctx, ny, steps, upwind):
+    """FAST mode (contracted arithmetic, one reciprocal for the nonlinear weights) against the bit-exact
+    kernel on 4096-cell periodic lines with square and cosine pulses (the benchmark's data), at the
+    benchmark's 65536 lines: within 4 ulps of max|u| after one RK3 step, within 1e-14 * max|u| after 20
+    (the bound stated in opflow_weno_rk3_mode's contract).  The Upwind operator in u_t + L(u) = 0 is
+    the downstream-biased stencil, which amplifies differences from step to step, so it is compared
+    over one step."""
+    nx = 4096
+    (ue, uf), umax = _weno_lines(ctx, nx, ny, 77)
+    dt = 0.5 / nx
+    api.weno_rk3(ue, dt, steps, upwind=upwind)
+    api.weno_rk3(uf, dt, steps, upwind=upwind, mode=capi.EVAL_FAST)
+    a, b = ue.download(), uf.download()
+    err = float(np.abs(a - b).max())
+    assert np.isfinite(b).all()
+    assert err <= (4 * 2.0 ** -52 if steps == 1 else 1e-14) * umax, err
+    assert err > 0.0  # FAST is a different evaluation, not the exact one
+
+
+def test_weno_rk3_fast_mode_long_runs_stay_within_the_schemes_own_sensitivity(ctx):
+    """Over 100 RK3 steps WENO5-JS amplifies rounding-level differences at the pulses' edges (the
+    nonlinear weights switch there): the exact scheme started from data moved by one ulp ends up to
+    ~1e-8 away from itself.  FAST's distance from EXACT after 100 steps stays below that distance."""
+    nx, ny, steps = 4096, 1024, 100
+    (ue, uf), umax = _weno_lines(ctx, nx, ny, 77)
+    host = ue.download()
+    sl = ue.index_slices(ue.assignableRange)
+    v = host[sl]
+    nz = v != 0
+    v[nz] = np.nextafter(v[nz], 2.0)
+    host[sl] = v
+    (up_, _), _ = _weno_lines(ctx, nx, ny, 77)
+    up_.upload(host)
+    dt = 0.5 / nx
+    api.weno_rk3(ue, dt, steps)
+    api.weno_rk3(up_, dt, steps)
+    api.weno_rk3(uf, dt, steps, mode=capi.EVAL_FAST)
+    a = ue.download()
+    ulp_spread = float(np.abs(up_.download() - a).max())
+    fast_err = float(np.abs(uf.download() - a).max())
+    assert 0.0 < fast_err <= ulp_spread, (fast_err, ulp_spread)
+
+
 PAD = sorted(f[:-4] for f in os.listdir(cm.GOLDEN) if f.startswith("pad_"))
 
 
