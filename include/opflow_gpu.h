@@ -382,6 +382,28 @@ typedef struct {
 
 int opflow_batch_create(opflow_ctx ctx, const opflow_problem_desc* problems, int n_problems,
                         const opflow_solve_params* params, opflow_batch* out);
+
+/* A user equation, as opflow_solver_create takes it (the equation of a makeEqnSolveHandler,
+ * HYPREEqnSolveHandler.hpp:44-108): the tree of lhs - rhs over `leaves`, the unknown as leaf slot
+ * `unknown` (its field is the target).  Any StencilPad-generated equation whose stencil is the
+ * (2*dim+1)-point star: variable coefficients, mixed boundary conditions, Helmholtz terms. */
+typedef struct {
+    const opflow_node* nodes;
+    int n_nodes;
+    const opflow_field* leaves;
+    int n_leaves;
+    int unknown;
+} opflow_equation;
+
+/* A batch of user equations (any sizes, any mix of operators) solved together like
+ * opflow_batch_create's problems.  Each problem is assembled from its fields at creation (generateAb);
+ * its right-hand side is the equation's (opflow_batch_set may replace it) and its initial guess the
+ * target's values (HYPREEqnSolveHandler::initx).  A singular problem (zero row sums, no Dirichlet
+ * side) is pinned as opflow_solver_solve pins it when params->pin_value, else its right-hand side is
+ * projected to zero mean.  The solution stays in the batch (opflow_batch_get / opflow_batch_vectors);
+ * the target fields are not written. */
+int opflow_batch_create_eqns(opflow_ctx ctx, const opflow_equation* eqns, int n_eqns, const opflow_solve_params* params,
+                             opflow_batch* out);
 /* Device pointers of problem i's unknown vector and right-hand side (x fastest over the unknowns). */
 int opflow_batch_vectors(opflow_batch b, int i, double** x, double** f, size_t* n_unknowns);
 /* Host copies: set problem i's right-hand side (and, unless x0 is NULL, its initial guess); read its
@@ -409,6 +431,14 @@ typedef struct {
     double* x_out;               /* buffer for the final solution, n unknowns, host or device (may be NULL) */
     const double* x0;            /* initial guess of the first solve, n unknowns, host or device (NULL: zero);
                                     a session restored from a checkpoint passes the checkpoint here and as f */
+    const opflow_equation* equation; /* NULL: the request is `problem`.  Otherwise a user equation (the
+                                    problem is ignored): it is assembled from its fields at admission, so
+                                    the fields must stay alive and unchanged until the request's result is
+                                    available.  steps must be 1 and f NULL (the right-hand side is the
+                                    equation's); x0 NULL starts from the target's values (initx); x_out
+                                    receives the solution over the target's assignable cells (x fastest);
+                                    the target field itself is not written.  A singular equation is pinned
+                                    when the server's params->pin_value, else projected to zero mean. */
 } opflow_request;
 
 typedef struct {

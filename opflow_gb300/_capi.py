@@ -77,9 +77,14 @@ class ProblemDesc(C.Structure):
                 ("alpha", C.c_double), ("beta", C.c_double)]
 
 
+class Equation(C.Structure):
+    _fields_ = [("nodes", C.POINTER(Node)), ("n_nodes", C.c_int), ("leaves", C.POINTER(C.c_void_p)), ("n_leaves", C.c_int),
+                ("unknown", C.c_int)]
+
+
 class Request(C.Structure):
     _fields_ = [("problem", ProblemDesc), ("steps", C.c_int), ("f", C.POINTER(C.c_double)), ("x_out", C.POINTER(C.c_double)),
-                ("x0", C.POINTER(C.c_double))]
+                ("x0", C.POINTER(C.c_double)), ("equation", C.POINTER(Equation))]
 
 
 class RequestResult(C.Structure):
@@ -148,6 +153,7 @@ _SIGS = {
     "opflow_solver_solve": [C.c_void_p, C.POINTER(SolveState)],
     "opflow_solver_destroy": [C.c_void_p],
     "opflow_batch_create": [C.c_void_p, C.POINTER(ProblemDesc), C.c_int, C.POINTER(SolveParams), C.POINTER(C.c_void_p)],
+    "opflow_batch_create_eqns": [C.c_void_p, C.POINTER(Equation), C.c_int, C.POINTER(SolveParams), C.POINTER(C.c_void_p)],
     "opflow_batch_vectors": [C.c_void_p, C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_size_t)],
     "opflow_batch_solve": [C.c_void_p, C.POINTER(SolveState)],
     "opflow_batch_set": [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_size_t],

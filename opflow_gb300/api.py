@@ -935,17 +935,42 @@ class Problem:
         return d
 
 
+def lower_equation(getter, target):
+    """The C ABI's form of makeEqnSolveHandler's equation: (opflow_equation, keep-alive objects).
+    `getter(e)` returns `lhs == rhs` in the unknown e; the target is leaf slot 0."""
+    eq = getter(target)
+    if not isinstance(eq, Equation):
+        raise TypeError("the equation getter must return `lhs == rhs` (use api.Eq for a scalar lhs)")
+    nodes, leaves = serialize(eq.residual_expr(), [target])
+    hs = (C.c_void_p * len(leaves))(*[f.handle.value for f in leaves])
+    e = capi.Equation()
+    e.nodes = C.cast(nodes, C.POINTER(capi.Node))
+    e.n_nodes = len(nodes)
+    e.leaves = C.cast(hs, C.POINTER(C.c_void_p))
+    e.n_leaves = len(leaves)
+    e.unknown = 0
+    return e, (nodes, hs, leaves)
+
+
 class Batch:
-    """Many independent problems solved together, one launch per multigrid operation for the batch."""
+    """Many independent problems solved together, one launch per multigrid operation for the batch.
+    `problems` holds Problem descriptions, or (getter, target) pairs of user equations
+    (opflow_batch_create_eqns: each assembled from its fields, started from its target's values)."""
 
     def __init__(self, problems, params=None, ctx=None):
         self.ctx = ctx or default_context()
         self.problems = list(problems)
-        arr = (capi.ProblemDesc * len(self.problems))(*[p.to_c() for p in self.problems])
         self.params = params or StructSolverParams()
         p = self.params.to_c()
         h = C.c_void_p()
-        check(lib().opflow_batch_create(self.ctx.handle, arr, len(self.problems), C.byref(p), C.byref(h)))
+        if self.problems and isinstance(self.problems[0], tuple):
+            lowered = [lower_equation(g, t) for g, t in self.problems]
+            self._keep = [k for _, k in lowered]
+            arr = (capi.Equation * len(lowered))(*[e for e, _ in lowered])
+            check(lib().opflow_batch_create_eqns(self.ctx.handle, arr, len(lowered), C.byref(p), C.byref(h)))
+        else:
+            arr = (capi.ProblemDesc * len(self.problems))(*[q.to_c() for q in self.problems])
+            check(lib().opflow_batch_create(self.ctx.handle, arr, len(self.problems), C.byref(p), C.byref(h)))
         self.handle = h
 
     def size(self, i):
@@ -1081,6 +1106,28 @@ class Server:
         rid = C.c_longlong(0)
         check(lib().opflow_server_submit(self.handle, C.byref(req), C.byref(rid)))
         self._keep[rid.value] = (f, out, x0)
+        return rid.value
+
+    def submit_equation(self, getter, target, out=None, x0=None):
+        """Queues one solve of a user equation (`getter(e)` returns `lhs == rhs` in the unknown e, as
+        for makeEqnSolveHandler): assembled from its fields at admission, so they must stay unchanged
+        until the result; started from the target's values unless x0 is given; the solution over the
+        target's assignable cells goes to `out` (the target itself is not written)."""
+        e, keep = lower_equation(getter, target)
+        req = capi.Request()
+        req.steps = 1
+        req.equation = C.pointer(e)
+        if x0 is not None:
+            x0, req.x0 = self._ptr(x0)
+        if out is not None:
+            if hasattr(out, "data_ptr") and getattr(out, "is_cuda", False):
+                out, req.x_out = self._ptr(out)
+            else:
+                assert out.dtype == np.float64 and out.flags["C_CONTIGUOUS"]
+                req.x_out = out.ctypes.data_as(C.POINTER(C.c_double))
+        rid = C.c_longlong(0)
+        check(lib().opflow_server_submit(self.handle, C.byref(req), C.byref(rid)))
+        self._keep[rid.value] = (e, keep, out, x0)
         return rid.value
 
     def checkpoint(self, rid, n):

@@ -45,8 +45,10 @@ using namespace opg;
 struct opflow_batch_s {
     opflow_ctx ctx;
     MGSystem* S = nullptr;
-    std::vector<opflow_field> fields;  // targets and right-hand-side fields
+    std::vector<opflow_field> fields;  // targets and right-hand-side fields (owned: problem batches only)
     opflow_solve_params params;
+    // equation batches: per problem, whether it is pinned (singular, no Dirichlet side, pin_value)
+    std::vector<char> pinned;
 };
 
 int opg::batch_problem_fields(opflow_ctx ctx, const opflow_problem_desc& pd, opflow_field* tgt, opflow_field* rhs) {
@@ -82,6 +84,20 @@ int opg::batch_problem_fields(opflow_ctx ctx, const opflow_problem_desc& pd, opf
     return OPFLOW_OK;
 }
 
+static MGSystem* new_batch_system(opflow_batch_s* B) {
+    B->S = new MGSystem();
+    MGSystem* S = B->S;
+    S->ctx = B->ctx;
+    S->arena.ctx = B->ctx;
+    S->precision = B->params.precision;
+    S->pre = B->params.pre_sweeps;
+    S->post = B->params.post_sweeps;
+    S->coarse_max = B->params.coarse_max > 0 ? B->params.coarse_max : 64;
+    S->tol = B->params.tol;
+    S->max_iter = B->params.max_iter;
+    return S;
+}
+
 extern "C" {
 
 int opflow_batch_create(opflow_ctx ctx, const opflow_problem_desc* problems, int n_problems, const opflow_solve_params* params, opflow_batch* out) {
@@ -90,16 +106,7 @@ int opflow_batch_create(opflow_ctx ctx, const opflow_problem_desc* problems, int
     B->ctx = ctx;
     if (params) B->params = *params;
     else opflow_solve_params_default(&B->params);
-    B->S = new MGSystem();
-    MGSystem* S = B->S;
-    S->ctx = ctx;
-    S->arena.ctx = ctx;
-    S->precision = B->params.precision;
-    S->pre = B->params.pre_sweeps;
-    S->post = B->params.post_sweeps;
-    S->coarse_max = B->params.coarse_max > 0 ? B->params.coarse_max : 64;
-    S->tol = B->params.tol;
-    S->max_iter = B->params.max_iter;
+    MGSystem* S = new_batch_system(B);
     int rc = OPFLOW_OK;
     for (int p = 0; p < n_problems && rc == OPFLOW_OK; ++p) {
         opflow_field t = nullptr, f = nullptr;
@@ -112,6 +119,44 @@ int opflow_batch_create(opflow_ctx ctx, const opflow_problem_desc* problems, int
         rc = mg_add_problem(S, t, tree.data(), (int) tree.size(), leaves, 2, 0);
     }
     if (rc == OPFLOW_OK) rc = mg_finalize(S);
+    if (rc) {
+        opflow_batch_destroy(B);
+        return rc;
+    }
+    *out = B;
+    return OPFLOW_OK;
+}
+
+int opflow_batch_create_eqns(opflow_ctx ctx, const opflow_equation* eqns, int n_eqns, const opflow_solve_params* params, opflow_batch* out) {
+    if (!ctx || !eqns || n_eqns <= 0 || !out) return fail(OPFLOW_E_INVALID, "bad batch arguments");
+    for (int p = 0; p < n_eqns; ++p) {
+        const opflow_equation& e = eqns[p];
+        if (!e.nodes || e.n_nodes <= 0 || !e.leaves || e.n_leaves <= 0 || e.unknown < 0 || e.unknown >= e.n_leaves)
+            return fail(OPFLOW_E_INVALID, "bad equation %d", p);
+        for (int i = 0; i < e.n_leaves; ++i)
+            if (!e.leaves[i]) return fail(OPFLOW_E_INVALID, "equation %d: null leaf %d", p, i);
+    }
+    auto* B = new opflow_batch_s();
+    B->ctx = ctx;
+    if (params) B->params = *params;
+    else opflow_solve_params_default(&B->params);
+    MGSystem* S = new_batch_system(B);
+    int rc = OPFLOW_OK;
+    for (int p = 0; p < n_eqns && rc == OPFLOW_OK; ++p)
+        rc = mg_add_problem(S, eqns[p].leaves[eqns[p].unknown], eqns[p].nodes, eqns[p].n_nodes, eqns[p].leaves, eqns[p].n_leaves, eqns[p].unknown);
+    if (rc == OPFLOW_OK) rc = mg_finalize(S);
+    // initial guesses: the targets' values (initx); singular problems pinned or projected
+    for (int p = 0; p < n_eqns && rc == OPFLOW_OK; ++p) {
+        ProblemHost& P = S->probs[p];
+        rc = mg_gather_target(ctx, P.target, S->kd_host[p].x);
+        const bool sing = P.singular && !P.has_dirichlet;
+        B->pinned.push_back(sing && B->params.pin_value);
+        if (rc == OPFLOW_OK && sing && !B->params.pin_value) {
+            const long long N = P.levels[0].N;
+            mg_add_scalar(ctx, P.b, N, -mg_sum(ctx, P.b, N) / (double) N);
+        }
+    }
+    if (rc == OPFLOW_OK) rc = cudaStreamSynchronize(ctx->stream) == cudaSuccess ? OPFLOW_OK : fail(OPFLOW_E_CUDA, "batch set-up");
     if (rc) {
         opflow_batch_destroy(B);
         return rc;
@@ -153,9 +198,31 @@ int opflow_batch_solve(opflow_batch b, opflow_solve_state* states) {
     opflow_ctx ctx = b->ctx;
     auto t0 = std::chrono::steady_clock::now();
     if (b->params.zero_guess) OPG_TRY(kr_launch_zero_x(ctx->stream, ctx->num_sms, S->dL, S->dK, S->dk0, S->nk0));
+    // pinned problems (equation batches): the singular system with b[0] := -(sum of the others), then
+    // the shift that makes the pinned unknown 0, and b[0] restored (as opflow_solver_solve does)
+    const int np0 = (int) S->probs.size();
+    std::vector<double> b_pin(np0, 0.);
+    for (int p = 0; p < (int) b->pinned.size(); ++p) {
+        if (!b->pinned[p]) continue;
+        ProblemHost& P = S->probs[p];
+        const long long N = P.levels[0].N;
+        const double sb = mg_sum(ctx, P.b, N);
+        OPG_CUDA(cudaMemcpy(&b_pin[p], P.b, 8, cudaMemcpyDeviceToHost));
+        const double nb0 = -(sb - b_pin[p]);
+        OPG_CUDA(cudaMemcpy(P.b, &nb0, 8, cudaMemcpyHostToDevice));
+    }
     OPG_TRY(mg_solve(S));
     std::vector<Scal> st;
     OPG_TRY(mg_states(S, st));
+    for (int p = 0; p < (int) b->pinned.size(); ++p) {
+        if (!b->pinned[p]) continue;
+        ProblemHost& P = S->probs[p];
+        const long long N = P.levels[0].N;
+        double shift = 0.;
+        OPG_CUDA(cudaMemcpy(&shift, S->kd_host[p].x, 8, cudaMemcpyDeviceToHost));
+        mg_add_scalar(ctx, S->kd_host[p].x, N, -shift);
+        OPG_CUDA(cudaMemcpy(P.b, &b_pin[p], 8, cudaMemcpyHostToDevice));
+    }
     // true residuals of every problem
     const int np = (int) S->probs.size();
     OPG_TRY(kr_launch_apply(ctx->stream, ctx->num_sms, S->dL, S->dK, S->dk0, S->nk0, nullptr, S->partial, 0));
@@ -166,7 +233,13 @@ int opflow_batch_solve(opflow_batch b, opflow_solve_state* states) {
     auto t1 = std::chrono::steady_clock::now();
     int all = 1;
     for (int p = 0; p < np; ++p) {
-        const double bb = red[2 * p], rr = red[2 * p + 1];
+        double bb = red[2 * p], rr = red[2 * p + 1];
+        if (p < (int) b->pinned.size() && b->pinned[p]) {
+            // a pinned problem's true residual in the singular operator is O(||b||) in its pinned row:
+            // its convergence is the flexible PCG's own residual of the pinned system
+            bb = st[p].bb;
+            rr = st[p].rr;
+        }
         const double rel = bb > 0 ? std::sqrt(rr / bb) : std::sqrt(rr);
         if (states) {
             states[p].iterations = st[p].iters;

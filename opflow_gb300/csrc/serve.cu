@@ -26,14 +26,18 @@ namespace opg {
 
 using Clock = std::chrono::steady_clock;
 
-double mg_sum(opflow_ctx ctx, const double* v, long long n);
-void mg_add_scalar(opflow_ctx ctx, double* v, long long n, double a);
 std::vector<opflow_node> helmholtz_tree(int ndim, double alpha, double beta);
 int batch_problem_fields(opflow_ctx ctx, const opflow_problem_desc& pd, opflow_field* tgt, opflow_field* rhs);
 
 struct Req {
     long long id = 0;
     opflow_problem_desc pd{};
+    // a user equation (opflow_request.equation): the tree, the caller's fields and the unknown's slot
+    bool eqn = false;
+    std::vector<opflow_node> nodes;
+    std::vector<opflow_field> leaves;
+    int unknown = 0;
+    size_t est = 0;  // the HBM estimate charged at admission
     int steps = 1;
     const double* f = nullptr;  // the caller's right-hand side, read at admission
     bool f_dev = false;         // f is device memory: checked for non-finite values on the device at admission
@@ -63,6 +67,9 @@ static size_t estimate_bytes(const opflow_problem_desc& pd) {
     for (int d = 0; d < pd.ndim; ++d) n *= (double) (pd.n[d] + 2);
     return (size_t) (n * 240.0) + (8u << 20);
 }
+
+// a user equation also keeps float64 and float32 coefficient arrays on every level
+static size_t estimate_bytes_eqn(long long cells) { return (size_t) ((double) cells * 420.0) + (8u << 20); }
 
 }  // namespace opg
 
@@ -114,7 +121,7 @@ __global__ void flag_nonfinite(const double* __restrict__ v, long long n, int* f
 // hierarchy, right-hand side, pinning, and the seed of the Krylov scalars
 static int setup_req(opflow_server S, Req* r, Scal* seed) {
     opflow_ctx ctx = &S->setup_ctx;
-    OPG_TRY(batch_problem_fields(ctx, r->pd, &r->t, &r->rhs));
+    if (!r->eqn) OPG_TRY(batch_problem_fields(ctx, r->pd, &r->t, &r->rhs));
     r->sys = new MGSystem();
     MGSystem* M = r->sys;
     M->ctx = ctx;
@@ -129,15 +136,26 @@ static int setup_req(opflow_server S, Req* r, Scal* seed) {
     // requests take the tuner's cached choices (from earlier solves of the shape or a cache file): timing
     // here would add to the request's latency and run beside the batch, which would skew it
     M->tune_measure = false;
-    std::vector<opflow_node> tree = helmholtz_tree(r->pd.ndim, r->pd.alpha, r->pd.beta);
-    opflow_field leaves[2] = {r->t, r->rhs};
-    OPG_TRY(mg_add_problem(M, r->t, tree.data(), (int) tree.size(), leaves, 2, 0));
-    OPG_TRY(mg_finalize(M));
-    r->N = M->probs[0].levels[0].N;
-    if (r->nf != r->N) return fail(OPFLOW_E_INVALID, "request %lld: f has %lld values, the problem %lld unknowns", r->id, r->nf, r->N);
-    // f, x0: host or device memory (unified addressing picks the direction)
-    OPG_CUDA(cudaMemcpyAsync(M->probs[0].b, r->f, r->N * 8, cudaMemcpyDefault, ctx->stream));
-    if (r->x0) OPG_CUDA(cudaMemcpyAsync(M->kd_host[0].x, r->x0, r->N * 8, cudaMemcpyDefault, ctx->stream));
+    if (r->eqn) {
+        // the caller's equation, assembled from its fields (generateAb); the fields are only read here
+        const opflow_field target = r->leaves[r->unknown];
+        OPG_TRY(mg_add_problem(M, target, r->nodes.data(), (int) r->nodes.size(), r->leaves.data(), (int) r->leaves.size(), r->unknown));
+        OPG_TRY(mg_finalize(M));
+        r->N = M->probs[0].levels[0].N;
+        if (r->nf != r->N) return fail(OPFLOW_E_INVALID, "request %lld: the equation has %lld unknowns, expected %lld", r->id, r->N, r->nf);
+        if (r->x0) OPG_CUDA(cudaMemcpyAsync(M->kd_host[0].x, r->x0, r->N * 8, cudaMemcpyDefault, ctx->stream));
+        else OPG_TRY(mg_gather_target(ctx, target, M->kd_host[0].x));  // initx
+    } else {
+        std::vector<opflow_node> tree = helmholtz_tree(r->pd.ndim, r->pd.alpha, r->pd.beta);
+        opflow_field leaves[2] = {r->t, r->rhs};
+        OPG_TRY(mg_add_problem(M, r->t, tree.data(), (int) tree.size(), leaves, 2, 0));
+        OPG_TRY(mg_finalize(M));
+        r->N = M->probs[0].levels[0].N;
+        if (r->nf != r->N) return fail(OPFLOW_E_INVALID, "request %lld: f has %lld values, the problem %lld unknowns", r->id, r->nf, r->N);
+        // f, x0: host or device memory (unified addressing picks the direction)
+        OPG_CUDA(cudaMemcpyAsync(M->probs[0].b, r->f, r->N * 8, cudaMemcpyDefault, ctx->stream));
+        if (r->x0) OPG_CUDA(cudaMemcpyAsync(M->kd_host[0].x, r->x0, r->N * 8, cudaMemcpyDefault, ctx->stream));
+    }
     if (r->f_dev) {
         // a host f was checked at submission; a device f is checked here, before the request joins a batch
         int* flag = (int*) ctx->scratch;
@@ -151,7 +169,10 @@ static int setup_req(opflow_server S, Req* r, Scal* seed) {
         if (h_flag) return fail(OPFLOW_E_NAN, "request %lld: non-finite value in the (device) right-hand side", r->id);
     }
     ProblemHost& P = M->probs[0];
-    r->pinned = P.singular && !P.has_dirichlet;
+    // a singular problem is pinned (a user equation only when the server's params ask for it, as
+    // opflow_solver_solve does; otherwise its right-hand side is projected to zero mean)
+    r->pinned = P.singular && !P.has_dirichlet && (!r->eqn || S->params.pin_value);
+    if (r->eqn && P.singular && !P.has_dirichlet && !r->pinned) mg_add_scalar(ctx, P.b, r->N, -mg_sum(ctx, P.b, r->N) / (double) r->N);
     if (r->pinned) {
         // the pinned system (first unknown held at 0): singular system with b[0] = -(sum of the others)
         const double sb = mg_sum(ctx, P.b, r->N);
@@ -163,7 +184,7 @@ static int setup_req(opflow_server S, Req* r, Scal* seed) {
     OPG_TRY(mg_prepare_problem(M, S->params.tol, M->dS));
     OPG_CUDA(cudaMemcpyAsync(seed, M->dS, sizeof(Scal), cudaMemcpyDeviceToHost, ctx->stream));
     OPG_CUDA(cudaStreamSynchronize(ctx->stream));
-    r->bytes = M->arena.total + (size_t) 2 * r->t->info.count * 8;
+    r->bytes = M->arena.total + (r->t ? (size_t) 2 * r->t->info.count * 8 : 0);
     return OPFLOW_OK;
 }
 
@@ -224,7 +245,7 @@ static void finish_req(opflow_server S, Req* r, int status) {
 // always admitted); called with the lock held
 static bool can_admit(opflow_server S) {
     if (S->pending.empty() || S->resident >= S->max_active) return false;
-    const size_t est = estimate_bytes(S->pending.front()->pd);
+    const size_t est = S->pending.front()->est;
     return !S->budget || S->used + est <= S->budget || S->resident == 0;
 }
 
@@ -240,7 +261,7 @@ static void admit_loop(opflow_server S) {
             if (!can_admit(S)) break;  // stopping, nothing left to admit
             r = S->pending.front();
             S->pending.pop_front();
-            r->admitted_bytes = estimate_bytes(r->pd);
+            r->admitted_bytes = r->est;
             S->used += r->admitted_bytes;
             S->resident++;
             S->in_setup++;
@@ -261,8 +282,8 @@ static void admit_loop(opflow_server S) {
         }
         r->sys->ctx = &S->own_ctx;
         r->sys->arena.ctx = &S->own_ctx;
-        r->t->ctx = &S->own_ctx;
-        r->rhs->ctx = &S->own_ctx;
+        if (r->t) r->t->ctx = &S->own_ctx;
+        if (r->rhs) r->rhs->ctx = &S->own_ctx;
         {
             std::lock_guard<std::mutex> lk(S->mu);
             S->ready.push_back(r);
@@ -454,8 +475,48 @@ int opflow_server_create(opflow_ctx ctx, const opflow_solve_params* params, size
     return OPFLOW_OK;
 }
 
+static int submit_equation(opflow_server S, const opflow_request* q, long long* id) {
+    const opflow_equation& e = *q->equation;
+    if (!e.nodes || e.n_nodes <= 0 || !e.leaves || e.n_leaves <= 0 || e.unknown < 0 || e.unknown >= e.n_leaves)
+        return fail(OPFLOW_E_INVALID, "bad equation");
+    if (q->steps != 1) return fail(OPFLOW_E_INVALID, "an equation request is one solve (steps must be 1)");
+    if (q->f) return fail(OPFLOW_E_INVALID, "an equation request takes its right-hand side from the equation (f must be NULL)");
+    for (int i = 0; i < e.n_leaves; ++i)
+        if (!e.leaves[i]) return fail(OPFLOW_E_INVALID, "null leaf %d", i);
+    const opflow_field target = e.leaves[e.unknown];
+    const long long n = assign_box(target->info).count();
+    if (n <= 0) return fail(OPFLOW_E_INVALID, "the target has no unknowns");
+    // the fields' pending work (uploads, assignments on their contexts' streams) completes first
+    for (int i = 0; i < e.n_leaves; ++i) OPG_CUDA(cudaStreamSynchronize(e.leaves[i]->ctx->stream));
+    auto* r = new Req();
+    r->eqn = true;
+    r->nodes.assign(e.nodes, e.nodes + e.n_nodes);
+    r->leaves.assign(e.leaves, e.leaves + e.n_leaves);
+    r->unknown = e.unknown;
+    r->est = estimate_bytes_eqn(n);
+    r->steps = 1;
+    r->x0 = q->x0;
+    r->nf = n;
+    r->x_out = q->x_out;
+    r->t_submit = Clock::now();
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        if (S->stop) { delete r; return fail(OPFLOW_E_INVALID, "server is shutting down"); }
+        r->id = S->next_id++;
+        S->reqs[r->id] = r;
+        S->pending.push_back(r);
+        S->submitted++;
+        if (!S->have_first) { S->t_first = r->t_submit; S->have_first = true; }
+    }
+    S->cv_admit.notify_one();
+    if (id) *id = r->id;
+    return OPFLOW_OK;
+}
+
 int opflow_server_submit(opflow_server S, const opflow_request* q, long long* id) {
-    if (!S || !q || !q->f) return fail(OPFLOW_E_INVALID, "null argument");
+    if (!S || !q) return fail(OPFLOW_E_INVALID, "null argument");
+    if (q->equation) return submit_equation(S, q, id);
+    if (!q->f) return fail(OPFLOW_E_INVALID, "null right-hand side");
     if (q->steps < 1) return fail(OPFLOW_E_INVALID, "steps must be >= 1");
     const opflow_problem_desc& pd = q->problem;
     if (pd.ndim < 1 || pd.ndim > 3) return fail(OPFLOW_E_INVALID, "bad problem dimension");
@@ -475,6 +536,7 @@ int opflow_server_submit(opflow_server S, const opflow_request* q, long long* id
     auto* r = new Req();
     r->f_dev = f_dev;
     r->pd = pd;
+    r->est = estimate_bytes(pd);
     r->steps = q->steps;
     r->f = q->f;
     r->x0 = q->x0;

@@ -1391,6 +1391,13 @@ void mg_destroy(MGSystem* S) {
 }
 
 // ================================================================================= single-problem API
+int mg_gather_target(opflow_ctx ctx, opflow_field target, double* x) {
+    const Box box = assign_box(target->info);
+    gather_box<<<gridN(ctx, box.count()), 256, 0, ctx->stream>>>(target->view(), box, x);
+    OPG_LAUNCHED();
+    return check_launch("gather_box");
+}
+
 void mg_add_scalar(opflow_ctx ctx, double* v, long long n, double a) {
     add_scalar<<<gridN(ctx, n), 256, 0, ctx->stream>>>(v, n, a);
     OPG_LAUNCHED();

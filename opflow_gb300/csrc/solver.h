@@ -172,6 +172,11 @@ int mg_run_iterations(MGSystem* S, int iters);
 // r = b - A x, p = 0 and scalars for one problem so that the next batched iteration starts it
 int mg_prepare_problem(MGSystem* single, double tol, Scal* out);
 int mg_add_problem(MGSystem* S, opflow_field target, const opflow_node* nodes, int n_nodes, const opflow_field* leaves, int n_leaves, int unknown);
+// x[0..N) := the target's values over its assignable box, x fastest (HYPREEqnSolveHandler::initx)
+int mg_gather_target(opflow_ctx ctx, opflow_field target, double* x);
+// sum of v[0..n) (synchronises ctx's stream); v[0..n) += a
+double mg_sum(opflow_ctx ctx, const double* v, long long n);
+void mg_add_scalar(opflow_ctx ctx, double* v, long long n, double a);
 int mg_finalize(MGSystem* S);
 int mg_solve(MGSystem* S);
 int mg_states(MGSystem* S, std::vector<Scal>& out);

@@ -5,6 +5,7 @@ the oracle, which assembles the reference's system itself (the generateAb restat
 - 2D Poisson, 2048^2 cells, homogeneous Neumann, pinned (FP64 and mixed precision);
 - 3D flux form div(exp(g) grad p) = f on 256^3 cells, Neumann, pinned (mixed precision);
 - every problem of the 512-problem batched configuration (mixed precision, one batched solve);
+- the 256^3 exp(g) equation served as a user-equation request, alone and in the serving mix;
 - every request of a served stream of the serving configuration's mix (one-shot solves and heat
   sessions), whose sessions are checked step by step: a session of k - 1 steps gives, bit for bit,
   the right-hand side of the k-th step (results are deterministic alone and in any mix).
@@ -133,3 +134,46 @@ def test_every_served_result_on_the_oracles_system(ctx):
         worst = max(worst, rel)
         assert rel <= 2e-10, (k, p.n, steps, rel)
     print("\n%d served requests (%d sessions): worst oracle residual %.3e" % (len(reqs), len(prev), worst))
+
+
+def test_served_256_expg_equation_alone_and_in_the_mix(ctx):
+    """The 256^3 exp(g) configuration's equation served as a user-equation request
+    (opflow_request.equation): bit-identical alone and in a mix of the serving configuration's
+    requests, and on the oracle's system to 2e-10."""
+    n = 256
+    p, f, K = cell_fields(ctx, n, 3, 3)
+    rng = np.random.default_rng(4321)
+    kk = K.download()
+    sl = K.index_slices(K.assignableRange)
+    kk[sl] = np.exp(wl.smooth_field(rng, n))
+    K.upload(kk)
+    ff = f.download()
+    v = rng.standard_normal(ff[sl].shape)
+    ff[sl] = v - v.mean()
+    f.upload(ff)
+    p.assign(0.0)
+    getter = lambda e: f == (api.dx(api.d1IntpCenterToCorner(K, 0) * api.dx(e)) + api.dy(api.d1IntpCenterToCorner(K, 1) * api.dy(e))
+                             + api.dz(api.d1IntpCenterToCorner(K, 2) * api.dz(e)))
+    params = api.StructSolverParams(tol=1e-10, maxIter=300, pinValue=True, precision="mixed")
+    outs = []
+    for mixed in (False, True):
+        srv = api.Server(params, max_active=16 if mixed else 1, ctx=ctx)
+        others = []
+        if mixed:
+            for q, fq, _ in wl.serve_mix(api, 9, 6):
+                o = np.zeros(fq.size)
+                others.append((srv.submit(q, fq, out=o), o))
+        out = np.zeros(n ** 3)
+        rid = srv.submit_equation(getter, p, out=out)
+        r = srv.result(rid)
+        assert all(srv.result(i)["status"] == capi.OK for i, _ in others)
+        srv.close()
+        assert r["status"] == capi.OK and r["rel_residual"] <= 1e-10, r
+        outs.append(out)
+    assert np.array_equal(outs[0], outs[1])
+    pa = p.download()
+    pa[sl] = outs[1].reshape(pa[sl].shape)
+    p.upload(pa)
+    rel = oracle_rel_residual(p, getter, True)
+    print("\nserved 256^3 exp(g): oracle %.3e" % rel)
+    assert rel <= 2e-10, rel
