@@ -310,7 +310,13 @@ enum opflow_krylov {
 };
 /* Preconditioners: the geometric multigrid V-cycle stands in for PFMG, SMG and CycRed; JACOBI is one
  * diagonal step z = D^-1 v; NONE the identity. */
-enum opflow_precond { OPFLOW_PRECOND_MG = 0, OPFLOW_PRECOND_JACOBI = 1, OPFLOW_PRECOND_NONE = 2 };
+enum opflow_precond {
+    OPFLOW_PRECOND_MG = 0,
+    OPFLOW_PRECOND_JACOBI = 1,
+    OPFLOW_PRECOND_NONE = 2,
+    OPFLOW_PRECOND_AMG = 3 /* equation sets only: smoothed-aggregation AMG over the whole coupled matrix
+                              (AMGCL's amg<smoothed_aggregation, spai0>, AMGCLEqnSolveHandler.hpp) */
+};
 
 typedef struct {
     double tol;           /* relative residual ||b-Ax||_2/||b||_2 target (reference: tol)        */

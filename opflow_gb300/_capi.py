@@ -64,7 +64,7 @@ class SolveParams(C.Structure):
 
 # enum opflow_krylov / opflow_precond
 KRYLOV_PCG, KRYLOV_GMRES, KRYLOV_FGMRES, KRYLOV_LGMRES, KRYLOV_BICGSTAB, KRYLOV_NONE = range(6)
-PRECOND_MG, PRECOND_JACOBI, PRECOND_NONE = range(3)
+PRECOND_MG, PRECOND_JACOBI, PRECOND_NONE, PRECOND_AMG = range(4)
 
 
 class SolveState(C.Structure):

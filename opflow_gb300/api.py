@@ -716,7 +716,9 @@ def describe(mesh, desc):
 STRUCT_SOLVERS = {"PCG": capi.KRYLOV_PCG, "GMRES": capi.KRYLOV_GMRES, "FGMRES": capi.KRYLOV_FGMRES,
                   "LGMRES": capi.KRYLOV_LGMRES, "BICGSTAB": capi.KRYLOV_BICGSTAB}
 STRUCT_PRECONDS = {"PFMG": capi.PRECOND_MG, "SMG": capi.PRECOND_MG, "CYCRED": capi.PRECOND_MG,
-                   "Jacobi": capi.PRECOND_JACOBI, "None": capi.PRECOND_NONE}
+                   "Jacobi": capi.PRECOND_JACOBI, "None": capi.PRECOND_NONE,
+                   # equation sets only: AMGCL's amg<smoothed_aggregation, spai0> (AMGCLEqnSolveHandler.hpp)
+                   "AMG": capi.PRECOND_AMG}
 
 
 class StructSolverParams:
@@ -821,7 +823,9 @@ class EqnSetSolveHandler:
     """makeEqnSolveHandler over an equation set / SolveEqns (src/Core/Equation/UnifiedSolve.hpp:69-100,
     AMGCLEqnSolveHandler.hpp:53-190): getters[k](*targets) returns equation k, solved for targets[k]
     jointly with the others.  `params` (one StructSolverParams) picks the outer iteration and the
-    block-diagonal preconditioner; `pins[k]` pins equation k's last unknown (CSRMatrixGenerator)."""
+    preconditioner: "AMG" (smoothed aggregation over the whole coupled matrix, AMGCL's
+    amg<smoothed_aggregation, spai0>), or a block-diagonal one ("PFMG": each equation's multigrid,
+    "Jacobi", "None"); `pins[k]` pins equation k's last unknown (CSRMatrixGenerator)."""
 
     def __init__(self, getters, targets, params=None, pins=None):
         if len(getters) != len(targets):

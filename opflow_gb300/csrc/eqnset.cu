@@ -12,9 +12,13 @@
 // unknown's assignable range.  A pinned equation's last row becomes an identity row with right-hand
 // side 0 (CSRMatrixGenerator::generate, pinValue).
 //
-// The system is solved by the host-driven Krylov methods (krylov.cu) with a block-diagonal
-// preconditioner: each equation's own multigrid hierarchy on its diagonal block (the engine's
-// stand-in for AMGCL's AMG), Jacobi on the assembled diagonal, or none.
+// The system is solved by the host-driven Krylov methods (krylov.cu) with one of:
+// - smoothed-aggregation AMG over the whole coupled matrix (OPFLOW_PRECOND_AMG, amg.h: AMGCL's
+//   amg<smoothed_aggregation, spai0>, the reference's choice), which also coarsens the couplings;
+// - a block-diagonal preconditioner: each equation's own geometric multigrid hierarchy on its diagonal
+//   block (OPFLOW_PRECOND_MG), leaving the off-diagonal couplings to the Krylov method;
+// - Jacobi on the assembled diagonal, or none.
+#include "amg.h"
 #include "solver.h"
 
 #include <algorithm>
@@ -179,6 +183,8 @@ struct opflow_eqnset_s {
     Arena mat;          // the ELL blocks (rebuilt with the matrix)
     KrylovWork* W = nullptr;
     std::vector<MGSystem*> mg;
+    AmgDev amg;
+    bool amg_built = false;
     bool first = true;
     bool have_matrix = false;
 };
@@ -208,6 +214,7 @@ struct SetOp : KrylovOp {
             OPG_LAUNCHED();
             return check_launch("div_by");
         }
+        if (pc == OPFLOW_PRECOND_AMG) return amg_vcycle(s->ctx, stream, s->amg, v, z);
         for (int k = 0; k < s->neq; ++k) {
             const long long Nk = s->boxes[k].count();
             if (!s->pin[k]) {
@@ -365,6 +372,54 @@ int build_mg(opflow_eqnset s) {
     return OPFLOW_OK;
 }
 
+// the assembled coupled matrix as host CSR (rows sorted by column, entries of one column merged)
+int host_csr(opflow_eqnset s, std::vector<std::vector<std::pair<long long, double>>>& R) {
+    R.assign((size_t) s->n, {});
+    for (const Ell& E : s->blocks) {
+        std::vector<int> c((size_t) E.nk * E.rows);
+        std::vector<double> v((size_t) E.nk * E.rows);
+        OPG_CUDA(cudaMemcpy(c.data(), E.col, c.size() * sizeof(int), cudaMemcpyDeviceToHost));
+        OPG_CUDA(cudaMemcpy(v.data(), E.val, v.size() * 8, cudaMemcpyDeviceToHost));
+        for (long long r = 0; r < E.rows; ++r)
+            for (int e = 0; e < E.nk; ++e) {
+                const int cc = c[(size_t) e * E.rows + r];
+                if (cc >= 0) R[(size_t) (s->off[E.k] + r)].push_back({cc, v[(size_t) e * E.rows + r]});
+            }
+    }
+    for (auto& row : R) {
+        std::sort(row.begin(), row.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+        // entries of several stencil offsets that fold onto one column add up
+        std::vector<std::pair<long long, double>> merged;
+        for (auto& pr : row) {
+            if (!merged.empty() && merged.back().first == pr.first) merged.back().second += pr.second;
+            else merged.push_back(pr);
+        }
+        row.swap(merged);
+    }
+    return OPFLOW_OK;
+}
+
+// the AMG hierarchy of the whole coupled matrix (set up on the host, cycled on the device)
+int build_amg(opflow_eqnset s) {
+    std::vector<std::vector<std::pair<long long, double>>> R;
+    OPG_TRY(host_csr(s, R));
+    HostCsr A;
+    A.n = A.m = s->n;
+    A.ptr.assign((size_t) s->n + 1, 0);
+    for (long long r = 0; r < s->n; ++r) {
+        for (auto& pr : R[(size_t) r]) {
+            A.col.push_back((int) pr.first);
+            A.val.push_back(pr.second);
+        }
+        A.ptr[(size_t) r + 1] = (long long) A.col.size();
+    }
+    AmgHost H;
+    OPG_TRY(amg_build_host(A, AmgParams{}, &H));
+    OPG_TRY(amg_upload(s->ctx, H, &s->amg));
+    s->amg_built = true;
+    return OPFLOW_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -376,7 +431,7 @@ int opflow_eqnset_create(opflow_ctx ctx, int n_eqn, const opflow_field* targets,
     opflow_solve_params p;
     if (params) p = *params;
     else opflow_solve_params_default(&p);
-    if (p.krylov < OPFLOW_KRYLOV_PCG || p.krylov > OPFLOW_KRYLOV_NONE || p.precond < OPFLOW_PRECOND_MG || p.precond > OPFLOW_PRECOND_NONE)
+    if (p.krylov < OPFLOW_KRYLOV_PCG || p.krylov > OPFLOW_KRYLOV_NONE || p.precond < OPFLOW_PRECOND_MG || p.precond > OPFLOW_PRECOND_AMG)
         return fail(OPFLOW_E_INVALID, "bad solver parameters");
     if (p.krylov == OPFLOW_KRYLOV_NONE && p.precond == OPFLOW_PRECOND_NONE) return fail(OPFLOW_E_INVALID, "no solver");
     if (p.kdim <= 0) p.kdim = 5;
@@ -448,6 +503,7 @@ int opflow_eqnset_solve(opflow_eqnset s, opflow_solve_state* state) {
     const bool rebuild = s->first || !s->params.static_mat;
     OPG_TRY(assemble(s, !rebuild && s->have_matrix));
     if (s->params.precond == OPFLOW_PRECOND_MG && (rebuild || s->mg.empty())) OPG_TRY(build_mg(s));
+    if (s->params.precond == OPFLOW_PRECOND_AMG && (rebuild || !s->amg_built)) OPG_TRY(build_amg(s));
     KrylovParams kp;
     kp.method = s->params.krylov;
     kp.precond = s->params.precond;
@@ -504,30 +560,10 @@ int opflow_eqnset_solve(opflow_eqnset s, opflow_solve_state* state) {
 int opflow_eqnset_csr(opflow_eqnset s, long long* n_rows, long long* nnz, long long* row_ptr, long long* cols, double* vals, double* rhs) {
     if (!s || !n_rows || !nnz) return fail(OPFLOW_E_INVALID, "null argument");
     if (!s->have_matrix) OPG_TRY(assemble(s, false));
-    std::vector<std::vector<std::pair<long long, double>>> R((size_t) s->n);
-    for (const Ell& E : s->blocks) {
-        std::vector<int> c((size_t) E.nk * E.rows);
-        std::vector<double> v((size_t) E.nk * E.rows);
-        OPG_CUDA(cudaMemcpy(c.data(), E.col, c.size() * sizeof(int), cudaMemcpyDeviceToHost));
-        OPG_CUDA(cudaMemcpy(v.data(), E.val, v.size() * 8, cudaMemcpyDeviceToHost));
-        for (long long r = 0; r < E.rows; ++r)
-            for (int e = 0; e < E.nk; ++e) {
-                const int cc = c[(size_t) e * E.rows + r];
-                if (cc >= 0) R[(size_t) (s->off[E.k] + r)].push_back({cc, v[(size_t) e * E.rows + r]});
-            }
-    }
+    std::vector<std::vector<std::pair<long long, double>>> R;
+    OPG_TRY(host_csr(s, R));
     long long total = 0;
-    for (auto& row : R) {
-        std::sort(row.begin(), row.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
-        // entries of several stencil offsets that fold onto one column add up
-        std::vector<std::pair<long long, double>> merged;
-        for (auto& pr : row) {
-            if (!merged.empty() && merged.back().first == pr.first) merged.back().second += pr.second;
-            else merged.push_back(pr);
-        }
-        row.swap(merged);
-        total += (long long) row.size();
-    }
+    for (auto& row : R) total += (long long) row.size();
     *n_rows = s->n;
     *nnz = total;
     if (row_ptr) {
@@ -550,6 +586,7 @@ int opflow_eqnset_destroy(opflow_eqnset s) {
     if (!s) return OPFLOW_OK;
     if (s->ctx) cudaStreamSynchronize(s->ctx->stream);
     release_mg(s);
+    amg_free(s->ctx, &s->amg);
     release_matrix(s);
     krylov_work_free(s->W);
     s->arena.release();

@@ -301,52 +301,62 @@ int bicgstab(Ctx& c, const KrylovParams& P, double* b, double* x, int* iters) {
     OPG_TRY(dot(c, b, b, &bnorm2));
     const double bnorm = std::sqrt(bnorm2);
     OPG_TRY(residual(c, b, x, r));
-    OPG_CUDA(cudaMemcpyAsync(rh, r, c.N * 8, cudaMemcpyDeviceToDevice, c.s));
-    OPG_CUDA(cudaMemsetAsync(p, 0, c.N * 8, c.s));
-    OPG_CUDA(cudaMemsetAsync(v, 0, c.N * 8, c.s));
     double rho_old = 1., alpha = 1., omega = 1., rr;
     OPG_TRY(dot(c, r, r, &rr));
     int it = 0;
-    while (!reached(std::sqrt(rr), bnorm, P) && it < P.max_iter) {
-        ++it;
-        double rho;
-        OPG_TRY(dot(c, rh, r, &rho));
-        if (rho == 0.) {  // breakdown: restart the shadow residual
-            OPG_CUDA(cudaMemcpyAsync(rh, r, c.N * 8, cudaMemcpyDeviceToDevice, c.s));
-            OPG_CUDA(cudaMemsetAsync(p, 0, c.N * 8, c.s));
-            OPG_CUDA(cudaMemsetAsync(v, 0, c.N * 8, c.s));
-            rho_old = alpha = omega = 1.;
+    // The recurrence residual drifts from b - A x on ill-conditioned systems (a pinned row): when it
+    // reports convergence the true residual is formed, and the iteration restarts from it (shadow
+    // residual reset) until the true residual meets the tolerance (at most four restarts).
+    for (int restarts = 0;; ++restarts) {
+        OPG_CUDA(cudaMemcpyAsync(rh, r, c.N * 8, cudaMemcpyDeviceToDevice, c.s));
+        OPG_CUDA(cudaMemsetAsync(p, 0, c.N * 8, c.s));
+        OPG_CUDA(cudaMemsetAsync(v, 0, c.N * 8, c.s));
+        rho_old = alpha = omega = 1.;
+        while (!reached(std::sqrt(rr), bnorm, P) && it < P.max_iter) {
+            ++it;
+            double rho;
             OPG_TRY(dot(c, rh, r, &rho));
-            if (rho == 0.) break;
+            if (rho == 0.) {  // breakdown: restart the shadow residual
+                OPG_CUDA(cudaMemcpyAsync(rh, r, c.N * 8, cudaMemcpyDeviceToDevice, c.s));
+                OPG_CUDA(cudaMemsetAsync(p, 0, c.N * 8, c.s));
+                OPG_CUDA(cudaMemsetAsync(v, 0, c.N * 8, c.s));
+                rho_old = alpha = omega = 1.;
+                OPG_TRY(dot(c, rh, r, &rho));
+                if (rho == 0.) break;
+            }
+            const double beta = (rho / rho_old) * (alpha / omega);
+            OPG_TRY(axpby(c, 1., r, beta, p, -beta * omega, v));  // p = r + beta (p - omega v)
+            OPG_TRY(precond(c, p, ph));
+            OPG_TRY(matvec(c, ph, v));
+            double rv;
+            OPG_TRY(dot(c, rh, v, &rv));
+            alpha = rv != 0. ? rho / rv : 0.;
+            OPG_CUDA(cudaMemcpyAsync(s, r, c.N * 8, cudaMemcpyDeviceToDevice, c.s));
+            OPG_TRY(axpby(c, -alpha, v, 1., s));  // s = r - alpha v
+            double ss;
+            OPG_TRY(dot(c, s, s, &ss));
+            if (reached(std::sqrt(ss), bnorm, P)) {
+                OPG_TRY(axpby(c, alpha, ph, 1., x));
+                rr = ss;
+                break;
+            }
+            OPG_TRY(precond(c, s, sh));
+            OPG_TRY(matvec(c, sh, t));
+            double ts, tt;
+            OPG_TRY(dot(c, t, s, &ts));
+            OPG_TRY(dot(c, t, t, &tt));
+            omega = tt != 0. ? ts / tt : 0.;
+            OPG_TRY(axpby(c, alpha, ph, 1., x, omega, sh));  // x += alpha ph + omega sh
+            OPG_CUDA(cudaMemcpyAsync(r, s, c.N * 8, cudaMemcpyDeviceToDevice, c.s));
+            OPG_TRY(axpby(c, -omega, t, 1., r));  // r = s - omega t
+            OPG_TRY(dot(c, r, r, &rr));
+            rho_old = rho;
+            if (omega == 0.) break;
         }
-        const double beta = (rho / rho_old) * (alpha / omega);
-        OPG_TRY(axpby(c, 1., r, beta, p, -beta * omega, v));  // p = r + beta (p - omega v)
-        OPG_TRY(precond(c, p, ph));
-        OPG_TRY(matvec(c, ph, v));
-        double rv;
-        OPG_TRY(dot(c, rh, v, &rv));
-        alpha = rv != 0. ? rho / rv : 0.;
-        OPG_CUDA(cudaMemcpyAsync(s, r, c.N * 8, cudaMemcpyDeviceToDevice, c.s));
-        OPG_TRY(axpby(c, -alpha, v, 1., s));  // s = r - alpha v
-        double ss;
-        OPG_TRY(dot(c, s, s, &ss));
-        if (reached(std::sqrt(ss), bnorm, P)) {
-            OPG_TRY(axpby(c, alpha, ph, 1., x));
-            rr = ss;
-            break;
-        }
-        OPG_TRY(precond(c, s, sh));
-        OPG_TRY(matvec(c, sh, t));
-        double ts, tt;
-        OPG_TRY(dot(c, t, s, &ts));
-        OPG_TRY(dot(c, t, t, &tt));
-        omega = tt != 0. ? ts / tt : 0.;
-        OPG_TRY(axpby(c, alpha, ph, 1., x, omega, sh));  // x += alpha ph + omega sh
-        OPG_CUDA(cudaMemcpyAsync(r, s, c.N * 8, cudaMemcpyDeviceToDevice, c.s));
-        OPG_TRY(axpby(c, -omega, t, 1., r));  // r = s - omega t
+        if (it >= P.max_iter || restarts >= 4) break;
+        OPG_TRY(residual(c, b, x, r));
         OPG_TRY(dot(c, r, r, &rr));
-        rho_old = rho;
-        if (omega == 0.) break;
+        if (reached(std::sqrt(rr), bnorm, P)) break;
     }
     *iters = it;
     return OPFLOW_OK;

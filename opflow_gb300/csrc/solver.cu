@@ -1486,6 +1486,7 @@ int opflow_solver_create(opflow_ctx ctx, opflow_field target, const opflow_node*
     if (!(p.tol > 0) || p.max_iter < 0 || p.pre_sweeps < 0 || p.post_sweeps < 0) return fail(OPFLOW_E_INVALID, "bad solver parameters");
     if (p.precision != OPFLOW_PREC_FP64 && p.precision != OPFLOW_PREC_MIXED) return fail(OPFLOW_E_INVALID, "bad precision");
     if (p.krylov < OPFLOW_KRYLOV_PCG || p.krylov > OPFLOW_KRYLOV_NONE) return fail(OPFLOW_E_INVALID, "bad Krylov method %d", p.krylov);
+    if (p.precond == OPFLOW_PRECOND_AMG) return fail(OPFLOW_E_UNSUPPORTED, "AMG preconditioning is for equation sets (opflow_eqnset_*)");
     if (p.precond < OPFLOW_PRECOND_MG || p.precond > OPFLOW_PRECOND_NONE) return fail(OPFLOW_E_INVALID, "bad preconditioner %d", p.precond);
     if (p.krylov == OPFLOW_KRYLOV_NONE && p.precond == OPFLOW_PRECOND_NONE) return fail(OPFLOW_E_INVALID, "no solver: neither a Krylov method nor a preconditioner");
     if (p.kdim <= 0) p.kdim = 5;

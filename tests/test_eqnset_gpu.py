@@ -3,6 +3,8 @@
 - EqnSetTest's cases (src test/Core/Equation/EqnSetTest.cpp): copies of `1.0 == d2x(e) + d2y(e)` solved
   as one system agree with the single-equation solve (Dirichlet) and with each other (pinned Neumann,
   the CSR generator's last-row pin).
+- BiCGStab + smoothed-aggregation AMG (the reference's AMGCL configuration) on those cases and on a
+  strongly coupled pair, where it needs fewer iterations than the block-diagonal multigrid.
 - A genuinely coupled pair u, v: the engine's assembled CSR equals the oracle's StencilPad assembly of
   every block, and the solution meets 1e-10 on that system.
 """
@@ -163,3 +165,64 @@ def test_three_equations_with_jacobi_and_static_matrix(ctx):
         A, b = _oracle_blocks(fs, getters)
         x = np.concatenate([_interior(f).reshape(-1) for f in fs])
         assert np.linalg.norm(b - A @ x) <= 1e-10 * np.linalg.norm(b)
+
+
+@pytest.mark.parametrize("bc", [capi.BC_DIRC, capi.BC_NEUM])
+def test_amg_bicgstab_on_eqnsettest_cases(ctx, bc):
+    """EqnSetTest's configuration: BiCGStab preconditioned by smoothed-aggregation AMG with SPAI-0
+    smoothing over the whole coupled matrix (amg<smoothed_aggregation, spai0> + bicgstab)."""
+    n = 48
+    p, p2, pt = (_center_field(ctx, n, bc, nm) for nm in ("p", "p2", "pt"))
+    # the pinned Neumann system's attainable relative residual in float64 is about 1e-12 at this size
+    tol = 1e-12 if bc == capi.BC_DIRC else 1e-10
+    prm = api.StructSolverParams(tol=tol, maxIter=500, solver="BICGSTAB", precond="AMG")
+    lap = lambda e: api.d2x(e) + api.d2y(e)
+    pins = [bc == capi.BC_NEUM] * 2
+    h = api.EqnSetSolveHandler([lambda e, e2: api.Eq(1.0, lap(e)), lambda e, e2: api.Eq(1.0, lap(e2))], [p, p2], prm, pins=pins)
+    st = h.solve()
+    assert st.converged and st.relerr <= tol, st
+    a, a2 = _interior(p), _interior(p2)
+    assert np.abs(a - a2).max() <= 1e-8 * np.abs(a).max()
+    if bc == capi.BC_DIRC:
+        st1 = api.Solve(lambda e: api.Eq(1.0, lap(e)), pt, api.StructSolverParams(tol=1e-13, maxIter=200))
+        assert st1.converged
+        at = _interior(pt)
+        assert np.abs(a - at).max() <= 1e-9 * np.abs(at).max()
+    else:
+        assert a[-1, -1] == 0.0 and a2[-1, -1] == 0.0
+
+
+def test_amg_coarsens_the_couplings_of_a_strongly_coupled_pair(ctx):
+    """u - 0.05 Lap(u) + c v = f, v - 0.05 Lap(v) - c u = g with a strong coupling c = 50: AMG over the
+    coupled matrix reaches 1e-10 on the oracle's assembly of every block in a fraction of the BiCGStab
+    iterations of the block-diagonal geometric multigrid, which leaves the couplings to the Krylov
+    method (measured at 24^2: 16 against 327)."""
+    n = 24
+    res = {}
+    for pc in ("AMG", "PFMG"):
+        u = _center_field(ctx, n, capi.BC_DIRC, "u", 0.5)
+        v = _center_field(ctx, n, capi.BC_DIRC, "v", -0.25)
+        f = _center_field(ctx, n, capi.BC_DIRC, "f")
+        rng = np.random.default_rng(8)
+        a = f.download()
+        sl = f.index_slices([tuple(f.info.assignable[d]) for d in range(2)])
+        a[sl] = rng.standard_normal(a[sl].shape)
+        f.upload(a)
+        lap = lambda e: api.d2x(e) + api.d2y(e)
+        getters = [lambda uu, vv: uu - 0.05 * lap(uu) + 50.0 * vv == f, lambda uu, vv: vv - 0.05 * lap(vv) - 50.0 * uu == 2.0 * f]
+        prm = api.StructSolverParams(tol=1e-11, maxIter=1000, solver="BICGSTAB", precond=pc)
+        h = api.EqnSetSolveHandler(getters, [u, v], prm)
+        st = h.solve()
+        assert st.converged, (pc, st)
+        A, b = _oracle_blocks([u, v], getters)
+        x = np.concatenate([_interior(u).reshape(-1), _interior(v).reshape(-1)])
+        assert np.linalg.norm(b - A @ x) <= 1e-10 * np.linalg.norm(b), pc
+        res[pc] = st.niter
+    print("\nstrongly coupled pair: BiCGStab iterations AMG %d, block-diagonal MG %d" % (res["AMG"], res["PFMG"]))
+    assert 4 * res["AMG"] < res["PFMG"], res
+
+
+def test_amg_is_for_equation_sets_only(ctx):
+    p = _center_field(ctx, 8, capi.BC_DIRC, "p")
+    with pytest.raises(Exception):
+        api.Solve(lambda e: api.Eq(1.0, api.d2x(e) + api.d2y(e)), p, api.StructSolverParams(solver="BICGSTAB", precond="AMG"))
