@@ -397,8 +397,12 @@ done_chain:
     return true;
 }
 
+// RHS_ONLY: the right-hand side alone (generateb): the same program on the pads' bias parts, which no
+// coefficient ever feeds, so b is bit-identical to the full assembly's
+template <bool RHS_ONLY>
 __global__ void __launch_bounds__(128) assemble_kernel(const PInstr* __restrict__ prog, int nprog, AsmParams P, double* __restrict__ coef,
                                                        double* __restrict__ rhs, int* __restrict__ err) {
+    const int NK = RHS_ONLY ? 0 : P.nk;
     const long long nx = P.box.hi[0] - P.box.lo[0], ny = P.box.hi[1] - P.box.lo[1], nz = P.box.hi[2] - P.box.lo[2];
     const long long total = nx * ny * nz;
     for (long long t = blockIdx.x * (long long) blockDim.x + threadIdx.x; t < total; t += (long long) gridDim.x * blockDim.x) {
@@ -423,8 +427,8 @@ __global__ void __launch_bounds__(128) assemble_kernel(const PInstr* __restrict_
                     int ki;
                     double c, b;
                     ok = st_leaf(P, cell, in.off, &ki, &c, &b);
-                    for (int q = 0; q < P.nk; ++q) st[psp].c[q] = 0.;
-                    if (ki >= 0) st[psp].c[ki] = c;
+                    for (int q = 0; q < NK; ++q) st[psp].c[q] = 0.;
+                    if (!RHS_ONLY && ki >= 0) st[psp].c[ki] = c;
                     st[psp].b = b;
                     psp++;
                     break;
@@ -434,7 +438,7 @@ __global__ void __launch_bounds__(128) assemble_kernel(const PInstr* __restrict_
                 case Q_X: sv[sp++] = P.mx[in.slot][cell[in.slot] + in.off[0] - P.es[in.slot]]; break;
                 case Q_NEG:
                     if (in.ta) {
-                        for (int q = 0; q < P.nk; ++q) st[psp - 1].c[q] = -st[psp - 1].c[q];
+                        for (int q = 0; q < NK; ++q) st[psp - 1].c[q] = -st[psp - 1].c[q];
                         st[psp - 1].b = -st[psp - 1].b;
                     } else sv[sp - 1] = -sv[sp - 1];
                     break;
@@ -472,21 +476,21 @@ __global__ void __launch_bounds__(128) assemble_kernel(const PInstr* __restrict_
                     PadVal& A = st[psp - 1];
                     const PadVal& B = st[psp - (in.ta && in.tb ? 0 : 1)];
                     if (in.op == Q_ADD) {
-                        if (in.ta && in.tb) { for (int q = 0; q < P.nk; ++q) A.c[q] = __dadd_rn(A.c[q], B.c[q]); A.b = __dadd_rn(A.b, B.b); }
+                        if (in.ta && in.tb) { for (int q = 0; q < NK; ++q) A.c[q] = __dadd_rn(A.c[q], B.c[q]); A.b = __dadd_rn(A.b, B.b); }
                         else if (in.ta) A.b = __dadd_rn(A.b, b);
                         else A.b = __dadd_rn(B.b, a);
                     } else if (in.op == Q_SUB) {
                         // pad - pad = a + (b * -1.0); pad - num = a + (-b); num - pad = StencilPad(a) + (b * -1.0)
-                        if (in.ta && in.tb) { for (int q = 0; q < P.nk; ++q) A.c[q] = __dadd_rn(A.c[q], __dmul_rn(B.c[q], -1.0)); A.b = __dadd_rn(A.b, __dmul_rn(B.b, -1.0)); }
+                        if (in.ta && in.tb) { for (int q = 0; q < NK; ++q) A.c[q] = __dadd_rn(A.c[q], __dmul_rn(B.c[q], -1.0)); A.b = __dadd_rn(A.b, __dmul_rn(B.b, -1.0)); }
                         else if (in.ta) A.b = __dadd_rn(A.b, -b);
-                        else { for (int q = 0; q < P.nk; ++q) A.c[q] = __dmul_rn(A.c[q], -1.0); A.b = __dadd_rn(a, __dmul_rn(A.b, -1.0)); }
+                        else { for (int q = 0; q < NK; ++q) A.c[q] = __dmul_rn(A.c[q], -1.0); A.b = __dadd_rn(a, __dmul_rn(A.b, -1.0)); }
                     } else if (in.op == Q_MUL) {
                         const double s = in.ta ? b : a;
-                        for (int q = 0; q < P.nk; ++q) A.c[q] = __dmul_rn(A.c[q], s);
+                        for (int q = 0; q < NK; ++q) A.c[q] = __dmul_rn(A.c[q], s);
                         A.b = __dmul_rn(A.b, s);
                     } else {  // pad / num = pad * (1. / num)
                         const double r = __ddiv_rn(1., b);
-                        for (int q = 0; q < P.nk; ++q) A.c[q] = __dmul_rn(A.c[q], r);
+                        for (int q = 0; q < NK; ++q) A.c[q] = __dmul_rn(A.c[q], r);
                         A.b = __dmul_rn(A.b, r);
                     }
                 }
@@ -496,7 +500,7 @@ __global__ void __launch_bounds__(128) assemble_kernel(const PInstr* __restrict_
             atomicExch(err, 1);
             continue;
         }
-        for (int q = 0; q < P.nk; ++q) {
+        for (int q = 0; q < NK; ++q) {
             const double v = st[0].c[q];
             coef[(long long) q * total + t] = v == 0. ? 0. : v;  // +0 for -0
         }
@@ -683,6 +687,7 @@ int asm_prepare(opflow_ctx ctx, opflow_field target, const opflow_node* nodes, i
 }
 
 int asm_run(opflow_ctx ctx, AsmPlan* plan, double* coef, double* rhs) {
+    if (!coef && !rhs) return fail(OPFLOW_E_INVALID, "assembly: no output");
     const long long N = plan->cells;
     if (N <= 0) return OPFLOW_OK;
     OPG_TRY(ensure_scratch(ctx, 64));
@@ -693,7 +698,8 @@ int asm_run(opflow_ctx ctx, AsmPlan* plan, double* coef, double* rhs) {
     cudaMemcpyAsync(dprog, plan->prog.data(), plan->prog.size() * sizeof(PInstr), cudaMemcpyHostToDevice, ctx->stream);
     long long blocks = (N + 127) / 128;
     if (blocks > (long long) ctx->num_sms * 32) blocks = (long long) ctx->num_sms * 32;
-    assemble_kernel<<<(int) blocks, 128, 0, ctx->stream>>>(dprog, (int) plan->prog.size(), plan->P, coef, rhs, err);
+    if (coef) assemble_kernel<false><<<(int) blocks, 128, 0, ctx->stream>>>(dprog, (int) plan->prog.size(), plan->P, coef, rhs, err);
+    else assemble_kernel<true><<<(int) blocks, 128, 0, ctx->stream>>>(dprog, (int) plan->prog.size(), plan->P, coef, rhs, err);
     OPG_LAUNCHED();
     int rc = check_launch("assemble_kernel");
     int herr = 0;

@@ -49,6 +49,7 @@ struct AsmPlan {
 int asm_prepare(opflow_ctx ctx, opflow_field target, const opflow_node* nodes, int n, const opflow_field* leaves, int nleaves, int unknown,
                 int pin, AsmPlan* plan, opflow_field rows = nullptr);
 // coef: [nk][cells] (SoA over the plan's K order), rhs: [cells] = -bias
+// coef == nullptr: the right-hand side alone (generateb), bit-identical to the full assembly's
 int asm_run(opflow_ctx ctx, AsmPlan* plan, double* coef, double* rhs);
 
 }  // namespace opg

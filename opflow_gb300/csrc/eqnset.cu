@@ -271,15 +271,16 @@ int assemble(opflow_eqnset s, bool rhs_only) {
         const long long Nk = s->boxes[k].count();
         bool rhs_done = false;
         for (int j : s->deps[k]) {
+            if (rhs_only && rhs_done) break;  // generateb: one right-hand-side evaluation per equation
             std::vector<opflow_field> L = leaves_for(s, j);
             AsmPlan plan;
             OPG_TRY(asm_prepare(ctx, s->targets[j], s->trees[k].data(), (int) s->trees[k].size(), L.data(), (int) L.size(), s->slot[j], 0, &plan,
                                 s->targets[k]));
             const int nk = plan.P.nk;
-            double* coef = (double*) dev_alloc(ctx, (size_t) nk * Nk * 8 + 8);
+            double* coef = rhs_only ? nullptr : (double*) dev_alloc(ctx, (size_t) nk * Nk * 8 + 8);
             double* rhs = (double*) dev_alloc(ctx, (size_t) Nk * 8 + 8);
             int* dK = (int*) dev_alloc(ctx, (size_t) nk * 3 * sizeof(int) + 16);
-            if (!coef || !rhs || !dK) return fail(OPFLOW_E_NOMEM, "coupled assembly buffers");
+            if ((!rhs_only && !coef) || !rhs || !dK) return fail(OPFLOW_E_NOMEM, "coupled assembly buffers");
             int rc = asm_run(ctx, &plan, coef, rhs);
             if (rc == OPFLOW_OK && !rhs_done) {
                 OPG_CUDA(cudaMemcpyAsync(s->b + s->off[k], rhs, Nk * 8, cudaMemcpyDeviceToDevice, ctx->stream));

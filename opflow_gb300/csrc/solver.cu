@@ -148,6 +148,30 @@ __global__ void add_scalar(double* v, long long n, double a) {
     for (long long t = blockIdx.x * (long long) blockDim.x + threadIdx.x; t < n; t += (long long) gridDim.x * blockDim.x) v[t] += a;
 }
 
+// The singular right-hand side on the device, without a host round trip: sum[0] = the partial sums
+// added in block order (as mg_sum adds them on the host); pinned: b[0] := -(sum - b[0]); else nothing
+// (the projection follows in add_scaled_sum)
+__global__ void singular_rhs(const double* partial, int nblk, double* b, int pinned, double* sum) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double s = 0.;
+    for (int i = 0; i < nblk; ++i) s += partial[i];
+    sum[0] = s;
+    if (pinned) b[0] = -(s - b[0]);
+}
+// v += -(*sum) / n (the projection onto zero mean)
+__global__ void add_scaled_sum(double* v, long long n, const double* sum) {
+    const double a = -*sum / (double) n;
+    for (long long t = blockIdx.x * (long long) blockDim.x + threadIdx.x; t < n; t += (long long) gridDim.x * blockDim.x) v[t] += a;
+}
+// x -= x[0] with x[0] first saved to *slot (so no thread reads it while another rewrites it)
+__global__ void save_first(const double* x, double* slot) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) slot[0] = x[0];
+}
+__global__ void sub_slot(double* v, long long n, const double* slot) {
+    const double a = -*slot;
+    for (long long t = blockIdx.x * (long long) blockDim.x + threadIdx.x; t < n; t += (long long) gridDim.x * blockDim.x) v[t] += a;
+}
+
 static int gridN(opflow_ctx ctx, long long n) {
     long long b = (n + 255) / 256;
     return (int) std::max(1LL, std::min(b, (long long) ctx->num_sms * 16));
@@ -1404,7 +1428,6 @@ void mg_add_scalar(opflow_ctx ctx, double* v, long long n, double a) {
 }
 
 double mg_sum(opflow_ctx ctx, const double* v, long long n);
-static double sum_device(opflow_ctx ctx, const double* v, long long n) { return mg_sum(ctx, v, n); }
 
 double mg_sum(opflow_ctx ctx, const double* v, long long n) {
     double* part = (double*) ctx->scratch + 64;
@@ -1434,6 +1457,9 @@ struct opflow_solver_s {
     bool first = true;
     // write counters of the leaves when the system was last assembled (the target's after its solve)
     std::vector<unsigned long long> assembled_versions;
+    // generateb's compiled plan (staticMat), made on the first re-solve
+    AsmPlan rhs_plan;
+    bool rhs_plan_ok = false;
 };
 
 // (the unknown's own values only seed the iteration, so its slot is left out)
@@ -1522,14 +1548,14 @@ int opflow_solver_solve(opflow_solver s, opflow_solve_state* state) {
     if (s->first && leaf_versions(s) != s->assembled_versions) OPG_TRY(build_system(s));
     else if (!s->first) {
         if (s->params.static_mat) {
-            AsmPlan plan;
-            OPG_TRY(asm_prepare(ctx, s->target, s->tree.data(), (int) s->tree.size(), s->leaves.data(), (int) s->leaves.size(), s->unknown, 0,
-                                &plan));
-            double* coef = nullptr;
-            OPG_CUDA(cudaMalloc(&coef, (size_t) plan.cells * plan.P.nk * sizeof(double)));
-            int rc = asm_run(ctx, &plan, coef, s->S->probs[0].b);
-            cudaFree(coef);
-            OPG_TRY(rc);
+            // generateb: the right-hand side alone, from a plan compiled once (the leaves' current buffers)
+            if (!s->rhs_plan_ok) {
+                OPG_TRY(asm_prepare(ctx, s->target, s->tree.data(), (int) s->tree.size(), s->leaves.data(), (int) s->leaves.size(), s->unknown, 0,
+                                    &s->rhs_plan));
+                s->rhs_plan_ok = true;
+            }
+            for (size_t k = 0; k < s->leaves.size(); ++k) s->rhs_plan.P.leaves[k] = s->leaves[k]->view();
+            OPG_TRY(asm_run(ctx, &s->rhs_plan, nullptr, s->S->probs[0].b));
         } else {
             OPG_TRY(build_system(s));
         }
@@ -1547,18 +1573,14 @@ int opflow_solver_solve(opflow_solver s, opflow_solve_state* state) {
         OPG_LAUNCHED();
     }
     const bool pinned = P.singular && !P.has_dirichlet && s->params.pin_value;
-    double b_pin = 0.;
+    OPG_TRY(ensure_scratch(ctx, 4096));
+    double* dsc = (double*) ctx->scratch;  // [40]: sum of b, [41]: pinned shift; [64..320): partial sums
     if (P.singular && !P.has_dirichlet) {
-        const double sb = sum_device(ctx, P.b, N);
-        if (pinned) {
-            // the pinned system equals the singular one with b[0] := -(sum of the others), shifted
-            OPG_CUDA(cudaMemcpy(&b_pin, P.b, 8, cudaMemcpyDeviceToHost));
-            const double nb0 = -(sb - b_pin);
-            OPG_CUDA(cudaMemcpy(P.b, &nb0, 8, cudaMemcpyHostToDevice));
-        } else {
-            add_scalar<<<gridN(ctx, N), 256, 0, ctx->stream>>>(P.b, N, -sb / (double) N);
-            OPG_LAUNCHED();
-        }
+        // the pinned system equals the singular one with b[0] := -(sum of the others), shifted after
+        sum_partials<<<256, 256, 0, ctx->stream>>>(P.b, N, dsc + 64);
+        singular_rhs<<<1, 32, 0, ctx->stream>>>(dsc + 64, 256, P.b, pinned ? 1 : 0, dsc + 40);
+        if (!pinned) add_scaled_sum<<<gridN(ctx, N), 256, 0, ctx->stream>>>(P.b, N, dsc + 40);
+        OPG_LAUNCHED();
     }
     auto t1 = clk::now();
     int iters = 0;
@@ -1577,13 +1599,11 @@ int opflow_solver_solve(opflow_solver s, opflow_solve_state* state) {
         kp.abs_tol = s->params.abs_tol;
         OPG_TRY(krylov_solve(S, kp, &iters));
     }
-    double shift = 0.;
     if (pinned) {
-        OPG_CUDA(cudaMemcpy(&shift, K.x, 8, cudaMemcpyDeviceToHost));
-        OPG_CUDA(cudaMemcpy(P.b, &b_pin, 8, cudaMemcpyHostToDevice));  // back to the reference's b (pinned row 0 -> 0 below)
-        const double zero = 0.;
-        OPG_CUDA(cudaMemcpy(P.b, &zero, 8, cudaMemcpyHostToDevice));
-        add_scalar<<<gridN(ctx, N), 256, 0, ctx->stream>>>(K.x, N, -shift);
+        // the reference's b (the pinned row's right-hand side is 0) and x shifted so that x[0] = 0
+        OPG_CUDA(cudaMemsetAsync(P.b, 0, 8, ctx->stream));
+        save_first<<<1, 32, 0, ctx->stream>>>(K.x, dsc + 41);
+        sub_slot<<<gridN(ctx, N), 256, 0, ctx->stream>>>(K.x, N, dsc + 41);
         OPG_LAUNCHED();
     }
     // true residual of the reference's system (a pinned system's first row, the identity with b = 0, is
