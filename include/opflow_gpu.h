@@ -513,9 +513,9 @@ int opflow_tune_clear(void);
  * values x fastest, norms two values.  Work is enqueued on `stream` (results valid after it completes).
  * The partial sums live in one static 1 MiB device array per device: grids needing more than 65536
  * chunks (one per 1024 cells of every x-row) are rejected with OPFLOW_E_INVALID; calls that overlap on
- * the GPU race on that array.  The first call on a device looks up the array's address with that
- * device current and keeps it: make it before any stream capture begins, and do not use the entry point
- * across a cudaDeviceReset of that device in the same process (the kept address would be stale). */
+ * the GPU race on that array.  Every call looks up the array's address in the current device's
+ * context (no allocation); the first call on a device may load the module, so make it before any
+ * stream capture begins. */
 int opflow_residual_norms_noalloc(void* stream, int ndim, const int* n, const int* periodic, const double* coef, const double* b,
                                   const double* x, double* r, double* norms);
 

@@ -16,25 +16,18 @@
 //   - All calls on one device share the array.  Each call writes every partial it later reads, so no
 //     entry has to start at zero; but calls whose kernels overlap on the GPU (different streams, or
 //     different host threads) race on the array: serialise them.
-//   - The first call on each device looks up the array's device address (cudaGetSymbolAddress) with
-//     that device current and keeps it; make that first call before any stream capture begins.  The
-//     kept address belongs to the device's context of that moment: after a cudaDeviceReset of the
-//     device the module is loaded again elsewhere, so the entry point must not be used across a reset.
+//   - Every call looks up the array's device address in the current device's context
+//     (cudaGetSymbolAddress, no allocation).  The first call on a device may load the module: make it
+//     before any stream capture begins.
 #include "internal.h"
-
-#include <mutex>
 
 #define OPFLOW_NOALLOC_MAX_CHUNKS 65536
 #define OPFLOW_NOALLOC_CHUNK 1024
-#define OPFLOW_NOALLOC_MAX_DEVICES 64
 
 namespace opg {
 
 // two float64 partial sums (b.b, r.r) per chunk
 static __device__ __align__(256) double g_noalloc_partials[2 * OPFLOW_NOALLOC_MAX_CHUNKS];
-
-static std::mutex g_noalloc_mu;
-static double* g_noalloc_addr[OPFLOW_NOALLOC_MAX_DEVICES] = {nullptr};
 
 struct NaGrid {
     int ndim, n[3], per[3];
@@ -122,21 +115,13 @@ __global__ void __launch_bounds__(256) na_reduce(const double* __restrict__ part
     }
 }
 
-// Device address of the static partial-sum array for the current device, looked up once per device.
+// Device address of the static partial-sum array in the current device's context, looked up on every
+// call (no allocation once the module is loaded, and never stale after a device reset).
 static int noalloc_scratch(double** out) {
-    int dev = -1;
-    OPG_CUDA(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= OPFLOW_NOALLOC_MAX_DEVICES) return fail(OPFLOW_E_INVALID, "device %d is beyond the %d devices this entry point tracks", dev,
-                                                                  OPFLOW_NOALLOC_MAX_DEVICES);
-    std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_addr[dev]) {
-        void* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partials);
-        if (e != cudaSuccess || !p)
-            return fail(OPFLOW_E_CUDA, "cudaGetSymbolAddress of the static residual scratch failed on device %d: %s", dev, cudaGetErrorString(e));
-        g_noalloc_addr[dev] = (double*) p;
-    }
-    *out = g_noalloc_addr[dev];
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partials);
+    if (e != cudaSuccess || !p) return fail(OPFLOW_E_CUDA, "cudaGetSymbolAddress of the static residual scratch failed: %s", cudaGetErrorString(e));
+    *out = (double*) p;
     return OPFLOW_OK;
 }
 
