@@ -405,6 +405,9 @@ __global__ void __launch_bounds__(128) assemble_kernel(const PInstr* __restrict_
     const int NK = RHS_ONLY ? 0 : P.nk;
     const long long nx = P.box.hi[0] - P.box.lo[0], ny = P.box.hi[1] - P.box.lo[1], nz = P.box.hi[2] - P.box.lo[2];
     const long long total = nx * ny * nz;
+    // the last divisor of a pad / num step and its reciprocal RN(1 / num): on a uniform mesh the same
+    // spacing divides every difference, so the float64 division runs once per thread, not per use
+    double last_div = 0., last_rec = __ddiv_rn(1., 0.);
     for (long long t = blockIdx.x * (long long) blockDim.x + threadIdx.x; t < total; t += (long long) gridDim.x * blockDim.x) {
         int cell[3];
         box_index(t, P.box, cell[0], cell[1], cell[2]);
@@ -489,7 +492,11 @@ __global__ void __launch_bounds__(128) assemble_kernel(const PInstr* __restrict_
                         for (int q = 0; q < NK; ++q) A.c[q] = __dmul_rn(A.c[q], s);
                         A.b = __dmul_rn(A.b, s);
                     } else {  // pad / num = pad * (1. / num)
-                        const double r = __ddiv_rn(1., b);
+                        if (__double_as_longlong(b) != __double_as_longlong(last_div)) {  // bit patterns: -0 is not +0
+                            last_div = b;
+                            last_rec = __ddiv_rn(1., b);
+                        }
+                        const double r = last_rec;
                         for (int q = 0; q < NK; ++q) A.c[q] = __dmul_rn(A.c[q], r);
                         A.b = __dmul_rn(A.b, r);
                     }

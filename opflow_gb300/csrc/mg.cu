@@ -783,6 +783,29 @@ __global__ void __launch_bounds__(256, 4) kr_apply(const LvlDev* __restrict__ Ls
     }
 }
 
+// A chunk whose cells form one contiguous run of an even number of cells from an even cell (full rows
+// of a level, or a row segment): the Krylov vector kernels then move two cells per access (16-byte
+// float64 and 8-byte float32 pairs; every vector is 256-byte aligned), which keeps twice the bytes in
+// flight per instruction on these latency-bound streaming passes.
+__device__ __forceinline__ bool chunk_pairs(const LvlDev& L, const Chunk& C, long long& start, long long& n) {
+    if (!(C.nrows == 1 || (C.i0 == 0 && C.cnt == L.n[0]))) return false;
+    start = cell_of(L, C.i0, C.j, C.k);
+    n = (long long) C.cnt * C.nrows;
+    return ((start | n) & 1) == 0;
+}
+template <typename T>
+struct Pair;
+template <>
+struct Pair<float> {
+    using V = float2;
+    __device__ static V make(double a, double b) { return make_float2((float) a, (float) b); }
+};
+template <>
+struct Pair<double> {
+    using V = double2;
+    __device__ static V make(double a, double b) { return make_double2(a, b); }
+};
+
 // x += alpha p, r -= alpha q, partial (r.r); the V-cycle's level-0 input b = (T) r, x = 0 alongside
 template <typename T>
 __global__ void __launch_bounds__(256, 4) kr_update(const LvlDev* __restrict__ Ls, const KrylovDev* __restrict__ K, const Chunk* __restrict__ ch, int nch,
@@ -804,17 +827,44 @@ __global__ void __launch_bounds__(256, 4) kr_update(const LvlDev* __restrict__ L
             const double* __restrict__ qp = Kp.q;
             T* __restrict__ vb = Sel<T>::b(L);
             T* __restrict__ vx = Sel<T>::x(L);
-            for (int rw = 0; rw < C.nrows; ++rw)
+            long long st, n;
+            if (chunk_pairs(L, C, st, n)) {
+                using V = typename Pair<T>::V;
+                double2* __restrict__ x2 = (double2*) (xp + st);
+                const double2* __restrict__ p2 = (const double2*) (pp + st);
+                double2* __restrict__ r2 = (double2*) (rp + st);
+                const double2* __restrict__ q2 = (const double2*) (qp + st);
+                V* __restrict__ b2 = (V*) (vb + st);
+                V* __restrict__ z2 = (V*) (vx + st);
 #pragma unroll 4
-                for (int t = threadIdx.x; t < C.cnt; t += blockDim.x) {
-                    const long long cell = cell_of(L, C.i0 + t, C.j + rw, C.k);
-                    xp[cell] = fma(al, pp[cell], xp[cell]);
-                    const double r = fma(-al, qp[cell], rp[cell]);
-                    rp[cell] = r;
-                    s = fma(r, r, s);
-                    vb[cell] = (T) r;
-                    vx[cell] = 0;
+                for (long long t = threadIdx.x; t < n / 2; t += blockDim.x) {
+                    double2 xv = x2[t];
+                    const double2 pv = p2[t], qv = q2[t];
+                    double2 rv = r2[t];
+                    xv.x = fma(al, pv.x, xv.x);
+                    xv.y = fma(al, pv.y, xv.y);
+                    rv.x = fma(-al, qv.x, rv.x);
+                    rv.y = fma(-al, qv.y, rv.y);
+                    x2[t] = xv;
+                    r2[t] = rv;
+                    s = fma(rv.x, rv.x, s);
+                    s = fma(rv.y, rv.y, s);
+                    b2[t] = Pair<T>::make(rv.x, rv.y);
+                    z2[t] = Pair<T>::make(0., 0.);
                 }
+            } else {
+                for (int rw = 0; rw < C.nrows; ++rw)
+#pragma unroll 4
+                    for (int t = threadIdx.x; t < C.cnt; t += blockDim.x) {
+                        const long long cell = cell_of(L, C.i0 + t, C.j + rw, C.k);
+                        xp[cell] = fma(al, pp[cell], xp[cell]);
+                        const double r = fma(-al, qp[cell], rp[cell]);
+                        rp[cell] = r;
+                        s = fma(r, r, s);
+                        vb[cell] = (T) r;
+                        vx[cell] = 0;
+                    }
+            }
         }
         const double a = block_sum(s, sh);
         if (threadIdx.x == 0) { partial[2 * c] = act ? a : 0.; partial[2 * c + 1] = 0.; }
@@ -838,14 +888,32 @@ __global__ void __launch_bounds__(256, 4) kr_from_vcycle(const LvlDev* __restric
         if (act) {
             const double* __restrict__ rp = Kp.r;
             const double* __restrict__ qp = Kp.q;
-            for (int rw = 0; rw < C.nrows; ++rw)
+            long long st, n;
+            if (chunk_pairs(L, C, st, n)) {
+                using V = typename Pair<T>::V;
+                const V* __restrict__ z2 = (const V*) (x + st);
+                const double2* __restrict__ r2 = (const double2*) (rp + st);
+                const double2* __restrict__ q2 = (const double2*) (qp + st);
 #pragma unroll 4
-                for (int t = threadIdx.x; t < C.cnt; t += blockDim.x) {
-                    const long long cell = cell_of(L, C.i0 + t, C.j + rw, C.k);
-                    const double z = (double) x[cell];
-                    s0 = fma(z, rp[cell], s0);
-                    s1 = fma(z, qp[cell], s1);
+                for (long long t = threadIdx.x; t < n / 2; t += blockDim.x) {
+                    const V zv = z2[t];
+                    const double2 rv = r2[t], qv = q2[t];
+                    const double za = (double) zv.x, zb = (double) zv.y;
+                    s0 = fma(za, rv.x, s0);
+                    s1 = fma(za, qv.x, s1);
+                    s0 = fma(zb, rv.y, s0);
+                    s1 = fma(zb, qv.y, s1);
                 }
+            } else {
+                for (int rw = 0; rw < C.nrows; ++rw)
+#pragma unroll 4
+                    for (int t = threadIdx.x; t < C.cnt; t += blockDim.x) {
+                        const long long cell = cell_of(L, C.i0 + t, C.j + rw, C.k);
+                        const double z = (double) x[cell];
+                        s0 = fma(z, rp[cell], s0);
+                        s1 = fma(z, qp[cell], s1);
+                    }
+            }
         }
         const double a = block_sum(s0, sh);
         const double b = block_sum(s1, sh);
@@ -877,13 +945,32 @@ __global__ void __launch_bounds__(256) kr_pupdate(const LvlDev* __restrict__ Ls,
         const double be = first ? 0. : sc[L.problem].beta;
         const T* __restrict__ x = Sel<T>::x(L);
         double* __restrict__ pp = Kp.p;
-        for (int rw = 0; rw < C.nrows; ++rw)
+        long long st, n;
+        if (chunk_pairs(L, C, st, n)) {
+            using V = typename Pair<T>::V;
+            const V* __restrict__ z2 = (const V*) (x + st);
+            double2* __restrict__ p2 = (double2*) (pp + st);
 #pragma unroll 4
-            for (int t = threadIdx.x; t < C.cnt; t += blockDim.x) {
-                const long long cell = cell_of(L, C.i0 + t, C.j + rw, C.k);
-                const double z = (double) x[cell];
-                pp[cell] = first ? z : fma(be, pp[cell], z);
+            for (long long t = threadIdx.x; t < n / 2; t += blockDim.x) {
+                const V zv = z2[t];
+                double2 pv;
+                if (first) pv = make_double2((double) zv.x, (double) zv.y);
+                else {
+                    pv = p2[t];
+                    pv.x = fma(be, pv.x, (double) zv.x);
+                    pv.y = fma(be, pv.y, (double) zv.y);
+                }
+                p2[t] = pv;
             }
+        } else {
+            for (int rw = 0; rw < C.nrows; ++rw)
+#pragma unroll 4
+                for (int t = threadIdx.x; t < C.cnt; t += blockDim.x) {
+                    const long long cell = cell_of(L, C.i0 + t, C.j + rw, C.k);
+                    const double z = (double) x[cell];
+                    pp[cell] = first ? z : fma(be, pp[cell], z);
+                }
+        }
     }
 }
 
