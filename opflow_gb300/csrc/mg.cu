@@ -791,7 +791,17 @@ __device__ __forceinline__ bool chunk_pairs(const LvlDev& L, const Chunk& C, lon
     if (!(C.nrows == 1 || (C.i0 == 0 && C.cnt == L.n[0]))) return false;
     start = cell_of(L, C.i0, C.j, C.k);
     n = (long long) C.cnt * C.nrows;
-    return ((start | n) & 1) == 0;
+    return true;
+}
+// Splits the contiguous run [start, start + n) into an odd head cell (start odd), the aligned pairs
+// [a, a + 2 np) and an odd tail cell; single(cell) is called by thread 0 for the head and the last
+// thread for the tail, pair(t) for pair t (cells a + 2t, a + 2t + 1) by the CTA's threads.
+__device__ __forceinline__ void split_run(long long start, long long n, long long& a, long long& np, long long& head, long long& tail) {
+    head = (start & 1) && n > 0 ? start : -1;
+    a = start + (head >= 0 ? 1 : 0);
+    const long long rest = n - (head >= 0 ? 1 : 0);
+    np = rest / 2;
+    tail = (rest & 1) ? a + 2 * np : -1;
 }
 template <typename T>
 struct Pair;
@@ -830,14 +840,26 @@ __global__ void __launch_bounds__(256, 4) kr_update(const LvlDev* __restrict__ L
             long long st, n;
             if (chunk_pairs(L, C, st, n)) {
                 using V = typename Pair<T>::V;
-                double2* __restrict__ x2 = (double2*) (xp + st);
-                const double2* __restrict__ p2 = (const double2*) (pp + st);
-                double2* __restrict__ r2 = (double2*) (rp + st);
-                const double2* __restrict__ q2 = (const double2*) (qp + st);
-                V* __restrict__ b2 = (V*) (vb + st);
-                V* __restrict__ z2 = (V*) (vx + st);
+                long long a0, np, head, tail;
+                split_run(st, n, a0, np, head, tail);
+                auto one = [&](long long cell) {
+                    xp[cell] = fma(al, pp[cell], xp[cell]);
+                    const double r = fma(-al, qp[cell], rp[cell]);
+                    rp[cell] = r;
+                    s = fma(r, r, s);
+                    vb[cell] = (T) r;
+                    vx[cell] = 0;
+                };
+                if (head >= 0 && threadIdx.x == 0) one(head);
+                if (tail >= 0 && threadIdx.x == blockDim.x - 1) one(tail);
+                double2* __restrict__ x2 = (double2*) (xp + a0);
+                const double2* __restrict__ p2 = (const double2*) (pp + a0);
+                double2* __restrict__ r2 = (double2*) (rp + a0);
+                const double2* __restrict__ q2 = (const double2*) (qp + a0);
+                V* __restrict__ b2 = (V*) (vb + a0);
+                V* __restrict__ z2 = (V*) (vx + a0);
 #pragma unroll 4
-                for (long long t = threadIdx.x; t < n / 2; t += blockDim.x) {
+                for (long long t = threadIdx.x; t < np; t += blockDim.x) {
                     double2 xv = x2[t];
                     const double2 pv = p2[t], qv = q2[t];
                     double2 rv = r2[t];
@@ -891,11 +913,20 @@ __global__ void __launch_bounds__(256, 4) kr_from_vcycle(const LvlDev* __restric
             long long st, n;
             if (chunk_pairs(L, C, st, n)) {
                 using V = typename Pair<T>::V;
-                const V* __restrict__ z2 = (const V*) (x + st);
-                const double2* __restrict__ r2 = (const double2*) (rp + st);
-                const double2* __restrict__ q2 = (const double2*) (qp + st);
+                long long a0, np, head, tail;
+                split_run(st, n, a0, np, head, tail);
+                auto one = [&](long long cell) {
+                    const double z = (double) x[cell];
+                    s0 = fma(z, rp[cell], s0);
+                    s1 = fma(z, qp[cell], s1);
+                };
+                if (head >= 0 && threadIdx.x == 0) one(head);
+                if (tail >= 0 && threadIdx.x == blockDim.x - 1) one(tail);
+                const V* __restrict__ z2 = (const V*) (x + a0);
+                const double2* __restrict__ r2 = (const double2*) (rp + a0);
+                const double2* __restrict__ q2 = (const double2*) (qp + a0);
 #pragma unroll 4
-                for (long long t = threadIdx.x; t < n / 2; t += blockDim.x) {
+                for (long long t = threadIdx.x; t < np; t += blockDim.x) {
                     const V zv = z2[t];
                     const double2 rv = r2[t], qv = q2[t];
                     const double za = (double) zv.x, zb = (double) zv.y;
@@ -948,10 +979,18 @@ __global__ void __launch_bounds__(256) kr_pupdate(const LvlDev* __restrict__ Ls,
         long long st, n;
         if (chunk_pairs(L, C, st, n)) {
             using V = typename Pair<T>::V;
-            const V* __restrict__ z2 = (const V*) (x + st);
-            double2* __restrict__ p2 = (double2*) (pp + st);
+            long long a0, np, head, tail;
+            split_run(st, n, a0, np, head, tail);
+            auto one = [&](long long cell) {
+                const double z = (double) x[cell];
+                pp[cell] = first ? z : fma(be, pp[cell], z);
+            };
+            if (head >= 0 && threadIdx.x == 0) one(head);
+            if (tail >= 0 && threadIdx.x == blockDim.x - 1) one(tail);
+            const V* __restrict__ z2 = (const V*) (x + a0);
+            double2* __restrict__ p2 = (double2*) (pp + a0);
 #pragma unroll 4
-            for (long long t = threadIdx.x; t < n / 2; t += blockDim.x) {
+            for (long long t = threadIdx.x; t < np; t += blockDim.x) {
                 const V zv = z2[t];
                 double2 pv;
                 if (first) pv = make_double2((double) zv.x, (double) zv.y);
