@@ -2,8 +2,9 @@
 
     OPFLOW_REFERENCE=<OpFlow tree> python tests/golden/make_adapter_golden.py
 
-For each example (examples/FTCS2D/FTCS-OMP.cpp, examples/CONV1D/CONV1D.cpp of the OpFlow tree, and
-tests/adapter/poisson_solve.cpp, a solve program on OpFlow's API) the source file is compiled as it is, with include/opflow_gb300/adapter ahead of OpFlow's include
+For each example (examples/FTCS2D/FTCS-OMP.cpp, examples/CONV1D/CONV1D.cpp and
+examples/EqnHandler/EqnHandler.cpp of the OpFlow tree, and tests/adapter/poisson_solve.cpp, a solve
+program on OpFlow's API) the source file is compiled as it is, with include/opflow_gb300/adapter ahead of OpFlow's include
 directories (its `#include <OpFlow>` then reads OpFlow's headers with CartesianField assignments routed
 to the engine), and linked with oracle/abi_double.c, the host stand-in of the engine's C ABI computed
 by the oracle.  The program runs with OPFLOW_ABI_RECORD set; the fields it creates and the assignment
@@ -36,7 +37,7 @@ import make_golden as mg  # noqa: E402
 
 # name -> (source, relative to the OpFlow tree unless it starts with "tests/")
 EXAMPLES = {"ftcs_omp": "examples/FTCS2D/FTCS-OMP.cpp", "conv1d": "examples/CONV1D/CONV1D.cpp",
-            "poisson_solve": "tests/adapter/poisson_solve.cpp"}
+            "poisson_solve": "tests/adapter/poisson_solve.cpp", "eqnhandler": "examples/EqnHandler/EqnHandler.cpp"}
 
 
 def source_path(ref, src):
@@ -129,6 +130,11 @@ def main():
                 out["reference"] = {"values": local.tolist(), "solves": [m for k, m, _ in recs if k == "SOLVE"],
                                     "note": "oracle/_ref/ref_solve program2d 64 0 1e-10 100 (the program on OpFlow + HYPRE); the "
                                             "adapter run on the stand-in C ABI (restated PCG + PFMG, warm starts) agrees to 1e-12"}
+            elif name == "eqnhandler":
+                # the example writes no field: the replay's solution is checked on the reference's system
+                # (the oracle's assembly of the recorded equation)
+                out["reference"] = {"note": "EqnHandler solves d2x(u) + d2y(u) == 1 with GMRES + PFMG and writes nothing; the "
+                                            "GPU replay's solution is checked against the oracle's assembly of that system"}
             else:
                 _, arr = cm.golden("conv1d_n101")
                 want = arr["u__data"]

@@ -13,6 +13,8 @@ OpFlow's expression types.  Checked here:
 - a solve program on OpFlow's API (tests/adapter/poisson_solve.cpp: Solve, then makeEqnSolveHandler
   solved twice): its recording holds the lowered equation and the solver parameters, and on the GPU the
   engine's solves reach the tolerance and agree with the reference's HYPRE solution;
+- examples/EqnHandler/EqnHandler.cpp (GMRES + PFMG, staticMat): on the GPU its solve meets the
+  handler's tolerance on the reference's system (oracle assembly);
 - where the OpFlow tree is named by OPFLOW_REFERENCE: the examples compile unchanged against the
   adapter and link against libopflow_gpu, and CONV1D, run on the host stand-in of the C ABI, writes the
   reference's values (the recording step, repeated).
@@ -25,6 +27,7 @@ import numpy as np
 import pytest
 
 import adapter_replay as ar
+import oracle_lib as orc
 import common as cm
 from opflow_gb300 import _capi as capi
 
@@ -97,7 +100,8 @@ def test_examples_compile_unchanged_against_the_adapter(tmp_path):
     subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle")])
     # linked against the engine itself
     for name, src in (("ftcs_omp", "examples/FTCS2D/FTCS-OMP.cpp"), ("conv1d", "examples/CONV1D/CONV1D.cpp"),
-                      ("poisson_solve", "tests/adapter/poisson_solve.cpp")):
+                      ("poisson_solve", "tests/adapter/poisson_solve.cpp"), ("eqnhandler", "examples/EqnHandler/EqnHandler.cpp"),
+                      ("ftcs1d", "examples/FTCS/FTCS.cpp"), ("liddriven2d", "examples/LidDriven/LidDriven2D.cpp")):
         _compile(ref, src, str(tmp_path / name), os.path.join(ROOT, "opflow_gb300"), "opflow_gpu")
     # CONV1D on the host stand-in of the C ABI writes the reference's values
     exe = str(tmp_path / "conv1d_double")
@@ -139,3 +143,42 @@ def test_recorded_solve_program_replays_on_the_gpu(ctx):
     got = ar.local_values(a, inf)
     want = np.array(rec["reference"]["values"])
     assert np.abs(got - want).max() <= 1e-8 * np.abs(want).max()
+
+
+def test_eqnhandler_recording_is_a_gmres_pfmg_handler():
+    """examples/EqnHandler/EqnHandler.cpp: makeEqnSolveHandler(d2x(e) + d2y(e) == 1.0, u,
+    PrecondStructSolver<GMRES, PFMG>) with staticMat, lowered by the adapter."""
+    rec = ar.load("eqnhandler")
+    assert rec["example"] == "examples/EqnHandler/EqnHandler.cpp"
+    solvers = [e for e in rec["events"] if e["ev"] == "solver"]
+    assert len(solvers) == 1 and sum(e["ev"] == "solve" for e in rec["events"]) == 1
+    p = solvers[0]["params"]
+    assert p["krylov"] == capi.KRYLOV_GMRES and p["precond"] == capi.PRECOND_MG and p["static_mat"] == 1
+    kinds = [n[0] for n in solvers[0]["nodes"]]
+    assert kinds.count(capi.NODE_D2) == 2 and kinds[-1] == capi.NODE_SUB and capi.NODE_CONST in kinds
+
+
+@pytest.mark.gpu
+def test_recorded_gmres_handler_replays_to_the_reference_system_on_the_gpu(ctx):
+    """The EqnHandler example's GMRES + multigrid solve, replayed through libopflow_gpu: the solution
+    meets the handler's tolerance on the reference's own system (the oracle's assembly of the recorded
+    equation, Dirichlet 0 on the 11 x 11 node mesh of [0, 10]^2)."""
+    rec = ar.load("eqnhandler")
+    states = []
+    out = ar.replay_gpu(rec, ctx, states)
+    assert len(states) == 1 and states[0].converged, (states[0].iterations, states[0].rel_residual)
+    ev = [e for e in rec["events"] if e["ev"] == "solver"][0]
+    fr = rec["fields"][0]
+    a, inf = out[fr["id"]]
+    from opflow_gb300 import api
+    # the recorded mesh and field description, as the example built them
+    mesh = api.CartesianMesh(2, fr["dims"][:2], fr["start"][:2], fr["pad_width"], [np.array(fr["x0"]), np.array(fr["x1"])],
+                             [np.array(fr["dx0"]), np.array(fr["dx1"])])
+    _, fd, _ = ar._descs(fr)
+    hf = orc.HostField(mesh, fd, data=a)
+    assert list(hf.data.shape) == [inf.data_dims[1], inf.data_dims[0]]
+    off, coef, rhs = orc.assemble(hf, ar._nodes(ev), [hf], 0, 0)
+    rng = hf.assignable()
+    x = hf.data[hf.slices(rng)].reshape(-1)
+    r, bn = orc.residual([q[1] - q[0] for q in rng], [0] * len(rng), off, coef, rhs, x)
+    assert r / bn <= 1e-8, r / bn
