@@ -703,9 +703,14 @@ int mg_finalize(MGSystem* S) {
     };
     if (const char* e = getenv("OPFLOW_MG_BOTTOM")) S->bottom_max = atoll(e);
     // level-0 chunks of the Krylov kernels: whole rows of one plane, about KCH cells each (rows longer
-    // than KCH are split), so the per-chunk reduction and its barriers are amortised over many cells
-    const int KCH = 8192;
+    // than KCH are split), so the per-chunk reduction and its barriers are amortised over many cells.
+    // KCH is 8192 for problems of at least 8192 cells per two SMs and halves (down to 1024) for smaller
+    // ones, so that a small problem alone still spreads over many SMs; it depends on the problem's size
+    // only, so a problem is chunked alike alone and in any batch.
     auto krylov_chunks = [&](int lvl_index, const LvlDev& L, std::vector<Chunk>& out) {
+        const long long per_two_sms = L.N / std::max(1, (ctx->num_sms + 1) / 2);
+        int KCH = 8192;
+        while (KCH > 1024 && KCH > per_two_sms) KCH /= 2;
         const int ny = L.ndim > 1 ? L.n[1] : 1, nz = L.ndim > 2 ? L.n[2] : 1;
         if (L.n[0] >= KCH) {
             for (int k = 0; k < nz; ++k)
