@@ -1133,6 +1133,11 @@ static int run_resident(opflow_ctx ctx, opflow_field dst, Plan& plan, unsigned l
     if (rc == OPFLOW_OK) rc = update_padding_full(dst, dst->buf[0]);
     if (rc == OPFLOW_OK) rc = update_padding_full(dst, dst->buf[1]);
     if (rc == OPFLOW_OK) dst->bc_fresh[0] = dst->bc_fresh[1] = true;
+    if (rc == OPFLOW_OK && steps > 2) {  // a TMA-staged step whose copy never completed
+        int err = 0;
+        rc = stencil_take_error(ctx->stream, &err);
+        if (rc == OPFLOW_OK && err) rc = fail(OPFLOW_E_CUDA, "a TMA-staged stencil step gave up waiting for its plane copies");
+    }
     return rc;
 }
 

@@ -7,9 +7,7 @@
 // batch.  T selects the precision of the V-cycle (float for the mixed form, double for the plain one);
 // the Krylov vectors, their updates and all inner products are float64.
 #include "mg_device.h"
-
-#include <cuda.h>
-#include <cudaTypedefs.h>
+#include "tma.h"
 
 #include <cstdlib>
 #include <type_traits>
@@ -345,49 +343,8 @@ __global__ void __launch_bounds__(32 * MG_ZT_Y) mg_prolong_z(const LvlDev* __res
 }
 
 // ---------------------------------------------------------------- TMA-staged z-marching smoother
-// TMA copies (global -> shared, completing on an mbarrier) and bounded mbarrier waits.  Every wait gives up after MBAR_SPINS polls; the kernel then records the failure in
-// g_mg_err, waits (bounded again) for the copies it issued and returns.
+// set by mg_smooth_zt when one of its bounded mbarrier waits (tma.h) gave up
 __device__ int g_mg_err;
-// polls of a wait (each suspends the thread for up to MBAR_SUSPEND_NS): about a second in all
-constexpr int MBAR_SPINS = 1 << 20;
-constexpr unsigned MBAR_SUSPEND_NS = 1000;
-
-__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned) __cvta_generic_to_shared(p); }
-__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
-__device__ __forceinline__ void mbar_arrive_expect(unsigned long long* bar, unsigned bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
-}
-// true once the phase of the given parity has completed; the thread is suspended (not spinning) while it
-// waits, for at most MBAR_SUSPEND_NS
-__device__ __forceinline__ bool mbar_test(unsigned long long* bar, unsigned parity) {
-    unsigned done;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(done)
-        : "r"(smem_addr(bar)), "r"(parity), "r"(MBAR_SUSPEND_NS)
-        : "memory");
-    return done != 0;
-}
-__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
-    for (int it = 0; it < MBAR_SPINS; ++it)
-        if (mbar_test(bar, parity)) return true;
-    return false;
-}
-
-// 3D tiled copy of a tensor map's box at (x, y, z) into shared memory, completing on `bar`
-__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z, unsigned long long* bar) {
-    asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_addr(dst)),
-                 "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_addr(bar))
-                 : "memory");
-}
-__device__ __forceinline__ void tensormap_acquire(const CUtensorMap* map) {
-    asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(map) : "memory");
-}
 
 // Red-black half sweep of a float32 class-table 3D level whose rows hold a multiple of 4 cells, the
 // planes staged in shared memory by TMA: a CTA owns 32 x-columns (one lane each, x origin a multiple
@@ -486,7 +443,8 @@ __global__ void __launch_bounds__(32 * MG_ZT_Y) mg_smooth_zt(const LvlDev* __res
         seq = base + (unsigned) (last - k0 + 2);
         if (failed) {
             // a copy never completed: record it, wait (bounded) for every copy this tile issued, stop
-            for (int p = k0 - 1; p <= issued; ++p) mbar_wait(&St.bar[slot_of(p)], phase_of(p));
+            // (the last fill of each slot: the earlier ones have completed)
+            for (int p = max(k0 - 1, issued - ZT_RING + 1); p <= issued; ++p) mbar_wait(&St.bar[slot_of(p)], phase_of(p));
             if (threadIdx.x == 0) atomicExch(&g_mg_err, 1);
             return;
         }
@@ -1106,16 +1064,7 @@ int mg_launch_smooth_zt(cudaStream_t s, int sms, const LvlDev* L, const Chunk* c
     return check_launch("mg_smooth_zt");
 }
 int mg_encode_zt_maps(const LvlDev& D, CUtensorMap* two) {
-    static const PFN_cuTensorMapEncodeTiled_v12000 enc = [] {
-        void* fn = nullptr;
-        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
-            q != cudaDriverEntryPointSuccess) {
-            cudaGetLastError();
-            fn = nullptr;
-        }
-        return (PFN_cuTensorMapEncodeTiled_v12000) fn;
-    }();
+    const PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
     if (!enc) return fail(OPFLOW_E_UNSUPPORTED, "cuTensorMapEncodeTiled is not available");
     const cuuint64_t dims[3] = {(cuuint64_t) D.n[0], (cuuint64_t) D.n[1], (cuuint64_t) D.n[2]};
     const cuuint64_t strides[2] = {(cuuint64_t) D.n[0] * 4, (cuuint64_t) D.n[0] * D.n[1] * 4};

@@ -11,6 +11,7 @@
 //   FAST  - exact 64-bit fixed point: values are converted once when staged, the second differences
 //           are exact integer sums, one 64x53-bit product per weight group, one rounding back.
 #include "stencil.h"
+#include "tma.h"
 #include "tune.h"
 
 #include <cstdio>
@@ -465,6 +466,156 @@ __global__ void __launch_bounds__(32 * RB_WARPS, RBX <= 4 ? 6 : (RBX <= 6 ? 5 : 
     }
 }
 
+// ------------------------------------------------------- 3D resident fixed point, TMA-staged planes
+// The steady-state step of a resident run (fixed point in, fixed point out) with its planes staged in
+// shared memory by TMA: a CTA owns FT_X x FT_Y points of the xy plane and a run of zchunk planes.  One
+// thread streams each plane's FT_W x FT_H box (the tile and its one-point halo, from (x origin - 1,
+// y origin - 1), an x coordinate on a 16-byte boundary) into a ring of FT_RING slots, up to
+// FT_RING - 2 planes ahead of the plane being updated; each slot's mbarrier counts the box's bytes.
+// One CTA barrier per plane: past it, the slot of the previous plane is refilled.
+// A thread updates FT_ROWS consecutive rows of one x-column: the centre values of planes k - 1 and k
+// stay in registers, the x and y neighbours and plane k + 1 come from shared memory, the results go
+// straight to global memory (64-bit coalesced stores).  The integer operations are those of
+// axis3d_fxres_kernel<0, *>, so the two give bit-identical fields.
+constexpr int FT_X = 64, FT_Y = 16, FT_ROWS = 4, FT_RING = 5;
+constexpr int FT_W = FT_X + 2, FT_H = FT_Y + 2;
+constexpr int FT_THREADS = FT_X * FT_Y / FT_ROWS;
+constexpr int FT_SLOT = ((FT_W * FT_H * 8 + 127) / 128) * 16;  // int64 per slot (a 128-byte multiple)
+constexpr unsigned FT_BYTES = FT_W * FT_H * 8;                  // bytes per plane box
+struct FtStage {
+    long long v[FT_RING][FT_SLOT];
+    unsigned long long bar[FT_RING];
+};
+static_assert((FT_W * 8) % 16 == 0, "box rows are 16-byte multiples");
+static_assert(FT_RING >= 3, "planes k and k + 1 are read while k + 2 is in flight");
+
+// set when a wait of axis3d_fxtma_kernel gave up
+__device__ int g_st_err;
+
+__global__ void __launch_bounds__(FT_THREADS, 4) axis3d_fxtma_kernel(const __grid_constant__ CUtensorMap map, FieldView in, FieldView out,
+                                                                   Box box, int iso, long long ws0, long long ws1, long long ws2, int zchunk,
+                                                                   int tiles_x) {
+    __shared__ __align__(128) FtStage St;
+    const int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
+    const int x0 = box.lo[0] + tx * FT_X, y0 = box.lo[1] + ty * FT_Y;
+    const int zs = box.lo[2] + blockIdx.y * zchunk;
+    const int ze = min(zs + zchunk, box.hi[2]);
+    if (zs >= ze) return;  // (the whole CTA)
+    const int lx = threadIdx.x % FT_X, ly0 = (threadIdx.x / FT_X) * FT_ROWS;
+    const int i = x0 + lx;
+    const bool vx = i < box.hi[0];
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < FT_RING; ++s) mbar_init(&St.bar[s], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    // plane p (zs - 1 .. ze) is this tile's plane number q = p - zs + 1: slot q % FT_RING, phase (q / FT_RING) & 1
+    auto slot_of = [&](int p) { return (p - zs + 1) % FT_RING; };
+    auto phase_of = [&](int p) { return (unsigned) ((p - zs + 1) / FT_RING) & 1u; };
+    const int cx = x0 - 1 - in.off[0], cy = y0 - 1 - in.off[1];
+    const bool producer = threadIdx.x == 0;
+    auto issue = [&](int p) {
+        const int s = slot_of(p);
+        mbar_arrive_expect(&St.bar[s], FT_BYTES);
+        tma_load_3d(&St.v[s][0], &map, cx, cy, p - in.off[2], &St.bar[s]);
+    };
+    const int last = ze;
+    int issued = min(zs - 1 + FT_RING - 1, last);  // planes zs - 1 .. issued fill every slot
+    if (producer)
+        for (int p = zs - 1; p <= issued; ++p) issue(p);
+    bool ok = mbar_wait(&St.bar[slot_of(zs - 1)], phase_of(zs - 1));
+    ok = ok && mbar_wait(&St.bar[slot_of(zs)], phase_of(zs));
+    long long below[FT_ROWS], cur[FT_ROWS];
+    const int at0 = (ly0 + 1) * FT_W + lx + 1;  // the thread's first point in a slot
+    if (ok) {
+        const long long* Sb = St.v[slot_of(zs - 1)];
+        const long long* Sc = St.v[slot_of(zs)];
+#pragma unroll
+        for (int r = 0; r < FT_ROWS; ++r) {
+            below[r] = Sb[at0 + r * FT_W];
+            cur[r] = Sc[at0 + r * FT_W];
+        }
+    }
+    double* const ocol = out.data + (i - out.off[0]) - (long long) out.off[1] * out.sy - (long long) out.off[2] * out.sz;
+    bool failed = false;
+    for (int k = zs; k < ze; ++k) {
+        ok = ok && mbar_wait(&St.bar[slot_of(k + 1)], phase_of(k + 1));
+        if (__syncthreads_or(!ok)) {  // (the same answer in every thread)
+            failed = true;
+            break;
+        }
+        if (issued < last) {  // every thread is past step k - 1: plane k - 1's slot takes plane k + FT_RING - 1
+            ++issued;
+            if (producer) issue(issued);
+        }
+        const long long* S = St.v[slot_of(k)];
+        const long long* A = St.v[slot_of(k + 1)];
+        long long above[FT_ROWS];
+#pragma unroll
+        for (int r = 0; r < FT_ROWS; ++r) above[r] = A[at0 + r * FT_W];
+#pragma unroll
+        for (int r = 0; r < FT_ROWS; ++r) {
+            const int at = at0 + r * FT_W;
+            const long long c = cur[r];
+            const long long l = S[at - 1], rr = S[at + 1];
+            const long long b = r == 0 ? S[at - FT_W] : cur[r - 1];
+            const long long t = r == FT_ROWS - 1 ? S[at + FT_W] : cur[r + 1];
+            const long long zb = below[r], za = above[r];
+            const int j = y0 + ly0 + r;
+            if (vx && j < box.hi[1]) {
+                long long q = c;
+                if (iso) {
+                    q += fx_mul_hi(((l + rr) + (b + t)) + ((zb + za) - 6 * c), ws0);
+                } else {
+                    q += fx_mul_hi((l + rr) - 2 * c, ws0);
+                    q += fx_mul_hi((b + t) - 2 * c, ws1);
+                    q += fx_mul_hi((zb + za) - 2 * c, ws2);
+                }
+                ocol[(long long) j * out.sy + (long long) k * out.sz] = __longlong_as_double(q);
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < FT_ROWS; ++r) {
+            below[r] = cur[r];
+            cur[r] = above[r];
+        }
+    }
+    if (failed) {
+        // a copy never completed: record it, wait (bounded) for every copy this tile issued, stop
+        // (the last fill of each slot: the earlier ones have completed)
+        if (producer) {
+            for (int p = max(zs - 1, issued - FT_RING + 1); p <= issued; ++p) mbar_wait(&St.bar[slot_of(p)], phase_of(p));
+            atomicExch(&g_st_err, 1);
+        }
+    }
+}
+
+// The TMA-staged steady-state step (default) or the register-blocked one: OPFLOW_FXRES_TMA=0|1, read at
+// every launch.
+static bool fxtma_enabled() {
+    const char* e = getenv("OPFLOW_FXRES_TMA");
+    return !(e && e[0] == '0');
+}
+
+int stencil_take_error(cudaStream_t s, int* err) {
+    int zero = 0;
+    OPG_CUDA(cudaMemcpyFromSymbolAsync(err, g_st_err, sizeof(int), 0, cudaMemcpyDeviceToHost, s));
+    OPG_CUDA(cudaStreamSynchronize(s));
+    if (*err) OPG_CUDA(cudaMemcpyToSymbolAsync(g_st_err, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, s));
+    return OPFLOW_OK;
+}
+
+// Whether the TMA-staged steady-state step takes this box of this buffer: rows and planes on 16-byte
+// strides, a 16-byte aligned buffer, the tiles' x origins minus one on even indices (16-byte boundaries)
+// and the box's halo inside the buffer.
+static bool fxtma_ok(const FieldView& in, const Box& box) {
+    if (((unsigned long long) in.data & 15ull) != 0 || (in.sy & 1) != 0 || (in.sz & 1) != 0) return false;
+    if (((box.lo[0] - 1 - in.off[0]) & 1) != 0) return false;
+    for (int d = 0; d < 3; ++d)
+        if (box.lo[d] - 1 < in.off[d] || box.hi[d] + 1 > in.off[d] + in.dims[d]) return false;
+    return in.dims[0] <= in.sy && (long long) in.dims[1] * in.sy <= in.sz;
+}
+
 bool axis_resident_ok(const AxisParams& P) {
     for (int d = 0; d < P.ndim; ++d) {
         const int g = P.iso ? 0 : d;
@@ -497,6 +648,29 @@ int axis_launch_resident(opflow_ctx ctx, const FieldView& in, const FieldView& o
     for (int d = 0; d < 3; ++d) {
         const int gi = P.iso ? 0 : d;
         ws[d] = (long long) (P.wm[gi] << (64 - P.wshift[gi]));
+    }
+    if (!first && !last && fxtma_enabled() && fxtma_ok(in, box)) {
+        const PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+        CUtensorMap map;
+        const cuuint64_t dims[3] = {(cuuint64_t) in.dims[0], (cuuint64_t) in.dims[1], (cuuint64_t) in.dims[2]};
+        const cuuint64_t strides[2] = {(cuuint64_t) in.sy * 8, (cuuint64_t) in.sz * 8};
+        const cuuint32_t boxd[3] = {FT_W, FT_H, 1}, ones[3] = {1, 1, 1};
+        if (enc && enc(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, (void*) in.data, dims, strides, boxd, ones, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                       CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS) {
+            // planes per CTA: OPFLOW_FXTMA_Z for sweeps
+            int zc = 32;
+            if (const char* e = getenv("OPFLOW_FXTMA_Z")) zc = std::max(4, std::min(1024, atoi(e)));
+            const int ftx = (nx + FT_X - 1) / FT_X, fty = (ny + FT_Y - 1) / FT_Y;
+            const int zch = (nz + zc - 1) / zc;
+            long long ws[3];
+            for (int d = 0; d < 3; ++d) {
+                const int gi = P.iso ? 0 : d;
+                ws[d] = (long long) (P.wm[gi] << (64 - P.wshift[gi]));
+            }
+            axis3d_fxtma_kernel<<<dim3(ftx * fty, zch), FT_THREADS, 0, ctx->stream>>>(map, in, out, box, P.iso, ws[0], ws[1], ws[2], zc, ftx);
+            OPG_LAUNCHED();
+            return check_launch("axis3d_fxtma_kernel");
+        }
     }
     const int mode = (first ? 1 : 0) | (last ? 2 : 0);
     auto go = [&](auto rb_tag) {

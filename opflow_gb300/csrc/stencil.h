@@ -27,5 +27,7 @@ int axis_launch(opflow_ctx ctx, const FieldView& in, const FieldView& out, const
 bool axis_resident_ok(const AxisParams& P);  // weights the resident kernel's product takes
 int axis_launch_resident(opflow_ctx ctx, const FieldView& in, const FieldView& out, const Box& box, const AxisParams& P,
                          const unsigned long long* maxslots, bool first, bool last);
+// Reads and clears the flag a TMA-staged step sets when one of its bounded waits gave up.
+int stencil_take_error(cudaStream_t s, int* err);
 
 }  // namespace opg
