@@ -1073,20 +1073,21 @@ static void free_plan(Plan* p) {
 }
 
 // A run of fixed-point steps can keep the field in fixed point between its steps when the update reads
-// only the destination (u = u + sum_d w_d (u(i-e_d) + u(i+e_d) - 2u), 3D), the values outside the
+// only the destination (u = u + sum_d w_d (u(i-e_d) + u(i+e_d) - 2u), 2D or 3D), the values outside the
 // update box are constants (node-centred Dirichlet on every side, no ghost layer: updatePadding rewrites
 // only those constants) and the weights obey the maximum principle (w_d >= 0, 1 - 2 sum w_d >= 0), so
 // that the initial bound on |u| holds for every step.  OPFLOW_FX_RESIDENT=0 turns it off.
 static bool resident_eligible(const Plan& plan, opflow_field dst, const opflow_field* leaves, int steps) {
-    if (plan.kind != PLAN_AXIS_FAST || !plan.aliased || steps < 2 || plan.axis.ndim != 3) return false;
+    if (plan.kind != PLAN_AXIS_FAST || !plan.aliased || steps < 2 || plan.axis.ndim < 2 || plan.axis.ndim != dst->info.ndim) return false;
     if (leaves[plan.src_slot] != dst || !dst->padding_is_step0_only()) return false;
     const char* e = getenv("OPFLOW_FX_RESIDENT");
     if (e && e[0] == '0') return false;
-    for (int d = 0; d < 3; ++d)
+    const int D = plan.axis.ndim;
+    for (int d = 0; d < D; ++d)
         for (int sd = 0; sd < 2; ++sd)
             if (dst->desc.loc[d] != OPFLOW_CORNER || dst->desc.bc_type[d][sd] != OPFLOW_BC_DIRC) return false;
     double sum = 0.;
-    for (int d = 0; d < 3; ++d) {
+    for (int d = 0; d < D; ++d) {
         const int g = plan.axis.iso ? 0 : d;
         if (plan.axis.wneg[g]) return false;
         sum += std::ldexp((double) plan.axis.wm[g], -plan.axis.wshift[g]);
@@ -1107,6 +1108,37 @@ static long long host_fx(double v, int E) {
     return (long long) std::round(x);
 }
 
+// `reps` replays of a graph of RES_GRAPH_STEPS steady-state resident steps (fixed point in and out),
+// captured from the field's current buffers; the field's buffer index ends where it started.
+constexpr int RES_GRAPH_STEPS = 32;
+static_assert(RES_GRAPH_STEPS % 2 == 0, "a replay returns the field to the buffer it started from");
+static int run_resident_graph(opflow_ctx ctx, opflow_field dst, Plan& plan, unsigned long long* maxslots, int reps) {
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    OPG_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = OPFLOW_OK;
+    const uint64_t before = g_launches.load();
+    FieldView a = dst->view(), b = dst->view_back();
+    for (int q = 0; q < RES_GRAPH_STEPS && rc == OPFLOW_OK; ++q) {
+        rc = axis_launch_resident(ctx, a, b, plan.box, plan.axis, maxslots, false, false);
+        std::swap(a, b);
+    }
+    const uint64_t per_replay = g_launches.load() - before;
+    g_launches.fetch_sub(per_replay);  // counted below, once per replay
+    const cudaError_t e_end = cudaStreamEndCapture(ctx->stream, &g);
+    if (rc == OPFLOW_OK && e_end != cudaSuccess) rc = fail(OPFLOW_E_CUDA, "resident-step graph capture failed: %s", cudaGetErrorString(e_end));
+    if (rc == OPFLOW_OK && cudaGraphInstantiate(&exec, g, 0) != cudaSuccess) rc = fail(OPFLOW_E_CUDA, "resident-step graph instantiation failed");
+    for (int r = 0; r < reps && rc == OPFLOW_OK; ++r) {
+        if (cudaGraphLaunch(exec, ctx->stream) != cudaSuccess) rc = fail(OPFLOW_E_CUDA, "resident-step graph launch failed");
+        g_launches.fetch_add(per_replay);
+    }
+    if (exec) cudaGraphExecDestroy(exec);
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    dst->version += (unsigned long long) reps * RES_GRAPH_STEPS;
+    return rc;
+}
+
 // K >= 2 steps with the field in fixed point between them: step 1 reads float64; then the boundary
 // nodes of both buffers take their constants' fixed-point bit patterns; the last step writes float64
 // and the boundary constants are written back as float64 into both buffers.
@@ -1121,6 +1153,14 @@ static int run_resident(opflow_ctx ctx, opflow_field dst, Plan& plan, unsigned l
         for (int sd = 0; sd < 2; ++sd) fxv[d][sd] = __builtin_bit_cast(double, host_fx(dst->desc.bc_value[d][sd], E));
     int rc = OPFLOW_OK;
     for (int s = 0; s < steps && rc == OPFLOW_OK; ++s) {
+        if (s == 1 && dst->info.ndim == 2 && steps - 2 >= 2 * RES_GRAPH_STEPS) {
+            // a long run of short (2D) steady-state steps: replays of one graph of RES_GRAPH_STEPS launches
+            // (an even count: every replay starts from the same buffer)
+            const int reps = (steps - 2) / RES_GRAPH_STEPS;
+            rc = run_resident_graph(ctx, dst, plan, maxslots, reps);
+            s += reps * RES_GRAPH_STEPS - 1;
+            continue;
+        }
         rc = axis_launch_resident(ctx, dst->view(), dst->view_back(), plan.box, plan.axis, maxslots, s == 0, s == steps - 1);
         dst->cur = 1 - dst->cur;
         dst->version++;
@@ -1133,7 +1173,7 @@ static int run_resident(opflow_ctx ctx, opflow_field dst, Plan& plan, unsigned l
     if (rc == OPFLOW_OK) rc = update_padding_full(dst, dst->buf[0]);
     if (rc == OPFLOW_OK) rc = update_padding_full(dst, dst->buf[1]);
     if (rc == OPFLOW_OK) dst->bc_fresh[0] = dst->bc_fresh[1] = true;
-    if (rc == OPFLOW_OK && steps > 2) {  // a TMA-staged step whose copy never completed
+    if (rc == OPFLOW_OK && steps > 2 && dst->info.ndim == 3) {  // a TMA-staged step whose copy never completed
         int err = 0;
         rc = stencil_take_error(ctx->stream, &err);
         if (rc == OPFLOW_OK && err) rc = fail(OPFLOW_E_CUDA, "a TMA-staged stencil step gave up waiting for its plane copies");

@@ -466,6 +466,57 @@ __global__ void __launch_bounds__(32 * RB_WARPS, RBX <= 4 ? 6 : (RBX <= 6 ? 5 : 
     }
 }
 
+// -------------------------------------------------------------------------- 2D resident fixed point
+// One step of a resident fixed-point run on a 2D grid (u + w_x (u(i-1) + u(i+1) - 2u) + w_y (...), or
+// one weight times the four neighbours' sum minus four times the centre): a warp covers 32 consecutive
+// x-columns and updates the 30 inner ones over R2 rows, loading its R2 + 2 rows at once (every load in
+// flight together: a 2D grid of this kind is usually L2-resident, so a step is one round trip plus the
+// bandwidth time), x neighbours by warp shuffles.  MODE bit 0: float64 in (converted as loaded), bit 1:
+// float64 out; the steady state converts nothing.
+constexpr int R2ROWS = 8;
+
+template <int MODE>
+__global__ void __launch_bounds__(32 * RB_WARPS) axis2d_fxres_kernel(FieldView in, FieldView out, Box box, int iso, long long ws0, long long ws1,
+                                                                   const unsigned long long* maxslots, unsigned long long bound_bits,
+                                                                   int tiles_x, int tiles_y) {
+    constexpr bool IN_F64 = (MODE & 1) != 0, OUT_F64 = (MODE & 2) != 0;
+    const int lane = threadIdx.x & 31;
+    const int warp = blockIdx.x * RB_WARPS + (threadIdx.x >> 5);
+    if (warp >= tiles_x * tiles_y) return;
+    const int tx = warp % tiles_x, ty = warp / tiles_x;
+    const int x0 = box.lo[0] + tx * RB_COLS, y0 = box.lo[1] + ty * R2ROWS;
+    const int i = x0 - 1 + lane;
+    const bool vx = lane >= 1 && lane <= RB_COLS && i < box.hi[0];
+    const int ic = min(i, box.hi[0]);
+    const int k = box.lo[2];
+    const int E = (MODE != 0) ? scale_exp(maxslots, 0, bound_bits) : 0;
+    long long v[R2ROWS + 2];
+#pragma unroll
+    for (int r = 0; r < R2ROWS + 2; ++r) {
+        const double d = ld3(in, ic, min(y0 - 1 + r, box.hi[1]), k);
+        if constexpr (IN_F64) v[r] = fx_from(d, E);
+        else v[r] = __double_as_longlong(d);
+    }
+    double* const orow = out.data + (i - out.off[0]) - (long long) out.off[1] * out.sy + (long long) (k - out.off[2]) * out.sz;
+#pragma unroll
+    for (int r = 0; r < R2ROWS; ++r) {
+        const long long c = v[r + 1];
+        const long long l = __shfl_up_sync(0xffffffffu, c, 1);
+        const long long rr = __shfl_down_sync(0xffffffffu, c, 1);
+        if (vx && y0 + r < box.hi[1]) {
+            const long long b = v[r], t = v[r + 2];
+            long long q = c;
+            if (iso) {
+                q += fx_mul_hi((l + rr) + (b + t) - 4 * c, ws0);
+            } else {
+                q += fx_mul_hi((l + rr) - 2 * c, ws0);
+                q += fx_mul_hi((b + t) - 2 * c, ws1);
+            }
+            orow[(long long) (y0 + r) * out.sy] = OUT_F64 ? fx_to(q, E) : __longlong_as_double(q);
+        }
+    }
+}
+
 // ------------------------------------------------------- 3D resident fixed point, TMA-staged planes
 // The steady-state step of a resident run (fixed point in, fixed point out) with its planes staged in
 // shared memory by TMA: a CTA owns FT_X x FT_Y points of the xy plane and a run of zchunk planes.  One
@@ -631,7 +682,22 @@ int axis_launch_resident(opflow_ctx ctx, const FieldView& in, const FieldView& o
     if (!axis_resident_ok(P)) return fail(OPFLOW_E_UNSUPPORTED, "weights outside the resident fixed-point kernel's range");
     const int nx = box.hi[0] - box.lo[0], ny = box.hi[1] - box.lo[1], nz = box.hi[2] - box.lo[2];
     if (nx <= 0 || ny <= 0 || nz <= 0) return OPFLOW_OK;
-    if (P.ndim != 3) return fail(OPFLOW_E_UNSUPPORTED, "the resident fixed-point kernel covers 3D grids");
+    if (P.ndim == 2) {
+        const int tiles_x = (nx + RB_COLS - 1) / RB_COLS, tiles_y = (ny + R2ROWS - 1) / R2ROWS;
+        const int g = (int) (((long long) tiles_x * tiles_y + RB_WARPS - 1) / RB_WARPS);
+        const int gi1 = P.iso ? 0 : 1;
+        const long long w0 = (long long) (P.wm[0] << (64 - P.wshift[0])), w1 = (long long) (P.wm[gi1] << (64 - P.wshift[gi1]));
+        const int mode = (first ? 1 : 0) | (last ? 2 : 0);
+        switch (mode) {
+            case 0: axis2d_fxres_kernel<0><<<g, 32 * RB_WARPS, 0, ctx->stream>>>(in, out, box, P.iso, w0, w1, maxslots, P.bound_bits, tiles_x, tiles_y); break;
+            case 1: axis2d_fxres_kernel<1><<<g, 32 * RB_WARPS, 0, ctx->stream>>>(in, out, box, P.iso, w0, w1, maxslots, P.bound_bits, tiles_x, tiles_y); break;
+            case 2: axis2d_fxres_kernel<2><<<g, 32 * RB_WARPS, 0, ctx->stream>>>(in, out, box, P.iso, w0, w1, maxslots, P.bound_bits, tiles_x, tiles_y); break;
+            default: axis2d_fxres_kernel<3><<<g, 32 * RB_WARPS, 0, ctx->stream>>>(in, out, box, P.iso, w0, w1, maxslots, P.bound_bits, tiles_x, tiles_y); break;
+        }
+        OPG_LAUNCHED();
+        return check_launch("axis2d_fxres_kernel");
+    }
+    if (P.ndim != 3) return fail(OPFLOW_E_UNSUPPORTED, "the resident fixed-point kernels cover 2D and 3D grids");
     // rows per warp: 6 (the measured best at 512^3); OPFLOW_FXRES_RB=4|6|8 for sweeps
     int rbx = 6;
     if (const char* e = getenv("OPFLOW_FXRES_RB")) rbx = atoi(e) == 4 ? 4 : (atoi(e) == 8 ? 8 : 6);

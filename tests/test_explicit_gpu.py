@@ -346,6 +346,35 @@ def test_fast_resident_run_at_the_512_config_within_1e14_of_exact(ctx, monkeypat
         assert rel <= 1e-14, (name, rel)
 
 
+@pytest.mark.parametrize("dims,steps,bcv", [((1025, 1025), 1000, 0.0), ((100, 37), 300, 0.5), ((33, 70), 200, -0.75)])
+def test_fast_resident_2d_runs_within_1e14_of_exact(ctx, monkeypatch, dims, steps, bcv):
+    """Resident fixed-point runs on 2D node grids (axis2d_fxres_kernel): the FTCS2D configuration (1025^2,
+    U[0,1) interior, Dirichlet 0, dt = 0.2 h^2, 1000 steps) and ragged grids with two weights and nonzero
+    Dirichlet values, against the bit-exact IEEE run: normwise relative error <= 1e-14, and so is the
+    per-step fixed-point form."""
+    mesh = cm.mesh_uniform(list(dims))
+    fd = cm.field_desc(2, capi.CORNER, [(capi.BC_DIRC, capi.BC_DIRC)] * 2, [(bcv, bcv)] * 2)
+    h0 = orc.HostField(mesh, fd)
+    cm.seeded_interior(h0, 2024, dims[0])
+    h0.update_padding()
+    hmin = 1.0 / (max(dims) - 1)
+    s = 0.2 * hmin * hmin
+    out = {}
+    for name, mode, env in (("exact", "exact", "1"), ("resident", "fast", "1"), ("per_step", "fast", "0")):
+        monkeypatch.setenv("OPFLOW_FX_RESIDENT", env)
+        u = gpu_field(ctx, mesh, fd, h0)
+        u.assign(cm.ftcs_expr(u, s, 2), steps=steps, mode=mode)
+        out[name] = u.download()
+        del u
+    e = out["exact"]
+    for name in ("resident", "per_step"):
+        rel = np.abs(out[name] - e).max() / np.abs(e).max()
+        print("\n%s x %d FTCS2D: %s fixed point vs exact: %.2e" % (dims, steps, name, rel))
+        assert rel <= 1e-14, (name, rel)
+    # the boundary nodes hold their float64 constants again
+    assert np.all(out["resident"][0, :] == bcv) and np.all(out["resident"][:, -1] == bcv)
+
+
 @pytest.mark.parametrize("dims", [(150, 83, 70), (96, 96, 96), (67, 40, 37)])
 def test_fast_resident_tma_staged_and_register_steps_bit_identical(ctx, monkeypatch, dims):
     """The steady-state step of a resident fixed-point run in its two forms - planes staged in shared
