@@ -346,37 +346,40 @@ __global__ void __launch_bounds__(32 * MG_ZT_Y) mg_prolong_z(const LvlDev* __res
 // set by mg_smooth_zt when one of its bounded mbarrier waits (tma.h) gave up
 __device__ int g_mg_err;
 
-// Red-black half sweep of a float32 class-table 3D level whose rows hold a multiple of 4 cells, the
-// planes staged in shared memory by TMA: a CTA owns 32 x-columns (one lane each, x origin a multiple
-// of 32) by MG_ZT_Y rows (one warp each) and a run of planes.  One thread streams each plane as two
-// tensor-map boxes - x: 40 x (MG_ZT_Y + 2) cells from (x origin - 4, y origin - 1), the halo, its x
-// coordinate on a 16-byte boundary; b: 32 x MG_ZT_Y - into a ring of ZT_RING slots, ZT_AHEAD planes
-// ahead of the plane being updated; each slot's mbarrier counts the bytes.  Cells outside the level
-// arrive as zeros: only boundary cells, which take the general path from global memory (queued), would
-// read them.  Updates go straight to global memory: a half sweep reads only the other colour, which it
-// never writes.  Interior cells use the interior class's coefficients in the other kernels' operation
-// order (bit-identical).  maps[2 * level] and maps[2 * level + 1] are the level's x and b maps.
-constexpr int ZT_RING = 8, ZT_AHEAD = 5, ZT_W = 40, ZT_H = MG_ZT_Y + 2;
-constexpr int ZT_XSLOT = ((ZT_W * ZT_H * 4 + 127) / 128) * 32;  // floats per x slot (128-byte multiple)
-constexpr unsigned ZT_BYTES = (ZT_W * ZT_H + 32 * MG_ZT_Y) * 4;   // bytes per plane (both boxes)
+// Red-black half sweep of a non-periodic float32 class-table 3D level whose rows hold a multiple of 4
+// cells, the planes staged in shared memory by TMA.  A CTA of 256 threads owns MG_ZT2_X x-columns (x
+// origin a multiple of MG_ZT2_X) by MG_ZT2_Y rows and a run of planes.  Thread (p, q) = (tid % 32,
+// tid / 32) holds the column pair 2p, 2p + 1 of rows 2q, 2q + 1 and updates, on every plane, the cell of
+// the colour in each of its two rows, so every thread updates two cells per plane.  One thread streams
+// each plane as two tensor-map boxes - x: (MG_ZT2_X + 8) x (MG_ZT2_Y + 2) cells from (x origin - 4,
+// y origin - 1), the halo, its x coordinate on a 16-byte boundary; b: MG_ZT2_X x MG_ZT2_Y - into a ring
+// of ZT_RING slots; each slot's mbarrier counts both boxes' bytes.  The planes k - 1, k, k + 1 are read
+// at step k while k + 2 .. k + 4 are in flight; past step k's barrier the slot of plane k - 2 takes
+// plane k + 4.  Updates go straight to global memory: a half sweep reads only the other colour, which
+// it never writes.  Interior cells use the interior class's coefficients in the other kernels' operation
+// order; cells on the level's faces take their class's coefficients and skip the absent neighbours, as
+// the per-cell path (stencil_parts) does, also from shared memory: bit-identical results.
+// maps[2 * level] and maps[2 * level + 1] are the level's x and b maps.
+constexpr int ZT_RING = 6, ZT_W = MG_ZT2_X + 8, ZT_H = MG_ZT2_Y + 2;
+constexpr int ZT_XSLOT = ((ZT_W * ZT_H * 4 + 127) / 128) * 32;    // floats per x slot (128-byte multiple)
+constexpr int ZT_BSLOT = MG_ZT2_X * MG_ZT2_Y;                      // floats per b slot (128-byte multiple)
+constexpr unsigned ZT_BYTES = (ZT_W * ZT_H + MG_ZT2_X * MG_ZT2_Y) * 4;  // bytes per plane (both boxes)
 struct ZtStage {
     float x[ZT_RING][ZT_XSLOT];
-    float b[ZT_RING][MG_ZT_Y * 32];
+    float b[ZT_RING][ZT_BSLOT];
     unsigned long long bar[ZT_RING];
 };
-// the slot refilled at step k held plane k + ZT_AHEAD - ZT_RING, last read at step k + ZT_AHEAD - ZT_RING + 1,
-// which every thread has left once it passes step k's first barrier
-static_assert(ZT_AHEAD + 2 <= ZT_RING, "a slot is refilled only after its plane is no longer read");
-static_assert((MG_ZT_Y * 32 * 4) % 128 == 0, "b slots on 128-byte boundaries");
+static_assert(MG_ZT2_X == 64 && MG_ZT2_Y == 16, "the thread layout covers 64 x 16 cells with 256 threads");
+static_assert((ZT_BSLOT * 4) % 128 == 0 && (ZT_W * 4) % 16 == 0, "slots on 128-byte boundaries, box rows 16-byte multiples");
+constexpr size_t ZT_SMEM = sizeof(ZtStage) + 128;  // (+ alignment of the dynamic shared memory to 128 bytes)
 
-__global__ void __launch_bounds__(32 * MG_ZT_Y) mg_smooth_zt(const LvlDev* __restrict__ Ls, const Chunk* __restrict__ ch, int nch, int color,
-                                                            const Scal* sc, const CUtensorMap* __restrict__ maps) {
-    __shared__ __align__(128) ZtStage St;
-    __shared__ ZQueue Q;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+__global__ void __launch_bounds__(256) mg_smooth_zt(const LvlDev* __restrict__ Ls, const Chunk* __restrict__ ch, int nch, int color,
+                                                   const Scal* sc, const CUtensorMap* __restrict__ maps) {
+    extern __shared__ unsigned char zt_raw[];
+    ZtStage& St = *reinterpret_cast<ZtStage*>(zt_raw + ((128 - (smem_addr(zt_raw) & 127)) & 127));
+    const int px = threadIdx.x & 31, ry = threadIdx.x >> 5;
     if (threadIdx.x == 0) {
         for (int s = 0; s < ZT_RING; ++s) mbar_init(&St.bar[s], 1);
-        Q.n = 0;
         mbar_fence_init();
     }
     __syncthreads();
@@ -386,6 +389,7 @@ __global__ void __launch_bounds__(32 * MG_ZT_Y) mg_smooth_zt(const LvlDev* __res
         if (!active(Ls, C, sc)) continue;
         const LvlDev& L = Ls[C.lvl];
         const int n0 = L.n[0], n1 = L.n[1], n2 = L.n[2];
+        const long long sy = n0, sz = (long long) n0 * n1;
         const int i0 = C.i0, j0 = C.j, k0 = C.k, k1 = min(C.k + C.nrows, n2);
         float* x = L.x32;
         const float* t = L.T32 + 13 * TSTRIDE;
@@ -403,52 +407,70 @@ __global__ void __launch_bounds__(32 * MG_ZT_Y) mg_smooth_zt(const LvlDev* __res
             tma_load_3d(&St.x[s][0], mx, i0 - 4, j0 - 1, p, &St.bar[s]);
             tma_load_3d(&St.b[s][0], mb, i0, j0, p, &St.bar[s]);
         };
-        int issued = min(k0 - 1 + ZT_AHEAD, last);  // the last plane issued
+        int issued = min(k0 - 1 + ZT_RING - 1, last);  // planes k0 - 1 .. issued fill every slot
         if (producer) {
             tensormap_acquire(mx);
             tensormap_acquire(mb);
             for (int p = k0 - 1; p <= issued; ++p) issue(p);
         }
-        int waited = k0 - 2;  // the last plane waited for
-        bool ok = true, failed = false;
+        bool ok = mbar_wait(&St.bar[slot_of(k0 - 1)], phase_of(k0 - 1));
+        ok = ok && mbar_wait(&St.bar[slot_of(k0)], phase_of(k0));
+        bool failed = false;
         for (int k = k0; k < k1; ++k) {
-            for (int p = waited + 1; p <= k + 1; ++p) ok = ok && mbar_wait(&St.bar[slot_of(p)], phase_of(p));
-            waited = k + 1;
+            ok = ok && mbar_wait(&St.bar[slot_of(k + 1)], phase_of(k + 1));
             if (__syncthreads_or(!ok)) {  // (the same answer in every thread)
                 failed = true;
                 break;
             }
-            if (issued < last) {  // every thread is past step k - 1: the refilled slot is no longer read
+            if (k > k0 && issued < last) {  // every thread is past step k - 1: plane k - 2's slot takes plane k + 4
                 ++issued;
                 if (producer) issue(issued);
             }
-            const int i = i0 + lane, j = j0 + warp;
-            if (i < n0 && j < n1 && ((i + j + k + color) & 1) == 0) {
-                if (i > 0 && i < n0 - 1 && j > 0 && j < n1 - 1 && k > 0 && k < n2 - 1) {
-                    const int at = (warp + 1) * ZT_W + lane + 4;
-                    const float* xc = &St.x[slot_of(k)][at];
-                    float acc = 0;
-                    acc += c1 * xc[-1];
-                    acc += c2 * xc[1];
-                    acc += c3 * xc[-ZT_W];
-                    acc += c4 * xc[ZT_W];
-                    acc += c5 * St.x[slot_of(k - 1)][at];
-                    acc += c6 * St.x[slot_of(k + 1)][at];
-                    x[((long long) k * n1 + j) * n0 + i] = (St.b[slot_of(k)][warp * 32 + lane] - acc) * cinv;
-                } else {
-                    zq_push(Q, 1u, k - k0, warp, lane);
+            const float* Xd = St.x[slot_of(k - 1)];
+            const float* Xc = St.x[slot_of(k)];
+            const float* Xu = St.x[slot_of(k + 1)];
+            const float* Bc = St.b[slot_of(k)];
+#pragma unroll
+            for (int r = 0; r < 2; ++r) {
+                const int ly = 2 * ry + r, j = j0 + ly;
+                const int lx = 2 * px + ((j + k + color) & 1), i = i0 + lx;  // (i0 is even)
+                if (i < n0 && j < n1) {
+                    const int at = (ly + 1) * ZT_W + lx + 4;
+                    const float bv = Bc[ly * MG_ZT2_X + lx];
+                    float v;
+                    if (i > 0 && i < n0 - 1 && j > 0 && j < n1 - 1 && k > 0 && k < n2 - 1) {
+                        float acc = 0;
+                        acc += c1 * Xc[at - 1];
+                        acc += c2 * Xc[at + 1];
+                        acc += c3 * Xc[at - ZT_W];
+                        acc += c4 * Xc[at + ZT_W];
+                        acc += c5 * Xd[at];
+                        acc += c6 * Xu[at];
+                        v = (bv - acc) * cinv;
+                    } else {
+                        // a face cell: its class's coefficients, the neighbours inside the level only
+                        const float* tc = L.T32 + (pos_class(i, n0) + 3 * pos_class(j, n1) + 9 * pos_class(k, n2)) * TSTRIDE;
+                        float acc = 0;
+                        if (i > 0) acc += tc[1] * Xc[at - 1];
+                        if (i < n0 - 1) acc += tc[2] * Xc[at + 1];
+                        if (j > 0) acc += tc[3] * Xc[at - ZT_W];
+                        if (j < n1 - 1) acc += tc[4] * Xc[at + ZT_W];
+                        if (k > 0) acc += tc[5] * Xd[at];
+                        if (k < n2 - 1) acc += tc[6] * Xu[at];
+                        v = (bv - acc) * tc[NSLOT];
+                    }
+                    x[(long long) k * sz + (long long) j * sy + i] = v;
                 }
             }
         }
         seq = base + (unsigned) (last - k0 + 2);
         if (failed) {
-            // a copy never completed: record it, wait (bounded) for every copy this tile issued, stop
-            // (the last fill of each slot: the earlier ones have completed)
+            // a copy never completed: record it, wait (bounded) for the last copy of each slot, stop
             for (int p = max(k0 - 1, issued - ZT_RING + 1); p <= issued; ++p) mbar_wait(&St.bar[slot_of(p)], phase_of(p));
             if (threadIdx.x == 0) atomicExch(&g_mg_err, 1);
             return;
         }
-        zq_drain(Q, C, [&](int ci, int cj, int ck) { cell_gs<float>(L, ci, cj, ck); }, 0);
+        __syncthreads();  // every thread is past the tile's last step before the next tile's planes refill the ring
     }
 }
 
@@ -1025,11 +1047,10 @@ int mg_launch_smooth(cudaStream_t s, int sms, bool f32, const LvlDev* L, const C
 // the z-marching variant: the system's (tuned) choice unless OPFLOW_MG_ZB = 2, 4, 8 (plane batch of the
 // register kernels) or 16 (the TMA-staged smoother where a level has its tiles)
 int mg_z_batch(int zb) {
-    static const int forced = [] {
-        const char* e = getenv("OPFLOW_MG_ZB");
-        const int v = e ? atoi(e) : 0;
-        return v == 2 || v == 4 || v == 8 || v == MG_ZB_TMA ? v : 0;
-    }();
+    // (read at every call: a process may switch it between solves)
+    const char* e = getenv("OPFLOW_MG_ZB");
+    const int v = e ? atoi(e) : 0;
+    const int forced = v == 2 || v == 4 || v == 8 || v == MG_ZB_TMA ? v : 0;
     return forced ? forced : zb;
 }
 // the register kernels' plane batch
@@ -1057,9 +1078,21 @@ int mg_launch_residual_z(cudaStream_t s, int sms, bool f32, const LvlDev* L, con
     OPG_LAUNCHED();
     return check_launch("mg_residual_z");
 }
+int mg_zt_resident(int sms) {
+    static const int per_sm = [] {
+        int b = 0;
+        if (cudaFuncSetAttribute(mg_smooth_zt, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) ZT_SMEM) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, mg_smooth_zt, 256, ZT_SMEM) != cudaSuccess) {
+            cudaGetLastError();
+            b = 0;
+        }
+        return std::max(1, b);
+    }();
+    return per_sm * sms;
+}
 int mg_launch_smooth_zt(cudaStream_t s, int sms, const LvlDev* L, const Chunk* ch, int nch, int color, const Scal* sc, const CUtensorMap* maps) {
     if (nch <= 0) return OPFLOW_OK;
-    mg_smooth_zt<<<grid_of(nch, sms), 32 * MG_ZT_Y, 0, s>>>(L, ch, nch, color, sc, maps);
+    mg_smooth_zt<<<std::max(1, std::min(nch, mg_zt_resident(sms))), 256, ZT_SMEM, s>>>(L, ch, nch, color, sc, maps);
     OPG_LAUNCHED();
     return check_launch("mg_smooth_zt");
 }
@@ -1068,7 +1101,11 @@ int mg_encode_zt_maps(const LvlDev& D, CUtensorMap* two) {
     if (!enc) return fail(OPFLOW_E_UNSUPPORTED, "cuTensorMapEncodeTiled is not available");
     const cuuint64_t dims[3] = {(cuuint64_t) D.n[0], (cuuint64_t) D.n[1], (cuuint64_t) D.n[2]};
     const cuuint64_t strides[2] = {(cuuint64_t) D.n[0] * 4, (cuuint64_t) D.n[0] * D.n[1] * 4};
-    const cuuint32_t box_x[3] = {ZT_W, ZT_H, 1}, box_b[3] = {32, MG_ZT_Y, 1}, ones[3] = {1, 1, 1};
+    const cuuint32_t box_x[3] = {ZT_W, ZT_H, 1}, box_b[3] = {MG_ZT2_X, MG_ZT2_Y, 1}, ones[3] = {1, 1, 1};
+    // (the kernel's ring and queue take more than the default 48 KB of dynamic shared memory; set once,
+    // outside any stream capture)
+    static const bool smem_ok = cudaFuncSetAttribute(mg_smooth_zt, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) ZT_SMEM) == cudaSuccess;
+    if (!smem_ok) return fail(OPFLOW_E_UNSUPPORTED, "mg_smooth_zt: %zu bytes of shared memory", ZT_SMEM);
     for (int q = 0; q < 2; ++q) {
         const CUresult r = enc(&two[q], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, q == 0 ? (void*) D.x32 : (void*) D.b32, dims, strides,
                                q == 0 ? box_x : box_b, ones, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,

@@ -16,10 +16,15 @@ constexpr long long MG_ZT_MIN = 32768;
 int mg_launch_smooth_z(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* ch, int nch, int color, const Scal* sc, int zb);
 // r = b - A x over the same tiles
 int mg_launch_residual_z(cudaStream_t s, int sms, bool f32, const LvlDev* L, const Chunk* ch, int nch, const Scal* sc, int zb);
-// the TMA-staged float32 smoother over its own tiles (Chunk{lvl, j, k, i0 = a multiple of 32, 32, planes});
-// maps: device array, the x and b tensor maps of level index l at [2 l] and [2 l + 1]
+// the TMA-staged float32 smoother of non-periodic levels over its own tiles (Chunk{lvl, j = a multiple
+// of MG_ZT2_Y, k, i0 = a multiple of MG_ZT2_X, MG_ZT2_X, planes <= MG_ZT2_Z}); maps: device array, the x
+// and b tensor maps of level index l at [2 l] and [2 l + 1]
+constexpr int MG_ZT2_X = 64, MG_ZT2_Y = 16, MG_ZT2_Z = 64;
 int mg_launch_smooth_zt(cudaStream_t s, int sms, const LvlDev* L, const Chunk* ch, int nch, int color, const Scal* sc, const CUtensorMap* maps);
-// encodes the x and b tensor maps of a float32 level for mg_smooth_zt (boxes 40 x (MG_ZT_Y + 2) and 32 x MG_ZT_Y)
+// CTAs of mg_smooth_zt resident at once on `sms` SMs (its grid)
+int mg_zt_resident(int sms);
+// encodes the x and b tensor maps of a float32 level for mg_smooth_zt (boxes (MG_ZT2_X + 8) x
+// (MG_ZT2_Y + 2) and MG_ZT2_X x MG_ZT2_Y)
 int mg_encode_zt_maps(const LvlDev& D, CUtensorMap* two);
 // reads (and clears) the kernels' failure flag: 1 after a bounded wait of mg_smooth_zt gave up
 int mg_take_error(cudaStream_t s, int* err);

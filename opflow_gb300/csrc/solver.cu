@@ -835,14 +835,29 @@ int mg_finalize(MGSystem* S) {
                             }
                     // the TMA-staged smoother's tiles: 16-byte aligned rows (float32, a multiple of 4 cells)
                     CUtensorMap two[2];
-                    if (f32 && D.n[0] % 4 == 0 && (reinterpret_cast<uintptr_t>(D.x32) & 15) == 0 && (reinterpret_cast<uintptr_t>(D.b32) & 15) == 0 &&
-                        mg_encode_zt_maps(D, two) == OPFLOW_OK) {
+                    if (f32 && D.n[0] % 4 == 0 && !D.per[0] && !D.per[1] && !D.per[2] && (reinterpret_cast<uintptr_t>(D.x32) & 15) == 0 &&
+                        (reinterpret_cast<uintptr_t>(D.b32) & 15) == 0 && mg_encode_zt_maps(D, two) == OPFLOW_OK) {
                         zt_maps[li] = {two[0], two[1]};
-                        for (int k0 = 0; k0 < D.n[2]; k0 += zz)
-                            for (int j0 = 0; j0 < D.n[1]; j0 += MG_ZT_Y)
-                                for (int i0 = 0; i0 < D.n[0]; i0 += 32) {
-                                    Chunk c{li, j0, k0, i0, 32};
-                                    c.nrows = std::min(zz, D.n[2] - k0);
+                        // planes per tile: the kernel's grid is one wave of resident CTAs striding over
+                        // the tiles, so a half sweep takes about (rounds of tiles) x (planes per tile + the
+                        // two halo planes); the run count along z that minimises it (at most
+                        // MG_ZT2_Z planes per tile); OPFLOW_MG_ZT_PLANES for sweeps
+                        const long long txy2 = (long long) ((D.n[0] + MG_ZT2_X - 1) / MG_ZT2_X) * ((D.n[1] + MG_ZT2_Y - 1) / MG_ZT2_Y);
+                        const long long R = mg_zt_resident(ctx->num_sms);
+                        int zz2 = MG_ZT2_Z;
+                        long long best = -1;
+                        for (int runs = 1; runs <= D.n[2]; ++runs) {
+                            const int zz = (D.n[2] + runs - 1) / runs;
+                            if (zz > MG_ZT2_Z) continue;
+                            const long long cost = ((txy2 * runs + R - 1) / R) * (zz + 2);
+                            if (best < 0 || cost < best) { best = cost; zz2 = zz; }
+                        }
+                        if (const char* e = getenv("OPFLOW_MG_ZT_PLANES")) zz2 = std::max(2, std::min(MG_ZT2_Z, atoi(e)));
+                        for (int k0 = 0; k0 < D.n[2]; k0 += zz2)
+                            for (int j0 = 0; j0 < D.n[1]; j0 += MG_ZT2_Y)
+                                for (int i0 = 0; i0 < D.n[0]; i0 += MG_ZT2_X) {
+                                    Chunk c{li, j0, k0, i0, MG_ZT2_X};
+                                    c.nrows = std::min(zz2, D.n[2] - k0);
                                     S->zt_ch[l].push_back(c);
                                 }
                     }

@@ -280,12 +280,20 @@ def test_fused_tiles_and_bottom_kernel_match_chunked_v_cycle(ctx, monkeypatch, p
     assert out["fused"][1] <= 1e-10
 
 
+@pytest.mark.parametrize("zb", ["tuned", "staged"])
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
 @pytest.mark.parametrize("case", ["neum_cell", "dirc_cell", "periodic_cell", "dirc_node", "neumvar_cell"])
-def test_z_marching_smoother_matches_chunked_v_cycle(ctx, monkeypatch, prec, case):
+def test_z_marching_smoother_matches_chunked_v_cycle(ctx, monkeypatch, prec, case, zb):
     """The z-marching 3D kernels reproduce the chunked V-cycle bit for bit, on ragged extents (tiles cut
-    in x, y and z) with Neumann, Dirichlet, periodic and node-centred levels.  (OPFLOW_MG_ZB in the
-    environment picks the register kernels' plane batch or, with 16, the staged smoother.)"""
+    in x, y and z) with Neumann, Dirichlet, periodic and node-centred levels: with the tuner's choice
+    per level, and with the TMA-staged smoother forced (OPFLOW_MG_ZB=16; float32 levels whose rows hold
+    a multiple of 4 cells)."""
+    if zb == "staged" and prec == "fp64":
+        pytest.skip("the TMA-staged smoother runs float32 levels (the mixed-precision V-cycle) only")
+    if zb == "staged":
+        monkeypatch.setenv("OPFLOW_MG_ZB", "16")
+    else:
+        monkeypatch.delenv("OPFLOW_MG_ZB", raising=False)
     bc = {"neum": capi.BC_NEUM, "neumvar": capi.BC_NEUM, "dirc": capi.BC_DIRC, "periodic": capi.BC_PERIODIC}[case.split("_")[0]]
     loc = capi.CENTER if case.endswith("cell") else capi.CORNER
     # large enough for z tiles of at least 4 planes on level 0, ragged in x (30- and 32-wide tiles), y
