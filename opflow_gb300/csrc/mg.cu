@@ -367,11 +367,14 @@ constexpr unsigned ZT_BYTES = (ZT_W * ZT_H + MG_ZT2_X * MG_ZT2_Y) * 4;  // bytes
 struct ZtStage {
     float x[ZT_RING][ZT_XSLOT];
     float b[ZT_RING][ZT_BSLOT];
+    float cls[NCLASS * TSTRIDE];  // the tile's level's class table (face cells read their class's row)
     unsigned long long bar[ZT_RING];
 };
 static_assert(MG_ZT2_X == 64 && MG_ZT2_Y == 16, "the thread layout covers 64 x 16 cells with 256 threads");
 static_assert((ZT_BSLOT * 4) % 128 == 0 && (ZT_W * 4) % 16 == 0, "slots on 128-byte boundaries, box rows 16-byte multiples");
 constexpr size_t ZT_SMEM = sizeof(ZtStage) + 128;  // (+ alignment of the dynamic shared memory to 128 bytes)
+// four CTAs per SM: 4 x (ZT_SMEM + the 1 KB the hardware reserves per CTA) within an SM's 228 KB
+static_assert(4 * (ZT_SMEM + 1024) <= 228 * 1024, "four resident CTAs per SM");
 
 __global__ void __launch_bounds__(256) mg_smooth_zt(const LvlDev* __restrict__ Ls, const Chunk* __restrict__ ch, int nch, int color,
                                                    const Scal* sc, const CUtensorMap* __restrict__ maps) {
@@ -394,6 +397,7 @@ __global__ void __launch_bounds__(256) mg_smooth_zt(const LvlDev* __restrict__ L
         float* x = L.x32;
         const float* t = L.T32 + 13 * TSTRIDE;
         const float c1 = t[1], c2 = t[2], c3 = t[3], c4 = t[4], c5 = t[5], c6 = t[6], cinv = t[NSLOT];
+        for (int e = threadIdx.x; e < NCLASS * TSTRIDE; e += blockDim.x) St.cls[e] = L.T32[e];  // (read after the first step's barrier)
         const CUtensorMap* mx = maps + 2 * C.lvl;
         const CUtensorMap* mb = mx + 1;
         const unsigned base = seq;  // plane k0 - 1 is plane number base
@@ -416,8 +420,25 @@ __global__ void __launch_bounds__(256) mg_smooth_zt(const LvlDev* __restrict__ L
         bool ok = mbar_wait(&St.bar[slot_of(k0 - 1)], phase_of(k0 - 1));
         ok = ok && mbar_wait(&St.bar[slot_of(k0)], phase_of(k0));
         bool failed = false;
+        // the slots of planes k - 1, k, k + 1 and the phase of plane k + 1's fill, advanced step by step
+        int sd = slot_of(k0 - 1), sc = slot_of(k0), su = slot_of(k0 + 1);
+        unsigned phu = phase_of(k0 + 1);
+        // per thread: whether its two candidate columns (even, odd) and its two rows are inside the
+        // level's faces, and its rows' global offsets
+        const int ia = i0 + 2 * px;
+        const bool xin0 = ia > 0 && ia < n0 - 1, xin1 = ia + 1 > 0 && ia + 1 < n0 - 1;
+        const bool xok0 = ia < n0, xok1 = ia + 1 < n0;
+        float* xrow[2];
+        bool yin[2], yok[2];
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+            const int j = j0 + 2 * ry + r;
+            yin[r] = j > 0 && j < n1 - 1;
+            yok[r] = j < n1;
+            xrow[r] = x + (long long) k0 * sz + (long long) j * sy + ia;
+        }
         for (int k = k0; k < k1; ++k) {
-            ok = ok && mbar_wait(&St.bar[slot_of(k + 1)], phase_of(k + 1));
+            ok = ok && mbar_wait(&St.bar[su], phu);
             if (__syncthreads_or(!ok)) {  // (the same answer in every thread)
                 failed = true;
                 break;
@@ -426,19 +447,21 @@ __global__ void __launch_bounds__(256) mg_smooth_zt(const LvlDev* __restrict__ L
                 ++issued;
                 if (producer) issue(issued);
             }
-            const float* Xd = St.x[slot_of(k - 1)];
-            const float* Xc = St.x[slot_of(k)];
-            const float* Xu = St.x[slot_of(k + 1)];
-            const float* Bc = St.b[slot_of(k)];
+            const float* Xd = St.x[sd];
+            const float* Xc = St.x[sc];
+            const float* Xu = St.x[su];
+            const float* Bc = St.b[sc];
+            const bool kin = k > 0 && k < n2 - 1;
 #pragma unroll
             for (int r = 0; r < 2; ++r) {
                 const int ly = 2 * ry + r, j = j0 + ly;
-                const int lx = 2 * px + ((j + k + color) & 1), i = i0 + lx;  // (i0 is even)
-                if (i < n0 && j < n1) {
+                const int e = (j + k + color) & 1;  // the colour's column of the pair (i0 is even)
+                const int lx = 2 * px + e, i = ia + e;
+                if ((e ? xok1 : xok0) && yok[r]) {
                     const int at = (ly + 1) * ZT_W + lx + 4;
                     const float bv = Bc[ly * MG_ZT2_X + lx];
                     float v;
-                    if (i > 0 && i < n0 - 1 && j > 0 && j < n1 - 1 && k > 0 && k < n2 - 1) {
+                    if ((e ? xin1 : xin0) && yin[r] && kin) {
                         float acc = 0;
                         acc += c1 * Xc[at - 1];
                         acc += c2 * Xc[at + 1];
@@ -449,7 +472,7 @@ __global__ void __launch_bounds__(256) mg_smooth_zt(const LvlDev* __restrict__ L
                         v = (bv - acc) * cinv;
                     } else {
                         // a face cell: its class's coefficients, the neighbours inside the level only
-                        const float* tc = L.T32 + (pos_class(i, n0) + 3 * pos_class(j, n1) + 9 * pos_class(k, n2)) * TSTRIDE;
+                        const float* tc = St.cls + (pos_class(i, n0) + 3 * pos_class(j, n1) + 9 * pos_class(k, n2)) * TSTRIDE;
                         float acc = 0;
                         if (i > 0) acc += tc[1] * Xc[at - 1];
                         if (i < n0 - 1) acc += tc[2] * Xc[at + 1];
@@ -459,8 +482,15 @@ __global__ void __launch_bounds__(256) mg_smooth_zt(const LvlDev* __restrict__ L
                         if (k < n2 - 1) acc += tc[6] * Xu[at];
                         v = (bv - acc) * tc[NSLOT];
                     }
-                    x[(long long) k * sz + (long long) j * sy + i] = v;
+                    xrow[r][e] = v;
                 }
+                xrow[r] += sz;
+            }
+            sd = sc;
+            sc = su;
+            if (++su == ZT_RING) {
+                su = 0;
+                phu ^= 1u;
             }
         }
         seq = base + (unsigned) (last - k0 + 2);
