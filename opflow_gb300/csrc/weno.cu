@@ -226,6 +226,42 @@ __device__ __forceinline__ void weno_stage(const double* __restrict__ u, const d
 // address the line's first cell, `stride` between its cells.
 constexpr int kWenoThreads = 256;
 
+// A line between global and shared memory.  A contiguous line (x lines) moves in 16-byte pairs from its
+// first 16-byte aligned cell, with a lone cell at either end taken by thread 0; other lines cell by
+// cell.  Plain copies: the values are the same whichever way they move.
+__device__ __forceinline__ void line_load(double* __restrict__ dst, const double* __restrict__ src, int n, long long stride) {
+    if (stride == 1) {
+        const int head = (reinterpret_cast<unsigned long long>(src) & 15ull) != 0 ? 1 : 0;  // (cells are 8-byte aligned)
+        const int np = (n - head) / 2;
+        const double2* __restrict__ s2 = reinterpret_cast<const double2*>(src + head);
+        for (int t = threadIdx.x; t < np; t += blockDim.x) {
+            const double2 v = s2[t];
+            dst[head + 2 * t] = v.x;
+            dst[head + 2 * t + 1] = v.y;
+        }
+        if (threadIdx.x == 0) {
+            if (head) dst[0] = src[0];
+            if (head + 2 * np < n) dst[n - 1] = src[n - 1];
+        }
+    } else {
+        for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i * stride];
+    }
+}
+__device__ __forceinline__ void line_store(double* __restrict__ dst, const double* __restrict__ src, int n, long long stride) {
+    if (stride == 1) {
+        const int head = (reinterpret_cast<unsigned long long>(dst) & 15ull) != 0 ? 1 : 0;
+        const int np = (n - head) / 2;
+        double2* __restrict__ d2 = reinterpret_cast<double2*>(dst + head);
+        for (int t = threadIdx.x; t < np; t += blockDim.x) d2[t] = make_double2(src[head + 2 * t], src[head + 2 * t + 1]);
+        if (threadIdx.x == 0) {
+            if (head) dst[0] = src[0];
+            if (head + 2 * np < n) dst[n - 1] = src[n - 1];
+        }
+    } else {
+        for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i * stride] = src[i];
+    }
+}
+
 template <int K, bool UP, bool FAST, int MINB>
 __global__ void __launch_bounds__(kWenoThreads, MINB) weno_rk3_kernel(FieldView u, FieldView u1, FieldView u2, int write_stages, Box lines, WenoParams P,
                                                           int steps) {
@@ -241,7 +277,7 @@ __global__ void __launch_bounds__(kWenoThreads, MINB) weno_rk3_kernel(FieldView 
         int idx0[3] = {a, b, c};
         const long long stride = P.dim == 0 ? 1 : (P.dim == 1 ? u.sy : u.sz);
         const long long base = (idx0[0] - u.off[0]) + (idx0[1] - u.off[1]) * u.sy + (idx0[2] - u.off[2]) * u.sz;
-        for (int i = threadIdx.x; i < n; i += blockDim.x) s0[i] = u.data[base + i * stride];
+        line_load(s0, u.data + base, n, stride);
         __syncthreads();
         for (int st = 0; st < steps; ++st) {
             weno_stage<K, UP, FAST, 0>(s0, s0, s1, n, P);
@@ -249,7 +285,7 @@ __global__ void __launch_bounds__(kWenoThreads, MINB) weno_rk3_kernel(FieldView 
             weno_stage<K, UP, FAST, 1>(s0, s1, s2, n, P);
             __syncthreads();
             if (write_stages && st == steps - 1) {
-                for (int i = threadIdx.x; i < n; i += blockDim.x) u1.data[base + i * stride] = s1[i];
+                line_store(u1.data + base, s1, n, stride);
                 __syncthreads();
             }
             // the third stage reads u and s2 only: its result replaces s1, which then becomes u
@@ -259,10 +295,8 @@ __global__ void __launch_bounds__(kWenoThreads, MINB) weno_rk3_kernel(FieldView 
             s0 = s1;
             s1 = t;
         }
-        for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            u.data[base + i * stride] = s0[i];
-            if (write_stages) u2.data[base + i * stride] = s2[i];
-        }
+        line_store(u.data + base, s0, n, stride);
+        if (write_stages) line_store(u2.data + base, s2, n, stride);
         __syncthreads();
         // the next line starts from the shared buffers' original order
         if (steps & 1) {
