@@ -848,7 +848,8 @@ def run_weno(args, torch, api, capi, np, ctx, stream, world, rank, local, dist):
                        "l2": "field 2.1 GB > L2; the run keeps each line in shared memory across its steps",
                        "parallelism": "replicas" if world > 1 else "single"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_src,
-                         "traffic": None, "kernel": "weno_rk3_kernel<16, false, %s, 2>" % ("true" if m == capi.EVAL_FAST else "false"),
+                         "traffic": traffic_for("weno_" + ("fast" if m == capi.EVAL_FAST else "exact")),
+                         "kernel": "weno_rk3_kernel<16, false, %s, 2>" % ("true" if m == capi.EVAL_FAST else "false"),
                          "algorithmic_bytes_per_launch": 16.0 * pts,
                          "note": "float64-issue-bound: HBM carries 16 B per point per launch of --steps RK3 steps"},
             "cpu_baseline": cpu,
