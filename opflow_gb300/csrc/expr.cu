@@ -1117,25 +1117,24 @@ static int run_resident_graph(opflow_ctx ctx, opflow_field dst, Plan& plan, unsi
     cudaGraphExec_t exec = nullptr;
     OPG_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     int rc = OPFLOW_OK;
-    const uint64_t before = g_launches.load();
     FieldView a = dst->view(), b = dst->view_back();
     for (int q = 0; q < RES_GRAPH_STEPS && rc == OPFLOW_OK; ++q) {
         rc = axis_launch_resident(ctx, a, b, plan.box, plan.axis, maxslots, false, false);
         std::swap(a, b);
     }
-    const uint64_t per_replay = g_launches.load() - before;
-    g_launches.fetch_sub(per_replay);  // counted below, once per replay
+    // a 2D resident step is one launch: the captured ones are counted once per replay instead
+    g_launches.fetch_sub((uint64_t) RES_GRAPH_STEPS);
     const cudaError_t e_end = cudaStreamEndCapture(ctx->stream, &g);
     if (rc == OPFLOW_OK && e_end != cudaSuccess) rc = fail(OPFLOW_E_CUDA, "resident-step graph capture failed: %s", cudaGetErrorString(e_end));
     if (rc == OPFLOW_OK && cudaGraphInstantiate(&exec, g, 0) != cudaSuccess) rc = fail(OPFLOW_E_CUDA, "resident-step graph instantiation failed");
     for (int r = 0; r < reps && rc == OPFLOW_OK; ++r) {
         if (cudaGraphLaunch(exec, ctx->stream) != cudaSuccess) rc = fail(OPFLOW_E_CUDA, "resident-step graph launch failed");
-        g_launches.fetch_add(per_replay);
+        g_launches.fetch_add((uint64_t) RES_GRAPH_STEPS);
+        dst->version += RES_GRAPH_STEPS;
     }
     if (exec) cudaGraphExecDestroy(exec);
     if (g) cudaGraphDestroy(g);
-    cudaGetLastError();
-    dst->version += (unsigned long long) reps * RES_GRAPH_STEPS;
+    if (rc != OPFLOW_OK) cudaGetLastError();
     return rc;
 }
 
