@@ -22,7 +22,8 @@ struct AxisParams {
 
 int axis_launch(opflow_ctx ctx, const FieldView& in, const FieldView& out, const Box& box, const AxisParams& P, bool fast,
                 unsigned long long* maxslots, int step);
-// One step of a run of fixed-point steps that keeps the update box in fixed point between steps (3D):
+// One step of a run of fixed-point steps that keeps the update box in fixed point between steps (2D or
+// 3D; in 3D the steady-state steps stage their planes by TMA where the buffer's strides allow):
 // `first` reads float64, `last` writes float64; maxslots[0] holds the initial max|u| bit pattern.
 bool axis_resident_ok(const AxisParams& P);  // weights the resident kernel's product takes
 int axis_launch_resident(opflow_ctx ctx, const FieldView& in, const FieldView& out, const Box& box, const AxisParams& P,
