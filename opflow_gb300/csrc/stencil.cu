@@ -10,6 +10,10 @@
 //           D2SecondOrderCentered.hpp:160-171, summed in tree order, then u + s*sum);
 //   FAST  - exact 64-bit fixed point: values are converted once when staged, the second differences
 //           are exact integer sums, one 64x53-bit product per weight group, one rounding back.
+//
+// A run of FAST steps on a Dirichlet node grid can keep the field in fixed point between its steps
+// (the resident kernels below): in 3D its steady-state steps stream their planes into shared memory
+// by TMA (axis3d_fxtma_kernel), in 2D a warp updates 30 columns x 8 rows with every load in flight.
 #include "stencil.h"
 #include "tma.h"
 #include "tune.h"
