@@ -537,7 +537,14 @@ class CartesianField(Expr):
 
     # ---- assignment ----
     def assign(self, expr, op="=", mode="exact", steps=1):
-        """`self <op>= expr` (Expr::operator=, +=, ... through FieldAssigner::assign)."""
+        """`self <op>= expr` (Expr::operator=, +=, ... through FieldAssigner::assign), `steps` times.
+
+        mode "exact": the reference's IEEE operations in its order (bit-identical); "fast": a linear
+        constant-coefficient stencil of one field in exact 64-bit fixed point (within 1e-14).  In fast
+        mode, `steps` >= 2 FTCS steps of a Dirichlet node grid without a ghost layer, with weights that
+        keep the maximum principle, run resident: the field stays in fixed point between the steps (3D
+        steady-state steps stage their planes in shared memory by TMA; long 2D runs replay a CUDA graph).
+        """
         if isinstance(expr, (int, float)):
             check(lib().opflow_field_fill(self.handle, _ARITH[op], float(expr)))
             return self
