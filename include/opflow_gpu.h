@@ -257,7 +257,11 @@ int opflow_assign_batch(opflow_ctx ctx, int n, const opflow_field* dsts, const i
                         const opflow_field* const* leaves, const int* n_leaves, int steps);
 
 /* Runs `steps` repetitions of the same assignment (one fused kernel per step where the expression has
- * a specialised kernel). */
+ * a specialised kernel).  In OPFLOW_EVAL_FAST mode, steps >= 2 of u = u + sum_d w_d (u(i-e_d) + u(i+e_d)
+ * - 2u) on a 2D or 3D node grid with Dirichlet sides and no ghost layer, with w_d >= 0 and
+ * 1 - 2 sum_d w_d >= 0, keep the field in 64-bit fixed point between the steps (one scale for the run;
+ * float64 again after the last step), within 1e-14 of the EXACT run.  OPFLOW_FX_RESIDENT=0 in the
+ * environment turns that off. */
 int opflow_assign_repeat(opflow_ctx ctx, opflow_field dst, int arith, const opflow_node* nodes, int n_nodes,
                          const opflow_field* leaves, int n_leaves, int mode, int steps);
 
