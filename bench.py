@@ -153,6 +153,26 @@ def ftcs_kernel_label(D, mode, steps):
     return "axis3d_rb_kernel<FAST>" if mode == "fast" else "axis3d_kernel<EXACT>"
 
 
+def replica_max(x, world, dist, device):
+    """The largest of the ranks' x: a time, the job's time being its slowest replica's; x at one rank."""
+    if world <= 1:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_min(x, world, dist, device):
+    """The smallest of the ranks' x: a rate, every replica doing the same work; x at one rank."""
+    if world <= 1:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MIN)
+    return float(t.item())
+
+
 def workload_cfg(name):
     if name == "ftcs3d":
         return dict(workload="ftcs3d", grid=[512, 512, 512], loc="node", bc="dirichlet 0", dt="0.1*h^2", init="8 seeded Gaussians",
@@ -815,9 +835,7 @@ def run_weno(args, torch, api, capi, np, ctx, stream, world, rank, local, dist):
     ms = ev0.elapsed_time(ev1)
     if world > 1:
         dist.barrier()
-        tt = torch.tensor([ms], device=torch.device("cuda", local))
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
+    ms = replica_max(ms, world, dist, torch.device("cuda", local))
     pts = nx * ny
     value = pts * args.steps * world / (ms * 1e-3) / 1e9
     # end to end: upload, one RK3 step, download, per step
@@ -974,10 +992,8 @@ def run_ours(args):
             fn = {"poisson2d": run_poisson2d, "serve": run_serve, "batched": run_batched, "poisson3d": run_poisson3d}[args.workload]
             r = fn(args, torch, api, capi, np, ctx, stream, world, rank, local)
         value = r["value"]
-        if world > 1:
-            tt = torch.tensor([value], device=torch.device("cuda", local))
-            dist.all_reduce(tt, op=dist.ReduceOp.MIN)  # every replica does the same work: slowest rank * N
-            value = float(tt.item()) * world
+        if world > 1:  # every replica does the same work: the slowest rank's rate times N
+            value = replica_min(value, world, dist, torch.device("cuda", local)) * world
         cpu = None
         if rank == 0 and not args.no_cpu_baseline and args.workload != "poisson3d":
             try:
@@ -1060,10 +1076,7 @@ def run_ours(args):
         dist.barrier()
     ms = ev0.elapsed_time(ev1)
     launches = capi.launch_count() - launches0
-    if world > 1:
-        tt = torch.tensor([ms], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
+    ms = replica_max(ms, world, dist, dev)
     ms_step = ms / args.steps
     value = pts * args.steps * world / (ms * 1e-3) / 1e9
 
